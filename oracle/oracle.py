@@ -1,0 +1,548 @@
+"""ORACLE - test infrastructure only. Never imported by the product path.
+
+CPU restatement of the reference's time-stepping path (pvthinker/Fluids2d):
+mesh masks and stencil orders, the flat-index flux sweeps (through the C
+restatement in ``sweeps.c``), the staggered C-grid operators, the masked
+5-point Poisson/Helmholtz operator solved with SuperLU, SSP-RK3 in increment
+form and the CFL time step. It serves three purposes:
+
+* the checker of the CUDA path in ``tests/`` and in ``__graft_entry__.smoke``;
+* the CPU-baseline leg of ``bench.py`` (numba-equivalent sweeps threaded
+  with OpenMP, numpy operators, SuperLU solves);
+* a restatement pinned against the reference itself: ``tests/golden/`` holds
+  outputs of the unmodified reference (run here with numba stubbed out) and
+  ``tests/test_oracle_golden.py`` checks this module against them.
+
+Each function cites the reference lines it follows. The numpy expressions
+keep the reference's operand order so that results agree bit for bit where
+the reference's own arithmetic is deterministic.
+"""
+from __future__ import annotations
+
+import ctypes
+import math
+import os
+
+import numpy as np
+import scipy.sparse as sparse
+import scipy.sparse.linalg as splinalg
+
+from . import build as _build
+
+METHODS = {"weno": 0, "upwind": 1, "centered": 2, "cweno": 3}
+
+_lib = None
+
+
+def lib():
+    global _lib
+    if _lib is None:
+        path = _build.build()
+        L = ctypes.CDLL(path)
+        dp = ctypes.POINTER(ctypes.c_double)
+        bp = ctypes.POINTER(ctypes.c_int8)
+        i64 = ctypes.c_int64
+        for sfx in ("", "_py"):
+            f = getattr(L, "oracle_compflux" + sfx)
+            f.argtypes = [ctypes.c_int, dp, dp, dp, bp, i64, i64, i64]
+            f.restype = None
+            f = getattr(L, "oracle_vortexforce" + sfx)
+            f.argtypes = [ctypes.c_int, dp, dp, dp, bp, i64, i64, ctypes.c_int,
+                          i64, i64]
+            f.restype = None
+            f = getattr(L, "oracle_innerproduct" + sfx)
+            f.argtypes = [ctypes.c_int, dp, dp, dp, bp, i64, i64, i64]
+            f.restype = None
+        L.oracle_set_order.argtypes = [bp, i64, i64, ctypes.c_int, bp]
+        L.oracle_set_order.restype = None
+        L.oracle_num_threads.restype = ctypes.c_int
+        _lib = L
+    return _lib
+
+
+def _dp(a):
+    assert a.dtype == np.float64 and a.flags.c_contiguous
+    return a.ctypes.data_as(ctypes.POINTER(ctypes.c_double))
+
+
+def _bp(a):
+    assert a.dtype == np.int8 and a.flags.c_contiguous
+    return a.ctypes.data_as(ctypes.POINTER(ctypes.c_int8))
+
+
+# ----------------------------------------------------------- sweeps ------
+# weno.py:412-436. `pysq` selects pow(x,2) (Python-float semantics, matches a
+# numba-less run of the reference bit for bit) or x*x (numba semantics).
+
+def compflux(flx, U, q, o, s, method="weno", pysq=True):
+    f = lib().oracle_compflux_py if pysq else lib().oracle_compflux
+    f(METHODS[method], _dp(flx), _dp(U), _dp(q), _bp(o), s, 0, q.size)
+
+
+def vortexforce(du, V, q, o, s, s2, sign, method="weno", pysq=True):
+    f = lib().oracle_vortexforce_py if pysq else lib().oracle_vortexforce
+    f(METHODS[method], _dp(du), _dp(V), _dp(q), _bp(o), s, s2, sign, 0,
+      du.size)
+
+
+def innerproduct(ke, U, q, o, s, method="weno", pysq=True):
+    f = lib().oracle_innerproduct_py if pysq else lib().oracle_innerproduct
+    f(METHODS[method], _dp(ke), _dp(U), _dp(q), _bp(o), s, 0, ke.size)
+
+
+def set_order(msk, shift, maxorder):
+    """meshes.py:146-186 (through the C restatement)."""
+    m = np.ascontiguousarray(msk, dtype=np.int8)
+    o = np.zeros(m.shape, dtype=np.int8)
+    lib().oracle_set_order(_bp(m), m.size, shift, maxorder, _bp(o))
+    return o
+
+
+# ------------------------------------------------------------- param -----
+
+class Param:
+    """The reference's parameter defaults (param.py:11-59), as a plain bag."""
+
+    def __init__(self, **kw):
+        self.model = "euler"
+        self.nx = 40
+        self.ny = 40
+        self.Lx = 1.0
+        self.Ly = 1.0
+        self.xperiodic = False
+        self.yperiodic = False
+        self.halowidth = 3
+        self.noslip = None
+        self.f0 = 10.0
+        self.beta = 0.0
+        self.g = 1
+        self.H = 1
+        self.tend = 1.0
+        self.dt = 0.0
+        self.maxite = 100
+        self.dtmax = 9e99
+        self.integrator = "rk3"
+        self.cfl = 0.9
+        self.compflux = "weno"
+        self.vortexforce = "weno"
+        self.innerproduct = "weno"
+        self.maxorder = 6
+        for k, v in kw.items():
+            setattr(self, k, v)
+
+
+# -------------------------------------------------------------- mesh -----
+
+def slipcoef(param, msk):
+    """noslip.py:4-36."""
+    coef = np.zeros(msk.shape)
+    coef[:, :] += msk
+    coef[:, 1:] += msk[:, :-1]
+    coef[1:, :] += msk[:-1, :]
+    coef[1:, 1:] += msk[:-1, :-1]
+    free = lambda x: 1 * (x == 4)  # noqa: E731
+    nos = lambda x: np.minimum(x, 1)  # noqa: E731
+    if (param.noslip is None) or (param.noslip is False):
+        return free(coef)
+    if param.noslip is True:
+        return nos(coef)
+    out = free(coef)
+    nh = param.halowidth
+    if "left" in param.noslip:
+        out[:, nh] = nos(coef[:, nh])
+    if "right" in param.noslip:
+        out[:, -nh] = nos(coef[:, -nh])
+    if "bottom" in param.noslip:
+        out[nh, :] = nos(coef[nh, :])
+    if "top" in param.noslip:
+        out[-nh, :] = nos(coef[-nh, :])
+    return out
+
+
+def gindex(msk):
+    """elliptic.py:198-203: row-major index of fluid points, -1 elsewhere."""
+    G = np.zeros(msk.shape, dtype="i")
+    G[msk == 0] = -1
+    G[msk == 1] = np.arange(int(np.sum(msk == 1)))
+    return G
+
+
+class Mesh:
+    """meshes.py:7-111 without the plotting helpers."""
+
+    def __init__(self, param):
+        self.param = param
+        h = param.halowidth
+        self.shape = (param.ny + 2 * h, param.nx + 2 * h)
+        self.nx, self.ny = param.nx, param.ny
+        self.dx = param.Lx / self.nx
+        self.dy = param.Ly / self.ny
+        self.area = self.dx * self.dy
+        self.xshift = 1
+        self.yshift = self.shape[-1]
+        self.msk = np.zeros(self.shape, dtype="i1")
+        xs = slice(None) if param.xperiodic else slice(h, -h)
+        ys = slice(None) if param.yperiodic else slice(h, -h)
+        self.msk[ys, xs] = 1
+        self.hb = 0
+        self.f = None
+        self.finalize()
+
+    def finalize(self):
+        p = self.param
+        self.set_masks()
+        self.slipcoef = slipcoef(p, self.msk)
+        mo = p.maxorder
+        self.ocx = set_order(self.msk, self.xshift, mo)
+        self.ocy = set_order(self.msk, self.yshift, mo)
+        mv = (1 * (self.slipcoef > 0)).astype(np.int8)
+        self.ovx = set_order(mv, -self.xshift, mo)
+        self.ovy = set_order(mv, -self.yshift, mo)
+        self.ovx *= self.msky
+        self.ovy *= self.mskx
+        self.okx = set_order(self.mskx, -self.xshift, mo)
+        self.oky = set_order(self.msky, -self.yshift, mo)
+        self._solvers = {}
+        if p.model in ("qg", "qgrsw", "rsw"):
+            self.maindiag = self.area * p.f0 ** 2 / (p.g * p.H)
+            self.qgcoef = p.f0 / +p.H
+
+    # The reference factorises its operators inside finalize(); here the
+    # factorisation is deferred to first use (rsw never solves).
+    @property
+    def poisson_vertices(self):
+        if "v" not in self._solvers:
+            self._solvers["v"] = Poisson2D(self, maindiag=0)
+        return self._solvers["v"]
+
+    @property
+    def qg_helmholtz(self):
+        if "h" not in self._solvers:
+            self._solvers["h"] = Poisson2D(self, maindiag=self.maindiag)
+        return self._solvers["h"]
+
+    def set_masks(self):
+        msk = self.msk
+        self.mskx = np.zeros(self.shape, dtype="i1")
+        self.mskx[:, 1:] = msk[:, 1:] * msk[:, :-1]
+        self.msky = np.zeros(self.shape, dtype="i1")
+        self.msky[1:, :] = msk[1:, :] * msk[:-1, :]
+        self.mskv = np.zeros(self.shape, dtype="i1")
+        self.mskv[1:, 1:] = (msk[:-1, 1:] * msk[:-1, :-1]
+                             * msk[1:, 1:] * msk[1:, :-1])
+
+    def fill(self, a):
+        """fill_halo_array, meshes.py:135-143."""
+        if self.param.xperiodic:
+            n = self.param.halowidth
+            a[:, :n] = a[:, -2 * n:-n]
+            a[:, -n:] = a[:, n:2 * n]
+
+
+def vertex_msk(mesh, location="v"):
+    """get_msk_from_mesh, elliptic.py:102-111: the vertex ("v") or cell ("c")
+    mask with the periodic halo columns removed."""
+    base = mesh.msk if location == "c" else mesh.mskv
+    if not mesh.param.xperiodic:
+        return base
+    n = mesh.param.halowidth
+    m = base * 1
+    m[:, :n] = 0
+    m[:, -n:] = 0
+    return m
+
+
+def laplacian(mesh, maindiag):
+    """Masked 5-point vertex operator with Dirichlet walls
+    (get_Laplacian_sparse, elliptic.py:114-195), assembled with numpy in the
+    reference's entry order (per point: west, east, south, north, diagonal)
+    so that SuperLU sees the same matrix."""
+    G = gindex(vertex_msk(mesh))
+    ny, nx = G.shape
+    N = int(np.sum(G > -1))
+    dx2 = mesh.dy / mesh.dx
+    dy2 = mesh.dx / mesh.dy
+    xper = mesh.param.xperiodic
+    n1 = mesh.param.halowidth if xper else 0
+    J, I = np.nonzero(G > -1)
+    Ipt = G[J, I]
+    west = np.where(I > n1, G[J, np.maximum(I - 1, 0)],
+                    G[J, -n1 - 1] if xper else -1)
+    east = np.where(I < nx - 1 - n1, G[J, np.minimum(I + 1, nx - 1)],
+                    G[J, n1] if xper else -1)
+    south = np.where(J > 0, G[np.maximum(J - 1, 0), I], -1)
+    north = np.where(J < ny - 1, G[np.minimum(J + 1, ny - 1), I], -1)
+    diag = -2 * (dx2 + dy2) - maindiag
+    cols = np.stack([west, east, south, north, Ipt], axis=1)
+    vals = np.stack([np.full(N, dx2), np.full(N, dx2), np.full(N, dy2),
+                     np.full(N, dy2), np.full(N, diag)], axis=1)
+    valid = cols > -1
+    rows = np.repeat(Ipt[:, None], 5, axis=1)
+    cnt = int(valid.sum())
+    data = np.zeros(5 * N)
+    row = np.zeros(5 * N, dtype="i")
+    col = np.zeros(5 * N, dtype="i")
+    data[:cnt] = vals[valid]
+    row[:cnt] = rows[valid]
+    col[:cnt] = cols[valid]
+    A = sparse.coo_matrix((data, (row, col)), shape=(N, N))
+    return A.tocsc(), G
+
+
+class Poisson2D:
+    """Poisson2D "v" (elliptic.py:71-87): LU factorisation once, then
+    back-substitution; only fluid points of x are written, then halo fill."""
+
+    def __init__(self, mesh, maindiag=0):
+        self.mesh = mesh
+        self.A, self.G = laplacian(mesh, maindiag)
+        self.lu = splinalg.splu(self.A)
+
+    def solve(self, b, x):
+        sel = self.G > -1
+        x[sel] = self.lu.solve(b[sel])
+        self.mesh.fill(x)
+        return x
+
+
+# --------------------------------------------------------- operators -----
+
+def div(mesh, Ux, Uy, delta):
+    """operators.py:104-107."""
+    delta[:, :-1] = -np.diff(Ux, axis=1)
+    delta[:-1, :] -= np.diff(Uy, axis=0)
+    delta *= mesh.msk
+
+
+def divflux(p, mesh, fx, fy, q, Ux, Uy, dq, pysq):
+    """operators.py:21-29."""
+    compflux(fx, Ux, q, mesh.ocx, mesh.xshift, p.compflux, pysq)
+    compflux(fy, Uy, q, mesh.ocy, mesh.yshift, p.compflux, pysq)
+    div(mesh, fx, fy, dq)
+
+
+def addvortexforce(p, mesh, Ux, Uy, omega, dux, duy, pysq):
+    """operators.py:6-15."""
+    vortexforce(dux, Uy, omega, mesh.ovy, mesh.yshift, mesh.xshift, +1,
+                p.vortexforce, pysq)
+    vortexforce(duy, Ux, omega, mesh.ovx, mesh.xshift, mesh.yshift, -1,
+                p.vortexforce, pysq)
+
+
+def addcoriolis(p, mesh, Ux, Uy, dux, duy):
+    """operators.py:32-39."""
+    f = p.f0 * mesh.area * 0.25
+    dux[:-1, 1:-1] += f * (Uy[:-1, :-2] + Uy[1:, :-2] +
+                           Uy[:-1, 1:-1] + Uy[1:, 1:-1])
+    duy[1:-1, :-1] -= f * (Ux[:-2, :-1] + Ux[:-2, 1:] +
+                           Ux[1:-1, :-1] + Ux[1:-1, 1:])
+
+
+def addgrad(mesh, phi, dux, duy):
+    """operators.py:49-53."""
+    dux[:, 1:] -= np.diff(phi, axis=1) * mesh.mskx[:, 1:]
+    duy[1:, :] -= np.diff(phi, axis=0) * mesh.msky[1:, :]
+
+
+def sharp(mesh, ux, uy, Ux, Uy):
+    """operators.py:59-62."""
+    Ux[:] = ux * (1 / mesh.dx ** 2)
+    Uy[:] = uy * (1 / mesh.dy ** 2)
+
+
+def compute_vorticity(mesh, ux, uy, omega):
+    """operators.py:67-72, 77."""
+    omega[1:, :] = -np.diff(ux, axis=0)
+    omega[:, 1:] += np.diff(uy, axis=1)
+    omega *= mesh.slipcoef
+
+
+def compute_kinetic_energy(p, mesh, ux, uy, Ux, Uy, ke, pysq):
+    """operators.py:80-96 (the WENO inner-product branch)."""
+    ke[:] = 0.
+    innerproduct(ke, Ux, ux, mesh.okx, mesh.xshift, p.innerproduct, pysq)
+    innerproduct(ke, Uy, uy, mesh.oky, mesh.yshift, p.innerproduct, pysq)
+    ke *= mesh.msk * 0.5
+
+
+def compute_pressure(p, mesh, h, out):
+    """operators.py:110-111."""
+    out[:] = (p.g / mesh.area) * (h + mesh.hb)
+
+
+def centerstovertices(mesh, c, v):
+    """operators.py:126-133 (addto=False)."""
+    v[1:, 1:] = 0.25 * (c[:-1, :-1] + c[1:, :-1] + c[:-1, 1:] + c[1:, 1:])
+    v *= mesh.mskv
+
+
+def perpgrad(mesh, psi, Ux, Uy, contravariant=False):
+    """operators.py:144-149."""
+    Ux[:-1, :] = -np.diff(psi, axis=0) * mesh.mskx[:-1, :]
+    Uy[:, :-1] = np.diff(psi, axis=1) * mesh.msky[:, :-1]
+    if contravariant:
+        Ux[:] *= (1 / mesh.dy ** 2)
+        Uy[:] *= (1 / mesh.dx ** 2)
+
+
+# ------------------------------------------------------------- model -----
+
+STATE_VARS = {
+    # states.py:7-17 (the models on the hot path); vector fields get .x/.y
+    "eulerpsi": ("omega", "U", "psi", "vomega", "flx"),
+    "rsw": ("u", "h", "U", "omega", "ke", "p", "flx", "pv"),
+    "qg": ("pv", "U", "h", "flx", "work", "psi"),
+}
+PROGNOSTIC = {"eulerpsi": ("omega",), "rsw": ("u", "h"), "qg": ("pv",)}
+VECTORS = ("u", "U", "flx")
+
+
+def _alloc(names, shape):
+    out = {}
+    for n in names:
+        if n in VECTORS:
+            out[n + ".x"] = np.zeros(shape)
+            out[n + ".y"] = np.zeros(shape)
+        else:
+            out[n] = np.zeros(shape)
+    return out
+
+
+class Model:
+    """Model + RKIntegrator(rk3) + the eulerpsi/rsw/qg equation sets
+    (model.py:13-87, integrators.py:63-107, equations.py:73-157)."""
+
+    def __init__(self, param, msk=None, pysq=True):
+        self.p = param
+        self.pysq = pysq
+        self.mesh = Mesh(param)
+        if msk is not None:
+            self.mesh.msk[:] = msk
+            self.mesh.finalize()
+        shape = self.mesh.shape
+        self.s = _alloc(STATE_VARS[param.model], shape)
+        self.prog = [k for k in self.s
+                     if k.split(".")[0] in PROGNOSTIC[param.model]]
+        self.scratch = [{k: np.zeros(shape) for k in self.prog}
+                        for _ in range(3)]
+        self.t = 0.0
+        self.ite = 0
+        self._c = 0.0
+        self.dt = param.dt if param.dt > 0 else 0.01
+
+    # -- equations ------------------------------------------------------
+    def rhs(self, s, ds):
+        p, m, sq = self.p, self.mesh, self.pysq
+        if p.model == "eulerpsi":
+            divflux(p, m, s["flx.x"], s["flx.y"], s["omega"], s["U.x"],
+                    s["U.y"], ds["omega"], sq)
+            m.fill(ds["omega"])
+        elif p.model == "qg":
+            divflux(p, m, s["flx.x"], s["flx.y"], s["pv"], s["U.x"],
+                    s["U.y"], ds["pv"], sq)
+            m.fill(ds["pv"])
+        elif p.model == "rsw":
+            addvortexforce(p, m, s["U.x"], s["U.y"], s["omega"], ds["u.x"],
+                           ds["u.y"], sq)
+            addcoriolis(p, m, s["U.x"], s["U.y"], ds["u.x"], ds["u.y"])
+            addgrad(m, s["ke"], ds["u.x"], ds["u.y"])
+            addgrad(m, s["p"], ds["u.x"], ds["u.y"])
+            divflux(p, m, s["flx.x"], s["flx.y"], s["h"], s["U.x"], s["U.y"],
+                    ds["h"], sq)
+            for k in ("u.x", "u.y", "h"):
+                m.fill(ds[k])
+
+    def diag(self, s=None):
+        s = self.s if s is None else s
+        p, m, sq = self.p, self.mesh, self.pysq
+        if p.model == "eulerpsi":
+            centerstovertices(m, s["omega"], s["vomega"])
+            m.poisson_vertices.solve(s["vomega"], s["psi"])
+            perpgrad(m, s["psi"], s["U.x"], s["U.y"], contravariant=True)
+            m.fill(s["U.x"])
+            m.fill(s["U.y"])
+        elif p.model == "qg":
+            pvback = m.hb * m.qgcoef
+            centerstovertices(m, s["pv"] - pvback, s["work"])
+            if p.beta != 0:
+                s["work"] -= m.f
+            m.qg_helmholtz.solve(s["work"], s["psi"])
+            perpgrad(m, s["psi"], s["U.x"], s["U.y"], contravariant=True)
+        elif p.model == "rsw":
+            sharp(m, s["u.x"], s["u.y"], s["U.x"], s["U.y"])
+            compute_vorticity(m, s["u.x"], s["u.y"], s["omega"])
+            compute_kinetic_energy(p, m, s["u.x"], s["u.y"], s["U.x"],
+                                   s["U.y"], s["ke"], sq)
+            compute_pressure(p, m, s["h"], s["p"])
+            m.fill(s["omega"])
+            m.fill(s["ke"])
+
+    # -- integrator -----------------------------------------------------
+    def _addto(self, coefs, dss):
+        """addto_list, integrators.py:154-174: y += sum(c*x)."""
+        for k in self.prog:
+            self.s[k][:] += sum((c * d[k] for c, d in zip(coefs, dss)))
+
+    def rk3(self, dt):
+        """integrators.py:92-107."""
+        ds1, ds2, ds3 = self.scratch
+        self.rhs(self.s, ds1)
+        self._addto([dt], [ds1])
+        self.diag()
+        self.rhs(self.s, ds2)
+        self._addto([-3 * dt / 4, dt / 4], [ds1, ds2])
+        self.diag()
+        self.rhs(self.s, ds3)
+        self._addto([-dt / 12, -dt / 12, 2 * dt / 3], [ds1, ds2, ds3])
+        self.diag()
+
+    def pushforward(self):
+        """timeline.py:20-35 (Kahan-summed time)."""
+        y = self.dt - self._c
+        t = self.t + y
+        self._c = (t - self.t) - y
+        self.t = t
+        self.ite += 1
+
+    def set_dt(self):
+        """model.py:71-87."""
+        p = self.p
+        if p.dt > 0:
+            self.dt = p.dt
+            return
+        if p.model == "rsw":
+            c = (p.g * p.H) ** 0.5
+            maxU = c / self.mesh.dx + c / self.mesh.dy
+        else:
+            maxU = (np.max(np.abs(self.s["U.x"])) +
+                    np.max(np.abs(self.s["U.y"])) + 1e-99)
+        self.dt = min(p.cfl / maxU, p.dtmax)
+
+    def step(self, n=1):
+        for _ in range(n):
+            self.rk3(self.dt)
+            self.pushforward()
+
+    def run_steps(self, n):
+        """n iterations of the Model.run loop body: set_dt then step(1)."""
+        dts = []
+        for _ in range(n):
+            self.set_dt()
+            dts.append(self.dt)
+            self.step(1)
+        return dts
+
+
+def num_threads():
+    return int(lib().oracle_num_threads())
+
+
+def rel_l2(a, b, mask=None):
+    a = np.asarray(a, dtype=np.float64)
+    b = np.asarray(b, dtype=np.float64)
+    if mask is not None:
+        a = a[mask]
+        b = b[mask]
+    nb = math.sqrt(float(np.sum(b * b)))
+    d = math.sqrt(float(np.sum((a - b) ** 2)))
+    return d / nb if nb > 0 else d

@@ -1,0 +1,157 @@
+"""Pin the oracle against outputs of the reference itself.
+
+The fixtures in tests/golden/ were produced by the unmodified reference
+(``make_golden.py``). Integer/mask outputs must match exactly; the flux
+sweeps, which the oracle restates expression by expression, must match bit for
+bit; solver and whole-step outputs are compared to 1e-13 relative (SuperLU is
+the same library on both sides, the tolerance only covers a different scipy
+build on another machine).
+"""
+import os
+
+import numpy as np
+import pytest
+
+from conftest import GOLDEN
+from oracle import oracle as O
+
+
+def load(name):
+    return np.load(os.path.join(GOLDEN, name), allow_pickle=False)
+
+
+def _noslip(s):
+    return eval(str(s))  # repr of None / True / list written by the generator
+
+
+@pytest.mark.parametrize("case", list(load("mesh.npz")["names"]))
+def test_mesh_bitexact(case):
+    g = load("mesh.npz")
+    nx, ny, xper, maxo = (int(v) for v in g[case + "/params"])
+    p = O.Param(model="eulerpsi", nx=nx, ny=ny, xperiodic=bool(xper),
+                maxorder=maxo, noslip=_noslip(g[case + "/noslip"]))
+    m = O.Mesh.__new__(O.Mesh)
+    # build like Mesh.__init__ but with the golden mask, without solvers
+    m.param = p
+    m.shape = (ny + 6, nx + 6)
+    m.xshift, m.yshift = 1, nx + 6
+    m.msk = g[case + "/msk"].copy()
+    m.set_masks()
+    for k in ("mskx", "msky", "mskv"):
+        np.testing.assert_array_equal(getattr(m, k), g[case + "/" + k], k)
+    sc = O.slipcoef(p, m.msk)
+    np.testing.assert_array_equal(sc, g[case + "/slipcoef"])
+    mv = (1 * (sc > 0)).astype(np.int8)
+    orders = {
+        "ocx": O.set_order(m.msk, 1, maxo),
+        "ocy": O.set_order(m.msk, nx + 6, maxo),
+        "ovx": O.set_order(mv, -1, maxo) * m.msky,
+        "ovy": O.set_order(mv, -(nx + 6), maxo) * m.mskx,
+        "okx": O.set_order(m.mskx, -1, maxo),
+        "oky": O.set_order(m.msky, -(nx + 6), maxo),
+    }
+    for k, v in orders.items():
+        np.testing.assert_array_equal(v, g[case + "/" + k], k)
+    np.testing.assert_array_equal(O.gindex(O.vertex_msk(m, "c")),
+                                  g[case + "/Gc"])
+    np.testing.assert_array_equal(O.gindex(O.vertex_msk(m, "v")),
+                                  g[case + "/Gv"])
+
+
+@pytest.mark.parametrize("method", ["weno", "upwind", "centered", "cweno"])
+def test_sweeps_bitexact(method):
+    g = load("sweeps.npz")
+    q, U, V = g["q"], g["U"], g["V"]
+    sx, sy = (int(v) for v in g["shifts"])
+    for d, s, s2, sign in (("x", sx, sy, -1), ("y", sy, sx, +1)):
+        flx = np.zeros_like(q)
+        O.compflux(flx, U, q, g["oc" + d], s, method, pysq=True)
+        np.testing.assert_array_equal(flx, g[f"compflux/{method}/{d}"])
+        du = np.zeros_like(q)
+        O.vortexforce(du, V, q, g["ov" + d], s, s2, sign, method, pysq=True)
+        np.testing.assert_array_equal(du, g[f"vortexforce/{method}/{d}"])
+        ke = g[f"innerproduct_in/{method}/{d}"].copy()
+        O.innerproduct(ke, U, q, g["ok" + d], s, method, pysq=True)
+        np.testing.assert_array_equal(ke, g[f"innerproduct/{method}/{d}"])
+
+
+def test_sweeps_numba_square_close():
+    """The x*x entry points (numba semantics) differ by rounding only."""
+    g = load("sweeps.npz")
+    q, U = g["q"], g["U"]
+    flx = np.zeros_like(q)
+    O.compflux(flx, U, q, g["ocx"], 1, "weno", pysq=False)
+    ref = g["compflux/weno/x"]
+    assert np.max(np.abs(flx - ref)) <= 1e-13 * np.max(np.abs(ref))
+
+
+@pytest.mark.parametrize("case", list(load("poisson.npz")["names"]))
+def test_poisson_vs_reference(case):
+    g = load("poisson.npz")
+    nx, ny, xper = (int(v) for v in g[case + "/params"])
+    f0 = float(g[case + "/f0"])
+    model = "qg" if float(g[case + "/maindiag"]) != 0 else "eulerpsi"
+    p = O.Param(model=model, nx=nx, ny=ny, xperiodic=bool(xper), f0=f0)
+    m = O.Model(p, msk=g[case + "/msk"])
+    solver = m.mesh.qg_helmholtz if model == "qg" else m.mesh.poisson_vertices
+    if model == "qg":
+        assert m.mesh.maindiag == float(g[case + "/maindiag"])
+    x = g[case + "/x0"].copy()
+    solver.solve(g[case + "/b"], x)
+    ref = g[case + "/x"]
+    assert np.max(np.abs(x - ref)) <= 1e-13 * np.max(np.abs(ref))
+
+
+MODEL_FILES = ["model_eulerpsi.npz", "model_eulerpsi_islands.npz",
+               "model_rsw.npz", "model_qg.npz"]
+
+
+def oracle_from_golden(g, pysq=True):
+    nx, ny, xper = (int(v) for v in g["params"])
+    Lx, Ly, f0, beta, gg, H, cfl = (float(v) for v in g["scalars"])
+    model = [k for k in g.files if k.startswith("ic/")]
+    names = {k[3:] for k in model}
+    kind = ("eulerpsi" if "omega" in names else
+            "rsw" if "h" in names else "qg")
+    p = O.Param(model=kind, nx=nx, ny=ny, xperiodic=bool(xper), Lx=Lx, Ly=Ly,
+                f0=f0, beta=beta, g=gg, H=H, cfl=cfl, tend=1e9,
+                maxite=10 ** 9)
+    m = O.Model(p, msk=g["msk"], pysq=pysq)
+    if "f" in g.files:
+        m.mesh.f = g["f"].copy()
+    for k in names:
+        m.s[k][:] = g["ic/" + k]
+    m.diag()
+    return m
+
+
+def _compare_state(m, g, prefix, tol):
+    worst = 0.0
+    for k, v in m.s.items():
+        ref = g[f"{prefix}/{k}"]
+        scale = max(np.max(np.abs(ref)), 1e-300)
+        err = np.max(np.abs(v - ref)) / scale
+        assert err <= tol, (prefix, k, err)
+        worst = max(worst, err)
+    return worst
+
+
+@pytest.mark.parametrize("fname", MODEL_FILES)
+def test_model_steps_vs_reference(fname):
+    g = load(fname)
+    m = oracle_from_golden(g)
+    _compare_state(m, g, "step0", 1e-13)
+    # one rhs evaluation on the initial state
+    ds = {k: np.zeros_like(v) for k, v in m.scratch[0].items()}
+    m.rhs(m.s, ds)
+    for k, v in ds.items():
+        ref = g["rhs0/" + k]
+        assert np.max(np.abs(v - ref)) <= 1e-13 * max(np.max(np.abs(ref)),
+                                                       1e-300), k
+    dts = g["dt"]
+    for k in range(1, len(dts) + 1):
+        m.set_dt()
+        assert abs(m.dt - dts[k - 1]) <= 1e-13 * dts[k - 1]
+        m.step(1)
+        _compare_state(m, g, f"step{k}", 1e-12)
+    assert abs(m.t - float(g["t"])) <= 1e-13 * float(g["t"])
