@@ -1,0 +1,393 @@
+"""Benchmark of the time-stepping hot path (one JSON line on stdout).
+
+Metric: cell-updates/s = nx*ny*steps / time (the inverse of the reference's
+own s/dof printout, model.py:89-93). A benchmark step is one model time step
+(SSP-RK3: three fused stage kernels plus their diagnostics) over the whole
+grid. Default workload: the rotating-shallow-water channel, 512x512,
+x-periodic, 3 islands, f=g=H=1, FP64, WENO5, SSP-RK3 (seeded synthetic
+inputs of that configuration's shapes; no dataset is involved).
+
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--impl gb300|reference]
+                  [--workload rsw512|eulerpsi256|qg4096|...]
+
+--impl gb300 (default): device-timed steps with L2 flushed between steps
+(`value`), end-to-end steps through the C ABI with the prognostic state
+copied from/to pinned host memory every step (`e2e`), the dominant kernel
+timed alone for the roofline, and the CPU oracle timed on a bounded sample.
+--impl reference: the reference algorithm's CPU implementation timed on the
+host cores (the oracle port: C sweeps threaded over all cores + numpy
+operators + SuperLU), on the same workload.
+Under torchrun (N > 1) every rank advances its own replica (no collective on
+the data path); the throughput is summed over ranks and timed by the slowest.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+WORKLOADS = {
+    # name: (model, builder kwargs, description)
+    "rsw512": ("rsw", dict(n=512, seed=0, nislands=3),
+               "rsw 512x512 x-periodic channel, 3 islands, f=g=H=1, WENO5, "
+               "SSP-RK3, FP64"),
+    "eulerpsi256": ("eulerpsi", dict(n=256, seed=0),
+                    "eulerpsi 256x256 closed basin, 8 Gaussian vortices, "
+                    "WENO5, SSP-RK3, cfl 0.8, FP64, MG-PCG vertex Poisson"),
+    "eulerpsi512": ("eulerpsi", dict(n=512, seed=0),
+                    "eulerpsi 512x512 closed basin, 8 Gaussian vortices, FP64"),
+    "qg4096": ("qg", dict(n=4096, seed=0, nislands=20),
+               "qg 4096x4096 basin, 20 islands, Rd=0.02, beta=1, FP64, "
+               "MG-PCG Helmholtz"),
+    "qg1024": ("qg", dict(n=1024, seed=0, nislands=20),
+               "qg 1024x1024 basin, 20 islands, Rd=0.02, beta=1, FP64"),
+}
+
+L2_BYTES = 126 * 2 ** 20
+
+
+def build_case(name):
+    from fluids2d_gb300 import workloads as wl
+    model, kw, desc = WORKLOADS[name]
+    if model == "rsw":
+        case = wl.rsw_case(**kw)
+    elif model == "eulerpsi":
+        case = wl.eulerpsi_case(**kw)
+    else:
+        case = wl.qg_case(**kw)
+    return model, case, desc
+
+
+def make_gpu_model(model, case, stream_ptr):
+    import fluids2d_gb300 as f2d
+    from fluids2d_gb300._lib import check, lib
+    p = f2d.Param()
+    p.model = model
+    p.nx, p.ny = case["nx"], case["ny"]
+    p.Lx, p.Ly = case["Lx"], case["Ly"]
+    p.xperiodic = case.get("xperiodic", False)
+    for k in ("f0", "g", "H", "beta"):
+        if k in case:
+            setattr(p, k, case[k])
+    if model == "eulerpsi":
+        p.cfl = 0.8
+    p.tend = 1e300
+    p.maxite = 10 ** 12
+    m = f2d.Model(p)
+    check(lib().f2d_model_set_stream(m._h, stream_ptr))
+    m.mesh.msk[:] = case["msk"]
+    m.mesh.finalize()
+    if "f" in case:
+        m.mesh.f = case["f"]
+    s = m.state
+    for k, v in case["fields"].items():
+        getattr(s, k)[:] = v
+    m.integrator.diag(s)
+    return m
+
+
+def prognostic_names(model):
+    return {"rsw": ["u.x", "u.y", "h"], "eulerpsi": ["omega"],
+            "qg": ["pv"]}[model]
+
+
+# algorithmic bytes per array point of the stage-2 launch of the fused stage
+# kernel (FP64): distinct arrays read + written once each
+STAGE2_BYTES = {
+    # rsw: read u.x,u.y,h,U.x,U.y,ke,p,omega + 3 ds1 (11 x 8) + code (4);
+    #      write u.x,u.y,h + 3 ds2 (6 x 8)
+    "rsw": 11 * 8 + 4 + 6 * 8,
+    # flux form: read q,U.x,U.y,ds1 (4 x 8) + code (4); write q, ds2 (2 x 8)
+    "eulerpsi": 4 * 8 + 4 + 2 * 8,
+    "qg": 4 * 8 + 4 + 2 * 8,
+}
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons sampled during the timed region."""
+    Q = ("clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+         "clocks_event_reasons.hw_slowdown,"
+         "clocks_event_reasons.hw_thermal_slowdown,"
+         "clocks_event_reasons.sw_thermal_slowdown,"
+         "clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index):
+        self.index = index
+        self.rows = []
+        self.proc = None
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.index), "--query-gpu=" + self.Q,
+                 "--format=csv,noheader,nounits", "-lms", "200"],
+                stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.thread = threading.Thread(target=self._read, daemon=True)
+            self.thread.start()
+        except OSError:
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            parts = [x.strip() for x in line.split(",")]
+            if len(parts) >= 8:
+                self.rows.append(parts)
+
+    def __exit__(self, *a):
+        if self.proc is not None:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+
+    def summary(self):
+        if not self.rows:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unsampled"]}
+        sm = [float(r[0]) for r in self.rows if r[0].replace(".", "").isdigit()]
+        mx = [float(r[1]) for r in self.rows if r[1].replace(".", "").isdigit()]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown",
+                 "sw_power_cap"]
+        reasons = set()
+        for r in self.rows:
+            for k, n in enumerate(names):
+                if r[4 + k].lower() == "active":
+                    reasons.add(n)
+        return {"sm_mhz": statistics.median(sm) if sm else None,
+                "sm_max_mhz": max(mx) if mx else None,
+                "reasons": sorted(reasons), "samples": len(self.rows)}
+
+
+def read_profile_traffic(kernel):
+    """DRAM bytes per launch of `kernel` from the committed ncu summary."""
+    path = os.path.join(ROOT, "profiles", f"{kernel}.md")
+    if not os.path.exists(path):
+        return None
+    for line in open(path):
+        if line.startswith("traffic_bytes_per_launch:"):
+            try:
+                return float(line.split(":", 1)[1].split()[0])
+            except ValueError:
+                return None
+    return None
+
+
+def cpu_oracle_rate(model, case, budget_s, max_steps=None, warmup=1):
+    """Oracle port (C sweeps on all host threads + numpy + SuperLU)."""
+    from oracle import oracle as O
+    p = O.Param(model=model, nx=case["nx"], ny=case["ny"],
+                xperiodic=case.get("xperiodic", False), Lx=case["Lx"],
+                Ly=case["Ly"], tend=1e300, maxite=10 ** 12)
+    for k in ("f0", "g", "H", "beta"):
+        if k in case:
+            setattr(p, k, case[k])
+    if model == "eulerpsi":
+        p.cfl = 0.8
+    om = O.Model(p, msk=case["msk"], pysq=False)
+    if "f" in case:
+        om.mesh.f = case["f"].copy()
+    for k, v in case["fields"].items():
+        om.s[k][:] = v
+    om.diag()
+    om.run_steps(warmup)
+    n = 0
+    t0 = time.perf_counter()
+    while True:
+        om.run_steps(1)
+        n += 1
+        el = time.perf_counter() - t0
+        if el >= budget_s or (max_steps and n >= max_steps):
+            break
+    cells = case["nx"] * case["ny"]
+    return cells * n / el, n, el, O.num_threads()
+
+
+def run_reference(args, rank, world):
+    """--impl reference: the CPU implementation of the path on host cores."""
+    model, case, desc = build_case(args.workload)
+    budget = float(os.environ.get("F2D_REF_BUDGET_S", "60"))
+    rate, n, el, cores = cpu_oracle_rate(model, case, budget,
+                                         max_steps=args.steps,
+                                         warmup=min(args.warmup, 1))
+    line = {
+        "metric": "cell-updates/s", "value": rate, "unit": "cell-updates/s",
+        "impl": "reference", "n_gpus": args.gpus, "steps": n,
+        "warmup": args.warmup, "ms_per_step": 1e3 * el / n,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+        "dtype": "f64", "data": "synthetic",
+        "config": {"workload": args.workload, "desc": desc},
+        "cpu_baseline": {
+            "value": rate, "unit": "cell-updates/s", "cores": cores,
+            "kind": "port",
+            "sample": f"{n} model steps (of the requested {args.steps}) of "
+                      f"{args.workload} on {cores} host threads, "
+                      f"{el:.1f} s, after {min(args.warmup, 1)} warm-up"},
+        "e2e": {"value": rate, "unit": "cell-updates/s",
+                "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+
+
+def run_gpu(args, rank, world):
+    import torch
+    dev = int(os.environ.get("LOCAL_RANK", "0"))
+    torch.cuda.set_device(dev)
+    from fluids2d_gb300._lib import check, lib
+    import ctypes
+
+    model, case, desc = build_case(args.workload)
+    stream = torch.cuda.current_stream()
+    m = make_gpu_model(model, case, ctypes.c_void_p(stream.cuda_stream))
+    h = m._h
+    L = lib()
+    cells = case["nx"] * case["ny"]
+    flush = torch.empty(2 * L2_BYTES // 4, dtype=torch.float32, device="cuda")
+
+    # warm-up (graph capture happens here)
+    for _ in range(args.warmup):
+        check(L.f2d_run(h, 1))
+    check(L.f2d_sync(h))
+    it0 = m.poisson_iterations()
+
+    # ---- device-timed steps, L2 flushed between steps ----------------------
+    ev0 = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
+    ev1 = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
+    if world > 1:
+        import torch.distributed as dist
+        dist.barrier()
+    torch.cuda.synchronize()
+    with ClockSampler(dev) as clk:
+        for k in range(args.steps):
+            flush.zero_()
+            ev0[k].record(stream)
+            check(L.f2d_run(h, 1))
+            ev1[k].record(stream)
+        torch.cuda.synchronize()
+    check(L.f2d_sync(h))
+    ms = sum(a.elapsed_time(b) for a, b in zip(ev0, ev1))
+    pcg_iters = m.poisson_iterations() - it0
+    if world > 1:
+        import torch.distributed as dist
+        t = torch.tensor([ms], device="cuda", dtype=torch.float64)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        ms = float(t.item())
+        dist.barrier()
+    value = world * cells * args.steps / (ms / 1e3)
+
+    # ---- end to end through the C ABI with pinned host state ---------------
+    names = prognostic_names(model)
+    host = {}
+    for n in names:
+        t = torch.empty((case["ny"] + 6, case["nx"] + 6), dtype=torch.float64,
+                        pin_memory=True)
+        host[n] = t
+        check(L.f2d_field_get(h, n.encode(), ctypes.c_void_p(t.data_ptr())))
+    e2e_steps = max(1, min(args.steps, 200))
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    for _ in range(e2e_steps):
+        for n in names:
+            check(L.f2d_field_set_async(h, n.encode(),
+                                        ctypes.c_void_p(host[n].data_ptr())))
+        check(L.f2d_run(h, 1))
+        for n in names:
+            check(L.f2d_field_get_async(h, n.encode(),
+                                        ctypes.c_void_p(host[n].data_ptr())))
+    check(L.f2d_sync(h))
+    e2e_s = time.perf_counter() - t0
+    bytes_io = len(names) * (case["ny"] + 6) * (case["nx"] + 6) * 8
+    e2e = world * cells * e2e_steps / e2e_s
+
+    # ---- roofline of the dominant kernel: the fused stage kernel -----------
+    avg = ctypes.c_double()
+    check(L.f2d_time_stage(h, 2, 20, 1, ctypes.byref(avg)))
+    npts = (case["ny"] + 6) * (case["nx"] + 6)
+    alg_bytes = STAGE2_BYTES[model] * npts
+    achieved = alg_bytes / (avg.value * 1e-3) / 1e9
+    peaks = {}
+    try:
+        peaks = json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json")))
+        peak, peak_src = float(peaks["hbm_gbs"]), "measured"
+    except Exception:
+        peak, peak_src = 6800.0, "fallback"
+    kname = {"rsw": "k_rsw_stage", "eulerpsi": "k_fluxform_stage",
+             "qg": "k_fluxform_stage"}[model]
+    traffic = read_profile_traffic(f"{kname}_{args.workload}")
+
+    # launches in the timed region: fixed kernels per step + Poisson bodies
+    _, nfix, body = m.stats()
+    launches = nfix * args.steps + body * pcg_iters
+
+    line = {
+        "metric": "cell-updates/s", "value": value, "unit": "cell-updates/s",
+        "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": ms / args.steps, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+        "data": "synthetic",
+        "config": {"workload": args.workload, "desc": desc,
+                   "grid": [case["ny"], case["nx"]],
+                   "l2": "flushed between timed steps (256 MB write)",
+                   "parallelism": f"replicas x{world}"},
+        "e2e": {"value": e2e, "unit": "cell-updates/s",
+                "h2d_bytes_per_step": bytes_io, "d2h_bytes_per_step": bytes_io,
+                "steps": e2e_steps},
+        "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak,
+                     "unit": "GB/s", "frac": achieved / peak,
+                     "traffic": traffic, "kernel": kname,
+                     "kernel_ms": avg.value, "alg_bytes_per_launch": alg_bytes,
+                     "peak_source": peak_src},
+        "gpu_launches": launches,
+        "poisson_iters": pcg_iters,
+        "clocks": clk.summary(),
+    }
+    if rank == 0 and not args.no_cpu_baseline:
+        budget = float(os.environ.get("F2D_CPU_BUDGET_S", "15"))
+        rate, n, el, cores = cpu_oracle_rate(model, case, budget)
+        line["cpu_baseline"] = {
+            "value": rate, "unit": "cell-updates/s", "cores": cores,
+            "kind": "port",
+            "sample": f"{n} model steps of {args.workload} after 1 warm-up, "
+                      f"{el:.1f} s on {cores} host threads"}
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=200)
+    ap.add_argument("--warmup", type=int, default=5)
+    ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--workload", default="rsw512", choices=sorted(WORKLOADS))
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    args = ap.parse_args()
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    if args.impl == "reference":
+        if rank == 0:
+            run_reference(args, rank, world)
+        return
+    if world > 1:
+        import torch
+        import torch.distributed as dist
+        torch.cuda.set_device(int(os.environ.get("LOCAL_RANK", "0")))
+        dist.init_process_group("nccl")
+    run_gpu(args, rank, world)
+    if world > 1:
+        import torch.distributed as dist
+        dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,873 @@
+// C ABI of the library: models, fields, time stepping captured into CUDA
+// graphs, and the Poisson solve (include/fluids2d_gb300.h).
+#include <cudaTypedefs.h>
+
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <map>
+#include <string>
+#include <vector>
+
+#include "../../include/fluids2d_gb300.h"
+#include "mesh_host.h"
+#include "mg.cuh"
+#include "stage.cuh"
+
+namespace f2d {
+int launch_compflux(int, double*, const double*, const double*, const int8_t*, long long,
+                    long long, long long, cudaStream_t);
+int launch_vortexforce(int, double*, const double*, const double*, const int8_t*,
+                       long long, long long, int, long long, long long, cudaStream_t);
+int launch_innerproduct(int, double*, const double*, const double*, const int8_t*,
+                        long long, long long, long long, cudaStream_t);
+}  // namespace f2d
+
+using namespace f2d;
+
+static thread_local std::string g_err;
+
+static int fail(int code, const std::string& msg)
+{
+    g_err = msg;
+    return code ? code : 1;
+}
+
+#define CK(call)                                                                   \
+    do {                                                                           \
+        cudaError_t e_ = (call);                                                   \
+        if (e_ != cudaSuccess)                                                     \
+            return fail((int)e_, std::string(#call) + ": " + cudaGetErrorString(e_)); \
+    } while (0)
+
+#define CKI(call)                                                  \
+    do {                                                           \
+        int e_ = (call);                                           \
+        if (e_)                                                    \
+            return fail(e_, std::string(#call) + ": " +            \
+                                cudaGetErrorString((cudaError_t)e_)); \
+    } while (0)
+
+// ---------------------------------------------------------------------------
+static PFN_cuTensorMapEncodeTiled_v12000 encode_fn()
+{
+    static PFN_cuTensorMapEncodeTiled_v12000 fn = nullptr;
+    if (!fn) {
+        void* ptr = nullptr;
+        cudaDriverEntryPointQueryResult q;
+        if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &ptr, 12000,
+                                             cudaEnableDefault, &q) == cudaSuccess &&
+            q == cudaDriverEntryPointSuccess)
+            fn = (PFN_cuTensorMapEncodeTiled_v12000)ptr;
+    }
+    return fn;
+}
+
+struct Field {
+    void* buf[2] = {nullptr, nullptr};
+    bool pingpong = false;
+};
+
+struct f2d_model_s {
+    f2d_params p;
+    Geom g;
+    MeshHost mesh;
+    int prec = 0;
+    size_t es = 8;
+    cudaStream_t stream = nullptr, s2 = nullptr;
+    bool own_stream = false;
+    uint32_t* d_code = nullptr;
+    uint8_t* d_gmask = nullptr;
+    void* d_fv = nullptr;  // mesh.f (qg beta-plane)
+    DevScalars* sc = nullptr;
+    double* partials = nullptr;
+    std::map<std::string, Field> fields;
+    std::vector<void*> allocs;
+    double dx, dy, area, rdx2, rdy2, goa, fc, maindiag, cx, cy, dt_const;
+    bool cfl_dt = true;
+    bool dt_applied = false;  // the constant dt of set_dt is in sc->dt
+    // multigrid: [0] vertex Poisson, [1] Helmholtz
+    MGHost mg[2];
+    bool mg_ready[2] = {false, false};
+    void *pr = nullptr, *pz = nullptr, *pp = nullptr, *pq = nullptr;
+    void *sb = nullptr, *sx = nullptr;  // scratch for f2d_poisson_solve
+    std::map<void*, CUtensorMap> tmaps;
+    int cur = 0;
+    // graphs: [kind][parity]; kinds: 0 diag, 1 step, 2 run, 3 solve0, 4 solve1
+    cudaGraphExec_t gx[5][2] = {};
+    int launches[5][2] = {};
+    int body_launches = 0;
+    int rec_launches = 0;
+};
+
+static void* dalloc(f2d_model_s* m, size_t bytes)
+{
+    void* p = nullptr;
+    if (cudaMalloc(&p, bytes) != cudaSuccess) return nullptr;
+    cudaMemset(p, 0, bytes);
+    m->allocs.push_back(p);
+    return p;
+}
+
+static size_t field_bytes(const f2d_model_s* m) { return (size_t)m->g.P * m->g.NY * m->es; }
+
+static int add_field(f2d_model_s* m, const char* name, bool pp)
+{
+    Field f;
+    f.pingpong = pp;
+    for (int k = 0; k < (pp ? 2 : 1); ++k) {
+        f.buf[k] = dalloc(m, field_bytes(m));
+        if (!f.buf[k]) return fail(2, std::string("out of device memory for ") + name);
+    }
+    m->fields[name] = f;
+    return 0;
+}
+
+static void* fb(f2d_model_s* m, const char* name, int parity = -1)
+{
+    auto it = m->fields.find(name);
+    if (it == m->fields.end()) return nullptr;
+    const Field& f = it->second;
+    if (!f.pingpong) return f.buf[0];
+    return f.buf[parity < 0 ? m->cur : parity];
+}
+
+static int make_tmap(f2d_model_s* m, void* buf)
+{
+    if (m->tmaps.count(buf)) return 0;
+    auto fn = encode_fn();
+    if (!fn) return fail(3, "cuTensorMapEncodeTiled is not available from the driver");
+    CUtensorMap map;
+    cuuint64_t dims[2] = {(cuuint64_t)m->g.NX, (cuuint64_t)m->g.NY};
+    cuuint64_t strides[1] = {(cuuint64_t)(m->g.P * m->es)};
+    cuuint32_t box[2] = {40, 14};  // tile + halo, stage.cu SW x SH
+    cuuint32_t estr[2] = {1, 1};
+    CUresult r = fn(&map, m->prec == 0 ? CU_TENSOR_MAP_DATA_TYPE_FLOAT64
+                                       : CU_TENSOR_MAP_DATA_TYPE_FLOAT32,
+                    2, buf, dims, strides, box, estr, CU_TENSOR_MAP_INTERLEAVE_NONE,
+                    CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_128B,
+                    CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+    if (r != CUDA_SUCCESS) return fail(3, "cuTensorMapEncodeTiled failed: " + std::to_string((int)r));
+    m->tmaps[buf] = map;
+    return 0;
+}
+
+static const CUtensorMap* tmap(f2d_model_s* m, void* buf) { return &m->tmaps[buf]; }
+
+// ---------------------------------------------------------------------------
+// Recording of diag / stage / step on a stream (eager or under capture).
+// ---------------------------------------------------------------------------
+static int ensure_mg(f2d_model_s* m, int which)
+{
+    if (m->mg_ready[which]) return 0;
+    const Geom& g = m->g;
+    std::vector<uint8_t> hm((size_t)g.P * g.NY, 0);
+    for (int j = 0; j < g.NY; ++j)
+        for (int i = 0; i < g.NX; ++i)
+            hm[(size_t)j * g.P + i] = m->mesh.gv[(size_t)j * g.NX + i] >= 0 ? 1 : 0;
+    // fluid vertices must lie in the node box (3+J, 3+I) of level 0
+    const int nyn = g.ny + 1, nxn = g.xper ? g.nx : g.nx + 1;
+    for (int j = 0; j < g.NY; ++j)
+        for (int i = 0; i < g.NX; ++i)
+            if (hm[(size_t)j * g.P + i] &&
+                (j < 3 || j >= 3 + nyn || i < 3 || i >= 3 + nxn))
+                return fail(4, "fluid vertex outside the interior (mask halo must be 0)");
+    const double md = which == 0 ? 0.0 : m->maindiag;
+    int e = mg_build(m->mg[which], nyn, nxn, g.P, 3 * g.P + 3, g.xper, hm.data(),
+                     m->d_gmask, m->pz, m->pr, m->cx, m->cy, md, m->prec);
+    if (e) return fail(e, "multigrid setup failed");
+    m->mg_ready[which] = true;
+    return 0;
+}
+
+static int rec_solve(f2d_model_s* m, int which, const void* b, void* x, cudaStream_t s)
+{
+    int e = ensure_mg(m, which);
+    if (e) return e;
+    PCGVecs v;
+    v.x = x;
+    v.b = b;
+    v.r = m->pr;
+    v.z = m->pz;
+    v.p = m->pp;
+    v.q = m->pq;
+    v.partials = m->partials;
+    const MGHost& mg = m->mg[which];
+    const int nl = (int)mg.lev.size();
+    m->body_launches = 3 * 2 * mg.ltail + 1 + 4;
+    (void)nl;
+    m->rec_launches += 2;
+    CKI(pcg_record(m->mg[which], v, m->sc, m->p.poisson_tol, m->p.poisson_maxit, s, m->s2));
+    if (m->g.xper) {
+        CKI(launch_fill_periodic(m->prec, x, m->g, s));
+        m->rec_launches += 1;
+    }
+    return 0;
+}
+
+static int rec_diag(f2d_model_s* m, int par, cudaStream_t s)
+{
+    const Geom& g = m->g;
+    switch (m->p.model) {
+    case F2D_MODEL_EULERPSI: {
+        CKI(launch_c2v(m->prec, fb(m, "omega", par), fb(m, "vomega"), m->d_code, nullptr, g, s));
+        m->rec_launches += 1;
+        int e = rec_solve(m, 0, fb(m, "vomega"), fb(m, "psi"), s);
+        if (e) return e;
+        CKI(launch_perpgrad(m->prec, fb(m, "psi"), fb(m, "U.x"), fb(m, "U.y"), m->d_code,
+                            m->rdy2, m->rdx2, 1, g, m->sc, m->partials, s));
+        m->rec_launches += 1;
+        return 0;
+    }
+    case F2D_MODEL_QG: {
+        const void* fv = m->p.beta != 0 ? m->d_fv : nullptr;
+        CKI(launch_c2v(m->prec, fb(m, "pv", par), fb(m, "work"), m->d_code, fv, g, s));
+        m->rec_launches += 1;
+        int e = rec_solve(m, 1, fb(m, "work"), fb(m, "psi"), s);
+        if (e) return e;
+        CKI(launch_perpgrad(m->prec, fb(m, "psi"), fb(m, "U.x"), fb(m, "U.y"), m->d_code,
+                            m->rdy2, m->rdx2, 0, g, m->sc, m->partials, s));
+        m->rec_launches += 1;
+        return 0;
+    }
+    case F2D_MODEL_RSW: {
+        RswDiag a;
+        a.ux = fb(m, "u.x", par);
+        a.uy = fb(m, "u.y", par);
+        a.h = fb(m, "h", par);
+        a.Ux = fb(m, "U.x");
+        a.Uy = fb(m, "U.y");
+        a.omega = fb(m, "omega");
+        a.ke = fb(m, "ke");
+        a.p = fb(m, "p");
+        a.rdx2 = m->rdx2;
+        a.rdy2 = m->rdy2;
+        a.goa = m->goa;
+        CKI(make_tmap(m, (void*)a.ux));
+        CKI(make_tmap(m, (void*)a.uy));
+        CKI(launch_rsw_diag(m->p.innerproduct, m->prec, tmap(m, (void*)a.ux),
+                            tmap(m, (void*)a.uy), a, m->d_code, g, m->sc, s));
+        m->rec_launches += 1;
+        return 0;
+    }
+    }
+    return fail(5, "unknown model");
+}
+
+// the fused right-hand-side + RK3-update kernel of stage k, parity par -> 1-par
+static int launch_stage_kernel(f2d_model_s* m, int k, int par, cudaStream_t s)
+{
+    const Geom& g = m->g;
+    const int out = 1 - par;
+    auto ds = [&](const char* f, int kk) -> void* {
+        return fb(m, (std::string("ds") + std::to_string(kk) + "." + f).c_str());
+    };
+    if (m->p.model == F2D_MODEL_RSW) {
+        RswIn a;
+        memset(&a, 0, sizeof(a));
+        a.ux = fb(m, "u.x", par);
+        a.uy = fb(m, "u.y", par);
+        a.h = fb(m, "h", par);
+        a.uxo = fb(m, "u.x", out);
+        a.uyo = fb(m, "u.y", out);
+        a.ho = fb(m, "h", out);
+        a.Ux = fb(m, "U.x");
+        a.Uy = fb(m, "U.y");
+        a.ke = fb(m, "ke");
+        a.p = fb(m, "p");
+        if (k < 3) {
+            a.dux = ds("u.x", k);
+            a.duy = ds("u.y", k);
+            a.dh = ds("h", k);
+        }
+        a.dux1 = ds("u.x", 1);
+        a.duy1 = ds("u.y", 1);
+        a.dh1 = ds("h", 1);
+        a.dux2 = ds("u.x", 2);
+        a.duy2 = ds("u.y", 2);
+        a.dh2 = ds("h", 2);
+        a.fc = m->fc;
+        void* om = fb(m, "omega");
+        CKI(make_tmap(m, (void*)a.h));
+        CKI(make_tmap(m, om));
+        CKI(launch_rsw_stage(m->p.vortexforce, m->prec, tmap(m, (void*)a.h), tmap(m, om), a,
+                             m->d_code, k, g, m->sc, s));
+    } else {
+        const char* q = m->p.model == F2D_MODEL_EULERPSI ? "omega" : "pv";
+        void* qin = fb(m, q, par);
+        CKI(make_tmap(m, qin));
+        CKI(launch_fluxform_stage(m->p.compflux, m->prec, tmap(m, qin), qin, fb(m, q, out),
+                                  fb(m, "U.x"), fb(m, "U.y"), m->d_code,
+                                  k < 3 ? ds(q, k) : nullptr, ds(q, 1), ds(q, 2), k, g,
+                                  m->sc, s));
+    }
+    m->rec_launches += 1;
+    return 0;
+}
+
+// one RK3 stage from parity `par` to 1-par, then the diagnostics
+static int rec_stage(f2d_model_s* m, int k, int par, cudaStream_t s)
+{
+    int e = launch_stage_kernel(m, k, par, s);
+    if (e) return e;
+    return rec_diag(m, 1 - par, s);
+}
+
+static int rec_step(f2d_model_s* m, int par, bool with_dt, cudaStream_t s)
+{
+    if (with_dt && m->cfl_dt) {
+        CKI(launch_set_dt(m->sc, s));
+        m->rec_launches += 1;
+    }
+    for (int k = 1; k <= 3; ++k) {
+        int e = rec_stage(m, k, par, s);
+        if (e) return e;
+        par = 1 - par;
+    }
+    CKI(launch_pushforward(m->sc, s));
+    m->rec_launches += 1;
+    return 0;
+}
+
+// capture kind (0 diag, 1 step, 2 run) for the current parity, then launch
+static int run_graph(f2d_model_s* m, int kind)
+{
+    const int par = m->cur;
+    if (!m->gx[kind][par]) {
+        // multigrid set-up allocates, so it happens before the capture
+        if (m->p.model != F2D_MODEL_RSW) {
+            int e0 = ensure_mg(m, m->p.model == F2D_MODEL_EULERPSI ? 0 : 1);
+            if (e0) return e0;
+        }
+        m->rec_launches = 0;
+        CK(cudaStreamBeginCapture(m->stream, cudaStreamCaptureModeRelaxed));
+        int e = 0;
+        if (kind == 0) e = rec_diag(m, par, m->stream);
+        else e = rec_step(m, par, kind == 2, m->stream);
+        cudaGraph_t graph = nullptr;
+        cudaError_t ce = cudaStreamEndCapture(m->stream, &graph);
+        if (e) {
+            if (graph) cudaGraphDestroy(graph);
+            return e;
+        }
+        if (ce != cudaSuccess) return fail((int)ce, std::string("capture: ") + cudaGetErrorString(ce));
+        cudaGraphExec_t ex;
+        ce = cudaGraphInstantiate(&ex, graph, 0);
+        cudaGraphDestroy(graph);
+        if (ce != cudaSuccess)
+            return fail((int)ce, std::string("graph instantiate: ") + cudaGetErrorString(ce));
+        m->gx[kind][par] = ex;
+        m->launches[kind][par] = m->rec_launches;
+    }
+    CK(cudaGraphLaunch(m->gx[kind][par], m->stream));
+    if (kind != 0) m->cur = 1 - par;  // three stages flip the parity
+    return 0;
+}
+
+static void drop_graphs(f2d_model_s* m)
+{
+    for (auto& k : m->gx)
+        for (auto& e : k)
+            if (e) {
+                cudaGraphExecDestroy(e);
+                e = nullptr;
+            }
+}
+
+static int setup_mesh(f2d_model_s* m, const int8_t* msk)
+{
+    std::string err;
+    if (mesh_build_host(m->p, msk, m->mesh, err)) return fail(7, err);
+    const Geom& g = m->g;
+    std::vector<uint32_t> code((size_t)g.P * g.NY, 0);
+    std::vector<uint8_t> gm((size_t)g.P * g.NY, 0);
+    for (int j = 0; j < g.NY; ++j)
+        for (int i = 0; i < g.NX; ++i) {
+            code[(size_t)j * g.P + i] = m->mesh.code[(size_t)j * g.NX + i];
+            gm[(size_t)j * g.P + i] = m->mesh.gv[(size_t)j * g.NX + i] >= 0;
+        }
+    CK(cudaMemcpy(m->d_code, code.data(), code.size() * 4, cudaMemcpyHostToDevice));
+    CK(cudaMemcpy(m->d_gmask, gm.data(), gm.size(), cudaMemcpyHostToDevice));
+    for (int w = 0; w < 2; ++w) {
+        mg_free(m->mg[w]);
+        m->mg_ready[w] = false;
+    }
+    drop_graphs(m);
+    return 0;
+}
+
+// ---------------------------------------------------------------------------
+extern "C" {
+
+int f2d_abi_version(void) { return F2D_ABI_VERSION; }
+const char* f2d_last_error(void) { return g_err.c_str(); }
+
+int f2d_params_default(f2d_params* p)
+{
+    if (!p) return fail(1, "null params");
+    memset(p, 0, sizeof(*p));
+    p->model = F2D_MODEL_EULERPSI;
+    p->nx = 40;
+    p->ny = 40;
+    p->halowidth = 3;
+    p->Lx = 1.0;
+    p->Ly = 1.0;
+    p->f0 = 10.0;
+    p->beta = 0.0;
+    p->g = 1.0;
+    p->H = 1.0;
+    p->cfl = 0.9;
+    p->dtmax = 9e99;
+    p->dt = 0.0;
+    p->compflux = p->vortexforce = p->innerproduct = F2D_METHOD_WENO;
+    p->maxorder = 6;
+    p->noslip = F2D_SLIP_FREE;
+    p->precision = F2D_PREC_FP64;
+    p->poisson_tol = 1e-12;
+    p->poisson_maxit = 200;
+    return 0;
+}
+
+int f2d_set_order(const int8_t* msk, int64_t n, int64_t shift, int maxorder, int8_t* order)
+{
+    if (!msk || !order || n < 0) return fail(1, "bad arguments");
+    set_order_host(msk, n, shift, maxorder, order);
+    return 0;
+}
+
+int f2d_mesh_build(const f2d_params* p, const int8_t* msk, int8_t* mskx, int8_t* msky,
+                   int8_t* mskv, double* slipcoef, int8_t* orders, int32_t* gv)
+{
+    if (!p) return fail(1, "null params");
+    MeshHost M;
+    std::string err;
+    if (mesh_build_host(*p, msk, M, err)) return fail(7, err);
+    const size_t N = (size_t)M.NY * M.NX;
+    if (mskx) memcpy(mskx, M.mskx.data(), N);
+    if (msky) memcpy(msky, M.msky.data(), N);
+    if (mskv) memcpy(mskv, M.mskv.data(), N);
+    if (slipcoef) memcpy(slipcoef, M.slip.data(), N * 8);
+    if (orders)
+        for (int k = 0; k < 6; ++k) memcpy(orders + k * N, M.ord[k].data(), N);
+    if (gv) memcpy(gv, M.gv.data(), N * 4);
+    return 0;
+}
+
+int f2d_compflux(int method, double* flx, const double* U, const double* q, const int8_t* o,
+                 int64_t s, int64_t i0, int64_t i1, void* stream)
+{
+    CKI(launch_compflux(method, flx, U, q, o, s, i0, i1, (cudaStream_t)stream));
+    return 0;
+}
+
+int f2d_vortexforce(int method, double* du, const double* V, const double* q,
+                    const int8_t* o, int64_t s, int64_t s2, int sign, int64_t i0, int64_t i1,
+                    void* stream)
+{
+    CKI(launch_vortexforce(method, du, V, q, o, s, s2, sign, i0, i1, (cudaStream_t)stream));
+    return 0;
+}
+
+int f2d_innerproduct(int method, double* ke, const double* U, const double* q,
+                     const int8_t* o, int64_t s, int64_t i0, int64_t i1, void* stream)
+{
+    CKI(launch_innerproduct(method, ke, U, q, o, s, i0, i1, (cudaStream_t)stream));
+    return 0;
+}
+
+int f2d_model_create(const f2d_params* p, const int8_t* msk, f2d_model* out)
+{
+    if (!p || !out) return fail(1, "null argument");
+    if (p->precision != F2D_PREC_FP64 && p->precision != F2D_PREC_FP32)
+        return fail(1, "unknown precision");
+    if (p->model < 0 || p->model > 2) return fail(1, "unknown model");
+    if (p->xperiodic && p->nx < 6) return fail(1, "x-periodic needs nx >= 6");
+    if (p->model == F2D_MODEL_RSW && p->vortexforce != p->compflux)
+        return fail(1, "the fused rsw stage uses one flux method for vortexforce and "
+                       "compflux; they must be equal");
+    auto* m = new f2d_model_s();
+    m->p = *p;
+    m->prec = p->precision == F2D_PREC_FP64 ? 0 : 1;
+    m->es = m->prec == 0 ? 8 : 4;
+    Geom& g = m->g;
+    g.ny = p->ny;
+    g.nx = p->nx;
+    g.NY = p->ny + 6;
+    g.NX = p->nx + 6;
+    g.P = (g.NX + 15) / 16 * 16;
+    g.xper = p->xperiodic ? 1 : 0;
+    // mesh constants, evaluated like the reference's Python expressions
+    m->dx = p->Lx / p->nx;
+    m->dy = p->Ly / p->ny;
+    m->area = m->dx * m->dy;
+    m->rdx2 = 1 / pow(m->dx, 2.0);
+    m->rdy2 = 1 / pow(m->dy, 2.0);
+    m->goa = p->g / m->area;
+    m->fc = p->f0 * m->area * 0.25;
+    m->maindiag = m->area * pow(p->f0, 2.0) / (p->g * p->H);
+    m->cx = m->dy / m->dx;  // dx2 of get_Laplacian_sparse (E-W)
+    m->cy = m->dx / m->dy;  // dy2 (N-S)
+    int e = 0;
+    auto bail = [&](int code) {
+        f2d_model_destroy(m);
+        return code;
+    };
+    if (cudaStreamCreateWithFlags(&m->stream, cudaStreamNonBlocking) != cudaSuccess ||
+        cudaStreamCreateWithFlags(&m->s2, cudaStreamNonBlocking) != cudaSuccess)
+        return bail(fail(2, "stream creation failed"));
+    m->own_stream = true;
+    m->d_code = (uint32_t*)dalloc(m, (size_t)g.P * g.NY * 4);
+    m->d_gmask = (uint8_t*)dalloc(m, (size_t)g.P * g.NY);
+    m->sc = (DevScalars*)dalloc(m, sizeof(DevScalars));
+    const size_t nb = pt_grid_blocks(g) + 64;
+    m->partials = (double*)dalloc(m, nb * 4 * sizeof(double));
+    if (!m->d_code || !m->d_gmask || !m->sc || !m->partials)
+        return bail(fail(2, "out of device memory"));
+    // fields of the state (states.py:7-17) and of the RK3 scratch
+    std::vector<std::pair<const char*, bool>> fl;
+    std::vector<const char*> prog;
+    if (p->model == F2D_MODEL_EULERPSI) {
+        fl = {{"omega", true}, {"U.x", false}, {"U.y", false}, {"psi", false},
+              {"vomega", false}, {"flx.x", false}, {"flx.y", false}};
+        prog = {"omega"};
+    } else if (p->model == F2D_MODEL_RSW) {
+        fl = {{"u.x", true}, {"u.y", true}, {"h", true}, {"U.x", false}, {"U.y", false},
+              {"omega", false}, {"ke", false}, {"p", false}, {"flx.x", false},
+              {"flx.y", false}, {"pv", false}};
+        prog = {"u.x", "u.y", "h"};
+    } else {
+        fl = {{"pv", true}, {"U.x", false}, {"U.y", false}, {"h", false}, {"flx.x", false},
+              {"flx.y", false}, {"work", false}, {"psi", false}};
+        prog = {"pv"};
+    }
+    for (auto& f : fl)
+        if ((e = add_field(m, f.first, f.second))) return bail(e);
+    for (int k = 1; k <= 2; ++k)
+        for (const char* f : prog)
+            if ((e = add_field(m, (std::string("ds") + std::to_string(k) + "." + f).c_str(),
+                               false)))
+                return bail(e);
+    if (p->model != F2D_MODEL_RSW) {
+        m->pr = dalloc(m, field_bytes(m));
+        m->pz = dalloc(m, field_bytes(m));
+        m->pp = dalloc(m, field_bytes(m));
+        m->pq = dalloc(m, field_bytes(m));
+        m->d_fv = dalloc(m, field_bytes(m));
+        if (!m->pr || !m->pz || !m->pp || !m->pq || !m->d_fv)
+            return bail(fail(2, "out of device memory"));
+    }
+    if ((e = setup_mesh(m, msk))) return bail(e);
+    // time line (timeline.py:4-12) and set_dt constants (model.py:71-87)
+    DevScalars h;
+    memset(&h, 0, sizeof(h));
+    h.dt = p->dt > 0 ? p->dt : 0.01;
+    h.cfl = p->cfl;
+    h.dtmax = p->dtmax;
+    m->cfl_dt = !(p->dt > 0) && p->model != F2D_MODEL_RSW;
+    if (p->dt > 0) m->dt_const = p->dt;
+    else if (p->model == F2D_MODEL_RSW) {
+        const double c = pow(p->g * p->H, 0.5);
+        const double maxU = c / m->dx + c / m->dy;
+        m->dt_const = fmin(p->cfl / maxU, p->dtmax);
+    }
+    if (cudaMemcpy(m->sc, &h, sizeof(h), cudaMemcpyHostToDevice) != cudaSuccess)
+        return bail(fail(2, "scalar upload failed"));
+    *out = m;
+    return 0;
+}
+
+int f2d_model_destroy(f2d_model m)
+{
+    if (!m) return 0;
+    if (m->stream) cudaStreamSynchronize(m->stream);
+    drop_graphs(m);
+    for (int w = 0; w < 2; ++w) mg_free(m->mg[w]);
+    for (void* p : m->allocs) cudaFree(p);
+    if (m->own_stream && m->stream) cudaStreamDestroy(m->stream);
+    if (m->s2) cudaStreamDestroy(m->s2);
+    delete m;
+    return 0;
+}
+
+int f2d_model_set_mask(f2d_model m, const int8_t* msk)
+{
+    if (!m || !msk) return fail(1, "null argument");
+    CK(cudaStreamSynchronize(m->stream));
+    return setup_mesh(m, msk);
+}
+
+int f2d_model_set_stream(f2d_model m, void* stream)
+{
+    if (!m) return fail(1, "null model");
+    CK(cudaStreamSynchronize(m->stream));
+    if (m->own_stream) cudaStreamDestroy(m->stream);
+    if (stream) {
+        m->stream = (cudaStream_t)stream;
+        m->own_stream = false;
+    } else {
+        CK(cudaStreamCreateWithFlags(&m->stream, cudaStreamNonBlocking));
+        m->own_stream = true;
+    }
+    return 0;
+}
+
+static int field_io(f2d_model m, const char* name, double* host, bool set, bool async)
+{
+    if (!m || !name || !host) return fail(1, "null argument");
+    void* d = fb(m, name);
+    if (!d) return fail(8, std::string("no field named ") + name);
+    const Geom& g = m->g;
+    if (m->prec != 0) return fail(9, "float32 fields: not available in this build");
+    if (set)
+        CK(cudaMemcpy2DAsync(d, g.P * 8, host, g.NX * 8, g.NX * 8, g.NY,
+                             cudaMemcpyHostToDevice, m->stream));
+    else
+        CK(cudaMemcpy2DAsync(host, g.NX * 8, d, g.P * 8, g.NX * 8, g.NY,
+                             cudaMemcpyDeviceToHost, m->stream));
+    if (set && (!strcmp(name, "U.x") || !strcmp(name, "U.y")))
+        CKI(launch_maxabs2(m->prec, fb(m, "U.x"), fb(m, "U.y"), g, m->sc, m->partials,
+                           m->stream));
+    if (!async) CK(cudaStreamSynchronize(m->stream));
+    return 0;
+}
+
+int f2d_field_set(f2d_model m, const char* name, const double* host)
+{
+    return field_io(m, name, (double*)host, true, false);
+}
+int f2d_field_get(f2d_model m, const char* name, double* host)
+{
+    return field_io(m, name, host, false, false);
+}
+int f2d_field_set_async(f2d_model m, const char* name, const double* host)
+{
+    return field_io(m, name, (double*)host, true, true);
+}
+int f2d_field_get_async(f2d_model m, const char* name, double* host)
+{
+    return field_io(m, name, host, false, true);
+}
+
+int f2d_field_device(f2d_model m, const char* name, void** ptr, int64_t* pitch, int* es)
+{
+    if (!m || !name) return fail(1, "null argument");
+    void* d = fb(m, name);
+    if (!d) return fail(8, std::string("no field named ") + name);
+    if (ptr) *ptr = d;
+    if (pitch) *pitch = m->g.P;
+    if (es) *es = (int)m->es;
+    return 0;
+}
+
+int f2d_field_names(f2d_model m, char* buf, size_t len)
+{
+    if (!m || !buf || !len) return fail(1, "null argument");
+    std::string s;
+    for (auto& kv : m->fields) {
+        if (kv.first.rfind("ds", 0) == 0) continue;
+        if (!s.empty()) s += ",";
+        s += kv.first;
+    }
+    if (s.size() + 1 > len) return fail(1, "buffer too small");
+    memcpy(buf, s.c_str(), s.size() + 1);
+    return 0;
+}
+
+int f2d_set_coriolis(f2d_model m, const double* f)
+{
+    if (!m || !f) return fail(1, "null argument");
+    if (!m->d_fv) return fail(8, "model has no vertex Coriolis field");
+    const Geom& g = m->g;
+    CK(cudaMemcpy2DAsync(m->d_fv, g.P * 8, f, g.NX * 8, g.NX * 8, g.NY,
+                         cudaMemcpyHostToDevice, m->stream));
+    CK(cudaStreamSynchronize(m->stream));
+    return 0;
+}
+
+int f2d_diag(f2d_model m)
+{
+    if (!m) return fail(1, "null model");
+    return run_graph(m, 0);
+}
+
+int f2d_step(f2d_model m, int n)
+{
+    if (!m) return fail(1, "null model");
+    for (int k = 0; k < n; ++k) {
+        int e = run_graph(m, 1);
+        if (e) return e;
+    }
+    return 0;
+}
+
+int f2d_set_dt(f2d_model m)
+{
+    if (!m) return fail(1, "null model");
+    if (m->cfl_dt) {
+        CKI(launch_set_dt(m->sc, m->stream));
+    } else {
+        CK(cudaMemcpyAsync(&m->sc->dt, &m->dt_const, 8, cudaMemcpyHostToDevice, m->stream));
+        CK(cudaStreamSynchronize(m->stream));
+        m->dt_applied = true;
+    }
+    return 0;
+}
+
+int f2d_run(f2d_model m, int n)
+{
+    if (!m) return fail(1, "null model");
+    if (!m->cfl_dt && !m->dt_applied) {
+        int e = f2d_set_dt(m);
+        if (e) return e;
+    }
+    for (int k = 0; k < n; ++k) {
+        int e = run_graph(m, 2);
+        if (e) return e;
+    }
+    return 0;
+}
+
+int f2d_time_get(f2d_model m, double* t, double* dt, int64_t* ite)
+{
+    if (!m) return fail(1, "null model");
+    DevScalars h;
+    CK(cudaMemcpyAsync(&h, m->sc, sizeof(h), cudaMemcpyDeviceToHost, m->stream));
+    CK(cudaStreamSynchronize(m->stream));
+    if (t) *t = h.t;
+    if (dt) *dt = h.dt;
+    if (ite) *ite = h.ite;
+    return 0;
+}
+
+int f2d_time_set(f2d_model m, double t, double dt, int64_t ite)
+{
+    if (!m) return fail(1, "null model");
+    DevScalars h;
+    CK(cudaMemcpyAsync(&h, m->sc, sizeof(h), cudaMemcpyDeviceToHost, m->stream));
+    CK(cudaStreamSynchronize(m->stream));
+    h.t = t;
+    h.dt = dt;
+    h.ite = ite;
+    h.c = 0.0;
+    m->dt_applied = false;
+    CK(cudaMemcpyAsync(m->sc, &h, sizeof(h), cudaMemcpyHostToDevice, m->stream));
+    CK(cudaStreamSynchronize(m->stream));
+    return 0;
+}
+
+int f2d_poisson_solve(f2d_model m, int which, const double* b, double* x, int* iters,
+                      double* relres)
+{
+    if (!m || !b || !x) return fail(1, "null argument");
+    if (which != 0 && which != 1) return fail(1, "which must be 0 or 1");
+    if (!m->pr) return fail(8, "this model has no Poisson workspace");
+    if (which == 1 && m->p.model == F2D_MODEL_EULERPSI)
+        return fail(8, "the Helmholtz operator exists for qg/rsw models only");
+    if (m->prec != 0) return fail(9, "float32 solve: not available in this build");
+    const Geom& g = m->g;
+    if (!m->sb) {
+        m->sb = dalloc(m, field_bytes(m));
+        m->sx = dalloc(m, field_bytes(m));
+        if (!m->sb || !m->sx) return fail(2, "out of device memory");
+    }
+    CK(cudaMemcpy2DAsync(m->sb, g.P * 8, b, g.NX * 8, g.NX * 8, g.NY, cudaMemcpyHostToDevice,
+                         m->stream));
+    CK(cudaMemcpy2DAsync(m->sx, g.P * 8, x, g.NX * 8, g.NX * 8, g.NY, cudaMemcpyHostToDevice,
+                         m->stream));
+    const int kind = 3 + which;
+    if (!m->gx[kind][0]) {
+        int e0 = ensure_mg(m, which);
+        if (e0) return e0;
+        m->rec_launches = 0;
+        CK(cudaStreamBeginCapture(m->stream, cudaStreamCaptureModeRelaxed));
+        int e = rec_solve(m, which, m->sb, m->sx, m->stream);
+        cudaGraph_t graph = nullptr;
+        cudaError_t ce = cudaStreamEndCapture(m->stream, &graph);
+        if (e) {
+            if (graph) cudaGraphDestroy(graph);
+            return e;
+        }
+        if (ce != cudaSuccess) return fail((int)ce, cudaGetErrorString(ce));
+        ce = cudaGraphInstantiate(&m->gx[kind][0], graph, 0);
+        cudaGraphDestroy(graph);
+        if (ce != cudaSuccess) return fail((int)ce, cudaGetErrorString(ce));
+    }
+    CK(cudaGraphLaunch(m->gx[kind][0], m->stream));
+    CK(cudaMemcpy2DAsync(x, g.NX * 8, m->sx, g.P * 8, g.NX * 8, g.NY, cudaMemcpyDeviceToHost,
+                         m->stream));
+    DevScalars h;
+    CK(cudaMemcpyAsync(&h, m->sc, sizeof(h), cudaMemcpyDeviceToHost, m->stream));
+    CK(cudaStreamSynchronize(m->stream));
+    if (iters) *iters = h.iter;
+    if (relres) *relres = h.bb > 0 ? sqrt(h.rr / h.bb) : 0.0;
+    return 0;
+}
+
+int f2d_sync(f2d_model m)
+{
+    if (!m) return fail(1, "null model");
+    CK(cudaStreamSynchronize(m->stream));
+    int st = 0;
+    CK(cudaMemcpy(&st, &m->sc->status, sizeof(int), cudaMemcpyDeviceToHost));
+    if (st) {
+        int zero = 0;
+        CK(cudaMemcpy(&m->sc->status, &zero, sizeof(int), cudaMemcpyHostToDevice));
+        std::string msg = "device status:";
+        if (st & ST_TMA_TIMEOUT) msg += " TMA tile load timed out;";
+        if (st & ST_PCG_MAXIT) msg += " Poisson solve reached max iterations;";
+        if (st & ST_NONFINITE) msg += " non-finite residual;";
+        return fail(100 + st, msg);
+    }
+    return 0;
+}
+
+int f2d_stats(f2d_model m, int64_t* poisson_iters, int64_t* launches_per_step,
+              int64_t* launches_per_iter)
+{
+    if (!m) return fail(1, "null model");
+    DevScalars h;
+    CK(cudaMemcpyAsync(&h, m->sc, sizeof(h), cudaMemcpyDeviceToHost, m->stream));
+    CK(cudaStreamSynchronize(m->stream));
+    if (poisson_iters) *poisson_iters = h.total_iters;
+    if (launches_per_step) {
+        // kernels outside the Poisson loop bodies of one step; each Poisson
+        // iteration adds body_launches more
+        int n = m->launches[2][0] ? m->launches[2][0] : m->launches[1][0];
+        *launches_per_step = n;
+    }
+    if (launches_per_iter) *launches_per_iter = m->p.model == F2D_MODEL_RSW ? 0 : m->body_launches;
+    return 0;
+}
+
+int f2d_time_stage(f2d_model m, int stage, int reps, int flush_l2, double* avg_ms)
+{
+    if (!m || !avg_ms || reps < 1 || stage < 1 || stage > 3) return fail(1, "bad arguments");
+    // the stage kernel reads parity cur and writes the other buffer; repeated
+    // launches recompute the same values, so the model state is unchanged
+    const size_t flush_bytes = 256ull << 20;  // twice the 126 MB L2
+    void* fl = nullptr;
+    if (flush_l2) CK(cudaMalloc(&fl, flush_bytes));
+    cudaEvent_t a, b;
+    CK(cudaEventCreate(&a));
+    CK(cudaEventCreate(&b));
+    double total = 0.0;
+    int e = 0;
+    for (int r = 0; r < reps && !e; ++r) {
+        if (fl) cudaMemsetAsync(fl, r & 0xff, flush_bytes, m->stream);
+        cudaEventRecord(a, m->stream);
+        e = launch_stage_kernel(m, stage, m->cur, m->stream);
+        cudaEventRecord(b, m->stream);
+        if (cudaEventSynchronize(b) != cudaSuccess) e = fail(2, "event sync failed");
+        float ms = 0.f;
+        cudaEventElapsedTime(&ms, a, b);
+        total += ms;
+    }
+    cudaEventDestroy(a);
+    cudaEventDestroy(b);
+    if (fl) cudaFree(fl);
+    if (e) return e;
+    *avg_ms = total / reps;
+    return 0;
+}
+
+}  // extern "C"

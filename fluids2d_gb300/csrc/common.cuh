@@ -1,0 +1,206 @@
+// Shared definitions of the fluids2d_gb300 CUDA library: array geometry,
+// per-point mask/order codes, device scalars, TMA/mbarrier helpers and
+// deterministic grid reductions.
+#pragma once
+#include <cuda.h>
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+namespace f2d {
+
+// ---------------------------------------------------------------------------
+// Array geometry. Every field is a (NY, NX) = (ny+6, nx+6) array as in the
+// reference (meshes.py:122-132), stored on the device with a row pitch P >= NX
+// (a multiple of 16 elements, so rows start on 128-byte boundaries and TMA
+// strides are legal).
+// ---------------------------------------------------------------------------
+struct Geom {
+    int NY, NX;      // rows, columns including the 3-cell halo
+    int ny, nx;      // interior size
+    long long P;     // device row pitch in elements
+    int xper;        // x-periodic: halo columns hold copies (meshes.py:135-143)
+};
+
+// Per-point code word packing the int8 masks and stencil orders of the
+// reference mesh (meshes.py:77-104): six 2-bit order levels and six flags.
+enum : uint32_t {
+    SH_OCX = 0, SH_OCY = 2, SH_OVX = 4, SH_OVY = 6, SH_OKX = 8, SH_OKY = 10,
+    B_MSK = 1u << 12, B_MSKX = 1u << 13, B_MSKY = 1u << 14,
+    B_MSKV = 1u << 15, B_SLIP = 1u << 16, B_GV = 1u << 17,
+};
+__host__ __device__ inline int lev(uint32_t c, int sh) { return (c >> sh) & 3; }
+
+// Status bits reported back to the host (f2d_last_error).
+enum : int {
+    ST_TMA_TIMEOUT = 1,    // a TMA tile load did not complete within 1 s
+    ST_PCG_MAXIT = 2,      // the Poisson solve stopped at max iterations
+    ST_NONFINITE = 4,      // a non-finite value reached a reduction
+};
+
+// Device-resident scalars of one model: the time line (timeline.py:4-35),
+// the CFL reduction and the Poisson-solver state.
+struct DevScalars {
+    double t, c, dt;        // time, Kahan compensation, time step
+    long long ite;
+    double maxUx, maxUy;    // max |U.x|, max |U.y| of the last diagnostic
+    double cfl, dtmax;      // set_dt parameters (model.py:71-87)
+    int status;
+    int pad0;
+    // Poisson solver (one at a time per model)
+    double bb, rr, rz, pq, alpha, beta;
+    double tol2;            // (relative tolerance)^2
+    int iter, maxit, converged, pad1;
+    long long total_iters;  // summed over solves, for diagnostics
+    unsigned int counter[8];  // last-block reduction tickets
+};
+
+// ---------------------------------------------------------------------------
+// Small PTX helpers: TMA tile loads through an mbarrier, with a time-bounded
+// wait so that a copy that never lands turns into a status bit, not a hang.
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ uint32_t smem_u32(const void* p)
+{
+    return static_cast<uint32_t>(__cvta_generic_to_shared(p));
+}
+
+__device__ __forceinline__ void mbar_init(uint64_t* bar, unsigned count)
+{
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(bar)),
+                 "r"(count)
+                 : "memory");
+    asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+}
+
+__device__ __forceinline__ void mbar_expect_tx(uint64_t* bar, uint32_t bytes)
+{
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(
+                     smem_u32(bar)),
+                 "r"(bytes)
+                 : "memory");
+}
+
+__device__ __forceinline__ void tma_load_2d(void* dst, const CUtensorMap* map,
+                                            int x, int y, uint64_t* bar)
+{
+    asm volatile(
+        "cp.async.bulk.tensor.2d.shared::cluster.global.mbarrier::complete_tx::bytes"
+        " [%0], [%1, {%2, %3}], [%4];" ::"r"(smem_u32(dst)),
+        "l"(reinterpret_cast<uint64_t>(map)), "r"(x), "r"(y), "r"(smem_u32(bar))
+        : "memory");
+}
+
+__device__ __forceinline__ uint64_t globaltimer_ns()
+{
+    uint64_t t;
+    asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+    return t;
+}
+
+// Wait for phase `parity` of the barrier; gives up after `limit_ns`.
+__device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity,
+                                          uint64_t limit_ns = 1000000000ull)
+{
+    const uint32_t a = smem_u32(bar);
+    uint64_t t0 = 0;
+    for (int spin = 0;; ++spin) {
+        uint32_t ok;
+        asm volatile(
+            "{ .reg .pred p; mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;"
+            " selp.u32 %0, 1, 0, p; }"
+            : "=r"(ok)
+            : "r"(a), "r"(parity)
+            : "memory");
+        if (ok) return true;
+        if (spin == 0) t0 = globaltimer_ns();
+        else if (globaltimer_ns() - t0 > limit_ns) return false;
+    }
+}
+
+// ---------------------------------------------------------------------------
+// Deterministic grid-wide reductions of up to N doubles: every block writes
+// its partial sums, the last block to finish (ticket counter) adds the
+// partials in a fixed order, so results do not depend on block scheduling.
+// ---------------------------------------------------------------------------
+template <int N>
+__device__ __forceinline__ void warp_sum(double (&v)[N])
+{
+#pragma unroll
+    for (int k = 0; k < N; ++k)
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) v[k] += __shfl_xor_sync(0xffffffffu, v[k], o);
+}
+
+template <int N>
+__device__ __forceinline__ void warp_max(double (&v)[N])
+{
+#pragma unroll
+    for (int k = 0; k < N; ++k)
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1)
+            v[k] = fmax(v[k], __shfl_xor_sync(0xffffffffu, v[k], o));
+}
+
+// Block-wide reduction; result valid in thread 0. `sh` needs 32*N doubles.
+template <int N, bool MAX>
+__device__ __forceinline__ void block_reduce(double (&v)[N], double* sh)
+{
+    const int nt = blockDim.x * blockDim.y;
+    const int tid = threadIdx.y * blockDim.x + threadIdx.x;
+    if (MAX) warp_max<N>(v); else warp_sum<N>(v);
+    const int w = tid >> 5, lane = tid & 31, nw = (nt + 31) >> 5;
+    __syncthreads();
+    if (lane == 0)
+#pragma unroll
+        for (int k = 0; k < N; ++k) sh[w * N + k] = v[k];
+    __syncthreads();
+    if (w == 0) {
+#pragma unroll
+        for (int k = 0; k < N; ++k)
+            v[k] = lane < nw ? sh[lane * N + k] : (MAX ? -INFINITY : 0.0);
+        if (MAX) warp_max<N>(v); else warp_sum<N>(v);
+    }
+}
+
+// Grid reduction of N values. Returns true in the single thread (thread 0
+// of the last block) that holds the grid result in `v`.
+template <int N, bool MAX>
+__device__ __forceinline__ bool grid_reduce(double (&v)[N], double* partials,
+                                            unsigned int* ticket)
+{
+    __shared__ double sh[32 * N];
+    __shared__ int s_last;
+    block_reduce<N, MAX>(v, sh);
+    const int tid = threadIdx.y * blockDim.x + threadIdx.x;
+    const unsigned nb = gridDim.x * gridDim.y;
+    const unsigned b = blockIdx.y * gridDim.x + blockIdx.x;
+    if (tid == 0) {
+#pragma unroll
+        for (int k = 0; k < N; ++k) partials[(size_t)b * N + k] = v[k];
+        __threadfence();
+        unsigned prev = atomicAdd(ticket, 1u);
+        s_last = (prev == nb - 1);
+    }
+    __syncthreads();
+    if (!s_last) return false;
+    __threadfence();
+    const int nt = blockDim.x * blockDim.y;
+    double acc[N];
+#pragma unroll
+    for (int k = 0; k < N; ++k) acc[k] = MAX ? -INFINITY : 0.0;
+    for (unsigned i = tid; i < nb; i += nt)
+#pragma unroll
+        for (int k = 0; k < N; ++k) {
+            double p = __ldcg(&partials[(size_t)i * N + k]);
+            acc[k] = MAX ? fmax(acc[k], p) : acc[k] + p;
+        }
+    block_reduce<N, MAX>(acc, sh);
+    if (tid == 0) {
+#pragma unroll
+        for (int k = 0; k < N; ++k) v[k] = acc[k];
+        *ticket = 0;  // ready for the next launch
+        return true;
+    }
+    return false;
+}
+
+}  // namespace f2d

@@ -1,0 +1,55 @@
+// Geometric multigrid-preconditioned conjugate gradients for the masked
+// 5-point vertex operator of the reference (elliptic.py:114-195: Dirichlet
+// at non-fluid vertices, optional Helmholtz diagonal, x-periodic wrap).
+#pragma once
+#include <vector>
+
+#include "common.cuh"
+
+namespace f2d {
+
+// One grid level. Node (J, I), 0 <= J < nyn, 0 <= I < nxn, lives at
+// base[off + J*pitch + I] of the level's arrays. Level 0 is the model's
+// vertex array (node (J,I) = array point (3+J, 3+I)).
+struct MGLevel {
+    void* x;            // level unknown (level 0: the preconditioned residual z)
+    void* b;            // level right-hand side (level 0: the CG residual r)
+    const uint8_t* m;   // 1 = fluid node
+    int nyn, nxn;
+    long long pitch, off;
+    int per;            // x-periodic wrap over nxn nodes
+    int pad;
+    double cx, cy;      // east-west and north-south couplings (dy/dx, dx/dy)
+    double diag, idiag; // -2(cx+cy) - maindiag and its inverse
+};
+
+struct MGHost {
+    std::vector<MGLevel> lev;
+    std::vector<void*> owned;  // device allocations of coarse levels
+    MGLevel* dlev = nullptr;   // device copy of lev
+    int ltail = 0;             // first level handled by the single-block tail
+    int ncoarse_sweeps = 4;    // (R,B)^k (B,R)^k on the coarsest level
+    int prec = 0;              // 0 = double, 1 = float
+};
+
+// PCG vectors on the model's vertex layout (level-0 geometry).
+struct PCGVecs {
+    void *x, *r, *z, *p, *q;  // x is the solution array (psi)
+    const void* b;            // right-hand side array
+    double* partials;         // >= 3 doubles per block of the level-0 grid
+};
+
+int mg_build(MGHost& mg, int nyn0, int nxn0, long long pitch0, long long off0,
+             int per, const uint8_t* hmask0 /* host, level-0 layout */,
+             const uint8_t* dmask0 /* device copy */, void* z0, void* r0,
+             double cx, double cy, double maindiag, int prec);
+void mg_free(MGHost& mg);
+
+// Record the whole solve on `s` (eagerly or under stream capture): init,
+// a conditional WHILE node over the PCG iteration (body captured on `s2`),
+// and the periodic halo fill. `cond` is the WHILE node's handle when the
+// solve is recorded into a graph; with cond == 0 the loop is host-driven.
+int pcg_record(MGHost& mg, const PCGVecs& v, DevScalars* sc, double tol,
+               int maxit, cudaStream_t s, cudaStream_t s2);
+
+}  // namespace f2d

@@ -1,0 +1,604 @@
+// Fused time-stepping kernels.
+//
+// One launch per RK stage computes the right-hand side of the reference's
+// equation set AND applies the SSP-RK3 increment (integrators.py:92-107,
+// addto 154-196) over a 32x8 tile, with the stencil inputs staged in shared
+// memory by TMA (halo of 3 cells) and every face flux evaluated once.
+//
+// Every array point is produced with the numpy-slice semantics of the
+// reference operators, including the halo rows and columns (the reference
+// applies the Coriolis and gradient terms there too, and those values feed
+// back into the interior). In an x-periodic domain the halo columns are the
+// reference's halo fill (meshes.py:135-143): the threads owning columns
+// [3,6) and [nx,nx+3) also write the copies, so no separate fill pass runs.
+#include "stage.cuh"
+#include "weno.cuh"
+
+namespace f2d {
+
+constexpr int TX = 32, TY = 8;           // cells per tile
+constexpr int SW = TX + 8, SH = TY + 6;  // staged tile: cols i0-4.., rows j0-3..
+constexpr int OX = 4, OY = 3;            // offset of cell (j0,i0) in the tile
+
+template <typename T>
+__device__ __forceinline__ T ldz(const T* __restrict__ a, int j, int i,
+                                 const Geom& g)
+{
+    return (j >= 0 && j < g.NY && i >= 0 && i < g.NX) ? a[(long long)j * g.P + i]
+                                                      : T(0);
+}
+
+// The RK3 increment of stage k (1, 2, 3) in the reference's evaluation order:
+// y += ((0 + c1*ds1) + c2*ds2) + c3*ds3 with (c) = (dt), (-3dt/4, dt/4),
+// (-dt/12, -dt/12, 2dt/3).
+template <typename T>
+__device__ __forceinline__ T rk3_increment(int stage, double dt, T d1, T d2, T d3)
+{
+    if (stage == 1) return T(dt) * d1;
+    if (stage == 2) return T(-3 * dt / 4) * d1 + T(dt / 4) * d2;
+    return (T(-dt / 12) * d1 + T(-dt / 12) * d2) + T(2 * dt / 3) * d3;
+}
+
+// Store v at (j,i) and, in an x-periodic domain, at its halo copy.
+// Returns false for points that belong to the halo copy of another thread.
+__device__ __forceinline__ bool periodic_owner(const Geom& g, int i)
+{
+    return !g.xper || (i >= 3 && i < g.nx + 3);
+}
+
+template <typename T>
+__device__ __forceinline__ void store_filled(T* __restrict__ a, const Geom& g,
+                                             int j, int i, T v)
+{
+    const long long r = (long long)j * g.P;
+    a[r + i] = v;
+    if (g.xper) {
+        if (i < 6) a[r + i + g.nx] = v;
+        else if (i >= g.nx) a[r + i - g.nx] = v;
+    }
+}
+
+// Issue the TMA loads of up to two (SH x SW) tiles and wait for them. All
+// threads wait on the barrier; returns false (uniformly) on timeout.
+template <typename T>
+__device__ __forceinline__ bool stage_tiles(T (*s0)[SW], const CUtensorMap* m0,
+                                            T (*s1)[SW], const CUtensorMap* m1,
+                                            int i0, int j0, uint64_t* bar,
+                                            int* status)
+{
+    const int t = threadIdx.y * blockDim.x + threadIdx.x;
+    if (t == 0) mbar_init(bar, 1);
+    __syncthreads();
+    if (t == 0) {
+        const uint32_t bytes = (uint32_t)(sizeof(T) * SW * SH * (s1 ? 2 : 1));
+        mbar_expect_tx(bar, bytes);
+        tma_load_2d(&s0[0][0], m0, i0 - OX, j0 - OY, bar);
+        if (s1) tma_load_2d(&s1[0][0], m1, i0 - OX, j0 - OY, bar);
+    }
+    bool ok = mbar_wait(bar, 0);
+    int all = __syncthreads_and(ok ? 1 : 0);
+    if (!all && t == 0) atomicOr(status, ST_TMA_TIMEOUT);
+    return all != 0;
+}
+
+// ---------------------------------------------------------------------------
+// Flux-form stage: dq = -div(U q) * msk (divflux/div, operators.py:21-29,
+// 104-107) for eulerpsi (q = omega) and qg (q = pv), then the RK3 update.
+// ---------------------------------------------------------------------------
+template <typename T, int M>
+__global__ void __launch_bounds__(TX * TY)
+k_fluxform_stage(const __grid_constant__ CUtensorMap tq, const T* __restrict__ qin,
+                 T* __restrict__ qout, const T* __restrict__ Ux,
+                 const T* __restrict__ Uy, const uint32_t* __restrict__ code,
+                 T* __restrict__ ds_out, const T* __restrict__ ds1,
+                 const T* __restrict__ ds2, int stage, Geom g, DevScalars* sc)
+{
+    __shared__ alignas(128) T sq[SH][SW];
+    __shared__ T sfx[TY][TX + 1];
+    __shared__ T sfy[TY + 1][TX];
+    __shared__ uint64_t bar;
+    const int tx = threadIdx.x, ty = threadIdx.y, t = ty * TX + tx;
+    const int i0 = blockIdx.x * TX, j0 = blockIdx.y * TY;
+
+    if (!stage_tiles<T>(sq, &tq, nullptr, nullptr, i0, j0, &bar, &sc->status))
+        return;
+
+    // x-faces (TY x TX+1) and y-faces (TY+1 x TX): each evaluated once.
+    auto xface = [&](int r, int c) {
+        const int j = j0 + r, i = i0 + c;
+        T f = T(0);
+        if (j < g.NY && i < g.NX) {
+            const long long o = (long long)j * g.P + i;
+            const int L = lev(code[o], SH_OCX);
+            if (L) {
+                const T U = Ux[o];
+                const T* w = &sq[r + OY][c + OX - 3];
+                f = face_value<M, T>(L, U, w[0], w[1], w[2], w[3], w[4], w[5]) * U;
+            }
+        }
+        sfx[r][c] = f;
+    };
+    auto yface = [&](int r, int c) {
+        const int j = j0 + r, i = i0 + c;
+        T f = T(0);
+        if (j < g.NY && i < g.NX) {
+            const long long o = (long long)j * g.P + i;
+            const int L = lev(code[o], SH_OCY);
+            if (L) {
+                const T U = Uy[o];
+                const int cc = c + OX;
+                f = face_value<M, T>(L, U, sq[r][cc], sq[r + 1][cc], sq[r + 2][cc],
+                                     sq[r + 3][cc], sq[r + 4][cc], sq[r + 5][cc]) *
+                    U;
+            }
+        }
+        sfy[r][c] = f;
+    };
+    xface(ty, tx);
+    yface(ty, tx);
+    if (t < TY) xface(t, TX);
+    else if (t < TY + TX) yface(TY, t - TY);
+    __syncthreads();
+
+    const int j = j0 + ty, i = i0 + tx;
+    if (j >= g.NY || i >= g.NX || !periodic_owner(g, i)) return;
+    const long long o = (long long)j * g.P + i;
+    const T msk = (code[o] & B_MSK) ? T(1) : T(0);
+    const T ds = (-(sfx[ty][tx + 1] - sfx[ty][tx]) - (sfy[ty + 1][tx] - sfy[ty][tx])) * msk;
+    const double dt = sc->dt;
+    T inc;
+    if (stage == 1) inc = rk3_increment<T>(1, dt, ds, T(0), T(0));
+    else if (stage == 2) inc = rk3_increment<T>(2, dt, ds1[o], ds, T(0));
+    else inc = rk3_increment<T>(3, dt, ds1[o], ds2[o], ds);
+    const T q = sq[ty + OY][tx + OX];
+    store_filled(qout, g, j, i, q + inc);
+    if (ds_out) store_filled(ds_out, g, j, i, ds);
+}
+
+// ---------------------------------------------------------------------------
+// Rotating shallow water right-hand side (equations.py:139-148) + RK3 update
+// of (u.x, u.y, h): vortex force (weno.vortexforce), Coriolis, gradients of
+// ke and p, mass flux divergence.
+// ---------------------------------------------------------------------------
+template <typename T, int M>
+__global__ void __launch_bounds__(TX * TY)
+k_rsw_stage(const __grid_constant__ CUtensorMap th,
+            const __grid_constant__ CUtensorMap tw, RswIn a,
+            const uint32_t* __restrict__ code, int stage, Geom g, DevScalars* sc)
+{
+    __shared__ alignas(128) T sh[SH][SW];
+    __shared__ alignas(128) T sw[SH][SW];
+    __shared__ T sfx[TY][TX + 1];
+    __shared__ T sfy[TY + 1][TX];
+    __shared__ uint64_t bar;
+    const int tx = threadIdx.x, ty = threadIdx.y, t = ty * TX + tx;
+    const int i0 = blockIdx.x * TX, j0 = blockIdx.y * TY;
+    const T* __restrict__ Ux = (const T*)a.Ux;
+    const T* __restrict__ Uy = (const T*)a.Uy;
+
+    if (!stage_tiles<T>(sh, &th, sw, &tw, i0, j0, &bar, &sc->status)) return;
+
+    // mass fluxes U*h at the faces (compflux, weno.py:349-363)
+    auto xface = [&](int r, int c) {
+        const int j = j0 + r, i = i0 + c;
+        T f = T(0);
+        if (j < g.NY && i < g.NX) {
+            const long long o = (long long)j * g.P + i;
+            const int L = lev(code[o], SH_OCX);
+            if (L) {
+                const T U = Ux[o];
+                const T* w = &sh[r + OY][c + OX - 3];
+                f = face_value<M, T>(L, U, w[0], w[1], w[2], w[3], w[4], w[5]) * U;
+            }
+        }
+        sfx[r][c] = f;
+    };
+    auto yface = [&](int r, int c) {
+        const int j = j0 + r, i = i0 + c;
+        T f = T(0);
+        if (j < g.NY && i < g.NX) {
+            const long long o = (long long)j * g.P + i;
+            const int L = lev(code[o], SH_OCY);
+            if (L) {
+                const T U = Uy[o];
+                const int cc = c + OX;
+                f = face_value<M, T>(L, U, sh[r][cc], sh[r + 1][cc], sh[r + 2][cc],
+                                     sh[r + 3][cc], sh[r + 4][cc], sh[r + 5][cc]) *
+                    U;
+            }
+        }
+        sfy[r][c] = f;
+    };
+    xface(ty, tx);
+    yface(ty, tx);
+    if (t < TY) xface(t, TX);
+    else if (t < TY + TX) yface(TY, t - TY);
+    __syncthreads();
+
+    const int j = j0 + ty, i = i0 + tx;
+    if (j >= g.NY || i >= g.NX || !periodic_owner(g, i)) return;
+    const long long o = (long long)j * g.P + i;
+    const uint32_t cd = code[o];
+    const T* __restrict__ ke = (const T*)a.ke;
+    const T* __restrict__ p = (const T*)a.p;
+
+    // du.x: vortex force along y (sign +1), weno.py:370-384 with s = row
+    // length, s2 = 1: omega window rows j-2..j+3 at column i.
+    T dux = T(0);
+    {
+        const int L = lev(cd, SH_OVY);
+        if (L) {
+            const T Vm = T(0.25) * (((Uy[o] + ldz(Uy, j + 1, i, g)) + ldz(Uy, j, i - 1, g)) +
+                                    ldz(Uy, j + 1, i - 1, g));
+            const int c = tx + OX, r = ty + OY;
+            dux = face_value<M, T>(L, Vm, sw[r - 2][c], sw[r - 1][c], sw[r][c],
+                                   sw[r + 1][c], sw[r + 2][c], sw[r + 3][c]) *
+                  Vm;
+        }
+    }
+    // du.y: vortex force along x (sign -1), s = 1, s2 = row length
+    T duy = T(0);
+    {
+        const int L = lev(cd, SH_OVX);
+        if (L) {
+            const T Vm = T(0.25) * (((Ux[o] + ldz(Ux, j, i + 1, g)) + ldz(Ux, j - 1, i, g)) +
+                                    ldz(Ux, j - 1, i + 1, g));
+            const T* w = &sw[ty + OY][tx + OX - 2];
+            duy = -face_value<M, T>(L, Vm, w[0], w[1], w[2], w[3], w[4], w[5]) * Vm;
+        }
+    }
+    // Coriolis (addcoriolis, operators.py:32-39)
+    const T fc = T(a.fc);
+    if (j <= g.NY - 2 && i >= 1 && i <= g.NX - 2)
+        dux += fc * (((ldz(Uy, j, i - 1, g) + ldz(Uy, j + 1, i - 1, g)) + Uy[o]) +
+                     ldz(Uy, j + 1, i, g));
+    if (j >= 1 && j <= g.NY - 2 && i <= g.NX - 2)
+        duy -= fc * (((ldz(Ux, j - 1, i, g) + ldz(Ux, j - 1, i + 1, g)) + Ux[o]) +
+                     ldz(Ux, j, i + 1, g));
+    // gradients of ke then p (addgrad, operators.py:49-56)
+    if (i >= 1) {
+        const T mx = (cd & B_MSKX) ? T(1) : T(0);
+        dux -= (ke[o] - ke[o - 1]) * mx;
+        dux -= (p[o] - p[o - 1]) * mx;
+    }
+    if (j >= 1) {
+        const T my = (cd & B_MSKY) ? T(1) : T(0);
+        duy -= (ke[o] - ke[o - g.P]) * my;
+        duy -= (p[o] - p[o - g.P]) * my;
+    }
+    // mass: dh = -div(flux) * msk
+    const T msk = (cd & B_MSK) ? T(1) : T(0);
+    const T dh = (-(sfx[ty][tx + 1] - sfx[ty][tx]) - (sfy[ty + 1][tx] - sfy[ty][tx])) * msk;
+
+    const double dt = sc->dt;
+    T ix, iy, ih;
+    if (stage == 1) {
+        ix = rk3_increment<T>(1, dt, dux, T(0), T(0));
+        iy = rk3_increment<T>(1, dt, duy, T(0), T(0));
+        ih = rk3_increment<T>(1, dt, dh, T(0), T(0));
+    } else if (stage == 2) {
+        ix = rk3_increment<T>(2, dt, ((const T*)a.dux1)[o], dux, T(0));
+        iy = rk3_increment<T>(2, dt, ((const T*)a.duy1)[o], duy, T(0));
+        ih = rk3_increment<T>(2, dt, ((const T*)a.dh1)[o], dh, T(0));
+    } else {
+        ix = rk3_increment<T>(3, dt, ((const T*)a.dux1)[o], ((const T*)a.dux2)[o], dux);
+        iy = rk3_increment<T>(3, dt, ((const T*)a.duy1)[o], ((const T*)a.duy2)[o], duy);
+        ih = rk3_increment<T>(3, dt, ((const T*)a.dh1)[o], ((const T*)a.dh2)[o], dh);
+    }
+    store_filled((T*)a.uxo, g, j, i, ((const T*)a.ux)[o] + ix);
+    store_filled((T*)a.uyo, g, j, i, ((const T*)a.uy)[o] + iy);
+    store_filled((T*)a.ho, g, j, i, sh[ty + OY][tx + OX] + ih);
+    if (a.dux) {
+        store_filled((T*)a.dux, g, j, i, dux);
+        store_filled((T*)a.duy, g, j, i, duy);
+        store_filled((T*)a.dh, g, j, i, dh);
+    }
+}
+
+// ---------------------------------------------------------------------------
+// Rotating shallow water diagnostics (equations.py:150-155): sharp, vorticity
+// (times slip coefficient), WENO kinetic energy, pressure; omega and ke get
+// the halo fill.
+// ---------------------------------------------------------------------------
+template <typename T, int M>
+__global__ void __launch_bounds__(TX * TY)
+k_rsw_diag(const __grid_constant__ CUtensorMap tux,
+           const __grid_constant__ CUtensorMap tuy, RswDiag a,
+           const uint32_t* __restrict__ code, Geom g, DevScalars* sc)
+{
+    __shared__ alignas(128) T sx[SH][SW];
+    __shared__ alignas(128) T sy[SH][SW];
+    __shared__ uint64_t bar;
+    const int tx = threadIdx.x, ty = threadIdx.y;
+    const int i0 = blockIdx.x * TX, j0 = blockIdx.y * TY;
+    if (!stage_tiles<T>(sx, &tux, sy, &tuy, i0, j0, &bar, &sc->status)) return;
+
+    const int j = j0 + ty, i = i0 + tx;
+    if (j >= g.NY || i >= g.NX) return;
+    const long long o = (long long)j * g.P + i;
+    const int r = ty + OY, c = tx + OX;
+    const T rdx2 = T(a.rdx2), rdy2 = T(a.rdy2);
+    const T ux = sx[r][c], uy = sy[r][c];
+    // sharp: U = u / dx^2 everywhere (no fill in the reference; u is filled)
+    ((T*)a.Ux)[o] = ux * rdx2;
+    ((T*)a.Uy)[o] = uy * rdy2;
+    ((T*)a.p)[o] = T(a.goa) * ((const T*)a.h)[o];
+    if (!periodic_owner(g, i)) return;  // omega and ke: halo fill copies
+    const uint32_t cd = code[o];
+    // vorticity: omega[1:,:] = -diff(u.x, 0); omega[:,1:] += diff(u.y, 1)
+    T om = T(0);
+    if (j >= 1) om = -(ux - sx[r - 1][c]);
+    if (i >= 1) om += uy - sy[r][c - 1];
+    om *= (cd & B_SLIP) ? T(1) : T(0);
+    // kinetic energy: innerproduct x then y, times msk*0.5 (operators.py:94-96)
+    T ke = T(0);
+    {
+        const int L = lev(cd, SH_OKX);
+        if (L) {
+            const T Um = T(0.5) * (ux * rdx2 + sx[r][c + 1] * rdx2);
+            const T* w = &sx[r][c - 2];
+            ke = face_value<M, T>(L, Um, w[0], w[1], w[2], w[3], w[4], w[5]) * Um;
+        }
+    }
+    {
+        const int L = lev(cd, SH_OKY);
+        if (L) {
+            const T Um = T(0.5) * (uy * rdy2 + sy[r + 1][c] * rdy2);
+            ke += face_value<M, T>(L, Um, sy[r - 2][c], sy[r - 1][c], sy[r][c],
+                                   sy[r + 1][c], sy[r + 2][c], sy[r + 3][c]) *
+                  Um;
+        }
+    }
+    ke *= (cd & B_MSK) ? T(0.5) : T(0);
+    store_filled((T*)a.omega, g, j, i, om);
+    store_filled((T*)a.ke, g, j, i, ke);
+}
+
+// ---------------------------------------------------------------------------
+// Vertex diagnostics of eulerpsi/qg.
+// ---------------------------------------------------------------------------
+
+// centerstovertices (operators.py:126-133) and, for qg with beta != 0, the
+// subtraction of the vertex Coriolis term (qg_inversion, operators.py:186-191)
+template <typename T>
+__global__ void k_c2v(const T* __restrict__ q, T* __restrict__ v,
+                      const uint32_t* __restrict__ code, const T* __restrict__ fv,
+                      Geom g)
+{
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    const int j = blockIdx.y * blockDim.y + threadIdx.y;
+    if (j >= g.NY || i >= g.NX) return;
+    const long long o = (long long)j * g.P + i;
+    T a = T(0);
+    if (j >= 1 && i >= 1)
+        a = T(0.25) * (((q[o - g.P - 1] + q[o - 1]) + q[o - g.P]) + q[o]);
+    a *= (code[o] & B_MSKV) ? T(1) : T(0);
+    if (fv) a -= fv[o];
+    v[o] = a;
+}
+
+// perpgrad with contravariant scaling (operators.py:144-149), optional halo
+// fill of U (eulerpsi fills, qg does not), and max|U.x|, max|U.y| for set_dt.
+template <typename T>
+__global__ void k_perpgrad(const T* __restrict__ psi, T* __restrict__ Ux,
+                           T* __restrict__ Uy, const uint32_t* __restrict__ code,
+                           double rdy2, double rdx2, int fillU, Geom g,
+                           DevScalars* sc, double* partials)
+{
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    const int j = blockIdx.y * blockDim.y + threadIdx.y;
+    double m[2] = {0.0, 0.0};
+    if (j < g.NY && i < g.NX) {
+        const long long o = (long long)j * g.P + i;
+        const bool own = !fillU || periodic_owner(g, i);
+        if (own) {
+            const uint32_t cd = code[o];
+            T ux = T(0), uy = T(0);
+            if (j <= g.NY - 2) ux = -(psi[o + g.P] - psi[o]) * ((cd & B_MSKX) ? T(1) : T(0));
+            if (i <= g.NX - 2) uy = (psi[o + 1] - psi[o]) * ((cd & B_MSKY) ? T(1) : T(0));
+            ux *= T(rdy2);
+            uy *= T(rdx2);
+            if (fillU) {
+                store_filled(Ux, g, j, i, ux);
+                store_filled(Uy, g, j, i, uy);
+            } else {
+                Ux[o] = ux;
+                Uy[o] = uy;
+            }
+            m[0] = fabs((double)ux);
+            m[1] = fabs((double)uy);
+        }
+    }
+    if (grid_reduce<2, true>(m, partials, &sc->counter[0])) {
+        sc->maxUx = m[0];
+        sc->maxUy = m[1];
+    }
+}
+
+// max |U.x|, max |U.y| of fields written by the host
+template <typename T>
+__global__ void k_maxabs2(const T* __restrict__ Ux, const T* __restrict__ Uy,
+                          Geom g, DevScalars* sc, double* partials)
+{
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    const int j = blockIdx.y * blockDim.y + threadIdx.y;
+    double m[2] = {0.0, 0.0};
+    if (j < g.NY && i < g.NX) {
+        const long long o = (long long)j * g.P + i;
+        m[0] = fabs((double)Ux[o]);
+        m[1] = fabs((double)Uy[o]);
+    }
+    if (grid_reduce<2, true>(m, partials, &sc->counter[0])) {
+        sc->maxUx = m[0];
+        sc->maxUy = m[1];
+    }
+}
+
+// periodic halo fill (meshes.py:135-143) of one array
+template <typename T>
+__global__ void k_fill_periodic(T* __restrict__ a, Geom g)
+{
+    const int k = blockIdx.x * blockDim.x + threadIdx.x;  // 0..5 per row
+    const int j = blockIdx.y * blockDim.y + threadIdx.y;
+    if (j >= g.NY || k >= 6) return;
+    const long long r = (long long)j * g.P;
+    if (k < 3) a[r + k] = a[r + g.NX - 6 + k];
+    else a[r + g.NX - 6 + k] = a[r + k];  // columns NX-3.. <- 3..
+}
+
+// set_dt (model.py:71-87) from the device-side max|U|
+__global__ void k_set_dt(DevScalars* sc)
+{
+    const double maxU = sc->maxUx + sc->maxUy + 1e-99;
+    sc->dt = fmin(sc->cfl / maxU, sc->dtmax);
+}
+
+// Time.pushforward (timeline.py:20-35): Kahan-summed t, ite += 1
+__global__ void k_pushforward(DevScalars* sc)
+{
+    const double y = sc->dt - sc->c;
+    const double t = sc->t + y;
+    sc->c = (t - sc->t) - y;
+    sc->t = t;
+    sc->ite += 1;
+}
+
+// ---------------------------------------------------------------------------
+// Host-side launchers
+// ---------------------------------------------------------------------------
+static dim3 tile_grid(const Geom& g)
+{
+    return dim3((g.NX + TX - 1) / TX, (g.NY + TY - 1) / TY);
+}
+
+int launch_fluxform_stage(int method, int prec, const CUtensorMap* tq,
+                          const void* qin, void* qout, const void* Ux,
+                          const void* Uy, const uint32_t* code, void* ds_out,
+                          const void* ds1, const void* ds2, int stage,
+                          const Geom& g, DevScalars* sc, cudaStream_t s)
+{
+    dim3 grid = tile_grid(g), block(TX, TY);
+#define F2D_FF(T, M)                                                              \
+    k_fluxform_stage<T, M><<<grid, block, 0, s>>>(                                \
+        *tq, (const T*)qin, (T*)qout, (const T*)Ux, (const T*)Uy, code, (T*)ds_out, \
+        (const T*)ds1, (const T*)ds2, stage, g, sc)
+#define F2D_DISPATCH(T)                                                  \
+    switch (method) {                                                    \
+    case METHOD_WENO: F2D_FF(T, METHOD_WENO); break;                     \
+    case METHOD_UPWIND: F2D_FF(T, METHOD_UPWIND); break;                 \
+    case METHOD_CENTERED: F2D_FF(T, METHOD_CENTERED); break;             \
+    default: F2D_FF(T, METHOD_CWENO); break;                             \
+    }
+    if (prec == 0) { F2D_DISPATCH(double) } else { F2D_DISPATCH(float) }
+#undef F2D_DISPATCH
+#undef F2D_FF
+    return (int)cudaGetLastError();
+}
+
+int launch_rsw_stage(int method, int prec, const CUtensorMap* th,
+                     const CUtensorMap* tw, const RswIn& a, const uint32_t* code,
+                     int stage, const Geom& g, DevScalars* sc, cudaStream_t s)
+{
+    dim3 grid = tile_grid(g), block(TX, TY);
+#define F2D_RS(T, M) k_rsw_stage<T, M><<<grid, block, 0, s>>>(*th, *tw, a, code, stage, g, sc)
+#define F2D_DISPATCH(T)                                      \
+    switch (method) {                                        \
+    case METHOD_WENO: F2D_RS(T, METHOD_WENO); break;         \
+    case METHOD_UPWIND: F2D_RS(T, METHOD_UPWIND); break;     \
+    case METHOD_CENTERED: F2D_RS(T, METHOD_CENTERED); break; \
+    default: F2D_RS(T, METHOD_CWENO); break;                 \
+    }
+    if (prec == 0) { F2D_DISPATCH(double) } else { F2D_DISPATCH(float) }
+#undef F2D_DISPATCH
+#undef F2D_RS
+    return (int)cudaGetLastError();
+}
+
+int launch_rsw_diag(int method, int prec, const CUtensorMap* tux,
+                    const CUtensorMap* tuy, const RswDiag& a, const uint32_t* code,
+                    const Geom& g, DevScalars* sc, cudaStream_t s)
+{
+    dim3 grid = tile_grid(g), block(TX, TY);
+#define F2D_RD(T, M) k_rsw_diag<T, M><<<grid, block, 0, s>>>(*tux, *tuy, a, code, g, sc)
+#define F2D_DISPATCH(T)                                      \
+    switch (method) {                                        \
+    case METHOD_WENO: F2D_RD(T, METHOD_WENO); break;         \
+    case METHOD_UPWIND: F2D_RD(T, METHOD_UPWIND); break;     \
+    case METHOD_CENTERED: F2D_RD(T, METHOD_CENTERED); break; \
+    default: F2D_RD(T, METHOD_CWENO); break;                 \
+    }
+    if (prec == 0) { F2D_DISPATCH(double) } else { F2D_DISPATCH(float) }
+#undef F2D_DISPATCH
+#undef F2D_RD
+    return (int)cudaGetLastError();
+}
+
+static dim3 pt_grid(const Geom& g) { return dim3((g.NX + 31) / 32, (g.NY + 7) / 8); }
+
+int launch_c2v(int prec, const void* q, void* v, const uint32_t* code,
+               const void* fv, const Geom& g, cudaStream_t s)
+{
+    if (prec == 0)
+        k_c2v<double><<<pt_grid(g), dim3(32, 8), 0, s>>>((const double*)q, (double*)v,
+                                                        code, (const double*)fv, g);
+    else
+        k_c2v<float><<<pt_grid(g), dim3(32, 8), 0, s>>>((const float*)q, (float*)v,
+                                                       code, (const float*)fv, g);
+    return (int)cudaGetLastError();
+}
+
+int launch_perpgrad(int prec, const void* psi, void* Ux, void* Uy,
+                    const uint32_t* code, double rdy2, double rdx2, int fillU,
+                    const Geom& g, DevScalars* sc, double* partials, cudaStream_t s)
+{
+    if (prec == 0)
+        k_perpgrad<double><<<pt_grid(g), dim3(32, 8), 0, s>>>(
+            (const double*)psi, (double*)Ux, (double*)Uy, code, rdy2, rdx2, fillU, g,
+            sc, partials);
+    else
+        k_perpgrad<float><<<pt_grid(g), dim3(32, 8), 0, s>>>(
+            (const float*)psi, (float*)Ux, (float*)Uy, code, rdy2, rdx2, fillU, g, sc,
+            partials);
+    return (int)cudaGetLastError();
+}
+
+int launch_maxabs2(int prec, const void* Ux, const void* Uy, const Geom& g,
+                   DevScalars* sc, double* partials, cudaStream_t s)
+{
+    if (prec == 0)
+        k_maxabs2<double><<<pt_grid(g), dim3(32, 8), 0, s>>>(
+            (const double*)Ux, (const double*)Uy, g, sc, partials);
+    else
+        k_maxabs2<float><<<pt_grid(g), dim3(32, 8), 0, s>>>(
+            (const float*)Ux, (const float*)Uy, g, sc, partials);
+    return (int)cudaGetLastError();
+}
+
+int launch_fill_periodic(int prec, void* a, const Geom& g, cudaStream_t s)
+{
+    if (!g.xper) return 0;
+    dim3 grid(1, (g.NY + 31) / 32), block(8, 32);
+    if (prec == 0) k_fill_periodic<double><<<grid, block, 0, s>>>((double*)a, g);
+    else k_fill_periodic<float><<<grid, block, 0, s>>>((float*)a, g);
+    return (int)cudaGetLastError();
+}
+
+int launch_set_dt(DevScalars* sc, cudaStream_t s)
+{
+    k_set_dt<<<1, 1, 0, s>>>(sc);
+    return (int)cudaGetLastError();
+}
+
+int launch_pushforward(DevScalars* sc, cudaStream_t s)
+{
+    k_pushforward<<<1, 1, 0, s>>>(sc);
+    return (int)cudaGetLastError();
+}
+
+size_t pt_grid_blocks(const Geom& g)
+{
+    dim3 d = pt_grid(g);
+    return (size_t)d.x * d.y;
+}
+
+}  // namespace f2d

@@ -1,0 +1,47 @@
+// Launchers of the fused stage and diagnostic kernels (stage.cu).
+#pragma once
+#include "common.cuh"
+
+namespace f2d {
+
+struct RswIn {
+    const void *ux, *uy, *h;        // prognostic, stage input
+    void *uxo, *uyo, *ho;           // prognostic, stage output
+    const void *Ux, *Uy, *ke, *p;   // diagnostics of the stage input
+    void *dux, *duy, *dh;           // this stage's tendencies (stored if != 0)
+    const void *dux1, *duy1, *dh1;  // earlier tendencies
+    const void *dux2, *duy2, *dh2;
+    double fc;                      // f0 * area * 0.25 (operators.py:33)
+};
+
+struct RswDiag {
+    const void *ux, *uy, *h;
+    void *Ux, *Uy, *omega, *ke, *p;
+    double rdx2, rdy2;  // 1/dx**2, 1/dy**2 (operators.py:62-63)
+    double goa;         // g/area (operators.py:111)
+};
+
+int launch_fluxform_stage(int method, int prec, const CUtensorMap* tq,
+                          const void* qin, void* qout, const void* Ux,
+                          const void* Uy, const uint32_t* code, void* ds_out,
+                          const void* ds1, const void* ds2, int stage,
+                          const Geom& g, DevScalars* sc, cudaStream_t s);
+int launch_rsw_stage(int method, int prec, const CUtensorMap* th,
+                     const CUtensorMap* tw, const RswIn& a, const uint32_t* code,
+                     int stage, const Geom& g, DevScalars* sc, cudaStream_t s);
+int launch_rsw_diag(int method, int prec, const CUtensorMap* tux,
+                    const CUtensorMap* tuy, const RswDiag& a, const uint32_t* code,
+                    const Geom& g, DevScalars* sc, cudaStream_t s);
+int launch_c2v(int prec, const void* q, void* v, const uint32_t* code,
+               const void* fv, const Geom& g, cudaStream_t s);
+int launch_perpgrad(int prec, const void* psi, void* Ux, void* Uy,
+                    const uint32_t* code, double rdy2, double rdx2, int fillU,
+                    const Geom& g, DevScalars* sc, double* partials, cudaStream_t s);
+int launch_maxabs2(int prec, const void* Ux, const void* Uy, const Geom& g,
+                   DevScalars* sc, double* partials, cudaStream_t s);
+int launch_fill_periodic(int prec, void* a, const Geom& g, cudaStream_t s);
+int launch_set_dt(DevScalars* sc, cudaStream_t s);
+int launch_pushforward(DevScalars* sc, cudaStream_t s);
+size_t pt_grid_blocks(const Geom& g);
+
+}  // namespace f2d

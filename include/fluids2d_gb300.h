@@ -1,0 +1,164 @@
+/*
+ * fluids2d_gb300 - C ABI of the GB300-native time-stepping path of Fluids2d.
+ *
+ * Plain pointers and sizes only. Every function returns 0 on success and a
+ * non-zero code otherwise; f2d_last_error() gives the message of the last
+ * failure on the calling thread. Arrays crossing the boundary use the
+ * reference's layout: C-contiguous (ny+6, nx+6) float64 (int8 for masks and
+ * stencil orders), halo width 3.
+ *
+ * Reference interfaces each entry point replaces are cited as
+ * file:line of pvthinker/Fluids2d.
+ */
+#ifndef FLUIDS2D_GB300_H
+#define FLUIDS2D_GB300_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define F2D_ABI_VERSION 1
+
+/* models (param.py:1-2); the hot path covers these three */
+enum { F2D_MODEL_EULERPSI = 0, F2D_MODEL_RSW = 1, F2D_MODEL_QG = 2 };
+/* flux methods (param.py:4, weno.py:338-343) */
+enum { F2D_METHOD_WENO = 0, F2D_METHOD_UPWIND = 1, F2D_METHOD_CENTERED = 2,
+       F2D_METHOD_CWENO = 3 };
+/* arithmetic of the stencils and of the multigrid cycle */
+enum { F2D_PREC_FP64 = 0, F2D_PREC_FP32 = 1 };
+/* param.noslip (noslip.py:18-34): None/False, True, or a list of sides */
+enum { F2D_SLIP_FREE = 0, F2D_SLIP_NOSLIP = 1, F2D_SLIP_SIDES = 2 };
+enum { F2D_SIDE_LEFT = 1, F2D_SIDE_RIGHT = 2, F2D_SIDE_BOTTOM = 4,
+       F2D_SIDE_TOP = 8 };
+
+/* The subset of fluids2d.Param (param.py:11-59) the stepping path reads. */
+typedef struct f2d_params {
+    int model;          /* F2D_MODEL_* */
+    int nx, ny;         /* interior cells */
+    int halowidth;      /* must be 3 */
+    int xperiodic;      /* 0/1 */
+    int yperiodic;      /* must be 0 */
+    double Lx, Ly;
+    double f0, beta, g, H;
+    double cfl, dtmax, dt; /* dt > 0: fixed time step (model.py:72-74) */
+    int compflux, vortexforce, innerproduct; /* F2D_METHOD_* */
+    int maxorder;
+    int noslip;         /* F2D_SLIP_* */
+    int noslip_sides;   /* F2D_SIDE_* bits when noslip == F2D_SLIP_SIDES */
+    int precision;      /* F2D_PREC_* */
+    double poisson_tol; /* relative residual of the Poisson solve */
+    int poisson_maxit;
+    int reserved[7];
+} f2d_params;
+
+typedef struct f2d_model_s *f2d_model;
+
+int f2d_abi_version(void);
+const char *f2d_last_error(void);
+
+/* Defaults of param.py:11-59 plus poisson_tol = 1e-12, maxit = 200. */
+int f2d_params_default(f2d_params *p);
+
+/* ---- host-side mesh construction (no GPU needed) ---------------------- */
+
+/* set_order (meshes.py:146-186): stencil orders of a flattened mask. */
+int f2d_set_order(const int8_t *msk, int64_t n, int64_t shift, int maxorder,
+                  int8_t *order);
+
+/* Mesh.finalize without the factorisations (meshes.py:34-37, 77-104;
+ * noslip.py:4-36; elliptic.py:102-111, 198-203). Outputs are (ny+6, nx+6)
+ * arrays; orders is 6 arrays back to back: oc.x, oc.y, ov.x, ov.y, ok.x,
+ * ok.y; gv is the vertex index G of Poisson2D(mesh, "v"). Any output
+ * pointer may be NULL. */
+int f2d_mesh_build(const f2d_params *p, const int8_t *msk, int8_t *mskx,
+                   int8_t *msky, int8_t *mskv, double *slipcoef,
+                   int8_t *orders, int32_t *gv);
+
+/* ---- flat-index sweeps on device arrays (weno.py:346-446) ------------- */
+/* CompFlux[method](flx, U, q, o, s, i0, i1), weno.py:349-363 */
+int f2d_compflux(int method, double *flx, const double *U, const double *q,
+                 const int8_t *o, int64_t s, int64_t i0, int64_t i1,
+                 void *stream);
+/* VortexForce[method](du, V, q, o, s, s2, sign, i0, i1), weno.py:370-384 */
+int f2d_vortexforce(int method, double *du, const double *V, const double *q,
+                    const int8_t *o, int64_t s, int64_t s2, int sign,
+                    int64_t i0, int64_t i1, void *stream);
+/* InnerProduct[method](ke, U, q, o, s, i0, i1), weno.py:391-403 */
+int f2d_innerproduct(int method, double *ke, const double *U, const double *q,
+                     const int8_t *o, int64_t s, int64_t i0, int64_t i1,
+                     void *stream);
+
+/* ---- models ------------------------------------------------------------ */
+
+/* Model(param) with the mask msk (meshes.py:18-52, model.py:14-24); msk may
+ * be NULL for the default mask (meshes.py:70-75). Device buffers are owned
+ * by the model. */
+int f2d_model_create(const f2d_params *p, const int8_t *msk, f2d_model *out);
+int f2d_model_destroy(f2d_model m);
+
+/* Mesh.finalize after editing the mask (meshes.py:34-52). */
+int f2d_model_set_mask(f2d_model m, const int8_t *msk);
+
+/* Stream the model runs on (cudaStream_t as void*); NULL = its own. */
+int f2d_model_set_stream(f2d_model m, void *stream);
+
+/* State fields by the reference's names (states.py:7-17): "omega", "psi",
+ * "vomega", "U.x", "U.y", "u.x", "u.y", "h", "ke", "p", "pv", "work", ...
+ * Host arrays are (ny+6, nx+6) float64. set/get synchronise the stream. */
+int f2d_field_set(f2d_model m, const char *name, const double *host);
+int f2d_field_get(f2d_model m, const char *name, double *host);
+/* Same, asynchronous on the model's stream (host memory should be pinned). */
+int f2d_field_set_async(f2d_model m, const char *name, const double *host);
+int f2d_field_get_async(f2d_model m, const char *name, double *host);
+/* Device address, row pitch (elements) and element size of a field. */
+int f2d_field_device(f2d_model m, const char *name, void **ptr,
+                     int64_t *pitch, int *elem_size);
+/* Names of the fields of the model, comma-separated. */
+int f2d_field_names(f2d_model m, char *buf, size_t len);
+
+/* mesh.f, the vertex Coriolis term of the beta-plane (qg_inversion,
+ * operators.py:186-191); (ny+6, nx+6) float64. */
+int f2d_set_coriolis(f2d_model m, const double *f_vertices);
+
+/* integrator.diag(state) (equations.py:80-84, 99-101, 150-155) */
+int f2d_diag(f2d_model m);
+/* Model.step(n) with the current time step (model.py:67-69) */
+int f2d_step(f2d_model m, int nsteps);
+/* n iterations of the Model.run loop body: set_dt then step(1)
+ * (model.py:45-51); the CFL time step is computed on the device. */
+int f2d_run(f2d_model m, int nsteps);
+/* Model.set_dt (model.py:71-87) */
+int f2d_set_dt(f2d_model m);
+/* Time (timeline.py:4-35) */
+int f2d_time_get(f2d_model m, double *t, double *dt, int64_t *ite);
+int f2d_time_set(f2d_model m, double t, double dt, int64_t ite);
+
+/* Poisson2D.solve(b, x) (elliptic.py:80-87) on the vertex operator
+ * (which = 0) or the qg Helmholtz operator (which = 1, meshes.py:42-47):
+ * only fluid points of x are written, then the halo fill. Host arrays. */
+int f2d_poisson_solve(f2d_model m, int which, const double *b, double *x,
+                      int *iters, double *relres);
+
+/* Wait for the model's stream; returns the device status (timeouts,
+ * non-converged solves, non-finite values) as an error. */
+int f2d_sync(f2d_model m);
+/* Time `reps` launches of the fused right-hand-side + RK3-update kernel of
+ * stage 1..3 on the model's stream with CUDA events (L2 flushed between
+ * launches when flush_l2 != 0); *avg_ms = mean milliseconds per launch.
+ * Repeated launches recompute the same output, so the state is unchanged.
+ * No reference counterpart: the measurement hook of the benchmark. */
+int f2d_time_stage(f2d_model m, int stage, int reps, int flush_l2,
+                   double *avg_ms);
+/* Counters: Poisson iterations summed over all solves since creation; the
+ * kernels one time step launches outside the Poisson loops; the kernels one
+ * Poisson iteration launches. No reference counterpart (instrumentation). */
+int f2d_stats(f2d_model m, int64_t *poisson_iters,
+              int64_t *launches_per_step, int64_t *launches_per_iter);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* FLUIDS2D_GB300_H */

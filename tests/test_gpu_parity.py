@@ -1,0 +1,279 @@
+"""GPU parity: the CUDA path against the reference (golden fixtures) and the
+oracle, through the C ABI.
+
+Tolerances (FP64 form): flux sweeps 1e-13 relative to the array's max (the
+kernels may contract multiply-adds into FMAs, the reference does not);
+Poisson/Helmholtz solves 1e-10 relative L2 (multigrid-PCG to a relative
+residual of 1e-12 against the reference's direct LU); whole model states
+1e-10 relative L2 per field and per step.
+"""
+import os
+
+import numpy as np
+import pytest
+
+from conftest import GOLDEN
+from oracle import oracle as O
+
+pytestmark = pytest.mark.gpu
+torch = pytest.importorskip("torch")
+
+import fluids2d_gb300 as f2d  # noqa: E402
+from fluids2d_gb300 import _lib, workloads as wl  # noqa: E402
+
+SWEEP_TOL = 1e-13
+SOLVE_TOL = 1e-10
+STEP_TOL = 1e-10
+
+
+@pytest.fixture(scope="module", autouse=True)
+def _need_gpu():
+    if not torch.cuda.is_available():
+        pytest.skip("no CUDA device")
+
+
+def load(name):
+    return np.load(os.path.join(GOLDEN, name), allow_pickle=False)
+
+
+def rel_l2(a, b):
+    nb = np.linalg.norm(b)
+    d = np.linalg.norm(a - b)
+    return d / nb if nb > 0 else d
+
+
+def dev(a):
+    return torch.from_numpy(np.ascontiguousarray(a)).cuda()
+
+
+def dptr(t):
+    return _lib.c_void_p(t.data_ptr())
+
+
+# ------------------------------------------------------------- sweeps ----
+@pytest.mark.parametrize("method", ["weno", "upwind", "centered", "cweno"])
+def test_sweeps_vs_reference(method):
+    g = load("sweeps.npz")
+    L = _lib.lib()
+    M = _lib.METHODS[method]
+    q, U, V = dev(g["q"]), dev(g["U"]), dev(g["V"])
+    sx, sy = (int(v) for v in g["shifts"])
+    n = g["q"].size
+    for d, s, s2, sign in (("x", sx, sy, -1), ("y", sy, sx, +1)):
+        o = dev(g["oc" + d])
+        flx = torch.zeros_like(q)
+        _lib.check(L.f2d_compflux(M, dptr(flx), dptr(U), dptr(q), dptr(o), s, 0,
+                                  n, None))
+        ref = g[f"compflux/{method}/{d}"]
+        torch.cuda.synchronize()
+        assert np.max(np.abs(flx.cpu().numpy() - ref)) <= SWEEP_TOL * np.max(np.abs(ref))
+        o = dev(g["ov" + d])
+        du = torch.zeros_like(q)
+        _lib.check(L.f2d_vortexforce(M, dptr(du), dptr(V), dptr(q), dptr(o), s, s2,
+                                     sign, 0, n, None))
+        ref = g[f"vortexforce/{method}/{d}"]
+        torch.cuda.synchronize()
+        assert np.max(np.abs(du.cpu().numpy() - ref)) <= SWEEP_TOL * np.max(np.abs(ref))
+        o = dev(g["ok" + d])
+        ke = dev(g[f"innerproduct_in/{method}/{d}"])
+        _lib.check(L.f2d_innerproduct(M, dptr(ke), dptr(U), dptr(q), dptr(o), s, 0,
+                                      n, None))
+        ref = g[f"innerproduct/{method}/{d}"]
+        torch.cuda.synchronize()
+        assert np.max(np.abs(ke.cpu().numpy() - ref)) <= SWEEP_TOL * np.max(np.abs(ref))
+
+
+# ------------------------------------------------------------ poisson ----
+def _model(kind, nx, ny, msk=None, **kw):
+    p = f2d.Param()
+    p.model = kind
+    p.nx, p.ny = nx, ny
+    for k, v in kw.items():
+        setattr(p, k, v)
+    m = f2d.Model(p)
+    if msk is not None:
+        m.mesh.msk[:] = msk
+        m.mesh.finalize()
+    return m
+
+
+@pytest.mark.parametrize("case", list(load("poisson.npz")["names"]))
+def test_poisson_vs_reference(case):
+    g = load("poisson.npz")
+    nx, ny, xper = (int(v) for v in g[case + "/params"])
+    helm = float(g[case + "/maindiag"]) != 0
+    m = _model("qg" if helm else "eulerpsi", nx, ny, g[case + "/msk"],
+               xperiodic=bool(xper), f0=float(g[case + "/f0"]))
+    solver = m.mesh.qg_helmholtz if helm else m.mesh.poisson_vertices
+    x = g[case + "/x0"].copy()
+    solver.solve(g[case + "/b"], x)
+    ref = g[case + "/x"]
+    assert rel_l2(x, ref) <= SOLVE_TOL, (rel_l2(x, ref), solver.last_iters)
+    # points the reference does not write keep their values
+    touched = (m.mesh.G_vertices >= 0)
+    if xper:
+        touched[:, :3] = touched[:, -3:] = True
+    np.testing.assert_array_equal(x[~touched], g[case + "/x0"][~touched])
+
+
+def test_poisson_zero_rhs():
+    m = _model("eulerpsi", 24, 20)
+    x = np.random.default_rng(0).normal(size=m.mesh.shape)
+    m.mesh.poisson_vertices.solve(np.zeros(m.mesh.shape), x)
+    assert np.all(x[m.mesh.G_vertices >= 0] == 0)
+
+
+# -------------------------------------------------------------- models ----
+MODEL_FILES = ["model_eulerpsi.npz", "model_eulerpsi_islands.npz",
+               "model_rsw.npz", "model_qg.npz"]
+
+
+def model_from_golden(g):
+    nx, ny, xper = (int(v) for v in g["params"])
+    Lx, Ly, f0, beta, gg, H, cfl = (float(v) for v in g["scalars"])
+    names = {k[3:] for k in g.files if k.startswith("ic/")}
+    kind = ("eulerpsi" if "omega" in names else "rsw" if "h" in names else "qg")
+    m = _model(kind, nx, ny, g["msk"], xperiodic=bool(xper), Lx=Lx, Ly=Ly, f0=f0,
+               beta=beta, g=gg, H=H, cfl=cfl, tend=1e300, maxite=10 ** 9)
+    if "f" in g.files:
+        m.mesh.f = g["f"]
+    s = m.state
+    for k in names:
+        getattr(s, k)[:] = g["ic/" + k]
+    m.integrator.diag(s)
+    return m
+
+
+def state_dict(m):
+    out = {}
+    s = m.state
+    for name in s._fields:
+        v = getattr(s, name)
+        if hasattr(v, "_fields"):
+            out[name + ".x"], out[name + ".y"] = v.x.copy(), v.y.copy()
+        else:
+            out[name] = v.copy()
+    return out
+
+
+def compare(m, ref_get, tol, skip=("flx.x", "flx.y")):
+    worst = {}
+    for k, v in state_dict(m).items():
+        if k in skip:
+            continue
+        r = ref_get(k)
+        if r is None or not np.any(r):
+            continue
+        worst[k] = rel_l2(v, r)
+    bad = {k: e for k, e in worst.items() if e > tol}
+    assert not bad, bad
+    return worst
+
+
+@pytest.mark.parametrize("fname", MODEL_FILES)
+def test_model_steps_vs_reference(fname):
+    g = load(fname)
+    m = model_from_golden(g)
+    getter = lambda pre: (lambda k: g[f"{pre}/{k}"] if f"{pre}/{k}" in g.files else None)  # noqa
+    compare(m, getter("step0"), STEP_TOL)
+    dts = g["dt"]
+    for k in range(1, len(dts) + 1):
+        m.advance(1)
+        assert abs(m.time.dt - dts[k - 1]) <= 1e-10 * dts[k - 1]
+        compare(m, getter(f"step{k}"), STEP_TOL)
+    m.sync()
+    assert abs(m.time.t - float(g["t"])) <= 1e-10 * float(g["t"])
+    assert m.time.ite == len(dts)
+
+
+def _oracle_like(case, kind):
+    p = O.Param(model=kind, nx=case["nx"], ny=case["ny"],
+                xperiodic=case.get("xperiodic", False), Lx=case["Lx"],
+                Ly=case["Ly"], tend=1e300, maxite=10 ** 9)
+    for k in ("f0", "g", "H", "beta"):
+        if k in case:
+            setattr(p, k, case[k])
+    om = O.Model(p, msk=case["msk"], pysq=False)
+    if "f" in case:
+        om.mesh.f = case["f"].copy()
+    for k, v in case["fields"].items():
+        om.s[k][:] = v
+    om.diag()
+    return om
+
+
+@pytest.mark.parametrize("kind", ["eulerpsi", "rsw", "qg"])
+def test_model_vs_oracle_larger(kind):
+    if kind == "eulerpsi":
+        case = wl.eulerpsi_case(n=128, ny=96, seed=5, nislands=3)
+    elif kind == "rsw":
+        case = wl.rsw_case(n=128, ny=96, seed=6, nislands=3)
+    else:
+        case = wl.qg_case(n=128, ny=128, seed=7, nislands=4)
+    om = _oracle_like(case, kind)
+    kw = dict(xperiodic=case.get("xperiodic", False), Lx=case["Lx"], Ly=case["Ly"],
+              tend=1e300, maxite=10 ** 9)
+    for k in ("f0", "g", "H", "beta"):
+        if k in case:
+            kw[k] = case[k]
+    m = _model(kind, case["nx"], case["ny"], case["msk"], **kw)
+    if "f" in case:
+        m.mesh.f = case["f"]
+    s = m.state
+    for k, v in case["fields"].items():
+        getattr(s, k)[:] = v
+    m.integrator.diag(s)
+    compare(m, lambda k: om.s.get(k), STEP_TOL)
+    for _ in range(4):
+        om.run_steps(1)
+        m.advance(1)
+        assert abs(m.time.dt - om.dt) <= 1e-10 * om.dt
+        compare(m, lambda k: om.s.get(k), STEP_TOL)
+    m.sync()
+
+
+# --------------------------------------------- size-independent checks ----
+def test_rsw_mass_conservation_full_size():
+    case = wl.rsw_case(n=512, seed=0, nislands=3)
+    m = _model("rsw", 512, 512, case["msk"], xperiodic=True, f0=1.0, g=1, H=1,
+               tend=1e300, maxite=10 ** 9)
+    m.state.h[:] = case["fields"]["h"]
+    m.integrator.diag(m.state)
+    inner = (slice(3, -3), slice(3, -3))
+    mass0 = float(np.sum(m.state.h[inner]))
+    m.advance(20)
+    m.sync()
+    mass1 = float(np.sum(m.state.h[inner]))
+    assert abs(mass1 - mass0) <= 1e-12 * abs(mass0)
+    assert np.all(np.isfinite(m.state.u.x))
+
+
+def test_eulerpsi_circulation_full_size():
+    case = wl.eulerpsi_case(n=256, seed=0)
+    m = _model("eulerpsi", 256, 256, case["msk"], cfl=0.8, tend=1e300,
+               maxite=10 ** 9)
+    m.state.omega[:] = case["fields"]["omega"]
+    m.integrator.diag(m.state)
+    w0 = m.state.omega.copy()
+    m.advance(10)
+    m.sync()
+    w1 = m.state.omega
+    assert abs(w1.sum() - w0.sum()) <= 1e-12 * np.abs(w0).sum()
+    # the Poisson solve of the last diagnostic is converged
+    psi = m.state.psi
+    lap = O.laplacian(O.Mesh(O.Param(model="eulerpsi", nx=256, ny=256)), 0)[0]
+    G = m.mesh.G_vertices
+    sel = G >= 0
+    b = m.state.vomega[sel]
+    r = b - lap @ psi[sel]
+    assert np.linalg.norm(r) <= 1e-10 * np.linalg.norm(b)
+
+
+def test_poisson_maxit_reports_status():
+    m = _model("eulerpsi", 64, 64, poisson_maxit=1, poisson_tol=1e-15)
+    case = wl.eulerpsi_case(n=64, seed=1)
+    m.state.omega[:] = case["fields"]["omega"]
+    m.integrator.diag(m.state)
+    with pytest.raises(f2d.F2DError, match="max iterations"):
+        m.sync()
+    m.sync()  # status is cleared once reported
