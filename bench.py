@@ -51,6 +51,9 @@ WORKLOADS = {
                "MG-PCG Helmholtz"),
     "qg1024": ("qg", dict(n=1024, seed=0, nislands=20),
                "qg 1024x1024 basin, 20 islands, Rd=0.02, beta=1, FP64"),
+    "rsw1024": ("rsw", dict(n=1024, seed=0, nislands=3),
+                "rsw 1024x1024 x-periodic channel, 3 islands, FP64 (profiling "
+                "size: working set above the L2)"),
 }
 
 L2_BYTES = 126 * 2 ** 20
@@ -247,7 +250,10 @@ def run_gpu(args, rank, world):
     import ctypes
 
     model, case, desc = build_case(args.workload)
-    stream = torch.cuda.current_stream()
+    # one non-default stream for the model, the L2 flushes and the events
+    stream = torch.cuda.Stream()
+    torch.cuda.set_stream(stream)
+    assert stream.cuda_stream != 0
     m = make_gpu_model(model, case, ctypes.c_void_p(stream.cuda_stream))
     h = m._h
     L = lib()
