@@ -83,6 +83,8 @@ _SIGS = {
     "f2d_sync": ([c_void_p], c_int),
     "f2d_time_stage": ([c_void_p, c_int, c_int, c_int, ctypes.POINTER(c_dbl)],
                        c_int),
+    "f2d_cfl_dt_noalloc": ([c_void_p, c_void_p, c_i64, c_i64, c_i64, c_dbl,
+                            c_dbl, c_void_p, c_void_p], c_int),
     "f2d_stats": ([c_void_p, ctypes.POINTER(c_i64), ctypes.POINTER(c_i64),
                    ctypes.POINTER(c_i64)], c_int),
 }

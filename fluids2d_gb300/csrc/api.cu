@@ -33,6 +33,9 @@ static int fail(int code, const std::string& msg)
     return code ? code : 1;
 }
 
+// error reporting for the other translation units of the library
+int f2d_internal_fail(int code, const char* msg) { return fail(code, msg); }
+
 #define CK(call)                                                                   \
     do {                                                                           \
         cudaError_t e_ = (call);                                                   \

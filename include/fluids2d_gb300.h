@@ -158,6 +158,26 @@ int f2d_time_stage(f2d_model m, int stage, int reps, int flush_l2,
 int f2d_stats(f2d_model m, int64_t *poisson_iters,
               int64_t *launches_per_step, int64_t *launches_per_iter);
 
+/* ---- allocation-free entry point ---------------------------------------- */
+
+/* No counterpart in the reference. For callers that must not allocate
+ * device memory (code recording a stream into a CUDA graph, frameworks that
+ * route all device memory through their own pool, loops where a cudaMalloc
+ * would synchronise the device): Model.set_dt's CFL step computed from
+ * caller-owned device arrays U.x, U.y of rows x cols points with row pitch
+ * `pitch` (elements). Writes out[0] = max|U.x|, out[1] = max|U.y|,
+ * out[2] = min(cfl / (out[0] + out[1] + 1e-99), dtmax) to the caller's device
+ * buffer `out` on `stream`; calls no cudaMalloc/cudaFree.
+ * Its reduction scratch is a fixed 128 KiB array inside the library, kept by
+ * every GPU that loads the library until exit, so rows * pitch is limited to
+ * 33,554,432 points (larger arrays are refused with an error). The first call
+ * on each device looks up that array's device address; make that first call
+ * before any stream capture. Calls share the array: calls that overlap on the
+ * GPU race and give wrong results, so serialise them on one stream. */
+int f2d_cfl_dt_noalloc(const double *Ux, const double *Uy, int64_t rows,
+                       int64_t cols, int64_t pitch, double cfl, double dtmax,
+                       double *out, void *stream);
+
 #ifdef __cplusplus
 }
 #endif
