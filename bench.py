@@ -59,9 +59,16 @@ WORKLOADS = {
 L2_BYTES = 126 * 2 ** 20
 
 
+def precision_of(name):
+    return "fp32" if name.endswith("_fp32") else "fp64"
+
+
 def build_case(name):
     from fluids2d_gb300 import workloads as wl
-    model, kw, desc = WORKLOADS[name]
+    base = name[:-5] if name.endswith("_fp32") else name
+    model, kw, desc = WORKLOADS[base]
+    if name.endswith("_fp32"):
+        desc = desc.replace("FP64", "FP32 stencils + FP32 multigrid, FP64 CG")
     if model == "rsw":
         case = wl.rsw_case(**kw)
     elif model == "eulerpsi":
@@ -71,7 +78,7 @@ def build_case(name):
     return model, case, desc
 
 
-def make_gpu_model(model, case, stream_ptr):
+def make_gpu_model(model, case, stream_ptr, precision="fp64"):
     import fluids2d_gb300 as f2d
     from fluids2d_gb300._lib import check, lib
     p = f2d.Param()
@@ -86,6 +93,7 @@ def make_gpu_model(model, case, stream_ptr):
         p.cfl = 0.8
     p.tend = 1e300
     p.maxite = 10 ** 12
+    p.precision = precision
     m = f2d.Model(p)
     check(lib().f2d_model_set_stream(m._h, stream_ptr))
     m.mesh.msk[:] = case["msk"]
@@ -186,6 +194,19 @@ def read_profile_traffic(kernel):
     return None
 
 
+def read_profile_value(kernel, key):
+    path = os.path.join(ROOT, "profiles", f"{kernel}.md")
+    if not os.path.exists(path):
+        return None
+    for line in open(path):
+        if line.startswith(key + ":"):
+            try:
+                return float(line.split(":", 1)[1].split()[0])
+            except ValueError:
+                return None
+    return None
+
+
 def cpu_oracle_rate(model, case, budget_s, max_steps=None, warmup=1):
     """Oracle port (C sweeps on all host threads + numpy + SuperLU)."""
     from oracle import oracle as O
@@ -254,7 +275,8 @@ def run_gpu(args, rank, world):
     stream = torch.cuda.Stream()
     torch.cuda.set_stream(stream)
     assert stream.cuda_stream != 0
-    m = make_gpu_model(model, case, ctypes.c_void_p(stream.cuda_stream))
+    prec = precision_of(args.workload)
+    m = make_gpu_model(model, case, ctypes.c_void_p(stream.cuda_stream), prec)
     h = m._h
     L = lib()
     cells = case["nx"] * case["ny"]
@@ -320,6 +342,8 @@ def run_gpu(args, rank, world):
     check(L.f2d_time_stage(h, 2, 20, 1, ctypes.byref(avg)))
     npts = (case["ny"] + 6) * (case["nx"] + 6)
     alg_bytes = STAGE2_BYTES[model] * npts
+    if prec == "fp32":  # 4-byte fields, the 4-byte code word unchanged
+        alg_bytes = ((STAGE2_BYTES[model] - 4) // 2 + 4) * npts
     achieved = alg_bytes / (avg.value * 1e-3) / 1e9
     peaks = {}
     try:
@@ -330,6 +354,7 @@ def run_gpu(args, rank, world):
     kname = {"rsw": "k_rsw_stage", "eulerpsi": "k_fluxform_stage",
              "qg": "k_fluxform_stage"}[model]
     traffic = read_profile_traffic(f"{kname}_{args.workload}")
+    fp64_pct = read_profile_value(f"{kname}_{args.workload}", "fp64_pipe_pct")
 
     # launches in the timed region: fixed kernels per step + Poisson bodies
     _, nfix, body = m.stats()
@@ -339,7 +364,8 @@ def run_gpu(args, rank, world):
         "metric": "cell-updates/s", "value": value, "unit": "cell-updates/s",
         "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
         "ms_per_step": ms / args.steps, "higher_is_better": True,
-        "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+        "scaling": "weak", "vs_baseline": None,
+        "dtype": "f32" if prec == "fp32" else "f64",
         "data": "synthetic",
         "config": {"workload": args.workload, "desc": desc,
                    "grid": [case["ny"], case["nx"]],
@@ -352,7 +378,9 @@ def run_gpu(args, rank, world):
                      "unit": "GB/s", "frac": achieved / peak,
                      "traffic": traffic, "kernel": kname,
                      "kernel_ms": avg.value, "alg_bytes_per_launch": alg_bytes,
-                     "peak_source": peak_src},
+                     "peak_source": peak_src,
+                     "binding_roof_ncu": ({"fp64_pipe_active_pct": fp64_pct}
+                                          if fp64_pct is not None else None)},
         "gpu_launches": launches,
         "poisson_iters": pcg_iters,
         "clocks": clk.summary(),
@@ -375,7 +403,8 @@ def main():
     ap.add_argument("--steps", type=int, default=200)
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
-    ap.add_argument("--workload", default="rsw512", choices=sorted(WORKLOADS))
+    ap.add_argument("--workload", default="rsw512",
+                    choices=sorted(WORKLOADS) + sorted(k + "_fp32" for k in WORKLOADS))
     ap.add_argument("--no-cpu-baseline", action="store_true")
     args = ap.parse_args()
     world = int(os.environ.get("WORLD_SIZE", "1"))

@@ -3,6 +3,7 @@
 #include <cudaTypedefs.h>
 
 #include <cmath>
+#include <cstdlib>
 #include <cstdio>
 #include <cstring>
 #include <map>
@@ -69,6 +70,7 @@ static PFN_cuTensorMapEncodeTiled_v12000 encode_fn()
 struct Field {
     void* buf[2] = {nullptr, nullptr};
     bool pingpong = false;
+    int es = 8;  // element size: 8 (FP64) or 4 (FP32)
 };
 
 struct f2d_model_s {
@@ -93,6 +95,8 @@ struct f2d_model_s {
     MGHost mg[2];
     bool mg_ready[2] = {false, false};
     void *pr = nullptr, *pz = nullptr, *pp = nullptr, *pq = nullptr;
+    void* prmg = nullptr;  // V-cycle right-hand side (== pr in FP64)
+    void* stage64 = nullptr;  // FP64 staging for field I/O of FP32 fields
     void *sb = nullptr, *sx = nullptr;  // scratch for f2d_poisson_solve
     std::map<void*, CUtensorMap> tmaps;
     int cur = 0;
@@ -112,14 +116,18 @@ static void* dalloc(f2d_model_s* m, size_t bytes)
     return p;
 }
 
-static size_t field_bytes(const f2d_model_s* m) { return (size_t)m->g.P * m->g.NY * m->es; }
+static size_t field_bytes(const f2d_model_s* m, size_t es)
+{
+    return (size_t)m->g.P * m->g.NY * es;
+}
 
-static int add_field(f2d_model_s* m, const char* name, bool pp)
+static int add_field(f2d_model_s* m, const char* name, bool pp, int es)
 {
     Field f;
     f.pingpong = pp;
+    f.es = es;
     for (int k = 0; k < (pp ? 2 : 1); ++k) {
-        f.buf[k] = dalloc(m, field_bytes(m));
+        f.buf[k] = dalloc(m, field_bytes(m, es));
         if (!f.buf[k]) return fail(2, std::string("out of device memory for ") + name);
     }
     m->fields[name] = f;
@@ -135,6 +143,13 @@ static void* fb(f2d_model_s* m, const char* name, int parity = -1)
     return f.buf[parity < 0 ? m->cur : parity];
 }
 
+static int field_es(f2d_model_s* m, const char* name)
+{
+    auto it = m->fields.find(name);
+    return it == m->fields.end() ? 0 : it->second.es;
+}
+
+// TMA tile map of a stencil-state buffer (element size of the state)
 static int make_tmap(f2d_model_s* m, void* buf)
 {
     if (m->tmaps.count(buf)) return 0;
@@ -177,7 +192,7 @@ static int ensure_mg(f2d_model_s* m, int which)
                 return fail(4, "fluid vertex outside the interior (mask halo must be 0)");
     const double md = which == 0 ? 0.0 : m->maindiag;
     int e = mg_build(m->mg[which], nyn, nxn, g.P, 3 * g.P + 3, g.xper, hm.data(),
-                     m->d_gmask, m->pz, m->pr, m->cx, m->cy, md, m->prec);
+                     m->d_gmask, m->pz, m->prmg, m->cx, m->cy, md, m->prec);
     if (e) return fail(e, "multigrid setup failed");
     m->mg_ready[which] = true;
     return 0;
@@ -194,15 +209,16 @@ static int rec_solve(f2d_model_s* m, int which, const void* b, void* x, cudaStre
     v.z = m->pz;
     v.p = m->pp;
     v.q = m->pq;
+    v.rmg = m->prmg;
     v.partials = m->partials;
     const MGHost& mg = m->mg[which];
     const int nl = (int)mg.lev.size();
-    m->body_launches = 3 * 2 * mg.ltail + 1 + 4;
+    m->body_launches = 5 * mg.ltail + 1 + (mg.ltail > 0 ? 3 : 4);
     (void)nl;
     m->rec_launches += 2;
     CKI(pcg_record(m->mg[which], v, m->sc, m->p.poisson_tol, m->p.poisson_maxit, s, m->s2));
     if (m->g.xper) {
-        CKI(launch_fill_periodic(m->prec, x, m->g, s));
+        CKI(launch_fill_periodic(0, x, m->g, s));  // psi is FP64
         m->rec_launches += 1;
     }
     return 0;
@@ -213,22 +229,23 @@ static int rec_diag(f2d_model_s* m, int par, cudaStream_t s)
     const Geom& g = m->g;
     switch (m->p.model) {
     case F2D_MODEL_EULERPSI: {
-        CKI(launch_c2v(m->prec, fb(m, "omega", par), fb(m, "vomega"), m->d_code, nullptr, g, s));
+        CKI(launch_c2v(m->prec, 0, fb(m, "omega", par), fb(m, "vomega"), m->d_code, nullptr, g,
+                       s));
         m->rec_launches += 1;
         int e = rec_solve(m, 0, fb(m, "vomega"), fb(m, "psi"), s);
         if (e) return e;
-        CKI(launch_perpgrad(m->prec, fb(m, "psi"), fb(m, "U.x"), fb(m, "U.y"), m->d_code,
+        CKI(launch_perpgrad(0, m->prec, fb(m, "psi"), fb(m, "U.x"), fb(m, "U.y"), m->d_code,
                             m->rdy2, m->rdx2, 1, g, m->sc, m->partials, s));
         m->rec_launches += 1;
         return 0;
     }
     case F2D_MODEL_QG: {
         const void* fv = m->p.beta != 0 ? m->d_fv : nullptr;
-        CKI(launch_c2v(m->prec, fb(m, "pv", par), fb(m, "work"), m->d_code, fv, g, s));
+        CKI(launch_c2v(m->prec, 0, fb(m, "pv", par), fb(m, "work"), m->d_code, fv, g, s));
         m->rec_launches += 1;
         int e = rec_solve(m, 1, fb(m, "work"), fb(m, "psi"), s);
         if (e) return e;
-        CKI(launch_perpgrad(m->prec, fb(m, "psi"), fb(m, "U.x"), fb(m, "U.y"), m->d_code,
+        CKI(launch_perpgrad(0, m->prec, fb(m, "psi"), fb(m, "U.x"), fb(m, "U.y"), m->d_code,
                             m->rdy2, m->rdx2, 0, g, m->sc, m->partials, s));
         m->rec_launches += 1;
         return 0;
@@ -332,10 +349,35 @@ static int rec_step(f2d_model_s* m, int par, bool with_dt, cudaStream_t s)
     return 0;
 }
 
+// F2D_EAGER=1 runs every recorded sequence directly on the stream (the
+// Poisson loop then synchronises once per iteration): a profiling aid, since
+// kernel profilers do not list kernels inside conditional graph nodes.
+static bool eager_mode()
+{
+    static int v = -1;
+    if (v < 0) {
+        const char* e = getenv("F2D_EAGER");
+        v = (e && *e && *e != '0') ? 1 : 0;
+    }
+    return v == 1;
+}
+
 // capture kind (0 diag, 1 step, 2 run) for the current parity, then launch
 static int run_graph(f2d_model_s* m, int kind)
 {
     const int par = m->cur;
+    if (eager_mode()) {
+        if (m->p.model != F2D_MODEL_RSW) {
+            int e0 = ensure_mg(m, m->p.model == F2D_MODEL_EULERPSI ? 0 : 1);
+            if (e0) return e0;
+        }
+        m->rec_launches = 0;
+        int e = kind == 0 ? rec_diag(m, par, m->stream) : rec_step(m, par, kind == 2, m->stream);
+        if (e) return e;
+        m->launches[kind][par] = m->rec_launches;
+        if (kind != 0) m->cur = 1 - par;
+        return 0;
+    }
     if (!m->gx[kind][par]) {
         // multigrid set-up allocates, so it happens before the capture
         if (m->p.model != F2D_MODEL_RSW) {
@@ -543,21 +585,32 @@ int f2d_model_create(const f2d_params* p, const int8_t* msk, f2d_model* out)
               {"flx.y", false}, {"work", false}, {"psi", false}};
         prog = {"pv"};
     }
+    // the Poisson solution and right-hand side are FP64 in both forms; the
+    // stencil state has the model's precision
+    auto is64 = [](const char* n) {
+        return !strcmp(n, "psi") || !strcmp(n, "vomega") || !strcmp(n, "work");
+    };
     for (auto& f : fl)
-        if ((e = add_field(m, f.first, f.second))) return bail(e);
+        if ((e = add_field(m, f.first, f.second, is64(f.first) ? 8 : (int)m->es)))
+            return bail(e);
     for (int k = 1; k <= 2; ++k)
         for (const char* f : prog)
             if ((e = add_field(m, (std::string("ds") + std::to_string(k) + "." + f).c_str(),
-                               false)))
+                               false, (int)m->es)))
                 return bail(e);
     if (p->model != F2D_MODEL_RSW) {
-        m->pr = dalloc(m, field_bytes(m));
-        m->pz = dalloc(m, field_bytes(m));
-        m->pp = dalloc(m, field_bytes(m));
-        m->pq = dalloc(m, field_bytes(m));
-        m->d_fv = dalloc(m, field_bytes(m));
-        if (!m->pr || !m->pz || !m->pp || !m->pq || !m->d_fv)
+        m->pr = dalloc(m, field_bytes(m, 8));
+        m->pp = dalloc(m, field_bytes(m, 8));
+        m->pq = dalloc(m, field_bytes(m, 8));
+        m->pz = dalloc(m, field_bytes(m, m->es));
+        m->prmg = m->prec == 0 ? m->pr : dalloc(m, field_bytes(m, 4));
+        m->d_fv = dalloc(m, field_bytes(m, 8));
+        if (!m->pr || !m->pz || !m->pp || !m->pq || !m->d_fv || !m->prmg)
             return bail(fail(2, "out of device memory"));
+    }
+    if (m->prec != 0) {
+        m->stage64 = dalloc(m, field_bytes(m, 8));
+        if (!m->stage64) return bail(fail(2, "out of device memory"));
     }
     if ((e = setup_mesh(m, msk))) return bail(e);
     // time line (timeline.py:4-12) and set_dt constants (model.py:71-87)
@@ -620,13 +673,18 @@ static int field_io(f2d_model m, const char* name, double* host, bool set, bool 
     void* d = fb(m, name);
     if (!d) return fail(8, std::string("no field named ") + name);
     const Geom& g = m->g;
-    if (m->prec != 0) return fail(9, "float32 fields: not available in this build");
-    if (set)
-        CK(cudaMemcpy2DAsync(d, g.P * 8, host, g.NX * 8, g.NX * 8, g.NY,
+    const int es = field_es(m, name);
+    // FP32 fields go through the FP64 staging array and a conversion kernel
+    void* d64 = es == 8 ? d : m->stage64;
+    if (set) {
+        CK(cudaMemcpy2DAsync(d64, g.P * 8, host, g.NX * 8, g.NX * 8, g.NY,
                              cudaMemcpyHostToDevice, m->stream));
-    else
-        CK(cudaMemcpy2DAsync(host, g.NX * 8, d, g.P * 8, g.NX * 8, g.NY,
+        if (es == 4) CKI(launch_convert(0, 1, d64, d, g, m->stream));
+    } else {
+        if (es == 4) CKI(launch_convert(1, 0, d, d64, g, m->stream));
+        CK(cudaMemcpy2DAsync(host, g.NX * 8, d64, g.P * 8, g.NX * 8, g.NY,
                              cudaMemcpyDeviceToHost, m->stream));
+    }
     if (set && (!strcmp(name, "U.x") || !strcmp(name, "U.y")))
         CKI(launch_maxabs2(m->prec, fb(m, "U.x"), fb(m, "U.y"), g, m->sc, m->partials,
                            m->stream));
@@ -658,7 +716,7 @@ int f2d_field_device(f2d_model m, const char* name, void** ptr, int64_t* pitch, 
     if (!d) return fail(8, std::string("no field named ") + name);
     if (ptr) *ptr = d;
     if (pitch) *pitch = m->g.P;
-    if (es) *es = (int)m->es;
+    if (es) *es = field_es(m, name);
     return 0;
 }
 
@@ -766,11 +824,10 @@ int f2d_poisson_solve(f2d_model m, int which, const double* b, double* x, int* i
     if (!m->pr) return fail(8, "this model has no Poisson workspace");
     if (which == 1 && m->p.model == F2D_MODEL_EULERPSI)
         return fail(8, "the Helmholtz operator exists for qg/rsw models only");
-    if (m->prec != 0) return fail(9, "float32 solve: not available in this build");
     const Geom& g = m->g;
     if (!m->sb) {
-        m->sb = dalloc(m, field_bytes(m));
-        m->sx = dalloc(m, field_bytes(m));
+        m->sb = dalloc(m, field_bytes(m, 8));
+        m->sx = dalloc(m, field_bytes(m, 8));
         if (!m->sb || !m->sx) return fail(2, "out of device memory");
     }
     CK(cudaMemcpy2DAsync(m->sb, g.P * 8, b, g.NX * 8, g.NX * 8, g.NY, cudaMemcpyHostToDevice,

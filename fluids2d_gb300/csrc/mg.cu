@@ -88,7 +88,11 @@ __device__ __forceinline__ S fine_res(const MGLevel& F, int J, int I)
     return lb<S>(F)[k] - (apply_off<S>(F, x, J, I) + S(F.diag) * x[k]);
 }
 
-// coarse right-hand side = P^T (fine residual)
+// coarse right-hand side = P^T (fine residual). After the pre-smoothing
+// (red from a zero guess, then black) the residual of every black node is
+// zero, and the fine nodes of full weighting that are black are exactly the
+// four edge neighbours of (2J, 2I); only the centre and the four corners
+// (all red) contribute.
 template <typename S>
 __device__ __forceinline__ void op_restrict(const MGLevel& F, const MGLevel& C, int J,
                                             int I)
@@ -97,11 +101,9 @@ __device__ __forceinline__ void op_restrict(const MGLevel& F, const MGLevel& C, 
     S v = S(0);
     if (C.m[k]) {
         const int fj = 2 * J, fi = 2 * I;
-        const S e = fine_res<S>(F, fj, fi - 1) + fine_res<S>(F, fj, fi + 1) +
-                    fine_res<S>(F, fj - 1, fi) + fine_res<S>(F, fj + 1, fi);
-        const S c = fine_res<S>(F, fj - 1, fi - 1) + fine_res<S>(F, fj - 1, fi + 1) +
-                    fine_res<S>(F, fj + 1, fi - 1) + fine_res<S>(F, fj + 1, fi + 1);
-        v = fine_res<S>(F, fj, fi) + S(0.5) * e + S(0.25) * c;
+        const S c = (fine_res<S>(F, fj - 1, fi - 1) + fine_res<S>(F, fj - 1, fi + 1)) +
+                    (fine_res<S>(F, fj + 1, fi - 1) + fine_res<S>(F, fj + 1, fi + 1));
+        v = fine_res<S>(F, fj, fi) + S(0.25) * c;
     }
     lb<S>(C)[k] = v;
 }
@@ -146,6 +148,42 @@ __global__ void k_mg_smooth(MGLevel L, int color, int zero_init)
     if (J < L.nyn && I < L.nxn) op_smooth<S>(L, J, I, color, zero_init != 0);
 }
 
+// Pre-smoothing from a zero guess in one pass: red nodes x = b/diag, black
+// nodes one Gauss-Seidel update against those red values, which are
+// recomputed from b instead of read back (same result as two half sweeps).
+template <typename S>
+__device__ __forceinline__ S red_from_zero(const MGLevel& L, int J, int I)
+{
+    if (J < 0 || J >= L.nyn) return S(0);
+    if (I < 0 || I >= L.nxn) {
+        if (!L.per) return S(0);
+        I = I < 0 ? I + L.nxn : I - L.nxn;
+    }
+    const long long k = nidx(L, J, I);
+    return L.m[k] ? lb<S>(L)[k] * S(L.idiag) : S(0);
+}
+
+template <typename S>
+__global__ void k_mg_presmooth(MGLevel L)
+{
+    const int I = blockIdx.x * blockDim.x + threadIdx.x;
+    const int J = blockIdx.y * blockDim.y + threadIdx.y;
+    if (J >= L.nyn || I >= L.nxn) return;
+    const long long k = nidx(L, J, I);
+    S v = S(0);
+    if (L.m[k]) {
+        const S* b = lb<S>(L);
+        if (((J + I) & 1) == 0) {
+            v = b[k] * S(L.idiag);
+        } else {
+            const S off = S(L.cx) * (red_from_zero<S>(L, J, I - 1) + red_from_zero<S>(L, J, I + 1)) +
+                          S(L.cy) * (red_from_zero<S>(L, J - 1, I) + red_from_zero<S>(L, J + 1, I));
+            v = (b[k] - off) * S(L.idiag);
+        }
+    }
+    lx<S>(L)[k] = v;
+}
+
 template <typename S>
 __global__ void k_mg_restrict(MGLevel F, MGLevel C)
 {
@@ -175,16 +213,50 @@ template <typename S>
 __global__ void __launch_bounds__(1024) k_mg_tail(const MGLevel* __restrict__ lev,
                                                   int l0, int nl, int ksweeps)
 {
+    // All tail levels live in shared memory (dense nyn x nxn, x, b, mask);
+    // only b of level l0 comes from global memory and only x of level l0 goes
+    // back, so each phase costs a barrier, not a global-memory round trip.
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    __shared__ MGLevel sl[16];
+    if (threadIdx.x == 0) {
+        size_t off = 0;
+        for (int l = l0; l < nl; ++l) {
+            MGLevel D = lev[l];
+            const size_t n = (size_t)D.nyn * D.nxn;
+            D.pitch = D.nxn;
+            D.off = 0;
+            D.x = smem_raw + off;
+            off += (n * sizeof(S) + 15) / 16 * 16;
+            D.b = smem_raw + off;
+            off += (n * sizeof(S) + 15) / 16 * 16;
+            D.m = (const uint8_t*)(smem_raw + off);
+            off += (n + 15) / 16 * 16;
+            sl[l - l0] = D;
+        }
+    }
+    __syncthreads();
+    for (int l = l0; l < nl; ++l) {
+        const MGLevel& L = lev[l];
+        const MGLevel& D = sl[l - l0];
+        const int n = L.nyn * L.nxn;
+        for (int k = threadIdx.x; k < n; k += blockDim.x) {
+            const long long g = nidx(L, k / L.nxn, k % L.nxn);
+            ((uint8_t*)D.m)[k] = L.m[g];
+            if (l == l0) ((S*)D.b)[k] = ((const S*)L.b)[g];
+        }
+    }
+    __syncthreads();
+    const int nt = nl - l0;
     // down: pre-smooth (red from zero, black) and restrict
-    for (int l = l0; l < nl - 1; ++l) {
-        const MGLevel L = lev[l], C = lev[l + 1];
+    for (int q = 0; q < nt - 1; ++q) {
+        const MGLevel L = sl[q], C = sl[q + 1];
         block_for<S>(L, [&](int J, int I) { op_smooth<S>(L, J, I, 0, true); });
         block_for<S>(L, [&](int J, int I) { op_smooth<S>(L, J, I, 1, false); });
         block_for<S>(C, [&](int J, int I) { op_restrict<S>(L, C, J, I); });
     }
     // coarsest: (R,B)^k (B,R)^k from a zero guess (palindromic = symmetric)
     {
-        const MGLevel L = lev[nl - 1];
+        const MGLevel L = sl[nt - 1];
         block_for<S>(L, [&](int J, int I) { op_smooth<S>(L, J, I, 0, true); });
         block_for<S>(L, [&](int J, int I) { op_smooth<S>(L, J, I, 1, false); });
         for (int s = 1; s < ksweeps; ++s) {
@@ -197,26 +269,56 @@ __global__ void __launch_bounds__(1024) k_mg_tail(const MGLevel* __restrict__ le
         }
     }
     // up: prolongate, post-smooth (black, red)
-    for (int l = nl - 2; l >= l0; --l) {
-        const MGLevel L = lev[l], C = lev[l + 1];
+    for (int q = nt - 2; q >= 0; --q) {
+        const MGLevel L = sl[q], C = sl[q + 1];
         block_for<S>(L, [&](int J, int I) { op_prolong<S>(C, L, J, I); });
         block_for<S>(L, [&](int J, int I) { op_smooth<S>(L, J, I, 1, false); });
         block_for<S>(L, [&](int J, int I) { op_smooth<S>(L, J, I, 0, false); });
     }
+    // level l0's x back to global memory
+    {
+        const MGLevel G = lev[l0];
+        const MGLevel L = sl[0];
+        const int n = L.nyn * L.nxn;
+        for (int k = threadIdx.x; k < n; k += blockDim.x)
+            ((S*)G.x)[nidx(G, k / L.nxn, k % L.nxn)] = ((const S*)L.x)[k];
+    }
+}
+
+// shared-memory bytes of the tail levels l0..nl-1
+static size_t tail_smem(const std::vector<MGLevel>& lev, int l0, size_t es)
+{
+    size_t off = 0;
+    for (size_t l = l0; l < lev.size(); ++l) {
+        const size_t n = (size_t)lev[l].nyn * lev[l].nxn;
+        off += 2 * ((n * es + 15) / 16 * 16) + (n + 15) / 16 * 16;
+    }
+    return off;
 }
 
 // ---- PCG kernels on level 0 ----------------------------------------------
-template <typename S>
-__device__ __forceinline__ S applyA(const MGLevel& L, const S* __restrict__ x, int J,
-                                    int I, long long k)
+// The Krylov vectors x, r, p, q and all dot products are FP64. The V-cycle
+// (type S) works on its own level-0 copies: rmg = (S) r as its right-hand
+// side and zmg as its result. With S = float this is the mixed-precision
+// form: the FP64 residual recurrence refines the FP32-preconditioned
+// iterate to FP64 accuracy. With S = double, rmg aliases r.
+__device__ __forceinline__ double applyA64(const MGLevel& L, const double* __restrict__ x,
+                                           int J, int I, long long k)
 {
-    return apply_off<S>(L, x, J, I) + S(L.diag) * x[k];
+    return apply_off<double>(L, x, J, I) + L.diag * x[k];
+}
+
+template <typename S>
+__device__ __forceinline__ void store_rmg(S* rmg, const double* r, long long k, double v)
+{
+    if ((const void*)rmg != (const void*)r) rmg[k] = S(v);
 }
 
 // r = b - A x, reductions <b,b>, <r,r>
 template <typename S>
-__global__ void k_pcg_init(MGLevel L, const S* __restrict__ x, const S* __restrict__ b,
-                           S* __restrict__ r, DevScalars* sc, double* partials,
+__global__ void k_pcg_init(MGLevel L, const double* __restrict__ x,
+                           const double* __restrict__ b, double* r, S* rmg,
+                           DevScalars* sc, double* partials,
                            cudaGraphConditionalHandle cond)
 {
     const int I = blockIdx.x * blockDim.x + threadIdx.x;
@@ -224,14 +326,15 @@ __global__ void k_pcg_init(MGLevel L, const S* __restrict__ x, const S* __restri
     double v[2] = {0.0, 0.0};
     if (J < L.nyn && I < L.nxn) {
         const long long k = nidx(L, J, I);
-        S rv = S(0);
+        double rv = 0.0;
         if (L.m[k]) {
-            const S bv = b[k];
-            rv = bv - applyA<S>(L, x, J, I, k);
-            v[0] = (double)bv * (double)bv;
-            v[1] = (double)rv * (double)rv;
+            const double bv = b[k];
+            rv = bv - applyA64(L, x, J, I, k);
+            v[0] = bv * bv;
+            v[1] = rv * rv;
         }
         r[k] = rv;
+        store_rmg<S>(rmg, r, k, rv);
     }
     if (grid_reduce<2, false>(v, partials, &sc->counter[1])) {
         sc->bb = v[0];
@@ -247,7 +350,7 @@ __global__ void k_pcg_init(MGLevel L, const S* __restrict__ x, const S* __restri
 
 // rz = <r, z>; beta = rz/rz_old (0 on the first iteration)
 template <typename S>
-__global__ void k_pcg_rz(MGLevel L, const S* __restrict__ r, const S* __restrict__ z,
+__global__ void k_pcg_rz(MGLevel L, const double* __restrict__ r, const S* __restrict__ z,
                          DevScalars* sc, double* partials)
 {
     const int I = blockIdx.x * blockDim.x + threadIdx.x;
@@ -255,7 +358,35 @@ __global__ void k_pcg_rz(MGLevel L, const S* __restrict__ r, const S* __restrict
     double v[1] = {0.0};
     if (J < L.nyn && I < L.nxn) {
         const long long k = nidx(L, J, I);
-        if (L.m[k]) v[0] = (double)r[k] * (double)z[k];
+        if (L.m[k]) v[0] = r[k] * (double)z[k];
+    }
+    if (grid_reduce<1, false>(v, partials, &sc->counter[2])) {
+        sc->beta = sc->iter == 0 ? 0.0 : v[0] / sc->rz;
+        sc->rz = v[0];
+    }
+}
+
+// Last red half sweep of the V-cycle on level 0 fused with rz = <r, z>
+// (r the FP64 CG residual) and beta = rz / rz_old.
+template <typename S>
+__global__ void k_mg_red_dot(MGLevel L, const double* __restrict__ r64, DevScalars* sc,
+                             double* partials)
+{
+    const int I = blockIdx.x * blockDim.x + threadIdx.x;
+    const int J = blockIdx.y * blockDim.y + threadIdx.y;
+    double v[1] = {0.0};
+    if (J < L.nyn && I < L.nxn) {
+        const long long k = nidx(L, J, I);
+        if (L.m[k]) {
+            S* x = lx<S>(L);
+            const S* b = lb<S>(L);
+            S z = x[k];
+            if (((J + I) & 1) == 0) {
+                z = (b[k] - apply_off<S>(L, x, J, I)) * S(L.idiag);
+                x[k] = z;
+            }
+            v[0] = r64[k] * (double)z;
+        }
     }
     if (grid_reduce<1, false>(v, partials, &sc->counter[2])) {
         sc->beta = sc->iter == 0 ? 0.0 : v[0] / sc->rz;
@@ -265,20 +396,19 @@ __global__ void k_pcg_rz(MGLevel L, const S* __restrict__ r, const S* __restrict
 
 // p = z + beta p
 template <typename S>
-__global__ void k_pcg_p(MGLevel L, const S* __restrict__ z, S* __restrict__ p,
+__global__ void k_pcg_p(MGLevel L, const S* __restrict__ z, double* __restrict__ p,
                         const DevScalars* sc)
 {
     const int I = blockIdx.x * blockDim.x + threadIdx.x;
     const int J = blockIdx.y * blockDim.y + threadIdx.y;
     if (J >= L.nyn || I >= L.nxn) return;
     const long long k = nidx(L, J, I);
-    const S beta = S(sc->beta);
-    p[k] = L.m[k] ? z[k] + beta * p[k] : S(0);
+    const double beta = sc->beta;
+    p[k] = L.m[k] ? (double)z[k] + beta * p[k] : 0.0;
 }
 
 // q = A p, pq = <p, q>, alpha = rz / pq
-template <typename S>
-__global__ void k_pcg_spmv(MGLevel L, const S* __restrict__ p, S* __restrict__ q,
+__global__ void k_pcg_spmv(MGLevel L, const double* __restrict__ p, double* __restrict__ q,
                            DevScalars* sc, double* partials)
 {
     const int I = blockIdx.x * blockDim.x + threadIdx.x;
@@ -286,10 +416,10 @@ __global__ void k_pcg_spmv(MGLevel L, const S* __restrict__ p, S* __restrict__ q
     double v[1] = {0.0};
     if (J < L.nyn && I < L.nxn) {
         const long long k = nidx(L, J, I);
-        S qv = S(0);
+        double qv = 0.0;
         if (L.m[k]) {
-            qv = applyA<S>(L, p, J, I, k);
-            v[0] = (double)p[k] * (double)qv;
+            qv = applyA64(L, p, J, I, k);
+            v[0] = p[k] * qv;
         }
         q[k] = qv;
     }
@@ -301,8 +431,8 @@ __global__ void k_pcg_spmv(MGLevel L, const S* __restrict__ p, S* __restrict__ q
 
 // x += alpha p, r -= alpha q, rr = <r,r>, convergence test, loop condition
 template <typename S>
-__global__ void k_pcg_xr(MGLevel L, S* __restrict__ x, S* __restrict__ r,
-                         const S* __restrict__ p, const S* __restrict__ q,
+__global__ void k_pcg_xr(MGLevel L, double* __restrict__ x, double* r, S* rmg,
+                         const double* __restrict__ p, const double* __restrict__ q,
                          DevScalars* sc, double* partials,
                          cudaGraphConditionalHandle cond)
 {
@@ -314,14 +444,16 @@ __global__ void k_pcg_xr(MGLevel L, S* __restrict__ x, S* __restrict__ r,
         const long long k = nidx(L, J, I);
         if (L.m[k]) {
             if (zero) {
-                x[k] = S(0);
-                r[k] = S(0);
+                x[k] = 0.0;
+                r[k] = 0.0;
+                store_rmg<S>(rmg, r, k, 0.0);
             } else {
-                const S a = S(sc->alpha);
+                const double a = sc->alpha;
                 x[k] += a * p[k];
-                const S rv = r[k] - a * q[k];
+                const double rv = r[k] - a * q[k];
                 r[k] = rv;
-                v[0] = (double)rv * (double)rv;
+                store_rmg<S>(rmg, r, k, rv);
+                v[0] = rv * rv;
             }
         }
     }
@@ -351,23 +483,28 @@ __global__ void k_pcg_setup(DevScalars* sc, double tol2, int maxit)
 // ---- host side -------------------------------------------------------------
 static dim3 lvl_grid(const MGLevel& L) { return dim3((L.nxn + 31) / 32, (L.nyn + 7) / 8); }
 
+// One V-cycle on levels 0..nl-1. With r64, the final red half sweep of
+// level 0 also forms rz = <r, z> (needs ltail > 0).
 template <typename S>
-static int vcycle_record(MGHost& mg, cudaStream_t s)
+static int vcycle_record(MGHost& mg, cudaStream_t s, const double* r64, DevScalars* sc,
+                         double* partials)
 {
     const int nl = (int)mg.lev.size();
     const dim3 blk(32, 8);
     for (int l = 0; l < mg.ltail; ++l) {
         const MGLevel& L = mg.lev[l];
-        k_mg_smooth<S><<<lvl_grid(L), blk, 0, s>>>(L, 0, 1);
-        k_mg_smooth<S><<<lvl_grid(L), blk, 0, s>>>(L, 1, 0);
+        k_mg_presmooth<S><<<lvl_grid(L), blk, 0, s>>>(L);
         k_mg_restrict<S><<<lvl_grid(mg.lev[l + 1]), blk, 0, s>>>(L, mg.lev[l + 1]);
     }
-    k_mg_tail<S><<<1, 1024, 0, s>>>(mg.dlev, mg.ltail, nl, mg.ncoarse_sweeps);
+    k_mg_tail<S><<<1, 1024, mg.tail_smem, s>>>(mg.dlev, mg.ltail, nl, mg.ncoarse_sweeps);
     for (int l = mg.ltail - 1; l >= 0; --l) {
         const MGLevel& L = mg.lev[l];
         k_mg_prolong<S><<<lvl_grid(L), blk, 0, s>>>(mg.lev[l + 1], L);
         k_mg_smooth<S><<<lvl_grid(L), blk, 0, s>>>(L, 1, 0);
-        k_mg_smooth<S><<<lvl_grid(L), blk, 0, s>>>(L, 0, 0);
+        if (l == 0 && r64)
+            k_mg_red_dot<S><<<lvl_grid(L), blk, 0, s>>>(L, r64, sc, partials);
+        else
+            k_mg_smooth<S><<<lvl_grid(L), blk, 0, s>>>(L, 0, 0);
     }
     return (int)cudaGetLastError();
 }
@@ -378,13 +515,16 @@ static int body_record(MGHost& mg, const PCGVecs& v, DevScalars* sc,
 {
     const MGLevel& L = mg.lev[0];
     const dim3 g = lvl_grid(L), blk(32, 8);
-    int e = vcycle_record<S>(mg, s);
+    const bool fuse = mg.ltail > 0;
+    int e = vcycle_record<S>(mg, s, fuse ? (const double*)v.r : nullptr, sc, v.partials);
     if (e) return e;
-    k_pcg_rz<S><<<g, blk, 0, s>>>(L, (const S*)v.r, (const S*)v.z, sc, v.partials);
-    k_pcg_p<S><<<g, blk, 0, s>>>(L, (const S*)v.z, (S*)v.p, sc);
-    k_pcg_spmv<S><<<g, blk, 0, s>>>(L, (const S*)v.p, (S*)v.q, sc, v.partials);
-    k_pcg_xr<S><<<g, blk, 0, s>>>(L, (S*)v.x, (S*)v.r, (const S*)v.p, (const S*)v.q, sc,
-                                  v.partials, cond);
+    if (!fuse)
+        k_pcg_rz<S><<<g, blk, 0, s>>>(L, (const double*)v.r, (const S*)v.z, sc, v.partials);
+    k_pcg_p<S><<<g, blk, 0, s>>>(L, (const S*)v.z, (double*)v.p, sc);
+    k_pcg_spmv<<<g, blk, 0, s>>>(L, (const double*)v.p, (double*)v.q, sc, v.partials);
+    k_pcg_xr<S><<<g, blk, 0, s>>>(L, (double*)v.x, (double*)v.r, (S*)v.rmg,
+                                  (const double*)v.p, (const double*)v.q, sc, v.partials,
+                                  cond);
     return (int)cudaGetLastError();
 }
 
@@ -403,8 +543,8 @@ static int pcg_record_t(MGHost& mg, const PCGVecs& v, DevScalars* sc, double tol
     k_pcg_setup<<<1, 1, 0, s>>>(sc, tol * tol, maxit);
     if (st != cudaStreamCaptureStatusActive) {
         // host-driven loop (used outside graphs): one sync per iteration
-        k_pcg_init<S><<<g, blk, 0, s>>>(L, (const S*)v.x, (const S*)v.b, (S*)v.r, sc,
-                                         v.partials, 0);
+        k_pcg_init<S><<<g, blk, 0, s>>>(L, (const double*)v.x, (const double*)v.b,
+                                         (double*)v.r, (S*)v.rmg, sc, v.partials, 0);
         for (int it = 0; it < maxit + 1; ++it) {
             DevScalars h;
             if ((ce = cudaMemcpyAsync(&h, sc, sizeof(h), cudaMemcpyDeviceToHost, s)) != cudaSuccess)
@@ -420,8 +560,8 @@ static int pcg_record_t(MGHost& mg, const PCGVecs& v, DevScalars* sc, double tol
     cudaGraphConditionalHandle cond;
     ce = cudaGraphConditionalHandleCreate(&cond, graph, 1, cudaGraphCondAssignDefault);
     if (ce != cudaSuccess) return (int)ce;
-    k_pcg_init<S><<<g, blk, 0, s>>>(L, (const S*)v.x, (const S*)v.b, (S*)v.r, sc,
-                                     v.partials, cond);
+    k_pcg_init<S><<<g, blk, 0, s>>>(L, (const double*)v.x, (const double*)v.b, (double*)v.r,
+                                     (S*)v.rmg, sc, v.partials, cond);
     if ((ce = cudaGetLastError()) != cudaSuccess) return (int)ce;
     ce = cudaStreamGetCaptureInfo(s, &st, nullptr, &graph, &deps, nullptr, &ndeps);
     if (ce != cudaSuccess) return (int)ce;
@@ -539,14 +679,27 @@ int mg_build(MGHost& mg, int nyn0, int nxn0, long long pitch0, long long off0, i
         nyn = cyn;
         nxn = cxn;
     }
-    // first level small enough for the single-block tail
+    // first level from which all coarser levels fit in one block's shared
+    // memory (at most 160 KB; 16 levels). In FP64 the tail starts at <= 1100
+    // nodes: one SM's FP64 rate makes larger levels cheaper as grid kernels.
     const int nl = (int)mg.lev.size();
+    const size_t budget = 160 * 1024;
+    const long long max_first = prec == 0 ? 1100 : 4500;
     mg.ltail = nl - 1;
     for (int l = 0; l < nl; ++l)
-        if ((long long)mg.lev[l].nyn * mg.lev[l].nxn <= 1100) {
+        if (nl - l <= 16 && tail_smem(mg.lev, l, es) <= budget &&
+            (long long)mg.lev[l].nyn * mg.lev[l].nxn <= max_first) {
             mg.ltail = l;
             break;
         }
+    mg.tail_smem = tail_smem(mg.lev, mg.ltail, es);
+    if (mg.tail_smem > budget) return 3;  // coarsest level alone too large
+    cudaError_t fe = prec == 0
+        ? cudaFuncSetAttribute(k_mg_tail<double>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                               (int)mg.tail_smem)
+        : cudaFuncSetAttribute(k_mg_tail<float>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                               (int)mg.tail_smem);
+    if (fe != cudaSuccess) return 4;
     const MGLevel& last = mg.lev[nl - 1];
     mg.ncoarse_sweeps = std::max(2, std::min(32, std::max(last.nyn, last.nxn) / 2));
     if (cudaMalloc(&mg.dlev, sizeof(MGLevel) * nl) != cudaSuccess) return 2;

@@ -29,12 +29,16 @@ struct MGHost {
     MGLevel* dlev = nullptr;   // device copy of lev
     int ltail = 0;             // first level handled by the single-block tail
     int ncoarse_sweeps = 4;    // (R,B)^k (B,R)^k on the coarsest level
+    size_t tail_smem = 0;      // dynamic shared memory of the tail kernel
     int prec = 0;              // 0 = double, 1 = float
 };
 
-// PCG vectors on the model's vertex layout (level-0 geometry).
+// PCG vectors on the model's vertex layout (level-0 geometry). x, b, r, p, q
+// are FP64; z and rmg are the V-cycle's level-0 result and right-hand side in
+// the multigrid precision (rmg == r when that is FP64).
 struct PCGVecs {
     void *x, *r, *z, *p, *q;  // x is the solution array (psi)
+    void* rmg;
     const void* b;            // right-hand side array
     double* partials;         // >= 3 doubles per block of the level-0 grid
 };

@@ -213,12 +213,13 @@ k_rsw_stage(const __grid_constant__ CUtensorMap th,
     yface(ty, tx);
     if (t < TY) xface(t, TX);
     else if (t < TY + TX) yface(TY, t - TY);
-    __syncthreads();
 
+    // The vortex force needs no shared fluxes: it is evaluated before the
+    // barrier, so warps with fewer faces above do not idle at it.
     const int j = j0 + ty, i = i0 + tx;
-    if (j >= g.NY || i >= g.NX || !periodic_owner(g, i)) return;
+    const bool live = j < g.NY && i < g.NX && periodic_owner(g, i);
     const long long o = (long long)j * g.P + i;
-    const uint32_t cd = code[o];
+    const uint32_t cd = live ? code[o] : 0u;
     const T* __restrict__ ke = (const T*)a.ke;
     const T* __restrict__ p = (const T*)a.p;
 
@@ -247,6 +248,9 @@ k_rsw_stage(const __grid_constant__ CUtensorMap th,
             duy = -face_value<M, T>(L, Vm, w[0], w[1], w[2], w[3], w[4], w[5]) * Vm;
         }
     }
+    __syncthreads();
+    if (!live) return;
+
     // Coriolis (addcoriolis, operators.py:32-39)
     const T fc = T(a.fc);
     if (j <= g.NY - 2 && i >= 1 && i <= g.NX - 2)
@@ -360,8 +364,10 @@ k_rsw_diag(const __grid_constant__ CUtensorMap tux,
 
 // centerstovertices (operators.py:126-133) and, for qg with beta != 0, the
 // subtraction of the vertex Coriolis term (qg_inversion, operators.py:186-191)
-template <typename T>
-__global__ void k_c2v(const T* __restrict__ q, T* __restrict__ v,
+// (the average is formed in the output precision: FP64 right-hand side of
+// the Poisson solve from an FP32 state in the mixed-precision form)
+template <typename Tin, typename T>
+__global__ void k_c2v(const Tin* __restrict__ q, T* __restrict__ v,
                       const uint32_t* __restrict__ code, const T* __restrict__ fv,
                       Geom g)
 {
@@ -371,7 +377,7 @@ __global__ void k_c2v(const T* __restrict__ q, T* __restrict__ v,
     const long long o = (long long)j * g.P + i;
     T a = T(0);
     if (j >= 1 && i >= 1)
-        a = T(0.25) * (((q[o - g.P - 1] + q[o - 1]) + q[o - g.P]) + q[o]);
+        a = T(0.25) * (((T(q[o - g.P - 1]) + T(q[o - 1])) + T(q[o - g.P])) + T(q[o]));
     a *= (code[o] & B_MSKV) ? T(1) : T(0);
     if (fv) a -= fv[o];
     v[o] = a;
@@ -379,8 +385,8 @@ __global__ void k_c2v(const T* __restrict__ q, T* __restrict__ v,
 
 // perpgrad with contravariant scaling (operators.py:144-149), optional halo
 // fill of U (eulerpsi fills, qg does not), and max|U.x|, max|U.y| for set_dt.
-template <typename T>
-__global__ void k_perpgrad(const T* __restrict__ psi, T* __restrict__ Ux,
+template <typename P, typename T>
+__global__ void k_perpgrad(const P* __restrict__ psi, T* __restrict__ Ux,
                            T* __restrict__ Uy, const uint32_t* __restrict__ code,
                            double rdy2, double rdx2, int fillU, Geom g,
                            DevScalars* sc, double* partials)
@@ -393,11 +399,12 @@ __global__ void k_perpgrad(const T* __restrict__ psi, T* __restrict__ Ux,
         const bool own = !fillU || periodic_owner(g, i);
         if (own) {
             const uint32_t cd = code[o];
-            T ux = T(0), uy = T(0);
-            if (j <= g.NY - 2) ux = -(psi[o + g.P] - psi[o]) * ((cd & B_MSKX) ? T(1) : T(0));
-            if (i <= g.NX - 2) uy = (psi[o + 1] - psi[o]) * ((cd & B_MSKY) ? T(1) : T(0));
-            ux *= T(rdy2);
-            uy *= T(rdx2);
+            P px = P(0), py = P(0);
+            if (j <= g.NY - 2) px = -(psi[o + g.P] - psi[o]) * ((cd & B_MSKX) ? P(1) : P(0));
+            if (i <= g.NX - 2) py = (psi[o + 1] - psi[o]) * ((cd & B_MSKY) ? P(1) : P(0));
+            px *= P(rdy2);
+            py *= P(rdx2);
+            const T ux = T(px), uy = T(py);
             if (fillU) {
                 store_filled(Ux, g, j, i, ux);
                 store_filled(Uy, g, j, i, uy);
@@ -432,6 +439,17 @@ __global__ void k_maxabs2(const T* __restrict__ Ux, const T* __restrict__ Uy,
         sc->maxUx = m[0];
         sc->maxUy = m[1];
     }
+}
+
+// precision conversion between pitched arrays (field I/O of FP32 models)
+template <typename Tin, typename Tout>
+__global__ void k_convert(const Tin* __restrict__ in, Tout* __restrict__ out, Geom g)
+{
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    const int j = blockIdx.y * blockDim.y + threadIdx.y;
+    if (j >= g.NY || i >= g.NX) return;
+    const long long o = (long long)j * g.P + i;
+    out[o] = Tout(in[o]);
 }
 
 // periodic halo fill (meshes.py:135-143) of one array
@@ -535,30 +553,52 @@ int launch_rsw_diag(int method, int prec, const CUtensorMap* tux,
 
 static dim3 pt_grid(const Geom& g) { return dim3((g.NX + 31) / 32, (g.NY + 7) / 8); }
 
-int launch_c2v(int prec, const void* q, void* v, const uint32_t* code,
+int launch_c2v(int prec_in, int prec_out, const void* q, void* v, const uint32_t* code,
                const void* fv, const Geom& g, cudaStream_t s)
 {
-    if (prec == 0)
-        k_c2v<double><<<pt_grid(g), dim3(32, 8), 0, s>>>((const double*)q, (double*)v,
-                                                        code, (const double*)fv, g);
+    const dim3 gr = pt_grid(g), bl(32, 8);
+    if (prec_in == 0 && prec_out == 0)
+        k_c2v<double, double><<<gr, bl, 0, s>>>((const double*)q, (double*)v, code,
+                                                (const double*)fv, g);
+    else if (prec_in == 1 && prec_out == 0)
+        k_c2v<float, double><<<gr, bl, 0, s>>>((const float*)q, (double*)v, code,
+                                               (const double*)fv, g);
     else
-        k_c2v<float><<<pt_grid(g), dim3(32, 8), 0, s>>>((const float*)q, (float*)v,
-                                                       code, (const float*)fv, g);
+        k_c2v<float, float><<<gr, bl, 0, s>>>((const float*)q, (float*)v, code,
+                                              (const float*)fv, g);
     return (int)cudaGetLastError();
 }
 
-int launch_perpgrad(int prec, const void* psi, void* Ux, void* Uy,
+int launch_perpgrad(int prec_psi, int prec_U, const void* psi, void* Ux, void* Uy,
                     const uint32_t* code, double rdy2, double rdx2, int fillU,
                     const Geom& g, DevScalars* sc, double* partials, cudaStream_t s)
 {
-    if (prec == 0)
-        k_perpgrad<double><<<pt_grid(g), dim3(32, 8), 0, s>>>(
-            (const double*)psi, (double*)Ux, (double*)Uy, code, rdy2, rdx2, fillU, g,
-            sc, partials);
+    const dim3 gr = pt_grid(g), bl(32, 8);
+    if (prec_psi == 0 && prec_U == 0)
+        k_perpgrad<double, double><<<gr, bl, 0, s>>>((const double*)psi, (double*)Ux,
+                                                     (double*)Uy, code, rdy2, rdx2, fillU,
+                                                     g, sc, partials);
+    else if (prec_psi == 0 && prec_U == 1)
+        k_perpgrad<double, float><<<gr, bl, 0, s>>>((const double*)psi, (float*)Ux,
+                                                    (float*)Uy, code, rdy2, rdx2, fillU, g,
+                                                    sc, partials);
     else
-        k_perpgrad<float><<<pt_grid(g), dim3(32, 8), 0, s>>>(
-            (const float*)psi, (float*)Ux, (float*)Uy, code, rdy2, rdx2, fillU, g, sc,
-            partials);
+        k_perpgrad<float, float><<<gr, bl, 0, s>>>((const float*)psi, (float*)Ux,
+                                                   (float*)Uy, code, rdy2, rdx2, fillU, g,
+                                                   sc, partials);
+    return (int)cudaGetLastError();
+}
+
+int launch_convert(int prec_in, int prec_out, const void* in, void* out, const Geom& g,
+                   cudaStream_t s)
+{
+    const dim3 gr = pt_grid(g), bl(32, 8);
+    if (prec_in == 0 && prec_out == 1)
+        k_convert<double, float><<<gr, bl, 0, s>>>((const double*)in, (float*)out, g);
+    else if (prec_in == 1 && prec_out == 0)
+        k_convert<float, double><<<gr, bl, 0, s>>>((const float*)in, (double*)out, g);
+    else
+        return 1;
     return (int)cudaGetLastError();
 }
 

@@ -32,11 +32,13 @@ int launch_rsw_stage(int method, int prec, const CUtensorMap* th,
 int launch_rsw_diag(int method, int prec, const CUtensorMap* tux,
                     const CUtensorMap* tuy, const RswDiag& a, const uint32_t* code,
                     const Geom& g, DevScalars* sc, cudaStream_t s);
-int launch_c2v(int prec, const void* q, void* v, const uint32_t* code,
+int launch_c2v(int prec_in, int prec_out, const void* q, void* v, const uint32_t* code,
                const void* fv, const Geom& g, cudaStream_t s);
-int launch_perpgrad(int prec, const void* psi, void* Ux, void* Uy,
+int launch_perpgrad(int prec_psi, int prec_U, const void* psi, void* Ux, void* Uy,
                     const uint32_t* code, double rdy2, double rdx2, int fillU,
                     const Geom& g, DevScalars* sc, double* partials, cudaStream_t s);
+int launch_convert(int prec_in, int prec_out, const void* in, void* out, const Geom& g,
+                   cudaStream_t s);
 int launch_maxabs2(int prec, const void* Ux, const void* Uy, const Geom& g,
                    DevScalars* sc, double* partials, cudaStream_t s);
 int launch_fill_periodic(int prec, void* a, const Geom& g, cudaStream_t s);

@@ -53,6 +53,37 @@ __device__ __forceinline__ T weno5z(T qmm, T qm, T q0, T qp, T qpp)
     return ((w1 * qi1 + w2 * qi2) + w3 * qi3) / ((w1 + w2) + w3);
 }
 
+// FP64 form of weno5z with one division instead of four: the weights
+// w_k = g_k (1 + tau/d_k), d_k = beta_k + eps, are scaled by d1 d2 d3, so
+// W_k = g_k (d_k + tau) prod_{m != k} d_m and the reconstruction is
+// sum W_k qi_k / sum W_k - the same value up to rounding. With d_k >= 1e-16
+// the products stay far inside the double range (>= 1e-48). On GB300 the
+// double divisions dominate the FP64 instruction count of the stencil.
+template <>
+__device__ __forceinline__ double weno5z<double>(double qmm, double qm, double q0,
+                                                 double qp, double qpp)
+{
+    const double eps = WenoConst<double>::eps5;
+    const double c13 = 1. / 3., c76 = 7. / 6., c116 = 11. / 6.;
+    const double c16 = 1. / 6., c56 = 5. / 6.;
+    const double qi1 = (c13 * qmm - c76 * qm) + c116 * q0;
+    const double qi2 = (-c16 * qm + c56 * q0) + c13 * qp;
+    const double qi3 = (c13 * q0 + c56 * qp) - c16 * qpp;
+    const double k1 = 13. / 12., k2 = 0.25;
+    const double a1 = (qmm - 2. * qm) + q0, b1 = (qmm - 4. * qm) + 3. * q0;
+    const double a2 = (qm - 2. * q0) + qp, b2 = qm - qp;
+    const double a3 = (q0 - 2. * qp) + qpp, b3 = (3. * q0 - 4. * qp) + qpp;
+    const double beta1 = k1 * (a1 * a1) + k2 * (b1 * b1);
+    const double beta2 = k1 * (a2 * a2) + k2 * (b2 * b2);
+    const double beta3 = k1 * (a3 * a3) + k2 * (b3 * b3);
+    const double tau5 = fabs(beta1 - beta3);
+    const double d1 = beta1 + eps, d2 = beta2 + eps, d3 = beta3 + eps;
+    const double W1 = (0.1 * (d1 + tau5)) * (d2 * d3);
+    const double W2 = (0.6 * (d2 + tau5)) * (d1 * d3);
+    const double W3 = (0.3 * (d3 + tau5)) * (d1 * d2);
+    return ((W1 * qi1 + W2 * qi2) + W3 * qi3) / ((W1 + W2) + W3);
+}
+
 // weno3z (weno.py:75-100): WENO-Z, 3rd order.
 template <typename T>
 __device__ __forceinline__ T weno3z(T qm, T q0, T qp)
@@ -66,6 +97,22 @@ __device__ __forceinline__ T weno3z(T qm, T q0, T qp)
     T w1 = (T(1.) / T(3.)) * (T(1) + tau / (beta1 + eps));
     T w2 = (T(2.) / T(3.)) * (T(1) + tau / (beta2 + eps));
     return (w1 * qi1 + w2 * qi2) / (w1 + w2);
+}
+
+// FP64 form of weno3z with one division (see weno5z<double>); d_k >= 1e-14.
+template <>
+__device__ __forceinline__ double weno3z<double>(double qm, double q0, double qp)
+{
+    const double eps = WenoConst<double>::eps3;
+    const double qi1 = -0.5 * qm + 1.5 * q0;
+    const double qi2 = 0.5 * (q0 + qp);
+    const double e1 = q0 - qm, e2 = qp - q0;
+    const double beta1 = e1 * e1, beta2 = e2 * e2;
+    const double tau = fabs(beta2 - beta1);
+    const double d1 = beta1 + eps, d2 = beta2 + eps;
+    const double W1 = ((1. / 3.) * (d1 + tau)) * d2;
+    const double W2 = ((2. / 3.) * (d2 + tau)) * d1;
+    return (W1 * qi1 + W2 * qi2) / (W1 + W2);
 }
 
 // up3 / up5 (weno.py:36-43): linear upwind reconstructions.

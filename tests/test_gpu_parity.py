@@ -277,3 +277,57 @@ def test_poisson_maxit_reports_status():
     with pytest.raises(f2d.F2DError, match="max iterations"):
         m.sync()
     m.sync()  # status is cleared once reported
+
+
+# ------------------------------------------------ FP32 + FP64 refinement ----
+# Stencils, RK3 state and the multigrid cycle in FP32; the Poisson solution
+# refined to FP64 accuracy by the FP64 CG residual recurrence. The solve
+# itself must match SuperLU to the FP64 tolerance; model states match the
+# FP64 oracle within FP32 rounding accumulated over 5 steps: 2e-5 relative
+# L2 for eulerpsi and qg; 1e-4 for rsw, whose velocity is driven by the
+# gradient of p = g h / area ~ 1 with O(1e-3) anomalies, so FP32 rounding of
+# p (6e-8) is amplified by the cancellation in grad p.
+FP32_STATE_TOL = {"eulerpsi": 2e-5, "qg": 2e-5, "rsw": 1e-4}
+
+
+@pytest.mark.parametrize("case", ["islands", "periodic", "helmholtz"])
+def test_fp32_model_poisson_reaches_fp64_accuracy(case):
+    g = load("poisson.npz")
+    nx, ny, xper = (int(v) for v in g[case + "/params"])
+    helm = float(g[case + "/maindiag"]) != 0
+    m = _model("qg" if helm else "eulerpsi", nx, ny, g[case + "/msk"],
+               xperiodic=bool(xper), f0=float(g[case + "/f0"]), precision="fp32")
+    solver = m.mesh.qg_helmholtz if helm else m.mesh.poisson_vertices
+    x = g[case + "/x0"].copy()
+    solver.solve(g[case + "/b"], x)
+    assert rel_l2(x, g[case + "/x"]) <= SOLVE_TOL, rel_l2(x, g[case + "/x"])
+
+
+@pytest.mark.parametrize("kind", ["eulerpsi", "rsw", "qg"])
+def test_fp32_model_vs_fp64_oracle(kind):
+    if kind == "eulerpsi":
+        case = wl.eulerpsi_case(n=128, ny=96, seed=5, nislands=3)
+    elif kind == "rsw":
+        case = wl.rsw_case(n=128, ny=96, seed=6, nislands=3)
+    else:
+        case = wl.qg_case(n=128, ny=128, seed=7, nislands=4)
+    om = _oracle_like(case, kind)
+    kw = dict(xperiodic=case.get("xperiodic", False), Lx=case["Lx"], Ly=case["Ly"],
+              tend=1e300, maxite=10 ** 9, precision="fp32")
+    for k in ("f0", "g", "H", "beta"):
+        if k in case:
+            kw[k] = case[k]
+    m = _model(kind, case["nx"], case["ny"], case["msk"], **kw)
+    if "f" in case:
+        m.mesh.f = case["f"]
+    s = m.state
+    for k, v in case["fields"].items():
+        getattr(s, k)[:] = v
+    m.integrator.diag(s)
+    for _ in range(5):
+        om.run_steps(1)
+        m.advance(1)
+    m.sync()
+    worst = compare(m, lambda k: om.s.get(k), FP32_STATE_TOL[kind])
+    print(f"FP32 {kind} rel L2 after 5 steps:",
+          {k: f"{v:.2e}" for k, v in worst.items()})
