@@ -59,6 +59,15 @@ WORKLOADS = {
 L2_BYTES = 126 * 2 ** 20
 
 
+ENSEMBLE_DESC = ("ensemble of 256 eulerpsi closed basins, sizes uniform in "
+                 "{64,128,192,256,384,512}^2, 0-4 islands each, 8 Gaussian "
+                 "vortices, WENO5, SSP-RK3, per-member CFL 0.8")
+
+
+def is_ensemble(name):
+    return name.startswith("ensemble")
+
+
 def precision_of(name):
     return "fp32" if name.endswith("_fp32") else "fp64"
 
@@ -237,8 +246,57 @@ def cpu_oracle_rate(model, case, budget_s, max_steps=None, warmup=1):
     return cells * n / el, n, el, O.num_threads()
 
 
+def ensemble_cpu_rate(budget_s, max_members=None):
+    """Oracle port over the members of the ensemble workload in order, one
+    model step each, until the time budget is used."""
+    from fluids2d_gb300 import workloads as wl
+    members = wl.ensemble_case()
+    cells = 0
+    n = 0
+    el = 0.0
+    cores = 1
+    for c in members[: max_members or len(members)]:
+        from oracle import oracle as O
+        p = O.Param(model="eulerpsi", nx=c["nx"], ny=c["ny"], cfl=0.8, tend=1e300,
+                    maxite=10 ** 12)
+        om = O.Model(p, msk=c["msk"], pysq=False)
+        om.s["omega"][:] = c["fields"]["omega"]
+        om.diag()
+        t0 = time.perf_counter()
+        om.run_steps(1)
+        el += time.perf_counter() - t0
+        cells += c["nx"] * c["ny"]
+        n += 1
+        cores = O.num_threads()
+        if el >= budget_s:
+            break
+    return cells / el, n, el, cores
+
+
 def run_reference(args, rank, world):
     """--impl reference: the CPU implementation of the path on host cores."""
+    if is_ensemble(args.workload):
+        budget = float(os.environ.get("F2D_REF_BUDGET_S", "60"))
+        rate, n, el, cores = ensemble_cpu_rate(budget)
+        line = {
+            "metric": "cell-updates/s", "value": rate, "unit": "cell-updates/s",
+            "impl": "reference", "n_gpus": args.gpus, "steps": 1,
+            "warmup": 0, "ms_per_step": None, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+            "data": "synthetic",
+            "config": {"workload": args.workload, "desc": ENSEMBLE_DESC},
+            "cpu_baseline": {
+                "value": rate, "unit": "cell-updates/s", "cores": cores,
+                "kind": "port",
+                "sample": f"one model step of each of the first {n} members "
+                          f"(of 256) of {args.workload}, {el:.1f} s of stepping "
+                          f"on {cores} host threads (set-up and SuperLU "
+                          f"factorisation excluded)"},
+            "e2e": {"value": rate, "unit": "cell-updates/s",
+                    "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+        }
+        print(json.dumps(line), flush=True)
+        return
     model, case, desc = build_case(args.workload)
     budget = float(os.environ.get("F2D_REF_BUDGET_S", "60"))
     rate, n, el, cores = cpu_oracle_rate(model, case, budget,
@@ -263,7 +321,141 @@ def run_reference(args, rank, world):
     print(json.dumps(line), flush=True)
 
 
+def run_gpu_ensemble(args, rank, world):
+    import ctypes
+    import torch
+    import fluids2d_gb300 as f2d
+    from fluids2d_gb300 import workloads as wl
+    from fluids2d_gb300._lib import check, lib
+    dev = int(os.environ.get("LOCAL_RANK", "0"))
+    torch.cuda.set_device(dev)
+    prec = precision_of(args.workload)
+    members = wl.ensemble_case(seed=rank)
+    p = f2d.Param()
+    p.model = "eulerpsi"
+    p.cfl = 0.8
+    p.tend = 1e300
+    p.maxite = 10 ** 12
+    p.precision = prec
+    e = f2d.Ensemble(p, [(c["nx"], c["ny"]) for c in members],
+                     [c["msk"] for c in members])
+    stream = torch.cuda.Stream()
+    torch.cuda.set_stream(stream)
+    e.set_stream(stream.cuda_stream)
+    for b, c in enumerate(members):
+        e.set_field(b, "omega", c["fields"]["omega"])
+    e.diag()
+    L = lib()
+    h = e._h
+    cells = sum(c["nx"] * c["ny"] for c in members)
+    flush = torch.empty(2 * L2_BYTES // 4, dtype=torch.float32, device="cuda")
+    for _ in range(args.warmup):
+        check(L.f2d_ensemble_run(h, 1))
+    e.sync()
+    st0 = e.stats()
+    it0, loop0 = st0["poisson_iters"], st0["loop_iters"]
+    ev0 = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
+    ev1 = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
+    if world > 1:
+        import torch.distributed as dist
+        dist.barrier()
+    torch.cuda.synchronize()
+    with ClockSampler(dev) as clk:
+        for k in range(args.steps):
+            flush.zero_()
+            ev0[k].record(stream)
+            check(L.f2d_ensemble_run(h, 1))
+            ev1[k].record(stream)
+        torch.cuda.synchronize()
+    e.sync()
+    ms = sum(a.elapsed_time(b) for a, b in zip(ev0, ev1))
+    st = e.stats()
+    pcg_iters = st["poisson_iters"] - it0
+    loops = st["loop_iters"] - loop0
+    if world > 1:
+        import torch.distributed as dist
+        t = torch.tensor([ms], device="cuda", dtype=torch.float64)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        ms = float(t.item())
+    value = world * cells * args.steps / (ms / 1e3)
+    # end to end: every member's vorticity from pinned host memory and back
+    host = []
+    for b, c in enumerate(members):
+        t = torch.empty((c["ny"] + 6, c["nx"] + 6), dtype=torch.float64,
+                        pin_memory=True)
+        check(L.f2d_ensemble_field_get(h, b, b"omega", ctypes.c_void_p(t.data_ptr())))
+        host.append(t)
+    e2e_steps = max(1, min(args.steps, 20))
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    for _ in range(e2e_steps):
+        for b, t in enumerate(host):
+            check(L.f2d_ensemble_field_set_async(h, b, b"omega",
+                                                 ctypes.c_void_p(t.data_ptr())))
+        check(L.f2d_ensemble_run(h, 1))
+        for b, t in enumerate(host):
+            check(L.f2d_ensemble_field_get_async(h, b, b"omega",
+                                                 ctypes.c_void_p(t.data_ptr())))
+    e.sync()
+    e2e_s = time.perf_counter() - t0
+    io = sum((c["ny"] + 6) * (c["nx"] + 6) * 8 for c in members)
+    e2e = world * cells * e2e_steps / e2e_s
+    # roofline: the batched flux-form stage kernel of all members
+    avg = ctypes.c_double()
+    check(L.f2d_ensemble_time_stage(h, 2, 10, 1, ctypes.byref(avg)))
+    npts = sum((c["ny"] + 6) * (c["nx"] + 6) for c in members)
+    per = STAGE2_BYTES["eulerpsi"]
+    if prec == "fp32":
+        per = (per - 4) // 2 + 4
+    alg_bytes = per * npts
+    achieved = alg_bytes / (avg.value * 1e-3) / 1e9
+    try:
+        peak, peak_src = float(json.load(open(os.path.join(
+            ROOT, "MEASURED_PEAKS.json")))["hbm_gbs"]), "measured"
+    except Exception:
+        peak, peak_src = 6800.0, "fallback"
+    kname = "k_ens_fluxform_stage"
+    line = {
+        "metric": "cell-updates/s", "value": value, "unit": "cell-updates/s",
+        "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": ms / args.steps, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None,
+        "dtype": "f32" if prec == "fp32" else "f64", "data": "synthetic",
+        "config": {"workload": args.workload, "desc": ENSEMBLE_DESC,
+                   "members": len(members), "cells": cells,
+                   "precision": ("FP32 stencils + FP32 multigrid, FP64 CG "
+                                 "(solution at FP64 accuracy)" if prec == "fp32"
+                                 else "FP64 throughout"),
+                   "l2": "flushed between timed steps (256 MB write)",
+                   "parallelism": f"replicas x{world}"},
+        "e2e": {"value": e2e, "unit": "cell-updates/s",
+                "h2d_bytes_per_step": io, "d2h_bytes_per_step": io,
+                "steps": e2e_steps},
+        "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak,
+                     "unit": "GB/s", "frac": achieved / peak,
+                     "traffic": read_profile_traffic(f"{kname}_{args.workload}"),
+                     "kernel": kname, "kernel_ms": avg.value,
+                     "alg_bytes_per_launch": alg_bytes, "peak_source": peak_src},
+        "gpu_launches": st["launches_per_step"] * args.steps
+                        + st["launches_per_iter"] * loops,
+        "poisson_iters_sum_over_members": pcg_iters,
+        "cg_loop_iters": loops,
+        "clocks": clk.summary(),
+    }
+    if rank == 0 and not args.no_cpu_baseline:
+        budget = float(os.environ.get("F2D_CPU_BUDGET_S", "15"))
+        rate, n, el, cores = ensemble_cpu_rate(budget)
+        line["cpu_baseline"] = {
+            "value": rate, "unit": "cell-updates/s", "cores": cores, "kind": "port",
+            "sample": f"one model step of each of the first {n} members, "
+                      f"{el:.1f} s on {cores} host threads"}
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+
+
 def run_gpu(args, rank, world):
+    if is_ensemble(args.workload):
+        return run_gpu_ensemble(args, rank, world)
     import torch
     dev = int(os.environ.get("LOCAL_RANK", "0"))
     torch.cuda.set_device(dev)
@@ -404,7 +596,8 @@ def main():
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--workload", default="rsw512",
-                    choices=sorted(WORKLOADS) + sorted(k + "_fp32" for k in WORKLOADS))
+                    choices=sorted(WORKLOADS) + sorted(k + "_fp32" for k in WORKLOADS)
+                    + ["ensemble256", "ensemble256_fp32"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
     args = ap.parse_args()
     world = int(os.environ.get("WORLD_SIZE", "1"))

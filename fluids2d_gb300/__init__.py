@@ -8,4 +8,5 @@ CUDA kernels for sm_103a behind the C ABI of ``include/fluids2d_gb300.h``.
 from .param import Param  # noqa: F401
 from .model import Model  # noqa: F401
 from . import tools  # noqa: F401
+from .ensemble import Ensemble  # noqa: F401
 from ._lib import F2DError  # noqa: F401

@@ -83,6 +83,24 @@ _SIGS = {
     "f2d_sync": ([c_void_p], c_int),
     "f2d_time_stage": ([c_void_p, c_int, c_int, c_int, ctypes.POINTER(c_dbl)],
                        c_int),
+    "f2d_ensemble_create": ([ctypes.POINTER(Params), c_int, c_void_p, c_void_p,
+                             c_void_p, ctypes.POINTER(c_void_p)], c_int),
+    "f2d_ensemble_destroy": ([c_void_p], c_int),
+    "f2d_ensemble_set_stream": ([c_void_p, c_void_p], c_int),
+    "f2d_ensemble_field_set": ([c_void_p, c_int, ctypes.c_char_p, c_void_p], c_int),
+    "f2d_ensemble_field_get": ([c_void_p, c_int, ctypes.c_char_p, c_void_p], c_int),
+    "f2d_ensemble_field_set_async": ([c_void_p, c_int, ctypes.c_char_p, c_void_p],
+                                     c_int),
+    "f2d_ensemble_field_get_async": ([c_void_p, c_int, ctypes.c_char_p, c_void_p],
+                                     c_int),
+    "f2d_ensemble_diag": ([c_void_p], c_int),
+    "f2d_ensemble_run": ([c_void_p, c_int], c_int),
+    "f2d_ensemble_time_get": ([c_void_p, c_int, ctypes.POINTER(c_dbl),
+                               ctypes.POINTER(c_dbl), ctypes.POINTER(c_i64)], c_int),
+    "f2d_ensemble_sync": ([c_void_p], c_int),
+    "f2d_ensemble_stats": ([c_void_p] + [ctypes.POINTER(c_i64)] * 5, c_int),
+    "f2d_ensemble_time_stage": ([c_void_p, c_int, c_int, c_int,
+                                 ctypes.POINTER(c_dbl)], c_int),
     "f2d_cfl_dt_noalloc": ([c_void_p, c_void_p, c_i64, c_i64, c_i64, c_dbl,
                             c_dbl, c_void_p, c_void_p], c_int),
     "f2d_stats": ([c_void_p, ctypes.POINTER(c_i64), ctypes.POINTER(c_i64),

@@ -2,6 +2,7 @@
 // graphs, and the Poisson solve (include/fluids2d_gb300.h).
 #include <cudaTypedefs.h>
 
+#include <algorithm>
 #include <cmath>
 #include <cstdlib>
 #include <cstdio>
@@ -12,7 +13,7 @@
 
 #include "../../include/fluids2d_gb300.h"
 #include "mesh_host.h"
-#include "mg.cuh"
+#include "solver.cuh"
 #include "stage.cuh"
 
 namespace f2d {
@@ -92,8 +93,9 @@ struct f2d_model_s {
     bool cfl_dt = true;
     bool dt_applied = false;  // the constant dt of set_dt is in sc->dt
     // multigrid: [0] vertex Poisson, [1] Helmholtz
-    MGHost mg[2];
-    bool mg_ready[2] = {false, false};
+    BatchSolver bs[2];  // [0] vertex Poisson, [1] qg Helmholtz
+    bool bs_ready[2] = {false, false};
+    void* pe = nullptr;  // inner correction of the refinement form (FP32)
     void *pr = nullptr, *pz = nullptr, *pp = nullptr, *pq = nullptr;
     void* prmg = nullptr;  // V-cycle right-hand side (== pr in FP64)
     void* stage64 = nullptr;  // FP64 staging for field I/O of FP32 fields
@@ -175,9 +177,15 @@ static const CUtensorMap* tmap(f2d_model_s* m, void* buf) { return &m->tmaps[buf
 // ---------------------------------------------------------------------------
 // Recording of diag / stage / step on a stream (eager or under capture).
 // ---------------------------------------------------------------------------
+static double env_double(const char* name, double dflt)
+{
+    const char* v = getenv(name);
+    return (v && *v) ? atof(v) : dflt;
+}
+
 static int ensure_mg(f2d_model_s* m, int which)
 {
-    if (m->mg_ready[which]) return 0;
+    if (m->bs_ready[which]) return 0;
     const Geom& g = m->g;
     std::vector<uint8_t> hm((size_t)g.P * g.NY, 0);
     for (int j = 0; j < g.NY; ++j)
@@ -190,11 +198,35 @@ static int ensure_mg(f2d_model_s* m, int which)
             if (hm[(size_t)j * g.P + i] &&
                 (j < 3 || j >= 3 + nyn || i < 3 || i >= 3 + nxn))
                 return fail(4, "fluid vertex outside the interior (mask halo must be 0)");
-    const double md = which == 0 ? 0.0 : m->maindiag;
-    int e = mg_build(m->mg[which], nyn, nxn, g.P, 3 * g.P + 3, g.xper, hm.data(),
-                     m->d_gmask, m->pz, m->prmg, m->cx, m->cy, md, m->prec);
+    BSMemberDesc d;
+    d.nyn = nyn;
+    d.nxn = nxn;
+    d.pitch = g.P;
+    d.off0 = 3 * g.P + 3;
+    d.per = g.xper;
+    d.hmask = hm.data();
+    d.hoff0 = 3 * g.P + 3;
+    d.cx = m->cx;
+    d.cy = m->cy;
+    d.maindiag = which == 0 ? 0.0 : m->maindiag;
+    BSVecs v;
+    memset(&v, 0, sizeof(v));
+    v.r64 = m->pr;
+    v.p = m->pp;
+    v.q = m->pq;
+    v.z = m->pz;
+    v.rin = m->prmg;
+    v.e = m->pe;
+    BatchSolver& bs = m->bs[which];
+    int e = bs_build(bs, {d}, m->d_gmask, m->prec, v, m->sc);
     if (e) return fail(e, "multigrid setup failed");
-    m->mg_ready[which] = true;
+    bs.tol = m->p.poisson_tol;
+    bs.maxit = m->p.poisson_maxit;
+    bs.tol_in = env_double("F2D_TOL_IN", 1e-4);
+    bs.maxit_in = (int)env_double("F2D_MAXIT_IN", 30);
+    bs.maxouter = std::max(2, m->p.poisson_maxit / 10);
+    bs.nu = (int)env_double("F2D_NU", 1);
+    m->bs_ready[which] = true;
     return 0;
 }
 
@@ -202,21 +234,13 @@ static int rec_solve(f2d_model_s* m, int which, const void* b, void* x, cudaStre
 {
     int e = ensure_mg(m, which);
     if (e) return e;
-    PCGVecs v;
-    v.x = x;
-    v.b = b;
-    v.r = m->pr;
-    v.z = m->pz;
-    v.p = m->pp;
-    v.q = m->pq;
-    v.rmg = m->prmg;
-    v.partials = m->partials;
-    const MGHost& mg = m->mg[which];
-    const int nl = (int)mg.lev.size();
-    m->body_launches = 5 * mg.ltail + 1 + (mg.ltail > 0 ? 3 : 4);
-    (void)nl;
-    m->rec_launches += 2;
-    CKI(pcg_record(m->mg[which], v, m->sc, m->p.poisson_tol, m->p.poisson_maxit, s, m->s2));
+    BatchSolver& bs = m->bs[which];
+    bs.v.x64 = x;
+    bs.v.b64 = (void*)b;
+    int fixed = 0;
+    CKI(bs_record(bs, s, m->s2, &fixed));
+    m->rec_launches += fixed;
+    m->body_launches = bs.body_launches;
     if (m->g.xper) {
         CKI(launch_fill_periodic(0, x, m->g, s));  // psi is FP64
         m->rec_launches += 1;
@@ -434,8 +458,8 @@ static int setup_mesh(f2d_model_s* m, const int8_t* msk)
     CK(cudaMemcpy(m->d_code, code.data(), code.size() * 4, cudaMemcpyHostToDevice));
     CK(cudaMemcpy(m->d_gmask, gm.data(), gm.size(), cudaMemcpyHostToDevice));
     for (int w = 0; w < 2; ++w) {
-        mg_free(m->mg[w]);
-        m->mg_ready[w] = false;
+        bs_free(m->bs[w]);
+        m->bs_ready[w] = false;
     }
     drop_graphs(m);
     return 0;
@@ -604,8 +628,9 @@ int f2d_model_create(const f2d_params* p, const int8_t* msk, f2d_model* out)
         m->pq = dalloc(m, field_bytes(m, 8));
         m->pz = dalloc(m, field_bytes(m, m->es));
         m->prmg = m->prec == 0 ? m->pr : dalloc(m, field_bytes(m, 4));
+        m->pe = m->prec == 0 ? m->pr : dalloc(m, field_bytes(m, 4));
         m->d_fv = dalloc(m, field_bytes(m, 8));
-        if (!m->pr || !m->pz || !m->pp || !m->pq || !m->d_fv || !m->prmg)
+        if (!m->pr || !m->pz || !m->pp || !m->pq || !m->d_fv || !m->prmg || !m->pe)
             return bail(fail(2, "out of device memory"));
     }
     if (m->prec != 0) {
@@ -637,7 +662,7 @@ int f2d_model_destroy(f2d_model m)
     if (!m) return 0;
     if (m->stream) cudaStreamSynchronize(m->stream);
     drop_graphs(m);
-    for (int w = 0; w < 2; ++w) mg_free(m->mg[w]);
+    for (int w = 0; w < 2; ++w) bs_free(m->bs[w]);
     for (void* p : m->allocs) cudaFree(p);
     if (m->own_stream && m->stream) cudaStreamDestroy(m->stream);
     if (m->s2) cudaStreamDestroy(m->s2);
@@ -869,6 +894,16 @@ int f2d_sync(f2d_model m)
     CK(cudaStreamSynchronize(m->stream));
     int st = 0;
     CK(cudaMemcpy(&st, &m->sc->status, sizeof(int), cudaMemcpyDeviceToHost));
+    for (int w = 0; w < 2; ++w)
+        if (m->bs_ready[w]) {
+            BSGlobals bg;
+            CK(cudaMemcpy(&bg, m->bs[w].eg, sizeof(bg), cudaMemcpyDeviceToHost));
+            if (bg.status) {
+                st |= bg.status;
+                int zero = 0;
+                CK(cudaMemcpy(&m->bs[w].eg->status, &zero, sizeof(int), cudaMemcpyHostToDevice));
+            }
+        }
     if (st) {
         int zero = 0;
         CK(cudaMemcpy(&m->sc->status, &zero, sizeof(int), cudaMemcpyHostToDevice));

@@ -52,6 +52,12 @@ struct DevScalars {
     int iter, maxit, converged, pad1;
     long long total_iters;  // summed over solves, for diagnostics
     unsigned int counter[8];  // last-block reduction tickets
+    // iterative refinement: FP32 inner CG for the correction of the FP64 x
+    double rr0, tol_in2;      // inner start residual^2, (inner tolerance)^2
+    int iter_in, maxit_in;    // inner iterations of the current round
+    int outer, maxouter;      // refinement rounds of the current solve
+    int conv_in, zero;        // inner loop done; right-hand side is zero
+    long long total_outer;    // refinement rounds summed over solves
 };
 
 // ---------------------------------------------------------------------------
@@ -161,6 +167,39 @@ __device__ __forceinline__ void block_reduce(double (&v)[N], double* sh)
     }
 }
 
+// Per-thread part of the final sum over partials[t0 .. t0+n) (N values
+// each): thread `tid` of `nth` adds entries tid, tid+nth, ... with four
+// independent accumulators (loads in flight), combined in a fixed order.
+template <int N, bool MAX>
+__device__ __forceinline__ void final_sum(double (&acc)[N], const double* partials, int t0,
+                                          int n, int tid, int nth)
+{
+    double a[4][N];
+#pragma unroll
+    for (int u = 0; u < 4; ++u)
+#pragma unroll
+        for (int k = 0; k < N; ++k) a[u][k] = MAX ? -INFINITY : 0.0;
+    int i = tid;
+    for (; i + 3 * nth < n; i += 4 * nth)
+#pragma unroll
+        for (int u = 0; u < 4; ++u)
+#pragma unroll
+            for (int k = 0; k < N; ++k) {
+                const double p = __ldcg(&partials[(size_t)(t0 + i + u * nth) * N + k]);
+                a[u][k] = MAX ? fmax(a[u][k], p) : a[u][k] + p;
+            }
+    for (int u = 0; i < n; i += nth, ++u)
+#pragma unroll
+        for (int k = 0; k < N; ++k) {
+            const double p = __ldcg(&partials[(size_t)(t0 + i) * N + k]);
+            a[u & 3][k] = MAX ? fmax(a[u & 3][k], p) : a[u & 3][k] + p;
+        }
+#pragma unroll
+    for (int k = 0; k < N; ++k)
+        acc[k] = MAX ? fmax(fmax(a[0][k], a[1][k]), fmax(a[2][k], a[3][k]))
+                     : (a[0][k] + a[1][k]) + (a[2][k] + a[3][k]);
+}
+
 // Grid reduction of N values. Returns true in the single thread (thread 0
 // of the last block) that holds the grid result in `v`.
 template <int N, bool MAX>
@@ -185,19 +224,64 @@ __device__ __forceinline__ bool grid_reduce(double (&v)[N], double* partials,
     __threadfence();
     const int nt = blockDim.x * blockDim.y;
     double acc[N];
-#pragma unroll
-    for (int k = 0; k < N; ++k) acc[k] = MAX ? -INFINITY : 0.0;
-    for (unsigned i = tid; i < nb; i += nt)
-#pragma unroll
-        for (int k = 0; k < N; ++k) {
-            double p = __ldcg(&partials[(size_t)i * N + k]);
-            acc[k] = MAX ? fmax(acc[k], p) : acc[k] + p;
-        }
+    final_sum<N, MAX>(acc, partials, 0, (int)nb, tid, nt);
     block_reduce<N, MAX>(acc, sh);
     if (tid == 0) {
 #pragma unroll
         for (int k = 0; k < N; ++k) v[k] = acc[k];
         *ticket = 0;  // ready for the next launch
+        return true;
+    }
+    return false;
+}
+
+// Segmented reduction: the blocks t0 .. t0+nt-1 of a launch form one segment
+// (one member of a batch) with its own ticket; true in thread 0 of the last
+// block of the segment, which holds the segment's result in `v`.
+template <int N, bool MAX>
+__device__ __forceinline__ bool seg_reduce(double (&v)[N], double* partials, int tile,
+                                           int t0, int nt, unsigned int* ticket)
+{
+    __shared__ double sh[32 * N];
+    __shared__ int s_last;
+    block_reduce<N, MAX>(v, sh);
+    const int tid = threadIdx.y * blockDim.x + threadIdx.x;
+    if (tid == 0) {
+#pragma unroll
+        for (int k = 0; k < N; ++k) partials[(size_t)tile * N + k] = v[k];
+        __threadfence();
+        const unsigned prev = atomicAdd(ticket, 1u);
+        s_last = (prev == (unsigned)nt - 1);
+    }
+    __syncthreads();
+    if (!s_last) return false;
+    __threadfence();
+    double acc[N];
+    final_sum<N, MAX>(acc, partials, t0, nt, tid, blockDim.x * blockDim.y);
+    block_reduce<N, MAX>(acc, sh);
+    if (tid == 0) {
+#pragma unroll
+        for (int k = 0; k < N; ++k) v[k] = acc[k];
+        *ticket = 0;
+        return true;
+    }
+    return false;
+}
+
+// whole-grid ticket: true in thread 0 of the block that finishes last
+__device__ __forceinline__ bool last_block(unsigned int* ticket)
+{
+    __shared__ int s_last;
+    __syncthreads();
+    if (threadIdx.x == 0 && threadIdx.y == 0) {
+        __threadfence();
+        const unsigned n = gridDim.x * gridDim.y;
+        s_last = (atomicAdd(ticket, 1u) == n - 1);
+    }
+    __syncthreads();
+    if (threadIdx.x == 0 && threadIdx.y == 0 && s_last) {
+        __threadfence();
+        *ticket = 0;
         return true;
     }
     return false;

@@ -33,27 +33,10 @@ struct MGHost {
     int prec = 0;              // 0 = double, 1 = float
 };
 
-// PCG vectors on the model's vertex layout (level-0 geometry). x, b, r, p, q
-// are FP64; z and rmg are the V-cycle's level-0 result and right-hand side in
-// the multigrid precision (rmg == r when that is FP64).
-struct PCGVecs {
-    void *x, *r, *z, *p, *q;  // x is the solution array (psi)
-    void* rmg;
-    const void* b;            // right-hand side array
-    double* partials;         // >= 3 doubles per block of the level-0 grid
-};
-
 int mg_build(MGHost& mg, int nyn0, int nxn0, long long pitch0, long long off0,
-             int per, const uint8_t* hmask0 /* host, level-0 layout */,
+             int per, const uint8_t* hmask0 /* host, level-0 layout */, long long hoff0,
              const uint8_t* dmask0 /* device copy */, void* z0, void* r0,
              double cx, double cy, double maindiag, int prec);
 void mg_free(MGHost& mg);
-
-// Record the whole solve on `s` (eagerly or under stream capture): init,
-// a conditional WHILE node over the PCG iteration (body captured on `s2`),
-// and the periodic halo fill. `cond` is the WHILE node's handle when the
-// solve is recorded into a graph; with cond == 0 the loop is host-driven.
-int pcg_record(MGHost& mg, const PCGVecs& v, DevScalars* sc, double tol,
-               int maxit, cudaStream_t s, cudaStream_t s2);
 
 }  // namespace f2d

@@ -1,0 +1,78 @@
+// Batched multigrid-preconditioned solver for the masked vertex
+// Poisson/Helmholtz operator of one or many models (a single model is a
+// batch of one). See solver.cu.
+#pragma once
+#include <vector>
+
+#include "mg.cuh"
+
+namespace f2d {
+
+constexpr int BS_LMAX = 16;           // levels per member
+constexpr int BS_TW = 32, BS_TH = 32;  // node tile: 32 x 32 nodes, 32 x 8 threads
+
+struct BSInfo {
+    int nl, ltail, ksweeps;  // levels, first tail level, coarsest sweeps
+    int n0, nn;              // range of the member in the level-0 tile table
+    int pad[3];
+};
+
+struct BSGlobals {
+    unsigned int ticket[4];
+    int active_out, active_in;  // members still iterating (outer / inner)
+    int status, pad;
+    long long loops_out, loops_in;  // loop iterations (all members together)
+};
+
+// Arena base pointers; members are told apart by the offsets inside their
+// level-0 descriptors (node (J, I) of member b at off0_b + J*pitch_b + I).
+struct BSVecs {
+    void* x64;  // solution (FP64, the model's psi)
+    void* b64;  // right-hand side (FP64)
+    void* r64;  // FP64 residual
+    void* p;    // CG direction (FP64 form: double; refinement: float)
+    void* q;    // A p (same precision as p)
+    void* z;    // preconditioned residual, multigrid precision
+    void* rin;  // inner residual of the refinement form (float), multigrid rhs
+    void* e;    // inner correction of the refinement form (float)
+};
+
+struct BSMemberDesc {
+    int nyn, nxn;
+    long long pitch, off0;  // level-0 node layout inside the arenas
+    int per;
+    const uint8_t* hmask;   // host fluid mask, node (J,I) at hoff0 + J*pitch + I
+    long long hoff0;
+    double cx, cy, maindiag;
+};
+
+struct BatchSolver {
+    int n = 0;
+    int mode = 0;  // 0: FP64 multigrid-PCG; 1: FP32 inner PCG + FP64 refinement
+    std::vector<MGHost> mg;
+    MGLevel* dlevs = nullptr;
+    BSInfo* dinfo = nullptr;
+    BSGlobals* eg = nullptr;
+    DevScalars* scs = nullptr;  // one per member, owned by the caller
+    double* partials = nullptr;
+    std::vector<int4*> tiles;  // node tiles per level (members reaching it)
+    std::vector<int> ntiles;
+    int maxl = 0;
+    size_t tail_smem = 0;
+    BSVecs v;
+    double tol = 1e-12, tol_in = 1e-4;
+    int maxit = 200, maxit_in = 30, maxouter = 20;
+    int nu = 1;  // red-black sweeps before and after each coarse correction
+    int body_launches = 0;
+    std::vector<void*> owned;
+};
+
+int bs_build(BatchSolver& s, const std::vector<BSMemberDesc>& members,
+             const uint8_t* dmask, int mode, const BSVecs& v, DevScalars* scs);
+void bs_free(BatchSolver& s);
+// Record one solve of every member on `st`: eagerly (host-driven loops, a
+// profiling aid) or, under stream capture, as conditional WHILE nodes whose
+// bodies are captured on `st2`.
+int bs_record(BatchSolver& s, cudaStream_t st, cudaStream_t st2, int* launches);
+
+}  // namespace f2d

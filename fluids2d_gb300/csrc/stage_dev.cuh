@@ -1,0 +1,154 @@
+// Device pieces of the fused stage kernels shared by the single-model kernels
+// (stage.cu) and the batched ensemble kernels (ensemble.cu).
+#pragma once
+#include "common.cuh"
+#include "weno.cuh"
+
+namespace f2d {
+
+constexpr int TX = 32, TY = 8;           // cells per tile
+constexpr int SW = TX + 8, SH = TY + 6;  // staged tile: cols i0-4.., rows j0-3..
+constexpr int OX = 4, OY = 3;            // offset of cell (j0,i0) in the tile
+
+template <typename T>
+__device__ __forceinline__ T ldz(const T* __restrict__ a, int j, int i,
+                                 const Geom& g)
+{
+    return (j >= 0 && j < g.NY && i >= 0 && i < g.NX) ? a[(long long)j * g.P + i]
+                                                      : T(0);
+}
+
+// The RK3 increment of stage k (1, 2, 3) in the reference's evaluation order:
+// y += ((0 + c1*ds1) + c2*ds2) + c3*ds3 with (c) = (dt), (-3dt/4, dt/4),
+// (-dt/12, -dt/12, 2dt/3).
+template <typename T>
+__device__ __forceinline__ T rk3_increment(int stage, double dt, T d1, T d2, T d3)
+{
+    if (stage == 1) return T(dt) * d1;
+    if (stage == 2) return T(-3 * dt / 4) * d1 + T(dt / 4) * d2;
+    return (T(-dt / 12) * d1 + T(-dt / 12) * d2) + T(2 * dt / 3) * d3;
+}
+
+// Store v at (j,i) and, in an x-periodic domain, at its halo copy.
+// Returns false for points that belong to the halo copy of another thread.
+__device__ __forceinline__ bool periodic_owner(const Geom& g, int i)
+{
+    return !g.xper || (i >= 3 && i < g.nx + 3);
+}
+
+template <typename T>
+__device__ __forceinline__ void store_filled(T* __restrict__ a, const Geom& g,
+                                             int j, int i, T v)
+{
+    const long long r = (long long)j * g.P;
+    a[r + i] = v;
+    if (g.xper) {
+        if (i < 6) a[r + i + g.nx] = v;
+        else if (i >= g.nx) a[r + i - g.nx] = v;
+    }
+}
+
+// Issue the TMA loads of up to two (SH x SW) tiles and wait for them. All
+// threads wait on the barrier; returns false (uniformly) on timeout.
+template <typename T>
+__device__ __forceinline__ bool stage_tiles(T (*s0)[SW], const CUtensorMap* m0,
+                                            T (*s1)[SW], const CUtensorMap* m1,
+                                            int i0, int j0, uint64_t* bar,
+                                            int* status)
+{
+    const int t = threadIdx.y * blockDim.x + threadIdx.x;
+    if (t == 0) mbar_init(bar, 1);
+    __syncthreads();
+    if (t == 0) {
+        const uint32_t bytes = (uint32_t)(sizeof(T) * SW * SH * (s1 ? 2 : 1));
+        mbar_expect_tx(bar, bytes);
+        tma_load_2d(&s0[0][0], m0, i0 - OX, j0 - OY, bar);
+        if (s1) tma_load_2d(&s1[0][0], m1, i0 - OX, j0 - OY, bar);
+    }
+    bool ok = mbar_wait(bar, 0);
+    int all = __syncthreads_and(ok ? 1 : 0);
+    if (!all && t == 0) atomicOr(status, ST_TMA_TIMEOUT);
+    return all != 0;
+}
+
+// ---------------------------------------------------------------------------
+// Flux-form stage on one tile: dq = -div(U q) * msk (divflux/div,
+// operators.py:21-29, 104-107) for eulerpsi (q = omega) and qg (q = pv), then
+// the RK3 update. `tq` is the TMA map of qin (param or global memory).
+// Returns after the (uniform) TMA timeout check; all threads must call it.
+// ---------------------------------------------------------------------------
+template <typename T, int M>
+struct FluxformSmem {
+    alignas(128) T sq[SH][SW];
+    T sfx[TY][TX + 1];
+    T sfy[TY + 1][TX];
+    uint64_t bar;
+};
+
+template <typename T, int M>
+__device__ __forceinline__ void fluxform_tile(
+    FluxformSmem<T, M>& sm, const CUtensorMap* tq, const T* __restrict__ qin,
+    T* __restrict__ qout, const T* __restrict__ Ux, const T* __restrict__ Uy,
+    const uint32_t* __restrict__ code, T* __restrict__ ds_out, const T* __restrict__ ds1,
+    const T* __restrict__ ds2, int stage, const Geom& g, double dt, int* status, int i0,
+    int j0)
+{
+    auto& sq = sm.sq;
+    auto& sfx = sm.sfx;
+    auto& sfy = sm.sfy;
+    const int tx = threadIdx.x, ty = threadIdx.y, t = ty * TX + tx;
+    (void)qin;
+    if (!stage_tiles<T>(sq, tq, nullptr, nullptr, i0, j0, &sm.bar, status)) return;
+
+    // x-faces (TY x TX+1) and y-faces (TY+1 x TX): each evaluated once.
+    auto xface = [&](int r, int c) {
+        const int j = j0 + r, i = i0 + c;
+        T f = T(0);
+        if (j < g.NY && i < g.NX) {
+            const long long o = (long long)j * g.P + i;
+            const int L = lev(code[o], SH_OCX);
+            if (L) {
+                const T U = Ux[o];
+                const T* w = &sq[r + OY][c + OX - 3];
+                f = face_value<M, T>(L, U, w[0], w[1], w[2], w[3], w[4], w[5]) * U;
+            }
+        }
+        sfx[r][c] = f;
+    };
+    auto yface = [&](int r, int c) {
+        const int j = j0 + r, i = i0 + c;
+        T f = T(0);
+        if (j < g.NY && i < g.NX) {
+            const long long o = (long long)j * g.P + i;
+            const int L = lev(code[o], SH_OCY);
+            if (L) {
+                const T U = Uy[o];
+                const int cc = c + OX;
+                f = face_value<M, T>(L, U, sq[r][cc], sq[r + 1][cc], sq[r + 2][cc],
+                                     sq[r + 3][cc], sq[r + 4][cc], sq[r + 5][cc]) *
+                    U;
+            }
+        }
+        sfy[r][c] = f;
+    };
+    xface(ty, tx);
+    yface(ty, tx);
+    if (t < TY) xface(t, TX);
+    else if (t < TY + TX) yface(TY, t - TY);
+    __syncthreads();
+
+    const int j = j0 + ty, i = i0 + tx;
+    if (j >= g.NY || i >= g.NX || !periodic_owner(g, i)) return;
+    const long long o = (long long)j * g.P + i;
+    const T msk = (code[o] & B_MSK) ? T(1) : T(0);
+    const T ds = (-(sfx[ty][tx + 1] - sfx[ty][tx]) - (sfy[ty + 1][tx] - sfy[ty][tx])) * msk;
+    T inc;
+    if (stage == 1) inc = rk3_increment<T>(1, dt, ds, T(0), T(0));
+    else if (stage == 2) inc = rk3_increment<T>(2, dt, ds1[o], ds, T(0));
+    else inc = rk3_increment<T>(3, dt, ds1[o], ds2[o], ds);
+    const T q = sq[ty + OY][tx + OX];
+    store_filled(qout, g, j, i, q + inc);
+    if (ds_out) store_filled(ds_out, g, j, i, ds);
+}
+
+}  // namespace f2d

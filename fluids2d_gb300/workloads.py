@@ -178,3 +178,18 @@ def qg_case(n=4096, seed=0, nislands=20, ny=None, Lx=1.0, Ly=1.0,
     fv = beta * (yv - Ly / 2) * area
     return dict(model="qg", nx=nx, ny=ny, Lx=Lx, Ly=Ly, msk=msk, f0=f0,
                 beta=beta, g=g, H=H, fields={"pv": pv}, f=fv)
+
+
+def ensemble_case(count=256, seed=0, sizes=(64, 128, 192, 256, 384, 512),
+                  max_islands=4, nvortices=8, radius=0.05):
+    """Batched ensemble of closed-basin eulerpsi members: grid sizes drawn
+    uniformly from `sizes`, 0..max_islands islands each, Gaussian-vortex
+    initial vorticity as in eulerpsi_case."""
+    rng = np.random.default_rng(seed)
+    members = []
+    for b in range(count):
+        n = int(rng.choice(sizes))
+        k = int(rng.integers(0, max_islands + 1))
+        members.append(eulerpsi_case(n=n, seed=seed * 100003 + b, nislands=k,
+                                     nvortices=nvortices, radius=radius))
+    return members

@@ -158,6 +158,51 @@ int f2d_time_stage(f2d_model m, int stage, int reps, int flush_l2,
 int f2d_stats(f2d_model m, int64_t *poisson_iters,
               int64_t *launches_per_step, int64_t *launches_per_iter);
 
+/* ---- batched ensembles ------------------------------------------------- */
+
+/* No single counterpart in the reference: tools.run_twin_experiments
+ * (tools.py:29-49) steps two models in lockstep; an ensemble advances
+ * `count` independent eulerpsi or qg models with their own nx[b], ny[b] and
+ * masks msks[b] (NULL entries: default mask) together, one kernel launch
+ * per operation for all members, each member with its own CFL time step.
+ * The common parameters (model, Lx, Ly, f0, beta, cfl, precision, Poisson
+ * tolerance...) come from p; p->dt must be 0. */
+typedef struct f2d_ensemble_s *f2d_ensemble;
+int f2d_ensemble_create(const f2d_params *p, int count, const int *nx,
+                        const int *ny, const int8_t *const *msks,
+                        f2d_ensemble *out);
+int f2d_ensemble_destroy(f2d_ensemble e);
+int f2d_ensemble_set_stream(f2d_ensemble e, void *stream);
+/* Fields of member b by the reference's names ("omega" or "pv", "psi",
+ * "vomega" or "work", "U.x", "U.y"; "f" sets the qg vertex Coriolis term);
+ * (ny[b]+6, nx[b]+6) float64 host arrays. */
+int f2d_ensemble_field_set(f2d_ensemble e, int member, const char *name,
+                           const double *host);
+int f2d_ensemble_field_get(f2d_ensemble e, int member, const char *name,
+                           double *host);
+int f2d_ensemble_field_set_async(f2d_ensemble e, int member, const char *name,
+                                 const double *host);
+int f2d_ensemble_field_get_async(f2d_ensemble e, int member, const char *name,
+                                 double *host);
+/* integrator.diag of every member (equations.py:80-84, 99-101) */
+int f2d_ensemble_diag(f2d_ensemble e);
+/* n iterations of set_dt + step(1) for every member (model.py:45-51) */
+int f2d_ensemble_run(f2d_ensemble e, int nsteps);
+int f2d_ensemble_time_get(f2d_ensemble e, int member, double *t, double *dt,
+                          int64_t *ite);
+int f2d_ensemble_sync(f2d_ensemble e);
+/* interior cells of all members, Poisson iterations summed over members,
+ * iterations of the batched CG loop (each runs the body once for all
+ * members still iterating), kernels per step outside the Poisson loops,
+ * kernels per loop iteration (instrumentation) */
+int f2d_ensemble_stats(f2d_ensemble e, int64_t *cells, int64_t *poisson_iters,
+                       int64_t *loop_iters, int64_t *launches_per_step,
+                       int64_t *launches_per_iter);
+/* f2d_time_stage for the batched stage kernel of all members (measurement
+ * hook of the benchmark; no reference counterpart). */
+int f2d_ensemble_time_stage(f2d_ensemble e, int stage, int reps, int flush_l2,
+                            double *avg_ms);
+
 /* ---- allocation-free entry point ---------------------------------------- */
 
 /* No counterpart in the reference. For callers that must not allocate

@@ -331,3 +331,66 @@ def test_fp32_model_vs_fp64_oracle(kind):
     worst = compare(m, lambda k: om.s.get(k), FP32_STATE_TOL[kind])
     print(f"FP32 {kind} rel L2 after 5 steps:",
           {k: f"{v:.2e}" for k, v in worst.items()})
+
+
+# ------------------------------------------------------------ ensembles ----
+def _ensemble(members, precision="fp64", kind="eulerpsi"):
+    p = f2d.Param()
+    p.model = kind
+    p.cfl = 0.8
+    p.tend = 1e300
+    p.maxite = 10 ** 9
+    p.precision = precision
+    if kind == "qg":
+        p.f0, p.beta = members[0]["f0"], members[0]["beta"]
+    e = f2d.Ensemble(p, [(c["nx"], c["ny"]) for c in members],
+                     [c["msk"] for c in members])
+    for b, c in enumerate(members):
+        for k, v in c["fields"].items():
+            e.set_field(b, k, v)
+        if "f" in c:
+            e.set_field(b, "f", c["f"])
+    e.diag()
+    return e
+
+
+@pytest.mark.parametrize("precision", ["fp64", "fp32"])
+def test_ensemble_members_match_single_models(precision):
+    """Every member equals the same case run alone (same kernels, same
+    per-member reductions), to the FP64 step tolerance."""
+    members = [wl.eulerpsi_case(n=64, ny=48, seed=11, nislands=2),
+               wl.eulerpsi_case(n=96, ny=96, seed=12, nislands=0),
+               wl.eulerpsi_case(n=40, ny=72, seed=13, nislands=3)]
+    e = _ensemble(members, precision)
+    e.run(4)
+    e.sync()
+    for b, c in enumerate(members):
+        m = _model("eulerpsi", c["nx"], c["ny"], c["msk"], cfl=0.8, tend=1e300,
+                   maxite=10 ** 9, precision=precision)
+        m.state.omega[:] = c["fields"]["omega"]
+        m.integrator.diag(m.state)
+        m.advance(4)
+        m.sync()
+        for k in ("omega", "psi", "U.x", "U.y"):
+            a = e.get_field(b, k)
+            r = getattr(m.state, k.split(".")[0])
+            r = getattr(r, k.split(".")[1]) if "." in k else r
+            assert rel_l2(a, r) <= STEP_TOL, (b, k, rel_l2(a, r))
+        t, dt, ite = e.time(b)
+        assert ite == 4 and abs(t - m.time.t) <= 1e-12 * t
+
+
+def test_ensemble_vs_oracle():
+    members = [wl.eulerpsi_case(n=48, ny=40, seed=21, nislands=2),
+               wl.eulerpsi_case(n=72, ny=64, seed=22, nislands=1)]
+    e = _ensemble(members, "fp64")
+    e.run(3)
+    e.sync()
+    for b, c in enumerate(members):
+        om = _oracle_like(c, "eulerpsi")
+        om.p.cfl = 0.8
+        om.dt = 0.01
+        om.diag()
+        om.run_steps(3)
+        for k in ("omega", "psi"):
+            assert rel_l2(e.get_field(b, k), om.s[k]) <= STEP_TOL
