@@ -2,10 +2,18 @@
 
 Metric: cell-updates/s = nx*ny*steps / time (the inverse of the reference's
 own s/dof printout, model.py:89-93). A benchmark step is one model time step
-(SSP-RK3: three fused stage kernels plus their diagnostics) over the whole
-grid. Default workload: the rotating-shallow-water channel, 512x512,
-x-periodic, 3 islands, f=g=H=1, FP64, WENO5, SSP-RK3 (seeded synthetic
-inputs of that configuration's shapes; no dataset is involved).
+(SSP-RK3: three fused stage kernels plus their diagnostics, including the
+Poisson solves) over the whole grid of every model of the workload.
+
+Default workload (the configuration the headline metric is quoted on): a
+batched ensemble of 256 eulerpsi closed basins with sizes drawn from
+{64,128,192,256,384,512}^2 and 0-4 islands each, Gaussian-vortex initial
+conditions, WENO5, SSP-RK3, per-member CFL, in the FP32 + FP64-refinement
+form; the same run times the plain FP64 form on the same members and reports
+the speed-up and the relative L2 difference of the vorticity between the two
+forms. Other workloads: rsw512 (rotating shallow water channel), eulerpsi256,
+qg1024/qg4096, each also with a _fp32 suffix. Inputs are seeded synthetic
+fields of those configurations' shapes; no dataset is involved.
 
   python bench.py [--gpus N] [--steps K] [--warmup W] [--impl gb300|reference]
                   [--workload rsw512|eulerpsi256|qg4096|...]
@@ -321,16 +329,8 @@ def run_reference(args, rank, world):
     print(json.dumps(line), flush=True)
 
 
-def run_gpu_ensemble(args, rank, world):
-    import ctypes
-    import torch
+def _ensemble_make(prec, members, stream):
     import fluids2d_gb300 as f2d
-    from fluids2d_gb300 import workloads as wl
-    from fluids2d_gb300._lib import check, lib
-    dev = int(os.environ.get("LOCAL_RANK", "0"))
-    torch.cuda.set_device(dev)
-    prec = precision_of(args.workload)
-    members = wl.ensemble_case(seed=rank)
     p = f2d.Param()
     p.model = "eulerpsi"
     p.cfl = 0.8
@@ -339,45 +339,85 @@ def run_gpu_ensemble(args, rank, world):
     p.precision = prec
     e = f2d.Ensemble(p, [(c["nx"], c["ny"]) for c in members],
                      [c["msk"] for c in members])
-    stream = torch.cuda.Stream()
-    torch.cuda.set_stream(stream)
     e.set_stream(stream.cuda_stream)
     for b, c in enumerate(members):
         e.set_field(b, "omega", c["fields"]["omega"])
     e.diag()
+    return e
+
+
+def _ensemble_time(e, steps, warmup, stream, flush, dev, world):
+    import torch
+    from fluids2d_gb300._lib import check, lib
     L = lib()
-    h = e._h
-    cells = sum(c["nx"] * c["ny"] for c in members)
-    flush = torch.empty(2 * L2_BYTES // 4, dtype=torch.float32, device="cuda")
-    for _ in range(args.warmup):
-        check(L.f2d_ensemble_run(h, 1))
+    for _ in range(warmup):
+        check(L.f2d_ensemble_run(e._h, 1))
     e.sync()
     st0 = e.stats()
-    it0, loop0 = st0["poisson_iters"], st0["loop_iters"]
-    ev0 = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
-    ev1 = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
+    ev0 = [torch.cuda.Event(enable_timing=True) for _ in range(steps)]
+    ev1 = [torch.cuda.Event(enable_timing=True) for _ in range(steps)]
     if world > 1:
         import torch.distributed as dist
         dist.barrier()
     torch.cuda.synchronize()
     with ClockSampler(dev) as clk:
-        for k in range(args.steps):
+        for k in range(steps):
             flush.zero_()
             ev0[k].record(stream)
-            check(L.f2d_ensemble_run(h, 1))
+            check(L.f2d_ensemble_run(e._h, 1))
             ev1[k].record(stream)
         torch.cuda.synchronize()
     e.sync()
     ms = sum(a.elapsed_time(b) for a, b in zip(ev0, ev1))
     st = e.stats()
-    pcg_iters = st["poisson_iters"] - it0
-    loops = st["loop_iters"] - loop0
     if world > 1:
         import torch.distributed as dist
         t = torch.tensor([ms], device="cuda", dtype=torch.float64)
         dist.all_reduce(t, op=dist.ReduceOp.MAX)
         ms = float(t.item())
+    return ms, st0, st, clk.summary()
+
+
+def run_gpu_ensemble(args, rank, world):
+    import ctypes
+    import torch
+    from fluids2d_gb300 import workloads as wl
+    from fluids2d_gb300._lib import check, lib
+    dev = int(os.environ.get("LOCAL_RANK", "0"))
+    torch.cuda.set_device(dev)
+    prec = precision_of(args.workload)
+    members = wl.ensemble_case(seed=rank)
+    stream = torch.cuda.Stream()
+    torch.cuda.set_stream(stream)
+    e = _ensemble_make(prec, members, stream)
+    L = lib()
+    h = e._h
+    cells = sum(c["nx"] * c["ny"] for c in members)
+    flush = torch.empty(2 * L2_BYTES // 4, dtype=torch.float32, device="cuda")
+    ms, st0, st, clocks = _ensemble_time(e, args.steps, args.warmup, stream, flush,
+                                         dev, world)
+    pcg_iters = st["poisson_iters"] - st0["poisson_iters"]
+    loops = st["loop_iters"] - st0["loop_iters"]
     value = world * cells * args.steps / (ms / 1e3)
+    # the plain FP64 form on the same members and step count, for the
+    # speed-up and the difference between the forms
+    fp64_form = None
+    if prec == "fp32" and not args.no_fp64_form:
+        e64 = _ensemble_make("fp64", members, stream)
+        ms64, _, _, _ = _ensemble_time(e64, args.steps, args.warmup, stream, flush,
+                                       dev, world)
+        num = den = 0.0
+        for b in range(len(members)):
+            a32 = e.get_field(b, "omega")
+            a64 = e64.get_field(b, "omega")
+            num += float(np.sum((a32 - a64) ** 2))
+            den += float(np.sum(a64 ** 2))
+        fp64_form = {"value": world * cells * args.steps / (ms64 / 1e3),
+                     "ms_per_step": ms64 / args.steps,
+                     "speedup_fp32_refine_vs_fp64": ms64 / ms,
+                     "omega_rel_l2_fp32_vs_fp64": (num / den) ** 0.5,
+                     "steps": args.warmup + args.steps}
+        del e64
     # end to end: every member's vorticity from pinned host memory and back
     host = []
     for b, c in enumerate(members):
@@ -423,8 +463,9 @@ def run_gpu_ensemble(args, rank, world):
         "dtype": "f32" if prec == "fp32" else "f64", "data": "synthetic",
         "config": {"workload": args.workload, "desc": ENSEMBLE_DESC,
                    "members": len(members), "cells": cells,
-                   "precision": ("FP32 stencils + FP32 multigrid, FP64 CG "
-                                 "(solution at FP64 accuracy)" if prec == "fp32"
+                   "precision": ("FP32 stencils + FP32 multigrid inner CG, FP64 "
+                                 "iterative refinement (Poisson solution at FP64 "
+                                 "accuracy, tol 1e-12)" if prec == "fp32"
                                  else "FP64 throughout"),
                    "l2": "flushed between timed steps (256 MB write)",
                    "parallelism": f"replicas x{world}"},
@@ -440,8 +481,10 @@ def run_gpu_ensemble(args, rank, world):
                         + st["launches_per_iter"] * loops,
         "poisson_iters_sum_over_members": pcg_iters,
         "cg_loop_iters": loops,
-        "clocks": clk.summary(),
+        "clocks": clocks,
     }
+    if fp64_form:
+        line["fp64_form"] = fp64_form
     if rank == 0 and not args.no_cpu_baseline:
         budget = float(os.environ.get("F2D_CPU_BUDGET_S", "15"))
         rate, n, el, cores = ensemble_cpu_rate(budget)
@@ -592,13 +635,15 @@ def run_gpu(args, rank, world):
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=200)
+    ap.add_argument("--steps", type=int, default=100)
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
-    ap.add_argument("--workload", default="rsw512",
+    ap.add_argument("--workload", default="ensemble256_fp32",
                     choices=sorted(WORKLOADS) + sorted(k + "_fp32" for k in WORKLOADS)
                     + ["ensemble256", "ensemble256_fp32"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-fp64-form", action="store_true",
+                    help="ensemble FP32 workload: skip the plain-FP64 comparison")
     args = ap.parse_args()
     world = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))

@@ -6,6 +6,8 @@
 #include <cuda_runtime.h>
 #include <stdint.h>
 
+#include <type_traits>
+
 namespace f2d {
 
 // ---------------------------------------------------------------------------
@@ -58,6 +60,11 @@ struct DevScalars {
     int outer, maxouter;      // refinement rounds of the current solve
     int conv_in, zero;        // inner loop done; right-hand side is zero
     long long total_outer;    // refinement rounds summed over solves
+    // SSP-RK3 increment coefficients of the current step (integrators.py:
+    // 92-107): dt; -3dt/4, dt/4; -dt/12, -dt/12, 2dt/3 - in FP64 and FP32,
+    // computed once per step so the stage kernels do no FP64 arithmetic
+    double rk[6];
+    float rkf[6];
 };
 
 // ---------------------------------------------------------------------------
@@ -202,13 +209,13 @@ __device__ __forceinline__ void final_sum(double (&acc)[N], const double* partia
 
 // Grid reduction of N values. Returns true in the single thread (thread 0
 // of the last block) that holds the grid result in `v`.
-template <int N, bool MAX>
+template <int N, bool MAX, bool PRE = false>
 __device__ __forceinline__ bool grid_reduce(double (&v)[N], double* partials,
                                             unsigned int* ticket)
 {
     __shared__ double sh[32 * N];
     __shared__ int s_last;
-    block_reduce<N, MAX>(v, sh);
+    if (!PRE) block_reduce<N, MAX>(v, sh);
     const int tid = threadIdx.y * blockDim.x + threadIdx.x;
     const unsigned nb = gridDim.x * gridDim.y;
     const unsigned b = blockIdx.y * gridDim.x + blockIdx.x;
@@ -238,13 +245,13 @@ __device__ __forceinline__ bool grid_reduce(double (&v)[N], double* partials,
 // Segmented reduction: the blocks t0 .. t0+nt-1 of a launch form one segment
 // (one member of a batch) with its own ticket; true in thread 0 of the last
 // block of the segment, which holds the segment's result in `v`.
-template <int N, bool MAX>
+template <int N, bool MAX, bool PRE = false>
 __device__ __forceinline__ bool seg_reduce(double (&v)[N], double* partials, int tile,
                                            int t0, int nt, unsigned int* ticket)
 {
     __shared__ double sh[32 * N];
     __shared__ int s_last;
-    block_reduce<N, MAX>(v, sh);
+    if (!PRE) block_reduce<N, MAX>(v, sh);
     const int tid = threadIdx.y * blockDim.x + threadIdx.x;
     if (tid == 0) {
 #pragma unroll
@@ -266,6 +273,108 @@ __device__ __forceinline__ bool seg_reduce(double (&v)[N], double* partials, int
         return true;
     }
     return false;
+}
+
+// Two-level segmented reduction: the tiles n0 .. n0+nn-1 of one segment are
+// grouped by 64; the last tile of a group sums the group's partials, the last
+// group of the segment sums the group sums. Same-address atomics stay at <= 64
+// per ticket whatever the segment size; the summation order is fixed.
+constexpr int RED_GROUP = 64;
+
+template <int N, bool PRE = false>
+__device__ __forceinline__ bool seg_reduce2(double (&v)[N], double* tpart, double* gpart,
+                                            unsigned int* gtick, int tile, int n0, int nn,
+                                            int g0, unsigned int* ticket)
+{
+    __shared__ double sh[32 * N];
+    __shared__ int s_last;
+    if (!PRE) block_reduce<N, false>(v, sh);  // PRE: v already the block total in thread 0
+    const int tid = threadIdx.y * blockDim.x + threadIdx.x;
+    const int nth = blockDim.x * blockDim.y;
+    const int lt = tile - n0, g = lt / RED_GROUP;
+    const int gbeg = g * RED_GROUP, gsz = min(RED_GROUP, nn - gbeg);
+    const int ng = (nn + RED_GROUP - 1) / RED_GROUP;
+    if (tid == 0) {
+#pragma unroll
+        for (int k = 0; k < N; ++k) tpart[(size_t)tile * N + k] = v[k];
+        __threadfence();
+        s_last = (atomicAdd(&gtick[g0 + g], 1u) == (unsigned)gsz - 1);
+    }
+    __syncthreads();
+    if (!s_last) return false;
+    __threadfence();
+    double acc[N];
+#pragma unroll
+    for (int k = 0; k < N; ++k)
+        acc[k] = tid < gsz ? __ldcg(&tpart[(size_t)(n0 + gbeg + tid) * N + k]) : 0.0;
+    (void)nth;
+    block_reduce<N, false>(acc, sh);
+    if (tid == 0) {
+#pragma unroll
+        for (int k = 0; k < N; ++k) gpart[(size_t)(g0 + g) * N + k] = acc[k];
+        gtick[g0 + g] = 0;
+        __threadfence();
+        s_last = (atomicAdd(ticket, 1u) == (unsigned)ng - 1);
+    }
+    __syncthreads();
+    if (!s_last) return false;
+    __threadfence();
+    final_sum<N, false>(acc, gpart, g0, ng, tid, nth);
+    block_reduce<N, false>(acc, sh);
+    if (tid == 0) {
+#pragma unroll
+        for (int k = 0; k < N; ++k) v[k] = acc[k];
+        *ticket = 0;
+        return true;
+    }
+    return false;
+}
+
+// Block total of per-thread FP32 values: warp sums in FP32 (shuffles), the
+// warp sums combined in FP64 by thread 0 in a fixed order. Result in thread 0.
+template <int N, bool MAX = false>
+__device__ __forceinline__ void block_total_f(const float (&a)[N], double (&out)[N])
+{
+    __shared__ float shf[32 * N];
+    float v[N];
+#pragma unroll
+    for (int k = 0; k < N; ++k) {
+        v[k] = a[k];
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) {
+            const float u = __shfl_xor_sync(0xffffffffu, v[k], o);
+            v[k] = MAX ? fmaxf(v[k], u) : v[k] + u;
+        }
+    }
+    const int tid = threadIdx.y * blockDim.x + threadIdx.x;
+    const int w = tid >> 5, lane = tid & 31, nw = (blockDim.x * blockDim.y + 31) >> 5;
+    __syncthreads();
+    if (lane == 0)
+#pragma unroll
+        for (int k = 0; k < N; ++k) shf[w * N + k] = v[k];
+    __syncthreads();
+    if (tid == 0)
+#pragma unroll
+        for (int k = 0; k < N; ++k) {
+            double t = MAX ? -INFINITY : 0.0;
+            for (int i = 0; i < nw; ++i)
+                t = MAX ? fmax(t, (double)shf[i * N + k]) : t + (double)shf[i * N + k];
+            out[k] = t;
+        }
+}
+
+// Block-level value of per-thread partials for the grid/segment reductions
+// below: FP32 partials via block_total_f (result in thread 0), FP64 ones
+// unchanged (the reduction's own FP64 block stage runs).
+template <int N, bool MAX, typename T>
+__device__ __forceinline__ void block_pre(const T (&a)[N], double (&out)[N])
+{
+    if constexpr (std::is_same<T, float>::value) {
+        block_total_f<N, MAX>(a, out);
+    } else {
+#pragma unroll
+        for (int k = 0; k < N; ++k) out[k] = a[k];
+    }
 }
 
 // whole-grid ticket: true in thread 0 of the block that finishes last

@@ -30,13 +30,12 @@ int f2d_internal_fail(int code, const char* msg);
 
 namespace f2d {
 
-constexpr int ENS_LMAX = 16;
-
-struct alignas(64) Member {
-    CUtensorMap tq[2];  // TMA maps of the two prognostic buffers (64B aligned)
+struct Member {
+    CUtensorMap tq[2];  // TMA maps of the two prognostic buffers (aligned as CUtensorMap)
     Geom g;
     long long off;      // element offset of the member in every arena
     double rdx2, rdy2;  // 1/dx**2, 1/dy**2
+    float frdx2, frdy2;  // the same in FP32
     int t0, nt;         // range in the cell-tile table
     int n0, nn;         // range in the level-0 node-tile table
     int nl, ltail, ksweeps;
@@ -46,6 +45,17 @@ struct alignas(64) Member {
 struct EnsGlobals {
     int status;  // TMA time-outs of the stage kernels
     int pad;
+};
+
+// 1/dx**2, 1/dy**2 of a member in precision T (no conversion in the kernel)
+template <typename T> struct Rd;
+template <> struct Rd<double> {
+    static __device__ __forceinline__ double x(const Member& m) { return m.rdx2; }
+    static __device__ __forceinline__ double y(const Member& m) { return m.rdy2; }
+};
+template <> struct Rd<float> {
+    static __device__ __forceinline__ float x(const Member& m) { return m.frdx2; }
+    static __device__ __forceinline__ float y(const Member& m) { return m.frdy2; }
 };
 
 template <typename T>
@@ -88,11 +98,10 @@ __global__ void k_ens_c2v(const int4* __restrict__ tiles, const Member* __restri
     if (j >= g.NY || i >= g.NX) return;
     const long long o = (long long)j * g.P + i;
     const Tin* q = at<Tin>(a.q[par], mb.off);
-    double v = 0.0;
-    if (j >= 1 && i >= 1)
-        v = 0.25 * ((((double)q[o - g.P - 1] + (double)q[o - 1]) + (double)q[o - g.P]) +
-                    (double)q[o]);
-    v *= (a.code[mb.off + o] & B_MSKV) ? 1.0 : 0.0;
+    Tin s = Tin(0);  // the average in the precision of the state
+    if (j >= 1 && i >= 1 && (a.code[mb.off + o] & B_MSKV))
+        s = Tin(0.25) * (((q[o - g.P - 1] + q[o - 1]) + q[o - g.P]) + q[o]);
+    double v = s;
     if (use_fv) v -= at<double>(a.fv, mb.off)[o];
     at<double>(a.rhs, mb.off)[o] = v;
 }
@@ -106,19 +115,19 @@ __global__ void k_ens_perpgrad(const int4* __restrict__ tiles, const Member* __r
     const Member& mb = mem[tl.x];
     const Geom g = mb.g;
     const int i = tl.y + threadIdx.x, j = tl.z + threadIdx.y;
-    double m[2] = {0.0, 0.0};
+    T m[2] = {T(0), T(0)};
     if (j < g.NY && i < g.NX) {
         const long long o = (long long)j * g.P + i;
         const bool own = !fillU || periodic_owner(g, i);
         if (own) {
+            // FP64 difference, scaling in the precision of U
             const double* psi = at<double>(a.psi, mb.off);
             const uint32_t cd = a.code[mb.off + o];
-            double px = 0.0, py = 0.0;
-            if (j <= g.NY - 2) px = -(psi[o + g.P] - psi[o]) * ((cd & B_MSKX) ? 1.0 : 0.0);
-            if (i <= g.NX - 2) py = (psi[o + 1] - psi[o]) * ((cd & B_MSKY) ? 1.0 : 0.0);
-            px *= mb.rdy2;
-            py *= mb.rdx2;
-            const T ux = T(px), uy = T(py);
+            T ux = T(0), uy = T(0);
+            if (j <= g.NY - 2 && (cd & B_MSKX))
+                ux = -T(psi[o + g.P] - psi[o]) * Rd<T>::y(mb);
+            if (i <= g.NX - 2 && (cd & B_MSKY))
+                uy = T(psi[o + 1] - psi[o]) * Rd<T>::x(mb);
             T* Ux = at<T>(a.Ux, mb.off);
             T* Uy = at<T>(a.Uy, mb.off);
             if (fillU) {
@@ -128,14 +137,17 @@ __global__ void k_ens_perpgrad(const int4* __restrict__ tiles, const Member* __r
                 Ux[o] = ux;
                 Uy[o] = uy;
             }
-            m[0] = fabs((double)ux);
-            m[1] = fabs((double)uy);
+            m[0] = fabs(ux);
+            m[1] = fabs(uy);
         }
     }
     DevScalars& sc = scs[tl.x];
-    if (seg_reduce<2, true>(m, partials, blockIdx.x, mb.t0, mb.nt, &sc.counter[0])) {
-        sc.maxUx = m[0];
-        sc.maxUy = m[1];
+    double w[2];
+    block_pre<2, true>(m, w);
+    if (seg_reduce<2, true, std::is_same<T, float>::value>(w, partials, blockIdx.x, mb.t0,
+                                                           mb.nt, &sc.counter[0])) {
+        sc.maxUx = w[0];
+        sc.maxUy = w[1];
     }
 }
 
@@ -409,6 +421,8 @@ int f2d_ensemble_create(const f2d_params* p, int count, const int* nxs, const in
         const double dx = q.Lx / q.nx, dy = q.Ly / q.ny;
         mb.rdx2 = 1 / pow(dx, 2.0);
         mb.rdy2 = 1 / pow(dy, 2.0);
+        mb.frdx2 = (float)mb.rdx2;
+        mb.frdy2 = (float)mb.rdy2;
         off += ((size_t)g.P * g.NY + 31) / 32 * 32;
     }
     e->total = off;

@@ -54,6 +54,10 @@ int mg_build(MGHost& mg, int nyn0, int nxn0, long long pitch0, long long off0, i
     L0.cy = cy;
     L0.diag = -2 * (cx + cy) - maindiag;
     L0.idiag = 1.0 / L0.diag;
+    L0.fcx = (float)L0.cx;
+    L0.fcy = (float)L0.cy;
+    L0.fdiag = (float)L0.diag;
+    L0.fidiag = (float)L0.idiag;
     mg.lev.push_back(L0);
 
     // host masks of each level, dense nyn x nxn
@@ -95,6 +99,10 @@ int mg_build(MGHost& mg, int nyn0, int nxn0, long long pitch0, long long off0, i
         C.cy = cy;
         C.diag = -2 * (cx + cy) - md;
         C.idiag = 1.0 / C.diag;
+        C.fcx = (float)C.cx;
+        C.fcy = (float)C.cy;
+        C.fdiag = (float)C.diag;
+        C.fidiag = (float)C.idiag;
         const size_t n = (size_t)C.pitch * cyn;
         void *x, *b, *m;
         if (cudaMalloc(&x, n * es) != cudaSuccess) return 2;
@@ -118,11 +126,11 @@ int mg_build(MGHost& mg, int nyn0, int nxn0, long long pitch0, long long off0, i
         nxn = cxn;
     }
     // first level from which all coarser levels fit in one block's shared
-    // memory (at most 160 KB; 16 levels). In FP64 the tail starts at <= 1100
-    // nodes: one SM's FP64 rate makes larger levels cheaper as grid kernels.
+    // memory (at most 160 KB; 16 levels), starting at <= 1100 nodes: the tail
+    // runs on one SM, so larger levels are cheaper as grid kernels.
     const int nl = (int)mg.lev.size();
     const size_t budget = 160 * 1024;
-    const long long max_first = prec == 0 ? 1100 : 4500;
+    const long long max_first = 1100;
     mg.ltail = nl - 1;
     for (int l = 0; l < nl; ++l)
         if (nl - l <= 16 && tail_smem(mg.lev, l, es) <= budget &&

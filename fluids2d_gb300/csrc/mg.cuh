@@ -21,6 +21,7 @@ struct MGLevel {
     int pad;
     double cx, cy;      // east-west and north-south couplings (dy/dx, dx/dy)
     double diag, idiag; // -2(cx+cy) - maindiag and its inverse
+    float fcx, fcy, fdiag, fidiag;  // the same in FP32 (no conversions in FP32 kernels)
 };
 
 struct MGHost {

@@ -9,31 +9,52 @@ __device__ __forceinline__ S* lx(const MGLevel& L) { return (S*)L.x; }
 template <typename S>
 __device__ __forceinline__ S* lb(const MGLevel& L) { return (S*)L.b; }
 
+// operator coefficients in the working precision
+template <typename S> struct Coef;
+template <> struct Coef<double> {
+    static __device__ __forceinline__ double cx(const MGLevel& L) { return L.cx; }
+    static __device__ __forceinline__ double cy(const MGLevel& L) { return L.cy; }
+    static __device__ __forceinline__ double diag(const MGLevel& L) { return L.diag; }
+    static __device__ __forceinline__ double idiag(const MGLevel& L) { return L.idiag; }
+};
+template <> struct Coef<float> {
+    static __device__ __forceinline__ float cx(const MGLevel& L) { return L.fcx; }
+    static __device__ __forceinline__ float cy(const MGLevel& L) { return L.fcy; }
+    static __device__ __forceinline__ float diag(const MGLevel& L) { return L.fdiag; }
+    static __device__ __forceinline__ float idiag(const MGLevel& L) { return L.fidiag; }
+};
+
 __device__ __forceinline__ long long nidx(const MGLevel& L, int J, int I)
 {
     return L.off + (long long)J * L.pitch + I;
 }
 
-// value of a neighbour node, 0 outside the level or at non-fluid nodes
+// value of a neighbour node, 0 outside the level or at non-fluid nodes. The
+// index is clamped into the level and both loads are issued unconditionally
+// (then selected), so the four neighbour loads of a stencil can be in flight
+// together; non-fluid values are never used, whatever they hold.
 template <typename S>
 __device__ __forceinline__ S nbv(const MGLevel& L, const S* __restrict__ x, int J,
                                  int I)
 {
-    if (J < 0 || J >= L.nyn) return S(0);
+    bool ok = (unsigned)J < (unsigned)L.nyn;
     if (I < 0 || I >= L.nxn) {
-        if (!L.per) return S(0);
-        I = I < 0 ? I + L.nxn : I - L.nxn;
+        if (L.per) I = I < 0 ? I + L.nxn : I - L.nxn;
+        else ok = false;
     }
-    const long long k = nidx(L, J, I);
-    return L.m[k] ? x[k] : S(0);
+    const int Jc = min(max(J, 0), L.nyn - 1), Ic = min(max(I, 0), L.nxn - 1);
+    const long long k = nidx(L, Jc, Ic);
+    const S v = x[k];
+    const uint8_t m = L.m[k];
+    return (ok && m) ? v : S(0);
 }
 
 template <typename S>
 __device__ __forceinline__ S apply_off(const MGLevel& L, const S* __restrict__ x,
                                        int J, int I)
 {
-    return S(L.cx) * (nbv(L, x, J, I - 1) + nbv(L, x, J, I + 1)) +
-           S(L.cy) * (nbv(L, x, J - 1, I) + nbv(L, x, J + 1, I));
+    return Coef<S>::cx(L) * (nbv(L, x, J, I - 1) + nbv(L, x, J, I + 1)) +
+           Coef<S>::cy(L) * (nbv(L, x, J - 1, I) + nbv(L, x, J + 1, I));
 }
 
 // ---- node operations (shared by the grid kernels and the tail block) ------
@@ -49,11 +70,11 @@ __device__ __forceinline__ void op_smooth(const MGLevel& L, int J, int I, int co
     const S* b = lb<S>(L);
     const bool mine = ((J + I) & 1) == color;
     if (zero_init) {
-        x[k] = (mine && L.m[k]) ? b[k] * S(L.idiag) : S(0);
+        x[k] = (mine && L.m[k]) ? b[k] * Coef<S>::idiag(L) : S(0);
         return;
     }
     if (!mine || !L.m[k]) return;
-    x[k] = (b[k] - apply_off<S>(L, x, J, I)) * S(L.idiag);
+    x[k] = (b[k] - apply_off<S>(L, x, J, I)) * Coef<S>::idiag(L);
 }
 
 // residual of the fine level at node (J, I) (0 at non-fluid nodes)
@@ -68,7 +89,7 @@ __device__ __forceinline__ S fine_res(const MGLevel& F, int J, int I)
     const long long k = nidx(F, J, I);
     if (!F.m[k]) return S(0);
     const S* x = lx<S>(F);
-    return lb<S>(F)[k] - (apply_off<S>(F, x, J, I) + S(F.diag) * x[k]);
+    return lb<S>(F)[k] - (apply_off<S>(F, x, J, I) + Coef<S>::diag(F) * x[k]);
 }
 
 // coarse right-hand side = P^T (fine residual). After the pre-smoothing
@@ -134,7 +155,7 @@ __device__ __forceinline__ S red_from_zero(const MGLevel& L, int J, int I)
         I = I < 0 ? I + L.nxn : I - L.nxn;
     }
     const long long k = nidx(L, J, I);
-    return L.m[k] ? lb<S>(L)[k] * S(L.idiag) : S(0);
+    return L.m[k] ? lb<S>(L)[k] * Coef<S>::idiag(L) : S(0);
 }
 
 // ---- the single-block tail: levels l0..nl-1 of the V-cycle ---------------
@@ -156,11 +177,11 @@ __device__ __forceinline__ void op_presmooth(const MGLevel& L, int J, int I)
     if (L.m[k]) {
         const S* b = lb<S>(L);
         if (((J + I) & 1) == 0) {
-            v = b[k] * S(L.idiag);
+            v = b[k] * Coef<S>::idiag(L);
         } else {
-            const S off = S(L.cx) * (red_from_zero<S>(L, J, I - 1) + red_from_zero<S>(L, J, I + 1)) +
-                          S(L.cy) * (red_from_zero<S>(L, J - 1, I) + red_from_zero<S>(L, J + 1, I));
-            v = (b[k] - off) * S(L.idiag);
+            const S off = Coef<S>::cx(L) * (red_from_zero<S>(L, J, I - 1) + red_from_zero<S>(L, J, I + 1)) +
+                          Coef<S>::cy(L) * (red_from_zero<S>(L, J - 1, I) + red_from_zero<S>(L, J + 1, I));
+            v = (b[k] - off) * Coef<S>::idiag(L);
         }
     }
     lx<S>(L)[k] = v;

@@ -21,6 +21,7 @@
 #include <algorithm>
 #include <cstdlib>
 #include <cstring>
+#include <type_traits>
 
 #include "mg_ops.cuh"
 #include "solver.cuh"
@@ -37,9 +38,44 @@ __device__ __forceinline__ void tile_nodes(const int4& tl, const MGLevel& L, F f
     }
 }
 
+// per-thread dot-product partial -> what seg_reduce2 expects: FP32 values
+// are summed per warp in FP32 and combined in FP64 (block total in thread 0);
+// FP64 values go to seg_reduce2's own FP64 block reduction.
+template <typename V>
+__device__ __forceinline__ void block_dot(V acc, double (&w)[1]);
+template <>
+__device__ __forceinline__ void block_dot<double>(double acc, double (&w)[1])
+{
+    w[0] = acc;
+}
+template <>
+__device__ __forceinline__ void block_dot<float>(float acc, double (&w)[1])
+{
+    const float a[1] = {acc};
+    w[0] = 0.0;
+    block_total_f<1>(a, w);
+}
+
 __device__ __forceinline__ bool bs_skip(const DevScalars& sc, int ir)
 {
     return sc.converged || (ir && sc.conv_in);
+}
+
+// Completion of a kernel over all members, counted per member: exactly one
+// block of every member calls this with mine = true (the last block of its
+// segmented reduction, or the first tile of a member whose work is skipped),
+// so the global ticket sees n increments, not one per block. True in the
+// thread that completes the count.
+__device__ __forceinline__ bool members_done(bool mine, unsigned int* ticket, int n)
+{
+    if (!mine) return false;
+    __threadfence();
+    if (atomicAdd(ticket, 1u) == (unsigned)n - 1) {
+        __threadfence();
+        *ticket = 0;
+        return true;
+    }
+    return false;
 }
 
 // ---- multigrid --------------------------------------------------------------
@@ -109,7 +145,7 @@ template <typename V>
 __device__ __forceinline__ V applyA(const MGLevel& L, const V* __restrict__ x, int J, int I,
                                     long long k)
 {
-    return apply_off<V>(L, x, J, I) + V(L.diag) * x[k];
+    return apply_off<V>(L, x, J, I) + Coef<V>::diag(L) * x[k];
 }
 
 // rz = <r, z>, beta = rz / rz_old (0 on the first iteration of a loop)
@@ -117,19 +153,22 @@ template <typename S, typename V>
 __global__ void __launch_bounds__(256)
 k_bs_rz(const int4* __restrict__ tiles, const BSInfo* __restrict__ info,
         const MGLevel* __restrict__ levs, const V* __restrict__ r, const S* __restrict__ z,
-        DevScalars* scs, double* partials, int ir)
+        DevScalars* scs, double* partials, double* gpart, unsigned int* gtick, int ir)
 {
     const int4 tl = tiles[blockIdx.x];
     DevScalars& sc = scs[tl.x];
     if (bs_skip(sc, ir)) return;
     const MGLevel L = levs[tl.x * BS_LMAX];
-    double w[1] = {0.0};
+    V acc = V(0);
     tile_nodes(tl, L, [&](int J, int I) {
         const long long k = nidx(L, J, I);
-        if (L.m[k]) w[0] += (double)r[k] * (double)z[k];
+        if (L.m[k]) acc += r[k] * V(z[k]);
     });
+    double w[1];
+    block_dot<V>(acc, w);
     const BSInfo in = info[tl.x];
-    if (seg_reduce<1, false>(w, partials, blockIdx.x, in.n0, in.nn, &sc.counter[2])) {
+    if (seg_reduce2<1, std::is_same<V, float>::value>(w, partials, gpart, gtick, blockIdx.x,
+                                                      in.n0, in.nn, in.g0, &sc.counter[2])) {
         const int first = ir ? sc.iter_in == 0 : sc.iter == 0;
         sc.beta = first ? 0.0 : w[0] / sc.rz;
         sc.rz = w[0];
@@ -161,24 +200,27 @@ template <typename V>
 __global__ void __launch_bounds__(256)
 k_bs_spmv(const int4* __restrict__ tiles, const BSInfo* __restrict__ info,
           const MGLevel* __restrict__ levs, const V* __restrict__ p, V* __restrict__ q,
-          DevScalars* scs, double* partials, int ir)
+          DevScalars* scs, double* partials, double* gpart, unsigned int* gtick, int ir)
 {
     const int4 tl = tiles[blockIdx.x];
     DevScalars& sc = scs[tl.x];
     if (bs_skip(sc, ir)) return;
     const MGLevel L = levs[tl.x * BS_LMAX];
-    double w[1] = {0.0};
+    V acc = V(0);
     tile_nodes(tl, L, [&](int J, int I) {
         const long long k = nidx(L, J, I);
         V qv = V(0);
         if (L.m[k]) {
             qv = applyA<V>(L, p, J, I, k);
-            w[0] += (double)p[k] * (double)qv;
+            acc += p[k] * qv;
         }
         q[k] = qv;
     });
+    double w[1];
+    block_dot<V>(acc, w);
     const BSInfo in = info[tl.x];
-    if (seg_reduce<1, false>(w, partials, blockIdx.x, in.n0, in.nn, &sc.counter[3])) {
+    if (seg_reduce2<1, std::is_same<V, float>::value>(w, partials, gpart, gtick, blockIdx.x,
+                                                      in.n0, in.nn, in.g0, &sc.counter[3])) {
         sc.pq = w[0];
         sc.alpha = sc.rz / w[0];
     }
@@ -193,16 +235,20 @@ __global__ void __launch_bounds__(256)
 k_bs_xr(const int4* __restrict__ tiles, const BSInfo* __restrict__ info,
         const MGLevel* __restrict__ levs, V* __restrict__ x, V* __restrict__ r,
         const V* __restrict__ p, const V* __restrict__ q, DevScalars* scs, double* partials,
-        BSGlobals* eg, cudaGraphConditionalHandle cond, int ir)
+        double* gpart, unsigned int* gtick, BSGlobals* eg, cudaGraphConditionalHandle cond,
+        int ir, int nmem)
 {
     const int4 tl = tiles[blockIdx.x];
     DevScalars& sc = scs[tl.x];
-    if (!bs_skip(sc, ir)) {
+    bool mine = false;
+    if (bs_skip(sc, ir)) {
+        mine = threadIdx.x == 0 && threadIdx.y == 0 && (int)blockIdx.x == info[tl.x].n0;
+    } else {
         const MGLevel L = levs[tl.x * BS_LMAX];
         const int zero = ir ? 0 : sc.pad1;
         const int first = ir && sc.iter_in == 0;
         const V a = V(sc.alpha);
-        double w[1] = {0.0};
+        V acc = V(0);
         tile_nodes(tl, L, [&](int J, int I) {
             const long long k = nidx(L, J, I);
             if (!L.m[k]) return;
@@ -214,10 +260,15 @@ k_bs_xr(const int4* __restrict__ tiles, const BSInfo* __restrict__ info,
             x[k] = (first ? V(0) : x[k]) + a * p[k];
             const V rv = r[k] - a * q[k];
             r[k] = rv;
-            w[0] += (double)rv * (double)rv;
+            acc += rv * rv;
         });
+        double w[1];
+        block_dot<V>(acc, w);
         const BSInfo in = info[tl.x];
-        if (seg_reduce<1, false>(w, partials, blockIdx.x, in.n0, in.nn, &sc.counter[4])) {
+        mine = seg_reduce2<1, std::is_same<V, float>::value>(w, partials, gpart, gtick,
+                                                             blockIdx.x, in.n0, in.nn, in.g0,
+                                                             &sc.counter[4]);
+        if (mine) {
             sc.total_iters += 1;
             const bool bad = !(w[0] == w[0]);
             if (bad) atomicOr(&eg->status, ST_NONFINITE);
@@ -242,7 +293,7 @@ k_bs_xr(const int4* __restrict__ tiles, const BSInfo* __restrict__ info,
             }
         }
     }
-    if (last_block(&eg->ticket[1])) {
+    if (members_done(mine, &eg->ticket[1], nmem)) {
         eg->loops_in += 1;
         const int act = ir ? *(volatile int*)&eg->active_in : *(volatile int*)&eg->active_out;
         if (cond) cudaGraphSetConditional(cond, act > 0 ? 1u : 0u);
@@ -254,7 +305,8 @@ __global__ void __launch_bounds__(256)
 k_bs_init(const int4* __restrict__ tiles, const BSInfo* __restrict__ info,
           const MGLevel* __restrict__ levs, const double* __restrict__ x,
           const double* __restrict__ b, double* __restrict__ r, DevScalars* scs,
-          double* partials, BSGlobals* eg, cudaGraphConditionalHandle cond)
+          double* partials, double* gpart, unsigned int* gtick, BSGlobals* eg,
+          cudaGraphConditionalHandle cond, int nmem)
 {
     const int4 tl = tiles[blockIdx.x];
     DevScalars& sc = scs[tl.x];
@@ -272,7 +324,8 @@ k_bs_init(const int4* __restrict__ tiles, const BSInfo* __restrict__ info,
         r[k] = rv;
     });
     const BSInfo in = info[tl.x];
-    if (seg_reduce<2, false>(w, partials, blockIdx.x, in.n0, in.nn, &sc.counter[1])) {
+    const bool mine = seg_reduce2<2>(w, partials, gpart, gtick, blockIdx.x, in.n0, in.nn, in.g0, &sc.counter[1]);
+    if (mine) {
         sc.bb = w[0];
         sc.rr = w[1];
         sc.iter = 0;
@@ -281,7 +334,7 @@ k_bs_init(const int4* __restrict__ tiles, const BSInfo* __restrict__ info,
         sc.pad1 = zero;
         if (!sc.converged) atomicAdd(&eg->active_out, 1);
     }
-    if (last_block(&eg->ticket[0])) {
+    if (members_done(mine, &eg->ticket[0], nmem)) {
         eg->loops_out += 1;
         if (cond) cudaGraphSetConditional(cond, *(volatile int*)&eg->active_out > 0 ? 1u : 0u);
     }
@@ -293,12 +346,15 @@ __global__ void __launch_bounds__(256)
 k_bs_refine(const int4* __restrict__ tiles, const BSInfo* __restrict__ info,
             const MGLevel* __restrict__ levs, const double* __restrict__ x,
             const double* __restrict__ b, double* __restrict__ r, float* __restrict__ rin,
-            DevScalars* scs, double* partials, BSGlobals* eg, int first,
-            cudaGraphConditionalHandle cond)
+            DevScalars* scs, double* partials, double* gpart, unsigned int* gtick,
+            BSGlobals* eg, int first, cudaGraphConditionalHandle cond, int nmem)
 {
     const int4 tl = tiles[blockIdx.x];
     DevScalars& sc = scs[tl.x];
-    if (!sc.converged) {
+    bool mine = false;
+    if (sc.converged) {
+        mine = threadIdx.x == 0 && threadIdx.y == 0 && (int)blockIdx.x == info[tl.x].n0;
+    } else {
         const MGLevel L = levs[tl.x * BS_LMAX];
         double w[2] = {0.0, 0.0};
         tile_nodes(tl, L, [&](int J, int I) {
@@ -314,7 +370,8 @@ k_bs_refine(const int4* __restrict__ tiles, const BSInfo* __restrict__ info,
             rin[k] = float(rv);
         });
         const BSInfo in = info[tl.x];
-        if (seg_reduce<2, false>(w, partials, blockIdx.x, in.n0, in.nn, &sc.counter[1])) {
+        mine = seg_reduce2<2>(w, partials, gpart, gtick, blockIdx.x, in.n0, in.nn, in.g0, &sc.counter[1]);
+        if (mine) {
             const double rr_prev = sc.rr;
             sc.bb = w[0];
             sc.rr = w[1];
@@ -347,7 +404,7 @@ k_bs_refine(const int4* __restrict__ tiles, const BSInfo* __restrict__ info,
             }
         }
     }
-    if (last_block(&eg->ticket[0])) {
+    if (members_done(mine, &eg->ticket[0], nmem)) {
         eg->loops_out += 1;
         if (cond) cudaGraphSetConditional(cond, *(volatile int*)&eg->active_out > 0 ? 1u : 0u);
     }
@@ -452,17 +509,18 @@ template <typename S, typename V>
 static int cg_body(BatchSolver& s, cudaStream_t st, cudaGraphConditionalHandle cond, int ir)
 {
     const dim3 blk(32, 8);
-    const int nt = s.ntiles[0];
+    const int nt = s.nrtiles;
     V* r = (V*)(ir ? s.v.rin : s.v.r64);
     V* x = (V*)(ir ? s.v.e : s.v.x64);
     int cnt = vcycle<S>(s, st, ir);
-    k_bs_rz<S, V><<<nt, blk, 0, st>>>(s.tiles[0], s.dinfo, s.dlevs, r, (const S*)s.v.z, s.scs,
-                                      s.partials, ir);
-    k_bs_p<S, V><<<nt, blk, 0, st>>>(s.tiles[0], s.dlevs, (const S*)s.v.z, (V*)s.v.p, s.scs, ir);
-    k_bs_spmv<V><<<nt, blk, 0, st>>>(s.tiles[0], s.dinfo, s.dlevs, (const V*)s.v.p, (V*)s.v.q,
-                                     s.scs, s.partials, ir);
-    k_bs_xr<V><<<nt, blk, 0, st>>>(s.tiles[0], s.dinfo, s.dlevs, x, r, (const V*)s.v.p,
-                                   (const V*)s.v.q, s.scs, s.partials, s.eg, cond, ir);
+    k_bs_rz<S, V><<<nt, blk, 0, st>>>(s.rtiles, s.dinfo, s.dlevs, r, (const S*)s.v.z, s.scs,
+                                      s.partials, s.gpart, s.gtick, ir);
+    k_bs_p<S, V><<<nt, blk, 0, st>>>(s.rtiles, s.dlevs, (const S*)s.v.z, (V*)s.v.p, s.scs, ir);
+    k_bs_spmv<V><<<nt, blk, 0, st>>>(s.rtiles, s.dinfo, s.dlevs, (const V*)s.v.p, (V*)s.v.q,
+                                     s.scs, s.partials, s.gpart, s.gtick, ir);
+    k_bs_xr<V><<<nt, blk, 0, st>>>(s.rtiles, s.dinfo, s.dlevs, x, r, (const V*)s.v.p,
+                                   (const V*)s.v.q, s.scs, s.partials, s.gpart, s.gtick, s.eg, cond, ir,
+                                   s.n);
     cnt += 4;
     s.body_launches = cnt;
     return (int)cudaGetLastError();
@@ -516,7 +574,7 @@ static cudaStream_t g_third = nullptr;  // body stream of nested loops
 int bs_record(BatchSolver& s, cudaStream_t st, cudaStream_t st2, int* launches)
 {
     const dim3 blk(32, 8);
-    const int nt = s.ntiles[0];
+    const int nt = s.nrtiles;
     int fixed = 0;
     k_bs_setup<<<(s.n + 127) / 128, 128, 0, st>>>(s.scs, s.n, s.tol * s.tol, s.maxit,
                                                    s.tol_in * s.tol_in, s.maxit_in, s.maxouter,
@@ -535,9 +593,9 @@ int bs_record(BatchSolver& s, cudaStream_t st, cudaStream_t st2, int* launches)
             e = cudaGraphConditionalHandleCreate(&cond, graph, 1, cudaGraphCondAssignDefault);
             if (e != cudaSuccess) return (int)e;
         }
-        k_bs_init<<<nt, blk, 0, st>>>(s.tiles[0], s.dinfo, s.dlevs, (const double*)s.v.x64,
+        k_bs_init<<<nt, blk, 0, st>>>(s.rtiles, s.dinfo, s.dlevs, (const double*)s.v.x64,
                                       (const double*)s.v.b64, (double*)s.v.r64, s.scs,
-                                      s.partials, s.eg, cond);
+                                      s.partials, s.gpart, s.gtick, s.eg, cond, s.n);
         fixed += 1;
         if (capturing) {
             int r = add_while(st, st2, &cond, 1, [&](cudaStream_t sb) {
@@ -567,17 +625,19 @@ int bs_record(BatchSolver& s, cudaStream_t st, cudaStream_t st2, int* launches)
         if (e != cudaSuccess) return (int)e;
     }
     k_bs_reset<<<1, 1, 0, st>>>(s.eg);
-    k_bs_refine<<<nt, blk, 0, st>>>(s.tiles[0], s.dinfo, s.dlevs, (const double*)s.v.x64,
+    k_bs_refine<<<nt, blk, 0, st>>>(s.rtiles, s.dinfo, s.dlevs, (const double*)s.v.x64,
                                     (const double*)s.v.b64, (double*)s.v.r64, (float*)s.v.rin,
-                                    s.scs, s.partials, s.eg, 1, cond_o);
+                                    s.scs, s.partials, s.gpart, s.gtick, s.eg, 1, cond_o,
+                                    s.n);
     fixed += 2;
     auto round_tail = [&](cudaStream_t sb) {
-        k_bs_correct<<<nt, blk, 0, sb>>>(s.tiles[0], s.dlevs, (double*)s.v.x64,
+        k_bs_correct<<<nt, blk, 0, sb>>>(s.rtiles, s.dlevs, (double*)s.v.x64,
                                          (const float*)s.v.e, s.scs);
         k_bs_reset<<<1, 1, 0, sb>>>(s.eg);
-        k_bs_refine<<<nt, blk, 0, sb>>>(s.tiles[0], s.dinfo, s.dlevs, (const double*)s.v.x64,
+        k_bs_refine<<<nt, blk, 0, sb>>>(s.rtiles, s.dinfo, s.dlevs, (const double*)s.v.x64,
                                         (const double*)s.v.b64, (double*)s.v.r64,
-                                        (float*)s.v.rin, s.scs, s.partials, s.eg, 0, cond_o);
+                                        (float*)s.v.rin, s.scs, s.partials, s.gpart, s.gtick,
+                                        s.eg, 0, cond_o, s.n);
     };
     if (capturing) {
         int r = add_while(st, st2, &cond_o, 1, [&](cudaStream_t sb) {
@@ -662,11 +722,27 @@ int bs_build(BatchSolver& s, const std::vector<BSMemberDesc>& members, const uin
         for (int b = 0; b < s.n; ++b) {
             if (l > info[b].ltail) continue;
             const MGLevel& L = levs[(size_t)b * BS_LMAX + l];
-            if (l == 0) info[b].n0 = (int)tiles[0].size();
             for (int J0 = 0; J0 < L.nyn; J0 += 8 * R)
                 for (int I0 = 0; I0 < L.nxn; I0 += BS_TW) tiles[l].push_back(make_int4(b, I0, J0, R));
-            if (l == 0) info[b].nn = (int)tiles[0].size() - info[b].n0;
         }
+    }
+    // Level-0 tiles of the Krylov kernels (32 x 8 nodes), with the member's
+    // reduction groups of 64 tiles.
+    std::vector<int4> rt;
+    int ngroups = 0;
+    for (int b = 0; b < s.n; ++b) {
+        const MGLevel& L = levs[(size_t)b * BS_LMAX];
+        const long long cols = (L.nxn + BS_TW - 1) / BS_TW;
+        const long long rows8 = (L.nyn + 7) / 8;
+        const int R = 1;
+        (void)cols;
+        (void)rows8;
+        info[b].n0 = (int)rt.size();
+        for (int J0 = 0; J0 < L.nyn; J0 += 8 * R)
+            for (int I0 = 0; I0 < L.nxn; I0 += BS_TW) rt.push_back(make_int4(b, I0, J0, R));
+        info[b].nn = (int)rt.size() - info[b].n0;
+        info[b].g0 = ngroups;
+        ngroups += (info[b].nn + RED_GROUP - 1) / RED_GROUP;
     }
     auto dal = [&](size_t bytes) -> void* {
         void* p = nullptr;
@@ -684,10 +760,21 @@ int bs_build(BatchSolver& s, const std::vector<BSMemberDesc>& members, const uin
                        cudaMemcpyHostToDevice) != cudaSuccess)
             return 2;
     }
+    s.nrtiles = (int)rt.size();
+    s.rtiles = (int4*)dal(rt.size() * sizeof(int4));
+    if (!s.rtiles ||
+        cudaMemcpy(s.rtiles, rt.data(), rt.size() * sizeof(int4), cudaMemcpyHostToDevice) !=
+            cudaSuccess)
+        return 2;
     s.dlevs = (MGLevel*)dal(levs.size() * sizeof(MGLevel));
     s.dinfo = (BSInfo*)dal(info.size() * sizeof(BSInfo));
     s.eg = (BSGlobals*)dal(sizeof(BSGlobals));
-    s.partials = (double*)dal((tiles[0].size() * 2 + 64) * sizeof(double));
+    s.partials = (double*)dal((rt.size() * 2 + 64) * sizeof(double));
+    s.gpart = (double*)dal(((size_t)ngroups * 2 + 64) * sizeof(double));
+    s.gtick = (unsigned int*)dal(((size_t)ngroups + 64) * sizeof(unsigned int));
+    if (!s.gpart || !s.gtick ||
+        cudaMemset(s.gtick, 0, ((size_t)ngroups + 64) * sizeof(unsigned int)) != cudaSuccess)
+        return 2;
     if (!s.dlevs || !s.dinfo || !s.eg || !s.partials) return 2;
     if (cudaMemcpy(s.dlevs, levs.data(), levs.size() * sizeof(MGLevel), cudaMemcpyHostToDevice) !=
             cudaSuccess ||

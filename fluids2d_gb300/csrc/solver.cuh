@@ -14,7 +14,8 @@ constexpr int BS_TW = 32, BS_TH = 32;  // node tile: 32 x 32 nodes, 32 x 8 threa
 struct BSInfo {
     int nl, ltail, ksweeps;  // levels, first tail level, coarsest sweeps
     int n0, nn;              // range of the member in the level-0 tile table
-    int pad[3];
+    int g0;                  // first reduction group of the member
+    int pad[2];
 };
 
 struct BSGlobals {
@@ -57,6 +58,10 @@ struct BatchSolver {
     double* partials = nullptr;
     std::vector<int4*> tiles;  // node tiles per level (members reaching it)
     std::vector<int> ntiles;
+    int4* rtiles = nullptr;    // level-0 tiles of the Krylov kernels
+    int nrtiles = 0;
+    double* gpart = nullptr;   // group sums of the two-level reductions
+    unsigned int* gtick = nullptr;
     int maxl = 0;
     size_t tail_smem = 0;
     BSVecs v;

@@ -47,6 +47,7 @@ k_rsw_stage(const __grid_constant__ CUtensorMap th,
     __shared__ alignas(128) T sw[SH][SW];
     __shared__ T sfx[TY][TX + 1];
     __shared__ T sfy[TY + 1][TX];
+    __shared__ T srk[4];  // RK3 coefficients, Coriolis parameter
     __shared__ uint64_t bar;
     const int tx = threadIdx.x, ty = threadIdx.y, t = ty * TX + tx;
     const int i0 = blockIdx.x * TX, j0 = blockIdx.y * TY;
@@ -125,11 +126,15 @@ k_rsw_stage(const __grid_constant__ CUtensorMap th,
             duy = -face_value<M, T>(L, Vm, w[0], w[1], w[2], w[3], w[4], w[5]) * Vm;
         }
     }
+    if (tx == 0 && ty == 0) {
+        rk3_coefs<T>(stage, sc->dt, srk);
+        srk[3] = T(a.fc);
+    }
     __syncthreads();
     if (!live) return;
 
     // Coriolis (addcoriolis, operators.py:32-39)
-    const T fc = T(a.fc);
+    const T fc = srk[3];
     if (j <= g.NY - 2 && i >= 1 && i <= g.NX - 2)
         dux += fc * (((ldz(Uy, j, i - 1, g) + ldz(Uy, j + 1, i - 1, g)) + Uy[o]) +
                      ldz(Uy, j + 1, i, g));
@@ -151,7 +156,7 @@ k_rsw_stage(const __grid_constant__ CUtensorMap th,
     const T msk = (cd & B_MSK) ? T(1) : T(0);
     const T dh = (-(sfx[ty][tx + 1] - sfx[ty][tx]) - (sfy[ty + 1][tx] - sfy[ty][tx])) * msk;
 
-    const double dt = sc->dt;
+    const T* dt = srk;
     T ix, iy, ih;
     if (stage == 1) {
         ix = rk3_increment<T>(1, dt, dux, T(0), T(0));
@@ -252,12 +257,12 @@ __global__ void k_c2v(const Tin* __restrict__ q, T* __restrict__ v,
     const int j = blockIdx.y * blockDim.y + threadIdx.y;
     if (j >= g.NY || i >= g.NX) return;
     const long long o = (long long)j * g.P + i;
-    T a = T(0);
-    if (j >= 1 && i >= 1)
-        a = T(0.25) * (((T(q[o - g.P - 1]) + T(q[o - 1])) + T(q[o - g.P])) + T(q[o]));
-    a *= (code[o] & B_MSKV) ? T(1) : T(0);
-    if (fv) a -= fv[o];
-    v[o] = a;
+    Tin a = Tin(0);
+    if (j >= 1 && i >= 1 && (code[o] & B_MSKV))
+        a = Tin(0.25) * (((q[o - g.P - 1] + q[o - 1]) + q[o - g.P]) + q[o]);
+    T b = T(a);
+    if (fv) b -= fv[o];
+    v[o] = b;
 }
 
 // perpgrad with contravariant scaling (operators.py:144-149), optional halo
@@ -265,23 +270,21 @@ __global__ void k_c2v(const Tin* __restrict__ q, T* __restrict__ v,
 template <typename P, typename T>
 __global__ void k_perpgrad(const P* __restrict__ psi, T* __restrict__ Ux,
                            T* __restrict__ Uy, const uint32_t* __restrict__ code,
-                           double rdy2, double rdx2, int fillU, Geom g,
+                           T rdy2, T rdx2, int fillU, Geom g,
                            DevScalars* sc, double* partials)
 {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     const int j = blockIdx.y * blockDim.y + threadIdx.y;
-    double m[2] = {0.0, 0.0};
+    T m[2] = {T(0), T(0)};
     if (j < g.NY && i < g.NX) {
         const long long o = (long long)j * g.P + i;
         const bool own = !fillU || periodic_owner(g, i);
         if (own) {
+            // the difference in the precision of psi, the scaling in that of U
             const uint32_t cd = code[o];
-            P px = P(0), py = P(0);
-            if (j <= g.NY - 2) px = -(psi[o + g.P] - psi[o]) * ((cd & B_MSKX) ? P(1) : P(0));
-            if (i <= g.NX - 2) py = (psi[o + 1] - psi[o]) * ((cd & B_MSKY) ? P(1) : P(0));
-            px *= P(rdy2);
-            py *= P(rdx2);
-            const T ux = T(px), uy = T(py);
+            T ux = T(0), uy = T(0);
+            if (j <= g.NY - 2 && (cd & B_MSKX)) ux = -T(psi[o + g.P] - psi[o]) * rdy2;
+            if (i <= g.NX - 2 && (cd & B_MSKY)) uy = T(psi[o + 1] - psi[o]) * rdx2;
             if (fillU) {
                 store_filled(Ux, g, j, i, ux);
                 store_filled(Uy, g, j, i, uy);
@@ -289,13 +292,16 @@ __global__ void k_perpgrad(const P* __restrict__ psi, T* __restrict__ Ux,
                 Ux[o] = ux;
                 Uy[o] = uy;
             }
-            m[0] = fabs((double)ux);
-            m[1] = fabs((double)uy);
+            m[0] = fabs(ux);
+            m[1] = fabs(uy);
         }
     }
-    if (grid_reduce<2, true>(m, partials, &sc->counter[0])) {
-        sc->maxUx = m[0];
-        sc->maxUy = m[1];
+    constexpr bool F = std::is_same<T, float>::value;
+    double w[2];
+    block_pre<2, true>(m, w);
+    if (grid_reduce<2, true, F>(w, partials, &sc->counter[0])) {
+        sc->maxUx = w[0];
+        sc->maxUy = w[1];
     }
 }
 

@@ -21,12 +21,31 @@ __device__ __forceinline__ T ldz(const T* __restrict__ a, int j, int i,
 // The RK3 increment of stage k (1, 2, 3) in the reference's evaluation order:
 // y += ((0 + c1*ds1) + c2*ds2) + c3*ds3 with (c) = (dt), (-3dt/4, dt/4),
 // (-dt/12, -dt/12, 2dt/3).
+// The coefficients are computed once per block (one thread, into shared
+// memory): per-thread FP64 divisions would load the FP64 pipe of the FP32
+// kernels.
 template <typename T>
-__device__ __forceinline__ T rk3_increment(int stage, double dt, T d1, T d2, T d3)
+__device__ __forceinline__ void rk3_coefs(int stage, double dt, T* c)
 {
-    if (stage == 1) return T(dt) * d1;
-    if (stage == 2) return T(-3 * dt / 4) * d1 + T(dt / 4) * d2;
-    return (T(-dt / 12) * d1 + T(-dt / 12) * d2) + T(2 * dt / 3) * d3;
+    if (stage == 1) {
+        c[0] = T(dt);
+        c[1] = c[2] = T(0);
+    } else if (stage == 2) {
+        c[0] = T(-3 * dt / 4);
+        c[1] = T(dt / 4);
+        c[2] = T(0);
+    } else {
+        c[0] = c[1] = T(-dt / 12);
+        c[2] = T(2 * dt / 3);
+    }
+}
+
+template <typename T>
+__device__ __forceinline__ T rk3_increment(int stage, const T* c, T d1, T d2, T d3)
+{
+    if (stage == 1) return c[0] * d1;
+    if (stage == 2) return c[0] * d1 + c[1] * d2;
+    return (c[0] * d1 + c[1] * d2) + c[2] * d3;
 }
 
 // Store v at (j,i) and, in an x-periodic domain, at its halo copy.
@@ -82,6 +101,7 @@ struct FluxformSmem {
     alignas(128) T sq[SH][SW];
     T sfx[TY][TX + 1];
     T sfy[TY + 1][TX];
+    T rk[3];
     uint64_t bar;
 };
 
@@ -135,6 +155,7 @@ __device__ __forceinline__ void fluxform_tile(
     yface(ty, tx);
     if (t < TY) xface(t, TX);
     else if (t < TY + TX) yface(TY, t - TY);
+    if (t == 0) rk3_coefs<T>(stage, dt, sm.rk);
     __syncthreads();
 
     const int j = j0 + ty, i = i0 + tx;
@@ -143,9 +164,9 @@ __device__ __forceinline__ void fluxform_tile(
     const T msk = (code[o] & B_MSK) ? T(1) : T(0);
     const T ds = (-(sfx[ty][tx + 1] - sfx[ty][tx]) - (sfy[ty + 1][tx] - sfy[ty][tx])) * msk;
     T inc;
-    if (stage == 1) inc = rk3_increment<T>(1, dt, ds, T(0), T(0));
-    else if (stage == 2) inc = rk3_increment<T>(2, dt, ds1[o], ds, T(0));
-    else inc = rk3_increment<T>(3, dt, ds1[o], ds2[o], ds);
+    if (stage == 1) inc = rk3_increment<T>(1, sm.rk, ds, T(0), T(0));
+    else if (stage == 2) inc = rk3_increment<T>(2, sm.rk, ds1[o], ds, T(0));
+    else inc = rk3_increment<T>(3, sm.rk, ds1[o], ds2[o], ds);
     const T q = sq[ty + OY][tx + OX];
     store_filled(qout, g, j, i, q + inc);
     if (ds_out) store_filled(ds_out, g, j, i, ds);
