@@ -97,6 +97,7 @@ struct f2d_model_s {
     bool bs_ready[2] = {false, false};
     void* pe = nullptr;  // inner correction of the refinement form (FP32)
     void *pr = nullptr, *pz = nullptr, *pp = nullptr, *pq = nullptr;
+    void *pp2 = nullptr, *pza = nullptr;
     void* prmg = nullptr;  // V-cycle right-hand side (== pr in FP64)
     void* stage64 = nullptr;  // FP64 staging for field I/O of FP32 fields
     void *sb = nullptr, *sx = nullptr;  // scratch for f2d_poisson_solve
@@ -213,8 +214,10 @@ static int ensure_mg(f2d_model_s* m, int which)
     memset(&v, 0, sizeof(v));
     v.r64 = m->pr;
     v.p = m->pp;
+    v.p2 = m->pp2;
     v.q = m->pq;
     v.z = m->pz;
+    v.za = m->pza;
     v.rin = m->prmg;
     v.e = m->pe;
     BatchSolver& bs = m->bs[which];
@@ -627,10 +630,13 @@ int f2d_model_create(const f2d_params* p, const int8_t* msk, f2d_model* out)
         m->pp = dalloc(m, field_bytes(m, 8));
         m->pq = dalloc(m, field_bytes(m, 8));
         m->pz = dalloc(m, field_bytes(m, m->es));
+        m->pp2 = dalloc(m, field_bytes(m, 8));
+        m->pza = dalloc(m, field_bytes(m, m->es));
         m->prmg = m->prec == 0 ? m->pr : dalloc(m, field_bytes(m, 4));
         m->pe = m->prec == 0 ? m->pr : dalloc(m, field_bytes(m, 4));
         m->d_fv = dalloc(m, field_bytes(m, 8));
-        if (!m->pr || !m->pz || !m->pp || !m->pq || !m->d_fv || !m->prmg || !m->pe)
+        if (!m->pr || !m->pz || !m->pp || !m->pq || !m->d_fv || !m->prmg || !m->pe ||
+            !m->pp2 || !m->pza)
             return bail(fail(2, "out of device memory"));
     }
     if (m->prec != 0) {

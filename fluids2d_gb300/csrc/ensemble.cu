@@ -445,15 +445,17 @@ int f2d_ensemble_create(const f2d_params* p, int count, const int* nxs, const in
     v.b64 = e->ar.rhs;
     v.r64 = A(8);
     v.p = A(8);
+    v.p2 = A(8);
     v.q = A(8);
     v.z = A(es);
+    v.za = A(es);
     v.rin = e->prec == 0 ? v.r64 : A(4);
     v.e = e->prec == 0 ? v.r64 : A(4);
     e->stage64 = A(8);
     e->scs = (DevScalars*)ens_alloc(e, sizeof(DevScalars) * count);
     e->eg = (EnsGlobals*)ens_alloc(e, sizeof(EnsGlobals));
     for (void* q : {e->ar.q[0], e->ar.q[1], e->ar.ds1, e->ar.ds2, e->ar.Ux, e->ar.Uy,
-                    e->ar.rhs, e->ar.psi, e->ar.fv, e->code, e->gmask, v.r64, v.p, v.q, v.z,
+                    e->ar.rhs, e->ar.psi, e->ar.fv, e->code, e->gmask, v.r64, v.p, v.p2, v.q, v.z, v.za,
                     v.rin, v.e, e->stage64, (void*)e->scs, (void*)e->eg})
         if (!q) return bail(f2d_internal_fail(2, "out of device memory for the ensemble"));
     e->ar.code = (const uint32_t*)e->code;

@@ -34,7 +34,8 @@ static size_t tail_smem(const std::vector<MGLevel>& lev, int l0, size_t es)
 
 // Build the level hierarchy from the level-0 fluid mask (host copy).
 int mg_build(MGHost& mg, int nyn0, int nxn0, long long pitch0, long long off0, int per,
-             const uint8_t* hmask0, long long hoff0, const uint8_t* dmask0, void* z0, void* r0, double cx,
+             const uint8_t* hmask0, long long hoff0, const uint8_t* dmask0, void* z0, void* za0,
+             void* r0, double cx,
              double cy, double maindiag, int prec)
 {
     mg_free(mg);
@@ -43,6 +44,7 @@ int mg_build(MGHost& mg, int nyn0, int nxn0, long long pitch0, long long off0, i
     MGLevel L0;
     memset(&L0, 0, sizeof(L0));
     L0.x = z0;
+    L0.xa = za0;
     L0.b = r0;
     L0.m = dmask0;
     L0.nyn = nyn0;
@@ -64,7 +66,8 @@ int mg_build(MGHost& mg, int nyn0, int nxn0, long long pitch0, long long off0, i
     std::vector<uint8_t> cur((size_t)nyn0 * nxn0);
     for (int J = 0; J < nyn0; ++J)
         for (int I = 0; I < nxn0; ++I)
-            cur[(size_t)J * nxn0 + I] = hmask0[hoff0 + (long long)J * pitch0 + I];
+            cur[(size_t)J * nxn0 + I] = hmask0[hoff0 + (long long)J * pitch0 + I] ? 1 : 0;
+    mg.hmask.push_back(cur);
     int nyn = nyn0, nxn = nxn0;
     double md = maindiag;
     const int max_levels = 16;
@@ -104,23 +107,28 @@ int mg_build(MGHost& mg, int nyn0, int nxn0, long long pitch0, long long off0, i
         C.fdiag = (float)C.diag;
         C.fidiag = (float)C.idiag;
         const size_t n = (size_t)C.pitch * cyn;
-        void *x, *b, *m;
+        void *x, *xa, *b, *m;
         if (cudaMalloc(&x, n * es) != cudaSuccess) return 2;
         mg.owned.push_back(x);
+        if (cudaMalloc(&xa, n * es) != cudaSuccess) return 2;
+        mg.owned.push_back(xa);
         if (cudaMalloc(&b, n * es) != cudaSuccess) return 2;
         mg.owned.push_back(b);
         if (cudaMalloc(&m, n) != cudaSuccess) return 2;
         mg.owned.push_back(m);
         cudaMemset(x, 0, n * es);
+        cudaMemset(xa, 0, n * es);
         cudaMemset(b, 0, n * es);
         std::vector<uint8_t> hm(n, 0);
         for (int J = 0; J < cyn; ++J)
             memcpy(&hm[(size_t)J * C.pitch], &cm[(size_t)J * cxn], cxn);
         if (cudaMemcpy(m, hm.data(), n, cudaMemcpyHostToDevice) != cudaSuccess) return 2;
         C.x = x;
+        C.xa = xa;
         C.b = b;
         C.m = (const uint8_t*)m;
         mg.lev.push_back(C);
+        mg.hmask.push_back(cm);
         cur.swap(cm);
         nyn = cyn;
         nxn = cxn;
@@ -156,6 +164,7 @@ void mg_free(MGHost& mg)
     if (mg.dlev) cudaFree(mg.dlev);
     mg.dlev = nullptr;
     mg.lev.clear();
+    mg.hmask.clear();
 }
 
 }  // namespace f2d

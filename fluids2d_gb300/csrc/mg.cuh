@@ -13,6 +13,7 @@ namespace f2d {
 // vertex array (node (J,I) = array point (3+J, 3+I)).
 struct MGLevel {
     void* x;            // level unknown (level 0: the preconditioned residual z)
+    void* xa;           // x after the pre-smoothing (read by the up leg)
     void* b;            // level right-hand side (level 0: the CG residual r)
     const uint8_t* m;   // 1 = fluid node
     int nyn, nxn;
@@ -32,11 +33,12 @@ struct MGHost {
     int ncoarse_sweeps = 4;    // (R,B)^k (B,R)^k on the coarsest level
     size_t tail_smem = 0;      // dynamic shared memory of the tail kernel
     int prec = 0;              // 0 = double, 1 = float
+    std::vector<std::vector<uint8_t>> hmask;  // host fluid masks, dense nyn x nxn per level
 };
 
 int mg_build(MGHost& mg, int nyn0, int nxn0, long long pitch0, long long off0,
              int per, const uint8_t* hmask0 /* host, level-0 layout */, long long hoff0,
-             const uint8_t* dmask0 /* device copy */, void* z0, void* r0,
+             const uint8_t* dmask0 /* device copy */, void* z0, void* za0, void* r0,
              double cx, double cy, double maindiag, int prec);
 void mg_free(MGHost& mg);
 

@@ -28,13 +28,86 @@
 
 namespace f2d {
 
-// node loop of a tile: tl.w rows per thread (a tile is 32 x 8*tl.w nodes)
-template <typename F>
-__device__ __forceinline__ void tile_nodes(const int4& tl, const MGLevel& L, F f)
+// ---- tiles staged in shared memory ---------------------------------------------
+// Grid kernels work on tiles of 32 x 32 nodes of one level of one member
+// (the int4 of a tile table: member, first column, first row, unused), run
+// by 32 x 8 threads; thread (tx, ty) owns tile rows ty + 8 q, q = 0..3. A
+// kernel that needs neighbours stages the tile and a halo of H nodes in
+// shared memory (rows J0-H .. J0+31+H, columns I0-H .. I0+31+H); nodes
+// outside the level read as non-fluid 0, and x-periodic levels wrap. Each
+// node is then loaded once per kernel with coalesced rows, all loads of a
+// thread in flight together, and the red-black sweeps of a V-cycle level run
+// on the staged region: a half sweep on nodes at distance >= s from the
+// region edge only needs the region, so the smoothing, residual and transfer
+// steps of a level fuse into one kernel with a halo as wide as the chain.
+constexpr int TQ = BS_TH / 8;  // rows per thread
+
+__device__ __forceinline__ int tid256() { return threadIdx.y * 32 + threadIdx.x; }
+
+// wrap (J, I) into the level; false outside it
+__device__ __forceinline__ bool in_level(const MGLevel& L, int J, int& I)
 {
-    for (int r = 0; r < tl.w; ++r) {
-        const int J = tl.z + threadIdx.y + 8 * r, I = tl.y + threadIdx.x;
-        if (J < L.nyn && I < L.nxn) f(J, I);
+    if (J < 0 || J >= L.nyn) return false;
+    if (I < 0) {
+        if (!L.per) return false;
+        I += L.nxn;
+    } else if (I >= L.nxn) {
+        if (!L.per) return false;
+        I -= L.nxn;
+    }
+    return I >= 0 && I < L.nxn;
+}
+
+// Stage mask and up to two arrays of a level on the region of halo H around
+// the tile at (J0, I0). Values at non-fluid nodes are staged as 0.
+template <int H, typename S, typename T2>
+__device__ __forceinline__ void stage_region(const MGLevel& L, int J0, int I0,
+                                             const S* __restrict__ ga, S* sa,
+                                             const T2* __restrict__ gb, T2* sb, uint8_t* sm)
+{
+    constexpr int W = BS_TW + 2 * H, N = W * W, IT = (N + 255) / 256;
+    const int t = tid256();
+#pragma unroll
+    for (int it = 0; it < IT; ++it) {
+        const int e = t + it * 256;
+        if (e < N) {
+            const int r = e / W, c = e - r * W;
+            const int J = J0 - H + r;
+            int I = I0 - H + c;
+            uint8_t mv = 0;
+            S av = S(0);
+            T2 bv = T2(0);
+            if (in_level(L, J, I)) {
+                const long long k = nidx(L, J, I);
+                mv = L.m[k];
+                if (ga) av = ga[k];
+                if (gb) bv = gb[k];
+            }
+            sm[e] = mv;
+            if (sa) sa[e] = mv ? av : S(0);
+            if (sb) sb[e] = mv ? bv : T2(0);
+        }
+    }
+}
+
+// Red-black half sweep of colour `color` (0: (J+I) even) on the nodes of the
+// staged region at distance >= s from its edge: x = (b - offdiag(x)) / diag.
+// The tile origin is even, so the colour of a region node is the parity of
+// its region coordinates.
+template <typename S, int W>
+__device__ __forceinline__ void half_sweep(S* sx, const S* sb, const uint8_t* sm, int s,
+                                           int color, S cx, S cy, S id)
+{
+    constexpr int HW = W / 2;
+    const int n = (W - 2 * s) * HW;
+    for (int e = tid256(); e < n; e += 256) {
+        const int rr = s + e / HW;
+        const int cc = 2 * (e % HW) + ((color + rr) & 1);
+        if (cc < s || cc >= W - s) continue;
+        const int q = rr * W + cc;
+        if (!sm[q]) continue;
+        const S off = cx * (sx[q - 1] + sx[q + 1]) + cy * (sx[q - W] + sx[q + W]);
+        sx[q] = (sb[q] - off) * id;
     }
 }
 
@@ -54,6 +127,16 @@ __device__ __forceinline__ void block_dot<float>(float acc, double (&w)[1])
     const float a[1] = {acc};
     w[0] = 0.0;
     block_total_f<1>(a, w);
+}
+
+template <typename V>
+__device__ __forceinline__ bool member_dot(V acc, double (&w)[1], double* partials,
+                                           double* gpart, unsigned int* gtick,
+                                           const BSInfo& in, unsigned int* ticket)
+{
+    block_dot<V>(acc, w);
+    return seg_reduce2<1, std::is_same<V, float>::value>(w, partials, gpart, gtick, blockIdx.x,
+                                                         in.n0, in.nn, in.g0, ticket);
 }
 
 __device__ __forceinline__ bool bs_skip(const DevScalars& sc, int ir)
@@ -78,149 +161,267 @@ __device__ __forceinline__ bool members_done(bool mine, unsigned int* ticket, in
     return false;
 }
 
+// rz = <r, z> of a member, beta = rz / rz_old (0 on the first iteration of
+// a loop); run by the thread that holds the member's total
+__device__ __forceinline__ void set_rz(DevScalars& sc, int ir, double rz)
+{
+    const int first = ir ? sc.iter_in == 0 : sc.iter == 0;
+    sc.beta = first ? 0.0 : rz / sc.rz;
+    sc.rz = rz;
+}
+
 // ---- multigrid --------------------------------------------------------------
-template <typename S>
+// Down leg of level l (l below the member's tail): pre-smoothing from a zero
+// guess - red x = b/diag, black Gauss-Seidel, then NU-1 more (red, black)
+// sweeps - and restriction of the residual to level l+1 (transpose of the
+// bilinear prolongation). After a black half sweep the black residuals are
+// zero, so only the red fine nodes (centre and corners of a coarse node)
+// contribute. Writes the pre-smoothed x of the tile (to xa) and the coarse
+// right-hand side of the coarse nodes whose centre lies in the tile.
+template <typename S, int NU>
 __global__ void __launch_bounds__(256)
-k_bs_presmooth(const int4* __restrict__ tiles, const BSInfo* __restrict__ info,
-               const MGLevel* __restrict__ levs, int l, const DevScalars* __restrict__ scs,
-               int ir)
+k_bs_down(const int4* __restrict__ tiles, const BSInfo* __restrict__ info,
+          const MGLevel* __restrict__ levs, int l, const DevScalars* __restrict__ scs, int ir)
 {
+    constexpr int H = 2 * NU + 1, W = BS_TW + 2 * H, N = W * W;
+    __shared__ S sx[N];
+    __shared__ S sb[N];
+    __shared__ uint8_t sm[N];
     const int4 tl = tiles[blockIdx.x];
     if (info[tl.x].ltail <= l || bs_skip(scs[tl.x], ir)) return;
-    const MGLevel L = levs[tl.x * BS_LMAX + l];
-    tile_nodes(tl, L, [&](int J, int I) { op_presmooth<S>(L, J, I); });
+    const MGLevel F = levs[tl.x * BS_LMAX + l];
+    const int I0 = tl.y, J0 = tl.z, t = tid256();
+    stage_region<H, S, S>(F, J0, I0, lb<S>(F), sb, (const S*)nullptr, (S*)nullptr, sm);
+    __syncthreads();
+    const S cx = Coef<S>::cx(F), cy = Coef<S>::cy(F), d = Coef<S>::diag(F),
+            id = Coef<S>::idiag(F);
+    for (int e = t; e < N; e += 256) {
+        const int r = e / W, c = e - r * W;
+        sx[e] = (((r + c) & 1) == 0) ? sb[e] * id : S(0);  // sb is 0 at non-fluid nodes
+    }
+    __syncthreads();
+#pragma unroll
+    for (int s = 1; s < 2 * NU; ++s) {
+        half_sweep<S, W>(sx, sb, sm, s, s & 1, cx, cy, id);
+        __syncthreads();
+    }
+    // residual at the red nodes of the region shrunk by 2 NU (in place of b)
+    {
+        constexpr int HW = W / 2, s = 2 * NU;
+        const int n = (W - 2 * s) * HW;
+        for (int e = t; e < n; e += 256) {
+            const int rr = s + e / HW;
+            const int cc = 2 * (e % HW) + (rr & 1);
+            if (cc < s || cc >= W - s) continue;
+            const int q = rr * W + cc;
+            S v = S(0);
+            if (sm[q]) {
+                const S off = cx * (sx[q - 1] + sx[q + 1]) + cy * (sx[q - W] + sx[q + W]);
+                v = sb[q] - (off + d * sx[q]);
+            }
+            sb[q] = v;
+        }
+    }
+    __syncthreads();
+    {
+        const MGLevel C = levs[tl.x * BS_LMAX + l + 1];
+        const int a = t >> 4, b = t & 15;
+        const int cJ = (J0 >> 1) + a, cI = (I0 >> 1) + b;
+        if (cJ < C.nyn && cI < C.nxn) {
+            const long long k = nidx(C, cJ, cI);
+            S v = S(0);
+            if (C.m[k]) {
+                const int q = (H + 2 * a) * W + H + 2 * b;
+                const S c4 = (sb[q - W - 1] + sb[q - W + 1]) + (sb[q + W - 1] + sb[q + W + 1]);
+                v = sb[q] + S(0.25) * c4;
+            }
+            lb<S>(C)[k] = v;
+        }
+    }
+    S* xa = (S*)F.xa;
+#pragma unroll
+    for (int qr = 0; qr < TQ; ++qr) {
+        const int r = threadIdx.y + 8 * qr, c = threadIdx.x;
+        const int J = J0 + r, I = I0 + c;
+        if (J < F.nyn && I < F.nxn) xa[nidx(F, J, I)] = sx[(r + H) * W + c + H];
+    }
 }
 
+// coarse value for the prolongation (0 outside the level; x is 0 at
+// non-fluid nodes)
 template <typename S>
-__global__ void __launch_bounds__(256)
-k_bs_restrict(const int4* __restrict__ tiles, const BSInfo* __restrict__ info,
-              const MGLevel* __restrict__ levs, int l, const DevScalars* __restrict__ scs,
-              int ir)
+__device__ __forceinline__ S cval_g(const MGLevel& C, int J, int I)
 {
-    const int4 tl = tiles[blockIdx.x];
-    if (info[tl.x].ltail <= l || bs_skip(scs[tl.x], ir)) return;
-    const MGLevel F = levs[tl.x * BS_LMAX + l], C = levs[tl.x * BS_LMAX + l + 1];
-    tile_nodes(tl, C, [&](int J, int I) { op_restrict<S>(F, C, J, I); });
+    if (J < 0 || J >= C.nyn) return S(0);
+    if (I >= C.nxn) {
+        if (!C.per) return S(0);
+        I -= C.nxn;
+    }
+    return lx<S>(C)[nidx(C, J, I)];
 }
 
-template <typename S>
+// Up leg of level l: x = xa + P (coarse x), then NU (black, red)
+// post-smoothing sweeps; writes x of the tile. On level 0 (RZ) the block
+// also forms its part of <r, z> (r = b, z = x) and the member's last block
+// sets rz and beta.
+template <typename S, int NU, bool RZ>
 __global__ void __launch_bounds__(256)
-k_bs_prolong(const int4* __restrict__ tiles, const BSInfo* __restrict__ info,
-             const MGLevel* __restrict__ levs, int l, const DevScalars* __restrict__ scs,
-             int ir)
+k_bs_up(const int4* __restrict__ tiles, const BSInfo* __restrict__ info,
+        const MGLevel* __restrict__ levs, int l, DevScalars* scs, int ir, double* partials,
+        double* gpart, unsigned int* gtick)
 {
+    constexpr int H = 2 * NU, W = BS_TW + 2 * H, N = W * W;
+    __shared__ S sx[N];
+    __shared__ S sb[N];
+    __shared__ uint8_t sm[N];
     const int4 tl = tiles[blockIdx.x];
-    if (info[tl.x].ltail <= l || bs_skip(scs[tl.x], ir)) return;
-    const MGLevel F = levs[tl.x * BS_LMAX + l], C = levs[tl.x * BS_LMAX + l + 1];
-    tile_nodes(tl, F, [&](int J, int I) { op_prolong<S>(C, F, J, I); });
+    DevScalars& sc = scs[tl.x];
+    const BSInfo in = info[tl.x];
+    if (in.ltail <= l || bs_skip(sc, ir)) return;
+    const MGLevel F = levs[tl.x * BS_LMAX + l];
+    const MGLevel C = levs[tl.x * BS_LMAX + l + 1];
+    const int I0 = tl.y, J0 = tl.z, t = tid256();
+    stage_region<H, S, S>(F, J0, I0, (const S*)F.xa, sx, lb<S>(F), sb, sm);
+    __syncthreads();
+    for (int e = t; e < N; e += 256) {
+        if (!sm[e]) continue;
+        const int r = e / W, c = e - r * W;
+        const int J = J0 - H + r;
+        int I = I0 - H + c;
+        in_level(F, J, I);  // fluid, so inside the level; wraps I
+        const int cj = J >> 1, ci = I >> 1, oj = J & 1, oi = I & 1;
+        S v;
+        if (!oj && !oi) v = cval_g<S>(C, cj, ci);
+        else if (!oj) v = S(0.5) * (cval_g<S>(C, cj, ci) + cval_g<S>(C, cj, ci + 1));
+        else if (!oi) v = S(0.5) * (cval_g<S>(C, cj, ci) + cval_g<S>(C, cj + 1, ci));
+        else
+            v = S(0.25) * ((cval_g<S>(C, cj, ci) + cval_g<S>(C, cj, ci + 1)) +
+                           (cval_g<S>(C, cj + 1, ci) + cval_g<S>(C, cj + 1, ci + 1)));
+        sx[e] += v;
+    }
+    __syncthreads();
+    const S cx = Coef<S>::cx(F), cy = Coef<S>::cy(F), id = Coef<S>::idiag(F);
+#pragma unroll
+    for (int s = 1; s <= 2 * NU; ++s) {
+        half_sweep<S, W>(sx, sb, sm, s, s & 1, cx, cy, id);
+        __syncthreads();
+    }
+    S* x = lx<S>(F);
+    S acc = S(0);
+#pragma unroll
+    for (int qr = 0; qr < TQ; ++qr) {
+        const int r = threadIdx.y + 8 * qr, c = threadIdx.x;
+        const int J = J0 + r, I = I0 + c;
+        const int q = (r + H) * W + c + H;
+        if (J < F.nyn && I < F.nxn) {
+            x[nidx(F, J, I)] = sx[q];
+            if (RZ) acc += sb[q] * sx[q];  // 0 at non-fluid nodes
+        }
+    }
+    if (RZ) {
+        double w[1];
+        if (member_dot<S>(acc, w, partials, gpart, gtick, in, &sc.counter[2])) set_rz(sc, ir, w[0]);
+    }
 }
 
-template <typename S>
-__global__ void __launch_bounds__(256)
-k_bs_smooth(const int4* __restrict__ tiles, const BSInfo* __restrict__ info,
-            const MGLevel* __restrict__ levs, int l, int color,
-            const DevScalars* __restrict__ scs, int ir)
-{
-    const int4 tl = tiles[blockIdx.x];
-    if (info[tl.x].ltail <= l || bs_skip(scs[tl.x], ir)) return;
-    const MGLevel L = levs[tl.x * BS_LMAX + l];
-    tile_nodes(tl, L, [&](int J, int I) { op_smooth<S>(L, J, I, color, false); });
-}
-
+// Coarse levels of every member in one block each (tail_vcycle). A member
+// whose level 0 is already in the tail also forms <r, z> here.
 template <typename S>
 __global__ void __launch_bounds__(1024)
-k_bs_tail(const BSInfo* __restrict__ info, const MGLevel* __restrict__ levs,
-          const DevScalars* __restrict__ scs, int ir, int nu)
+k_bs_tail(const BSInfo* __restrict__ info, const MGLevel* __restrict__ levs, DevScalars* scs,
+          int ir, int nu)
 {
     const int b = blockIdx.x;
-    if (bs_skip(scs[b], ir)) return;
+    DevScalars& sc = scs[b];
+    if (bs_skip(sc, ir)) return;
     extern __shared__ __align__(16) unsigned char smem_raw[];
     __shared__ MGLevel sl[16];
     const BSInfo in = info[b];
     tail_vcycle<S>(&levs[b * BS_LMAX], in.ltail, in.nl, in.ksweeps, smem_raw, sl, nu);
+    if (in.ltail != 0) return;
+    const MGLevel D = sl[0];
+    const int n = D.nyn * D.nxn;
+    S acc = S(0);
+    for (int k = threadIdx.x; k < n; k += blockDim.x)
+        if (D.m[k]) acc += ((const S*)D.b)[k] * ((const S*)D.x)[k];
+    double w[1];
+    if constexpr (std::is_same<S, float>::value) {
+        const float a[1] = {acc};
+        block_total_f<1>(a, w);
+    } else {
+        __shared__ double sh[32];
+        w[0] = acc;
+        block_reduce<1, false>(w, sh);
+    }
+    if (threadIdx.x == 0) set_rz(sc, ir, w[0]);
 }
 
 // ---- Krylov kernels on level 0 ------------------------------------------------
-template <typename V>
-__device__ __forceinline__ V applyA(const MGLevel& L, const V* __restrict__ x, int J, int I,
-                                    long long k)
-{
-    return apply_off<V>(L, x, J, I) + Coef<V>::diag(L) * x[k];
-}
-
-// rz = <r, z>, beta = rz / rz_old (0 on the first iteration of a loop)
+// p = z (first iteration) or z + beta p_old, q = A p, <p, q>, alpha = rz/<p,q>.
+// p is formed on the tile and a one-node halo (the halo redundantly, from
+// z and p_old), so A p needs no second pass; p_old and p live in two
+// buffers chosen by the parity of the member's iteration count (p_old of
+// the halo belongs to other blocks and must not be overwritten meanwhile).
 template <typename S, typename V>
 __global__ void __launch_bounds__(256)
-k_bs_rz(const int4* __restrict__ tiles, const BSInfo* __restrict__ info,
-        const MGLevel* __restrict__ levs, const V* __restrict__ r, const S* __restrict__ z,
-        DevScalars* scs, double* partials, double* gpart, unsigned int* gtick, int ir)
+k_bs_pq(const int4* __restrict__ tiles, const BSInfo* __restrict__ info,
+        const MGLevel* __restrict__ levs, const S* __restrict__ z, V* __restrict__ p0,
+        V* __restrict__ p1, V* __restrict__ q, DevScalars* scs, double* partials, double* gpart,
+        unsigned int* gtick, int ir)
 {
+    constexpr int H = 1, W = BS_TW + 2, N = W * W, IT = (N + 255) / 256;
+    __shared__ V sp[N];
+    __shared__ uint8_t sm[N];
     const int4 tl = tiles[blockIdx.x];
     DevScalars& sc = scs[tl.x];
     if (bs_skip(sc, ir)) return;
-    const MGLevel L = levs[tl.x * BS_LMAX];
-    V acc = V(0);
-    tile_nodes(tl, L, [&](int J, int I) {
-        const long long k = nidx(L, J, I);
-        if (L.m[k]) acc += r[k] * V(z[k]);
-    });
-    double w[1];
-    block_dot<V>(acc, w);
     const BSInfo in = info[tl.x];
-    if (seg_reduce2<1, std::is_same<V, float>::value>(w, partials, gpart, gtick, blockIdx.x,
-                                                      in.n0, in.nn, in.g0, &sc.counter[2])) {
-        const int first = ir ? sc.iter_in == 0 : sc.iter == 0;
-        sc.beta = first ? 0.0 : w[0] / sc.rz;
-        sc.rz = w[0];
-    }
-}
-
-// p = z (first iteration) or z + beta p
-template <typename S, typename V>
-__global__ void __launch_bounds__(256)
-k_bs_p(const int4* __restrict__ tiles, const MGLevel* __restrict__ levs,
-       const S* __restrict__ z, V* __restrict__ p, const DevScalars* __restrict__ scs, int ir)
-{
-    const int4 tl = tiles[blockIdx.x];
-    const DevScalars& sc = scs[tl.x];
-    if (bs_skip(sc, ir)) return;
     const MGLevel L = levs[tl.x * BS_LMAX];
-    const int first = ir ? sc.iter_in == 0 : sc.iter == 0;
+    const int it = ir ? sc.iter_in : sc.iter;
+    const bool first = it == 0;
+    const V* __restrict__ pold = (it & 1) ? p1 : p0;
+    V* __restrict__ pnew = (it & 1) ? p0 : p1;
     const V beta = V(sc.beta);
-    tile_nodes(tl, L, [&](int J, int I) {
-        const long long k = nidx(L, J, I);
-        V v = V(0);
-        if (L.m[k]) v = first ? V(z[k]) : V(z[k]) + beta * p[k];
-        p[k] = v;
-    });
-}
-
-// q = A p, pq = <p, q>, alpha = rz / pq
-template <typename V>
-__global__ void __launch_bounds__(256)
-k_bs_spmv(const int4* __restrict__ tiles, const BSInfo* __restrict__ info,
-          const MGLevel* __restrict__ levs, const V* __restrict__ p, V* __restrict__ q,
-          DevScalars* scs, double* partials, double* gpart, unsigned int* gtick, int ir)
-{
-    const int4 tl = tiles[blockIdx.x];
-    DevScalars& sc = scs[tl.x];
-    if (bs_skip(sc, ir)) return;
-    const MGLevel L = levs[tl.x * BS_LMAX];
-    V acc = V(0);
-    tile_nodes(tl, L, [&](int J, int I) {
-        const long long k = nidx(L, J, I);
-        V qv = V(0);
-        if (L.m[k]) {
-            qv = applyA<V>(L, p, J, I, k);
-            acc += p[k] * qv;
+    const int I0 = tl.y, J0 = tl.z, t = tid256();
+#pragma unroll
+    for (int k2 = 0; k2 < IT; ++k2) {
+        const int e = t + k2 * 256;
+        if (e < N) {
+            const int r = e / W, c = e - r * W;
+            const int J = J0 - H + r;
+            int I = I0 - H + c;
+            uint8_t mv = 0;
+            V zv = V(0), pv = V(0);
+            if (in_level(L, J, I)) {
+                const long long k = nidx(L, J, I);
+                mv = L.m[k];
+                zv = V(z[k]);
+                if (!first) pv = pold[k];
+            }
+            sm[e] = mv;
+            sp[e] = mv ? (first ? zv : zv + beta * pv) : V(0);
         }
-        q[k] = qv;
-    });
+    }
+    __syncthreads();
+    const V cx = Coef<V>::cx(L), cy = Coef<V>::cy(L), d = Coef<V>::diag(L);
+    V acc = V(0);
+#pragma unroll
+    for (int qr = 0; qr < TQ; ++qr) {
+        const int r = threadIdx.y + 8 * qr, c = threadIdx.x;
+        const int J = J0 + r, I = I0 + c;
+        const int e = (r + H) * W + c + H;
+        const V pv = sp[e];
+        V qv = V(0);
+        if (sm[e]) qv = (cx * (sp[e - 1] + sp[e + 1]) + cy * (sp[e - W] + sp[e + W])) + d * pv;
+        if (J < L.nyn && I < L.nxn) {  // (a wrapped periodic column is not the tile's)
+            const long long k = nidx(L, J, I);
+            pnew[k] = pv;
+            q[k] = qv;
+            acc += pv * qv;
+        }
+    }
     double w[1];
-    block_dot<V>(acc, w);
-    const BSInfo in = info[tl.x];
-    if (seg_reduce2<1, std::is_same<V, float>::value>(w, partials, gpart, gtick, blockIdx.x,
-                                                      in.n0, in.nn, in.g0, &sc.counter[3])) {
+    if (member_dot<V>(acc, w, partials, gpart, gtick, in, &sc.counter[3])) {
         sc.pq = w[0];
         sc.alpha = sc.rz / w[0];
     }
@@ -234,40 +435,54 @@ template <typename V>
 __global__ void __launch_bounds__(256)
 k_bs_xr(const int4* __restrict__ tiles, const BSInfo* __restrict__ info,
         const MGLevel* __restrict__ levs, V* __restrict__ x, V* __restrict__ r,
-        const V* __restrict__ p, const V* __restrict__ q, DevScalars* scs, double* partials,
-        double* gpart, unsigned int* gtick, BSGlobals* eg, cudaGraphConditionalHandle cond,
-        int ir, int nmem)
+        const V* __restrict__ p0, const V* __restrict__ p1, const V* __restrict__ q,
+        DevScalars* scs, double* partials, double* gpart, unsigned int* gtick, BSGlobals* eg,
+        cudaGraphConditionalHandle cond, int ir, int nmem)
 {
     const int4 tl = tiles[blockIdx.x];
     DevScalars& sc = scs[tl.x];
+    const BSInfo in = info[tl.x];
     bool mine = false;
     if (bs_skip(sc, ir)) {
-        mine = threadIdx.x == 0 && threadIdx.y == 0 && (int)blockIdx.x == info[tl.x].n0;
+        mine = threadIdx.x == 0 && threadIdx.y == 0 && (int)blockIdx.x == in.n0;
     } else {
         const MGLevel L = levs[tl.x * BS_LMAX];
         const int zero = ir ? 0 : sc.pad1;
-        const int first = ir && sc.iter_in == 0;
+        const int it = ir ? sc.iter_in : sc.iter;
+        const bool first = ir && it == 0;
+        const V* __restrict__ p = (it & 1) ? p0 : p1;  // written by k_bs_pq
         const V a = V(sc.alpha);
+        long long k[TQ];
+        bool ok[TQ];
+        uint8_t mv[TQ];
+        V xv[TQ], pv[TQ], rv[TQ], qv[TQ];
+#pragma unroll
+        for (int qr = 0; qr < TQ; ++qr) {
+            const int J = tl.z + threadIdx.y + 8 * qr, I = tl.y + threadIdx.x;
+            ok[qr] = J < L.nyn && I < L.nxn;
+            k[qr] = nidx(L, min(J, L.nyn - 1), min(I, L.nxn - 1));
+            mv[qr] = L.m[k[qr]];
+            xv[qr] = first ? V(0) : x[k[qr]];
+            pv[qr] = p[k[qr]];
+            rv[qr] = r[k[qr]];
+            qv[qr] = q[k[qr]];
+        }
         V acc = V(0);
-        tile_nodes(tl, L, [&](int J, int I) {
-            const long long k = nidx(L, J, I);
-            if (!L.m[k]) return;
+#pragma unroll
+        for (int qr = 0; qr < TQ; ++qr) {
+            if (!ok[qr] || !mv[qr]) continue;
             if (zero) {
-                x[k] = V(0);
-                r[k] = V(0);
-                return;
+                x[k[qr]] = V(0);
+                r[k[qr]] = V(0);
+                continue;
             }
-            x[k] = (first ? V(0) : x[k]) + a * p[k];
-            const V rv = r[k] - a * q[k];
-            r[k] = rv;
-            acc += rv * rv;
-        });
+            x[k[qr]] = xv[qr] + a * pv[qr];
+            const V rn = rv[qr] - a * qv[qr];
+            r[k[qr]] = rn;
+            acc += rn * rn;
+        }
         double w[1];
-        block_dot<V>(acc, w);
-        const BSInfo in = info[tl.x];
-        mine = seg_reduce2<1, std::is_same<V, float>::value>(w, partials, gpart, gtick,
-                                                             blockIdx.x, in.n0, in.nn, in.g0,
-                                                             &sc.counter[4]);
+        mine = member_dot<V>(acc, w, partials, gpart, gtick, in, &sc.counter[4]);
         if (mine) {
             sc.total_iters += 1;
             const bool bad = !(w[0] == w[0]);
@@ -300,6 +515,48 @@ k_bs_xr(const int4* __restrict__ tiles, const BSInfo* __restrict__ info,
     }
 }
 
+// FP64 residual r = b - A x of the tile (x staged with a one-node halo);
+// the per-thread sums of b*b and r*r; optionally the FP32 copy of r.
+__device__ __forceinline__ void residual64(const int4& tl, const MGLevel& L,
+                                           const double* __restrict__ x,
+                                           const double* __restrict__ b, double* __restrict__ r,
+                                           float* __restrict__ rin, double (&w)[2])
+{
+    constexpr int H = 1, W = BS_TW + 2, N = W * W;
+    __shared__ double sx[N];
+    __shared__ uint8_t sm[N];
+    stage_region<H, double, double>(L, tl.z, tl.y, x, sx, (const double*)nullptr,
+                                    (double*)nullptr, sm);
+    double bv[TQ];
+    long long k[TQ];
+    bool ok[TQ];
+#pragma unroll
+    for (int qr = 0; qr < TQ; ++qr) {
+        const int J = tl.z + threadIdx.y + 8 * qr, I = tl.y + threadIdx.x;
+        ok[qr] = J < L.nyn && I < L.nxn;
+        k[qr] = nidx(L, min(J, L.nyn - 1), min(I, L.nxn - 1));
+        bv[qr] = b[k[qr]];
+    }
+    __syncthreads();
+    const double cx = L.cx, cy = L.cy, d = L.diag;
+#pragma unroll
+    for (int qr = 0; qr < TQ; ++qr) {
+        const int rr = threadIdx.y + 8 * qr, c = threadIdx.x;
+        const int e = (rr + H) * W + c + H;
+        double rv = 0.0;
+        if (sm[e] && ok[qr]) {
+            rv = bv[qr] - ((cx * (sx[e - 1] + sx[e + 1]) + cy * (sx[e - W] + sx[e + W])) +
+                           d * sx[e]);
+            w[0] += bv[qr] * bv[qr];
+            w[1] += rv * rv;
+        }
+        if (ok[qr]) {
+            r[k[qr]] = rv;
+            if (rin) rin[k[qr]] = float(rv);
+        }
+    }
+}
+
 // FP64 form: r = b - A x, <b,b>, <r,r>, per-member start state
 __global__ void __launch_bounds__(256)
 k_bs_init(const int4* __restrict__ tiles, const BSInfo* __restrict__ info,
@@ -312,17 +569,7 @@ k_bs_init(const int4* __restrict__ tiles, const BSInfo* __restrict__ info,
     DevScalars& sc = scs[tl.x];
     const MGLevel L = levs[tl.x * BS_LMAX];
     double w[2] = {0.0, 0.0};
-    tile_nodes(tl, L, [&](int J, int I) {
-        const long long k = nidx(L, J, I);
-        double rv = 0.0;
-        if (L.m[k]) {
-            const double bv = b[k];
-            rv = bv - applyA<double>(L, x, J, I, k);
-            w[0] += bv * bv;
-            w[1] += rv * rv;
-        }
-        r[k] = rv;
-    });
+    residual64(tl, L, x, b, r, nullptr, w);
     const BSInfo in = info[tl.x];
     const bool mine = seg_reduce2<2>(w, partials, gpart, gtick, blockIdx.x, in.n0, in.nn, in.g0, &sc.counter[1]);
     if (mine) {
@@ -357,18 +604,7 @@ k_bs_refine(const int4* __restrict__ tiles, const BSInfo* __restrict__ info,
     } else {
         const MGLevel L = levs[tl.x * BS_LMAX];
         double w[2] = {0.0, 0.0};
-        tile_nodes(tl, L, [&](int J, int I) {
-            const long long k = nidx(L, J, I);
-            double rv = 0.0;
-            if (L.m[k]) {
-                const double bv = b[k];
-                rv = bv - applyA<double>(L, x, J, I, k);
-                w[0] += bv * bv;
-                w[1] += rv * rv;
-            }
-            r[k] = rv;
-            rin[k] = float(rv);
-        });
+        residual64(tl, L, x, b, r, rin, w);
         const BSInfo in = info[tl.x];
         mine = seg_reduce2<2>(w, partials, gpart, gtick, blockIdx.x, in.n0, in.nn, in.g0, &sc.counter[1]);
         if (mine) {
@@ -421,10 +657,23 @@ k_bs_correct(const int4* __restrict__ tiles, const MGLevel* __restrict__ levs,
     if (sc.converged) return;
     const MGLevel L = levs[tl.x * BS_LMAX];
     const int zero = sc.zero;
-    tile_nodes(tl, L, [&](int J, int I) {
-        const long long k = nidx(L, J, I);
-        if (L.m[k]) x[k] = zero ? 0.0 : x[k] + (double)e[k];
-    });
+    long long k[TQ];
+    bool ok[TQ];
+    uint8_t mv[TQ];
+    double xv[TQ];
+    float ev[TQ];
+#pragma unroll
+    for (int qr = 0; qr < TQ; ++qr) {
+        const int J = tl.z + threadIdx.y + 8 * qr, I = tl.y + threadIdx.x;
+        ok[qr] = J < L.nyn && I < L.nxn;
+        k[qr] = nidx(L, min(J, L.nyn - 1), min(I, L.nxn - 1));
+        mv[qr] = L.m[k[qr]];
+        xv[qr] = x[k[qr]];
+        ev[qr] = e[k[qr]];
+    }
+#pragma unroll
+    for (int qr = 0; qr < TQ; ++qr)
+        if (ok[qr] && mv[qr]) x[k[qr]] = zero ? 0.0 : xv[qr] + (double)ev[qr];
 }
 
 __global__ void k_bs_setup(DevScalars* scs, int n, double tol2, int maxit, double tol_in2,
@@ -475,33 +724,37 @@ static bool bs_eager()
     return v == 1;
 }
 
-// one V-cycle for all members still iterating
-template <typename S>
-static int vcycle(BatchSolver& s, cudaStream_t st, int ir)
+// one V-cycle for all members still iterating: a down kernel per grid level,
+// the tail, an up kernel per grid level (the level-0 one also forms <r, z>)
+template <typename S, int NU>
+static int vcycle_nu(BatchSolver& s, cudaStream_t st, int ir)
 {
     const dim3 blk(32, 8);
     int cnt = 0;
     for (int l = 0; l < s.maxl; ++l) {
-        k_bs_presmooth<S><<<s.ntiles[l], blk, 0, st>>>(s.tiles[l], s.dinfo, s.dlevs, l, s.scs, ir);
-        for (int k = 1; k < s.nu; ++k) {
-            k_bs_smooth<S><<<s.ntiles[l], blk, 0, st>>>(s.tiles[l], s.dinfo, s.dlevs, l, 0, s.scs, ir);
-            k_bs_smooth<S><<<s.ntiles[l], blk, 0, st>>>(s.tiles[l], s.dinfo, s.dlevs, l, 1, s.scs, ir);
-        }
-        k_bs_restrict<S><<<s.ntiles[l + 1], blk, 0, st>>>(s.tiles[l + 1], s.dinfo, s.dlevs, l,
-                                                          s.scs, ir);
-        cnt += 2 + 2 * (s.nu - 1);
+        k_bs_down<S, NU><<<s.ntiles[l], blk, 0, st>>>(s.tiles[l], s.dinfo, s.dlevs, l, s.scs, ir);
+        cnt += 1;
     }
-    k_bs_tail<S><<<s.n, 1024, s.tail_smem, st>>>(s.dinfo, s.dlevs, s.scs, ir, s.nu);
+    k_bs_tail<S><<<s.n, 1024, s.tail_smem, st>>>(s.dinfo, s.dlevs, s.scs, ir, NU);
     cnt += 1;
-    for (int l = s.maxl - 1; l >= 0; --l) {
-        k_bs_prolong<S><<<s.ntiles[l], blk, 0, st>>>(s.tiles[l], s.dinfo, s.dlevs, l, s.scs, ir);
-        for (int k = 0; k < s.nu; ++k) {
-            k_bs_smooth<S><<<s.ntiles[l], blk, 0, st>>>(s.tiles[l], s.dinfo, s.dlevs, l, 1, s.scs, ir);
-            k_bs_smooth<S><<<s.ntiles[l], blk, 0, st>>>(s.tiles[l], s.dinfo, s.dlevs, l, 0, s.scs, ir);
-        }
-        cnt += 1 + 2 * s.nu;
+    for (int l = s.maxl - 1; l >= 1; --l) {
+        k_bs_up<S, NU, false><<<s.ntiles[l], blk, 0, st>>>(s.tiles[l], s.dinfo, s.dlevs, l,
+                                                          s.scs, ir, s.partials, s.gpart,
+                                                          s.gtick);
+        cnt += 1;
+    }
+    if (s.maxl > 0) {
+        k_bs_up<S, NU, true><<<s.ntiles[0], blk, 0, st>>>(s.tiles[0], s.dinfo, s.dlevs, 0, s.scs,
+                                                         ir, s.partials, s.gpart, s.gtick);
+        cnt += 1;
     }
     return cnt;
+}
+
+template <typename S>
+static int vcycle(BatchSolver& s, cudaStream_t st, int ir)
+{
+    return s.nu >= 2 ? vcycle_nu<S, 2>(s, st, ir) : vcycle_nu<S, 1>(s, st, ir);
 }
 
 // the CG loop body; FP64 form (S = V = double) or the inner FP32 loop
@@ -513,15 +766,13 @@ static int cg_body(BatchSolver& s, cudaStream_t st, cudaGraphConditionalHandle c
     V* r = (V*)(ir ? s.v.rin : s.v.r64);
     V* x = (V*)(ir ? s.v.e : s.v.x64);
     int cnt = vcycle<S>(s, st, ir);
-    k_bs_rz<S, V><<<nt, blk, 0, st>>>(s.rtiles, s.dinfo, s.dlevs, r, (const S*)s.v.z, s.scs,
-                                      s.partials, s.gpart, s.gtick, ir);
-    k_bs_p<S, V><<<nt, blk, 0, st>>>(s.rtiles, s.dlevs, (const S*)s.v.z, (V*)s.v.p, s.scs, ir);
-    k_bs_spmv<V><<<nt, blk, 0, st>>>(s.rtiles, s.dinfo, s.dlevs, (const V*)s.v.p, (V*)s.v.q,
-                                     s.scs, s.partials, s.gpart, s.gtick, ir);
+    k_bs_pq<S, V><<<nt, blk, 0, st>>>(s.rtiles, s.dinfo, s.dlevs, (const S*)s.v.z, (V*)s.v.p,
+                                      (V*)s.v.p2, (V*)s.v.q, s.scs, s.partials, s.gpart,
+                                      s.gtick, ir);
     k_bs_xr<V><<<nt, blk, 0, st>>>(s.rtiles, s.dinfo, s.dlevs, x, r, (const V*)s.v.p,
-                                   (const V*)s.v.q, s.scs, s.partials, s.gpart, s.gtick, s.eg, cond, ir,
-                                   s.n);
-    cnt += 4;
+                                   (const V*)s.v.p2, (const V*)s.v.q, s.scs, s.partials,
+                                   s.gpart, s.gtick, s.eg, cond, ir, s.n);
+    cnt += 2;
     s.body_launches = cnt;
     return (int)cudaGetLastError();
 }
@@ -696,7 +947,7 @@ int bs_build(BatchSolver& s, const std::vector<BSMemberDesc>& members, const uin
         // level 0 of the multigrid: x = z, b = the residual driving the cycle
         void* r0 = mode == 0 ? v.r64 : v.rin;
         int e = mg_build(s.mg[b], d.nyn, d.nxn, d.pitch, d.off0, d.per, d.hmask, d.hoff0, dmask,
-                         v.z, r0, d.cx, d.cy, d.maindiag, mode == 0 ? 0 : 1);
+                         v.z, v.za, r0, d.cx, d.cy, d.maindiag, mode == 0 ? 0 : 1);
         if (e) return e;
         const int nl = (int)s.mg[b].lev.size();
         if (nl > BS_LMAX) return 5;
@@ -708,64 +959,62 @@ int bs_build(BatchSolver& s, const std::vector<BSMemberDesc>& members, const uin
         s.tail_smem = std::max(s.tail_smem, s.mg[b].tail_smem);
         for (int l = 0; l < nl; ++l) levs[(size_t)b * BS_LMAX + l] = s.mg[b].lev[l];
     }
-    // Tiles of 32 x 8R nodes (R rows per thread): R = 4 when a level holds
-    // enough nodes to fill the GPU several times over (fewer, fuller blocks),
-    // R = 1 otherwise (more blocks for small levels).
-    std::vector<std::vector<int4>> tiles(s.maxl + 1);
-    for (int l = 0; l <= s.maxl; ++l) {
-        long long nodes = 0;
-        for (int b = 0; b < s.n; ++b)
-            if (l <= info[b].ltail)
-                nodes += (long long)levs[(size_t)b * BS_LMAX + l].nyn *
-                         levs[(size_t)b * BS_LMAX + l].nxn;
-        const int R = nodes >= 4ll * 1024 * 1024 ? 4 : 1;
-        for (int b = 0; b < s.n; ++b) {
-            if (l > info[b].ltail) continue;
-            const MGLevel& L = levs[(size_t)b * BS_LMAX + l];
-            for (int J0 = 0; J0 < L.nyn; J0 += 8 * R)
-                for (int I0 = 0; I0 < L.nxn; I0 += BS_TW) tiles[l].push_back(make_int4(b, I0, J0, R));
-        }
-    }
-    // Level-0 tiles of the Krylov kernels (32 x 8 nodes), with the member's
-    // reduction groups of 64 tiles.
-    std::vector<int4> rt;
+    // Tile tables of 32 x 32 nodes. Level 0 (all members; the Krylov
+    // kernels and the first multigrid level) with the members' reduction
+    // groups of RED_GROUP tiles; level l >= 1 for the members whose grid
+    // levels reach below it. Tiles without a fluid node are left out (their
+    // nodes stay 0 in every vector), but every member keeps at least one
+    // level-0 tile for its reductions.
+    auto has_fluid = [&](int b, int l, int J0, int I0) {
+        const std::vector<uint8_t>& hm = s.mg[b].hmask[l];
+        const MGLevel& L = levs[(size_t)b * BS_LMAX + l];
+        for (int J = J0; J < std::min(L.nyn, J0 + BS_TH); ++J)
+            for (int I = I0; I < std::min(L.nxn, I0 + BS_TW); ++I)
+                if (hm[(size_t)J * L.nxn + I]) return true;
+        return false;
+    };
+    std::vector<std::vector<int4>> tiles(std::max(1, s.maxl));
+    std::vector<int4>& rt = tiles[0];
     int ngroups = 0;
     for (int b = 0; b < s.n; ++b) {
         const MGLevel& L = levs[(size_t)b * BS_LMAX];
-        const long long cols = (L.nxn + BS_TW - 1) / BS_TW;
-        const long long rows8 = (L.nyn + 7) / 8;
-        const int R = 1;
-        (void)cols;
-        (void)rows8;
         info[b].n0 = (int)rt.size();
-        for (int J0 = 0; J0 < L.nyn; J0 += 8 * R)
-            for (int I0 = 0; I0 < L.nxn; I0 += BS_TW) rt.push_back(make_int4(b, I0, J0, R));
+        for (int J0 = 0; J0 < L.nyn; J0 += BS_TH)
+            for (int I0 = 0; I0 < L.nxn; I0 += BS_TW)
+                if (has_fluid(b, 0, J0, I0)) rt.push_back(make_int4(b, I0, J0, 0));
+        if ((int)rt.size() == info[b].n0) rt.push_back(make_int4(b, 0, 0, 0));
         info[b].nn = (int)rt.size() - info[b].n0;
         info[b].g0 = ngroups;
         ngroups += (info[b].nn + RED_GROUP - 1) / RED_GROUP;
     }
+    for (int l = 1; l < s.maxl; ++l)
+        for (int b = 0; b < s.n; ++b) {
+            if (info[b].ltail <= l) continue;
+            const MGLevel& L = levs[(size_t)b * BS_LMAX + l];
+            for (int J0 = 0; J0 < L.nyn; J0 += BS_TH)
+                for (int I0 = 0; I0 < L.nxn; I0 += BS_TW)
+                    if (has_fluid(b, l, J0, I0)) tiles[l].push_back(make_int4(b, I0, J0, 0));
+        }
     auto dal = [&](size_t bytes) -> void* {
         void* p = nullptr;
         if (cudaMalloc(&p, bytes) != cudaSuccess) return nullptr;
         s.owned.push_back(p);
         return p;
     };
-    s.tiles.assign(s.maxl + 1, nullptr);
-    s.ntiles.assign(s.maxl + 1, 0);
-    for (int l = 0; l <= s.maxl; ++l) {
+    const int ntab = (int)tiles.size();
+    s.tiles.assign(ntab, nullptr);
+    s.ntiles.assign(ntab, 0);
+    for (int l = 0; l < ntab; ++l) {
         s.ntiles[l] = (int)tiles[l].size();
         s.tiles[l] = (int4*)dal(std::max<size_t>(1, tiles[l].size()) * sizeof(int4));
         if (!s.tiles[l]) return 2;
-        if (cudaMemcpy(s.tiles[l], tiles[l].data(), tiles[l].size() * sizeof(int4),
+        if (!tiles[l].empty() &&
+            cudaMemcpy(s.tiles[l], tiles[l].data(), tiles[l].size() * sizeof(int4),
                        cudaMemcpyHostToDevice) != cudaSuccess)
             return 2;
     }
-    s.nrtiles = (int)rt.size();
-    s.rtiles = (int4*)dal(rt.size() * sizeof(int4));
-    if (!s.rtiles ||
-        cudaMemcpy(s.rtiles, rt.data(), rt.size() * sizeof(int4), cudaMemcpyHostToDevice) !=
-            cudaSuccess)
-        return 2;
+    s.nrtiles = s.ntiles[0];
+    s.rtiles = s.tiles[0];
     s.dlevs = (MGLevel*)dal(levs.size() * sizeof(MGLevel));
     s.dinfo = (BSInfo*)dal(info.size() * sizeof(BSInfo));
     s.eg = (BSGlobals*)dal(sizeof(BSGlobals));

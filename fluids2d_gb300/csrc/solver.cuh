@@ -32,8 +32,10 @@ struct BSVecs {
     void* b64;  // right-hand side (FP64)
     void* r64;  // FP64 residual
     void* p;    // CG direction (FP64 form: double; refinement: float)
+    void* p2;   // second CG direction buffer (p alternates between the two)
     void* q;    // A p (same precision as p)
     void* z;    // preconditioned residual, multigrid precision
+    void* za;   // level-0 multigrid x after the pre-smoothing (as z)
     void* rin;  // inner residual of the refinement form (float), multigrid rhs
     void* e;    // inner correction of the refinement form (float)
 };
