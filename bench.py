@@ -378,6 +378,36 @@ def _ensemble_time(e, steps, warmup, stream, flush, dev, world):
     return ms, st0, st, clk.summary()
 
 
+def plain_fp64_ms_per_step(members, stream, flush, steps=3, warmup=2, stride=4):
+    """Time of one ensemble step in the plain FP64 form: every member as its
+    own single FP64 model, advanced one after another (no batching). Times a
+    systematic sample (every `stride`-th member; the members are independent
+    draws) with CUDA events and scales the summed per-step time to all
+    members. Returns (ms per ensemble step, members timed)."""
+    import ctypes
+    import torch
+    from fluids2d_gb300._lib import check, lib
+    L = lib()
+    sample = members[::stride]
+    tot = 0.0
+    for c in sample:
+        m = make_gpu_model("eulerpsi", c, ctypes.c_void_p(stream.cuda_stream), "fp64")
+        for _ in range(warmup):
+            check(L.f2d_run(m._h, 1))
+        check(L.f2d_sync(m._h))
+        ev0 = [torch.cuda.Event(enable_timing=True) for _ in range(steps)]
+        ev1 = [torch.cuda.Event(enable_timing=True) for _ in range(steps)]
+        for k in range(steps):
+            flush.zero_()
+            ev0[k].record(stream)
+            check(L.f2d_run(m._h, 1))
+            ev1[k].record(stream)
+        torch.cuda.synchronize()
+        tot += sum(a.elapsed_time(b) for a, b in zip(ev0, ev1)) / steps
+        del m
+    return tot * len(members) / len(sample), len(sample)
+
+
 def run_gpu_ensemble(args, rank, world):
     import ctypes
     import torch
@@ -418,6 +448,13 @@ def run_gpu_ensemble(args, rank, world):
                      "omega_rel_l2_fp32_vs_fp64": (num / den) ** 0.5,
                      "steps": args.warmup + args.steps}
         del e64
+        pms, nsamp = plain_fp64_ms_per_step(members, stream, flush)
+        fp64_form["plain_fp64_per_member"] = {
+            "value": world * cells / (pms / 1e3), "ms_per_step": pms,
+            "speedup_fp32_refine_batched_vs_plain_fp64": pms / (ms / args.steps),
+            "sample": f"{nsamp} of {len(members)} members (every 4th), each a "
+                      "single FP64 model, 2 warm-up + 3 timed steps, summed "
+                      "per-step times scaled to all members"}
     # end to end: every member's vorticity from pinned host memory and back
     host = []
     for b, c in enumerate(members):

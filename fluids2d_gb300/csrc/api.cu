@@ -228,7 +228,7 @@ static int ensure_mg(f2d_model_s* m, int which)
     bs.tol_in = env_double("F2D_TOL_IN", 1e-4);
     bs.maxit_in = (int)env_double("F2D_MAXIT_IN", 30);
     bs.maxouter = std::max(2, m->p.poisson_maxit / 10);
-    bs.nu = (int)env_double("F2D_NU", 1);
+    bs.nu = (int)env_double("F2D_NU", 2);
     m->bs_ready[which] = true;
     return 0;
 }

@@ -524,7 +524,7 @@ int f2d_ensemble_create(const f2d_params* p, int count, const int* nxs, const in
         e->bs.tol_in = (ti && *ti) ? atof(ti) : 1e-4;
         e->bs.maxouter = std::max(2, p->poisson_maxit / 10);
         const char* nu = getenv("F2D_NU");
-        e->bs.nu = (nu && *nu) ? atoi(nu) : 1;
+        e->bs.nu = (nu && *nu) ? atoi(nu) : 2;
     }
     e->ncell = (int)cells.size();
     e->cell_tiles = (int4*)ens_alloc(e, cells.size() * sizeof(int4));

@@ -191,13 +191,32 @@ k_bs_down(const int4* __restrict__ tiles, const BSInfo* __restrict__ info,
     if (info[tl.x].ltail <= l || bs_skip(scs[tl.x], ir)) return;
     const MGLevel F = levs[tl.x * BS_LMAX + l];
     const int I0 = tl.y, J0 = tl.z, t = tid256();
-    stage_region<H, S, S>(F, J0, I0, lb<S>(F), sb, (const S*)nullptr, (S*)nullptr, sm);
-    __syncthreads();
     const S cx = Coef<S>::cx(F), cy = Coef<S>::cy(F), d = Coef<S>::diag(F),
             id = Coef<S>::idiag(F);
-    for (int e = t; e < N; e += 256) {
-        const int r = e / W, c = e - r * W;
-        sx[e] = (((r + c) & 1) == 0) ? sb[e] * id : S(0);  // sb is 0 at non-fluid nodes
+    {
+        // stage b and the mask; x = b/diag on red fluid nodes, 0 elsewhere
+        constexpr int IT = (N + 255) / 256;
+        const S* __restrict__ gb = lb<S>(F);
+#pragma unroll
+        for (int k2 = 0; k2 < IT; ++k2) {
+            const int e = t + k2 * 256;
+            if (e < N) {
+                const int r = e / W, c = e - r * W;
+                const int J = J0 - H + r;
+                int I = I0 - H + c;
+                uint8_t mv = 0;
+                S bv = S(0);
+                if (in_level(F, J, I)) {
+                    const long long k = nidx(F, J, I);
+                    mv = F.m[k];
+                    bv = gb[k];
+                }
+                bv = mv ? bv : S(0);
+                sm[e] = mv;
+                sb[e] = bv;
+                sx[e] = (((r + c) & 1) == 0) ? bv * id : S(0);
+            }
+        }
     }
     __syncthreads();
 #pragma unroll
@@ -247,23 +266,14 @@ k_bs_down(const int4* __restrict__ tiles, const BSInfo* __restrict__ info,
     }
 }
 
-// coarse value for the prolongation (0 outside the level; x is 0 at
-// non-fluid nodes)
-template <typename S>
-__device__ __forceinline__ S cval_g(const MGLevel& C, int J, int I)
-{
-    if (J < 0 || J >= C.nyn) return S(0);
-    if (I >= C.nxn) {
-        if (!C.per) return S(0);
-        I -= C.nxn;
-    }
-    return lx<S>(C)[nidx(C, J, I)];
-}
-
 // Up leg of level l: x = xa + P (coarse x), then NU (black, red)
-// post-smoothing sweeps; writes x of the tile. On level 0 (RZ) the block
-// also forms its part of <r, z> (r = b, z = x) and the member's last block
-// sets rz and beta.
+// post-smoothing sweeps; writes x of the tile. The coarse nodes the region
+// interpolates from (rows and columns (J0-H)/2 .. (J0+31+H)/2 + 1) are staged
+// too: 0 outside the coarse level and at non-fluid nodes, wrapped when
+// x-periodic (an even fine period makes the wrapped fine node's coarse
+// neighbours the wrapped coarse ones). On level 0 (RZ) the block also forms
+// its part of <r, z> (r = b, z = x) and the member's last block sets rz and
+// beta.
 template <typename S, int NU, bool RZ>
 __global__ void __launch_bounds__(256)
 k_bs_up(const int4* __restrict__ tiles, const BSInfo* __restrict__ info,
@@ -271,8 +281,10 @@ k_bs_up(const int4* __restrict__ tiles, const BSInfo* __restrict__ info,
         double* gpart, unsigned int* gtick)
 {
     constexpr int H = 2 * NU, W = BS_TW + 2 * H, N = W * W;
+    constexpr int CW = BS_TW / 2 + 1 + H, CN = CW * CW, CIT = (CN + 255) / 256;
     __shared__ S sx[N];
     __shared__ S sb[N];
+    __shared__ S sc2[CN];
     __shared__ uint8_t sm[N];
     const int4 tl = tiles[blockIdx.x];
     DevScalars& sc = scs[tl.x];
@@ -281,22 +293,35 @@ k_bs_up(const int4* __restrict__ tiles, const BSInfo* __restrict__ info,
     const MGLevel F = levs[tl.x * BS_LMAX + l];
     const MGLevel C = levs[tl.x * BS_LMAX + l + 1];
     const int I0 = tl.y, J0 = tl.z, t = tid256();
+    const int cj0 = (J0 - H) >> 1, ci0 = (I0 - H) >> 1;
+    {
+        const S* __restrict__ cxg = lx<S>(C);
+#pragma unroll
+        for (int k2 = 0; k2 < CIT; ++k2) {
+            const int e = t + k2 * 256;
+            if (e < CN) {
+                const int r = e / CW, c = e - r * CW;
+                int I = ci0 + c;
+                S v = S(0);
+                if (in_level(C, cj0 + r, I)) v = cxg[nidx(C, cj0 + r, I)];
+                sc2[e] = v;
+            }
+        }
+    }
     stage_region<H, S, S>(F, J0, I0, (const S*)F.xa, sx, lb<S>(F), sb, sm);
     __syncthreads();
     for (int e = t; e < N; e += 256) {
         if (!sm[e]) continue;
         const int r = e / W, c = e - r * W;
-        const int J = J0 - H + r;
-        int I = I0 - H + c;
-        in_level(F, J, I);  // fluid, so inside the level; wraps I
-        const int cj = J >> 1, ci = I >> 1, oj = J & 1, oi = I & 1;
+        // coarse indices relative to the staged coarse region
+        const int J = J0 - H + r, I = I0 - H + c;
+        const int q = ((J >> 1) - cj0) * CW + ((I >> 1) - ci0);
+        const int oj = J & 1, oi = I & 1;
         S v;
-        if (!oj && !oi) v = cval_g<S>(C, cj, ci);
-        else if (!oj) v = S(0.5) * (cval_g<S>(C, cj, ci) + cval_g<S>(C, cj, ci + 1));
-        else if (!oi) v = S(0.5) * (cval_g<S>(C, cj, ci) + cval_g<S>(C, cj + 1, ci));
-        else
-            v = S(0.25) * ((cval_g<S>(C, cj, ci) + cval_g<S>(C, cj, ci + 1)) +
-                           (cval_g<S>(C, cj + 1, ci) + cval_g<S>(C, cj + 1, ci + 1)));
+        if (!oj && !oi) v = sc2[q];
+        else if (!oj) v = S(0.5) * (sc2[q] + sc2[q + 1]);
+        else if (!oi) v = S(0.5) * (sc2[q] + sc2[q + CW]);
+        else v = S(0.25) * ((sc2[q] + sc2[q + 1]) + (sc2[q + CW] + sc2[q + CW + 1]));
         sx[e] += v;
     }
     __syncthreads();

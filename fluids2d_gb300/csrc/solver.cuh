@@ -69,7 +69,7 @@ struct BatchSolver {
     BSVecs v;
     double tol = 1e-12, tol_in = 1e-4;
     int maxit = 200, maxit_in = 30, maxouter = 20;
-    int nu = 1;  // red-black sweeps before and after each coarse correction
+    int nu = 2;  // red-black sweeps before and after each coarse correction (1 or 2)
     int body_launches = 0;
     std::vector<void*> owned;
 };
