@@ -95,7 +95,7 @@ def build_case(name):
     return model, case, desc
 
 
-def make_gpu_model(model, case, stream_ptr, precision="fp64"):
+def make_gpu_model(model, case, stream_ptr, precision="fp64", tol=None):
     import fluids2d_gb300 as f2d
     from fluids2d_gb300._lib import check, lib
     p = f2d.Param()
@@ -111,6 +111,8 @@ def make_gpu_model(model, case, stream_ptr, precision="fp64"):
     p.tend = 1e300
     p.maxite = 10 ** 12
     p.precision = precision
+    if tol is not None:
+        p.poisson_tol = tol
     m = f2d.Model(p)
     check(lib().f2d_model_set_stream(m._h, stream_ptr))
     m.mesh.msk[:] = case["msk"]
@@ -533,7 +535,121 @@ def run_gpu_ensemble(args, rank, world):
         print(json.dumps(line), flush=True)
 
 
+def run_gpu_adjoint(args, rank, world):
+    """Differentiation workload: eulerpsi 512x512 closed basin, loss = final
+    enstrophy + L2 misfit to a seeded target after 400 fixed-dt steps,
+    gradient w.r.t. the initial vorticity through the adjoint kernels with
+    checkpoints every 20 steps; FP32 forward (FP64-refined Poisson) by
+    default. Reports the gradient throughput, the cost of forward+backward
+    relative to a plain forward of the same steps, the FP32 gradient against
+    the FP64 one, and the FP64 gradient against central finite differences
+    along random directions."""
+    import ctypes
+    import torch
+    from fluids2d_gb300 import workloads as wl
+    from fluids2d_gb300.adjoint import rollout
+    from fluids2d_gb300._lib import check, lib
+    dev = int(os.environ.get("LOCAL_RANK", "0"))
+    torch.cuda.set_device(dev)
+    n = int(os.environ.get("F2D_ADJ_N", "512"))
+    nsteps = int(os.environ.get("F2D_ADJ_STEPS", "400"))
+    every = 20
+    prec = "fp64" if args.workload.endswith("_fp64") else "fp32"
+    case = wl.eulerpsi_case(n=n, seed=rank)
+    rng = np.random.default_rng(1000 + rank)
+    target_np = wl.band_limited_field(n, n, 2, 8, seed=2000 + rank) * case["fields"][
+        "omega"].std() * case["msk"]
+    area = (1.0 / n) ** 2
+    stream = torch.cuda.Stream()
+    torch.cuda.set_stream(stream)
+
+    def model(precision, tol=None):
+        return make_gpu_model("eulerpsi", case, ctypes.c_void_p(stream.cuda_stream),
+                              precision, tol)
+
+    m = model(prec)
+    m.set_dt()
+    dt = m.time.dt  # the CFL step of the initial state, then held fixed
+    target = torch.tensor(target_np, device="cuda")
+    w0 = torch.tensor(case["fields"]["omega"], device="cuda")
+
+    def loss_fn(w):
+        return (0.5 * (w ** 2).mean() + ((w - target) ** 2).mean()) / area ** 2
+
+    def timed(fn):
+        torch.cuda.synchronize()
+        a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        a.record(stream)
+        out = fn()
+        b.record(stream)
+        torch.cuda.synchronize()
+        return out, a.elapsed_time(b)
+
+    # plain forward of the same steps (no checkpoints), graph-captured steps
+    L = lib()
+    for _ in range(args.warmup):
+        check(L.f2d_step(m._h, 1))
+    check(L.f2d_sync(m._h))
+    _, ms_plain = timed(lambda: (check(L.f2d_step(m._h, nsteps)), check(L.f2d_sync(m._h))))
+    # warm-up of the differentiable path (graph captures), then timed
+    x = w0.clone().requires_grad_(True)
+    g = torch.autograd.grad(loss_fn(rollout(m, x, min(nsteps, 2 * every), dt, every)), x)
+    x = w0.clone().requires_grad_(True)
+    wT, ms_fwd = timed(lambda: rollout(m, x, nsteps, dt, every))
+    lo = loss_fn(wT)
+    (g,), ms_bwd = timed(lambda: torch.autograd.grad(lo, x))
+    cells = n * n
+    # FP64 gradient for the precision comparison and the finite differences
+    m64 = model("fp64", tol=1e-14)
+    x64 = w0.clone().requires_grad_(True)
+    (g64,) = torch.autograd.grad(loss_fn(rollout(m64, x64, nsteps, dt, every)), x64)
+    fluid = torch.tensor(case["msk"] > 0, device="cuda")
+    ndir = int(os.environ.get("F2D_ADJ_FD_DIRS", "16"))
+    errs = []
+    with torch.no_grad():
+        for k in range(ndir):
+            v = torch.tensor(rng.standard_normal(w0.shape), device="cuda") * fluid
+            h = 1e-7 * float(w0.abs().max()) / float(v.abs().max())
+            fp = loss_fn(rollout(m64, w0 + h * v, nsteps, dt, every))
+            fm = loss_fn(rollout(m64, w0 - h * v, nsteps, dt, every))
+            fd = float(fp - fm) / (2 * h)
+            an = float((g64 * v).sum())
+            errs.append(abs(fd - an) / abs(an))
+    gdiff = float(torch.linalg.norm(g - g64) / torch.linalg.norm(g64))
+    value = world * cells * nsteps / ((ms_fwd + ms_bwd) / 1e3)
+    line = {
+        "metric": "cell-updates/s", "value": value, "unit": "cell-updates/s",
+        "n_gpus": world, "steps": nsteps, "warmup": args.warmup,
+        "ms_per_step": (ms_fwd + ms_bwd) / nsteps, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None,
+        "dtype": "f32" if prec == "fp32" else "f64", "data": "synthetic",
+        "config": {"workload": args.workload,
+                   "desc": f"gradient of final enstrophy + L2 misfit to a seeded "
+                           f"target after {nsteps} fixed-dt RK3 steps of eulerpsi "
+                           f"{n}x{n} closed basin w.r.t. the initial vorticity; "
+                           f"adjoint WENO5/RK3/Poisson kernels, checkpoints every "
+                           f"{every} steps",
+                   "precision": prec, "parallelism": f"replicas x{world}"},
+        "adjoint": {
+            "ms_forward_plain": ms_plain, "ms_forward_checkpointed": ms_fwd,
+            "ms_backward": ms_bwd,
+            "cost_forward_plus_backward_over_forward": (ms_fwd + ms_bwd) / ms_plain,
+            "cost_backward_over_forward": ms_bwd / ms_plain,
+            "grad_rel_l2_vs_fp64_gradient": gdiff,
+            "fd_directions": ndir,
+            "fd_rel_err_max": max(errs) if errs else None,
+            "fd_rel_err_median": float(np.median(errs)) if errs else None,
+            "fd_setup": "FP64 forward, Poisson tol 1e-14, central differences, "
+                        "step 1e-7 max|omega0|, random directions on fluid cells"},
+        "gpu_launches": None,
+    }
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+
+
 def run_gpu(args, rank, world):
+    if args.workload.startswith("adjoint"):
+        return run_gpu_adjoint(args, rank, world)
     if is_ensemble(args.workload):
         return run_gpu_ensemble(args, rank, world)
     import torch
@@ -677,7 +793,8 @@ def main():
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--workload", default="ensemble256_fp32",
                     choices=sorted(WORKLOADS) + sorted(k + "_fp32" for k in WORKLOADS)
-                    + ["ensemble256", "ensemble256_fp32"])
+                    + ["ensemble256", "ensemble256_fp32", "adjoint512",
+                       "adjoint512_fp64"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-fp64-form", action="store_true",
                     help="ensemble FP32 workload: skip the plain-FP64 comparison")

@@ -12,6 +12,7 @@
 #include <vector>
 
 #include "../../include/fluids2d_gb300.h"
+#include "adjoint.cuh"
 #include "mesh_host.h"
 #include "solver.cuh"
 #include "stage.cuh"
@@ -74,6 +75,21 @@ struct Field {
     int es = 8;  // element size: 8 (FP64) or 4 (FP32)
 };
 
+// Workspace of the discrete adjoint (eulerpsi): checkpoints of the
+// vorticity, the snapshot arena of one recomputed segment (3 stage states
+// per step, each with its face velocities) and the FP64 adjoint fields.
+struct AdjState {
+    int nsteps = 0, every = 0, nckpt = 0, cap_every = 0;
+    double dt = 0, dt_graph = 0;
+    bool ready = false;
+    std::vector<void*> ckpt;
+    void* arena = nullptr;
+    int* slot = nullptr;
+    double *yb = nullptr, *d1 = nullptr, *d2 = nullptr, *d3 = nullptr;
+    double *gx = nullptr, *gy = nullptr, *ubx = nullptr, *uby = nullptr;
+    double *psib = nullptr, *rb = nullptr;
+};
+
 struct f2d_model_s {
     f2d_params p;
     Geom g;
@@ -103,9 +119,11 @@ struct f2d_model_s {
     void *sb = nullptr, *sx = nullptr;  // scratch for f2d_poisson_solve
     std::map<void*, CUtensorMap> tmaps;
     int cur = 0;
-    // graphs: [kind][parity]; kinds: 0 diag, 1 step, 2 run, 3 solve0, 4 solve1
-    cudaGraphExec_t gx[5][2] = {};
-    int launches[5][2] = {};
+    // graphs: [kind][parity]; kinds: 0 diag, 1 step, 2 run, 3 solve0, 4 solve1,
+    // 5 step with adjoint snapshots, 6 adjoint step
+    cudaGraphExec_t gx[7][2] = {};
+    int launches[7][2] = {};
+    AdjState adj;
     int body_launches = 0;
     int rec_launches = 0;
 };
@@ -376,6 +394,63 @@ static int rec_step(f2d_model_s* m, int par, bool with_dt, cudaStream_t s)
     return 0;
 }
 
+// one step that first snapshots every stage state (w, U.x, U.y) into the
+// adjoint arena (slot counter on the device, advanced per stage)
+static int rec_step_snap(f2d_model_s* m, int par, cudaStream_t s)
+{
+    AdjState& a = m->adj;
+    const long long fsz = (long long)m->g.P * m->g.NY;
+    for (int k = 1; k <= 3; ++k) {
+        CKI(launch_adj_snap(m->prec, fb(m, "omega", par), fb(m, "U.x"), fb(m, "U.y"), a.arena,
+                            fsz, a.slot, s));
+        CKI(launch_adj_slot(a.slot, 1, s));
+        m->rec_launches += 2;
+        int e = rec_stage(m, k, par, s);
+        if (e) return e;
+        par = 1 - par;
+    }
+    CKI(launch_pushforward(m->sc, s));
+    m->rec_launches += 1;
+    return 0;
+}
+
+// yb += D'(w)^T db for the stage state of snapshot slot (*slot + soff)
+static int rec_adj_vjp(f2d_model_s* m, int soff, const double* db, cudaStream_t s)
+{
+    AdjState& a = m->adj;
+    const Geom& g = m->g;
+    const long long fsz = (long long)g.P * g.NY;
+    CKI(launch_adj_vjp_pre(m->p.compflux, m->prec, g, m->d_code, a.arena, fsz, a.slot, soff, db,
+                           a.gx, a.gy, a.ubx, a.uby, m->rdx2, m->rdy2, a.psib, s));
+    m->rec_launches += 2;
+    int e = rec_solve(m, 0, a.psib, a.rb, s);
+    if (e) return e;
+    CKI(launch_adj_vjp_post(g, m->d_code, a.gx, a.gy, fsz, a.rb, a.yb, s));
+    m->rec_launches += 1;
+    return 0;
+}
+
+// one adjoint RK3 step (integrators.py:92-107 reversed, fixed dt): the
+// stages' snapshots are slots (*slot - 3) .. (*slot - 1)
+static int rec_adj_step(f2d_model_s* m, cudaStream_t s)
+{
+    AdjState& a = m->adj;
+    const Geom& g = m->g;
+    const double dt = a.dt;
+    CKI(launch_adj_slot(a.slot, -3, s));
+    CKI(launch_adj_comb(g, a.yb, a.d1, a.d2, a.d3, 0, -dt / 12, -dt / 12, 2 * dt / 3, s));
+    m->rec_launches += 2;
+    int e = rec_adj_vjp(m, 2, a.d3, s);
+    if (e) return e;
+    CKI(launch_adj_comb(g, a.yb, a.d1, a.d2, a.d3, 1, -3 * dt / 4, dt / 4, 0, s));
+    m->rec_launches += 1;
+    e = rec_adj_vjp(m, 1, a.d2, s);
+    if (e) return e;
+    CKI(launch_adj_comb(g, a.yb, a.d1, a.d2, a.d3, 2, dt, 0, 0, s));
+    m->rec_launches += 1;
+    return rec_adj_vjp(m, 0, a.d1, s);
+}
+
 // F2D_EAGER=1 runs every recorded sequence directly on the stream (the
 // Poisson loop then synchronises once per iteration): a profiling aid, since
 // kernel profilers do not list kernels inside conditional graph nodes.
@@ -389,7 +464,22 @@ static bool eager_mode()
     return v == 1;
 }
 
-// capture kind (0 diag, 1 step, 2 run) for the current parity, then launch
+static int record_kind(f2d_model_s* m, int kind, int par, cudaStream_t s)
+{
+    switch (kind) {
+    case 0: return rec_diag(m, par, s);
+    case 1: return rec_step(m, par, false, s);
+    case 2: return rec_step(m, par, true, s);
+    case 5: return rec_step_snap(m, par, s);
+    case 6: return rec_adj_step(m, s);
+    }
+    return fail(1, "unknown graph kind");
+}
+
+static bool flips(int kind) { return kind == 1 || kind == 2 || kind == 5; }
+
+// capture kind (0 diag, 1 step, 2 run, 5 snapshot step, 6 adjoint step) for
+// the current parity, then launch
 static int run_graph(f2d_model_s* m, int kind)
 {
     const int par = m->cur;
@@ -399,10 +489,10 @@ static int run_graph(f2d_model_s* m, int kind)
             if (e0) return e0;
         }
         m->rec_launches = 0;
-        int e = kind == 0 ? rec_diag(m, par, m->stream) : rec_step(m, par, kind == 2, m->stream);
+        int e = record_kind(m, kind, par, m->stream);
         if (e) return e;
         m->launches[kind][par] = m->rec_launches;
-        if (kind != 0) m->cur = 1 - par;
+        if (flips(kind)) m->cur = 1 - par;
         return 0;
     }
     if (!m->gx[kind][par]) {
@@ -413,9 +503,7 @@ static int run_graph(f2d_model_s* m, int kind)
         }
         m->rec_launches = 0;
         CK(cudaStreamBeginCapture(m->stream, cudaStreamCaptureModeRelaxed));
-        int e = 0;
-        if (kind == 0) e = rec_diag(m, par, m->stream);
-        else e = rec_step(m, par, kind == 2, m->stream);
+        int e = record_kind(m, kind, par, m->stream);
         cudaGraph_t graph = nullptr;
         cudaError_t ce = cudaStreamEndCapture(m->stream, &graph);
         if (e) {
@@ -432,7 +520,7 @@ static int run_graph(f2d_model_s* m, int kind)
         m->launches[kind][par] = m->rec_launches;
     }
     CK(cudaGraphLaunch(m->gx[kind][par], m->stream));
-    if (kind != 0) m->cur = 1 - par;  // three stages flip the parity
+    if (flips(kind)) m->cur = 1 - par;  // three stages flip the parity
     return 0;
 }
 
@@ -968,6 +1056,141 @@ int f2d_time_stage(f2d_model m, int stage, int reps, int flush_l2, double* avg_m
     if (fl) cudaFree(fl);
     if (e) return e;
     *avg_ms = total / reps;
+    return 0;
+}
+
+// ---- discrete adjoint of the eulerpsi step ------------------------------------
+static int adj_check(f2d_model m)
+{
+    if (!m) return fail(1, "null model");
+    if (m->p.model != F2D_MODEL_EULERPSI) return fail(1, "the adjoint covers the eulerpsi model");
+    if (m->g.xper) return fail(1, "the adjoint covers closed (non-periodic) domains");
+    if (m->p.compflux != F2D_METHOD_WENO && m->p.compflux != F2D_METHOD_UPWIND)
+        return fail(1, "the adjoint covers the weno and upwind flux methods");
+    return 0;
+}
+
+// device FP64 (NY x NX, unpitched) <-> a field of the model (any precision)
+static int adj_put(f2d_model_s* m, void* field, const double* src)
+{
+    const Geom& g = m->g;
+    void* d64 = m->es == 8 ? field : m->stage64;
+    CK(cudaMemcpy2DAsync(d64, g.P * 8, src, g.NX * 8, g.NX * 8, g.NY, cudaMemcpyDeviceToDevice,
+                         m->stream));
+    if (m->es == 4) CKI(launch_convert(0, 1, d64, field, g, m->stream));
+    return 0;
+}
+
+static int adj_take(f2d_model_s* m, const void* field, double* dst)
+{
+    const Geom& g = m->g;
+    const void* d64 = field;
+    if (m->es == 4) {
+        CKI(launch_convert(1, 0, field, m->stage64, g, m->stream));
+        d64 = m->stage64;
+    }
+    CK(cudaMemcpy2DAsync(dst, g.NX * 8, d64, g.P * 8, g.NX * 8, g.NY, cudaMemcpyDeviceToDevice,
+                         m->stream));
+    return 0;
+}
+
+int f2d_adjoint_forward(f2d_model m, const double* w0, double* wT, int nsteps, double dt,
+                        int every)
+{
+    int e = adj_check(m);
+    if (e) return e;
+    if (!w0 || !wT || nsteps < 0 || every < 1 || !(dt > 0)) return fail(1, "bad arguments");
+    e = ensure_mg(m, 0);
+    if (e) return e;
+    AdjState& a = m->adj;
+    const Geom& g = m->g;
+    const size_t fb64 = field_bytes(m, 8), fbs = field_bytes(m, m->es);
+    if (!a.yb) {
+        double** v[] = {&a.yb, &a.d1, &a.d2, &a.d3, &a.ubx, &a.uby, &a.psib, &a.rb};
+        for (double** p : v)
+            if (!(*p = (double*)dalloc(m, fb64))) return fail(2, "out of device memory");
+        a.gx = (double*)dalloc(m, 6 * fb64);
+        a.gy = (double*)dalloc(m, 6 * fb64);
+        a.slot = (int*)dalloc(m, 256);
+        if (!a.gx || !a.gy || !a.slot) return fail(2, "out of device memory");
+    }
+    if (every > a.cap_every) {
+        a.arena = dalloc(m, (size_t)every * 9 * fbs);
+        if (!a.arena) return fail(2, "out of device memory");
+        a.cap_every = every;
+        for (int kind : {5, 6})
+            for (auto& k : m->gx[kind])
+                if (k) {
+                    cudaGraphExecDestroy(k);
+                    k = nullptr;
+                }
+    }
+    const int nck = nsteps / every + 1;
+    while ((int)a.ckpt.size() < nck) {
+        void* c = dalloc(m, fbs);
+        if (!c) return fail(2, "out of device memory");
+        a.ckpt.push_back(c);
+    }
+    a.nsteps = nsteps;
+    a.every = every;
+    a.nckpt = nck;
+    a.dt = dt;
+    if (a.dt_graph != dt)
+        for (auto& k : m->gx[6])
+            if (k) {
+                cudaGraphExecDestroy(k);
+                k = nullptr;
+            }
+    // fixed time step for the stage kernels
+    m->dt_const = dt;
+    m->cfl_dt = false;
+    CK(cudaMemcpyAsync(&m->sc->dt, &m->dt_const, 8, cudaMemcpyHostToDevice, m->stream));
+    m->dt_applied = true;
+    if ((e = adj_put(m, fb(m, "omega", m->cur), w0))) return e;
+    if ((e = run_graph(m, 0))) return e;
+    for (int n = 0; n < nsteps; ++n) {
+        if (n % every == 0)
+            CK(cudaMemcpyAsync(a.ckpt[n / every], fb(m, "omega", m->cur), fbs,
+                               cudaMemcpyDeviceToDevice, m->stream));
+        if ((e = run_graph(m, 1))) return e;
+    }
+    if ((e = adj_take(m, fb(m, "omega", m->cur), wT))) return e;
+    (void)g;
+    a.ready = true;
+    return 0;
+}
+
+int f2d_adjoint_backward(f2d_model m, const double* lamT, double* lam0)
+{
+    int e = adj_check(m);
+    if (e) return e;
+    AdjState& a = m->adj;
+    if (!a.ready) return fail(9, "f2d_adjoint_forward must run first");
+    if (!lamT || !lam0) return fail(1, "null argument");
+    const Geom& g = m->g;
+    const size_t fbs = field_bytes(m, m->es);
+    CK(cudaMemcpy2DAsync(a.yb, g.P * 8, lamT, g.NX * 8, g.NX * 8, g.NY,
+                         cudaMemcpyDeviceToDevice, m->stream));
+    CK(cudaMemsetAsync(a.rb, 0, field_bytes(m, 8), m->stream));
+    // the time step of the forward run (the model's dt may have changed)
+    m->dt_const = a.dt;
+    CK(cudaMemcpyAsync(&m->sc->dt, &m->dt_const, 8, cudaMemcpyHostToDevice, m->stream));
+    for (int sgm = a.nckpt - 1; sgm >= 0; --sgm) {
+        const int n0 = sgm * a.every;
+        const int n = std::min(a.every, a.nsteps - n0);
+        if (n <= 0) continue;
+        CK(cudaMemcpyAsync(fb(m, "omega", m->cur), a.ckpt[sgm], fbs, cudaMemcpyDeviceToDevice,
+                           m->stream));
+        if ((e = run_graph(m, 0))) return e;
+        CK(cudaMemsetAsync(a.slot, 0, sizeof(int), m->stream));
+        for (int k = 0; k < n; ++k)
+            if ((e = run_graph(m, 5))) return e;
+        for (int k = 0; k < n; ++k)
+            if ((e = run_graph(m, 6))) return e;
+        a.dt_graph = a.dt;
+    }
+    CK(cudaMemcpy2DAsync(lam0, g.NX * 8, a.yb, g.P * 8, g.NX * 8, g.NY,
+                         cudaMemcpyDeviceToDevice, m->stream));
     return 0;
 }
 

@@ -288,6 +288,12 @@ class Model:
             check(lib().f2d_field_set(self._h, name.encode(), ptr(a)))
         self._host_dirty = False
 
+    def _device_state_changed(self):
+        """The device state was written by a library call (the adjoint
+        rollouts) outside step/run: host arrays are refreshed on next use."""
+        self._host_dirty = False
+        self._device_newer = True
+
     # -- time stepping ---------------------------------------------------
     def step(self, nsteps=1):
         """model.py:67-69 (time.dt is the current device dt)."""

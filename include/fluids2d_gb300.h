@@ -203,6 +203,27 @@ int f2d_ensemble_stats(f2d_ensemble e, int64_t *cells, int64_t *poisson_iters,
 int f2d_ensemble_time_stage(f2d_ensemble e, int stage, int reps, int flush_l2,
                             double *avg_ms);
 
+/* ---- discrete adjoint (eulerpsi, closed basin, weno/upwind fluxes) ------ */
+
+/* No counterpart in the reference (it has no differentiation); the forward
+ * map is its RK3 step (integrators.py:92-107) of equations.py:73-86 with the
+ * time step held fixed at dt. Runs nsteps steps from w0 and writes the final
+ * vorticity to wT. w0 and wT are DEVICE FP64 arrays of (ny+6) x (nx+6)
+ * points, rows contiguous. Keeps the vorticity every `every` steps as a
+ * checkpoint for f2d_adjoint_backward. Leaves the model on a constant time
+ * step dt. Stream-ordered on the model's stream (no synchronisation). */
+int f2d_adjoint_forward(f2d_model m, const double *w0, double *wT, int nsteps,
+                        double dt, int every);
+/* Gradient pull-back of the last f2d_adjoint_forward: lam0 = (dwT/dw0)^T lamT
+ * (device FP64 arrays as above). Recomputes each checkpoint segment while
+ * recording the stage states, then runs the adjoint steps backwards: the
+ * discrete adjoint of the WENO-Z flux divergence with its smoothness weights
+ * differentiated exactly, of perpgrad and of the centre-to-vertex average,
+ * and the same masked Poisson solve for the adjoint streamfunction. The
+ * adjoint arithmetic is FP64 for either forward precision. Afterwards the
+ * model holds the state at the end of the first segment. */
+int f2d_adjoint_backward(f2d_model m, const double *lamT, double *lam0);
+
 /* ---- allocation-free entry point ---------------------------------------- */
 
 /* No counterpart in the reference. For callers that must not allocate
