@@ -14,6 +14,7 @@
 #include "../../include/fluids2d_gb300.h"
 #include "adjoint.cuh"
 #include "mesh_host.h"
+#include "stage_dev.cuh"
 #include "solver.cuh"
 #include "stage.cuh"
 
@@ -179,7 +180,9 @@ static int make_tmap(f2d_model_s* m, void* buf)
     CUtensorMap map;
     cuuint64_t dims[2] = {(cuuint64_t)m->g.NX, (cuuint64_t)m->g.NY};
     cuuint64_t strides[1] = {(cuuint64_t)(m->g.P * m->es)};
-    cuuint32_t box[2] = {40, 14};  // tile + halo, stage.cu SW x SH
+    // tile + halo: SW x FSH for the flux-form stage, SW x SH for rsw
+    cuuint32_t box[2] = {(cuuint32_t)SW,
+                         (cuuint32_t)(m->p.model == F2D_MODEL_RSW ? SH : FSH)};
     cuuint32_t estr[2] = {1, 1};
     CUresult r = fn(&map, m->prec == 0 ? CU_TENSOR_MAP_DATA_TYPE_FLOAT64
                                        : CU_TENSOR_MAP_DATA_TYPE_FLOAT32,

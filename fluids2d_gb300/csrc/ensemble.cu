@@ -94,16 +94,24 @@ __global__ void k_ens_c2v(const int4* __restrict__ tiles, const Member* __restri
     const int4 tl = tiles[blockIdx.x];
     const Member& mb = mem[tl.x];
     const Geom g = mb.g;
-    const int i = tl.y + threadIdx.x, j = tl.z + threadIdx.y;
-    if (j >= g.NY || i >= g.NX) return;
-    const long long o = (long long)j * g.P + i;
+    const int i = tl.y + threadIdx.x;
+    if (i >= g.NX) return;
     const Tin* q = at<Tin>(a.q[par], mb.off);
-    Tin s = Tin(0);  // the average in the precision of the state
-    if (j >= 1 && i >= 1 && (a.code[mb.off + o] & B_MSKV))
-        s = Tin(0.25) * (((q[o - g.P - 1] + q[o - 1]) + q[o - g.P]) + q[o]);
-    double v = s;
-    if (use_fv) v -= at<double>(a.fv, mb.off)[o];
-    at<double>(a.rhs, mb.off)[o] = v;
+    const uint32_t* code = a.code + mb.off;
+    const double* fv = use_fv ? at<double>(a.fv, mb.off) : nullptr;
+    double* rhs = at<double>(a.rhs, mb.off);
+#pragma unroll
+    for (int r = 0; r < FRT; ++r) {
+        const int j = tl.z + threadIdx.y + 8 * r;
+        if (j >= g.NY) break;
+        const long long o = (long long)j * g.P + i;
+        Tin s = Tin(0);  // the average in the precision of the state
+        if (j >= 1 && i >= 1 && (code[o] & B_MSKV))
+            s = Tin(0.25) * (((q[o - g.P - 1] + q[o - 1]) + q[o - g.P]) + q[o]);
+        double v = s;
+        if (fv) v -= fv[o];
+        rhs[o] = v;
+    }
 }
 
 // perpgrad (contravariant) from FP64 psi, optional halo fill, per-member max|U|
@@ -114,9 +122,11 @@ __global__ void k_ens_perpgrad(const int4* __restrict__ tiles, const Member* __r
     const int4 tl = tiles[blockIdx.x];
     const Member& mb = mem[tl.x];
     const Geom g = mb.g;
-    const int i = tl.y + threadIdx.x, j = tl.z + threadIdx.y;
     T m[2] = {T(0), T(0)};
-    if (j < g.NY && i < g.NX) {
+#pragma unroll
+    for (int r = 0; r < FRT; ++r) {
+        const int i = tl.y + threadIdx.x, j = tl.z + threadIdx.y + 8 * r;
+        if (j >= g.NY || i >= g.NX) continue;
         const long long o = (long long)j * g.P + i;
         const bool own = !fillU || periodic_owner(g, i);
         if (own) {
@@ -137,8 +147,8 @@ __global__ void k_ens_perpgrad(const int4* __restrict__ tiles, const Member* __r
                 Ux[o] = ux;
                 Uy[o] = uy;
             }
-            m[0] = fabs(ux);
-            m[1] = fabs(uy);
+            m[0] = fmax(m[0], fabs(ux));
+            m[1] = fmax(m[1], fabs(uy));
         }
     }
     DevScalars& sc = scs[tl.x];
@@ -485,7 +495,7 @@ int f2d_ensemble_create(const f2d_params* p, int count, const int* nxs, const in
         for (int k = 0; k < 2; ++k) {
             cuuint64_t dims[2] = {(cuuint64_t)g.NX, (cuuint64_t)g.NY};
             cuuint64_t strides[1] = {(cuuint64_t)(g.P * es)};
-            cuuint32_t box[2] = {(cuuint32_t)SW, (cuuint32_t)SH};
+            cuuint32_t box[2] = {(cuuint32_t)SW, (cuuint32_t)FSH};
             cuuint32_t estr[2] = {1, 1};
             CUresult r = enc(&mb.tq[k],
                              e->prec == 0 ? CU_TENSOR_MAP_DATA_TYPE_FLOAT64
@@ -511,7 +521,7 @@ int f2d_ensemble_create(const f2d_params* p, int count, const int* nxs, const in
         d.maindiag = p->model == F2D_MODEL_QG ? area * pow(p->f0, 2.0) / (p->g * p->H) : 0.0;
         // cell tiles
         mb.t0 = (int)cells.size();
-        for (int j0 = 0; j0 < g.NY; j0 += TY)
+        for (int j0 = 0; j0 < g.NY; j0 += FTY)
             for (int i0 = 0; i0 < g.NX; i0 += TX) cells.push_back(make_int4(b, i0, j0, 0));
         mb.nt = (int)cells.size() - mb.t0;
     }

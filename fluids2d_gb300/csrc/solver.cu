@@ -845,8 +845,6 @@ static int read_globals(const BatchSolver& s, cudaStream_t st, BSGlobals* h)
     return (int)e;
 }
 
-static cudaStream_t g_third = nullptr;  // body stream of nested loops
-
 int bs_record(BatchSolver& s, cudaStream_t st, cudaStream_t st2, int* launches)
 {
     const dim3 blk(32, 8);
@@ -891,8 +889,8 @@ int bs_record(BatchSolver& s, cudaStream_t st, cudaStream_t st2, int* launches)
         return (int)cudaGetLastError();
     }
     // refinement form
-    if (!g_third) {
-        e = cudaStreamCreateWithFlags(&g_third, cudaStreamNonBlocking);
+    if (!s.s3) {  // the solver's own body stream of the nested loop
+        e = cudaStreamCreateWithFlags(&s.s3, cudaStreamNonBlocking);
         if (e != cudaSuccess) return (int)e;
     }
     cudaGraphConditionalHandle cond_o = 0;
@@ -927,7 +925,7 @@ int bs_record(BatchSolver& s, cudaStream_t st, cudaStream_t st2, int* launches)
             e2 = cudaGraphConditionalHandleCreate(&cond_i, g2, 0, 0);
             if (e2 != cudaSuccess) return (int)e2;
             k_bs_arm<<<1, 1, 0, sb>>>(s.eg, cond_i);
-            int r2 = add_while(sb, g_third, &cond_i, 0, [&](cudaStream_t sc3) {
+            int r2 = add_while(sb, s.s3, &cond_i, 0, [&](cudaStream_t sc3) {
                 return cg_body<float, float>(s, sc3, cond_i, 1);
             });
             if (r2) return r2;
@@ -1056,17 +1054,33 @@ int bs_build(BatchSolver& s, const std::vector<BSMemberDesc>& members, const uin
             cudaSuccess ||
         cudaMemset(s.eg, 0, sizeof(BSGlobals)) != cudaSuccess)
         return 2;
-    cudaError_t fe = mode == 0
-        ? cudaFuncSetAttribute(k_bs_tail<double>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                               (int)s.tail_smem)
-        : cudaFuncSetAttribute(k_bs_tail<float>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                               (int)s.tail_smem);
-    if (fe != cudaSuccess) return 4;
+    // The dynamic shared-memory limit is an attribute of the tail kernel, not
+    // of this solver: raise it to the largest tail any solver of the process
+    // needs and never lower it, or the launches (and new graph captures) of
+    // an existing solver with a larger tail would fail. (One host thread and
+    // one device per process, as everywhere in this library.)
+    static size_t tail_attr[2] = {0, 0};
+    const int ti = mode == 0 ? 0 : 1;
+    if (s.tail_smem > tail_attr[ti]) {
+        cudaError_t fe = mode == 0
+            ? cudaFuncSetAttribute(k_bs_tail<double>,
+                                   cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                   (int)s.tail_smem)
+            : cudaFuncSetAttribute(k_bs_tail<float>,
+                                   cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                   (int)s.tail_smem);
+        if (fe != cudaSuccess) return 4;
+        tail_attr[ti] = s.tail_smem;
+    }
     return 0;
 }
 
 void bs_free(BatchSolver& s)
 {
+    if (s.s3) {
+        cudaStreamDestroy(s.s3);
+        s.s3 = nullptr;
+    }
     for (auto& m : s.mg) mg_free(m);
     s.mg.clear();
     for (void* p : s.owned) cudaFree(p);

@@ -71,6 +71,7 @@ struct BatchSolver {
     int maxit = 200, maxit_in = 30, maxouter = 20;
     int nu = 2;  // red-black sweeps before and after each coarse correction (1 or 2)
     int body_launches = 0;
+    cudaStream_t s3 = nullptr;  // capture stream of the inner loop body (own per solver)
     std::vector<void*> owned;
 };
 

@@ -2,7 +2,8 @@
 //
 // One launch per RK stage computes the right-hand side of the reference's
 // equation set AND applies the SSP-RK3 increment (integrators.py:92-107,
-// addto 154-196) over a 32x8 tile, with the stencil inputs staged in shared
+// addto 154-196) over a tile (32x32 cells for the flux-form models, 32x8
+// for rsw), with the stencil inputs staged in shared
 // memory by TMA (halo of 3 cells) and every face flux evaluated once.
 //
 // Every array point is produced with the numpy-slice semantics of the
@@ -29,7 +30,7 @@ k_fluxform_stage(const __grid_constant__ CUtensorMap tq, const T* __restrict__ q
 {
     __shared__ FluxformSmem<T, M> sm;
     fluxform_tile<T, M>(sm, &tq, qin, qout, Ux, Uy, code, ds_out, ds1, ds2, stage, g, sc->dt,
-                        &sc->status, blockIdx.x * TX, blockIdx.y * TY);
+                        &sc->status, blockIdx.x * TX, blockIdx.y * FTY);
 }
 
 // ---------------------------------------------------------------------------
@@ -254,15 +255,19 @@ __global__ void k_c2v(const Tin* __restrict__ q, T* __restrict__ v,
                       Geom g)
 {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    const int j = blockIdx.y * blockDim.y + threadIdx.y;
-    if (j >= g.NY || i >= g.NX) return;
-    const long long o = (long long)j * g.P + i;
-    Tin a = Tin(0);
-    if (j >= 1 && i >= 1 && (code[o] & B_MSKV))
-        a = Tin(0.25) * (((q[o - g.P - 1] + q[o - 1]) + q[o - g.P]) + q[o]);
-    T b = T(a);
-    if (fv) b -= fv[o];
-    v[o] = b;
+    if (i >= g.NX) return;
+#pragma unroll
+    for (int r = 0; r < FRT; ++r) {
+        const int j = blockIdx.y * FTY + threadIdx.y + 8 * r;
+        if (j >= g.NY) break;
+        const long long o = (long long)j * g.P + i;
+        Tin a = Tin(0);
+        if (j >= 1 && i >= 1 && (code[o] & B_MSKV))
+            a = Tin(0.25) * (((q[o - g.P - 1] + q[o - 1]) + q[o - g.P]) + q[o]);
+        T b = T(a);
+        if (fv) b -= fv[o];
+        v[o] = b;
+    }
 }
 
 // perpgrad with contravariant scaling (operators.py:144-149), optional halo
@@ -274,9 +279,11 @@ __global__ void k_perpgrad(const P* __restrict__ psi, T* __restrict__ Ux,
                            DevScalars* sc, double* partials)
 {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    const int j = blockIdx.y * blockDim.y + threadIdx.y;
     T m[2] = {T(0), T(0)};
-    if (j < g.NY && i < g.NX) {
+#pragma unroll
+    for (int r = 0; r < FRT; ++r) {
+        const int j = blockIdx.y * FTY + threadIdx.y + 8 * r;
+        if (j >= g.NY || i >= g.NX) continue;
         const long long o = (long long)j * g.P + i;
         const bool own = !fillU || periodic_owner(g, i);
         if (own) {
@@ -292,8 +299,8 @@ __global__ void k_perpgrad(const P* __restrict__ psi, T* __restrict__ Ux,
                 Ux[o] = ux;
                 Uy[o] = uy;
             }
-            m[0] = fabs(ux);
-            m[1] = fabs(uy);
+            m[0] = fmax(m[0], fabs(ux));
+            m[1] = fmax(m[1], fabs(uy));
         }
     }
     constexpr bool F = std::is_same<T, float>::value;
@@ -372,13 +379,18 @@ static dim3 tile_grid(const Geom& g)
     return dim3((g.NX + TX - 1) / TX, (g.NY + TY - 1) / TY);
 }
 
+static dim3 ftile_grid(const Geom& g)
+{
+    return dim3((g.NX + TX - 1) / TX, (g.NY + FTY - 1) / FTY);
+}
+
 int launch_fluxform_stage(int method, int prec, const CUtensorMap* tq,
                           const void* qin, void* qout, const void* Ux,
                           const void* Uy, const uint32_t* code, void* ds_out,
                           const void* ds1, const void* ds2, int stage,
                           const Geom& g, DevScalars* sc, cudaStream_t s)
 {
-    dim3 grid = tile_grid(g), block(TX, TY);
+    dim3 grid = ftile_grid(g), block(TX, TY);
 #define F2D_FF(T, M)                                                              \
     k_fluxform_stage<T, M><<<grid, block, 0, s>>>(                                \
         *tq, (const T*)qin, (T*)qout, (const T*)Ux, (const T*)Uy, code, (T*)ds_out, \
@@ -435,11 +447,13 @@ int launch_rsw_diag(int method, int prec, const CUtensorMap* tux,
 }
 
 static dim3 pt_grid(const Geom& g) { return dim3((g.NX + 31) / 32, (g.NY + 7) / 8); }
+// 32 x 32 points per block, FRT rows per thread
+static dim3 pt4_grid(const Geom& g) { return dim3((g.NX + 31) / 32, (g.NY + FTY - 1) / FTY); }
 
 int launch_c2v(int prec_in, int prec_out, const void* q, void* v, const uint32_t* code,
                const void* fv, const Geom& g, cudaStream_t s)
 {
-    const dim3 gr = pt_grid(g), bl(32, 8);
+    const dim3 gr = pt4_grid(g), bl(32, 8);
     if (prec_in == 0 && prec_out == 0)
         k_c2v<double, double><<<gr, bl, 0, s>>>((const double*)q, (double*)v, code,
                                                 (const double*)fv, g);
@@ -456,7 +470,7 @@ int launch_perpgrad(int prec_psi, int prec_U, const void* psi, void* Ux, void* U
                     const uint32_t* code, double rdy2, double rdx2, int fillU,
                     const Geom& g, DevScalars* sc, double* partials, cudaStream_t s)
 {
-    const dim3 gr = pt_grid(g), bl(32, 8);
+    const dim3 gr = pt4_grid(g), bl(32, 8);
     if (prec_psi == 0 && prec_U == 0)
         k_perpgrad<double, double><<<gr, bl, 0, s>>>((const double*)psi, (double*)Ux,
                                                      (double*)Uy, code, rdy2, rdx2, fillU,

@@ -6,9 +6,13 @@
 
 namespace f2d {
 
-constexpr int TX = 32, TY = 8;           // cells per tile
+constexpr int TX = 32, TY = 8;           // cells per tile (32 x 8 threads)
 constexpr int SW = TX + 8, SH = TY + 6;  // staged tile: cols i0-4.., rows j0-3..
 constexpr int OX = 4, OY = 3;            // offset of cell (j0,i0) in the tile
+// The flux-form stage runs 32 x 32-cell tiles (4 rows per thread): a quarter
+// of the blocks, each waiting once for its TMA tile, and 1.48x instead of
+// 2.19x staged cells per cell.
+constexpr int FRT = 4, FTY = 8 * FRT, FSH = FTY + 6;
 
 template <typename T>
 __device__ __forceinline__ T ldz(const T* __restrict__ a, int j, int i,
@@ -69,7 +73,7 @@ __device__ __forceinline__ void store_filled(T* __restrict__ a, const Geom& g,
 
 // Issue the TMA loads of up to two (SH x SW) tiles and wait for them. All
 // threads wait on the barrier; returns false (uniformly) on timeout.
-template <typename T>
+template <typename T, int SHR = SH>
 __device__ __forceinline__ bool stage_tiles(T (*s0)[SW], const CUtensorMap* m0,
                                             T (*s1)[SW], const CUtensorMap* m1,
                                             int i0, int j0, uint64_t* bar,
@@ -79,7 +83,7 @@ __device__ __forceinline__ bool stage_tiles(T (*s0)[SW], const CUtensorMap* m0,
     if (t == 0) mbar_init(bar, 1);
     __syncthreads();
     if (t == 0) {
-        const uint32_t bytes = (uint32_t)(sizeof(T) * SW * SH * (s1 ? 2 : 1));
+        const uint32_t bytes = (uint32_t)(sizeof(T) * SW * SHR * (s1 ? 2 : 1));
         mbar_expect_tx(bar, bytes);
         tma_load_2d(&s0[0][0], m0, i0 - OX, j0 - OY, bar);
         if (s1) tma_load_2d(&s1[0][0], m1, i0 - OX, j0 - OY, bar);
@@ -98,9 +102,9 @@ __device__ __forceinline__ bool stage_tiles(T (*s0)[SW], const CUtensorMap* m0,
 // ---------------------------------------------------------------------------
 template <typename T, int M>
 struct FluxformSmem {
-    alignas(128) T sq[SH][SW];
-    T sfx[TY][TX + 1];
-    T sfy[TY + 1][TX];
+    alignas(128) T sq[FSH][SW];
+    T sfx[FTY][TX + 1];
+    T sfy[FTY + 1][TX];
     T rk[3];
     uint64_t bar;
 };
@@ -118,9 +122,9 @@ __device__ __forceinline__ void fluxform_tile(
     auto& sfy = sm.sfy;
     const int tx = threadIdx.x, ty = threadIdx.y, t = ty * TX + tx;
     (void)qin;
-    if (!stage_tiles<T>(sq, tq, nullptr, nullptr, i0, j0, &sm.bar, status)) return;
+    if (!stage_tiles<T, FSH>(sq, tq, nullptr, nullptr, i0, j0, &sm.bar, status)) return;
 
-    // x-faces (TY x TX+1) and y-faces (TY+1 x TX): each evaluated once.
+    // x-faces (FTY x TX+1) and y-faces (FTY+1 x TX): each evaluated once.
     auto xface = [&](int r, int c) {
         const int j = j0 + r, i = i0 + c;
         T f = T(0);
@@ -151,25 +155,33 @@ __device__ __forceinline__ void fluxform_tile(
         }
         sfy[r][c] = f;
     };
-    xface(ty, tx);
-    yface(ty, tx);
-    if (t < TY) xface(t, TX);
-    else if (t < TY + TX) yface(TY, t - TY);
+#pragma unroll
+    for (int q = 0; q < FRT; ++q) {
+        xface(ty + 8 * q, tx);
+        yface(ty + 8 * q, tx);
+    }
+    if (t < FTY) xface(t, TX);
+    else if (t < FTY + TX) yface(FTY, t - FTY);
     if (t == 0) rk3_coefs<T>(stage, dt, sm.rk);
     __syncthreads();
 
-    const int j = j0 + ty, i = i0 + tx;
-    if (j >= g.NY || i >= g.NX || !periodic_owner(g, i)) return;
-    const long long o = (long long)j * g.P + i;
-    const T msk = (code[o] & B_MSK) ? T(1) : T(0);
-    const T ds = (-(sfx[ty][tx + 1] - sfx[ty][tx]) - (sfy[ty + 1][tx] - sfy[ty][tx])) * msk;
-    T inc;
-    if (stage == 1) inc = rk3_increment<T>(1, sm.rk, ds, T(0), T(0));
-    else if (stage == 2) inc = rk3_increment<T>(2, sm.rk, ds1[o], ds, T(0));
-    else inc = rk3_increment<T>(3, sm.rk, ds1[o], ds2[o], ds);
-    const T q = sq[ty + OY][tx + OX];
-    store_filled(qout, g, j, i, q + inc);
-    if (ds_out) store_filled(ds_out, g, j, i, ds);
+    const int i = i0 + tx;
+    if (i >= g.NX || !periodic_owner(g, i)) return;
+#pragma unroll
+    for (int q = 0; q < FRT; ++q) {
+        const int r = ty + 8 * q, j = j0 + r;
+        if (j >= g.NY) break;
+        const long long o = (long long)j * g.P + i;
+        const T msk = (code[o] & B_MSK) ? T(1) : T(0);
+        const T ds = (-(sfx[r][tx + 1] - sfx[r][tx]) - (sfy[r + 1][tx] - sfy[r][tx])) * msk;
+        T inc;
+        if (stage == 1) inc = rk3_increment<T>(1, sm.rk, ds, T(0), T(0));
+        else if (stage == 2) inc = rk3_increment<T>(2, sm.rk, ds1[o], ds, T(0));
+        else inc = rk3_increment<T>(3, sm.rk, ds1[o], ds2[o], ds);
+        const T qv = sq[r + OY][tx + OX];
+        store_filled(qout, g, j, i, qv + inc);
+        if (ds_out) store_filled(ds_out, g, j, i, ds);
+    }
 }
 
 }  // namespace f2d

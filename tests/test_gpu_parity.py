@@ -356,8 +356,12 @@ def _ensemble(members, precision="fp64", kind="eulerpsi"):
 
 @pytest.mark.parametrize("precision", ["fp64", "fp32"])
 def test_ensemble_members_match_single_models(precision):
-    """Every member equals the same case run alone (same kernels, same
-    per-member reductions), to the FP64 step tolerance."""
+    """Every member equals the same case run alone (same device code, same
+    per-member reductions): FP64 to the step tolerance; FP32 to 1e-6, since
+    the batched and the single-model stage kernels are separate
+    instantiations whose multiply-adds the compiler may contract into FMAs
+    differently, and FP32 rounding differences grow through the steps."""
+    tol = STEP_TOL if precision == "fp64" else 1e-6
     members = [wl.eulerpsi_case(n=64, ny=48, seed=11, nislands=2),
                wl.eulerpsi_case(n=96, ny=96, seed=12, nislands=0),
                wl.eulerpsi_case(n=40, ny=72, seed=13, nislands=3)]
@@ -375,7 +379,7 @@ def test_ensemble_members_match_single_models(precision):
             a = e.get_field(b, k)
             r = getattr(m.state, k.split(".")[0])
             r = getattr(r, k.split(".")[1]) if "." in k else r
-            assert rel_l2(a, r) <= STEP_TOL, (b, k, rel_l2(a, r))
+            assert rel_l2(a, r) <= tol, (b, k, rel_l2(a, r))
         t, dt, ite = e.time(b)
         assert ite == 4 and abs(t - m.time.t) <= 1e-12 * t
 
