@@ -60,6 +60,8 @@ int mg_build(MGHost& mg, int nyn0, int nxn0, long long pitch0, long long off0, i
     L0.fcy = (float)L0.cy;
     L0.fdiag = (float)L0.diag;
     L0.fidiag = (float)L0.idiag;
+    L0.md = maindiag;
+    L0.fmd = (float)maindiag;
     mg.lev.push_back(L0);
 
     // host masks of each level, dense nyn x nxn
@@ -106,6 +108,8 @@ int mg_build(MGHost& mg, int nyn0, int nxn0, long long pitch0, long long off0, i
         C.fcy = (float)C.cy;
         C.fdiag = (float)C.diag;
         C.fidiag = (float)C.idiag;
+        C.md = md;
+        C.fmd = (float)md;
         const size_t n = (size_t)C.pitch * cyn;
         void *x, *xa, *b, *m;
         if (cudaMalloc(&x, n * es) != cudaSuccess) return 2;

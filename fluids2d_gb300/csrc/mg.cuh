@@ -23,6 +23,8 @@ struct MGLevel {
     double cx, cy;      // east-west and north-south couplings (dy/dx, dx/dy)
     double diag, idiag; // -2(cx+cy) - maindiag and its inverse
     float fcx, fcy, fdiag, fidiag;  // the same in FP32 (no conversions in FP32 kernels)
+    double md;          // maindiag of the level: diag = -2 (cx + cy) - md
+    float fmd;
 };
 
 struct MGHost {

@@ -16,13 +16,29 @@ template <> struct Coef<double> {
     static __device__ __forceinline__ double cy(const MGLevel& L) { return L.cy; }
     static __device__ __forceinline__ double diag(const MGLevel& L) { return L.diag; }
     static __device__ __forceinline__ double idiag(const MGLevel& L) { return L.idiag; }
+    static __device__ __forceinline__ double md(const MGLevel& L) { return L.md; }
 };
 template <> struct Coef<float> {
     static __device__ __forceinline__ float cx(const MGLevel& L) { return L.fcx; }
     static __device__ __forceinline__ float cy(const MGLevel& L) { return L.fcy; }
     static __device__ __forceinline__ float diag(const MGLevel& L) { return L.fdiag; }
     static __device__ __forceinline__ float idiag(const MGLevel& L) { return L.fidiag; }
+    static __device__ __forceinline__ float md(const MGLevel& L) { return L.fmd; }
 };
+
+// A x at a fluid node from its value c and the four neighbour values (0 at
+// non-fluid nodes), written with differences to the centre:
+//   cx ((xW - c) + (xE - c)) + cy ((xS - c) + (xN - c)) - md c,
+// which equals cx (xW + xE) + cy (xS + xN) + diag c for diag = -2(cx+cy) - md
+// but, for the smooth fields of a converging solve, loses far fewer digits
+// to cancellation (the plain form's rounding error grows with the condition
+// number, this one's with its square root) - what limits the accuracy of the
+// FP32 Krylov products and of the refinement residual.
+template <typename S>
+__device__ __forceinline__ S apply_diff(S cx, S cy, S md, S c, S w, S e, S s, S n)
+{
+    return (cx * ((w - c) + (e - c)) + cy * ((s - c) + (n - c))) - md * c;
+}
 
 __device__ __forceinline__ long long nidx(const MGLevel& L, int J, int I)
 {

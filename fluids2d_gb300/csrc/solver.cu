@@ -234,10 +234,9 @@ k_bs_down(const int4* __restrict__ tiles, const BSInfo* __restrict__ info,
             if (cc < s || cc >= W - s) continue;
             const int q = rr * W + cc;
             S v = S(0);
-            if (sm[q]) {
-                const S off = cx * (sx[q - 1] + sx[q + 1]) + cy * (sx[q - W] + sx[q + W]);
-                v = sb[q] - (off + d * sx[q]);
-            }
+            if (sm[q])
+                v = sb[q] - apply_diff<S>(cx, cy, Coef<S>::md(F), sx[q], sx[q - 1], sx[q + 1],
+                                          sx[q - W], sx[q + W]);
             sb[q] = v;
         }
     }
@@ -428,7 +427,7 @@ k_bs_pq(const int4* __restrict__ tiles, const BSInfo* __restrict__ info,
         }
     }
     __syncthreads();
-    const V cx = Coef<V>::cx(L), cy = Coef<V>::cy(L), d = Coef<V>::diag(L);
+    const V cx = Coef<V>::cx(L), cy = Coef<V>::cy(L), md = Coef<V>::md(L);
     V acc = V(0);
 #pragma unroll
     for (int qr = 0; qr < TQ; ++qr) {
@@ -437,7 +436,7 @@ k_bs_pq(const int4* __restrict__ tiles, const BSInfo* __restrict__ info,
         const int e = (r + H) * W + c + H;
         const V pv = sp[e];
         V qv = V(0);
-        if (sm[e]) qv = (cx * (sp[e - 1] + sp[e + 1]) + cy * (sp[e - W] + sp[e + W])) + d * pv;
+        if (sm[e]) qv = apply_diff<V>(cx, cy, md, pv, sp[e - 1], sp[e + 1], sp[e - W], sp[e + W]);
         if (J < L.nyn && I < L.nxn) {  // (a wrapped periodic column is not the tile's)
             const long long k = nidx(L, J, I);
             pnew[k] = pv;
@@ -563,15 +562,15 @@ __device__ __forceinline__ void residual64(const int4& tl, const MGLevel& L,
         bv[qr] = b[k[qr]];
     }
     __syncthreads();
-    const double cx = L.cx, cy = L.cy, d = L.diag;
+    const double cx = L.cx, cy = L.cy, md = L.md;
 #pragma unroll
     for (int qr = 0; qr < TQ; ++qr) {
         const int rr = threadIdx.y + 8 * qr, c = threadIdx.x;
         const int e = (rr + H) * W + c + H;
         double rv = 0.0;
         if (sm[e] && ok[qr]) {
-            rv = bv[qr] - ((cx * (sx[e - 1] + sx[e + 1]) + cy * (sx[e - W] + sx[e + W])) +
-                           d * sx[e]);
+            rv = bv[qr] - apply_diff<double>(cx, cy, md, sx[e], sx[e - 1], sx[e + 1], sx[e - W],
+                                             sx[e + W]);
             w[0] += bv[qr] * bv[qr];
             w[1] += rv * rv;
         }

@@ -122,62 +122,101 @@ __device__ __forceinline__ void fluxform_tile(
     auto& sfy = sm.sfy;
     const int tx = threadIdx.x, ty = threadIdx.y, t = ty * TX + tx;
     (void)qin;
-    if (!stage_tiles<T, FSH>(sq, tq, nullptr, nullptr, i0, j0, &sm.bar, status)) return;
-
-    // x-faces (FTY x TX+1) and y-faces (FTY+1 x TX): each evaluated once.
-    auto xface = [&](int r, int c) {
-        const int j = j0 + r, i = i0 + c;
+    // 1. the TMA load of the staged tile (q with its 3-cell halo) ...
+    if (t == 0) mbar_init(&sm.bar, 1);
+    __syncthreads();
+    if (t == 0) {
+        mbar_expect_tx(&sm.bar, (uint32_t)(sizeof(T) * SW * FSH));
+        tma_load_2d(&sq[0][0], tq, i0 - OX, j0 - OY, &sm.bar);
+    }
+    // 2. ... overlapped with this thread's plain loads: the code word and
+    // face velocities of its cells (faces (j,i) of x and y share the index
+    // of cell (j,i)), the earlier stage tendencies, and the extra column of
+    // x-faces / row of y-faces of the tile edge; all unconditional (clamped
+    // index, then masked), so they are in flight together.
+    const int i = i0 + tx;
+    uint32_t cd[FRT];
+    T ux[FRT], uy[FRT], d1[FRT], d2[FRT];
+#pragma unroll
+    for (int q = 0; q < FRT; ++q) {
+        const int j = j0 + ty + 8 * q;
+        const bool in = j < g.NY && i < g.NX;
+        const long long o = (long long)min(j, g.NY - 1) * g.P + min(i, g.NX - 1);
+        const uint32_t c = code[o];
+        const T u = Ux[o], v = Uy[o];
+        cd[q] = in ? c : 0u;
+        ux[q] = u;
+        uy[q] = v;
+        d1[q] = stage >= 2 ? ds1[o] : T(0);
+        d2[q] = stage == 3 ? ds2[o] : T(0);
+    }
+    uint32_t ce = 0u;
+    T ue = T(0);
+    int er = 0, ec = 0, ex = 0;  // edge face: x (ex = 1) at (t, TX) or y (ex = 2) at (FTY, t-FTY)
+    if (t < FTY + TX) {
+        ex = t < FTY ? 1 : 2;
+        er = t < FTY ? t : FTY;
+        ec = t < FTY ? TX : t - FTY;
+        const int j = j0 + er, ii = i0 + ec;
+        const bool in = j < g.NY && ii < g.NX;
+        const long long o = (long long)min(j, g.NY - 1) * g.P + min(ii, g.NX - 1);
+        const uint32_t c = code[o];
+        const T u = ex == 1 ? Ux[o] : Uy[o];
+        ce = in ? c : 0u;
+        ue = u;
+    }
+    // 3. wait for the tile (bounded; uniform time-out exit)
+    {
+        const bool ok = mbar_wait(&sm.bar, 0);
+        const int all = __syncthreads_and(ok ? 1 : 0);
+        if (!all) {
+            if (t == 0) atomicOr(status, ST_TMA_TIMEOUT);
+            return;
+        }
+    }
+    // 4. fluxes at the faces, each evaluated once (zero without an order)
+    auto xflux = [&](int r, int c, uint32_t cw, T U) {
+        const int L = lev(cw, SH_OCX);
         T f = T(0);
-        if (j < g.NY && i < g.NX) {
-            const long long o = (long long)j * g.P + i;
-            const int L = lev(code[o], SH_OCX);
-            if (L) {
-                const T U = Ux[o];
-                const T* w = &sq[r + OY][c + OX - 3];
-                f = face_value<M, T>(L, U, w[0], w[1], w[2], w[3], w[4], w[5]) * U;
-            }
+        if (L) {
+            const T* w = &sq[r + OY][c + OX - 3];
+            f = face_value<M, T>(L, U, w[0], w[1], w[2], w[3], w[4], w[5]) * U;
         }
         sfx[r][c] = f;
     };
-    auto yface = [&](int r, int c) {
-        const int j = j0 + r, i = i0 + c;
+    auto yflux = [&](int r, int c, uint32_t cw, T U) {
+        const int L = lev(cw, SH_OCY);
         T f = T(0);
-        if (j < g.NY && i < g.NX) {
-            const long long o = (long long)j * g.P + i;
-            const int L = lev(code[o], SH_OCY);
-            if (L) {
-                const T U = Uy[o];
-                const int cc = c + OX;
-                f = face_value<M, T>(L, U, sq[r][cc], sq[r + 1][cc], sq[r + 2][cc],
-                                     sq[r + 3][cc], sq[r + 4][cc], sq[r + 5][cc]) *
-                    U;
-            }
+        if (L) {
+            const int cc = c + OX;
+            f = face_value<M, T>(L, U, sq[r][cc], sq[r + 1][cc], sq[r + 2][cc], sq[r + 3][cc],
+                                 sq[r + 4][cc], sq[r + 5][cc]) *
+                U;
         }
         sfy[r][c] = f;
     };
 #pragma unroll
     for (int q = 0; q < FRT; ++q) {
-        xface(ty + 8 * q, tx);
-        yface(ty + 8 * q, tx);
+        xflux(ty + 8 * q, tx, cd[q], ux[q]);
+        yflux(ty + 8 * q, tx, cd[q], uy[q]);
     }
-    if (t < FTY) xface(t, TX);
-    else if (t < FTY + TX) yface(FTY, t - FTY);
+    if (ex == 1) xflux(er, ec, ce, ue);
+    else if (ex == 2) yflux(er, ec, ce, ue);
     if (t == 0) rk3_coefs<T>(stage, dt, sm.rk);
     __syncthreads();
 
-    const int i = i0 + tx;
+    // 5. tendency, RK3 update and stores of this thread's cells
     if (i >= g.NX || !periodic_owner(g, i)) return;
 #pragma unroll
     for (int q = 0; q < FRT; ++q) {
         const int r = ty + 8 * q, j = j0 + r;
         if (j >= g.NY) break;
-        const long long o = (long long)j * g.P + i;
-        const T msk = (code[o] & B_MSK) ? T(1) : T(0);
+        const T msk = (cd[q] & B_MSK) ? T(1) : T(0);
         const T ds = (-(sfx[r][tx + 1] - sfx[r][tx]) - (sfy[r + 1][tx] - sfy[r][tx])) * msk;
         T inc;
         if (stage == 1) inc = rk3_increment<T>(1, sm.rk, ds, T(0), T(0));
-        else if (stage == 2) inc = rk3_increment<T>(2, sm.rk, ds1[o], ds, T(0));
-        else inc = rk3_increment<T>(3, sm.rk, ds1[o], ds2[o], ds);
+        else if (stage == 2) inc = rk3_increment<T>(2, sm.rk, d1[q], ds, T(0));
+        else inc = rk3_increment<T>(3, sm.rk, d1[q], d2[q], ds);
         const T qv = sq[r + OY][tx + OX];
         store_filled(qout, g, j, i, qv + inc);
         if (ds_out) store_filled(ds_out, g, j, i, ds);
