@@ -72,6 +72,28 @@ ENSEMBLE_DESC = ("ensemble of 256 eulerpsi closed basins, sizes uniform in "
                  "vortices, WENO5, SSP-RK3, per-member CFL 0.8")
 
 
+def max_over_ranks(x, world):
+    """The maximum of a per-rank number over the process group (the timing
+    rule: the slowest replica's time); the number itself for one process.
+    The reduction tensor lives on the backend's device (CUDA for NCCL, the
+    host for gloo)."""
+    if world <= 1:
+        return float(x)
+    import torch
+    import torch.distributed as dist
+    dev = "cuda" if dist.get_backend() == "nccl" else "cpu"
+    t = torch.tensor([float(x)], dtype=torch.float64, device=dev)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    dist.barrier()
+    return float(t.item())
+
+
+def replica_value(cells, steps, ms, world):
+    """Whole-job cell-updates/s of `world` replicas that each advanced
+    `cells` cells `steps` times, timed by the slowest (ms)."""
+    return world * cells * steps / (ms / 1e3)
+
+
 def is_ensemble(name):
     return name.startswith("ensemble")
 
@@ -370,13 +392,8 @@ def _ensemble_time(e, steps, warmup, stream, flush, dev, world):
             ev1[k].record(stream)
         torch.cuda.synchronize()
     e.sync()
-    ms = sum(a.elapsed_time(b) for a, b in zip(ev0, ev1))
+    ms = max_over_ranks(sum(a.elapsed_time(b) for a, b in zip(ev0, ev1)), world)
     st = e.stats()
-    if world > 1:
-        import torch.distributed as dist
-        t = torch.tensor([ms], device="cuda", dtype=torch.float64)
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        ms = float(t.item())
     return ms, st0, st, clk.summary()
 
 
@@ -430,7 +447,7 @@ def run_gpu_ensemble(args, rank, world):
                                          dev, world)
     pcg_iters = st["poisson_iters"] - st0["poisson_iters"]
     loops = st["loop_iters"] - st0["loop_iters"]
-    value = world * cells * args.steps / (ms / 1e3)
+    value = replica_value(cells, args.steps, ms, world)
     # the plain FP64 form on the same members and step count, for the
     # speed-up and the difference between the forms
     fp64_form = None
@@ -691,15 +708,9 @@ def run_gpu(args, rank, world):
             ev1[k].record(stream)
         torch.cuda.synchronize()
     check(L.f2d_sync(h))
-    ms = sum(a.elapsed_time(b) for a, b in zip(ev0, ev1))
+    ms = max_over_ranks(sum(a.elapsed_time(b) for a, b in zip(ev0, ev1)), world)
     pcg_iters = m.poisson_iterations() - it0
-    if world > 1:
-        import torch.distributed as dist
-        t = torch.tensor([ms], device="cuda", dtype=torch.float64)
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        ms = float(t.item())
-        dist.barrier()
-    value = world * cells * args.steps / (ms / 1e3)
+    value = replica_value(cells, args.steps, ms, world)
 
     # ---- end to end through the C ABI with pinned host state ---------------
     names = prognostic_names(model)
