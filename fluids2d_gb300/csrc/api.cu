@@ -246,7 +246,7 @@ static int ensure_mg(f2d_model_s* m, int which)
     if (e) return fail(e, "multigrid setup failed");
     bs.tol = m->p.poisson_tol;
     bs.maxit = m->p.poisson_maxit;
-    bs.tol_in = env_double("F2D_TOL_IN", 1e-4);
+    bs.tol_in = env_double("F2D_TOL_IN", 1e-6);
     bs.maxit_in = (int)env_double("F2D_MAXIT_IN", 30);
     bs.maxouter = std::max(2, m->p.poisson_maxit / 10);
     bs.nu = (int)env_double("F2D_NU", 2);

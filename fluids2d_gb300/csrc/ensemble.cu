@@ -531,7 +531,7 @@ int f2d_ensemble_create(const f2d_params* p, int count, const int* nxs, const in
         e->bs.tol = p->poisson_tol;
         e->bs.maxit = p->poisson_maxit;
         const char* ti = getenv("F2D_TOL_IN");
-        e->bs.tol_in = (ti && *ti) ? atof(ti) : 1e-4;
+        e->bs.tol_in = (ti && *ti) ? atof(ti) : 1e-6;
         e->bs.maxouter = std::max(2, p->poisson_maxit / 10);
         const char* nu = getenv("F2D_NU");
         e->bs.nu = (nu && *nu) ? atoi(nu) : 2;

@@ -29,18 +29,21 @@
 namespace f2d {
 
 // ---- tiles staged in shared memory ---------------------------------------------
-// Grid kernels work on tiles of 32 x 32 nodes of one level of one member
-// (the int4 of a tile table: member, first column, first row, unused), run
-// by 32 x 8 threads; thread (tx, ty) owns tile rows ty + 8 q, q = 0..3. A
-// kernel that needs neighbours stages the tile and a halo of H nodes in
-// shared memory (rows J0-H .. J0+31+H, columns I0-H .. I0+31+H); nodes
+// Grid kernels work on tiles of 32 x 64 nodes (columns x rows) of one level of
+// one member (the int4 of a tile table: member, first column, first row,
+// unused), run by 32 x 8 threads; thread (tx, ty) owns tile rows ty + 8 q,
+// q = 0..7. A kernel that needs neighbours stages the tile and a halo of H
+// nodes in shared memory (rows J0-H .. J0+63+H, columns I0-H .. I0+31+H); nodes
 // outside the level read as non-fluid 0, and x-periodic levels wrap. Each
 // node is then loaded once per kernel with coalesced rows, all loads of a
 // thread in flight together, and the red-black sweeps of a V-cycle level run
 // on the staged region: a half sweep on nodes at distance >= s from the
 // region edge only needs the region, so the smoothing, residual and transfer
 // steps of a level fuse into one kernel with a halo as wide as the chain.
-constexpr int TQ = BS_TH / 8;  // rows per thread
+// staged region of halo H around a tile of TH rows: WX columns, WY rows
+template <int H, int TH> struct Reg {
+    static constexpr int WX = BS_TW + 2 * H, WY = TH + 2 * H, N = WX * WY;
+};
 
 __device__ __forceinline__ int tid256() { return threadIdx.y * 32 + threadIdx.x; }
 
@@ -60,12 +63,12 @@ __device__ __forceinline__ bool in_level(const MGLevel& L, int J, int& I)
 
 // Stage mask and up to two arrays of a level on the region of halo H around
 // the tile at (J0, I0). Values at non-fluid nodes are staged as 0.
-template <int H, typename S, typename T2>
+template <int H, int TH, typename S, typename T2>
 __device__ __forceinline__ void stage_region(const MGLevel& L, int J0, int I0,
                                              const S* __restrict__ ga, S* sa,
                                              const T2* __restrict__ gb, T2* sb, uint8_t* sm)
 {
-    constexpr int W = BS_TW + 2 * H, N = W * W, IT = (N + 255) / 256;
+    constexpr int W = Reg<H, TH>::WX, N = Reg<H, TH>::N, IT = (N + 255) / 256;
     const int t = tid256();
 #pragma unroll
     for (int it = 0; it < IT; ++it) {
@@ -94,12 +97,12 @@ __device__ __forceinline__ void stage_region(const MGLevel& L, int J0, int I0,
 // staged region at distance >= s from its edge: x = (b - offdiag(x)) / diag.
 // The tile origin is even, so the colour of a region node is the parity of
 // its region coordinates.
-template <typename S, int W>
+template <typename S, int W, int WY>
 __device__ __forceinline__ void half_sweep(S* sx, const S* sb, const uint8_t* sm, int s,
                                            int color, S cx, S cy, S id)
 {
     constexpr int HW = W / 2;
-    const int n = (W - 2 * s) * HW;
+    const int n = (WY - 2 * s) * HW;
     for (int e = tid256(); e < n; e += 256) {
         const int rr = s + e / HW;
         const int cc = 2 * (e % HW) + ((color + rr) & 1);
@@ -178,15 +181,17 @@ __device__ __forceinline__ void set_rz(DevScalars& sc, int ir, double rz)
 // zero, so only the red fine nodes (centre and corners of a coarse node)
 // contribute. Writes the pre-smoothed x of the tile (to xa) and the coarse
 // right-hand side of the coarse nodes whose centre lies in the tile.
-template <typename S, int NU>
+template <typename S, int NU, int TH>
 __global__ void __launch_bounds__(256)
 k_bs_down(const int4* __restrict__ tiles, const BSInfo* __restrict__ info,
           const MGLevel* __restrict__ levs, int l, const DevScalars* __restrict__ scs, int ir)
 {
-    constexpr int H = 2 * NU + 1, W = BS_TW + 2 * H, N = W * W;
-    __shared__ S sx[N];
-    __shared__ S sb[N];
-    __shared__ uint8_t sm[N];
+    constexpr int H = 2 * NU + 1, W = Reg<H, TH>::WX, WY = Reg<H, TH>::WY,
+                  N = Reg<H, TH>::N, TQ = TH / 8;
+    extern __shared__ __align__(16) unsigned char dsm[];
+    S* sx = (S*)dsm;
+    S* sb = sx + N;
+    uint8_t* sm = (uint8_t*)(sb + N);
     const int4 tl = tiles[blockIdx.x];
     if (info[tl.x].ltail <= l || bs_skip(scs[tl.x], ir)) return;
     const MGLevel F = levs[tl.x * BS_LMAX + l];
@@ -221,13 +226,13 @@ k_bs_down(const int4* __restrict__ tiles, const BSInfo* __restrict__ info,
     __syncthreads();
 #pragma unroll
     for (int s = 1; s < 2 * NU; ++s) {
-        half_sweep<S, W>(sx, sb, sm, s, s & 1, cx, cy, id);
+        half_sweep<S, W, WY>(sx, sb, sm, s, s & 1, cx, cy, id);
         __syncthreads();
     }
     // residual at the red nodes of the region shrunk by 2 NU (in place of b)
     {
         constexpr int HW = W / 2, s = 2 * NU;
-        const int n = (W - 2 * s) * HW;
+        const int n = (WY - 2 * s) * HW;
         for (int e = t; e < n; e += 256) {
             const int rr = s + e / HW;
             const int cc = 2 * (e % HW) + (rr & 1);
@@ -242,18 +247,25 @@ k_bs_down(const int4* __restrict__ tiles, const BSInfo* __restrict__ info,
     }
     __syncthreads();
     {
+        // coarse nodes with their centre in the tile: (TH/2) x (BS_TW/2)
         const MGLevel C = levs[tl.x * BS_LMAX + l + 1];
-        const int a = t >> 4, b = t & 15;
-        const int cJ = (J0 >> 1) + a, cI = (I0 >> 1) + b;
-        if (cJ < C.nyn && cI < C.nxn) {
-            const long long k = nidx(C, cJ, cI);
-            S v = S(0);
-            if (C.m[k]) {
-                const int q = (H + 2 * a) * W + H + 2 * b;
-                const S c4 = (sb[q - W - 1] + sb[q - W + 1]) + (sb[q + W - 1] + sb[q + W + 1]);
-                v = sb[q] + S(0.25) * c4;
+        static_assert((TH / 2) * (BS_TW / 2) % 256 == 0, "coarse nodes per thread");
+#pragma unroll
+        for (int k2 = 0; k2 < (TH / 2) * (BS_TW / 2) / 256; ++k2) {
+            const int e = t + 256 * k2;
+            const int a = e / (BS_TW / 2), b = e % (BS_TW / 2);
+            const int cJ = (J0 >> 1) + a, cI = (I0 >> 1) + b;
+            if (cJ < C.nyn && cI < C.nxn) {
+                const long long k = nidx(C, cJ, cI);
+                S v = S(0);
+                if (C.m[k]) {
+                    const int q = (H + 2 * a) * W + H + 2 * b;
+                    const S c4 =
+                        (sb[q - W - 1] + sb[q - W + 1]) + (sb[q + W - 1] + sb[q + W + 1]);
+                    v = sb[q] + S(0.25) * c4;
+                }
+                lb<S>(C)[k] = v;
             }
-            lb<S>(C)[k] = v;
         }
     }
     S* xa = (S*)F.xa;
@@ -273,18 +285,20 @@ k_bs_down(const int4* __restrict__ tiles, const BSInfo* __restrict__ info,
 // neighbours the wrapped coarse ones). On level 0 (RZ) the block also forms
 // its part of <r, z> (r = b, z = x) and the member's last block sets rz and
 // beta.
-template <typename S, int NU, bool RZ>
+template <typename S, int NU, bool RZ, int TH>
 __global__ void __launch_bounds__(256)
 k_bs_up(const int4* __restrict__ tiles, const BSInfo* __restrict__ info,
         const MGLevel* __restrict__ levs, int l, DevScalars* scs, int ir, double* partials,
         double* gpart, unsigned int* gtick)
 {
-    constexpr int H = 2 * NU, W = BS_TW + 2 * H, N = W * W;
-    constexpr int CW = BS_TW / 2 + 1 + H, CN = CW * CW, CIT = (CN + 255) / 256;
-    __shared__ S sx[N];
-    __shared__ S sb[N];
-    __shared__ S sc2[CN];
-    __shared__ uint8_t sm[N];
+    constexpr int H = 2 * NU, W = Reg<H, TH>::WX, WY = Reg<H, TH>::WY, N = Reg<H, TH>::N;
+    constexpr int CW = BS_TW / 2 + 1 + H, CWY = TH / 2 + 1 + H, CN = CW * CWY, TQ = TH / 8;
+    constexpr int CIT = (CN + 255) / 256;
+    extern __shared__ __align__(16) unsigned char dsm[];
+    S* sx = (S*)dsm;
+    S* sb = sx + N;
+    S* sc2 = sb + N;
+    uint8_t* sm = (uint8_t*)(sc2 + CN);
     const int4 tl = tiles[blockIdx.x];
     DevScalars& sc = scs[tl.x];
     const BSInfo in = info[tl.x];
@@ -307,7 +321,7 @@ k_bs_up(const int4* __restrict__ tiles, const BSInfo* __restrict__ info,
             }
         }
     }
-    stage_region<H, S, S>(F, J0, I0, (const S*)F.xa, sx, lb<S>(F), sb, sm);
+    stage_region<H, TH, S, S>(F, J0, I0, (const S*)F.xa, sx, lb<S>(F), sb, sm);
     __syncthreads();
     for (int e = t; e < N; e += 256) {
         if (!sm[e]) continue;
@@ -327,7 +341,7 @@ k_bs_up(const int4* __restrict__ tiles, const BSInfo* __restrict__ info,
     const S cx = Coef<S>::cx(F), cy = Coef<S>::cy(F), id = Coef<S>::idiag(F);
 #pragma unroll
     for (int s = 1; s <= 2 * NU; ++s) {
-        half_sweep<S, W>(sx, sb, sm, s, s & 1, cx, cy, id);
+        half_sweep<S, W, WY>(sx, sb, sm, s, s & 1, cx, cy, id);
         __syncthreads();
     }
     S* x = lx<S>(F);
@@ -386,14 +400,15 @@ k_bs_tail(const BSInfo* __restrict__ info, const MGLevel* __restrict__ levs, Dev
 // z and p_old), so A p needs no second pass; p_old and p live in two
 // buffers chosen by the parity of the member's iteration count (p_old of
 // the halo belongs to other blocks and must not be overwritten meanwhile).
-template <typename S, typename V>
+template <typename S, typename V, int TH>
 __global__ void __launch_bounds__(256)
 k_bs_pq(const int4* __restrict__ tiles, const BSInfo* __restrict__ info,
         const MGLevel* __restrict__ levs, const S* __restrict__ z, V* __restrict__ p0,
         V* __restrict__ p1, V* __restrict__ q, DevScalars* scs, double* partials, double* gpart,
         unsigned int* gtick, int ir)
 {
-    constexpr int H = 1, W = BS_TW + 2, N = W * W, IT = (N + 255) / 256;
+    constexpr int H = 1, W = Reg<H, TH>::WX, N = Reg<H, TH>::N, IT = (N + 255) / 256;
+    constexpr int TQ = TH / 8;
     __shared__ V sp[N];
     __shared__ uint8_t sm[N];
     const int4 tl = tiles[blockIdx.x];
@@ -455,7 +470,7 @@ k_bs_pq(const int4* __restrict__ tiles, const BSInfo* __restrict__ info,
 // condition. FP64 form: x is the solution. Refinement form: x is the inner
 // correction e (started from 0) and convergence is relative to the round's
 // starting residual.
-template <typename V>
+template <typename V, int TH>
 __global__ void __launch_bounds__(256)
 k_bs_xr(const int4* __restrict__ tiles, const BSInfo* __restrict__ info,
         const MGLevel* __restrict__ levs, V* __restrict__ x, V* __restrict__ r,
@@ -476,34 +491,40 @@ k_bs_xr(const int4* __restrict__ tiles, const BSInfo* __restrict__ info,
         const bool first = ir && it == 0;
         const V* __restrict__ p = (it & 1) ? p0 : p1;  // written by k_bs_pq
         const V a = V(sc.alpha);
-        long long k[TQ];
-        bool ok[TQ];
-        uint8_t mv[TQ];
-        V xv[TQ], pv[TQ], rv[TQ], qv[TQ];
-#pragma unroll
-        for (int qr = 0; qr < TQ; ++qr) {
-            const int J = tl.z + threadIdx.y + 8 * qr, I = tl.y + threadIdx.x;
-            ok[qr] = J < L.nyn && I < L.nxn;
-            k[qr] = nidx(L, min(J, L.nyn - 1), min(I, L.nxn - 1));
-            mv[qr] = L.m[k[qr]];
-            xv[qr] = first ? V(0) : x[k[qr]];
-            pv[qr] = p[k[qr]];
-            rv[qr] = r[k[qr]];
-            qv[qr] = q[k[qr]];
-        }
         V acc = V(0);
+        // rows in batches of 4: the loads of a batch are in flight together,
+        // without the register cost of holding all rows of the tile
+        constexpr int QB = 4;
 #pragma unroll
-        for (int qr = 0; qr < TQ; ++qr) {
-            if (!ok[qr] || !mv[qr]) continue;
-            if (zero) {
-                x[k[qr]] = V(0);
-                r[k[qr]] = V(0);
-                continue;
+        for (int q0 = 0; q0 < TH / 8; q0 += QB) {
+            long long k[QB];
+            bool ok[QB];
+            uint8_t mv[QB];
+            V xv[QB], pv[QB], rv[QB], qv[QB];
+#pragma unroll
+            for (int qr = 0; qr < QB; ++qr) {
+                const int J = tl.z + threadIdx.y + 8 * (q0 + qr), I = tl.y + threadIdx.x;
+                ok[qr] = J < L.nyn && I < L.nxn;
+                k[qr] = nidx(L, min(J, L.nyn - 1), min(I, L.nxn - 1));
+                mv[qr] = L.m[k[qr]];
+                xv[qr] = first ? V(0) : x[k[qr]];
+                pv[qr] = p[k[qr]];
+                rv[qr] = r[k[qr]];
+                qv[qr] = q[k[qr]];
             }
-            x[k[qr]] = xv[qr] + a * pv[qr];
-            const V rn = rv[qr] - a * qv[qr];
-            r[k[qr]] = rn;
-            acc += rn * rn;
+#pragma unroll
+            for (int qr = 0; qr < QB; ++qr) {
+                if (!ok[qr] || !mv[qr]) continue;
+                if (zero) {
+                    x[k[qr]] = V(0);
+                    r[k[qr]] = V(0);
+                    continue;
+                }
+                x[k[qr]] = xv[qr] + a * pv[qr];
+                const V rn = rv[qr] - a * qv[qr];
+                r[k[qr]] = rn;
+                acc += rn * rn;
+            }
         }
         double w[1];
         mine = member_dot<V>(acc, w, partials, gpart, gtick, in, &sc.counter[4]);
@@ -541,16 +562,17 @@ k_bs_xr(const int4* __restrict__ tiles, const BSInfo* __restrict__ info,
 
 // FP64 residual r = b - A x of the tile (x staged with a one-node halo);
 // the per-thread sums of b*b and r*r; optionally the FP32 copy of r.
+template <int TH>
 __device__ __forceinline__ void residual64(const int4& tl, const MGLevel& L,
                                            const double* __restrict__ x,
                                            const double* __restrict__ b, double* __restrict__ r,
                                            float* __restrict__ rin, double (&w)[2])
 {
-    constexpr int H = 1, W = BS_TW + 2, N = W * W;
+    constexpr int H = 1, W = Reg<H, TH>::WX, N = Reg<H, TH>::N, TQ = TH / 8;
     __shared__ double sx[N];
     __shared__ uint8_t sm[N];
-    stage_region<H, double, double>(L, tl.z, tl.y, x, sx, (const double*)nullptr,
-                                    (double*)nullptr, sm);
+    stage_region<H, TH, double, double>(L, tl.z, tl.y, x, sx, (const double*)nullptr,
+                                        (double*)nullptr, sm);
     double bv[TQ];
     long long k[TQ];
     bool ok[TQ];
@@ -582,6 +604,7 @@ __device__ __forceinline__ void residual64(const int4& tl, const MGLevel& L,
 }
 
 // FP64 form: r = b - A x, <b,b>, <r,r>, per-member start state
+template <int TH>
 __global__ void __launch_bounds__(256)
 k_bs_init(const int4* __restrict__ tiles, const BSInfo* __restrict__ info,
           const MGLevel* __restrict__ levs, const double* __restrict__ x,
@@ -593,7 +616,7 @@ k_bs_init(const int4* __restrict__ tiles, const BSInfo* __restrict__ info,
     DevScalars& sc = scs[tl.x];
     const MGLevel L = levs[tl.x * BS_LMAX];
     double w[2] = {0.0, 0.0};
-    residual64(tl, L, x, b, r, nullptr, w);
+    residual64<TH>(tl, L, x, b, r, nullptr, w);
     const BSInfo in = info[tl.x];
     const bool mine = seg_reduce2<2>(w, partials, gpart, gtick, blockIdx.x, in.n0, in.nn, in.g0, &sc.counter[1]);
     if (mine) {
@@ -613,6 +636,7 @@ k_bs_init(const int4* __restrict__ tiles, const BSInfo* __restrict__ info,
 
 // Refinement form: r64 = b - A x (FP64), the FP32 copy that drives the next
 // inner solve, <b,b> and <r,r>; per member: converged, or start a new round.
+template <int TH>
 __global__ void __launch_bounds__(256)
 k_bs_refine(const int4* __restrict__ tiles, const BSInfo* __restrict__ info,
             const MGLevel* __restrict__ levs, const double* __restrict__ x,
@@ -628,7 +652,7 @@ k_bs_refine(const int4* __restrict__ tiles, const BSInfo* __restrict__ info,
     } else {
         const MGLevel L = levs[tl.x * BS_LMAX];
         double w[2] = {0.0, 0.0};
-        residual64(tl, L, x, b, r, rin, w);
+        residual64<TH>(tl, L, x, b, r, rin, w);
         const BSInfo in = info[tl.x];
         mine = seg_reduce2<2>(w, partials, gpart, gtick, blockIdx.x, in.n0, in.nn, in.g0, &sc.counter[1]);
         if (mine) {
@@ -671,6 +695,7 @@ k_bs_refine(const int4* __restrict__ tiles, const BSInfo* __restrict__ info,
 }
 
 // x += e (FP64); a member with a zero right-hand side gets x = 0
+template <int TH>
 __global__ void __launch_bounds__(256)
 k_bs_correct(const int4* __restrict__ tiles, const MGLevel* __restrict__ levs,
              double* __restrict__ x, const float* __restrict__ e,
@@ -681,6 +706,7 @@ k_bs_correct(const int4* __restrict__ tiles, const MGLevel* __restrict__ levs,
     if (sc.converged) return;
     const MGLevel L = levs[tl.x * BS_LMAX];
     const int zero = sc.zero;
+    constexpr int TQ = TH / 8;
     long long k[TQ];
     bool ok[TQ];
     uint8_t mv[TQ];
@@ -748,54 +774,87 @@ static bool bs_eager()
     return v == 1;
 }
 
+// dynamic shared memory of the down and up kernels (staged region, coarse
+// region, mask)
+template <typename S, int NU, int TH>
+static size_t down_smem()
+{
+    constexpr size_t N = Reg<2 * NU + 1, TH>::N;
+    return 2 * N * sizeof(S) + N;
+}
+template <typename S, int NU, int TH>
+static size_t up_smem()
+{
+    constexpr int H = 2 * NU;
+    constexpr size_t N = Reg<H, TH>::N, CN = (size_t)(BS_TW / 2 + 1 + H) * (TH / 2 + 1 + H);
+    return (2 * N + CN) * sizeof(S) + N;
+}
+
+template <typename S, int NU, int TH>
+static int set_level_attrs()
+{
+    cudaError_t e = cudaFuncSetAttribute(k_bs_down<S, NU, TH>,
+                                         cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                         (int)down_smem<S, NU, TH>());
+    if (e == cudaSuccess)
+        e = cudaFuncSetAttribute(k_bs_up<S, NU, false, TH>,
+                                 cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                 (int)up_smem<S, NU, TH>());
+    if (e == cudaSuccess)
+        e = cudaFuncSetAttribute(k_bs_up<S, NU, true, TH>,
+                                 cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                 (int)up_smem<S, NU, TH>());
+    return (int)e;
+}
+
 // one V-cycle for all members still iterating: a down kernel per grid level,
 // the tail, an up kernel per grid level (the level-0 one also forms <r, z>)
-template <typename S, int NU>
+template <typename S, int NU, int TH>
 static int vcycle_nu(BatchSolver& s, cudaStream_t st, int ir)
 {
     const dim3 blk(32, 8);
     int cnt = 0;
     for (int l = 0; l < s.maxl; ++l) {
-        k_bs_down<S, NU><<<s.ntiles[l], blk, 0, st>>>(s.tiles[l], s.dinfo, s.dlevs, l, s.scs, ir);
+        k_bs_down<S, NU, TH><<<s.ntiles[l], blk, down_smem<S, NU, TH>(), st>>>(
+            s.tiles[l], s.dinfo, s.dlevs, l, s.scs, ir);
         cnt += 1;
     }
     k_bs_tail<S><<<s.n, 1024, s.tail_smem, st>>>(s.dinfo, s.dlevs, s.scs, ir, NU);
     cnt += 1;
     for (int l = s.maxl - 1; l >= 1; --l) {
-        k_bs_up<S, NU, false><<<s.ntiles[l], blk, 0, st>>>(s.tiles[l], s.dinfo, s.dlevs, l,
-                                                          s.scs, ir, s.partials, s.gpart,
-                                                          s.gtick);
+        k_bs_up<S, NU, false, TH><<<s.ntiles[l], blk, up_smem<S, NU, TH>(), st>>>(
+            s.tiles[l], s.dinfo, s.dlevs, l, s.scs, ir, s.partials, s.gpart, s.gtick);
         cnt += 1;
     }
     if (s.maxl > 0) {
-        k_bs_up<S, NU, true><<<s.ntiles[0], blk, 0, st>>>(s.tiles[0], s.dinfo, s.dlevs, 0, s.scs,
-                                                         ir, s.partials, s.gpart, s.gtick);
+        k_bs_up<S, NU, true, TH><<<s.ntiles[0], blk, up_smem<S, NU, TH>(), st>>>(
+            s.tiles[0], s.dinfo, s.dlevs, 0, s.scs, ir, s.partials, s.gpart, s.gtick);
         cnt += 1;
     }
     return cnt;
 }
 
-template <typename S>
+template <typename S, int TH>
 static int vcycle(BatchSolver& s, cudaStream_t st, int ir)
 {
-    return s.nu >= 2 ? vcycle_nu<S, 2>(s, st, ir) : vcycle_nu<S, 1>(s, st, ir);
+    return s.nu >= 2 ? vcycle_nu<S, 2, TH>(s, st, ir) : vcycle_nu<S, 1, TH>(s, st, ir);
 }
 
 // the CG loop body; FP64 form (S = V = double) or the inner FP32 loop
-template <typename S, typename V>
+template <typename S, typename V, int TH>
 static int cg_body(BatchSolver& s, cudaStream_t st, cudaGraphConditionalHandle cond, int ir)
 {
     const dim3 blk(32, 8);
     const int nt = s.nrtiles;
     V* r = (V*)(ir ? s.v.rin : s.v.r64);
     V* x = (V*)(ir ? s.v.e : s.v.x64);
-    int cnt = vcycle<S>(s, st, ir);
-    k_bs_pq<S, V><<<nt, blk, 0, st>>>(s.rtiles, s.dinfo, s.dlevs, (const S*)s.v.z, (V*)s.v.p,
-                                      (V*)s.v.p2, (V*)s.v.q, s.scs, s.partials, s.gpart,
-                                      s.gtick, ir);
-    k_bs_xr<V><<<nt, blk, 0, st>>>(s.rtiles, s.dinfo, s.dlevs, x, r, (const V*)s.v.p,
-                                   (const V*)s.v.p2, (const V*)s.v.q, s.scs, s.partials,
-                                   s.gpart, s.gtick, s.eg, cond, ir, s.n);
+    int cnt = vcycle<S, TH>(s, st, ir);
+    k_bs_pq<S, V, TH><<<nt, blk, 0, st>>>(s.rtiles, s.dinfo, s.dlevs, (const S*)s.v.z,
+                                          (V*)s.v.p, (V*)s.v.p2, (V*)s.v.q, s.scs, s.partials,
+                                          s.gpart, s.gtick, ir);
+    k_bs_xr<V, TH><<<nt, blk, 0, st>>>(s.rtiles, s.dinfo, s.dlevs, x, r, (const V*)s.v.p,
+                                       (const V*)s.v.p2, (const V*)s.v.q, s.scs, s.partials,
+                                       s.gpart, s.gtick, s.eg, cond, ir, s.n);
     cnt += 2;
     s.body_launches = cnt;
     return (int)cudaGetLastError();
@@ -844,7 +903,8 @@ static int read_globals(const BatchSolver& s, cudaStream_t st, BSGlobals* h)
     return (int)e;
 }
 
-int bs_record(BatchSolver& s, cudaStream_t st, cudaStream_t st2, int* launches)
+template <int TH>
+static int bs_record_t(BatchSolver& s, cudaStream_t st, cudaStream_t st2, int* launches)
 {
     const dim3 blk(32, 8);
     const int nt = s.nrtiles;
@@ -866,13 +926,13 @@ int bs_record(BatchSolver& s, cudaStream_t st, cudaStream_t st2, int* launches)
             e = cudaGraphConditionalHandleCreate(&cond, graph, 1, cudaGraphCondAssignDefault);
             if (e != cudaSuccess) return (int)e;
         }
-        k_bs_init<<<nt, blk, 0, st>>>(s.rtiles, s.dinfo, s.dlevs, (const double*)s.v.x64,
+        k_bs_init<TH><<<nt, blk, 0, st>>>(s.rtiles, s.dinfo, s.dlevs, (const double*)s.v.x64,
                                       (const double*)s.v.b64, (double*)s.v.r64, s.scs,
                                       s.partials, s.gpart, s.gtick, s.eg, cond, s.n);
         fixed += 1;
         if (capturing) {
             int r = add_while(st, st2, &cond, 1, [&](cudaStream_t sb) {
-                return cg_body<double, double>(s, sb, cond, 0);
+                return cg_body<double, double, TH>(s, sb, cond, 0);
             });
             if (r) return r;
         } else {
@@ -880,7 +940,7 @@ int bs_record(BatchSolver& s, cudaStream_t st, cudaStream_t st2, int* launches)
                 int r = read_globals(s, st, &h);
                 if (r) return r;
                 if (h.active_out <= 0) break;
-                r = cg_body<double, double>(s, st, 0, 0);
+                r = cg_body<double, double, TH>(s, st, 0, 0);
                 if (r) return r;
             }
         }
@@ -898,16 +958,16 @@ int bs_record(BatchSolver& s, cudaStream_t st, cudaStream_t st2, int* launches)
         if (e != cudaSuccess) return (int)e;
     }
     k_bs_reset<<<1, 1, 0, st>>>(s.eg);
-    k_bs_refine<<<nt, blk, 0, st>>>(s.rtiles, s.dinfo, s.dlevs, (const double*)s.v.x64,
+    k_bs_refine<TH><<<nt, blk, 0, st>>>(s.rtiles, s.dinfo, s.dlevs, (const double*)s.v.x64,
                                     (const double*)s.v.b64, (double*)s.v.r64, (float*)s.v.rin,
                                     s.scs, s.partials, s.gpart, s.gtick, s.eg, 1, cond_o,
                                     s.n);
     fixed += 2;
     auto round_tail = [&](cudaStream_t sb) {
-        k_bs_correct<<<nt, blk, 0, sb>>>(s.rtiles, s.dlevs, (double*)s.v.x64,
+        k_bs_correct<TH><<<nt, blk, 0, sb>>>(s.rtiles, s.dlevs, (double*)s.v.x64,
                                          (const float*)s.v.e, s.scs);
         k_bs_reset<<<1, 1, 0, sb>>>(s.eg);
-        k_bs_refine<<<nt, blk, 0, sb>>>(s.rtiles, s.dinfo, s.dlevs, (const double*)s.v.x64,
+        k_bs_refine<TH><<<nt, blk, 0, sb>>>(s.rtiles, s.dinfo, s.dlevs, (const double*)s.v.x64,
                                         (const double*)s.v.b64, (double*)s.v.r64,
                                         (float*)s.v.rin, s.scs, s.partials, s.gpart, s.gtick,
                                         s.eg, 0, cond_o, s.n);
@@ -925,7 +985,7 @@ int bs_record(BatchSolver& s, cudaStream_t st, cudaStream_t st2, int* launches)
             if (e2 != cudaSuccess) return (int)e2;
             k_bs_arm<<<1, 1, 0, sb>>>(s.eg, cond_i);
             int r2 = add_while(sb, s.s3, &cond_i, 0, [&](cudaStream_t sc3) {
-                return cg_body<float, float>(s, sc3, cond_i, 1);
+                return cg_body<float, float, TH>(s, sc3, cond_i, 1);
             });
             if (r2) return r2;
             round_tail(sb);
@@ -941,7 +1001,7 @@ int bs_record(BatchSolver& s, cudaStream_t st, cudaStream_t st2, int* launches)
                 r = read_globals(s, st, &h);
                 if (r) return r;
                 if (h.active_in <= 0) break;
-                r = cg_body<float, float>(s, st, 0, 1);
+                r = cg_body<float, float, TH>(s, st, 0, 1);
                 if (r) return r;
             }
             round_tail(st);
@@ -949,6 +1009,12 @@ int bs_record(BatchSolver& s, cudaStream_t st, cudaStream_t st2, int* launches)
     }
     if (launches) *launches = fixed;
     return (int)cudaGetLastError();
+}
+
+int bs_record(BatchSolver& s, cudaStream_t st, cudaStream_t st2, int* launches)
+{
+    return s.th == 64 ? bs_record_t<64>(s, st, st2, launches)
+                      : bs_record_t<32>(s, st, st2, launches);
 }
 
 int bs_build(BatchSolver& s, const std::vector<BSMemberDesc>& members, const uint8_t* dmask,
@@ -981,7 +1047,17 @@ int bs_build(BatchSolver& s, const std::vector<BSMemberDesc>& members, const uin
         s.tail_smem = std::max(s.tail_smem, s.mg[b].tail_smem);
         for (int l = 0; l < nl; ++l) levs[(size_t)b * BS_LMAX + l] = s.mg[b].lev[l];
     }
-    // Tile tables of 32 x 32 nodes. Level 0 (all members; the Krylov
+    // Tile height: 64 rows when level 0 holds enough nodes to fill the GPU
+    // many times over (fewer, fuller blocks), else 32 (more blocks for small
+    // problems, which are latency-bound).
+    {
+        long long n0 = 0;
+        for (int b = 0; b < s.n; ++b)
+            n0 += (long long)levs[(size_t)b * BS_LMAX].nyn * levs[(size_t)b * BS_LMAX].nxn;
+        s.th = n0 >= 2ll * 1024 * 1024 ? 64 : 32;
+    }
+    const int TH = s.th;
+    // Tile tables of 32 x TH nodes. Level 0 (all members; the Krylov
     // kernels and the first multigrid level) with the members' reduction
     // groups of RED_GROUP tiles; level l >= 1 for the members whose grid
     // levels reach below it. Tiles without a fluid node are left out (their
@@ -990,7 +1066,7 @@ int bs_build(BatchSolver& s, const std::vector<BSMemberDesc>& members, const uin
     auto has_fluid = [&](int b, int l, int J0, int I0) {
         const std::vector<uint8_t>& hm = s.mg[b].hmask[l];
         const MGLevel& L = levs[(size_t)b * BS_LMAX + l];
-        for (int J = J0; J < std::min(L.nyn, J0 + BS_TH); ++J)
+        for (int J = J0; J < std::min(L.nyn, J0 + TH); ++J)
             for (int I = I0; I < std::min(L.nxn, I0 + BS_TW); ++I)
                 if (hm[(size_t)J * L.nxn + I]) return true;
         return false;
@@ -1001,7 +1077,7 @@ int bs_build(BatchSolver& s, const std::vector<BSMemberDesc>& members, const uin
     for (int b = 0; b < s.n; ++b) {
         const MGLevel& L = levs[(size_t)b * BS_LMAX];
         info[b].n0 = (int)rt.size();
-        for (int J0 = 0; J0 < L.nyn; J0 += BS_TH)
+        for (int J0 = 0; J0 < L.nyn; J0 += TH)
             for (int I0 = 0; I0 < L.nxn; I0 += BS_TW)
                 if (has_fluid(b, 0, J0, I0)) rt.push_back(make_int4(b, I0, J0, 0));
         if ((int)rt.size() == info[b].n0) rt.push_back(make_int4(b, 0, 0, 0));
@@ -1013,7 +1089,7 @@ int bs_build(BatchSolver& s, const std::vector<BSMemberDesc>& members, const uin
         for (int b = 0; b < s.n; ++b) {
             if (info[b].ltail <= l) continue;
             const MGLevel& L = levs[(size_t)b * BS_LMAX + l];
-            for (int J0 = 0; J0 < L.nyn; J0 += BS_TH)
+            for (int J0 = 0; J0 < L.nyn; J0 += TH)
                 for (int I0 = 0; I0 < L.nxn; I0 += BS_TW)
                     if (has_fluid(b, l, J0, I0)) tiles[l].push_back(make_int4(b, I0, J0, 0));
         }
@@ -1058,6 +1134,15 @@ int bs_build(BatchSolver& s, const std::vector<BSMemberDesc>& members, const uin
     // needs and never lower it, or the launches (and new graph captures) of
     // an existing solver with a larger tail would fail. (One host thread and
     // one device per process, as everywhere in this library.)
+    static bool level_attrs = false;  // constant per kernel instantiation: once
+    if (!level_attrs) {
+        if (set_level_attrs<float, 1, 32>() || set_level_attrs<float, 2, 32>() ||
+            set_level_attrs<double, 1, 32>() || set_level_attrs<double, 2, 32>() ||
+            set_level_attrs<float, 1, 64>() || set_level_attrs<float, 2, 64>() ||
+            set_level_attrs<double, 1, 64>() || set_level_attrs<double, 2, 64>())
+            return 4;
+        level_attrs = true;
+    }
     static size_t tail_attr[2] = {0, 0};
     const int ti = mode == 0 ? 0 : 1;
     if (s.tail_smem > tail_attr[ti]) {

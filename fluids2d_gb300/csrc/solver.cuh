@@ -9,7 +9,7 @@
 namespace f2d {
 
 constexpr int BS_LMAX = 16;           // levels per member
-constexpr int BS_TW = 32, BS_TH = 32;  // node tile: 32 x 32 nodes, 32 x 8 threads
+constexpr int BS_TW = 32;  // node tile: 32 columns x 32 or 64 rows, 32 x 8 threads
 
 struct BSInfo {
     int nl, ltail, ksweeps;  // levels, first tail level, coarsest sweeps
@@ -67,9 +67,10 @@ struct BatchSolver {
     int maxl = 0;
     size_t tail_smem = 0;
     BSVecs v;
-    double tol = 1e-12, tol_in = 1e-4;
+    double tol = 1e-12, tol_in = 1e-6;
     int maxit = 200, maxit_in = 30, maxouter = 20;
     int nu = 2;  // red-black sweeps before and after each coarse correction (1 or 2)
+    int th = 32;  // tile rows (32 or 64), chosen by bs_build
     int body_launches = 0;
     cudaStream_t s3 = nullptr;  // capture stream of the inner loop body (own per solver)
     std::vector<void*> owned;
