@@ -71,7 +71,7 @@ struct EnsArenas {
 };
 
 template <typename T, int M>
-__global__ void __launch_bounds__(TX * TY)
+__global__ void __launch_bounds__(TX * TY, sizeof(T) == 4 ? 5 : 3)
 k_ens_fluxform_stage(const int4* __restrict__ tiles, const Member* __restrict__ mem,
                      EnsArenas a, int par, int stage, DevScalars* scs, EnsGlobals* eg)
 {

@@ -21,7 +21,7 @@ namespace f2d {
 // Flux-form stage kernel of one model (tile = block index).
 // ---------------------------------------------------------------------------
 template <typename T, int M>
-__global__ void __launch_bounds__(TX * TY)
+__global__ void __launch_bounds__(TX * TY, sizeof(T) == 4 ? 5 : 3)
 k_fluxform_stage(const __grid_constant__ CUtensorMap tq, const T* __restrict__ qin,
                  T* __restrict__ qout, const T* __restrict__ Ux,
                  const T* __restrict__ Uy, const uint32_t* __restrict__ code,

@@ -84,6 +84,35 @@ __device__ __forceinline__ double weno5z<double>(double qmm, double qm, double q
     return ((W1 * qi1 + W2 * qi2) + W3 * qi3) / ((W1 + W2) + W3);
 }
 
+// FP32 form of weno5z: the three weight quotients tau/d_k and the final
+// normalisation use the fast single-precision division (__fdividef, ~2 ulp;
+// d_k >= 1e-16 and the denominator of the normalisation is >= 1, far inside
+// its range). In FP32 the IEEE division sequences are a large share of the
+// stencil's instructions; 2 ulp is within the FP32 form's own rounding.
+template <>
+__device__ __forceinline__ float weno5z<float>(float qmm, float qm, float q0, float qp,
+                                               float qpp)
+{
+    const float eps = WenoConst<float>::eps5;
+    const float c13 = 1.f / 3.f, c76 = 7.f / 6.f, c116 = 11.f / 6.f;
+    const float c16 = 1.f / 6.f, c56 = 5.f / 6.f;
+    const float qi1 = (c13 * qmm - c76 * qm) + c116 * q0;
+    const float qi2 = (-c16 * qm + c56 * q0) + c13 * qp;
+    const float qi3 = (c13 * q0 + c56 * qp) - c16 * qpp;
+    const float k1 = 13.f / 12.f, k2 = 0.25f;
+    const float a1 = (qmm - 2.f * qm) + q0, b1 = (qmm - 4.f * qm) + 3.f * q0;
+    const float a2 = (qm - 2.f * q0) + qp, b2 = qm - qp;
+    const float a3 = (q0 - 2.f * qp) + qpp, b3 = (3.f * q0 - 4.f * qp) + qpp;
+    const float beta1 = k1 * (a1 * a1) + k2 * (b1 * b1);
+    const float beta2 = k1 * (a2 * a2) + k2 * (b2 * b2);
+    const float beta3 = k1 * (a3 * a3) + k2 * (b3 * b3);
+    const float tau5 = fabsf(beta1 - beta3);
+    const float w1 = 0.1f * (1.f + __fdividef(tau5, beta1 + eps));
+    const float w2 = 0.6f * (1.f + __fdividef(tau5, beta2 + eps));
+    const float w3 = 0.3f * (1.f + __fdividef(tau5, beta3 + eps));
+    return __fdividef((w1 * qi1 + w2 * qi2) + w3 * qi3, (w1 + w2) + w3);
+}
+
 // weno3z (weno.py:75-100): WENO-Z, 3rd order.
 template <typename T>
 __device__ __forceinline__ T weno3z(T qm, T q0, T qp)
@@ -97,6 +126,21 @@ __device__ __forceinline__ T weno3z(T qm, T q0, T qp)
     T w1 = (T(1.) / T(3.)) * (T(1) + tau / (beta1 + eps));
     T w2 = (T(2.) / T(3.)) * (T(1) + tau / (beta2 + eps));
     return (w1 * qi1 + w2 * qi2) / (w1 + w2);
+}
+
+// FP32 form of weno3z with the fast division (see weno5z<float>).
+template <>
+__device__ __forceinline__ float weno3z<float>(float qm, float q0, float qp)
+{
+    const float eps = WenoConst<float>::eps3;
+    const float qi1 = -0.5f * qm + 1.5f * q0;
+    const float qi2 = 0.5f * (q0 + qp);
+    const float d1 = q0 - qm, d2 = qp - q0;
+    const float beta1 = d1 * d1, beta2 = d2 * d2;
+    const float tau = fabsf(beta2 - beta1);
+    const float w1 = (1.f / 3.f) * (1.f + __fdividef(tau, beta1 + eps));
+    const float w2 = (2.f / 3.f) * (1.f + __fdividef(tau, beta2 + eps));
+    return __fdividef(w1 * qi1 + w2 * qi2, w1 + w2);
 }
 
 // FP64 form of weno3z with one division (see weno5z<double>); d_k >= 1e-14.
