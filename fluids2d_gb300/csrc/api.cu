@@ -1062,6 +1062,23 @@ int f2d_time_stage(f2d_model m, int stage, int reps, int flush_l2, double* avg_m
     return 0;
 }
 
+int f2d_time_solver(f2d_model m, int reps, int flush_l2, double* avg_ms, int64_t* nodes,
+                    int* elem_bytes)
+{
+    if (!m || !avg_ms) return fail(1, "null argument");
+    if (m->p.model == F2D_MODEL_RSW) return fail(1, "rsw has no Poisson solve");
+    const int which = m->p.model == F2D_MODEL_EULERPSI ? 0 : 1;
+    if (!m->bs_ready[which]) return fail(9, "the solver has not run yet");
+    CK(cudaStreamSynchronize(m->stream));
+    long long n = 0;
+    int es = 0;
+    int e = bs_time_down(m->bs[which], m->stream, reps, flush_l2, avg_ms, &n, &es);
+    if (e) return fail(e, "solver kernel timing failed (no grid level?)");
+    if (nodes) *nodes = n;
+    if (elem_bytes) *elem_bytes = es;
+    return 0;
+}
+
 // ---- discrete adjoint of the eulerpsi step ------------------------------------
 static int adj_check(f2d_model m)
 {

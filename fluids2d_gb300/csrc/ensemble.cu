@@ -718,6 +718,20 @@ int f2d_ensemble_stats(f2d_ensemble e, int64_t* cells, int64_t* poisson_iters_su
     return 0;
 }
 
+int f2d_ensemble_time_solver(f2d_ensemble e, int reps, int flush_l2, double* avg_ms,
+                             int64_t* nodes, int* elem_bytes)
+{
+    if (!e || !avg_ms) return f2d_internal_fail(1, "null argument");
+    ECK(cudaStreamSynchronize(e->stream));
+    long long n = 0;
+    int es = 0;
+    int r = bs_time_down(e->bs, e->stream, reps, flush_l2, avg_ms, &n, &es);
+    if (r) return f2d_internal_fail(r, "solver kernel timing failed (no grid level?)");
+    if (nodes) *nodes = n;
+    if (elem_bytes) *elem_bytes = es;
+    return 0;
+}
+
 int f2d_ensemble_time_stage(f2d_ensemble e, int stage, int reps, int flush_l2,
                             double* avg_ms)
 {

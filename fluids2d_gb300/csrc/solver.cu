@@ -1011,6 +1011,72 @@ static int bs_record_t(BatchSolver& s, cudaStream_t st, cudaStream_t st2, int* l
     return (int)cudaGetLastError();
 }
 
+// Measurement hook: time `reps` launches of the level-0 down kernel (the
+// largest share of the solver's time) on the current level-0 right-hand side
+// of every member, L2 flushed between launches when asked. Every member's
+// convergence flags are cleared first so that no block returns early; the
+// next solve's set-up resets them. *nodes = level-0 nodes of all members,
+// *es = element size of the multigrid vectors.
+__global__ void k_bs_activate(DevScalars* scs, int n)
+{
+    const int b = blockIdx.x * blockDim.x + threadIdx.x;
+    if (b < n) {
+        scs[b].converged = 0;
+        scs[b].conv_in = 0;
+    }
+}
+
+template <typename S, int NU, int TH>
+static void launch_down0(BatchSolver& s, cudaStream_t st, int ir)
+{
+    k_bs_down<S, NU, TH><<<s.ntiles[0], dim3(32, 8), down_smem<S, NU, TH>(), st>>>(
+        s.tiles[0], s.dinfo, s.dlevs, 0, s.scs, ir);
+}
+
+int bs_time_down(BatchSolver& s, cudaStream_t st, int reps, int flush_l2, double* avg_ms,
+                 long long* nodes, int* es)
+{
+    if (s.maxl < 1 || reps < 1) return 1;
+    long long n0 = 0;
+    for (const MGHost& g : s.mg) n0 += (long long)g.lev[0].nyn * g.lev[0].nxn;
+    if (nodes) *nodes = n0;
+    if (es) *es = s.mode == 0 ? 8 : 4;
+    const size_t flush_bytes = 256ull << 20;
+    void* fl = nullptr;
+    if (flush_l2 && cudaMalloc(&fl, flush_bytes) != cudaSuccess) return 2;
+    cudaEvent_t a, b;
+    cudaEventCreate(&a);
+    cudaEventCreate(&b);
+    k_bs_activate<<<(s.n + 127) / 128, 128, 0, st>>>(s.scs, s.n);
+    const int ir = s.mode == 1 ? 1 : 0;
+    double total = 0.0;
+    int err = 0;
+    for (int r = 0; r < reps && !err; ++r) {
+        if (fl) cudaMemsetAsync(fl, r & 0xff, flush_bytes, st);
+        cudaEventRecord(a, st);
+        const bool two = s.nu >= 2, big = s.th == 64;
+        if (s.mode == 0) {
+            if (two) big ? launch_down0<double, 2, 64>(s, st, ir) : launch_down0<double, 2, 32>(s, st, ir);
+            else big ? launch_down0<double, 1, 64>(s, st, ir) : launch_down0<double, 1, 32>(s, st, ir);
+        } else {
+            if (two) big ? launch_down0<float, 2, 64>(s, st, ir) : launch_down0<float, 2, 32>(s, st, ir);
+            else big ? launch_down0<float, 1, 64>(s, st, ir) : launch_down0<float, 1, 32>(s, st, ir);
+        }
+        cudaEventRecord(b, st);
+        if (cudaEventSynchronize(b) != cudaSuccess) err = 3;
+        float ms = 0.f;
+        cudaEventElapsedTime(&ms, a, b);
+        total += ms;
+    }
+    if (!err && cudaGetLastError() != cudaSuccess) err = 3;
+    cudaEventDestroy(a);
+    cudaEventDestroy(b);
+    if (fl) cudaFree(fl);
+    if (err) return err;
+    *avg_ms = total / reps;
+    return 0;
+}
+
 int bs_record(BatchSolver& s, cudaStream_t st, cudaStream_t st2, int* launches)
 {
     return s.th == 64 ? bs_record_t<64>(s, st, st2, launches)

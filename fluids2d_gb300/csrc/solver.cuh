@@ -79,6 +79,9 @@ struct BatchSolver {
 int bs_build(BatchSolver& s, const std::vector<BSMemberDesc>& members,
              const uint8_t* dmask, int mode, const BSVecs& v, DevScalars* scs);
 void bs_free(BatchSolver& s);
+// measurement hook: mean ms of the level-0 down kernel over `reps` launches
+int bs_time_down(BatchSolver& s, cudaStream_t st, int reps, int flush_l2, double* avg_ms,
+                 long long* nodes, int* es);
 // Record one solve of every member on `st`: eagerly (host-driven loops, a
 // profiling aid) or, under stream capture, as conditional WHILE nodes whose
 // bodies are captured on `st2`.

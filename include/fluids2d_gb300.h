@@ -152,6 +152,14 @@ int f2d_sync(f2d_model m);
  * No reference counterpart: the measurement hook of the benchmark. */
 int f2d_time_stage(f2d_model m, int stage, int reps, int flush_l2,
                    double *avg_ms);
+/* Time `reps` launches of the Poisson solver's level-0 down kernel
+ * (pre-smoothing + residual + restriction of the V-cycle, the solver's largest
+ * share) on the current right-hand side, L2 flushed between launches when
+ * flush_l2 != 0; *avg_ms = mean ms, *nodes = level-0 nodes, *elem_bytes = 4
+ * or 8 (multigrid precision). Measurement hook of the benchmark; no
+ * reference counterpart. The model must have solved once. */
+int f2d_time_solver(f2d_model m, int reps, int flush_l2, double *avg_ms,
+                    int64_t *nodes, int *elem_bytes);
 /* Counters: Poisson iterations summed over all solves since creation; the
  * kernels one time step launches outside the Poisson loops; the kernels one
  * Poisson iteration launches. No reference counterpart (instrumentation). */
@@ -202,6 +210,9 @@ int f2d_ensemble_stats(f2d_ensemble e, int64_t *cells, int64_t *poisson_iters,
  * hook of the benchmark; no reference counterpart). */
 int f2d_ensemble_time_stage(f2d_ensemble e, int stage, int reps, int flush_l2,
                             double *avg_ms);
+/* f2d_time_solver for the batched solver of all members. */
+int f2d_ensemble_time_solver(f2d_ensemble e, int reps, int flush_l2, double *avg_ms,
+                             int64_t *nodes, int *elem_bytes);
 
 /* ---- discrete adjoint (eulerpsi, closed basin, weno/upwind fluxes) ------ */
 
