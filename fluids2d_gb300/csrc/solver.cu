@@ -93,24 +93,31 @@ __device__ __forceinline__ void stage_region(const MGLevel& L, int J0, int I0,
     }
 }
 
-// Red-black half sweep of colour `color` (0: (J+I) even) on the nodes of the
-// staged region at distance >= s from its edge: x = (b - offdiag(x)) / diag.
-// The tile origin is even, so the colour of a region node is the parity of
-// its region coordinates.
+// Red-black half sweep of colour `color` (0: (J+I) even) on the staged
+// region: every node of that colour in rows 1..WY-2 gets
+// x = (b - offdiag(x)) / diag at fluid nodes (non-fluid nodes keep x = 0). The tile origin is even, so the colour of
+// a region node is the parity of its region coordinates. Nodes within s of
+// the region edge are updated from neighbours that are no longer exact (or,
+// in columns 0 and W-1, from the neighbouring row); by induction the values
+// at distance >= s from the edge are exact after half sweep s, and the kernels
+// only read those afterwards. Updating the whole region keeps the loop free
+// of range tests, with a compile-time trip count.
 template <typename S, int W, int WY>
-__device__ __forceinline__ void half_sweep(S* sx, const S* sb, const uint8_t* sm, int s,
-                                           int color, S cx, S cy, S id)
+__device__ __forceinline__ void half_sweep(S* sx, const S* sb, const uint8_t* sm, int color,
+                                           S cx, S cy, S id)
 {
-    constexpr int HW = W / 2;
-    const int n = (WY - 2 * s) * HW;
-    for (int e = tid256(); e < n; e += 256) {
-        const int rr = s + e / HW;
+    constexpr int HW = W / 2, n = (WY - 2) * HW, IT = (n + 255) / 256;
+    const int t = tid256();
+#pragma unroll
+    for (int it = 0; it < IT; ++it) {
+        const int e = t + 256 * it;
+        if (n % 256 != 0 && e >= n) break;
+        const int rr = 1 + e / HW;
         const int cc = 2 * (e % HW) + ((color + rr) & 1);
-        if (cc < s || cc >= W - s) continue;
         const int q = rr * W + cc;
-        if (!sm[q]) continue;
         const S off = cx * (sx[q - 1] + sx[q + 1]) + cy * (sx[q - W] + sx[q + W]);
-        sx[q] = (sb[q] - off) * id;
+        const S v = (sb[q] - off) * id;
+        sx[q] = sm[q] ? v : S(0);
     }
 }
 
@@ -226,23 +233,24 @@ k_bs_down(const int4* __restrict__ tiles, const BSInfo* __restrict__ info,
     __syncthreads();
 #pragma unroll
     for (int s = 1; s < 2 * NU; ++s) {
-        half_sweep<S, W, WY>(sx, sb, sm, s, s & 1, cx, cy, id);
+        half_sweep<S, W, WY>(sx, sb, sm, s & 1, cx, cy, id);
         __syncthreads();
     }
-    // residual at the red nodes of the region shrunk by 2 NU (in place of b)
+    // residual at the red nodes (in place of b; exact at distance >= 2 NU
+    // from the region edge, which is all the restriction reads)
     {
-        constexpr int HW = W / 2, s = 2 * NU;
-        const int n = (WY - 2 * s) * HW;
-        for (int e = t; e < n; e += 256) {
-            const int rr = s + e / HW;
+        constexpr int HW = W / 2, n = (WY - 2) * HW, IT = (n + 255) / 256;
+        const S md = Coef<S>::md(F);
+#pragma unroll
+        for (int it = 0; it < IT; ++it) {
+            const int e = t + 256 * it;
+            if (n % 256 != 0 && e >= n) break;
+            const int rr = 1 + e / HW;
             const int cc = 2 * (e % HW) + (rr & 1);
-            if (cc < s || cc >= W - s) continue;
             const int q = rr * W + cc;
-            S v = S(0);
-            if (sm[q])
-                v = sb[q] - apply_diff<S>(cx, cy, Coef<S>::md(F), sx[q], sx[q - 1], sx[q + 1],
-                                          sx[q - W], sx[q + W]);
-            sb[q] = v;
+            const S v = sb[q] - apply_diff<S>(cx, cy, md, sx[q], sx[q - 1], sx[q + 1],
+                                              sx[q - W], sx[q + W]);
+            sb[q] = sm[q] ? v : S(0);
         }
     }
     __syncthreads();
@@ -321,7 +329,32 @@ k_bs_up(const int4* __restrict__ tiles, const BSInfo* __restrict__ info,
             }
         }
     }
-    stage_region<H, TH, S, S>(F, J0, I0, (const S*)F.xa, sx, lb<S>(F), sb, sm);
+    const S cx = Coef<S>::cx(F), cy = Coef<S>::cy(F), id = Coef<S>::idiag(F);
+    {
+        constexpr int IT = (N + 255) / 256;
+        const S* __restrict__ gx = (const S*)F.xa;
+        const S* __restrict__ gb = lb<S>(F);
+#pragma unroll
+        for (int k2 = 0; k2 < IT; ++k2) {
+            const int e = t + k2 * 256;
+            if (e < N) {
+                const int r = e / W, c = e - r * W;
+                const int J = J0 - H + r;
+                int I = I0 - H + c;
+                uint8_t mv = 0;
+                S xv = S(0), bv = S(0);
+                if (in_level(F, J, I)) {
+                    const long long k = nidx(F, J, I);
+                    mv = F.m[k];
+                    xv = gx[k];
+                    bv = gb[k];
+                }
+                sm[e] = mv;
+                sx[e] = mv ? xv : S(0);
+                sb[e] = mv ? bv : S(0);
+            }
+        }
+    }
     __syncthreads();
     for (int e = t; e < N; e += 256) {
         if (!sm[e]) continue;
@@ -338,10 +371,9 @@ k_bs_up(const int4* __restrict__ tiles, const BSInfo* __restrict__ info,
         sx[e] += v;
     }
     __syncthreads();
-    const S cx = Coef<S>::cx(F), cy = Coef<S>::cy(F), id = Coef<S>::idiag(F);
 #pragma unroll
     for (int s = 1; s <= 2 * NU; ++s) {
-        half_sweep<S, W, WY>(sx, sb, sm, s, s & 1, cx, cy, id);
+        half_sweep<S, W, WY>(sx, sb, sm, s & 1, cx, cy, id);
         __syncthreads();
     }
     S* x = lx<S>(F);
