@@ -359,14 +359,15 @@ static int launch_stage_kernel(f2d_model_s* m, int k, int par, cudaStream_t s)
         CKI(make_tmap(m, (void*)a.h));
         CKI(make_tmap(m, om));
         CKI(launch_rsw_stage(m->p.vortexforce, m->prec, tmap(m, (void*)a.h), tmap(m, om), a,
-                             m->d_code, k, g, m->sc, s));
+                             m->d_code, k | (m->p.integrator << 4), g, m->sc, s));
     } else {
         const char* q = m->p.model == F2D_MODEL_EULERPSI ? "omega" : "pv";
         void* qin = fb(m, q, par);
         CKI(make_tmap(m, qin));
         CKI(launch_fluxform_stage(m->p.compflux, m->prec, tmap(m, qin), qin, fb(m, q, out),
                                   fb(m, "U.x"), fb(m, "U.y"), m->d_code,
-                                  k < 3 ? ds(q, k) : nullptr, ds(q, 1), ds(q, 2), k, g,
+                                  k < 3 ? ds(q, k) : nullptr, ds(q, 1), ds(q, 2),
+                                  k | (m->p.integrator << 4), g,
                                   m->sc, s));
     }
     m->rec_launches += 1;
@@ -387,7 +388,9 @@ static int rec_step(f2d_model_s* m, int par, bool with_dt, cudaStream_t s)
         CKI(launch_set_dt(m->sc, s));
         m->rec_launches += 1;
     }
-    for (int k = 1; k <= 3; ++k) {
+    // SSP-RK3 / enrk3: 3 stages, ef: 1 (an odd count: a step flips the parity)
+    const int nst = m->p.integrator == F2D_INTEG_EF ? 1 : 3;
+    for (int k = 1; k <= nst; ++k) {
         int e = rec_stage(m, k, par, s);
         if (e) return e;
         par = 1 - par;
@@ -644,6 +647,8 @@ int f2d_model_create(const f2d_params* p, const int8_t* msk, f2d_model* out)
     if (p->precision != F2D_PREC_FP64 && p->precision != F2D_PREC_FP32)
         return fail(1, "unknown precision");
     if (p->model < 0 || p->model > 2) return fail(1, "unknown model");
+    if (p->integrator < F2D_INTEG_RK3 || p->integrator > F2D_INTEG_ENRK3)
+        return fail(1, "unknown integrator (rk3, ef, enrk3)");
     if (p->xperiodic && p->nx < 6) return fail(1, "x-periodic needs nx >= 6");
     if (p->model == F2D_MODEL_RSW && p->vortexforce != p->compflux)
         return fail(1, "the fused rsw stage uses one flux method for vortexforce and "
@@ -1087,6 +1092,7 @@ static int adj_check(f2d_model m)
     if (m->g.xper) return fail(1, "the adjoint covers closed (non-periodic) domains");
     if (m->p.compflux != F2D_METHOD_WENO && m->p.compflux != F2D_METHOD_UPWIND)
         return fail(1, "the adjoint covers the weno and upwind flux methods");
+    if (m->p.integrator != F2D_INTEG_RK3) return fail(1, "the adjoint covers SSP-RK3");
     return 0;
 }
 

@@ -308,10 +308,12 @@ static int ens_record_step(f2d_ensemble_s* e, int par, cudaStream_t s)
     const dim3 blk(32, 8);
     k_ens_set_dt<<<(e->n + 127) / 128, 128, 0, s>>>(e->scs, e->n);
     e->rec += 1;
-    for (int k = 1; k <= 3; ++k) {
+    const int nst = e->p.integrator == F2D_INTEG_EF ? 1 : 3;  // odd: flips the parity
+    for (int k = 1; k <= nst; ++k) {
+        const int sk = k | (e->p.integrator << 4);
 #define ENS_FF(T, M)                                                                       \
     k_ens_fluxform_stage<T, M><<<e->ncell, blk, 0, s>>>(e->cell_tiles, e->dmem, e->ar, par, \
-                                                        k, e->scs, e->eg)
+                                                        sk, e->scs, e->eg)
         const int M = e->p.compflux;
         if (e->prec == 0) {
             if (M == METHOD_WENO) ENS_FF(double, METHOD_WENO);
@@ -392,6 +394,8 @@ int f2d_ensemble_create(const f2d_params* p, int count, const int* nxs, const in
         return f2d_internal_fail(1, "bad ensemble arguments");
     if (p->model != F2D_MODEL_EULERPSI && p->model != F2D_MODEL_QG)
         return f2d_internal_fail(1, "ensembles run the eulerpsi and qg models");
+    if (p->integrator < F2D_INTEG_RK3 || p->integrator > F2D_INTEG_ENRK3)
+        return f2d_internal_fail(1, "unknown integrator (rk3, ef, enrk3)");
     if (p->dt > 0)
         return f2d_internal_fail(1, "ensembles use the per-member CFL time step (dt = 0)");
     auto* e = new f2d_ensemble_s();
@@ -751,7 +755,9 @@ int f2d_ensemble_time_stage(f2d_ensemble e, int stage, int reps, int flush_l2,
         cudaEventRecord(a, e->stream);
 #define ENS_FF(T, M)                                                                       \
     k_ens_fluxform_stage<T, M><<<e->ncell, blk, 0, e->stream>>>(e->cell_tiles, e->dmem,   \
-                                                                e->ar, par, stage, e->scs, \
+                                                                e->ar, par,               \
+                                                                stage | (e->p.integrator << 4), \
+                                                                e->scs,                   \
                                                                 e->eg)
         const int M = e->p.compflux;
         if (e->prec == 0) {

@@ -50,6 +50,8 @@ k_rsw_stage(const __grid_constant__ CUtensorMap th,
     __shared__ T sfy[TY + 1][TX];
     __shared__ T srk[4];  // RK3 coefficients, Coriolis parameter
     __shared__ uint64_t bar;
+    const int sk = stage;  // stage | integrator << 4
+    stage &= 15;
     const int tx = threadIdx.x, ty = threadIdx.y, t = ty * TX + tx;
     const int i0 = blockIdx.x * TX, j0 = blockIdx.y * TY;
     const T* __restrict__ Ux = (const T*)a.Ux;
@@ -128,7 +130,7 @@ k_rsw_stage(const __grid_constant__ CUtensorMap th,
         }
     }
     if (tx == 0 && ty == 0) {
-        rk3_coefs<T>(stage, sc->dt, srk);
+        rk3_coefs<T>(sk, sc->dt, srk);
         srk[3] = T(a.fc);
     }
     __syncthreads();

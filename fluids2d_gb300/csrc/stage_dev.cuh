@@ -31,6 +31,30 @@ __device__ __forceinline__ T ldz(const T* __restrict__ a, int j, int i,
 template <typename T>
 __device__ __forceinline__ void rk3_coefs(int stage, double dt, T* c)
 {
+    // stage = k | (integrator << 4); the coefficients of ef (integrators.py:
+    // 116-123) and enrk3 (140-155) in the reference's evaluation order
+    const int integ = stage >> 4;
+    stage &= 15;
+    if (integ == 1) {
+        c[0] = T(dt);
+        c[1] = c[2] = T(0);
+        return;
+    }
+    if (integ == 2) {
+        if (stage == 1) {
+            c[0] = T(dt / 3);
+            c[1] = c[2] = T(0);
+        } else if (stage == 2) {
+            c[0] = T(-dt / 3 - 5 * dt / 48);
+            c[1] = T(15 * dt / 16);
+            c[2] = T(0);
+        } else {
+            c[0] = T(5 * dt / 48 + dt / 10);
+            c[1] = T(-7 * dt / 16);
+            c[2] = T(2 * dt / 5);
+        }
+        return;
+    }
     if (stage == 1) {
         c[0] = T(dt);
         c[1] = c[2] = T(0);
@@ -121,6 +145,8 @@ __device__ __forceinline__ void fluxform_tile(
     auto& sfx = sm.sfx;
     auto& sfy = sm.sfy;
     const int tx = threadIdx.x, ty = threadIdx.y, t = ty * TX + tx;
+    const int sk = stage;  // stage | integrator << 4
+    stage &= 15;
     (void)qin;
     // 1. the TMA load of the staged tile (q with its 3-cell halo) ...
     if (t == 0) mbar_init(&sm.bar, 1);
@@ -202,7 +228,7 @@ __device__ __forceinline__ void fluxform_tile(
     }
     if (ex == 1) xflux(er, ec, ce, ue);
     else if (ex == 2) yflux(er, ec, ce, ue);
-    if (t == 0) rk3_coefs<T>(stage, dt, sm.rk);
+    if (t == 0) rk3_coefs<T>(sk, dt, sm.rk);
     __syncthreads();
 
     // 5. tendency, RK3 update and stores of this thread's cells

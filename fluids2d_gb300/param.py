@@ -15,7 +15,7 @@ _integrators = ["rk3", "ef", "enrk3", "LFRA"]
 
 # models and integrators the GPU path implements
 SUPPORTED_MODELS = ("eulerpsi", "rsw", "qg")
-SUPPORTED_INTEGRATORS = ("rk3",)
+SUPPORTED_INTEGRATORS = ("rk3", "ef", "enrk3")
 EXTRA = ("precision", "poisson_tol", "poisson_maxit")
 
 
@@ -90,7 +90,8 @@ class Param:
                 f"{', '.join(SUPPORTED_MODELS)}")
         if self.integrator not in SUPPORTED_INTEGRATORS:
             raise NotImplementedError(
-                f"integrator {self.integrator!r}: the GPU path implements rk3")
+                f"integrator {self.integrator!r}: the GPU path implements "
+                f"{', '.join(SUPPORTED_INTEGRATORS)}")
         if self.tracer not in (None, "None"):
             raise NotImplementedError("tracer equations are not implemented")
         if self.halowidth != 3:

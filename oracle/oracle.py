@@ -496,6 +496,26 @@ class Model:
         self._addto([-dt / 12, -dt / 12, 2 * dt / 3], [ds1, ds2, ds3])
         self.diag()
 
+    def ef(self, dt):
+        """integrators.py:116-123."""
+        (ds1,) = self.scratch[:1]
+        self.rhs(self.s, ds1)
+        self._addto([dt], [ds1])
+        self.diag()
+
+    def enrk3(self, dt):
+        """integrators.py:140-155."""
+        ds1, ds2, ds3 = self.scratch
+        self.rhs(self.s, ds1)
+        self._addto([dt / 3], [ds1])
+        self.diag()
+        self.rhs(self.s, ds2)
+        self._addto([-dt / 3 - 5 * dt / 48, 15 * dt / 16], [ds1, ds2])
+        self.diag()
+        self.rhs(self.s, ds3)
+        self._addto([5 * dt / 48 + dt / 10, -7 * dt / 16, 2 * dt / 5], [ds1, ds2, ds3])
+        self.diag()
+
     def pushforward(self):
         """timeline.py:20-35 (Kahan-summed time)."""
         y = self.dt - self._c
@@ -519,8 +539,10 @@ class Model:
         self.dt = min(p.cfl / maxU, p.dtmax)
 
     def step(self, n=1):
+        integ = {"rk3": self.rk3, "ef": self.ef,
+                 "enrk3": self.enrk3}[getattr(self.p, "integrator", "rk3")]
         for _ in range(n):
-            self.rk3(self.dt)
+            integ(self.dt)
             self.pushforward()
 
     def run_steps(self, n):

@@ -208,6 +208,8 @@ def run_model(case, nsteps, fname, cfl=None, extra=None):
                                 p.H, p.cfl])}
     if "f" in case:
         out["f"] = case["f"].copy()
+    if extra and "integrator" in extra:
+        out["integrator"] = np.array(extra["integrator"])
     for k, v in case["fields"].items():
         out["ic/" + k] = v.copy()
 
@@ -255,8 +257,19 @@ def model_cases():
     run_model(c, 5, "model_qg.npz")
 
 
+def integrator_cases():
+    """The reference's other Runge-Kutta integrators (integrators.py:116-155)."""
+    c = wl.eulerpsi_case(n=40, ny=32, seed=2, nislands=2, nvortices=5,
+                         radius=0.08)
+    run_model(c, 4, "model_eulerpsi_ef.npz", cfl=0.4, extra={"integrator": "ef"})
+    run_model(c, 4, "model_eulerpsi_enrk3.npz", cfl=0.8,
+              extra={"integrator": "enrk3"})
+    c = wl.rsw_case(n=40, ny=32, seed=3, nislands=2)
+    run_model(c, 4, "model_rsw_enrk3.npz", extra={"integrator": "enrk3"})
+
+
 if __name__ == "__main__":
-    which = sys.argv[1:] or ["mesh", "sweeps", "poisson", "models"]
+    which = sys.argv[1:] or ["mesh", "sweeps", "poisson", "models", "integrators"]
     if "mesh" in which:
         mesh_cases()
     if "sweeps" in which:
@@ -265,3 +278,5 @@ if __name__ == "__main__":
         poisson_cases()
     if "models" in which:
         model_cases()
+    if "integrators" in which:
+        integrator_cases()

@@ -125,7 +125,8 @@ def test_poisson_zero_rhs():
 
 # -------------------------------------------------------------- models ----
 MODEL_FILES = ["model_eulerpsi.npz", "model_eulerpsi_islands.npz",
-               "model_rsw.npz", "model_qg.npz"]
+               "model_rsw.npz", "model_qg.npz", "model_eulerpsi_ef.npz",
+               "model_eulerpsi_enrk3.npz", "model_rsw_enrk3.npz"]
 
 
 def model_from_golden(g):
@@ -133,8 +134,10 @@ def model_from_golden(g):
     Lx, Ly, f0, beta, gg, H, cfl = (float(v) for v in g["scalars"])
     names = {k[3:] for k in g.files if k.startswith("ic/")}
     kind = ("eulerpsi" if "omega" in names else "rsw" if "h" in names else "qg")
+    integ = str(g["integrator"]) if "integrator" in g.files else "rk3"
     m = _model(kind, nx, ny, g["msk"], xperiodic=bool(xper), Lx=Lx, Ly=Ly, f0=f0,
-               beta=beta, g=gg, H=H, cfl=cfl, tend=1e300, maxite=10 ** 9)
+               beta=beta, g=gg, H=H, cfl=cfl, tend=1e300, maxite=10 ** 9,
+               integrator=integ)
     if "f" in g.files:
         m.mesh.f = g["f"]
     s = m.state
@@ -186,10 +189,10 @@ def test_model_steps_vs_reference(fname):
     assert m.time.ite == len(dts)
 
 
-def _oracle_like(case, kind):
+def _oracle_like(case, kind, **extra):
     p = O.Param(model=kind, nx=case["nx"], ny=case["ny"],
                 xperiodic=case.get("xperiodic", False), Lx=case["Lx"],
-                Ly=case["Ly"], tend=1e300, maxite=10 ** 9)
+                Ly=case["Ly"], tend=1e300, maxite=10 ** 9, **extra)
     for k in ("f0", "g", "H", "beta"):
         if k in case:
             setattr(p, k, case[k])
@@ -225,6 +228,36 @@ def test_model_vs_oracle_larger(kind):
     m.integrator.diag(s)
     compare(m, lambda k: om.s.get(k), STEP_TOL)
     for _ in range(4):
+        om.run_steps(1)
+        m.advance(1)
+        assert abs(m.time.dt - om.dt) <= 1e-10 * om.dt
+        compare(m, lambda k: om.s.get(k), STEP_TOL)
+    m.sync()
+
+
+@pytest.mark.parametrize("kind", ["eulerpsi", "rsw"])
+@pytest.mark.parametrize("method", ["upwind", "centered", "cweno"])
+def test_model_flux_methods_vs_oracle(kind, method):
+    """The fused stage kernels with the reference's other flux methods
+    (weno.py:338-343): whole steps against the oracle."""
+    if kind == "eulerpsi":
+        case = wl.eulerpsi_case(n=64, ny=48, seed=15, nislands=2)
+        extra = dict(compflux=method)
+    else:
+        case = wl.rsw_case(n=64, ny=48, seed=16, nislands=2)
+        extra = dict(compflux=method, vortexforce=method, innerproduct=method)
+    om = _oracle_like(case, kind, **extra)
+    kw = dict(xperiodic=case.get("xperiodic", False), Lx=case["Lx"], Ly=case["Ly"],
+              tend=1e300, maxite=10 ** 9, **extra)
+    for k in ("f0", "g", "H", "beta"):
+        if k in case:
+            kw[k] = case[k]
+    m = _model(kind, case["nx"], case["ny"], case["msk"], **kw)
+    s = m.state
+    for k, v in case["fields"].items():
+        getattr(s, k)[:] = v
+    m.integrator.diag(s)
+    for _ in range(3):
         om.run_steps(1)
         m.advance(1)
         assert abs(m.time.dt - om.dt) <= 1e-10 * om.dt
