@@ -15,7 +15,8 @@ from fluids2d_gb300 import _lib
 def declared_functions():
     names = set()
     for h in glob.glob(os.path.join(ROOT, "include", "*.h")):
-        src = open(h).read()
+        with open(h) as f:
+            src = f.read()
         src = re.sub(r"/\*.*?\*/", "", src, flags=re.S)
         names.update(re.findall(r"\b(f2d_[a-z0-9_]+)\s*\(", src))
     return sorted(names)
