@@ -45,7 +45,7 @@ def _worker(rank, world, port, out):
 def test_replica_timing_and_value_over_gloo():
     world = 2
     port = _free_port()
-    with mp.Manager() as man:
+    with mp.get_context("spawn").Manager() as man:
         out = man.dict()
         mp.spawn(_worker, args=(world, port, out), nprocs=world, join=True)
         res = dict(out)
