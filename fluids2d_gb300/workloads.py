@@ -180,6 +180,44 @@ def qg_case(n=4096, seed=0, nislands=20, ny=None, Lx=1.0, Ly=1.0,
                 beta=beta, g=g, H=H, fields={"pv": pv}, f=fv)
 
 
+def euler_case(n=128, seed=0, nislands=2, ny=None, Lx=1.0, Ly=1.0, xperiodic=False,
+               nvortices=6, radius=0.08, noise=0.05):
+    """Euler (momentum-pressure form) with an initial velocity that is not
+    divergence-free: the covariant velocity of a streamfunction made of
+    Gaussian vortices (form of vortex.py's initial condition) plus a random
+    divergent part of relative size `noise`, masked by mskx/msky, so that the
+    first diagnostic's pressure projection has work to do."""
+    nx = n
+    ny = n if ny is None else ny
+    x, y = grid_coords(nx, ny, Lx, Ly, which="c")
+    msk = default_mask(nx, ny, xperiodic=xperiodic)
+    if nislands:
+        carve_islands(msk, x, y, nislands, 0.03 * Lx, 0.08 * Lx, seed + 1000,
+                      Lx, Ly, margin=0.1 * Lx)
+    xv, yv = grid_coords(nx, ny, Lx, Ly, which="v")
+    psi = gaussian_vortices(xv, yv, nvortices, radius * Lx, seed, Lx, Ly)
+    psi *= (Lx / nx) * (Ly / ny) * 0.5
+    mx = np.zeros_like(msk)
+    mx[:, 1:] = msk[:, 1:] * msk[:, :-1]
+    my = np.zeros_like(msk)
+    my[1:, :] = msk[1:, :] * msk[:-1, :]
+    ux = np.zeros(msk.shape)
+    uy = np.zeros(msk.shape)
+    ux[:-1, :] = -(psi[1:, :] - psi[:-1, :])
+    uy[:, :-1] = psi[:, 1:] - psi[:, :-1]
+    rng = np.random.default_rng(seed + 7)
+    scale = noise * max(np.abs(ux).max(), np.abs(uy).max(), 1e-300)
+    ux = (ux + scale * rng.standard_normal(msk.shape)) * mx
+    uy = (uy + scale * rng.standard_normal(msk.shape)) * my
+    if xperiodic:
+        hw = 3
+        for a in (ux, uy):
+            a[:, :hw] = a[:, -2 * hw:-hw]
+            a[:, -hw:] = a[:, hw:2 * hw]
+    return dict(model="euler", nx=nx, ny=ny, Lx=Lx, Ly=Ly, msk=msk,
+                xperiodic=xperiodic, fields={"u.x": ux, "u.y": uy})
+
+
 def ensemble_case(count=256, seed=0, sizes=(64, 128, 192, 256, 384, 512),
                   max_islands=4, nvortices=8, radius=0.05):
     """Batched ensemble of closed-basin eulerpsi members: grid sizes drawn

@@ -216,6 +216,14 @@ class Mesh:
         return self._solvers["v"]
 
     @property
+    def poisson_centers(self):
+        """Poisson2D(mesh, "c"): Neumann cell-centred operator (singular; the
+        reference factorises it anyway and SuperLU picks the constant)."""
+        if "c" not in self._solvers:
+            self._solvers["c"] = Poisson2D(self, maindiag=0, location="c")
+        return self._solvers["c"]
+
+    @property
     def qg_helmholtz(self):
         if "h" not in self._solvers:
             self._solvers["h"] = Poisson2D(self, maindiag=self.maindiag)
@@ -252,12 +260,13 @@ def vertex_msk(mesh, location="v"):
     return m
 
 
-def laplacian(mesh, maindiag):
-    """Masked 5-point vertex operator with Dirichlet walls
-    (get_Laplacian_sparse, elliptic.py:114-195), assembled with numpy in the
-    reference's entry order (per point: west, east, south, north, diagonal)
-    so that SuperLU sees the same matrix."""
-    G = gindex(vertex_msk(mesh))
+def laplacian(mesh, maindiag, location="v"):
+    """Masked 5-point operator (get_Laplacian_sparse, elliptic.py:114-195):
+    vertices with Dirichlet walls, or cell centres with Neumann walls (the
+    diagonal is minus the sum of the present neighbours' couplings),
+    assembled with numpy in the reference's entry order (per point: west,
+    east, south, north, diagonal) so that SuperLU sees the same matrix."""
+    G = gindex(vertex_msk(mesh, location))
     ny, nx = G.shape
     N = int(np.sum(G > -1))
     dx2 = mesh.dy / mesh.dx
@@ -272,10 +281,17 @@ def laplacian(mesh, maindiag):
                     G[J, n1] if xper else -1)
     south = np.where(J > 0, G[np.maximum(J - 1, 0), I], -1)
     north = np.where(J < ny - 1, G[np.minimum(J + 1, ny - 1), I], -1)
-    diag = -2 * (dx2 + dy2) - maindiag
+    if location == "v":
+        diag = np.full(N, -2 * (dx2 + dy2) - maindiag)
+    else:
+        # sum_extra_diag accumulated in the reference's order
+        sed = np.zeros(N)
+        for nb, c in ((west, dx2), (east, dx2), (south, dy2), (north, dy2)):
+            sed = np.where(nb > -1, sed + c, sed)
+        diag = -sed - maindiag
     cols = np.stack([west, east, south, north, Ipt], axis=1)
     vals = np.stack([np.full(N, dx2), np.full(N, dx2), np.full(N, dy2),
-                     np.full(N, dy2), np.full(N, diag)], axis=1)
+                     np.full(N, dy2), diag], axis=1)
     valid = cols > -1
     rows = np.repeat(Ipt[:, None], 5, axis=1)
     cnt = int(valid.sum())
@@ -293,9 +309,9 @@ class Poisson2D:
     """Poisson2D "v" (elliptic.py:71-87): LU factorisation once, then
     back-substitution; only fluid points of x are written, then halo fill."""
 
-    def __init__(self, mesh, maindiag=0):
+    def __init__(self, mesh, maindiag=0, location="v"):
         self.mesh = mesh
-        self.A, self.G = laplacian(mesh, maindiag)
+        self.A, self.G = laplacian(mesh, maindiag, location)
         self.lu = splinalg.splu(self.A)
 
     def solve(self, b, x):
@@ -365,6 +381,24 @@ def compute_kinetic_energy(p, mesh, ux, uy, Ux, Uy, ke, pysq):
     ke *= mesh.msk * 0.5
 
 
+def div_vector(mesh, Ux, Uy, delta):
+    """div (operators.py:104-107) of a vector field; delta's last column
+    keeps its previous value, as in the reference."""
+    delta[:, :-1] = -np.diff(Ux, axis=1)
+    delta[:-1, :] -= np.diff(Uy, axis=0)
+    delta *= mesh.msk
+
+
+def pressure_projection(mesh, Ux, Uy, delta, p, ux, uy):
+    """operators.py:114-119."""
+    sharp(mesh, ux, uy, Ux, Uy)
+    div_vector(mesh, Ux, Uy, delta)
+    mesh.poisson_centers.solve(-delta * mesh.area, p)
+    addgrad(mesh, p, ux, uy)
+    mesh.fill(ux)
+    mesh.fill(uy)
+
+
 def compute_pressure(p, mesh, h, out):
     """operators.py:110-111."""
     out[:] = (p.g / mesh.area) * (h + mesh.hb)
@@ -388,12 +422,14 @@ def perpgrad(mesh, psi, Ux, Uy, contravariant=False):
 # ------------------------------------------------------------- model -----
 
 STATE_VARS = {
+    "euler": ("u", "U", "omega", "ke", "p", "div", "flx"),
     # states.py:7-17 (the models on the hot path); vector fields get .x/.y
     "eulerpsi": ("omega", "U", "psi", "vomega", "flx"),
     "rsw": ("u", "h", "U", "omega", "ke", "p", "flx", "pv"),
     "qg": ("pv", "U", "h", "flx", "work", "psi"),
 }
-PROGNOSTIC = {"eulerpsi": ("omega",), "rsw": ("u", "h"), "qg": ("pv",)}
+PROGNOSTIC = {"eulerpsi": ("omega",), "rsw": ("u", "h"), "qg": ("pv",),
+              "euler": ("u",)}
 VECTORS = ("u", "U", "flx")
 
 
@@ -451,6 +487,13 @@ class Model:
                     ds["h"], sq)
             for k in ("u.x", "u.y", "h"):
                 m.fill(ds[k])
+        elif p.model == "euler":
+            # equations.py:11-15
+            addvortexforce(p, m, s["U.x"], s["U.y"], s["omega"], ds["u.x"],
+                           ds["u.y"], sq)
+            addgrad(m, s["ke"], ds["u.x"], ds["u.y"])
+            for k in ("u.x", "u.y"):
+                m.fill(ds[k])
 
     def diag(self, s=None):
         s = self.s if s is None else s
@@ -468,6 +511,16 @@ class Model:
                 s["work"] -= m.f
             m.qg_helmholtz.solve(s["work"], s["psi"])
             perpgrad(m, s["psi"], s["U.x"], s["U.y"], contravariant=True)
+        elif p.model == "euler":
+            # equations.py:17-22
+            pressure_projection(m, s["U.x"], s["U.y"], s["div"], s["p"],
+                                s["u.x"], s["u.y"])
+            sharp(m, s["u.x"], s["u.y"], s["U.x"], s["U.y"])
+            compute_vorticity(m, s["u.x"], s["u.y"], s["omega"])
+            compute_kinetic_energy(p, m, s["u.x"], s["u.y"], s["U.x"],
+                                   s["U.y"], s["ke"], sq)
+            m.fill(s["omega"])
+            m.fill(s["ke"])
         elif p.model == "rsw":
             sharp(m, s["u.x"], s["u.y"], s["U.x"], s["U.y"])
             compute_vorticity(m, s["u.x"], s["u.y"], s["omega"])

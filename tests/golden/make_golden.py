@@ -198,7 +198,10 @@ def run_model(case, nsteps, fname, cfl=None, extra=None):
     if "f" in case:
         m.mesh.f = case["f"].copy()
     for k, v in case["fields"].items():
-        getattr(m.state, k)[:] = v
+        if "." in k:
+            getattr(getattr(m.state, k.split(".")[0]), k.split(".")[1])[:] = v
+        else:
+            getattr(m.state, k)[:] = v
     m.integrator.diag(m.state)
 
     out = {"msk": case["msk"].copy(),
@@ -257,6 +260,15 @@ def model_cases():
     run_model(c, 5, "model_qg.npz")
 
 
+def euler_cases():
+    """The euler model (equations.py:9-24): momentum-pressure form with the
+    Neumann cell-centred pressure projection (operators.py:114-119)."""
+    c = wl.euler_case(n=40, ny=32, seed=5, nislands=2)
+    run_model(c, 4, "model_euler.npz", cfl=0.5)
+    c = wl.euler_case(n=40, ny=32, seed=6, nislands=2, xperiodic=True)
+    run_model(c, 4, "model_euler_periodic.npz", cfl=0.5)
+
+
 def integrator_cases():
     """The reference's other Runge-Kutta integrators (integrators.py:116-155)."""
     c = wl.eulerpsi_case(n=40, ny=32, seed=2, nislands=2, nvortices=5,
@@ -269,7 +281,8 @@ def integrator_cases():
 
 
 if __name__ == "__main__":
-    which = sys.argv[1:] or ["mesh", "sweeps", "poisson", "models", "integrators"]
+    which = sys.argv[1:] or ["mesh", "sweeps", "poisson", "models", "integrators",
+                             "euler"]
     if "mesh" in which:
         mesh_cases()
     if "sweeps" in which:
@@ -280,3 +293,5 @@ if __name__ == "__main__":
         model_cases()
     if "integrators" in which:
         integrator_cases()
+    if "euler" in which:
+        euler_cases()

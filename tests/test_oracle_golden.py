@@ -104,7 +104,8 @@ def test_poisson_vs_reference(case):
 
 MODEL_FILES = ["model_eulerpsi.npz", "model_eulerpsi_islands.npz",
                "model_rsw.npz", "model_qg.npz", "model_eulerpsi_ef.npz",
-               "model_eulerpsi_enrk3.npz", "model_rsw_enrk3.npz"]
+               "model_eulerpsi_enrk3.npz", "model_rsw_enrk3.npz",
+               "model_euler.npz", "model_euler_periodic.npz"]
 
 
 def oracle_from_golden(g, pysq=True):
@@ -113,7 +114,7 @@ def oracle_from_golden(g, pysq=True):
     model = [k for k in g.files if k.startswith("ic/")]
     names = {k[3:] for k in model}
     kind = ("eulerpsi" if "omega" in names else
-            "rsw" if "h" in names else "qg")
+            "rsw" if "h" in names else "euler" if "u.x" in names else "qg")
     integ = str(g["integrator"]) if "integrator" in g.files else "rk3"
     p = O.Param(model=kind, nx=nx, ny=ny, xperiodic=bool(xper), Lx=Lx, Ly=Ly,
                 f0=f0, beta=beta, g=gg, H=H, cfl=cfl, tend=1e9,
