@@ -20,7 +20,7 @@ LIB = os.path.join(BUILD, "libfluids2d_gb300.so")
 INCLUDE = os.path.join(ROOT, "include")
 
 SOURCES = ["api.cu", "stage.cu", "mg.cu", "sweeps.cu", "mesh_host.cu",
-           "noalloc.cu", "ensemble.cu", "solver.cu", "adjoint.cu"]
+           "noalloc.cu", "ensemble.cu", "solver.cu", "adjoint.cu", "nsolver.cu"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 FLAGS = ["-std=c++17", "-O3", "-lineinfo", "-Xcompiler", "-fPIC",
          "-Xcompiler", "-O2", "--expt-relaxed-constexpr", "-I", INCLUDE]

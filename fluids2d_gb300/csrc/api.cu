@@ -14,6 +14,7 @@
 #include "../../include/fluids2d_gb300.h"
 #include "adjoint.cuh"
 #include "mesh_host.h"
+#include "nsolver.cuh"
 #include "stage_dev.cuh"
 #include "solver.cuh"
 #include "stage.cuh"
@@ -125,6 +126,10 @@ struct f2d_model_s {
     cudaGraphExec_t gx[7][2] = {};
     int launches[7][2] = {};
     AdjState adj;
+    // euler: the Neumann cell-centred pressure solve and its right-hand side
+    NSolver ns;
+    bool ns_ready = false;
+    double* nrhs = nullptr;
     int body_launches = 0;
     int rec_launches = 0;
 };
@@ -182,7 +187,10 @@ static int make_tmap(f2d_model_s* m, void* buf)
     cuuint64_t strides[1] = {(cuuint64_t)(m->g.P * m->es)};
     // tile + halo: SW x FSH for the flux-form stage, SW x SH for rsw
     cuuint32_t box[2] = {(cuuint32_t)SW,
-                         (cuuint32_t)(m->p.model == F2D_MODEL_RSW ? SH : FSH)};
+                         (cuuint32_t)(m->p.model == F2D_MODEL_RSW ||
+                                              m->p.model == F2D_MODEL_EULER
+                                          ? SH
+                                          : FSH)};
     cuuint32_t estr[2] = {1, 1};
     CUresult r = fn(&map, m->prec == 0 ? CU_TENSOR_MAP_DATA_TYPE_FLOAT64
                                        : CU_TENSOR_MAP_DATA_TYPE_FLOAT32,
@@ -254,6 +262,29 @@ static int ensure_mg(f2d_model_s* m, int which)
     return 0;
 }
 
+// the Neumann cell-centred solver of the euler model (Poisson2D(mesh, "c"),
+// elliptic.py:71-87): fluid cells of vertex_msk(mesh, "c"), i.e. msk with the
+// periodic halo columns removed, inside the interior box (3+J, 3+I)
+static int ensure_ns(f2d_model_s* m)
+{
+    if (m->ns_ready) return 0;
+    const Geom& g = m->g;
+    std::vector<uint8_t> hm((size_t)g.P * g.NY, 0);
+    for (int j = 3; j < 3 + g.ny; ++j)
+        for (int i = 3; i < 3 + g.nx; ++i)
+            hm[(size_t)j * g.P + i] = m->mesh.msk[(size_t)j * g.NX + i] ? 1 : 0;
+    int e = ns_build(m->ns, g.ny, g.nx, g.P, 3 * (long long)g.P + 3, g.xper, hm.data(),
+                     (double*)fb(m, "p"), m->nrhs, m->cx, m->cy);
+    if (e == 6) return fail(4, "the euler model needs at least one fluid cell");
+    if (e) return fail(e, "Neumann multigrid setup failed");
+    m->ns.tol = m->p.poisson_tol;
+    m->ns.maxit = m->p.poisson_maxit;
+    m->ns_ready = true;
+    return 0;
+}
+
+static bool eager_mode();
+
 static int rec_solve(f2d_model_s* m, int which, const void* b, void* x, cudaStream_t s)
 {
     int e = ensure_mg(m, which);
@@ -298,8 +329,42 @@ static int rec_diag(f2d_model_s* m, int par, cudaStream_t s)
         m->rec_launches += 1;
         return 0;
     }
+    case F2D_MODEL_EULER: {
+        // pressure_projection (operators.py:114-119), then sharp, vorticity,
+        // kinetic energy (equations.py:17-22)
+        CKI(launch_euler_div(m->prec, fb(m, "u.x", par), fb(m, "u.y", par), fb(m, "div"),
+                             m->nrhs, m->d_code, m->rdx2, m->rdy2, m->area, g, s));
+        int e = ensure_ns(m);
+        if (e) return e;
+        int fixed = 0;
+        CKI(ns_record(m->ns, s, m->s2, eager_mode(), &fixed));
+        if (g.xper) CKI(launch_fill_periodic(0, fb(m, "p"), g, s));
+        CKI(launch_euler_project(m->prec, fb(m, "u.x", par), fb(m, "u.y", par),
+                                 (const double*)fb(m, "p"), m->d_code, g, s));
+        m->rec_launches += 3 + fixed + (g.xper ? 1 : 0);
+        RswDiag a;
+        memset(&a, 0, sizeof(a));
+        a.ux = fb(m, "u.x", par);
+        a.uy = fb(m, "u.y", par);
+        a.Ux = fb(m, "U.x");
+        a.Uy = fb(m, "U.y");
+        a.omega = fb(m, "omega");
+        a.ke = fb(m, "ke");
+        a.rdx2 = m->rdx2;
+        a.rdy2 = m->rdy2;
+        a.euler = 1;
+        CKI(make_tmap(m, (void*)a.ux));
+        CKI(make_tmap(m, (void*)a.uy));
+        CKI(launch_rsw_diag(m->p.innerproduct, m->prec, tmap(m, (void*)a.ux),
+                            tmap(m, (void*)a.uy), a, m->d_code, g, m->sc, s));
+        // max|U.x|, max|U.y| for set_dt (model.py:83-85)
+        CKI(launch_maxabs2(m->prec, a.Ux, a.Uy, g, m->sc, m->partials, s));
+        m->rec_launches += 2;
+        return 0;
+    }
     case F2D_MODEL_RSW: {
         RswDiag a;
+        memset(&a, 0, sizeof(a));
         a.ux = fb(m, "u.x", par);
         a.uy = fb(m, "u.y", par);
         a.h = fb(m, "h", par);
@@ -330,9 +395,13 @@ static int launch_stage_kernel(f2d_model_s* m, int k, int par, cudaStream_t s)
     auto ds = [&](const char* f, int kk) -> void* {
         return fb(m, (std::string("ds") + std::to_string(kk) + "." + f).c_str());
     };
-    if (m->p.model == F2D_MODEL_RSW) {
+    if (m->p.model == F2D_MODEL_RSW || m->p.model == F2D_MODEL_EULER) {
+        // rsw; euler = the same momentum kernel without the mass equation,
+        // Coriolis and pressure (equations.py:11-15)
+        const bool eu = m->p.model == F2D_MODEL_EULER;
         RswIn a;
         memset(&a, 0, sizeof(a));
+        a.euler = eu ? 1 : 0;
         a.ux = fb(m, "u.x", par);
         a.uy = fb(m, "u.y", par);
         a.h = fb(m, "h", par);
@@ -356,9 +425,10 @@ static int launch_stage_kernel(f2d_model_s* m, int k, int par, cudaStream_t s)
         a.dh2 = ds("h", 2);
         a.fc = m->fc;
         void* om = fb(m, "omega");
-        CKI(make_tmap(m, (void*)a.h));
+        void* hm = eu ? om : (void*)a.h;  // euler stages no thickness tile
+        CKI(make_tmap(m, hm));
         CKI(make_tmap(m, om));
-        CKI(launch_rsw_stage(m->p.vortexforce, m->prec, tmap(m, (void*)a.h), tmap(m, om), a,
+        CKI(launch_rsw_stage(m->p.vortexforce, m->prec, tmap(m, hm), tmap(m, om), a,
                              m->d_code, k | (m->p.integrator << 4), g, m->sc, s));
     } else {
         const char* q = m->p.model == F2D_MODEL_EULERPSI ? "omega" : "pv";
@@ -490,8 +560,11 @@ static int run_graph(f2d_model_s* m, int kind)
 {
     const int par = m->cur;
     if (eager_mode()) {
-        if (m->p.model != F2D_MODEL_RSW) {
+        if (m->p.model == F2D_MODEL_EULERPSI || m->p.model == F2D_MODEL_QG) {
             int e0 = ensure_mg(m, m->p.model == F2D_MODEL_EULERPSI ? 0 : 1);
+            if (e0) return e0;
+        } else if (m->p.model == F2D_MODEL_EULER) {
+            int e0 = ensure_ns(m);
             if (e0) return e0;
         }
         m->rec_launches = 0;
@@ -503,8 +576,11 @@ static int run_graph(f2d_model_s* m, int kind)
     }
     if (!m->gx[kind][par]) {
         // multigrid set-up allocates, so it happens before the capture
-        if (m->p.model != F2D_MODEL_RSW) {
+        if (m->p.model == F2D_MODEL_EULERPSI || m->p.model == F2D_MODEL_QG) {
             int e0 = ensure_mg(m, m->p.model == F2D_MODEL_EULERPSI ? 0 : 1);
+            if (e0) return e0;
+        } else if (m->p.model == F2D_MODEL_EULER) {
+            int e0 = ensure_ns(m);
             if (e0) return e0;
         }
         m->rec_launches = 0;
@@ -558,6 +634,8 @@ static int setup_mesh(f2d_model_s* m, const int8_t* msk)
         bs_free(m->bs[w]);
         m->bs_ready[w] = false;
     }
+    ns_free(m->ns);
+    m->ns_ready = false;
     drop_graphs(m);
     return 0;
 }
@@ -646,7 +724,10 @@ int f2d_model_create(const f2d_params* p, const int8_t* msk, f2d_model* out)
     if (!p || !out) return fail(1, "null argument");
     if (p->precision != F2D_PREC_FP64 && p->precision != F2D_PREC_FP32)
         return fail(1, "unknown precision");
-    if (p->model < 0 || p->model > 2) return fail(1, "unknown model");
+    if (p->model < 0 || p->model > 3) return fail(1, "unknown model");
+    if (p->model == F2D_MODEL_EULER && p->precision != F2D_PREC_FP64)
+        return fail(1, "the euler model runs in FP64");
+
     if (p->integrator < F2D_INTEG_RK3 || p->integrator > F2D_INTEG_ENRK3)
         return fail(1, "unknown integrator (rk3, ef, enrk3)");
     if (p->xperiodic && p->nx < 6) return fail(1, "x-periodic needs nx >= 6");
@@ -698,6 +779,11 @@ int f2d_model_create(const f2d_params* p, const int8_t* msk, f2d_model* out)
         fl = {{"omega", true}, {"U.x", false}, {"U.y", false}, {"psi", false},
               {"vomega", false}, {"flx.x", false}, {"flx.y", false}};
         prog = {"omega"};
+    } else if (p->model == F2D_MODEL_EULER) {
+        fl = {{"u.x", true}, {"u.y", true}, {"U.x", false}, {"U.y", false},
+              {"omega", false}, {"ke", false}, {"p", false}, {"div", false},
+              {"flx.x", false}, {"flx.y", false}};
+        prog = {"u.x", "u.y"};
     } else if (p->model == F2D_MODEL_RSW) {
         fl = {{"u.x", true}, {"u.y", true}, {"h", true}, {"U.x", false}, {"U.y", false},
               {"omega", false}, {"ke", false}, {"p", false}, {"flx.x", false},
@@ -721,7 +807,10 @@ int f2d_model_create(const f2d_params* p, const int8_t* msk, f2d_model* out)
             if ((e = add_field(m, (std::string("ds") + std::to_string(k) + "." + f).c_str(),
                                false, (int)m->es)))
                 return bail(e);
-    if (p->model != F2D_MODEL_RSW) {
+    if (p->model == F2D_MODEL_EULER) {
+        m->nrhs = (double*)dalloc(m, field_bytes(m, 8));
+        if (!m->nrhs) return bail(fail(2, "out of device memory"));
+    } else if (p->model != F2D_MODEL_RSW) {
         m->pr = dalloc(m, field_bytes(m, 8));
         m->pp = dalloc(m, field_bytes(m, 8));
         m->pq = dalloc(m, field_bytes(m, 8));
@@ -765,6 +854,7 @@ int f2d_model_destroy(f2d_model m)
     if (m->stream) cudaStreamSynchronize(m->stream);
     drop_graphs(m);
     for (int w = 0; w < 2; ++w) bs_free(m->bs[w]);
+    ns_free(m->ns);
     for (void* p : m->allocs) cudaFree(p);
     if (m->own_stream && m->stream) cudaStreamDestroy(m->stream);
     if (m->s2) cudaStreamDestroy(m->s2);
@@ -1006,6 +1096,15 @@ int f2d_sync(f2d_model m)
                 CK(cudaMemcpy(&m->bs[w].eg->status, &zero, sizeof(int), cudaMemcpyHostToDevice));
             }
         }
+    if (m->ns_ready) {
+        NGlobals ng;
+        CK(cudaMemcpy(&ng, m->ns.eg, sizeof(ng), cudaMemcpyDeviceToHost));
+        if (ng.status) {
+            st |= ng.status;
+            int zero = 0;
+            CK(cudaMemcpy(&m->ns.eg->status, &zero, sizeof(int), cudaMemcpyHostToDevice));
+        }
+    }
     if (st) {
         int zero = 0;
         CK(cudaMemcpy(&m->sc->status, &zero, sizeof(int), cudaMemcpyHostToDevice));
@@ -1026,6 +1125,11 @@ int f2d_stats(f2d_model m, int64_t* poisson_iters, int64_t* launches_per_step,
     CK(cudaMemcpyAsync(&h, m->sc, sizeof(h), cudaMemcpyDeviceToHost, m->stream));
     CK(cudaStreamSynchronize(m->stream));
     if (poisson_iters) *poisson_iters = h.total_iters;
+    if (poisson_iters && m->ns_ready) {
+        DevScalars hn;
+        CK(cudaMemcpy(&hn, m->ns.sc, sizeof(hn), cudaMemcpyDeviceToHost));
+        *poisson_iters = hn.total_iters;
+    }
     if (launches_per_step) {
         // kernels outside the Poisson loop bodies of one step; each Poisson
         // iteration adds body_launches more
@@ -1072,6 +1176,8 @@ int f2d_time_solver(f2d_model m, int reps, int flush_l2, double* avg_ms, int64_t
 {
     if (!m || !avg_ms) return fail(1, "null argument");
     if (m->p.model == F2D_MODEL_RSW) return fail(1, "rsw has no Poisson solve");
+    if (m->p.model == F2D_MODEL_EULER)
+        return fail(1, "the euler model's Neumann solve has no timing hook");
     const int which = m->p.model == F2D_MODEL_EULERPSI ? 0 : 1;
     if (!m->bs_ready[which]) return fail(9, "the solver has not run yet");
     CK(cudaStreamSynchronize(m->stream));

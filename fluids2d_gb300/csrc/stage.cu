@@ -90,10 +90,12 @@ k_rsw_stage(const __grid_constant__ CUtensorMap th,
         }
         sfy[r][c] = f;
     };
-    xface(ty, tx);
-    yface(ty, tx);
-    if (t < TY) xface(t, TX);
-    else if (t < TY + TX) yface(TY, t - TY);
+    if (!a.euler) {
+        xface(ty, tx);
+        yface(ty, tx);
+        if (t < TY) xface(t, TX);
+        else if (t < TY + TX) yface(TY, t - TY);
+    }
 
     // The vortex force needs no shared fluxes: it is evaluated before the
     // barrier, so warps with fewer faces above do not idle at it.
@@ -136,51 +138,53 @@ k_rsw_stage(const __grid_constant__ CUtensorMap th,
     __syncthreads();
     if (!live) return;
 
-    // Coriolis (addcoriolis, operators.py:32-39)
+    // Coriolis (addcoriolis, operators.py:32-39); the euler model
+    // (equations.py:11-15) has neither Coriolis nor a pressure gradient here
     const T fc = srk[3];
-    if (j <= g.NY - 2 && i >= 1 && i <= g.NX - 2)
+    if (!a.euler && j <= g.NY - 2 && i >= 1 && i <= g.NX - 2)
         dux += fc * (((ldz(Uy, j, i - 1, g) + ldz(Uy, j + 1, i - 1, g)) + Uy[o]) +
                      ldz(Uy, j + 1, i, g));
-    if (j >= 1 && j <= g.NY - 2 && i <= g.NX - 2)
+    if (!a.euler && j >= 1 && j <= g.NY - 2 && i <= g.NX - 2)
         duy -= fc * (((ldz(Ux, j - 1, i, g) + ldz(Ux, j - 1, i + 1, g)) + Ux[o]) +
                      ldz(Ux, j, i + 1, g));
     // gradients of ke then p (addgrad, operators.py:49-56)
     if (i >= 1) {
         const T mx = (cd & B_MSKX) ? T(1) : T(0);
         dux -= (ke[o] - ke[o - 1]) * mx;
-        dux -= (p[o] - p[o - 1]) * mx;
+        if (!a.euler) dux -= (p[o] - p[o - 1]) * mx;
     }
     if (j >= 1) {
         const T my = (cd & B_MSKY) ? T(1) : T(0);
         duy -= (ke[o] - ke[o - g.P]) * my;
-        duy -= (p[o] - p[o - g.P]) * my;
+        if (!a.euler) duy -= (p[o] - p[o - g.P]) * my;
     }
     // mass: dh = -div(flux) * msk
     const T msk = (cd & B_MSK) ? T(1) : T(0);
     const T dh = (-(sfx[ty][tx + 1] - sfx[ty][tx]) - (sfy[ty + 1][tx] - sfy[ty][tx])) * msk;
 
     const T* dt = srk;
-    T ix, iy, ih;
+    T ix, iy, ih = T(0);
+    const bool hm = !a.euler;  // mass equation (rsw)
     if (stage == 1) {
         ix = rk3_increment<T>(1, dt, dux, T(0), T(0));
         iy = rk3_increment<T>(1, dt, duy, T(0), T(0));
-        ih = rk3_increment<T>(1, dt, dh, T(0), T(0));
+        if (hm) ih = rk3_increment<T>(1, dt, dh, T(0), T(0));
     } else if (stage == 2) {
         ix = rk3_increment<T>(2, dt, ((const T*)a.dux1)[o], dux, T(0));
         iy = rk3_increment<T>(2, dt, ((const T*)a.duy1)[o], duy, T(0));
-        ih = rk3_increment<T>(2, dt, ((const T*)a.dh1)[o], dh, T(0));
+        if (hm) ih = rk3_increment<T>(2, dt, ((const T*)a.dh1)[o], dh, T(0));
     } else {
         ix = rk3_increment<T>(3, dt, ((const T*)a.dux1)[o], ((const T*)a.dux2)[o], dux);
         iy = rk3_increment<T>(3, dt, ((const T*)a.duy1)[o], ((const T*)a.duy2)[o], duy);
-        ih = rk3_increment<T>(3, dt, ((const T*)a.dh1)[o], ((const T*)a.dh2)[o], dh);
+        if (hm) ih = rk3_increment<T>(3, dt, ((const T*)a.dh1)[o], ((const T*)a.dh2)[o], dh);
     }
     store_filled((T*)a.uxo, g, j, i, ((const T*)a.ux)[o] + ix);
     store_filled((T*)a.uyo, g, j, i, ((const T*)a.uy)[o] + iy);
-    store_filled((T*)a.ho, g, j, i, sh[ty + OY][tx + OX] + ih);
+    if (hm) store_filled((T*)a.ho, g, j, i, sh[ty + OY][tx + OX] + ih);
     if (a.dux) {
         store_filled((T*)a.dux, g, j, i, dux);
         store_filled((T*)a.duy, g, j, i, duy);
-        store_filled((T*)a.dh, g, j, i, dh);
+        if (hm) store_filled((T*)a.dh, g, j, i, dh);
     }
 }
 
@@ -211,7 +215,7 @@ k_rsw_diag(const __grid_constant__ CUtensorMap tux,
     // sharp: U = u / dx^2 everywhere (no fill in the reference; u is filled)
     ((T*)a.Ux)[o] = ux * rdx2;
     ((T*)a.Uy)[o] = uy * rdy2;
-    ((T*)a.p)[o] = T(a.goa) * ((const T*)a.h)[o];
+    if (!a.euler) ((T*)a.p)[o] = T(a.goa) * ((const T*)a.h)[o];
     if (!periodic_owner(g, i)) return;  // omega and ke: halo fill copies
     const uint32_t cd = code[o];
     // vorticity: omega[1:,:] = -diff(u.x, 0); omega[:,1:] += diff(u.y, 1)
@@ -531,6 +535,72 @@ int launch_set_dt(DevScalars* sc, cudaStream_t s)
 int launch_pushforward(DevScalars* sc, cudaStream_t s)
 {
     k_pushforward<<<1, 1, 0, s>>>(sc);
+    return (int)cudaGetLastError();
+}
+
+// ---------------------------------------------------------------------------
+// euler model: the pressure projection around the Neumann solve
+// (pressure_projection, operators.py:114-119).
+// ---------------------------------------------------------------------------
+
+// U = sharp(u) (computed on the fly), delta = div(U) * msk into dv - whose
+// last column keeps its previous value, like the reference's div
+// (operators.py:104-107) - and the solve's right-hand side -delta * area
+template <typename T>
+__global__ void k_euler_div(const T* __restrict__ ux, const T* __restrict__ uy, T* dv,
+                            double* __restrict__ rhs, const uint32_t* __restrict__ code,
+                            T rdx2, T rdy2, double area, Geom g)
+{
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    const int j = blockIdx.y * blockDim.y + threadIdx.y;
+    if (j >= g.NY || i >= g.NX) return;
+    const long long o = (long long)j * g.P + i;
+    T d = i <= g.NX - 2 ? -(ux[o + 1] * rdx2 - ux[o] * rdx2) : dv[o];
+    if (j <= g.NY - 2) d -= uy[o + g.P] * rdy2 - uy[o] * rdy2;
+    d *= (code[o] & B_MSK) ? T(1) : T(0);
+    dv[o] = d;
+    rhs[o] = -(double)d * area;
+}
+
+// u -= grad p (addgrad, operators.py:49-53), then the halo fill of u
+template <typename T>
+__global__ void k_euler_project(T* ux, T* uy, const double* __restrict__ p,
+                                const uint32_t* __restrict__ code, Geom g)
+{
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    const int j = blockIdx.y * blockDim.y + threadIdx.y;
+    if (j >= g.NY || i >= g.NX || !periodic_owner(g, i)) return;
+    const long long o = (long long)j * g.P + i;
+    const uint32_t cd = code[o];
+    T vx = ux[o], vy = uy[o];
+    if (i >= 1) vx -= T((p[o] - p[o - 1]) * ((cd & B_MSKX) ? 1.0 : 0.0));
+    if (j >= 1) vy -= T((p[o] - p[o - g.P]) * ((cd & B_MSKY) ? 1.0 : 0.0));
+    store_filled(ux, g, j, i, vx);
+    store_filled(uy, g, j, i, vy);
+}
+
+int launch_euler_div(int prec, const void* ux, const void* uy, void* dv, double* rhs,
+                     const uint32_t* code, double rdx2, double rdy2, double area,
+                     const Geom& g, cudaStream_t s)
+{
+    const dim3 gr = pt_grid(g), bl(32, 8);
+    if (prec == 0)
+        k_euler_div<double><<<gr, bl, 0, s>>>((const double*)ux, (const double*)uy, (double*)dv,
+                                              rhs, code, rdx2, rdy2, area, g);
+    else
+        k_euler_div<float><<<gr, bl, 0, s>>>((const float*)ux, (const float*)uy, (float*)dv, rhs,
+                                             code, (float)rdx2, (float)rdy2, area, g);
+    return (int)cudaGetLastError();
+}
+
+int launch_euler_project(int prec, void* ux, void* uy, const double* p, const uint32_t* code,
+                         const Geom& g, cudaStream_t s)
+{
+    const dim3 gr = pt_grid(g), bl(32, 8);
+    if (prec == 0)
+        k_euler_project<double><<<gr, bl, 0, s>>>((double*)ux, (double*)uy, p, code, g);
+    else
+        k_euler_project<float><<<gr, bl, 0, s>>>((float*)ux, (float*)uy, p, code, g);
     return (int)cudaGetLastError();
 }
 

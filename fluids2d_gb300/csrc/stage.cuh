@@ -12,6 +12,7 @@ struct RswIn {
     const void *dux1, *duy1, *dh1;  // earlier tendencies
     const void *dux2, *duy2, *dh2;
     double fc;                      // f0 * area * 0.25 (operators.py:33)
+    int euler;                      // euler model: vortex force + grad ke only
 };
 
 struct RswDiag {
@@ -19,6 +20,7 @@ struct RswDiag {
     void *Ux, *Uy, *omega, *ke, *p;
     double rdx2, rdy2;  // 1/dx**2, 1/dy**2 (operators.py:62-63)
     double goa;         // g/area (operators.py:111)
+    int euler;          // euler model: no pressure from h
 };
 
 int launch_fluxform_stage(int method, int prec, const CUtensorMap* tq,
@@ -45,5 +47,11 @@ int launch_fill_periodic(int prec, void* a, const Geom& g, cudaStream_t s);
 int launch_set_dt(DevScalars* sc, cudaStream_t s);
 int launch_pushforward(DevScalars* sc, cudaStream_t s);
 size_t pt_grid_blocks(const Geom& g);
+// euler pressure projection around the Neumann solve
+int launch_euler_div(int prec, const void* ux, const void* uy, void* dv, double* rhs,
+                     const uint32_t* code, double rdx2, double rdy2, double area,
+                     const Geom& g, cudaStream_t s);
+int launch_euler_project(int prec, void* ux, void* uy, const double* p, const uint32_t* code,
+                         const Geom& g, cudaStream_t s);
 
 }  // namespace f2d

@@ -25,6 +25,7 @@ from .param import Param
 # states.py:7-17 for the models of the GPU path
 MODEL_SPECS = {
     "eulerpsi": (("omega", "U", "psi", "vomega", "flx"), ("omega",)),
+    "euler": (("u", "U", "omega", "ke", "p", "div", "flx"), ("u",)),
     "rsw": (("u", "h", "U", "omega", "ke", "p", "flx", "pv"), ("u", "h")),
     "qg": (("pv", "U", "h", "flx", "work", "psi"), ("pv",)),
 }

@@ -14,7 +14,7 @@ _methods_extended = _methods + ["classic"]
 _integrators = ["rk3", "ef", "enrk3", "LFRA"]
 
 # models and integrators the GPU path implements
-SUPPORTED_MODELS = ("eulerpsi", "rsw", "qg")
+SUPPORTED_MODELS = ("eulerpsi", "rsw", "qg", "euler")
 SUPPORTED_INTEGRATORS = ("rk3", "ef", "enrk3")
 EXTRA = ("precision", "poisson_tol", "poisson_maxit")
 
@@ -98,8 +98,10 @@ class Param:
             raise NotImplementedError("halowidth must be 3")
         if self.yperiodic:
             raise NotImplementedError("yperiodic is not supported")
-        if self.model == "rsw" and self.innerproduct == "classic":
+        if self.model in ("rsw", "euler") and self.innerproduct == "classic":
             raise NotImplementedError("innerproduct='classic' is not implemented")
+        if self.model == "euler" and getattr(self, "precision", "fp64") != "fp64":
+            raise NotImplementedError("the euler model runs in FP64")
         assert self.precision in ("fp64", "fp32")
 
 
