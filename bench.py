@@ -59,6 +59,10 @@ WORKLOADS = {
                "MG-PCG Helmholtz"),
     "qg1024": ("qg", dict(n=1024, seed=0, nislands=20),
                "qg 1024x1024 basin, 20 islands, Rd=0.02, beta=1, FP64"),
+    "euler512": ("euler", dict(n=512, seed=0, nislands=3),
+                 "euler (momentum-pressure) 512x512 closed basin, 3 islands, WENO5 "
+                 "vortex force, SSP-RK3, cfl 0.5, FP64, Neumann multigrid-PCG "
+                 "pressure projection"),
     "rsw1024": ("rsw", dict(n=1024, seed=0, nislands=3),
                 "rsw 1024x1024 x-periodic channel, 3 islands, FP64 (profiling "
                 "size: working set above the L2)"),
@@ -134,6 +138,8 @@ def build_case(name):
         desc = desc.replace("FP64", "FP32 stencils + FP32 multigrid, FP64 CG")
     if model == "rsw":
         case = wl.rsw_case(**kw)
+    elif model == "euler":
+        case = wl.euler_case(**kw)
     elif model == "eulerpsi":
         case = wl.eulerpsi_case(**kw)
     else:
@@ -154,6 +160,8 @@ def make_gpu_model(model, case, stream_ptr, precision="fp64", tol=None):
             setattr(p, k, case[k])
     if model == "eulerpsi":
         p.cfl = 0.8
+    if model == "euler":
+        p.cfl = 0.5
     p.tend = 1e300
     p.maxite = 10 ** 12
     p.precision = precision
@@ -167,14 +175,17 @@ def make_gpu_model(model, case, stream_ptr, precision="fp64", tol=None):
         m.mesh.f = case["f"]
     s = m.state
     for k, v in case["fields"].items():
-        getattr(s, k)[:] = v
+        if "." in k:
+            getattr(getattr(s, k.split(".")[0]), k.split(".")[1])[:] = v
+        else:
+            getattr(s, k)[:] = v
     m.integrator.diag(s)
     return m
 
 
 def prognostic_names(model):
     return {"rsw": ["u.x", "u.y", "h"], "eulerpsi": ["omega"],
-            "qg": ["pv"]}[model]
+            "qg": ["pv"], "euler": ["u.x", "u.y"]}[model]
 
 
 # algorithmic bytes per array point of the stage-2 launch of the fused stage
@@ -183,6 +194,9 @@ STAGE2_BYTES = {
     # rsw: read u.x,u.y,h,U.x,U.y,ke,p,omega + 3 ds1 (11 x 8) + code (4);
     #      write u.x,u.y,h + 3 ds2 (6 x 8)
     "rsw": 11 * 8 + 4 + 6 * 8,
+    # euler (momentum kernel without the mass equation): read u.x, u.y, U.x,
+    # U.y, ke, omega + 2 ds1 (8 x 8) + code; write u.x, u.y + 2 ds2 (4 x 8)
+    "euler": 8 * 8 + 4 + 4 * 8,
     # flux form: read q,U.x,U.y,ds1 (4 x 8) + code (4); write q, ds2 (2 x 8)
     "eulerpsi": 4 * 8 + 4 + 2 * 8,
     "qg": 4 * 8 + 4 + 2 * 8,
@@ -283,6 +297,8 @@ def cpu_oracle_rate(model, case, budget_s, max_steps=None, warmup=1):
             setattr(p, k, case[k])
     if model == "eulerpsi":
         p.cfl = 0.8
+    if model == "euler":
+        p.cfl = 0.5
     om = O.Model(p, msk=case["msk"], pysq=False)
     if "f" in case:
         om.mesh.f = case["f"].copy()
@@ -789,7 +805,7 @@ def run_gpu(args, rank, world):
     except Exception:
         peak, peak_src = 6800.0, "fallback"
     kname = {"rsw": "k_rsw_stage", "eulerpsi": "k_fluxform_stage",
-             "qg": "k_fluxform_stage"}[model]
+             "qg": "k_fluxform_stage", "euler": "k_rsw_stage"}[model]
     traffic = read_profile_traffic(f"{kname}_{args.workload}")
     fp64_pct = read_profile_value(f"{kname}_{args.workload}", "fp64_pipe_pct")
 

@@ -17,9 +17,13 @@
 // Preconditioner: cell-centred V-cycle with red-black Gauss-Seidel (nu sweeps
 // per leg, symmetric order), coarse cells = 2x2 agglomerates (fluid if any
 // child is), restriction = sum of the children's residuals, prolongation =
-// the parent's value, coarse couplings = the sums of the fine face couplings
-// they contain (the exact Galerkin operator R A P for this R and P), coarsest
-// level by (R,B)^k (B,R)^k in one thread block. Single component assumed (a
+// the parent's value, coarse couplings = half the sum of the fine face
+// couplings a coarse face contains. (The sum itself is the Galerkin operator
+// R A P for this R and P; with piecewise-constant P it is twice too stiff for
+// smooth errors, and the coarse correction comes out halved - half the sum is
+// the re-discretised coupling where the face is fully open and keeps the
+// partial openings of masked faces.) Coarsest level by (R,B)^k (B,R)^k in one
+// thread block. Single component assumed (a
 // fluid domain made of several disconnected parts would need a projection
 // per part).
 #include <algorithm>
@@ -294,13 +298,14 @@ static int ns_vcycle(NSolver& s, cudaStream_t st)
     int cnt = 0;
     // level 0 of the cycle: x = z (from zero), b = r
     for (int l = 0; l < nl - 1; ++l) {
-        k_ns_zero<<<ngrid(s.lev[l]), blk, 0, st>>>(s.dlev, l);
+        // x = 0 before the pre-smoothing (coarse levels: set by the restriction)
+        if (l == 0) k_ns_zero<<<ngrid(s.lev[l]), blk, 0, st>>>(s.dlev, l);
         for (int k = 0; k < s.nu; ++k) {
             k_ns_smooth<<<ngrid(s.lev[l]), blk, 0, st>>>(s.dlev, l, 0);
             k_ns_smooth<<<ngrid(s.lev[l]), blk, 0, st>>>(s.dlev, l, 1);
         }
         k_ns_restrict<<<ngrid(s.lev[l + 1]), blk, 0, st>>>(s.dlev, l);
-        cnt += 2 + 2 * s.nu;
+        cnt += (l == 0 ? 2 : 1) + 2 * s.nu;
     }
     k_ns_coarse<<<1, 1024, 0, st>>>(s.dlev, nl - 1, s.ksweeps);
     cnt += 1;
@@ -475,8 +480,8 @@ int ns_build(NSolver& s, int nyn, int nxn, long long pitch, long long off, int p
                     if (2 * J < ny && fi < nxc) sy += fy[(size_t)(2 * J) * nxc + fi];
                 }
                 cm[(size_t)J * cx_n + I] = v;
-                cfx[(size_t)J * cx_n + I] = sx;
-                cfy[(size_t)J * cx_n + I] = sy;
+                cfx[(size_t)J * cx_n + I] = 0.5 * sx;
+                cfy[(size_t)J * cx_n + I] = 0.5 * sy;
             }
         NLevel C;
         memset(&C, 0, sizeof(C));
