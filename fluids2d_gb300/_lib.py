@@ -21,7 +21,7 @@ c_void_p = ctypes.c_void_p
 MODELS = {"eulerpsi": 0, "rsw": 1, "qg": 2, "euler": 3}
 METHODS = {"weno": 0, "upwind": 1, "centered": 2, "cweno": 3}
 PRECISIONS = {"fp64": 0, "fp32": 1}
-INTEGRATORS = {"rk3": 0, "ef": 1, "enrk3": 2}
+INTEGRATORS = {"rk3": 0, "ef": 1, "enrk3": 2, "LFRA": 3}
 SIDES = {"left": 1, "right": 2, "bottom": 4, "top": 8}
 
 
@@ -41,7 +41,8 @@ class Params(ctypes.Structure):
         ("precision", c_int),
         ("poisson_tol", c_dbl), ("poisson_maxit", c_int),
         ("integrator", c_int),
-        ("reserved", c_int * 6),
+        ("ragamma", c_dbl),
+        ("reserved", c_int * 4),
     ]
 
 
@@ -179,6 +180,7 @@ def params_struct(p):
     s.poisson_tol = float(getattr(p, "poisson_tol", 1e-12))
     s.poisson_maxit = int(getattr(p, "poisson_maxit", 200))
     s.integrator = INTEGRATORS[getattr(p, "integrator", "rk3")]
+    s.ragamma = float(getattr(p, "RAgamma", 0.1))
     return s
 
 

@@ -392,6 +392,7 @@ static int launch_stage_kernel(f2d_model_s* m, int k, int par, cudaStream_t s)
 {
     const Geom& g = m->g;
     const int out = 1 - par;
+    const bool lf = m->p.integrator == F2D_INTEG_LFRA;
     auto ds = [&](const char* f, int kk) -> void* {
         return fb(m, (std::string("ds") + std::to_string(kk) + "." + f).c_str());
     };
@@ -412,14 +413,17 @@ static int launch_stage_kernel(f2d_model_s* m, int k, int par, cudaStream_t s)
         a.Uy = fb(m, "U.y");
         a.ke = fb(m, "ke");
         a.p = fb(m, "p");
-        if (k < 3) {
-            a.dux = ds("u.x", k);
-            a.duy = ds("u.y", k);
-            a.dh = ds("h", k);
+        // LFRA: the filtered previous state alternates between the two
+        // tendency buffers with the parity (in: 1 + par, out: 2 - par)
+        const int kin = lf ? 1 + par : 1, kout = lf ? 2 - par : k;
+        if (kout < 3) {
+            a.dux = ds("u.x", kout);
+            a.duy = ds("u.y", kout);
+            a.dh = ds("h", kout);
         }
-        a.dux1 = ds("u.x", 1);
-        a.duy1 = ds("u.y", 1);
-        a.dh1 = ds("h", 1);
+        a.dux1 = ds("u.x", kin);
+        a.duy1 = ds("u.y", kin);
+        a.dh1 = ds("h", kin);
         a.dux2 = ds("u.x", 2);
         a.duy2 = ds("u.y", 2);
         a.dh2 = ds("h", 2);
@@ -436,7 +440,8 @@ static int launch_stage_kernel(f2d_model_s* m, int k, int par, cudaStream_t s)
         CKI(make_tmap(m, qin));
         CKI(launch_fluxform_stage(m->p.compflux, m->prec, tmap(m, qin), qin, fb(m, q, out),
                                   fb(m, "U.x"), fb(m, "U.y"), m->d_code,
-                                  k < 3 ? ds(q, k) : nullptr, ds(q, 1), ds(q, 2),
+                                  lf ? ds(q, 2 - par) : k < 3 ? ds(q, k) : nullptr,
+                                  ds(q, lf ? 1 + par : 1), ds(q, 2),
                                   k | (m->p.integrator << 4), g,
                                   m->sc, s));
     }
@@ -458,8 +463,9 @@ static int rec_step(f2d_model_s* m, int par, bool with_dt, cudaStream_t s)
         CKI(launch_set_dt(m->sc, s));
         m->rec_launches += 1;
     }
-    // SSP-RK3 / enrk3: 3 stages, ef: 1 (an odd count: a step flips the parity)
-    const int nst = m->p.integrator == F2D_INTEG_EF ? 1 : 3;
+    // SSP-RK3 / enrk3: 3 stages, ef and LFRA: 1 (an odd count: a step flips
+    // the parity)
+    const int nst = m->p.integrator == F2D_INTEG_EF || m->p.integrator == F2D_INTEG_LFRA ? 1 : 3;
     for (int k = 1; k <= nst; ++k) {
         int e = rec_stage(m, k, par, s);
         if (e) return e;
@@ -669,6 +675,8 @@ int f2d_params_default(f2d_params* p)
     p->precision = F2D_PREC_FP64;
     p->poisson_tol = 1e-12;
     p->poisson_maxit = 200;
+    p->integrator = F2D_INTEG_RK3;
+    p->ragamma = 0.1;
     return 0;
 }
 
@@ -728,8 +736,8 @@ int f2d_model_create(const f2d_params* p, const int8_t* msk, f2d_model* out)
     if (p->model == F2D_MODEL_EULER && p->precision != F2D_PREC_FP64)
         return fail(1, "the euler model runs in FP64");
 
-    if (p->integrator < F2D_INTEG_RK3 || p->integrator > F2D_INTEG_ENRK3)
-        return fail(1, "unknown integrator (rk3, ef, enrk3)");
+    if (p->integrator < F2D_INTEG_RK3 || p->integrator > F2D_INTEG_LFRA)
+        return fail(1, "unknown integrator (rk3, ef, enrk3, LFRA)");
     if (p->xperiodic && p->nx < 6) return fail(1, "x-periodic needs nx >= 6");
     if (p->model == F2D_MODEL_RSW && p->vortexforce != p->compflux)
         return fail(1, "the fused rsw stage uses one flux method for vortexforce and "
@@ -835,6 +843,7 @@ int f2d_model_create(const f2d_params* p, const int8_t* msk, f2d_model* out)
     h.dt = p->dt > 0 ? p->dt : 0.01;
     h.cfl = p->cfl;
     h.dtmax = p->dtmax;
+    h.ragamma = p->ragamma;
     m->cfl_dt = !(p->dt > 0) && p->model != F2D_MODEL_RSW;
     if (p->dt > 0) m->dt_const = p->dt;
     else if (p->model == F2D_MODEL_RSW) {

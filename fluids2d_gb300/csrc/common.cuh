@@ -60,11 +60,9 @@ struct DevScalars {
     int outer, maxouter;      // refinement rounds of the current solve
     int conv_in, zero;        // inner loop done; right-hand side is zero
     long long total_outer;    // refinement rounds summed over solves
-    // SSP-RK3 increment coefficients of the current step (integrators.py:
-    // 92-107): dt; -3dt/4, dt/4; -dt/12, -dt/12, 2dt/3 - in FP64 and FP32,
-    // computed once per step so the stage kernels do no FP64 arithmetic
-    double rk[6];
-    float rkf[6];
+    // Robert-Asselin filter coefficient of the leap-frog integrator
+    // (param.py:50 RAgamma, integrators.py:39-55)
+    double ragamma;
 };
 
 // ---------------------------------------------------------------------------

@@ -79,11 +79,18 @@ k_ens_fluxform_stage(const int4* __restrict__ tiles, const Member* __restrict__ 
     const int4 tl = tiles[blockIdx.x];
     const Member& mb = mem[tl.x];
     const long long o = mb.off;
+    const int k = stage & 15;  // stage = k | integrator << 4
+    const DevScalars& sc = scs[tl.x];
+    // LFRA: one stage; the filtered previous state alternates between the
+    // tendency arenas with the parity (in: ds1 at parity 0, out: the other)
+    const bool lf = ((stage >> 4) & 15) == 3;
+    if (lf && sc.ite == 0) stage |= 256;
+    void* pin = lf && par ? a.ds2 : a.ds1;
+    void* pout = lf ? (par ? a.ds1 : a.ds2) : k < 3 ? (k == 1 ? a.ds1 : a.ds2) : nullptr;
     fluxform_tile<T, M>(sm, &mb.tq[par], at<T>(a.q[par], o), at<T>(a.q[1 - par], o),
                         at<T>(a.Ux, o), at<T>(a.Uy, o), a.code + o,
-                        stage < 3 ? at<T>(stage == 1 ? a.ds1 : a.ds2, o) : nullptr,
-                        at<T>(a.ds1, o), at<T>(a.ds2, o), stage, mb.g, scs[tl.x].dt,
-                        &eg->status, tl.y, tl.z);
+                        pout ? at<T>(pout, o) : nullptr, at<T>(pin, o), at<T>(a.ds2, o),
+                        stage, mb.g, sc.dt, sc.ragamma, &eg->status, tl.y, tl.z);
 }
 
 // centerstovertices (+ beta-plane term) into the FP64 right-hand side
@@ -308,7 +315,8 @@ static int ens_record_step(f2d_ensemble_s* e, int par, cudaStream_t s)
     const dim3 blk(32, 8);
     k_ens_set_dt<<<(e->n + 127) / 128, 128, 0, s>>>(e->scs, e->n);
     e->rec += 1;
-    const int nst = e->p.integrator == F2D_INTEG_EF ? 1 : 3;  // odd: flips the parity
+    const int nst = e->p.integrator == F2D_INTEG_EF || e->p.integrator == F2D_INTEG_LFRA
+                        ? 1 : 3;  // odd: flips the parity
     for (int k = 1; k <= nst; ++k) {
         const int sk = k | (e->p.integrator << 4);
 #define ENS_FF(T, M)                                                                       \
@@ -394,8 +402,8 @@ int f2d_ensemble_create(const f2d_params* p, int count, const int* nxs, const in
         return f2d_internal_fail(1, "bad ensemble arguments");
     if (p->model != F2D_MODEL_EULERPSI && p->model != F2D_MODEL_QG)
         return f2d_internal_fail(1, "ensembles run the eulerpsi and qg models");
-    if (p->integrator < F2D_INTEG_RK3 || p->integrator > F2D_INTEG_ENRK3)
-        return f2d_internal_fail(1, "unknown integrator (rk3, ef, enrk3)");
+    if (p->integrator < F2D_INTEG_RK3 || p->integrator > F2D_INTEG_LFRA)
+        return f2d_internal_fail(1, "unknown integrator (rk3, ef, enrk3, LFRA)");
     if (p->dt > 0)
         return f2d_internal_fail(1, "ensembles use the per-member CFL time step (dt = 0)");
     auto* e = new f2d_ensemble_s();
@@ -555,6 +563,7 @@ int f2d_ensemble_create(const f2d_params* p, int count, const int* nxs, const in
         h.dt = 0.01;
         h.cfl = p->cfl;
         h.dtmax = p->dtmax;
+        h.ragamma = p->ragamma;
     }
     cudaMemcpy(e->scs, hs.data(), sizeof(DevScalars) * count, cudaMemcpyHostToDevice);
     if (cudaDeviceSynchronize() != cudaSuccess)

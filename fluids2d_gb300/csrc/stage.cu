@@ -29,8 +29,9 @@ k_fluxform_stage(const __grid_constant__ CUtensorMap tq, const T* __restrict__ q
                  const T* __restrict__ ds2, int stage, Geom g, DevScalars* sc)
 {
     __shared__ FluxformSmem<T, M> sm;
+    if (((stage >> 4) & 15) == 3 && sc->ite == 0) stage |= 256;  // first LFRA step
     fluxform_tile<T, M>(sm, &tq, qin, qout, Ux, Uy, code, ds_out, ds1, ds2, stage, g, sc->dt,
-                        &sc->status, blockIdx.x * TX, blockIdx.y * FTY);
+                        sc->ragamma, &sc->status, blockIdx.x * TX, blockIdx.y * FTY);
 }
 
 // ---------------------------------------------------------------------------
@@ -51,6 +52,7 @@ k_rsw_stage(const __grid_constant__ CUtensorMap th,
     __shared__ T srk[4];  // RK3 coefficients, Coriolis parameter
     __shared__ uint64_t bar;
     const int sk = stage;  // stage | integrator << 4
+    const bool lf = ((sk >> 4) & 15) == 3;
     stage &= 15;
     const int tx = threadIdx.x, ty = threadIdx.y, t = ty * TX + tx;
     const int i0 = blockIdx.x * TX, j0 = blockIdx.y * TY;
@@ -132,7 +134,7 @@ k_rsw_stage(const __grid_constant__ CUtensorMap th,
         }
     }
     if (tx == 0 && ty == 0) {
-        rk3_coefs<T>(sk, sc->dt, srk);
+        rk3_coefs<T>(sk, sc->dt, srk, sc->ragamma);
         srk[3] = T(a.fc);
     }
     __syncthreads();
@@ -165,6 +167,24 @@ k_rsw_stage(const __grid_constant__ CUtensorMap th,
     const T* dt = srk;
     T ix, iy, ih = T(0);
     const bool hm = !a.euler;  // mass equation (rsw)
+    if (lf) {
+        // leap-frog + Robert-Asselin: dux1.. = filtered previous state in,
+        // dux.. = out (buffers alternating with the parity)
+        const bool first = sc->ite == 0;
+        T qn, pn;
+        lfra_update<T>(first, srk, ((const T*)a.ux)[o], ((const T*)a.dux1)[o], dux, qn, pn);
+        store_filled((T*)a.uxo, g, j, i, qn);
+        store_filled((T*)a.dux, g, j, i, pn);
+        lfra_update<T>(first, srk, ((const T*)a.uy)[o], ((const T*)a.duy1)[o], duy, qn, pn);
+        store_filled((T*)a.uyo, g, j, i, qn);
+        store_filled((T*)a.duy, g, j, i, pn);
+        if (hm) {
+            lfra_update<T>(first, srk, sh[ty + OY][tx + OX], ((const T*)a.dh1)[o], dh, qn, pn);
+            store_filled((T*)a.ho, g, j, i, qn);
+            store_filled((T*)a.dh, g, j, i, pn);
+        }
+        return;
+    }
     if (stage == 1) {
         ix = rk3_increment<T>(1, dt, dux, T(0), T(0));
         iy = rk3_increment<T>(1, dt, duy, T(0), T(0));

@@ -29,12 +29,19 @@ __device__ __forceinline__ T ldz(const T* __restrict__ a, int j, int i,
 // memory): per-thread FP64 divisions would load the FP64 pipe of the FP32
 // kernels.
 template <typename T>
-__device__ __forceinline__ void rk3_coefs(int stage, double dt, T* c)
+__device__ __forceinline__ void rk3_coefs(int stage, double dt, T* c, double gamma = 0.0)
 {
     // stage = k | (integrator << 4); the coefficients of ef (integrators.py:
-    // 116-123) and enrk3 (140-155) in the reference's evaluation order
-    const int integ = stage >> 4;
+    // 116-123) and enrk3 (140-155) in the reference's evaluation order; LFRA
+    // (39-55): dt, 2 dt and the filter coefficient
+    const int integ = (stage >> 4) & 15;
     stage &= 15;
+    if (integ == 3) {
+        c[0] = T(dt);
+        c[1] = T(2 * dt);
+        c[2] = T(gamma);
+        return;
+    }
     if (integ == 1) {
         c[0] = T(dt);
         c[1] = c[2] = T(0);
@@ -74,6 +81,25 @@ __device__ __forceinline__ T rk3_increment(int stage, const T* c, T d1, T d2, T 
     if (stage == 1) return c[0] * d1;
     if (stage == 2) return c[0] * d1 + c[1] * d2;
     return (c[0] * d1 + c[1] * d2) + c[2] * d3;
+}
+
+// Leap-frog step with the Robert-Asselin filter at one point (integrators.py:
+// 39-55) from the current value q, the filtered previous value pv and the
+// tendency ds; c = {dt, 2 dt, gamma}. The first step (ite == 0) is Euler
+// forward and keeps q as the previous value; afterwards the new value is
+// pv + 2 dt ds and the filtered current value q + gamma (new + pv - 2 q) is
+// the next step's previous value (rightpermute leaves sa == sb == it).
+template <typename T>
+__device__ __forceinline__ void lfra_update(bool first, const T* c, T q, T pv, T ds, T& qn,
+                                            T& pn)
+{
+    if (first) {
+        qn = q + c[0] * ds;
+        pn = q;
+    } else {
+        qn = pv + c[1] * ds;
+        pn = q + ((c[2] * qn + c[2] * pv) + (T(-2) * c[2]) * q);
+    }
 }
 
 // Store v at (j,i) and, in an x-periodic domain, at its halo copy.
@@ -138,14 +164,15 @@ __device__ __forceinline__ void fluxform_tile(
     FluxformSmem<T, M>& sm, const CUtensorMap* tq, const T* __restrict__ qin,
     T* __restrict__ qout, const T* __restrict__ Ux, const T* __restrict__ Uy,
     const uint32_t* __restrict__ code, T* __restrict__ ds_out, const T* __restrict__ ds1,
-    const T* __restrict__ ds2, int stage, const Geom& g, double dt, int* status, int i0,
-    int j0)
+    const T* __restrict__ ds2, int stage, const Geom& g, double dt, double gamma,
+    int* status, int i0, int j0)
 {
     auto& sq = sm.sq;
     auto& sfx = sm.sfx;
     auto& sfy = sm.sfy;
     const int tx = threadIdx.x, ty = threadIdx.y, t = ty * TX + tx;
-    const int sk = stage;  // stage | integrator << 4
+    const int sk = stage;  // stage | integrator << 4 | first LFRA step << 8
+    const bool lf = ((sk >> 4) & 15) == 3;
     stage &= 15;
     (void)qin;
     // 1. the TMA load of the staged tile (q with its 3-cell halo) ...
@@ -173,7 +200,7 @@ __device__ __forceinline__ void fluxform_tile(
         cd[q] = in ? c : 0u;
         ux[q] = u;
         uy[q] = v;
-        d1[q] = stage >= 2 ? ds1[o] : T(0);
+        d1[q] = stage >= 2 || lf ? ds1[o] : T(0);
         d2[q] = stage == 3 ? ds2[o] : T(0);
     }
     uint32_t ce = 0u;
@@ -228,7 +255,7 @@ __device__ __forceinline__ void fluxform_tile(
     }
     if (ex == 1) xflux(er, ec, ce, ue);
     else if (ex == 2) yflux(er, ec, ce, ue);
-    if (t == 0) rk3_coefs<T>(sk, dt, sm.rk);
+    if (t == 0) rk3_coefs<T>(sk, dt, sm.rk, gamma);
     __syncthreads();
 
     // 5. tendency, RK3 update and stores of this thread's cells
@@ -239,6 +266,14 @@ __device__ __forceinline__ void fluxform_tile(
         if (j >= g.NY) break;
         const T msk = (cd[q] & B_MSK) ? T(1) : T(0);
         const T ds = (-(sfx[r][tx + 1] - sfx[r][tx]) - (sfy[r + 1][tx] - sfy[r][tx])) * msk;
+        if (lf) {
+            // LFRA: ds1 = the filtered previous state in, ds_out = out
+            T qn, pn;
+            lfra_update<T>(sk & 256, sm.rk, sq[r + OY][tx + OX], d1[q], ds, qn, pn);
+            store_filled(qout, g, j, i, qn);
+            store_filled(ds_out, g, j, i, pn);
+            continue;
+        }
         T inc;
         if (stage == 1) inc = rk3_increment<T>(1, sm.rk, ds, T(0), T(0));
         else if (stage == 2) inc = rk3_increment<T>(2, sm.rk, d1[q], ds, T(0));

@@ -217,7 +217,9 @@ class Mesh:
 
 
 class Integrator:
-    """RKIntegrator(rk3) facade (integrators.py:63-79)."""
+    """The integrator facade (integrators.py:9-79): RKIntegrator for rk3, ef
+    and enrk3, LFRAintegrator for LFRA; the scratch states live on the
+    device."""
 
     def __init__(self, model):
         self._m = model

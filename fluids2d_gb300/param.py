@@ -15,7 +15,7 @@ _integrators = ["rk3", "ef", "enrk3", "LFRA"]
 
 # models and integrators the GPU path implements
 SUPPORTED_MODELS = ("eulerpsi", "rsw", "qg", "euler")
-SUPPORTED_INTEGRATORS = ("rk3", "ef", "enrk3")
+SUPPORTED_INTEGRATORS = ("rk3", "ef", "enrk3", "LFRA")
 EXTRA = ("precision", "poisson_tol", "poisson_maxit")
 
 

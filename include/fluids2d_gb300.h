@@ -28,9 +28,10 @@ enum { F2D_MODEL_EULERPSI = 0, F2D_MODEL_RSW = 1, F2D_MODEL_QG = 2,
 /* flux methods (param.py:4, weno.py:338-343) */
 enum { F2D_METHOD_WENO = 0, F2D_METHOD_UPWIND = 1, F2D_METHOD_CENTERED = 2,
        F2D_METHOD_CWENO = 3 };
-/* Runge-Kutta integrators (integrators.py:63-131): SSP-RK3, Euler forward,
- * energy-conserving RK3 */
-enum { F2D_INTEG_RK3 = 0, F2D_INTEG_EF = 1, F2D_INTEG_ENRK3 = 2 };
+/* integrators (integrators.py:9-131): SSP-RK3, Euler forward,
+ * energy-conserving RK3, leap-frog with Robert-Asselin filter */
+enum { F2D_INTEG_RK3 = 0, F2D_INTEG_EF = 1, F2D_INTEG_ENRK3 = 2,
+       F2D_INTEG_LFRA = 3 };
 /* arithmetic of the stencils and of the multigrid cycle */
 enum { F2D_PREC_FP64 = 0, F2D_PREC_FP32 = 1 };
 /* param.noslip (noslip.py:18-34): None/False, True, or a list of sides */
@@ -56,7 +57,8 @@ typedef struct f2d_params {
     double poisson_tol; /* relative residual of the Poisson solve */
     int poisson_maxit;
     int integrator;     /* F2D_INTEG_* */
-    int reserved[6];
+    double ragamma;     /* Robert-Asselin coefficient of LFRA (param.py:50) */
+    int reserved[4];
 } f2d_params;
 
 typedef struct f2d_model_s *f2d_model;

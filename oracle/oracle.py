@@ -122,6 +122,7 @@ class Param:
         self.maxite = 100
         self.dtmax = 9e99
         self.integrator = "rk3"
+        self.RAgamma = 0.1
         self.cfl = 0.9
         self.compflux = "weno"
         self.vortexforce = "weno"
@@ -569,6 +570,28 @@ class Model:
         self._addto([5 * dt / 48 + dt / 10, -7 * dt / 16, 2 * dt / 5], [ds1, ds2, ds3])
         self.diag()
 
+    def lfra(self, dt):
+        """integrators.py:39-55 (LFRA) with rightpermute (134-137): Euler
+        forward at ite == 0 (sb = sa = s), then sa += 2 dt ds;
+        s += gamma sa + gamma sb - 2 gamma s; (sb, s, sa) <- (s, sa, s)."""
+        sb, sa, ds = self.scratch
+        gam = getattr(self.p, "RAgamma", 0.1)
+        self.rhs(self.s, ds)
+        if self.ite == 0:
+            for k in self.prog:
+                sb[k][:] = self.s[k]
+                sa[k][:] = self.s[k]
+            self._addto([dt], [ds])
+        else:
+            for k in self.prog:
+                sa[k][:] += sum((c * d[k] for c, d in zip([2 * dt], [ds])))
+            self._addto([gam, gam, -2 * gam], [sa, sb, self.s])
+            for k in self.prog:
+                sb[k][:] = self.s[k]
+                self.s[k][:] = sa[k]
+                sa[k][:] = sb[k]
+        self.diag()
+
     def pushforward(self):
         """timeline.py:20-35 (Kahan-summed time)."""
         y = self.dt - self._c
@@ -592,8 +615,8 @@ class Model:
         self.dt = min(p.cfl / maxU, p.dtmax)
 
     def step(self, n=1):
-        integ = {"rk3": self.rk3, "ef": self.ef,
-                 "enrk3": self.enrk3}[getattr(self.p, "integrator", "rk3")]
+        integ = {"rk3": self.rk3, "ef": self.ef, "enrk3": self.enrk3,
+                 "LFRA": self.lfra}[getattr(self.p, "integrator", "rk3")]
         for _ in range(n):
             integ(self.dt)
             self.pushforward()

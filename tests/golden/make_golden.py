@@ -213,6 +213,8 @@ def run_model(case, nsteps, fname, cfl=None, extra=None):
         out["f"] = case["f"].copy()
     if extra and "integrator" in extra:
         out["integrator"] = np.array(extra["integrator"])
+    if extra and "RAgamma" in extra:
+        out["RAgamma"] = np.array(float(extra["RAgamma"]))
     for k, v in case["fields"].items():
         out["ic/" + k] = v.copy()
 
@@ -278,11 +280,31 @@ def integrator_cases():
               extra={"integrator": "enrk3"})
     c = wl.rsw_case(n=40, ny=32, seed=3, nislands=2)
     run_model(c, 4, "model_rsw_enrk3.npz", extra={"integrator": "enrk3"})
+    lfra_cases()
+
+
+def lfra_cases():
+    """Leap-frog with the Robert-Asselin filter (integrators.py:20-55): an
+    Euler-forward first step, then leap-frog steps."""
+    c = wl.eulerpsi_case(n=40, ny=32, seed=2, nislands=2, nvortices=5,
+                         radius=0.08)
+    run_model(c, 6, "model_eulerpsi_lfra.npz", cfl=0.4,
+              extra={"integrator": "LFRA"})
+    c = wl.qg_case(n=40, ny=32, seed=4, nislands=3, kmin=2, kmax=8)
+    run_model(c, 5, "model_qg_lfra.npz", cfl=0.4,
+              extra={"integrator": "LFRA", "RAgamma": 0.2})
+    c = wl.rsw_case(n=40, ny=32, seed=3, nislands=2)
+    run_model(c, 6, "model_rsw_lfra.npz", cfl=0.4, extra={"integrator": "LFRA"})
+    c = wl.euler_case(n=40, ny=32, seed=6, nislands=2, xperiodic=True)
+    run_model(c, 5, "model_euler_lfra_periodic.npz", cfl=0.4,
+              extra={"integrator": "LFRA"})
 
 
 if __name__ == "__main__":
     which = sys.argv[1:] or ["mesh", "sweeps", "poisson", "models", "integrators",
                              "euler"]
+    if "lfra" in which:
+        lfra_cases()
     if "mesh" in which:
         mesh_cases()
     if "sweeps" in which:

@@ -127,7 +127,9 @@ def test_poisson_zero_rhs():
 MODEL_FILES = ["model_eulerpsi.npz", "model_eulerpsi_islands.npz",
                "model_rsw.npz", "model_qg.npz", "model_eulerpsi_ef.npz",
                "model_eulerpsi_enrk3.npz", "model_rsw_enrk3.npz",
-               "model_euler.npz", "model_euler_periodic.npz"]
+               "model_euler.npz", "model_euler_periodic.npz",
+               "model_eulerpsi_lfra.npz", "model_qg_lfra.npz", "model_rsw_lfra.npz",
+               "model_euler_lfra_periodic.npz"]
 
 
 def model_from_golden(g):
@@ -137,9 +139,10 @@ def model_from_golden(g):
     kind = ("eulerpsi" if "omega" in names else "rsw" if "h" in names else
             "euler" if "u.x" in names else "qg")
     integ = str(g["integrator"]) if "integrator" in g.files else "rk3"
+    gam = float(g["RAgamma"]) if "RAgamma" in g.files else 0.1
     m = _model(kind, nx, ny, g["msk"], xperiodic=bool(xper), Lx=Lx, Ly=Ly, f0=f0,
                beta=beta, g=gg, H=H, cfl=cfl, tend=1e300, maxite=10 ** 9,
-               integrator=integ)
+               integrator=integ, RAgamma=gam)
     if "f" in g.files:
         m.mesh.f = g["f"]
     s = m.state
@@ -384,17 +387,19 @@ def test_fp32_model_poisson_reaches_fp64_accuracy(case):
     assert rel_l2(x, g[case + "/x"]) <= SOLVE_TOL, rel_l2(x, g[case + "/x"])
 
 
-@pytest.mark.parametrize("kind", ["eulerpsi", "rsw", "qg"])
-def test_fp32_model_vs_fp64_oracle(kind):
+@pytest.mark.parametrize("kind,integrator",
+                         [("eulerpsi", "rk3"), ("rsw", "rk3"), ("qg", "rk3"),
+                          ("eulerpsi", "LFRA"), ("rsw", "LFRA")])
+def test_fp32_model_vs_fp64_oracle(kind, integrator):
     if kind == "eulerpsi":
         case = wl.eulerpsi_case(n=128, ny=96, seed=5, nislands=3)
     elif kind == "rsw":
         case = wl.rsw_case(n=128, ny=96, seed=6, nislands=3)
     else:
         case = wl.qg_case(n=128, ny=128, seed=7, nislands=4)
-    om = _oracle_like(case, kind)
+    om = _oracle_like(case, kind, integrator=integrator)
     kw = dict(xperiodic=case.get("xperiodic", False), Lx=case["Lx"], Ly=case["Ly"],
-              tend=1e300, maxite=10 ** 9, precision="fp32")
+              tend=1e300, maxite=10 ** 9, precision="fp32", integrator=integrator)
     for k in ("f0", "g", "H", "beta"):
         if k in case:
             kw[k] = case[k]
@@ -410,14 +415,50 @@ def test_fp32_model_vs_fp64_oracle(kind):
         m.advance(1)
     m.sync()
     worst = compare(m, lambda k: om.s.get(k), FP32_STATE_TOL[kind])
-    print(f"FP32 {kind} rel L2 after 5 steps:",
+    print(f"FP32 {kind} {integrator} rel L2 after 5 steps:",
           {k: f"{v:.2e}" for k, v in worst.items()})
 
 
+@pytest.mark.parametrize("kind", ["eulerpsi", "rsw"])
+def test_lfra_restart_is_euler_forward(kind):
+    """LFRA's first step is taken at ite == 0 (integrators.py:33): resetting
+    the time line to ite = 0 restarts with an Euler-forward step, whatever the
+    stored previous state; the leap-frog steps that follow match the oracle
+    restarted from the same state."""
+    case = (wl.eulerpsi_case(n=64, ny=48, seed=3, nislands=2) if kind == "eulerpsi"
+            else wl.rsw_case(n=64, ny=48, seed=4, nislands=2))
+    kw = dict(Lx=case["Lx"], Ly=case["Ly"], tend=1e300, maxite=10 ** 9,
+              integrator="LFRA", cfl=0.4)
+    for k in ("f0", "g", "H", "beta"):
+        if k in case:
+            kw[k] = case[k]
+    m = _model(kind, case["nx"], case["ny"], case["msk"], **kw)
+    s = m.state
+    for k, v in case["fields"].items():
+        getattr(s, k)[:] = v
+    m.integrator.diag(s)
+    m.advance(3)
+    m.sync()
+    # restart from the state reached: a fresh oracle (ite = 0) from it
+    om = _oracle_like(case, kind, integrator="LFRA", cfl=0.4)
+    for k in om.prog:
+        v = getattr(m.state, k.split(".")[0])
+        om.s[k][:] = getattr(v, k.split(".")[1]) if "." in k else v
+    om.diag()
+    m.time.ite = 0
+    m.time.t = 0.0
+    for _ in range(3):
+        om.run_steps(1)
+        m.advance(1)
+    m.sync()
+    compare(m, lambda k: om.s.get(k), STEP_TOL)
+
+
 # ------------------------------------------------------------ ensembles ----
-def _ensemble(members, precision="fp64", kind="eulerpsi"):
+def _ensemble(members, precision="fp64", kind="eulerpsi", integrator="rk3"):
     p = f2d.Param()
     p.model = kind
+    p.integrator = integrator
     p.cfl = 0.8
     p.tend = 1e300
     p.maxite = 10 ** 9
@@ -435,8 +476,10 @@ def _ensemble(members, precision="fp64", kind="eulerpsi"):
     return e
 
 
-@pytest.mark.parametrize("precision", ["fp64", "fp32"])
-def test_ensemble_members_match_single_models(precision):
+@pytest.mark.parametrize("precision,integrator",
+                         [("fp64", "rk3"), ("fp32", "rk3"), ("fp64", "enrk3"),
+                          ("fp64", "LFRA"), ("fp32", "LFRA")])
+def test_ensemble_members_match_single_models(precision, integrator):
     """Every member equals the same case run alone (same device code, same
     per-member reductions): FP64 to the step tolerance; FP32 to 1e-6, since
     the batched and the single-model stage kernels are separate
@@ -446,12 +489,12 @@ def test_ensemble_members_match_single_models(precision):
     members = [wl.eulerpsi_case(n=64, ny=48, seed=11, nislands=2),
                wl.eulerpsi_case(n=96, ny=96, seed=12, nislands=0),
                wl.eulerpsi_case(n=40, ny=72, seed=13, nislands=3)]
-    e = _ensemble(members, precision)
+    e = _ensemble(members, precision, integrator=integrator)
     e.run(4)
     e.sync()
     for b, c in enumerate(members):
         m = _model("eulerpsi", c["nx"], c["ny"], c["msk"], cfl=0.8, tend=1e300,
-                   maxite=10 ** 9, precision=precision)
+                   maxite=10 ** 9, precision=precision, integrator=integrator)
         m.state.omega[:] = c["fields"]["omega"]
         m.integrator.diag(m.state)
         m.advance(4)

@@ -105,7 +105,9 @@ def test_poisson_vs_reference(case):
 MODEL_FILES = ["model_eulerpsi.npz", "model_eulerpsi_islands.npz",
                "model_rsw.npz", "model_qg.npz", "model_eulerpsi_ef.npz",
                "model_eulerpsi_enrk3.npz", "model_rsw_enrk3.npz",
-               "model_euler.npz", "model_euler_periodic.npz"]
+               "model_euler.npz", "model_euler_periodic.npz",
+               "model_eulerpsi_lfra.npz", "model_qg_lfra.npz", "model_rsw_lfra.npz",
+               "model_euler_lfra_periodic.npz"]
 
 
 def oracle_from_golden(g, pysq=True):
@@ -116,9 +118,10 @@ def oracle_from_golden(g, pysq=True):
     kind = ("eulerpsi" if "omega" in names else
             "rsw" if "h" in names else "euler" if "u.x" in names else "qg")
     integ = str(g["integrator"]) if "integrator" in g.files else "rk3"
+    gam = float(g["RAgamma"]) if "RAgamma" in g.files else 0.1
     p = O.Param(model=kind, nx=nx, ny=ny, xperiodic=bool(xper), Lx=Lx, Ly=Ly,
                 f0=f0, beta=beta, g=gg, H=H, cfl=cfl, tend=1e9,
-                maxite=10 ** 9, integrator=integ)
+                maxite=10 ** 9, integrator=integ, RAgamma=gam)
     m = O.Model(p, msk=g["msk"], pysq=pysq)
     if "f" in g.files:
         m.mesh.f = g["f"].copy()
