@@ -63,6 +63,11 @@ WORKLOADS = {
                  "euler (momentum-pressure) 512x512 closed basin, 3 islands, WENO5 "
                  "vortex force, SSP-RK3, cfl 0.5, FP64, Neumann multigrid-PCG "
                  "pressure projection"),
+    "boussinesq512": ("boussinesq", dict(n=512, seed=0, nislands=3),
+                      "boussinesq (momentum-pressure + buoyancy) 512x512 closed "
+                      "basin, 3 islands, stratification + 2 bubbles, WENO5, "
+                      "SSP-RK3, cfl 0.5, FP64, Neumann multigrid-PCG pressure "
+                      "projection"),
     "rsw1024": ("rsw", dict(n=1024, seed=0, nislands=3),
                 "rsw 1024x1024 x-periodic channel, 3 islands, FP64 (profiling "
                 "size: working set above the L2)"),
@@ -140,6 +145,8 @@ def build_case(name):
         case = wl.rsw_case(**kw)
     elif model == "euler":
         case = wl.euler_case(**kw)
+    elif model == "boussinesq":
+        case = wl.boussinesq_case(**kw)
     elif model == "eulerpsi":
         case = wl.eulerpsi_case(**kw)
     else:
@@ -160,7 +167,7 @@ def make_gpu_model(model, case, stream_ptr, precision="fp64", tol=None):
             setattr(p, k, case[k])
     if model == "eulerpsi":
         p.cfl = 0.8
-    if model == "euler":
+    if model in ("euler", "boussinesq"):
         p.cfl = 0.5
     p.tend = 1e300
     p.maxite = 10 ** 12
@@ -185,7 +192,8 @@ def make_gpu_model(model, case, stream_ptr, precision="fp64", tol=None):
 
 def prognostic_names(model):
     return {"rsw": ["u.x", "u.y", "h"], "eulerpsi": ["omega"],
-            "qg": ["pv"], "euler": ["u.x", "u.y"]}[model]
+            "qg": ["pv"], "euler": ["u.x", "u.y"],
+            "boussinesq": ["b", "u.x", "u.y"]}[model]
 
 
 # algorithmic bytes per array point of the stage-2 launch of the fused stage
@@ -197,6 +205,8 @@ STAGE2_BYTES = {
     # euler (momentum kernel without the mass equation): read u.x, u.y, U.x,
     # U.y, ke, omega + 2 ds1 (8 x 8) + code; write u.x, u.y + 2 ds2 (4 x 8)
     "euler": 8 * 8 + 4 + 4 * 8,
+    # boussinesq: euler + b and its ds1 read, b and its ds2 written
+    "boussinesq": 10 * 8 + 4 + 6 * 8,
     # flux form: read q,U.x,U.y,ds1 (4 x 8) + code (4); write q, ds2 (2 x 8)
     "eulerpsi": 4 * 8 + 4 + 2 * 8,
     "qg": 4 * 8 + 4 + 2 * 8,
@@ -297,7 +307,7 @@ def cpu_oracle_rate(model, case, budget_s, max_steps=None, warmup=1):
             setattr(p, k, case[k])
     if model == "eulerpsi":
         p.cfl = 0.8
-    if model == "euler":
+    if model in ("euler", "boussinesq"):
         p.cfl = 0.5
     om = O.Model(p, msk=case["msk"], pysq=False)
     if "f" in case:
@@ -805,7 +815,8 @@ def run_gpu(args, rank, world):
     except Exception:
         peak, peak_src = 6800.0, "fallback"
     kname = {"rsw": "k_rsw_stage", "eulerpsi": "k_fluxform_stage",
-             "qg": "k_fluxform_stage", "euler": "k_rsw_stage"}[model]
+             "qg": "k_fluxform_stage", "euler": "k_rsw_stage",
+             "boussinesq": "k_rsw_stage"}[model]
     traffic = read_profile_traffic(f"{kname}_{args.workload}")
     fp64_pct = read_profile_value(f"{kname}_{args.workload}", "fp64_pipe_pct")
 

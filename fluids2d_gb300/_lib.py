@@ -18,7 +18,7 @@ c_i64 = ctypes.c_int64
 c_dbl = ctypes.c_double
 c_void_p = ctypes.c_void_p
 
-MODELS = {"eulerpsi": 0, "rsw": 1, "qg": 2, "euler": 3}
+MODELS = {"eulerpsi": 0, "rsw": 1, "qg": 2, "euler": 3, "boussinesq": 4}
 METHODS = {"weno": 0, "upwind": 1, "centered": 2, "cweno": 3}
 PRECISIONS = {"fp64": 0, "fp32": 1}
 INTEGRATORS = {"rk3": 0, "ef": 1, "enrk3": 2, "LFRA": 3}

@@ -143,6 +143,13 @@ static void* dalloc(f2d_model_s* m, size_t bytes)
     return p;
 }
 
+// the models stepped in momentum-pressure form with the Neumann pressure
+// projection (euler, boussinesq: equations.py:9-44)
+static bool projected(int model)
+{
+    return model == F2D_MODEL_EULER || model == F2D_MODEL_BOUSSINESQ;
+}
+
 static size_t field_bytes(const f2d_model_s* m, size_t es)
 {
     return (size_t)m->g.P * m->g.NY * es;
@@ -187,8 +194,7 @@ static int make_tmap(f2d_model_s* m, void* buf)
     cuuint64_t strides[1] = {(cuuint64_t)(m->g.P * m->es)};
     // tile + halo: SW x FSH for the flux-form stage, SW x SH for rsw
     cuuint32_t box[2] = {(cuuint32_t)SW,
-                         (cuuint32_t)(m->p.model == F2D_MODEL_RSW ||
-                                              m->p.model == F2D_MODEL_EULER
+                         (cuuint32_t)(m->p.model == F2D_MODEL_RSW || projected(m->p.model)
                                           ? SH
                                           : FSH)};
     cuuint32_t estr[2] = {1, 1};
@@ -329,9 +335,11 @@ static int rec_diag(f2d_model_s* m, int par, cudaStream_t s)
         m->rec_launches += 1;
         return 0;
     }
-    case F2D_MODEL_EULER: {
+    case F2D_MODEL_EULER:
+    case F2D_MODEL_BOUSSINESQ: {
         // pressure_projection (operators.py:114-119), then sharp, vorticity,
-        // kinetic energy (equations.py:17-22)
+        // kinetic energy (equations.py:17-22; the boussinesq diag, 37-43, is
+        // the same: its fill(s.u) names no mesh and fills nothing)
         CKI(launch_euler_div(m->prec, fb(m, "u.x", par), fb(m, "u.y", par), fb(m, "div"),
                              m->nrhs, m->d_code, m->rdx2, m->rdy2, m->area, g, s));
         int e = ensure_ns(m);
@@ -396,19 +404,23 @@ static int launch_stage_kernel(f2d_model_s* m, int k, int par, cudaStream_t s)
     auto ds = [&](const char* f, int kk) -> void* {
         return fb(m, (std::string("ds") + std::to_string(kk) + "." + f).c_str());
     };
-    if (m->p.model == F2D_MODEL_RSW || m->p.model == F2D_MODEL_EULER) {
+    if (m->p.model == F2D_MODEL_RSW || projected(m->p.model)) {
         // rsw; euler = the same momentum kernel without the mass equation,
-        // Coriolis and pressure (equations.py:11-15)
+        // Coriolis and pressure (equations.py:11-15); boussinesq = euler +
+        // buoyancy + the flux divergence of b in the place of h (29-35)
         const bool eu = m->p.model == F2D_MODEL_EULER;
+        const bool bq = m->p.model == F2D_MODEL_BOUSSINESQ;
+        const char* hn = bq ? "b" : "h";
         RswIn a;
         memset(&a, 0, sizeof(a));
-        a.euler = eu ? 1 : 0;
+        a.euler = eu ? 1 : bq ? 2 : 0;
+        a.bdy = 0.5 * m->dy;
         a.ux = fb(m, "u.x", par);
         a.uy = fb(m, "u.y", par);
-        a.h = fb(m, "h", par);
+        a.h = eu ? nullptr : fb(m, hn, par);
         a.uxo = fb(m, "u.x", out);
         a.uyo = fb(m, "u.y", out);
-        a.ho = fb(m, "h", out);
+        a.ho = eu ? nullptr : fb(m, hn, out);
         a.Ux = fb(m, "U.x");
         a.Uy = fb(m, "U.y");
         a.ke = fb(m, "ke");
@@ -419,14 +431,14 @@ static int launch_stage_kernel(f2d_model_s* m, int k, int par, cudaStream_t s)
         if (kout < 3) {
             a.dux = ds("u.x", kout);
             a.duy = ds("u.y", kout);
-            a.dh = ds("h", kout);
+            a.dh = eu ? nullptr : ds(hn, kout);
         }
         a.dux1 = ds("u.x", kin);
         a.duy1 = ds("u.y", kin);
-        a.dh1 = ds("h", kin);
+        a.dh1 = eu ? nullptr : ds(hn, kin);
         a.dux2 = ds("u.x", 2);
         a.duy2 = ds("u.y", 2);
-        a.dh2 = ds("h", 2);
+        a.dh2 = eu ? nullptr : ds(hn, 2);
         a.fc = m->fc;
         void* om = fb(m, "omega");
         void* hm = eu ? om : (void*)a.h;  // euler stages no thickness tile
@@ -569,7 +581,7 @@ static int run_graph(f2d_model_s* m, int kind)
         if (m->p.model == F2D_MODEL_EULERPSI || m->p.model == F2D_MODEL_QG) {
             int e0 = ensure_mg(m, m->p.model == F2D_MODEL_EULERPSI ? 0 : 1);
             if (e0) return e0;
-        } else if (m->p.model == F2D_MODEL_EULER) {
+        } else if (projected(m->p.model)) {
             int e0 = ensure_ns(m);
             if (e0) return e0;
         }
@@ -585,7 +597,7 @@ static int run_graph(f2d_model_s* m, int kind)
         if (m->p.model == F2D_MODEL_EULERPSI || m->p.model == F2D_MODEL_QG) {
             int e0 = ensure_mg(m, m->p.model == F2D_MODEL_EULERPSI ? 0 : 1);
             if (e0) return e0;
-        } else if (m->p.model == F2D_MODEL_EULER) {
+        } else if (projected(m->p.model)) {
             int e0 = ensure_ns(m);
             if (e0) return e0;
         }
@@ -732,16 +744,17 @@ int f2d_model_create(const f2d_params* p, const int8_t* msk, f2d_model* out)
     if (!p || !out) return fail(1, "null argument");
     if (p->precision != F2D_PREC_FP64 && p->precision != F2D_PREC_FP32)
         return fail(1, "unknown precision");
-    if (p->model < 0 || p->model > 3) return fail(1, "unknown model");
-    if (p->model == F2D_MODEL_EULER && p->precision != F2D_PREC_FP64)
-        return fail(1, "the euler model runs in FP64");
+    if (p->model < 0 || p->model > 4) return fail(1, "unknown model");
+    if (projected(p->model) && p->precision != F2D_PREC_FP64)
+        return fail(1, "the euler and boussinesq models run in FP64");
 
     if (p->integrator < F2D_INTEG_RK3 || p->integrator > F2D_INTEG_LFRA)
         return fail(1, "unknown integrator (rk3, ef, enrk3, LFRA)");
     if (p->xperiodic && p->nx < 6) return fail(1, "x-periodic needs nx >= 6");
-    if (p->model == F2D_MODEL_RSW && p->vortexforce != p->compflux)
-        return fail(1, "the fused rsw stage uses one flux method for vortexforce and "
-                       "compflux; they must be equal");
+    if ((p->model == F2D_MODEL_RSW || p->model == F2D_MODEL_BOUSSINESQ) &&
+        p->vortexforce != p->compflux)
+        return fail(1, "the fused rsw/boussinesq stage uses one flux method for "
+                       "vortexforce and compflux; they must be equal");
     auto* m = new f2d_model_s();
     m->p = *p;
     m->prec = p->precision == F2D_PREC_FP64 ? 0 : 1;
@@ -792,6 +805,11 @@ int f2d_model_create(const f2d_params* p, const int8_t* msk, f2d_model* out)
               {"omega", false}, {"ke", false}, {"p", false}, {"div", false},
               {"flx.x", false}, {"flx.y", false}};
         prog = {"u.x", "u.y"};
+    } else if (p->model == F2D_MODEL_BOUSSINESQ) {
+        fl = {{"b", true}, {"u.x", true}, {"u.y", true}, {"U.x", false}, {"U.y", false},
+              {"omega", false}, {"ke", false}, {"p", false}, {"div", false},
+              {"flx.x", false}, {"flx.y", false}};
+        prog = {"b", "u.x", "u.y"};
     } else if (p->model == F2D_MODEL_RSW) {
         fl = {{"u.x", true}, {"u.y", true}, {"h", true}, {"U.x", false}, {"U.y", false},
               {"omega", false}, {"ke", false}, {"p", false}, {"flx.x", false},
@@ -815,7 +833,7 @@ int f2d_model_create(const f2d_params* p, const int8_t* msk, f2d_model* out)
             if ((e = add_field(m, (std::string("ds") + std::to_string(k) + "." + f).c_str(),
                                false, (int)m->es)))
                 return bail(e);
-    if (p->model == F2D_MODEL_EULER) {
+    if (projected(p->model)) {
         m->nrhs = (double*)dalloc(m, field_bytes(m, 8));
         if (!m->nrhs) return bail(fail(2, "out of device memory"));
     } else if (p->model != F2D_MODEL_RSW) {
@@ -1185,8 +1203,9 @@ int f2d_time_solver(f2d_model m, int reps, int flush_l2, double* avg_ms, int64_t
 {
     if (!m || !avg_ms) return fail(1, "null argument");
     if (m->p.model == F2D_MODEL_RSW) return fail(1, "rsw has no Poisson solve");
-    if (m->p.model == F2D_MODEL_EULER)
-        return fail(1, "the euler model's Neumann solve has no timing hook");
+    if (projected(m->p.model))
+        return fail(1, "the Neumann solve of the euler and boussinesq models has no "
+                       "timing hook");
     const int which = m->p.model == F2D_MODEL_EULERPSI ? 0 : 1;
     if (!m->bs_ready[which]) return fail(9, "the solver has not run yet");
     CK(cudaStreamSynchronize(m->stream));

@@ -37,7 +37,10 @@ k_fluxform_stage(const __grid_constant__ CUtensorMap tq, const T* __restrict__ q
 // ---------------------------------------------------------------------------
 // Rotating shallow water right-hand side (equations.py:139-148) + RK3 update
 // of (u.x, u.y, h): vortex force (weno.vortexforce), Coriolis, gradients of
-// ke and p, mass flux divergence.
+// ke and p, mass flux divergence. The same kernel steps the euler model
+// (vortex force and grad ke, equations.py:11-15) and the boussinesq model
+// (euler + buoyancy, with the flux divergence of b in place of h,
+// equations.py:29-35).
 // ---------------------------------------------------------------------------
 template <typename T, int M>
 __global__ void __launch_bounds__(TX * TY)
@@ -92,7 +95,7 @@ k_rsw_stage(const __grid_constant__ CUtensorMap th,
         }
         sfy[r][c] = f;
     };
-    if (!a.euler) {
+    if (a.euler != 1) {
         xface(ty, tx);
         yface(ty, tx);
         if (t < TY) xface(t, TX);
@@ -140,25 +143,29 @@ k_rsw_stage(const __grid_constant__ CUtensorMap th,
     __syncthreads();
     if (!live) return;
 
-    // Coriolis (addcoriolis, operators.py:32-39); the euler model
-    // (equations.py:11-15) has neither Coriolis nor a pressure gradient here
+    // Coriolis (addcoriolis, operators.py:32-39); the euler and boussinesq
+    // models (equations.py:11-15, 29-35) have neither Coriolis nor a pressure
+    // gradient here
     const T fc = srk[3];
-    if (!a.euler && j <= g.NY - 2 && i >= 1 && i <= g.NX - 2)
+    if (a.euler == 0 && j <= g.NY - 2 && i >= 1 && i <= g.NX - 2)
         dux += fc * (((ldz(Uy, j, i - 1, g) + ldz(Uy, j + 1, i - 1, g)) + Uy[o]) +
                      ldz(Uy, j + 1, i, g));
-    if (!a.euler && j >= 1 && j <= g.NY - 2 && i <= g.NX - 2)
+    if (a.euler == 0 && j >= 1 && j <= g.NY - 2 && i <= g.NX - 2)
         duy -= fc * (((ldz(Ux, j - 1, i, g) + ldz(Ux, j - 1, i + 1, g)) + Ux[o]) +
                      ldz(Ux, j, i + 1, g));
     // gradients of ke then p (addgrad, operators.py:49-56)
     if (i >= 1) {
         const T mx = (cd & B_MSKX) ? T(1) : T(0);
         dux -= (ke[o] - ke[o - 1]) * mx;
-        if (!a.euler) dux -= (p[o] - p[o - 1]) * mx;
+        if (a.euler == 0) dux -= (p[o] - p[o - 1]) * mx;
     }
     if (j >= 1) {
         const T my = (cd & B_MSKY) ? T(1) : T(0);
         duy -= (ke[o] - ke[o - g.P]) * my;
-        if (!a.euler) duy -= (p[o] - p[o - g.P]) * my;
+        if (a.euler == 0) duy -= (p[o] - p[o - g.P]) * my;
+        // boussinesq buoyancy (operators.py:152-153), after the gradients
+        if (a.euler == 2)
+            duy += (T(a.bdy) * (sh[ty + OY][tx + OX] + sh[ty + OY - 1][tx + OX])) * my;
     }
     // mass: dh = -div(flux) * msk
     const T msk = (cd & B_MSK) ? T(1) : T(0);
@@ -166,7 +173,7 @@ k_rsw_stage(const __grid_constant__ CUtensorMap th,
 
     const T* dt = srk;
     T ix, iy, ih = T(0);
-    const bool hm = !a.euler;  // mass equation (rsw)
+    const bool hm = a.euler != 1;  // mass (rsw) or buoyancy (boussinesq) equation
     if (lf) {
         // leap-frog + Robert-Asselin: dux1.. = filtered previous state in,
         // dux.. = out (buffers alternating with the parity)

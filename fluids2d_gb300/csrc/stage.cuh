@@ -12,7 +12,10 @@ struct RswIn {
     const void *dux1, *duy1, *dh1;  // earlier tendencies
     const void *dux2, *duy2, *dh2;
     double fc;                      // f0 * area * 0.25 (operators.py:33)
-    int euler;                      // euler model: vortex force + grad ke only
+    double bdy;                     // 0.5 * dy (addbuoyancy, operators.py:152-153)
+    // 0 rsw; 1 euler (vortex force + grad ke only); 2 boussinesq (euler +
+    // buoyancy, with the buoyancy b advected in place of h)
+    int euler;
 };
 
 struct RswDiag {

@@ -26,6 +26,7 @@ from .param import Param
 MODEL_SPECS = {
     "eulerpsi": (("omega", "U", "psi", "vomega", "flx"), ("omega",)),
     "euler": (("u", "U", "omega", "ke", "p", "div", "flx"), ("u",)),
+    "boussinesq": (("b", "u", "U", "omega", "ke", "p", "div", "flx"), ("b", "u")),
     "rsw": (("u", "h", "U", "omega", "ke", "p", "flx", "pv"), ("u", "h")),
     "qg": (("pv", "U", "h", "flx", "work", "psi"), ("pv",)),
 }

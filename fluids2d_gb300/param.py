@@ -14,7 +14,7 @@ _methods_extended = _methods + ["classic"]
 _integrators = ["rk3", "ef", "enrk3", "LFRA"]
 
 # models and integrators the GPU path implements
-SUPPORTED_MODELS = ("eulerpsi", "rsw", "qg", "euler")
+SUPPORTED_MODELS = ("eulerpsi", "rsw", "qg", "euler", "boussinesq")
 SUPPORTED_INTEGRATORS = ("rk3", "ef", "enrk3", "LFRA")
 EXTRA = ("precision", "poisson_tol", "poisson_maxit")
 
@@ -98,10 +98,11 @@ class Param:
             raise NotImplementedError("halowidth must be 3")
         if self.yperiodic:
             raise NotImplementedError("yperiodic is not supported")
-        if self.model in ("rsw", "euler") and self.innerproduct == "classic":
+        if self.model in ("rsw", "euler", "boussinesq") and self.innerproduct == "classic":
             raise NotImplementedError("innerproduct='classic' is not implemented")
-        if self.model == "euler" and getattr(self, "precision", "fp64") != "fp64":
-            raise NotImplementedError("the euler model runs in FP64")
+        if (self.model in ("euler", "boussinesq")
+                and getattr(self, "precision", "fp64") != "fp64"):
+            raise NotImplementedError(f"the {self.model} model runs in FP64")
         assert self.precision in ("fp64", "fp32")
 
 

@@ -218,6 +218,37 @@ def euler_case(n=128, seed=0, nislands=2, ny=None, Lx=1.0, Ly=1.0, xperiodic=Fal
                 xperiodic=xperiodic, fields={"u.x": ux, "u.y": uy})
 
 
+def boussinesq_case(n=128, seed=0, nislands=2, ny=None, Lx=1.0, Ly=1.0,
+                    xperiodic=False, nbubbles=2, strat=0.5, **kw):
+    """Boussinesq (momentum-pressure form with buoyancy b): the velocity of
+    euler_case plus a buoyancy field of a stable linear stratification and
+    Gaussian bubbles, masked by msk. The amplitude is set so that the
+    buoyancy force changes u by about a tenth of its size per CFL step."""
+    c = euler_case(n=n, seed=seed, nislands=nislands, ny=ny, Lx=Lx, Ly=Ly,
+                   xperiodic=xperiodic, **kw)
+    nx, ny = c["nx"], c["ny"]
+    x, y = grid_coords(nx, ny, Lx, Ly, which="c")
+    rng = np.random.default_rng(seed + 31)
+    dx, dy = Lx / nx, Ly / ny
+    umax = max(np.abs(c["fields"]["u.x"]).max(), np.abs(c["fields"]["u.y"]).max(),
+               1e-300)
+    amp = 0.1 * umax ** 2 / (dy * dx ** 2)
+    b = strat * amp * (y / Ly - 0.5)
+    for _ in range(nbubbles):
+        x0, y0 = rng.uniform(0.2, 0.8) * Lx, rng.uniform(0.2, 0.5) * Ly
+        r0 = rng.uniform(0.06, 0.12) * Lx
+        b = b + amp * rng.choice([-1.0, 1.0]) * np.exp(-((x - x0) ** 2 + (y - y0) ** 2)
+                                                      / r0 ** 2)
+    b = b * c["msk"]
+    if xperiodic:
+        hw = 3
+        b[:, :hw] = b[:, -2 * hw:-hw]
+        b[:, -hw:] = b[:, hw:2 * hw]
+    c["model"] = "boussinesq"
+    c["fields"]["b"] = b
+    return c
+
+
 def ensemble_case(count=256, seed=0, sizes=(64, 128, 192, 256, 384, 512),
                   max_islands=4, nvortices=8, radius=0.05):
     """Batched ensemble of closed-basin eulerpsi members: grid sizes drawn

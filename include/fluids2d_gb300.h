@@ -22,9 +22,9 @@ extern "C" {
 
 #define F2D_ABI_VERSION 1
 
-/* models (param.py:1-2); the hot path covers these three */
+/* models (param.py:1-2) the GPU path implements */
 enum { F2D_MODEL_EULERPSI = 0, F2D_MODEL_RSW = 1, F2D_MODEL_QG = 2,
-       F2D_MODEL_EULER = 3 };
+       F2D_MODEL_EULER = 3, F2D_MODEL_BOUSSINESQ = 4 };
 /* flux methods (param.py:4, weno.py:338-343) */
 enum { F2D_METHOD_WENO = 0, F2D_METHOD_UPWIND = 1, F2D_METHOD_CENTERED = 2,
        F2D_METHOD_CWENO = 3 };

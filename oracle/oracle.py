@@ -361,6 +361,11 @@ def addgrad(mesh, phi, dux, duy):
     duy[1:, :] -= np.diff(phi, axis=0) * mesh.msky[1:, :]
 
 
+def addbuoyancy(mesh, b, duy):
+    """operators.py:152-153."""
+    duy[1:, :] += (0.5 * mesh.dy) * (b[1:, :] + b[:-1, :]) * mesh.msky[1:, :]
+
+
 def sharp(mesh, ux, uy, Ux, Uy):
     """operators.py:59-62."""
     Ux[:] = ux * (1 / mesh.dx ** 2)
@@ -424,13 +429,14 @@ def perpgrad(mesh, psi, Ux, Uy, contravariant=False):
 
 STATE_VARS = {
     "euler": ("u", "U", "omega", "ke", "p", "div", "flx"),
+    "boussinesq": ("b", "u", "U", "omega", "ke", "p", "div", "flx"),
     # states.py:7-17 (the models on the hot path); vector fields get .x/.y
     "eulerpsi": ("omega", "U", "psi", "vomega", "flx"),
     "rsw": ("u", "h", "U", "omega", "ke", "p", "flx", "pv"),
     "qg": ("pv", "U", "h", "flx", "work", "psi"),
 }
 PROGNOSTIC = {"eulerpsi": ("omega",), "rsw": ("u", "h"), "qg": ("pv",),
-              "euler": ("u",)}
+              "euler": ("u",), "boussinesq": ("b", "u")}
 VECTORS = ("u", "U", "flx")
 
 
@@ -495,6 +501,16 @@ class Model:
             addgrad(m, s["ke"], ds["u.x"], ds["u.y"])
             for k in ("u.x", "u.y"):
                 m.fill(ds[k])
+        elif p.model == "boussinesq":
+            # equations.py:29-35
+            addvortexforce(p, m, s["U.x"], s["U.y"], s["omega"], ds["u.x"],
+                           ds["u.y"], sq)
+            addgrad(m, s["ke"], ds["u.x"], ds["u.y"])
+            addbuoyancy(m, s["b"], ds["u.y"])
+            divflux(p, m, s["flx.x"], s["flx.y"], s["b"], s["U.x"], s["U.y"],
+                    ds["b"], sq)
+            for k in ("u.x", "u.y", "b"):
+                m.fill(ds[k])
 
     def diag(self, s=None):
         s = self.s if s is None else s
@@ -512,8 +528,9 @@ class Model:
                 s["work"] -= m.f
             m.qg_helmholtz.solve(s["work"], s["psi"])
             perpgrad(m, s["psi"], s["U.x"], s["U.y"], contravariant=True)
-        elif p.model == "euler":
-            # equations.py:17-22
+        elif p.model in ("euler", "boussinesq"):
+            # equations.py:17-22; the boussinesq diag (37-43) is the same:
+            # its fill(s.u) passes no mesh and fills nothing
             pressure_projection(m, s["U.x"], s["U.y"], s["div"], s["p"],
                                 s["u.x"], s["u.y"])
             sharp(m, s["u.x"], s["u.y"], s["U.x"], s["U.y"])

@@ -271,6 +271,18 @@ def euler_cases():
     run_model(c, 4, "model_euler_periodic.npz", cfl=0.5)
 
 
+def boussinesq_cases():
+    """The boussinesq model (equations.py:27-44): euler + buoyancy force
+    (operators.py:152-153) + the flux divergence of the buoyancy b."""
+    c = wl.boussinesq_case(n=40, ny=32, seed=8, nislands=2)
+    run_model(c, 4, "model_boussinesq.npz", cfl=0.5)
+    c = wl.boussinesq_case(n=40, ny=32, seed=9, nislands=1, xperiodic=True)
+    run_model(c, 4, "model_boussinesq_periodic.npz", cfl=0.5)
+    c = wl.boussinesq_case(n=40, ny=32, seed=10, nislands=2)
+    run_model(c, 4, "model_boussinesq_lfra.npz", cfl=0.4,
+              extra={"integrator": "LFRA"})
+
+
 def integrator_cases():
     """The reference's other Runge-Kutta integrators (integrators.py:116-155)."""
     c = wl.eulerpsi_case(n=40, ny=32, seed=2, nislands=2, nvortices=5,
@@ -302,9 +314,11 @@ def lfra_cases():
 
 if __name__ == "__main__":
     which = sys.argv[1:] or ["mesh", "sweeps", "poisson", "models", "integrators",
-                             "euler"]
+                             "euler", "boussinesq"]
     if "lfra" in which:
         lfra_cases()
+    if "boussinesq" in which:
+        boussinesq_cases()
     if "mesh" in which:
         mesh_cases()
     if "sweeps" in which:

@@ -129,7 +129,8 @@ MODEL_FILES = ["model_eulerpsi.npz", "model_eulerpsi_islands.npz",
                "model_eulerpsi_enrk3.npz", "model_rsw_enrk3.npz",
                "model_euler.npz", "model_euler_periodic.npz",
                "model_eulerpsi_lfra.npz", "model_qg_lfra.npz", "model_rsw_lfra.npz",
-               "model_euler_lfra_periodic.npz"]
+               "model_euler_lfra_periodic.npz", "model_boussinesq.npz",
+               "model_boussinesq_periodic.npz", "model_boussinesq_lfra.npz"]
 
 
 def model_from_golden(g):
@@ -137,6 +138,7 @@ def model_from_golden(g):
     Lx, Ly, f0, beta, gg, H, cfl = (float(v) for v in g["scalars"])
     names = {k[3:] for k in g.files if k.startswith("ic/")}
     kind = ("eulerpsi" if "omega" in names else "rsw" if "h" in names else
+            "boussinesq" if "b" in names else
             "euler" if "u.x" in names else "qg")
     integ = str(g["integrator"]) if "integrator" in g.files else "rk3"
     gam = float(g["RAgamma"]) if "RAgamma" in g.files else 0.1
@@ -222,10 +224,12 @@ def _oracle_like(case, kind, **extra):
     return om
 
 
-@pytest.mark.parametrize("kind", ["eulerpsi", "rsw", "qg", "euler"])
+@pytest.mark.parametrize("kind", ["eulerpsi", "rsw", "qg", "euler", "boussinesq"])
 def test_model_vs_oracle_larger(kind):
     if kind == "euler":
         case = wl.euler_case(n=128, ny=96, seed=5, nislands=3)
+    elif kind == "boussinesq":
+        case = wl.boussinesq_case(n=128, ny=96, seed=5, nislands=3)
     elif kind == "eulerpsi":
         case = wl.eulerpsi_case(n=128, ny=96, seed=5, nislands=3)
     elif kind == "rsw":
@@ -257,7 +261,7 @@ def test_model_vs_oracle_larger(kind):
     m.sync()
 
 
-@pytest.mark.parametrize("kind", ["eulerpsi", "rsw"])
+@pytest.mark.parametrize("kind", ["eulerpsi", "rsw", "boussinesq"])
 @pytest.mark.parametrize("method", ["upwind", "centered", "cweno"])
 def test_model_flux_methods_vs_oracle(kind, method):
     """The fused stage kernels with the reference's other flux methods
@@ -265,6 +269,9 @@ def test_model_flux_methods_vs_oracle(kind, method):
     if kind == "eulerpsi":
         case = wl.eulerpsi_case(n=64, ny=48, seed=15, nislands=2)
         extra = dict(compflux=method)
+    elif kind == "boussinesq":
+        case = wl.boussinesq_case(n=64, ny=48, seed=17, nislands=2)
+        extra = dict(compflux=method, vortexforce=method, innerproduct=method)
     else:
         case = wl.rsw_case(n=64, ny=48, seed=16, nislands=2)
         extra = dict(compflux=method, vortexforce=method, innerproduct=method)
@@ -288,6 +295,37 @@ def test_model_flux_methods_vs_oracle(kind, method):
 
 
 # --------------------------------------------- size-independent checks ----
+def test_boussinesq_buoyancy_conservation_full_size():
+    """Closed basin with islands at 512^2: the flux-form buoyancy equation
+    conserves the total buoyancy (sum over the fluid cells) to round-off,
+    and the projected velocity stays divergence-free."""
+    case = wl.boussinesq_case(n=512, seed=23, nislands=4)
+    m = _model("boussinesq", 512, 512, case["msk"], cfl=0.5, tend=1e300,
+               maxite=10 ** 9)
+    s = m.state
+    for k, v in case["fields"].items():
+        if "." in k:
+            getattr(getattr(s, k.split(".")[0]), k.split(".")[1])[:] = v
+        else:
+            getattr(s, k)[:] = v
+    m.integrator.diag(s)
+    fl = m.mesh.msk > 0
+    b0 = float(np.sum(m.state.b[fl]))
+    babs = float(np.sum(np.abs(m.state.b[fl])))
+    m.advance(10)
+    m.sync()
+    s = m.state
+    assert abs(float(np.sum(s.b[fl])) - b0) <= 1e-12 * babs
+    Ux, Uy = s.U.x, s.U.y
+    d = np.zeros_like(Ux)
+    d[:, :-1] = -np.diff(Ux, axis=1)
+    d[:-1, :] -= np.diff(Uy, axis=0)
+    scale = np.abs(Ux).max() + np.abs(Uy).max()
+    assert np.abs(d[fl]).max() <= 1e-9 * scale
+    # buoyancy did work: the state moved
+    assert rel_l2(s.b, case["fields"]["b"]) > 1e-4
+
+
 @pytest.mark.parametrize("xper", [False, True])
 def test_euler_projection_divergence_free(xper):
     """After the pressure projection the discrete divergence of U vanishes at

@@ -107,7 +107,8 @@ MODEL_FILES = ["model_eulerpsi.npz", "model_eulerpsi_islands.npz",
                "model_eulerpsi_enrk3.npz", "model_rsw_enrk3.npz",
                "model_euler.npz", "model_euler_periodic.npz",
                "model_eulerpsi_lfra.npz", "model_qg_lfra.npz", "model_rsw_lfra.npz",
-               "model_euler_lfra_periodic.npz"]
+               "model_euler_lfra_periodic.npz", "model_boussinesq.npz",
+               "model_boussinesq_periodic.npz", "model_boussinesq_lfra.npz"]
 
 
 def oracle_from_golden(g, pysq=True):
@@ -116,7 +117,8 @@ def oracle_from_golden(g, pysq=True):
     model = [k for k in g.files if k.startswith("ic/")]
     names = {k[3:] for k in model}
     kind = ("eulerpsi" if "omega" in names else
-            "rsw" if "h" in names else "euler" if "u.x" in names else "qg")
+            "rsw" if "h" in names else "boussinesq" if "b" in names else
+            "euler" if "u.x" in names else "qg")
     integ = str(g["integrator"]) if "integrator" in g.files else "rk3"
     gam = float(g["RAgamma"]) if "RAgamma" in g.files else 0.1
     p = O.Param(model=kind, nx=nx, ny=ny, xperiodic=bool(xper), Lx=Lx, Ly=Ly,
