@@ -42,7 +42,8 @@ class Params(ctypes.Structure):
         ("poisson_tol", c_dbl), ("poisson_maxit", c_int),
         ("integrator", c_int),
         ("ragamma", c_dbl),
-        ("reserved", c_int * 4),
+        ("tracer", c_int),
+        ("reserved", c_int * 3),
     ]
 
 
@@ -181,6 +182,8 @@ def params_struct(p):
     s.poisson_maxit = int(getattr(p, "poisson_maxit", 200))
     s.integrator = INTEGRATORS[getattr(p, "integrator", "rk3")]
     s.ragamma = float(getattr(p, "RAgamma", 0.1))
+    tr = getattr(p, "tracer", None)
+    s.tracer = 0 if tr is None or tr == "None" else 1
     return s
 
 

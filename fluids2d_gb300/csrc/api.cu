@@ -184,7 +184,7 @@ static int field_es(f2d_model_s* m, const char* name)
 }
 
 // TMA tile map of a stencil-state buffer (element size of the state)
-static int make_tmap(f2d_model_s* m, void* buf)
+static int make_tmap(f2d_model_s* m, void* buf, bool flux_tile = false)
 {
     if (m->tmaps.count(buf)) return 0;
     auto fn = encode_fn();
@@ -192,9 +192,11 @@ static int make_tmap(f2d_model_s* m, void* buf)
     CUtensorMap map;
     cuuint64_t dims[2] = {(cuuint64_t)m->g.NX, (cuuint64_t)m->g.NY};
     cuuint64_t strides[1] = {(cuuint64_t)(m->g.P * m->es)};
-    // tile + halo: SW x FSH for the flux-form stage, SW x SH for rsw
+    // tile + halo: SW x FSH for the flux-form stage (and the tracer of any
+    // model), SW x SH for the momentum kernel of rsw, euler and boussinesq
     cuuint32_t box[2] = {(cuuint32_t)SW,
-                         (cuuint32_t)(m->p.model == F2D_MODEL_RSW || projected(m->p.model)
+                         (cuuint32_t)(!flux_tile && (m->p.model == F2D_MODEL_RSW ||
+                                                     projected(m->p.model))
                                           ? SH
                                           : FSH)};
     cuuint32_t estr[2] = {1, 1};
@@ -458,6 +460,19 @@ static int launch_stage_kernel(f2d_model_s* m, int k, int par, cudaStream_t s)
                                   m->sc, s));
     }
     m->rec_launches += 1;
+    if (m->p.tracer) {
+        // the passive tracer equation appended to the model's right-hand side
+        // (addtracerequation, equations.py:217-226): divflux of the tracer
+        // with the stage input's U, same integrator coefficients
+        void* qin = fb(m, "tracer", par);
+        CKI(make_tmap(m, qin, true));
+        CKI(launch_fluxform_stage(m->p.compflux, m->prec, tmap(m, qin), qin,
+                                  fb(m, "tracer", out), fb(m, "U.x"), fb(m, "U.y"), m->d_code,
+                                  lf ? ds("tracer", 2 - par) : k < 3 ? ds("tracer", k) : nullptr,
+                                  ds("tracer", lf ? 1 + par : 1), ds("tracer", 2),
+                                  k | (m->p.integrator << 4), g, m->sc, s));
+        m->rec_launches += 1;
+    }
     return 0;
 }
 
@@ -819,6 +834,11 @@ int f2d_model_create(const f2d_params* p, const int8_t* msk, f2d_model* out)
         fl = {{"pv", true}, {"U.x", false}, {"U.y", false}, {"h", false}, {"flx.x", false},
               {"flx.y", false}, {"work", false}, {"psi", false}};
         prog = {"pv"};
+    }
+    if (p->tracer) {
+        // states.py:31-34: the tracer is the last prognostic variable
+        fl.push_back({"tracer", true});
+        prog.push_back("tracer");
     }
     // the Poisson solution and right-hand side are FP64 in both forms; the
     // stencil state has the model's precision
@@ -1227,6 +1247,7 @@ static int adj_check(f2d_model m)
     if (m->p.compflux != F2D_METHOD_WENO && m->p.compflux != F2D_METHOD_UPWIND)
         return fail(1, "the adjoint covers the weno and upwind flux methods");
     if (m->p.integrator != F2D_INTEG_RK3) return fail(1, "the adjoint covers SSP-RK3");
+    if (m->p.tracer) return fail(1, "the adjoint covers the eulerpsi model without a tracer");
     return 0;
 }
 

@@ -402,6 +402,7 @@ int f2d_ensemble_create(const f2d_params* p, int count, const int* nxs, const in
         return f2d_internal_fail(1, "bad ensemble arguments");
     if (p->model != F2D_MODEL_EULERPSI && p->model != F2D_MODEL_QG)
         return f2d_internal_fail(1, "ensembles run the eulerpsi and qg models");
+    if (p->tracer) return f2d_internal_fail(1, "ensembles carry no tracer equation");
     if (p->integrator < F2D_INTEG_RK3 || p->integrator > F2D_INTEG_LFRA)
         return f2d_internal_fail(1, "unknown integrator (rk3, ef, enrk3, LFRA)");
     if (p->dt > 0)

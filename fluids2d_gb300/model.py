@@ -34,8 +34,23 @@ VECTORS = ("u", "U", "flx", "v")
 Vector = namedtuple("vector", ("x", "y"))
 
 
-def _allocate_state(model, shape):
-    names, _ = MODEL_SPECS[model]
+def has_tracer(param):
+    tr = getattr(param, "tracer", None)
+    return tr is not None and tr != "None"
+
+
+def _specs(param):
+    """states.py:22-34: with a tracer, the variables are the prognostic ones,
+    the tracer, then the rest."""
+    names, prog = MODEL_SPECS[param.model]
+    if has_tracer(param):
+        prog = prog + (param.tracer,)
+        names = prog + names[len(prog) - 1:]
+    return names, prog
+
+
+def _allocate_state(param, shape):
+    names, _ = _specs(param)
     State = namedtuple("state", names)
     content = {}
     for n in names:
@@ -46,8 +61,9 @@ def _allocate_state(model, shape):
     return State(**content)
 
 
-def _flat_fields(state):
-    """(device name, host array) pairs: vector fields become 'U.x', 'U.y'."""
+def _flat_fields(state, tracer=None):
+    """(device name, host array) pairs: vector fields become 'U.x', 'U.y';
+    the tracer (named by param.tracer) is the device field 'tracer'."""
     out = []
     for name in state._fields:
         v = getattr(state, name)
@@ -55,7 +71,7 @@ def _flat_fields(state):
             out.append((name + ".x", v.x))
             out.append((name + ".y", v.y))
         else:
-            out.append((name, v))
+            out.append(("tracer" if name == tracer else name, v))
     return out
 
 
@@ -248,7 +264,8 @@ class Model:
         check(lib().f2d_model_create(ctypes.byref(s), None, ctypes.byref(h)))
         self._h = h
         self.mesh = Mesh(self)
-        self._state = _allocate_state(param.model, self.mesh.shape)
+        self._state = _allocate_state(param, self.mesh.shape)
+        self._tracer = param.tracer if has_tracer(param) else None
         self._host_dirty = False
         self._device_newer = False
         self.integrator = Integrator(self)
@@ -276,7 +293,7 @@ class Model:
     def _pull(self):
         if not self._device_newer:
             return
-        for name, arr in _flat_fields(self._state):
+        for name, arr in _flat_fields(self._state, self._tracer):
             if name.startswith("flx"):
                 continue
             check(lib().f2d_field_get(self._h, name.encode(), ptr(arr)))
@@ -285,7 +302,7 @@ class Model:
     def _push(self):
         if not self._host_dirty:
             return
-        for name, arr in _flat_fields(self._state):
+        for name, arr in _flat_fields(self._state, self._tracer):
             if name.startswith("flx"):
                 continue
             a = np.ascontiguousarray(arr, dtype=np.float64)

@@ -15,6 +15,14 @@ _integrators = ["rk3", "ef", "enrk3", "LFRA"]
 
 # models and integrators the GPU path implements
 SUPPORTED_MODELS = ("eulerpsi", "rsw", "qg", "euler", "boussinesq")
+# the state variables of those models (states.py:7-17)
+MODEL_VARIABLES = {
+    "eulerpsi": ("omega", "U", "psi", "vomega", "flx"),
+    "euler": ("u", "U", "omega", "ke", "p", "div", "flx"),
+    "boussinesq": ("b", "u", "U", "omega", "ke", "p", "div", "flx"),
+    "rsw": ("u", "h", "U", "omega", "ke", "p", "flx", "pv"),
+    "qg": ("pv", "U", "h", "flx", "work", "psi"),
+}
 SUPPORTED_INTEGRATORS = ("rk3", "ef", "enrk3", "LFRA")
 EXTRA = ("precision", "poisson_tol", "poisson_maxit")
 
@@ -93,7 +101,10 @@ class Param:
                 f"integrator {self.integrator!r}: the GPU path implements "
                 f"{', '.join(SUPPORTED_INTEGRATORS)}")
         if self.tracer not in (None, "None"):
-            raise NotImplementedError("tracer equations are not implemented")
+            names = MODEL_VARIABLES.get(self.model, ())
+            if not isinstance(self.tracer, str) or self.tracer in names:
+                raise ValueError(f"tracer name {self.tracer!r} must be a new "
+                                 "state variable name")
         if self.halowidth != 3:
             raise NotImplementedError("halowidth must be 3")
         if self.yperiodic:

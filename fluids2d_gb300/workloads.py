@@ -131,8 +131,9 @@ def eulerpsi_case(n=256, seed=0, nislands=0, nvortices=8, radius=0.05,
 
 
 def rsw_case(n=512, seed=0, nislands=3, ny=None, Lx=1.0, Ly=1.0,
-             f0=1.0, g=1.0, H=1.0):
-    """Rotating shallow water in an x-periodic channel with islands.
+             f0=1.0, g=1.0, H=1.0, xperiodic=True):
+    """Rotating shallow water in an x-periodic channel (or a closed basin)
+    with islands.
 
     h = (H + 0.1*Gaussian bump of radius 0.1 L + N(0, 1e-3)) * msk * area,
     u = 0.
@@ -140,7 +141,7 @@ def rsw_case(n=512, seed=0, nislands=3, ny=None, Lx=1.0, Ly=1.0,
     nx = n
     ny = n if ny is None else ny
     x, y = grid_coords(nx, ny, Lx, Ly, which="c")
-    msk = default_mask(nx, ny, xperiodic=True)
+    msk = default_mask(nx, ny, xperiodic=xperiodic)
     carve_islands(msk, x, y, nislands, 0.03 * Lx, 0.08 * Lx, seed + 1000,
                   Lx, Ly, margin=0.1 * Lx)
     rng = np.random.default_rng(seed)
@@ -148,12 +149,37 @@ def rsw_case(n=512, seed=0, nislands=3, ny=None, Lx=1.0, Ly=1.0,
     r0 = 0.1 * Lx
     bump = np.exp(-((x - 0.5 * Lx) ** 2 + (y - 0.5 * Ly) ** 2) / (2 * r0 ** 2))
     h = (H + 0.1 * bump + rng.normal(0.0, 1e-3, size=x.shape)) * msk * area
-    # periodic halo columns hold copies of the interior (the halo fill)
-    hw = 3
-    h[:, :hw] = h[:, -2 * hw:-hw]
-    h[:, -hw:] = h[:, hw:2 * hw]
+    if xperiodic:
+        # periodic halo columns hold copies of the interior (the halo fill)
+        hw = 3
+        h[:, :hw] = h[:, -2 * hw:-hw]
+        h[:, -hw:] = h[:, hw:2 * hw]
     return dict(model="rsw", nx=nx, ny=ny, Lx=Lx, Ly=Ly, msk=msk,
-                xperiodic=True, f0=f0, g=g, H=H, fields={"h": h})
+                xperiodic=xperiodic, f0=f0, g=g, H=H, fields={"h": h})
+
+
+def add_tracer(case, name="q", seed=0, nblobs=3):
+    """A passive tracer field `name` (param.tracer) on top of a case: a sum
+    of Gaussian blobs plus a smooth gradient, masked by msk, with the
+    x-periodic halo fill where the case is x-periodic."""
+    nx, ny, Lx, Ly = case["nx"], case["ny"], case["Lx"], case["Ly"]
+    x, y = grid_coords(nx, ny, Lx, Ly, which="c")
+    rng = np.random.default_rng(seed + 77)
+    q = 0.5 * (x / Lx)
+    for _ in range(nblobs):
+        x0, y0 = rng.uniform(0.2, 0.8) * Lx, rng.uniform(0.2, 0.8) * Ly
+        r0 = rng.uniform(0.05, 0.12) * Lx
+        q = q + np.exp(-((x - x0) ** 2 + (y - y0) ** 2) / r0 ** 2)
+    q = q * case["msk"]
+    if case.get("xperiodic"):
+        hw = 3
+        q[:, :hw] = q[:, -2 * hw:-hw]
+        q[:, -hw:] = q[:, hw:2 * hw]
+    out = dict(case)
+    out["fields"] = dict(case["fields"])
+    out["fields"][name] = q
+    out["tracer"] = name
+    return out
 
 
 def qg_case(n=4096, seed=0, nislands=20, ny=None, Lx=1.0, Ly=1.0,

@@ -58,7 +58,9 @@ typedef struct f2d_params {
     int poisson_maxit;
     int integrator;     /* F2D_INTEG_* */
     double ragamma;     /* Robert-Asselin coefficient of LFRA (param.py:50) */
-    int reserved[4];
+    int tracer;         /* 1: a passive tracer field "tracer" (param.py:57,
+                           equations.py:217-226) */
+    int reserved[3];
 } f2d_params;
 
 typedef struct f2d_model_s *f2d_model;

@@ -123,6 +123,7 @@ class Param:
         self.dtmax = 9e99
         self.integrator = "rk3"
         self.RAgamma = 0.1
+        self.tracer = None
         self.cfl = 0.9
         self.compflux = "weno"
         self.vortexforce = "weno"
@@ -463,9 +464,15 @@ class Model:
             self.mesh.msk[:] = msk
             self.mesh.finalize()
         shape = self.mesh.shape
+        tr = getattr(param, "tracer", None)
+        self.tracer = None if tr in (None, "None") else tr
         self.s = _alloc(STATE_VARS[param.model], shape)
         self.prog = [k for k in self.s
                      if k.split(".")[0] in PROGNOSTIC[param.model]]
+        if self.tracer:
+            # states.py:31-34: the tracer is the last prognostic variable
+            self.s[self.tracer] = np.zeros(shape)
+            self.prog.append(self.tracer)
         self.scratch = [{k: np.zeros(shape) for k in self.prog}
                         for _ in range(3)]
         self.t = 0.0
@@ -511,6 +518,11 @@ class Model:
                     ds["b"], sq)
             for k in ("u.x", "u.y", "b"):
                 m.fill(ds[k])
+
+        if self.tracer:
+            # addtracerequation (equations.py:217-226): no halo fill
+            divflux(p, m, s["flx.x"], s["flx.y"], s[self.tracer], s["U.x"],
+                    s["U.y"], ds[self.tracer], sq)
 
     def diag(self, s=None):
         s = self.s if s is None else s

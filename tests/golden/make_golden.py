@@ -215,6 +215,8 @@ def run_model(case, nsteps, fname, cfl=None, extra=None):
         out["integrator"] = np.array(extra["integrator"])
     if extra and "RAgamma" in extra:
         out["RAgamma"] = np.array(float(extra["RAgamma"]))
+    if extra and "tracer" in extra:
+        out["tracer"] = np.array(extra["tracer"])
     for k, v in case["fields"].items():
         out["ic/" + k] = v.copy()
 
@@ -283,6 +285,26 @@ def boussinesq_cases():
               extra={"integrator": "LFRA"})
 
 
+def tracer_cases():
+    """A passive tracer appended to each model's equations
+    (addtracerequation, equations.py:217-226) in closed basins (the
+    reference does not fill the tracer tendency's x-periodic halo)."""
+    c = wl.add_tracer(wl.eulerpsi_case(n=40, ny=32, seed=2, nislands=2,
+                                       nvortices=5, radius=0.08), seed=1)
+    run_model(c, 4, "model_eulerpsi_tracer.npz", cfl=0.8, extra={"tracer": "q"})
+    c = wl.add_tracer(wl.qg_case(n=40, ny=32, seed=4, nislands=3, kmin=2,
+                                 kmax=8), name="c", seed=2)
+    run_model(c, 4, "model_qg_tracer_lfra.npz", cfl=0.4,
+              extra={"tracer": "c", "integrator": "LFRA"})
+    c = wl.add_tracer(wl.rsw_case(n=40, ny=32, seed=3, nislands=2,
+                                  xperiodic=False), seed=3)
+    run_model(c, 4, "model_rsw_tracer.npz", extra={"tracer": "q"})
+    c = wl.add_tracer(wl.boussinesq_case(n=40, ny=32, seed=8, nislands=2),
+                      name="s", seed=4)
+    run_model(c, 4, "model_boussinesq_tracer.npz", cfl=0.5,
+              extra={"tracer": "s"})
+
+
 def integrator_cases():
     """The reference's other Runge-Kutta integrators (integrators.py:116-155)."""
     c = wl.eulerpsi_case(n=40, ny=32, seed=2, nislands=2, nvortices=5,
@@ -314,11 +336,13 @@ def lfra_cases():
 
 if __name__ == "__main__":
     which = sys.argv[1:] or ["mesh", "sweeps", "poisson", "models", "integrators",
-                             "euler", "boussinesq"]
+                             "euler", "boussinesq", "tracer"]
     if "lfra" in which:
         lfra_cases()
     if "boussinesq" in which:
         boussinesq_cases()
+    if "tracer" in which:
+        tracer_cases()
     if "mesh" in which:
         mesh_cases()
     if "sweeps" in which:

@@ -130,7 +130,9 @@ MODEL_FILES = ["model_eulerpsi.npz", "model_eulerpsi_islands.npz",
                "model_euler.npz", "model_euler_periodic.npz",
                "model_eulerpsi_lfra.npz", "model_qg_lfra.npz", "model_rsw_lfra.npz",
                "model_euler_lfra_periodic.npz", "model_boussinesq.npz",
-               "model_boussinesq_periodic.npz", "model_boussinesq_lfra.npz"]
+               "model_boussinesq_periodic.npz", "model_boussinesq_lfra.npz",
+               "model_eulerpsi_tracer.npz", "model_qg_tracer_lfra.npz",
+               "model_rsw_tracer.npz", "model_boussinesq_tracer.npz"]
 
 
 def model_from_golden(g):
@@ -142,9 +144,10 @@ def model_from_golden(g):
             "euler" if "u.x" in names else "qg")
     integ = str(g["integrator"]) if "integrator" in g.files else "rk3"
     gam = float(g["RAgamma"]) if "RAgamma" in g.files else 0.1
+    tracer = str(g["tracer"]) if "tracer" in g.files else None
     m = _model(kind, nx, ny, g["msk"], xperiodic=bool(xper), Lx=Lx, Ly=Ly, f0=f0,
                beta=beta, g=gg, H=H, cfl=cfl, tend=1e300, maxite=10 ** 9,
-               integrator=integ, RAgamma=gam)
+               integrator=integ, RAgamma=gam, tracer=tracer)
     if "f" in g.files:
         m.mesh.f = g["f"]
     s = m.state
@@ -298,6 +301,35 @@ def test_model_flux_methods_vs_oracle(kind, method):
 
 
 # --------------------------------------------- size-independent checks ----
+def test_tracer_constant_and_conserved_periodic():
+    """x-periodic boussinesq channel at 256^2 with a passive tracer: a tracer
+    that is 1 on every fluid cell stays 1 under the divergence-free flow (to
+    the projection's tolerance), and its total over the fluid cells is
+    conserved to round-off."""
+    case = wl.boussinesq_case(n=256, seed=24, nislands=3, xperiodic=True)
+    m = _model("boussinesq", 256, 256, case["msk"], xperiodic=True, cfl=0.5,
+               tend=1e300, maxite=10 ** 9, tracer="q")
+    s = m.state
+    for k, v in case["fields"].items():
+        if "." in k:
+            getattr(getattr(s, k.split(".")[0]), k.split(".")[1])[:] = v
+        else:
+            getattr(s, k)[:] = v
+    s.q[:] = case["msk"].astype(np.float64)
+    m.integrator.diag(s)
+    fl = m.mesh.msk > 0
+    fl[:, :3] = False
+    fl[:, -3:] = False
+    q0 = float(np.sum(m.state.q[fl]))
+    m.advance(8)
+    m.sync()
+    q = m.state.q
+    assert np.abs(q[fl] - 1.0).max() <= 1e-8
+    assert abs(float(np.sum(q[fl])) - q0) <= 1e-12 * q0
+    # the flow moved (the buoyancy field changed)
+    assert rel_l2(m.state.b, case["fields"]["b"]) > 1e-4
+
+
 def test_boussinesq_buoyancy_conservation_full_size():
     """Closed basin with islands at 512^2: the flux-form buoyancy equation
     conserves the total buoyancy (sum over the fluid cells) to round-off,

@@ -108,7 +108,9 @@ MODEL_FILES = ["model_eulerpsi.npz", "model_eulerpsi_islands.npz",
                "model_euler.npz", "model_euler_periodic.npz",
                "model_eulerpsi_lfra.npz", "model_qg_lfra.npz", "model_rsw_lfra.npz",
                "model_euler_lfra_periodic.npz", "model_boussinesq.npz",
-               "model_boussinesq_periodic.npz", "model_boussinesq_lfra.npz"]
+               "model_boussinesq_periodic.npz", "model_boussinesq_lfra.npz",
+               "model_eulerpsi_tracer.npz", "model_qg_tracer_lfra.npz",
+               "model_rsw_tracer.npz", "model_boussinesq_tracer.npz"]
 
 
 def oracle_from_golden(g, pysq=True):
@@ -121,9 +123,10 @@ def oracle_from_golden(g, pysq=True):
             "euler" if "u.x" in names else "qg")
     integ = str(g["integrator"]) if "integrator" in g.files else "rk3"
     gam = float(g["RAgamma"]) if "RAgamma" in g.files else 0.1
+    tracer = str(g["tracer"]) if "tracer" in g.files else None
     p = O.Param(model=kind, nx=nx, ny=ny, xperiodic=bool(xper), Lx=Lx, Ly=Ly,
                 f0=f0, beta=beta, g=gg, H=H, cfl=cfl, tend=1e9,
-                maxite=10 ** 9, integrator=integ, RAgamma=gam)
+                maxite=10 ** 9, integrator=integ, RAgamma=gam, tracer=tracer)
     m = O.Model(p, msk=g["msk"], pysq=pysq)
     if "f" in g.files:
         m.mesh.f = g["f"].copy()
