@@ -68,6 +68,11 @@ WORKLOADS = {
                       "basin, 3 islands, stratification + 2 bubbles, WENO5, "
                       "SSP-RK3, cfl 0.5, FP64, Neumann multigrid-PCG pressure "
                       "projection"),
+    "qgrsw512": ("qgrsw", dict(n=512, seed=0, nislands=3, xperiodic=False, f0=10.0),
+                 "qgrsw 512x512 closed basin, 3 islands, f0=10, g=H=1, WENO5, "
+                 "SSP-RK3, cfl 0.5, FP64, RSW tendency projected on the QG "
+                 "manifold by an MG-PCG Helmholtz solve every stage; initial "
+                 "state = qg_projection of a thickness bump"),
     "rsw1024": ("rsw", dict(n=1024, seed=0, nislands=3),
                 "rsw 1024x1024 x-periodic channel, 3 islands, FP64 (profiling "
                 "size: working set above the L2)"),
@@ -143,6 +148,11 @@ def build_case(name):
         desc = desc.replace("FP64", "FP32 stencils + FP32 multigrid, FP64 CG")
     if model == "rsw":
         case = wl.rsw_case(**kw)
+    elif model == "qgrsw":
+        case = wl.rsw_case(**kw)
+        z = np.zeros_like(case["fields"]["h"])
+        case["model"] = "qgrsw"
+        case["fields"] = {"u.x": z, "u.y": z.copy(), "h": case["fields"]["h"]}
     elif model == "euler":
         case = wl.euler_case(**kw)
     elif model == "boussinesq":
@@ -167,7 +177,7 @@ def make_gpu_model(model, case, stream_ptr, precision="fp64", tol=None):
             setattr(p, k, case[k])
     if model == "eulerpsi":
         p.cfl = 0.8
-    if model in ("euler", "boussinesq"):
+    if model in ("euler", "boussinesq", "qgrsw"):
         p.cfl = 0.5
     p.tend = 1e300
     p.maxite = 10 ** 12
@@ -186,14 +196,16 @@ def make_gpu_model(model, case, stream_ptr, precision="fp64", tol=None):
             getattr(getattr(s, k.split(".")[0]), k.split(".")[1])[:] = v
         else:
             getattr(s, k)[:] = v
-    m.integrator.diag(s)
+    if model == "qgrsw":
+        m.qg_projection()  # the initial state on the QG manifold
+    m.integrator.diag(m.state)
     return m
 
 
 def prognostic_names(model):
     return {"rsw": ["u.x", "u.y", "h"], "eulerpsi": ["omega"],
             "qg": ["pv"], "euler": ["u.x", "u.y"],
-            "boussinesq": ["b", "u.x", "u.y"]}[model]
+            "boussinesq": ["b", "u.x", "u.y"], "qgrsw": ["u.x", "u.y", "h"]}[model]
 
 
 # algorithmic bytes per array point of the stage-2 launch of the fused stage
@@ -207,6 +219,9 @@ STAGE2_BYTES = {
     "euler": 8 * 8 + 4 + 4 * 8,
     # boussinesq: euler + b and its ds1 read, b and its ds2 written
     "boussinesq": 10 * 8 + 4 + 6 * 8,
+    # qgrsw (momentum kernel in tendency mode): read h, omega, U.x, U.y
+    # (4 x 8) + code; write the raw du.x, du.y, dh (3 x 8)
+    "qgrsw": 4 * 8 + 4 + 3 * 8,
     # flux form: read q,U.x,U.y,ds1 (4 x 8) + code (4); write q, ds2 (2 x 8)
     "eulerpsi": 4 * 8 + 4 + 2 * 8,
     "qg": 4 * 8 + 4 + 2 * 8,
@@ -307,13 +322,16 @@ def cpu_oracle_rate(model, case, budget_s, max_steps=None, warmup=1):
             setattr(p, k, case[k])
     if model == "eulerpsi":
         p.cfl = 0.8
-    if model in ("euler", "boussinesq"):
+    if model in ("euler", "boussinesq", "qgrsw"):
         p.cfl = 0.5
     om = O.Model(p, msk=case["msk"], pysq=False)
     if "f" in case:
         om.mesh.f = case["f"].copy()
     for k, v in case["fields"].items():
         om.s[k][:] = v
+    if model == "qgrsw":
+        s = om.s
+        O.qg_projection(om.mesh, s["u.x"], s["u.y"], s["h"], s["pv"], s["psi"])
     om.diag()
     om.run_steps(warmup)
     n = 0
@@ -816,7 +834,7 @@ def run_gpu(args, rank, world):
         peak, peak_src = 6800.0, "fallback"
     kname = {"rsw": "k_rsw_stage", "eulerpsi": "k_fluxform_stage",
              "qg": "k_fluxform_stage", "euler": "k_rsw_stage",
-             "boussinesq": "k_rsw_stage"}[model]
+             "boussinesq": "k_rsw_stage", "qgrsw": "k_rsw_stage"}[model]
     traffic = read_profile_traffic(f"{kname}_{args.workload}")
     fp64_pct = read_profile_value(f"{kname}_{args.workload}", "fp64_pipe_pct")
 

@@ -18,7 +18,7 @@ c_i64 = ctypes.c_int64
 c_dbl = ctypes.c_double
 c_void_p = ctypes.c_void_p
 
-MODELS = {"eulerpsi": 0, "rsw": 1, "qg": 2, "euler": 3, "boussinesq": 4}
+MODELS = {"eulerpsi": 0, "rsw": 1, "qg": 2, "euler": 3, "boussinesq": 4, "qgrsw": 5}
 METHODS = {"weno": 0, "upwind": 1, "centered": 2, "cweno": 3}
 PRECISIONS = {"fp64": 0, "fp32": 1}
 INTEGRATORS = {"rk3": 0, "ef": 1, "enrk3": 2, "LFRA": 3}
@@ -76,6 +76,7 @@ _SIGS = {
     "f2d_field_names": ([c_void_p, ctypes.c_char_p, ctypes.c_size_t], c_int),
     "f2d_set_coriolis": ([c_void_p, c_void_p], c_int),
     "f2d_diag": ([c_void_p], c_int),
+    "f2d_qg_projection": ([c_void_p], c_int),
     "f2d_step": ([c_void_p, c_int], c_int),
     "f2d_run": ([c_void_p, c_int], c_int),
     "f2d_set_dt": ([c_void_p], c_int),

@@ -196,6 +196,7 @@ static int make_tmap(f2d_model_s* m, void* buf, bool flux_tile = false)
     // model), SW x SH for the momentum kernel of rsw, euler and boussinesq
     cuuint32_t box[2] = {(cuuint32_t)SW,
                          (cuuint32_t)(!flux_tile && (m->p.model == F2D_MODEL_RSW ||
+                                                     m->p.model == F2D_MODEL_QGRSW ||
                                                      projected(m->p.model))
                                           ? SH
                                           : FSH)};
@@ -372,6 +373,28 @@ static int rec_diag(f2d_model_s* m, int par, cudaStream_t s)
         m->rec_launches += 2;
         return 0;
     }
+    case F2D_MODEL_QGRSW: {
+        // sharp, vorticity and its fill (equations.py:127-133)
+        RswDiag a;
+        memset(&a, 0, sizeof(a));
+        a.ux = fb(m, "u.x", par);
+        a.uy = fb(m, "u.y", par);
+        a.Ux = fb(m, "U.x");
+        a.Uy = fb(m, "U.y");
+        a.omega = fb(m, "omega");
+        a.rdx2 = m->rdx2;
+        a.rdy2 = m->rdy2;
+        a.euler = 1;
+        a.noke = 1;
+        CKI(make_tmap(m, (void*)a.ux));
+        CKI(make_tmap(m, (void*)a.uy));
+        CKI(launch_rsw_diag(m->p.innerproduct, m->prec, tmap(m, (void*)a.ux),
+                            tmap(m, (void*)a.uy), a, m->d_code, g, m->sc, s));
+        // max|U.x|, max|U.y| for set_dt (model.py:83-85)
+        CKI(launch_maxabs2(m->prec, a.Ux, a.Uy, g, m->sc, m->partials, s));
+        m->rec_launches += 2;
+        return 0;
+    }
     case F2D_MODEL_RSW: {
         RswDiag a;
         memset(&a, 0, sizeof(a));
@@ -397,9 +420,12 @@ static int rec_diag(f2d_model_s* m, int par, cudaStream_t s)
     return fail(5, "unknown model");
 }
 
+static int rec_qgrsw_stage(f2d_model_s* m, int k, int par, cudaStream_t s);
+
 // the fused right-hand-side + RK3-update kernel of stage k, parity par -> 1-par
 static int launch_stage_kernel(f2d_model_s* m, int k, int par, cudaStream_t s)
 {
+    if (m->p.model == F2D_MODEL_QGRSW) return rec_qgrsw_stage(m, k, par, s);
     const Geom& g = m->g;
     const int out = 1 - par;
     const bool lf = m->p.integrator == F2D_INTEG_LFRA;
@@ -473,6 +499,116 @@ static int launch_stage_kernel(f2d_model_s* m, int k, int par, cudaStream_t s)
                                   k | (m->p.integrator << 4), g, m->sc, s));
         m->rec_launches += 1;
     }
+    return 0;
+}
+
+// qgrsw stage (equations.py:106-125): the raw RSW tendency (vortex force,
+// Coriolis, mass flux; momentum kernel in tendency mode), the vertex PV of it
+// (vorticity + stretching), the Helmholtz solve, then the projected tendency
+// (perpgrad, thickness) and the integrator update in one pass. The raw
+// tendency lives in ds3, the projected one of stage k < 3 in ds<k> (LFRA:
+// the filtered previous state alternates between ds1 and ds2 with the
+// parity).
+static int rec_qgrsw_stage(f2d_model_s* m, int k, int par, cudaStream_t s)
+{
+    const Geom& g = m->g;
+    const int out = 1 - par;
+    const bool lf = m->p.integrator == F2D_INTEG_LFRA;
+    // the raw tendency always goes to ds3 (read by the projection pass while
+    // it writes the projected tendency of stage k < 3 into ds<k>)
+    const int kt = 3;
+    const int sk = k | (m->p.integrator << 4);
+    auto ds = [&](const char* f, int kk) -> void* {
+        return fb(m, (std::string("ds") + std::to_string(kk) + "." + f).c_str());
+    };
+    RswIn a;
+    memset(&a, 0, sizeof(a));
+    a.euler = 3;
+    a.ux = fb(m, "u.x", par);
+    a.uy = fb(m, "u.y", par);
+    a.h = fb(m, "h", par);
+    a.Ux = fb(m, "U.x");
+    a.Uy = fb(m, "U.y");
+    a.dux = ds("u.x", kt);
+    a.duy = ds("u.y", kt);
+    a.dh = ds("h", kt);
+    a.fc = m->fc;
+    void* om = fb(m, "omega");
+    CKI(make_tmap(m, (void*)a.h));
+    CKI(make_tmap(m, om));
+    CKI(launch_rsw_stage(m->p.vortexforce, m->prec, tmap(m, (void*)a.h), tmap(m, om), a,
+                         m->d_code, sk, g, m->sc, s));
+    // add_stretching's -f0/H (operators.py:199)
+    const double cs = -m->p.f0 / m->p.H;
+    CKI(launch_qgrsw_pv(m->prec, a.dux, a.duy, a.dh, (double*)fb(m, "pv"), m->d_code, cs, 0.0,
+                        g, s));
+    m->rec_launches += 2;
+    int e = rec_solve(m, 1, fb(m, "pv"), fb(m, "psi"), s);
+    if (e) return e;
+    QgProj q;
+    memset(&q, 0, sizeof(q));
+    q.ux = a.ux;
+    q.uy = a.uy;
+    q.h = a.h;
+    q.uxo = fb(m, "u.x", out);
+    q.uyo = fb(m, "u.y", out);
+    q.ho = fb(m, "h", out);
+    q.cx = a.dux;
+    q.cy = a.duy;
+    q.ch = a.dh;
+    if (!lf && k < 3) {
+        q.sx = ds("u.x", k);
+        q.sy = ds("u.y", k);
+        q.sh = ds("h", k);
+    }
+    const int k1 = lf ? 1 + par : 1;
+    q.d1x = ds("u.x", k1);
+    q.d1y = ds("u.y", k1);
+    q.d1h = ds("h", k1);
+    q.d2x = ds("u.x", 2);
+    q.d2y = ds("u.y", 2);
+    q.d2h = ds("h", 2);
+    if (lf) {
+        q.px = ds("u.x", 2 - par);
+        q.py = ds("u.y", 2 - par);
+        q.ph = ds("h", 2 - par);
+    }
+    // thickness_from_psi's f0 * area / g (operators.py:208)
+    q.c2 = m->p.f0 * m->area / m->p.g;
+    q.mode = 0;
+    q.store = !lf && k < 3;
+    CKI(launch_qgrsw_update(m->prec, q, (const double*)fb(m, "psi"), m->d_code, sk, g, m->sc,
+                            s));
+    m->rec_launches += 1;
+    return 0;
+}
+
+// qg_projection (operators.py:176-183, anomaly=False) of the state at
+// parity par in place: PV of (u, h - h0), Helmholtz solve into psi, then
+// u = perpgrad(psi), h = verticestocenters(psi f0 area / g) + h0, times msk
+static int rec_qg_projection(f2d_model_s* m, int par, cudaStream_t s)
+{
+    const Geom& g = m->g;
+    const double h0 = m->p.H * m->area;  // H * area - hb, hb = 0 (meshes.py:47)
+    void* ux = fb(m, "u.x", par);
+    void* uy = fb(m, "u.y", par);
+    void* h = fb(m, "h", par);
+    CKI(launch_qgrsw_pv(m->prec, ux, uy, h, (double*)fb(m, "pv"), m->d_code,
+                        -m->p.f0 / m->p.H, h0, g, s));
+    m->rec_launches += 1;
+    int e = rec_solve(m, 1, fb(m, "pv"), fb(m, "psi"), s);
+    if (e) return e;
+    QgProj q;
+    memset(&q, 0, sizeof(q));
+    q.cx = ux;
+    q.cy = uy;
+    q.ch = h;
+    q.c2 = m->p.f0 * m->area / m->p.g;
+    q.h0 = h0;
+    q.mode = 1;
+    CKI(launch_qgrsw_update(m->prec, q, (const double*)fb(m, "psi"), m->d_code, 1, g, m->sc,
+                            s));
+    m->rec_launches += 1;
     return 0;
 }
 
@@ -579,6 +715,7 @@ static int record_kind(f2d_model_s* m, int kind, int par, cudaStream_t s)
     case 0: return rec_diag(m, par, s);
     case 1: return rec_step(m, par, false, s);
     case 2: return rec_step(m, par, true, s);
+    case 3: return rec_qg_projection(m, par, s);
     case 5: return rec_step_snap(m, par, s);
     case 6: return rec_adj_step(m, s);
     }
@@ -587,13 +724,15 @@ static int record_kind(f2d_model_s* m, int kind, int par, cudaStream_t s)
 
 static bool flips(int kind) { return kind == 1 || kind == 2 || kind == 5; }
 
-// capture kind (0 diag, 1 step, 2 run, 5 snapshot step, 6 adjoint step) for
+// capture kind (0 diag, 1 step, 2 run, 3 qg projection of the state,
+// 5 snapshot step, 6 adjoint step) for
 // the current parity, then launch
 static int run_graph(f2d_model_s* m, int kind)
 {
     const int par = m->cur;
     if (eager_mode()) {
-        if (m->p.model == F2D_MODEL_EULERPSI || m->p.model == F2D_MODEL_QG) {
+        if (m->p.model == F2D_MODEL_EULERPSI || m->p.model == F2D_MODEL_QG ||
+            m->p.model == F2D_MODEL_QGRSW) {
             int e0 = ensure_mg(m, m->p.model == F2D_MODEL_EULERPSI ? 0 : 1);
             if (e0) return e0;
         } else if (projected(m->p.model)) {
@@ -609,7 +748,8 @@ static int run_graph(f2d_model_s* m, int kind)
     }
     if (!m->gx[kind][par]) {
         // multigrid set-up allocates, so it happens before the capture
-        if (m->p.model == F2D_MODEL_EULERPSI || m->p.model == F2D_MODEL_QG) {
+        if (m->p.model == F2D_MODEL_EULERPSI || m->p.model == F2D_MODEL_QG ||
+            m->p.model == F2D_MODEL_QGRSW) {
             int e0 = ensure_mg(m, m->p.model == F2D_MODEL_EULERPSI ? 0 : 1);
             if (e0) return e0;
         } else if (projected(m->p.model)) {
@@ -759,14 +899,15 @@ int f2d_model_create(const f2d_params* p, const int8_t* msk, f2d_model* out)
     if (!p || !out) return fail(1, "null argument");
     if (p->precision != F2D_PREC_FP64 && p->precision != F2D_PREC_FP32)
         return fail(1, "unknown precision");
-    if (p->model < 0 || p->model > 4) return fail(1, "unknown model");
+    if (p->model < 0 || p->model > 5) return fail(1, "unknown model");
     if (projected(p->model) && p->precision != F2D_PREC_FP64)
         return fail(1, "the euler and boussinesq models run in FP64");
 
     if (p->integrator < F2D_INTEG_RK3 || p->integrator > F2D_INTEG_LFRA)
         return fail(1, "unknown integrator (rk3, ef, enrk3, LFRA)");
     if (p->xperiodic && p->nx < 6) return fail(1, "x-periodic needs nx >= 6");
-    if ((p->model == F2D_MODEL_RSW || p->model == F2D_MODEL_BOUSSINESQ) &&
+    if ((p->model == F2D_MODEL_RSW || p->model == F2D_MODEL_BOUSSINESQ ||
+         p->model == F2D_MODEL_QGRSW) &&
         p->vortexforce != p->compflux)
         return fail(1, "the fused rsw/boussinesq stage uses one flux method for "
                        "vortexforce and compflux; they must be equal");
@@ -825,6 +966,11 @@ int f2d_model_create(const f2d_params* p, const int8_t* msk, f2d_model* out)
               {"omega", false}, {"ke", false}, {"p", false}, {"div", false},
               {"flx.x", false}, {"flx.y", false}};
         prog = {"b", "u.x", "u.y"};
+    } else if (p->model == F2D_MODEL_QGRSW) {
+        fl = {{"u.x", true}, {"u.y", true}, {"h", true}, {"U.x", false}, {"U.y", false},
+              {"omega", false}, {"ke", false}, {"p", false}, {"flx.x", false},
+              {"flx.y", false}, {"pv", false}, {"psi", false}};
+        prog = {"u.x", "u.y", "h"};
     } else if (p->model == F2D_MODEL_RSW) {
         fl = {{"u.x", true}, {"u.y", true}, {"h", true}, {"U.x", false}, {"U.y", false},
               {"omega", false}, {"ke", false}, {"p", false}, {"flx.x", false},
@@ -842,13 +988,17 @@ int f2d_model_create(const f2d_params* p, const int8_t* msk, f2d_model* out)
     }
     // the Poisson solution and right-hand side are FP64 in both forms; the
     // stencil state has the model's precision
-    auto is64 = [](const char* n) {
-        return !strcmp(n, "psi") || !strcmp(n, "vomega") || !strcmp(n, "work");
+    auto is64 = [&](const char* n) {
+        return !strcmp(n, "psi") || !strcmp(n, "vomega") || !strcmp(n, "work") ||
+               (p->model == F2D_MODEL_QGRSW && !strcmp(n, "pv"));
     };
     for (auto& f : fl)
         if ((e = add_field(m, f.first, f.second, is64(f.first) ? 8 : (int)m->es)))
             return bail(e);
-    for (int k = 1; k <= 2; ++k)
+    // qgrsw keeps the third stage's (or LFRA's) tendency too: it is
+    // projected between the tendency kernel and the update
+    const int nds = p->model == F2D_MODEL_QGRSW ? 3 : 2;
+    for (int k = 1; k <= nds; ++k)
         for (const char* f : prog)
             if ((e = add_field(m, (std::string("ds") + std::to_string(k) + "." + f).c_str(),
                                false, (int)m->es)))
@@ -1013,6 +1163,13 @@ int f2d_diag(f2d_model m)
 {
     if (!m) return fail(1, "null model");
     return run_graph(m, 0);
+}
+
+int f2d_qg_projection(f2d_model m)
+{
+    if (!m) return fail(1, "null model");
+    if (m->p.model != F2D_MODEL_QGRSW) return fail(1, "qg_projection acts on a qgrsw model");
+    return run_graph(m, 3);
 }
 
 int f2d_step(f2d_model m, int n)

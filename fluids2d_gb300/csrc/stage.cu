@@ -105,7 +105,10 @@ k_rsw_stage(const __grid_constant__ CUtensorMap th,
     // The vortex force needs no shared fluxes: it is evaluated before the
     // barrier, so warps with fewer faces above do not idle at it.
     const int j = j0 + ty, i = i0 + tx;
-    const bool live = j < g.NY && i < g.NX && periodic_owner(g, i);
+    // qgrsw's raw tendency is consumed before any halo fill (the reference
+    // forms the PV from it, operators.py:179-180): every point, halo columns
+    // included, is evaluated locally with the numpy-slice semantics
+    const bool live = j < g.NY && i < g.NX && (a.euler == 3 || periodic_owner(g, i));
     const long long o = (long long)j * g.P + i;
     const uint32_t cd = live ? code[o] : 0u;
     const T* __restrict__ ke = (const T*)a.ke;
@@ -145,21 +148,22 @@ k_rsw_stage(const __grid_constant__ CUtensorMap th,
 
     // Coriolis (addcoriolis, operators.py:32-39); the euler and boussinesq
     // models (equations.py:11-15, 29-35) have neither Coriolis nor a pressure
-    // gradient here
+    // gradient here, qgrsw (106-125) has Coriolis but no gradient forces
     const T fc = srk[3];
-    if (a.euler == 0 && j <= g.NY - 2 && i >= 1 && i <= g.NX - 2)
+    const bool cor = a.euler == 0 || a.euler == 3;
+    if (cor && j <= g.NY - 2 && i >= 1 && i <= g.NX - 2)
         dux += fc * (((ldz(Uy, j, i - 1, g) + ldz(Uy, j + 1, i - 1, g)) + Uy[o]) +
                      ldz(Uy, j + 1, i, g));
-    if (a.euler == 0 && j >= 1 && j <= g.NY - 2 && i <= g.NX - 2)
+    if (cor && j >= 1 && j <= g.NY - 2 && i <= g.NX - 2)
         duy -= fc * (((ldz(Ux, j - 1, i, g) + ldz(Ux, j - 1, i + 1, g)) + Ux[o]) +
                      ldz(Ux, j, i + 1, g));
     // gradients of ke then p (addgrad, operators.py:49-56)
-    if (i >= 1) {
+    if (i >= 1 && a.euler != 3) {
         const T mx = (cd & B_MSKX) ? T(1) : T(0);
         dux -= (ke[o] - ke[o - 1]) * mx;
         if (a.euler == 0) dux -= (p[o] - p[o - 1]) * mx;
     }
-    if (j >= 1) {
+    if (j >= 1 && a.euler != 3) {
         const T my = (cd & B_MSKY) ? T(1) : T(0);
         duy -= (ke[o] - ke[o - g.P]) * my;
         if (a.euler == 0) duy -= (p[o] - p[o - g.P]) * my;
@@ -170,6 +174,14 @@ k_rsw_stage(const __grid_constant__ CUtensorMap th,
     // mass: dh = -div(flux) * msk
     const T msk = (cd & B_MSK) ? T(1) : T(0);
     const T dh = (-(sfx[ty][tx + 1] - sfx[ty][tx]) - (sfy[ty + 1][tx] - sfy[ty][tx])) * msk;
+    if (a.euler == 3) {
+        // qgrsw: the raw tendency, projected by the Helmholtz solve before
+        // the integrator update
+        ((T*)a.dux)[o] = dux;
+        ((T*)a.duy)[o] = duy;
+        ((T*)a.dh)[o] = dh;
+        return;
+    }
 
     const T* dt = srk;
     T ix, iy, ih = T(0);
@@ -250,6 +262,10 @@ k_rsw_diag(const __grid_constant__ CUtensorMap tux,
     if (j >= 1) om = -(ux - sx[r - 1][c]);
     if (i >= 1) om += uy - sy[r][c - 1];
     om *= (cd & B_SLIP) ? T(1) : T(0);
+    if (a.noke) {
+        store_filled((T*)a.omega, g, j, i, om);
+        return;
+    }
     // kinetic energy: innerproduct x then y, times msk*0.5 (operators.py:94-96)
     T ke = T(0);
     {
@@ -628,6 +644,162 @@ int launch_euler_project(int prec, void* ux, void* uy, const double* p, const ui
         k_euler_project<double><<<gr, bl, 0, s>>>((double*)ux, (double*)uy, p, code, g);
     else
         k_euler_project<float><<<gr, bl, 0, s>>>((float*)ux, (float*)uy, p, code, g);
+    return (int)cudaGetLastError();
+}
+
+// ---------------------------------------------------------------------------
+// qgrsw: projection of the RSW tendency on the QG manifold (qg_projection,
+// operators.py:176-211) around the Helmholtz solve of the vertex PV.
+// ---------------------------------------------------------------------------
+
+// pv = compute_vorticity(u) * slipcoef (operators.py:67-77), then
+// pv[1:, 1:] += 0.25 * sum of the four (h - h0) * cs around the vertex and
+// pv *= mskv (add_stretching, 194-201 with centerstovertices(addto), 126-133);
+// cs = -f0/H. Row 0 is 0 (slipcoef is 0 there). FP64 out.
+template <typename T>
+__global__ void k_qgrsw_pv(const T* __restrict__ ux, const T* __restrict__ uy,
+                           const T* __restrict__ h, double* __restrict__ pv,
+                           const uint32_t* __restrict__ code, double cs, double h0, Geom g)
+{
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    const int j = blockIdx.y * blockDim.y + threadIdx.y;
+    if (j >= g.NY || i >= g.NX) return;
+    const long long o = (long long)j * g.P + i;
+    const uint32_t cd = code[o];
+    double v = 0.0;
+    if (j >= 1) v = -((double)ux[o] - (double)ux[o - g.P]);
+    if (i >= 1) v += (double)uy[o] - (double)uy[o - 1];
+    v *= (cd & B_SLIP) ? 1.0 : 0.0;
+    if (j >= 1 && i >= 1) {
+        const double a00 = ((double)h[o - g.P - 1] - h0) * cs;
+        const double a10 = ((double)h[o - 1] - h0) * cs;
+        const double a01 = ((double)h[o - g.P] - h0) * cs;
+        const double a11 = ((double)h[o] - h0) * cs;
+        v += 0.25 * (((a00 + a10) + a01) + a11);
+    }
+    pv[o] = v * ((cd & B_MSKV) ? 1.0 : 0.0);
+}
+
+// From the solution psi: u = perpgrad(psi) (operators.py:144-146, not
+// contravariant), h = verticestocenters(psi * c2) (136-141; + h0 in the state
+// form) times msk (thickness_from_psi, 204-211). Points the reference does
+// not assign (the last row of u.x, the last column of u.y, the last row and
+// column of h) keep their incoming value. A cell with no wet vertex gets 0
+// where the reference's (1/0) * 0 gives nan (a land cell).
+// Mode 0: the projected tendency is filled (equations.py:124: x-periodic
+// halo columns are copies of the interior columns), and the integrator (RK3
+// increment, or the LFRA step) updates EVERY point of the state from its own
+// value, as the reference's addto does over the whole array: the state's
+// halo columns are not refilled (they need not be copies of the interior).
+// Mode 1 (the state form, no fill): every point evaluated locally, in place.
+template <typename T>
+__device__ __forceinline__ void qg_project_point(const QgProj& a, const double* psi,
+                                                 const uint32_t* code, const Geom& g,
+                                                 int j, int i, T& dux, T& duy, T& dh)
+{
+    const long long o = (long long)j * g.P + i;
+    const uint32_t cd = code[o];
+    dux = ((const T*)a.cx)[o];
+    duy = ((const T*)a.cy)[o];
+    dh = ((const T*)a.ch)[o];
+    if (j <= g.NY - 2) dux = T(-(psi[o + g.P] - psi[o]) * ((cd & B_MSKX) ? 1.0 : 0.0));
+    if (i <= g.NX - 2) duy = T((psi[o + 1] - psi[o]) * ((cd & B_MSKY) ? 1.0 : 0.0));
+    double hv = (double)dh;
+    if (j <= g.NY - 2 && i <= g.NX - 2) {
+        const int coef = ((code[o] & B_MSKV) ? 1 : 0) + ((code[o + g.P] & B_MSKV) ? 1 : 0) +
+                         ((code[o + 1] & B_MSKV) ? 1 : 0) +
+                         ((code[o + g.P + 1] & B_MSKV) ? 1 : 0);
+        const double sum = ((psi[o] * a.c2 + psi[o + g.P] * a.c2) + psi[o + 1] * a.c2) +
+                           psi[o + g.P + 1] * a.c2;
+        hv = coef ? (1.0 / coef) * sum : 0.0;
+    }
+    dh = T((hv + a.h0) * ((cd & B_MSK) ? 1.0 : 0.0));
+}
+
+template <typename T>
+__global__ void k_qgrsw_update(QgProj a, const double* __restrict__ psi,
+                               const uint32_t* __restrict__ code, int sk, Geom g,
+                               DevScalars* sc)
+{
+    __shared__ T c[3];
+    const bool lf = ((sk >> 4) & 15) == 3;
+    const int stage = sk & 15;
+    if (threadIdx.x == 0 && threadIdx.y == 0 && a.mode == 0)
+        rk3_coefs<T>(sk, sc->dt, c, sc->ragamma);
+    __syncthreads();
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    const int j = blockIdx.y * blockDim.y + threadIdx.y;
+    if (j >= g.NY || i >= g.NX) return;
+    const long long o = (long long)j * g.P + i;
+    T dux, duy, dh;
+    if (a.mode == 1) {
+        qg_project_point<T>(a, psi, code, g, j, i, dux, duy, dh);
+        ((T*)a.cx)[o] = dux;
+        ((T*)a.cy)[o] = duy;
+        ((T*)a.ch)[o] = dh;
+        return;
+    }
+    // the filled tendency: a periodic halo column takes its interior copy's
+    const int io = !g.xper ? i : i < 3 ? i + g.nx : i >= g.nx + 3 ? i - g.nx : i;
+    qg_project_point<T>(a, psi, code, g, j, io, dux, duy, dh);
+    const T ux = ((const T*)a.ux)[o], uy = ((const T*)a.uy)[o], h = ((const T*)a.h)[o];
+    if (lf) {
+        const bool first = sc->ite == 0;
+        T qn, pn;
+        lfra_update<T>(first, c, ux, ((const T*)a.d1x)[o], dux, qn, pn);
+        ((T*)a.uxo)[o] = qn;
+        ((T*)a.px)[o] = pn;
+        lfra_update<T>(first, c, uy, ((const T*)a.d1y)[o], duy, qn, pn);
+        ((T*)a.uyo)[o] = qn;
+        ((T*)a.py)[o] = pn;
+        lfra_update<T>(first, c, h, ((const T*)a.d1h)[o], dh, qn, pn);
+        ((T*)a.ho)[o] = qn;
+        ((T*)a.ph)[o] = pn;
+        return;
+    }
+    T ix, iy, ih;
+    if (stage == 1) {
+        ix = rk3_increment<T>(1, c, dux, T(0), T(0));
+        iy = rk3_increment<T>(1, c, duy, T(0), T(0));
+        ih = rk3_increment<T>(1, c, dh, T(0), T(0));
+    } else if (stage == 2) {
+        ix = rk3_increment<T>(2, c, ((const T*)a.d1x)[o], dux, T(0));
+        iy = rk3_increment<T>(2, c, ((const T*)a.d1y)[o], duy, T(0));
+        ih = rk3_increment<T>(2, c, ((const T*)a.d1h)[o], dh, T(0));
+    } else {
+        ix = rk3_increment<T>(3, c, ((const T*)a.d1x)[o], ((const T*)a.d2x)[o], dux);
+        iy = rk3_increment<T>(3, c, ((const T*)a.d1y)[o], ((const T*)a.d2y)[o], duy);
+        ih = rk3_increment<T>(3, c, ((const T*)a.d1h)[o], ((const T*)a.d2h)[o], dh);
+    }
+    ((T*)a.uxo)[o] = ux + ix;
+    ((T*)a.uyo)[o] = uy + iy;
+    ((T*)a.ho)[o] = h + ih;
+    if (a.store) {
+        ((T*)a.sx)[o] = dux;
+        ((T*)a.sy)[o] = duy;
+        ((T*)a.sh)[o] = dh;
+    }
+}
+
+int launch_qgrsw_pv(int prec, const void* ux, const void* uy, const void* h, double* pv,
+                    const uint32_t* code, double cs, double h0, const Geom& g, cudaStream_t s)
+{
+    const dim3 gr = pt_grid(g), bl(32, 8);
+    if (prec == 0)
+        k_qgrsw_pv<double><<<gr, bl, 0, s>>>((const double*)ux, (const double*)uy,
+                                             (const double*)h, pv, code, cs, h0, g);
+    else
+        k_qgrsw_pv<float><<<gr, bl, 0, s>>>((const float*)ux, (const float*)uy,
+                                            (const float*)h, pv, code, cs, h0, g);
+    return (int)cudaGetLastError();
+}
+
+int launch_qgrsw_update(int prec, const QgProj& a, const double* psi, const uint32_t* code,
+                        int stage, const Geom& g, DevScalars* sc, cudaStream_t s)
+{
+    const dim3 gr = pt_grid(g), bl(32, 8);
+    if (prec == 0) k_qgrsw_update<double><<<gr, bl, 0, s>>>(a, psi, code, stage, g, sc);
+    else k_qgrsw_update<float><<<gr, bl, 0, s>>>(a, psi, code, stage, g, sc);
     return (int)cudaGetLastError();
 }
 

@@ -14,7 +14,9 @@ struct RswIn {
     double fc;                      // f0 * area * 0.25 (operators.py:33)
     double bdy;                     // 0.5 * dy (addbuoyancy, operators.py:152-153)
     // 0 rsw; 1 euler (vortex force + grad ke only); 2 boussinesq (euler +
-    // buoyancy, with the buoyancy b advected in place of h)
+    // buoyancy, with the buoyancy b advected in place of h); 3 qgrsw (the
+    // raw tendency of vortex force, Coriolis and mass flux into dux/duy/dh,
+    // no update)
     int euler;
 };
 
@@ -24,6 +26,7 @@ struct RswDiag {
     double rdx2, rdy2;  // 1/dx**2, 1/dy**2 (operators.py:62-63)
     double goa;         // g/area (operators.py:111)
     int euler;          // euler model: no pressure from h
+    int noke;           // qgrsw: no kinetic energy (equations.py:127-133)
 };
 
 int launch_fluxform_stage(int method, int prec, const CUtensorMap* tq,
@@ -54,6 +57,27 @@ size_t pt_grid_blocks(const Geom& g);
 int launch_euler_div(int prec, const void* ux, const void* uy, void* dv, double* rhs,
                      const uint32_t* code, double rdx2, double rdy2, double area,
                      const Geom& g, cudaStream_t s);
+// qgrsw: the QG projection of a tendency (or of the state) around the
+// Helmholtz solve (qg_projection, operators.py:176-211)
+struct QgProj {
+    const void *ux, *uy, *h;        // state in (the update's base)
+    void *uxo, *uyo, *ho;           // state out
+    void *cx, *cy, *ch;             // raw tendency (state form: the state, in place)
+    void *sx, *sy, *sh;             // projected tendency out (if store)
+    const void *d1x, *d1y, *d1h;    // earlier projected tendencies (RK) or the
+    const void *d2x, *d2y, *d2h;    //   filtered previous state (LFRA, d1)
+    void *px, *py, *ph;             // LFRA: filtered state out
+    double c2;                      // f0 * area / g (thickness_from_psi)
+    double h0;                      // state mode: H * area - hb, else 0
+    int mode;                       // 0: tendency + integrator update;
+                                    // 1: project the state (cx.. in place)
+    int store;                      // keep the projected tendency in sx..
+};
+int launch_qgrsw_pv(int prec, const void* ux, const void* uy, const void* h, double* pv,
+                    const uint32_t* code, double cs, double h0, const Geom& g,
+                    cudaStream_t s);
+int launch_qgrsw_update(int prec, const QgProj& a, const double* psi, const uint32_t* code,
+                        int stage, const Geom& g, DevScalars* sc, cudaStream_t s);
 int launch_euler_project(int prec, void* ux, void* uy, const double* p, const uint32_t* code,
                          const Geom& g, cudaStream_t s);
 

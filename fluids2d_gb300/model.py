@@ -29,6 +29,7 @@ MODEL_SPECS = {
     "boussinesq": (("b", "u", "U", "omega", "ke", "p", "div", "flx"), ("b", "u")),
     "rsw": (("u", "h", "U", "omega", "ke", "p", "flx", "pv"), ("u", "h")),
     "qg": (("pv", "U", "h", "flx", "work", "psi"), ("pv",)),
+    "qgrsw": (("u", "h", "U", "omega", "ke", "p", "flx", "pv", "psi"), ("u", "h")),
 }
 VECTORS = ("u", "U", "flx", "v")
 Vector = namedtuple("vector", ("x", "y"))
@@ -320,6 +321,14 @@ class Model:
         """model.py:67-69 (time.dt is the current device dt)."""
         self._push()
         check(lib().f2d_step(self._h, int(nsteps)))
+        self._device_newer = True
+
+    def qg_projection(self):
+        """qg_projection(mesh, s.u, s.h, s.pv, s.psi) (operators.py:176-183,
+        anomaly=False) on the model's state, on the GPU: the qgrsw initial
+        state of the reference's geostrophic-adjustment set-up."""
+        self._push()
+        check(lib().f2d_qg_projection(self._h))
         self._device_newer = True
 
     def set_dt(self):

@@ -14,7 +14,7 @@ _methods_extended = _methods + ["classic"]
 _integrators = ["rk3", "ef", "enrk3", "LFRA"]
 
 # models and integrators the GPU path implements
-SUPPORTED_MODELS = ("eulerpsi", "rsw", "qg", "euler", "boussinesq")
+SUPPORTED_MODELS = ("eulerpsi", "rsw", "qg", "euler", "boussinesq", "qgrsw")
 # the state variables of those models (states.py:7-17)
 MODEL_VARIABLES = {
     "eulerpsi": ("omega", "U", "psi", "vomega", "flx"),
@@ -22,6 +22,7 @@ MODEL_VARIABLES = {
     "boussinesq": ("b", "u", "U", "omega", "ke", "p", "div", "flx"),
     "rsw": ("u", "h", "U", "omega", "ke", "p", "flx", "pv"),
     "qg": ("pv", "U", "h", "flx", "work", "psi"),
+    "qgrsw": ("u", "h", "U", "omega", "ke", "p", "flx", "pv", "psi"),
 }
 SUPPORTED_INTEGRATORS = ("rk3", "ef", "enrk3", "LFRA")
 EXTRA = ("precision", "poisson_tol", "poisson_maxit")

@@ -24,7 +24,7 @@ extern "C" {
 
 /* models (param.py:1-2) the GPU path implements */
 enum { F2D_MODEL_EULERPSI = 0, F2D_MODEL_RSW = 1, F2D_MODEL_QG = 2,
-       F2D_MODEL_EULER = 3, F2D_MODEL_BOUSSINESQ = 4 };
+       F2D_MODEL_EULER = 3, F2D_MODEL_BOUSSINESQ = 4, F2D_MODEL_QGRSW = 5 };
 /* flux methods (param.py:4, weno.py:338-343) */
 enum { F2D_METHOD_WENO = 0, F2D_METHOD_UPWIND = 1, F2D_METHOD_CENTERED = 2,
        F2D_METHOD_CWENO = 3 };
@@ -134,6 +134,10 @@ int f2d_set_coriolis(f2d_model m, const double *f_vertices);
 
 /* integrator.diag(state) (equations.py:80-84, 99-101, 150-155) */
 int f2d_diag(f2d_model m);
+/* qg_projection(mesh, s.u, s.h, s.pv, s.psi) (operators.py:176-183, the
+ * anomaly=False form used to set a qgrsw initial state): the state's (u, h)
+ * in place, pv and psi of the projection; qgrsw models only. */
+int f2d_qg_projection(f2d_model m);
 /* Model.step(n) with the current time step (model.py:67-69) */
 int f2d_step(f2d_model m, int nsteps);
 /* n iterations of the Model.run loop body: set_dt then step(1)

@@ -417,6 +417,44 @@ def centerstovertices(mesh, c, v):
     v *= mesh.mskv
 
 
+def centerstovertices_add(mesh, c, v):
+    """operators.py:126-129, 133 (addto=True)."""
+    v[1:, 1:] += 0.25 * (c[:-1, :-1] + c[1:, :-1] + c[:-1, 1:] + c[1:, 1:])
+    v *= mesh.mskv
+
+
+def verticestocenters(mesh, vh, h):
+    """operators.py:136-141. A cell with no wet vertex gets (1/0) * 0 = nan,
+    as in the reference."""
+    m = mesh.mskv
+    coef = m[:-1, :-1] + m[1:, :-1] + m[:-1, 1:] + m[1:, 1:]
+    with np.errstate(divide="ignore", invalid="ignore"):
+        h[:-1, :-1] = (1 / coef) * (vh[:-1, :-1] + vh[1:, :-1] + vh[:-1, 1:]
+                                    + vh[1:, 1:])
+        h *= mesh.msk
+
+
+def qg_projection(mesh, ux, uy, h, pv, psi, anomaly=False):
+    """operators.py:176-183 with add_stretching (194-201) and
+    thickness_from_psi (204-211): project (u, h) on the QG manifold through
+    the Helmholtz solve of the PV."""
+    p = mesh.param
+    f0, H, g = p.f0, p.H, p.g
+    compute_vorticity(mesh, ux, uy, pv)
+    if anomaly:
+        centerstovertices_add(mesh, h * (-f0 / H), pv)
+    else:
+        h0 = H * mesh.area - mesh.hb
+        centerstovertices_add(mesh, (h - h0) * (-f0 / H), pv)
+    mesh.qg_helmholtz.solve(pv, psi)
+    verticestocenters(mesh, psi * (f0 * mesh.area / g), h)
+    if not anomaly:
+        h += (H * mesh.area) - mesh.hb
+    with np.errstate(invalid="ignore"):
+        h *= mesh.msk
+    perpgrad(mesh, psi, ux, uy)
+
+
 def perpgrad(mesh, psi, Ux, Uy, contravariant=False):
     """operators.py:144-149."""
     Ux[:-1, :] = -np.diff(psi, axis=0) * mesh.mskx[:-1, :]
@@ -435,9 +473,10 @@ STATE_VARS = {
     "eulerpsi": ("omega", "U", "psi", "vomega", "flx"),
     "rsw": ("u", "h", "U", "omega", "ke", "p", "flx", "pv"),
     "qg": ("pv", "U", "h", "flx", "work", "psi"),
+    "qgrsw": ("u", "h", "U", "omega", "ke", "p", "flx", "pv", "psi"),
 }
 PROGNOSTIC = {"eulerpsi": ("omega",), "rsw": ("u", "h"), "qg": ("pv",),
-              "euler": ("u",), "boussinesq": ("b", "u")}
+              "euler": ("u",), "boussinesq": ("b", "u"), "qgrsw": ("u", "h")}
 VECTORS = ("u", "U", "flx")
 
 
@@ -519,6 +558,18 @@ class Model:
             for k in ("u.x", "u.y", "b"):
                 m.fill(ds[k])
 
+        elif p.model == "qgrsw":
+            # equations.py:106-125: the RSW tendency without the gradient
+            # forces, projected on the QG manifold (anomaly form)
+            addvortexforce(p, m, s["U.x"], s["U.y"], s["omega"], ds["u.x"],
+                           ds["u.y"], sq)
+            addcoriolis(p, m, s["U.x"], s["U.y"], ds["u.x"], ds["u.y"])
+            divflux(p, m, s["flx.x"], s["flx.y"], s["h"], s["U.x"], s["U.y"],
+                    ds["h"], sq)
+            qg_projection(m, ds["u.x"], ds["u.y"], ds["h"], s["pv"], s["psi"],
+                          anomaly=True)
+            for k in ("u.x", "u.y", "h"):
+                m.fill(ds[k])
         if self.tracer:
             # addtracerequation (equations.py:217-226): no halo fill
             divflux(p, m, s["flx.x"], s["flx.y"], s[self.tracer], s["U.x"],
@@ -551,6 +602,11 @@ class Model:
                                    s["U.y"], s["ke"], sq)
             m.fill(s["omega"])
             m.fill(s["ke"])
+        elif p.model == "qgrsw":
+            # equations.py:127-133
+            sharp(m, s["u.x"], s["u.y"], s["U.x"], s["U.y"])
+            compute_vorticity(m, s["u.x"], s["u.y"], s["omega"])
+            m.fill(s["omega"])
         elif p.model == "rsw":
             sharp(m, s["u.x"], s["u.y"], s["U.x"], s["U.y"])
             compute_vorticity(m, s["u.x"], s["u.y"], s["omega"])

@@ -181,7 +181,7 @@ def poisson_cases():
 
 
 # -------------------------------------------------------------- models ----
-def run_model(case, nsteps, fname, cfl=None, extra=None):
+def run_model(case, nsteps, fname, cfl=None, extra=None, setup=None):
     kw = dict(xperiodic=case.get("xperiodic", False), Lx=case["Lx"],
               Ly=case["Ly"], tend=1e9, maxite=10 ** 9)
     for k in ("f0", "g", "H", "beta"):
@@ -202,9 +202,19 @@ def run_model(case, nsteps, fname, cfl=None, extra=None):
             getattr(getattr(m.state, k.split(".")[0]), k.split(".")[1])[:] = v
         else:
             getattr(m.state, k)[:] = v
+    if setup is not None:
+        # an initial-state operator of the reference (e.g. qg_projection);
+        # the fixture's initial condition is the state it leaves
+        setup(m)
+        case = dict(case)
+        case["fields"] = {}
+        for name in setup.fields:
+            v = getattr(m.state, name.split(".")[0])
+            v = getattr(v, name.split(".")[1]) if "." in name else v
+            case["fields"][name] = v.copy()
     m.integrator.diag(m.state)
 
-    out = {"msk": case["msk"].copy(),
+    out = {"msk": case["msk"].copy(), "model": np.array(case["model"]),
            "params": np.array([case["nx"], case["ny"],
                                int(kw["xperiodic"])]),
            "scalars": np.array([case["Lx"], case["Ly"], p.f0, p.beta, p.g,
@@ -305,6 +315,31 @@ def tracer_cases():
               extra={"tracer": "s"})
 
 
+def qgrsw_cases():
+    """The qgrsw model (equations.py:104-135): the RSW tendency projected on
+    the QG manifold each stage (qg_projection, operators.py:176-211). The
+    initial state is h of a shallow-water bump projected by the reference's
+    qg_projection (anomaly=False), as in its geostrophic-adjustment
+    experiment; the reference writes nan into cells without a wet vertex."""
+    from fluids2d.operators import qg_projection
+
+    def project(m):
+        s = m.state
+        qg_projection(m.mesh, s.u, s.h, s.pv, s.psi)
+    project.fields = ("u.x", "u.y", "h", "pv", "psi")
+
+    for xper, seed, fname, extra in ((False, 3, "model_qgrsw.npz", None),
+                                     (True, 5, "model_qgrsw_periodic.npz", None),
+                                     (False, 7, "model_qgrsw_lfra.npz",
+                                      {"integrator": "LFRA"})):
+        c = wl.rsw_case(n=40, ny=32, seed=seed, nislands=2, xperiodic=xper, f0=10.0)
+        c["model"] = "qgrsw"
+        c["fields"] = {"u.x": np.zeros_like(c["fields"]["h"]),
+                       "u.y": np.zeros_like(c["fields"]["h"]),
+                       "h": c["fields"]["h"]}
+        run_model(c, 4, fname, cfl=0.5, extra=extra, setup=project)
+
+
 def integrator_cases():
     """The reference's other Runge-Kutta integrators (integrators.py:116-155)."""
     c = wl.eulerpsi_case(n=40, ny=32, seed=2, nislands=2, nvortices=5,
@@ -336,13 +371,15 @@ def lfra_cases():
 
 if __name__ == "__main__":
     which = sys.argv[1:] or ["mesh", "sweeps", "poisson", "models", "integrators",
-                             "euler", "boussinesq", "tracer"]
+                             "euler", "boussinesq", "tracer", "qgrsw"]
     if "lfra" in which:
         lfra_cases()
     if "boussinesq" in which:
         boussinesq_cases()
     if "tracer" in which:
         tracer_cases()
+    if "qgrsw" in which:
+        qgrsw_cases()
     if "mesh" in which:
         mesh_cases()
     if "sweeps" in which:

@@ -132,14 +132,16 @@ MODEL_FILES = ["model_eulerpsi.npz", "model_eulerpsi_islands.npz",
                "model_euler_lfra_periodic.npz", "model_boussinesq.npz",
                "model_boussinesq_periodic.npz", "model_boussinesq_lfra.npz",
                "model_eulerpsi_tracer.npz", "model_qg_tracer_lfra.npz",
-               "model_rsw_tracer.npz", "model_boussinesq_tracer.npz"]
+               "model_rsw_tracer.npz", "model_boussinesq_tracer.npz",
+               "model_qgrsw.npz", "model_qgrsw_periodic.npz", "model_qgrsw_lfra.npz"]
 
 
 def model_from_golden(g):
     nx, ny, xper = (int(v) for v in g["params"])
     Lx, Ly, f0, beta, gg, H, cfl = (float(v) for v in g["scalars"])
     names = {k[3:] for k in g.files if k.startswith("ic/")}
-    kind = ("eulerpsi" if "omega" in names else "rsw" if "h" in names else
+    kind = (str(g["model"]) if "model" in g.files else
+            "eulerpsi" if "omega" in names else "rsw" if "h" in names else
             "boussinesq" if "b" in names else
             "euler" if "u.x" in names else "qg")
     integ = str(g["integrator"]) if "integrator" in g.files else "rk3"
@@ -178,7 +180,30 @@ def compare(m, ref_get, tol, skip=("flx.x", "flx.y")):
         if k in skip:
             continue
         r = ref_get(k)
-        if r is None or not np.any(r):
+        if r is None:
+            continue
+        fin = np.isfinite(r)
+        if not fin.all():
+            # qgrsw: the reference's thickness_from_psi writes nan ((1/0)*0)
+            # into cells without a wet vertex (land); the GPU writes 0 there
+            fl = (m.mesh.mskv if k in ("pv", "psi") else m.mesh.msk) > 0
+            assert not np.any(~fin & fl), k
+            v, r = np.where(fin, v, 0.0), np.where(fin, r, 0.0)
+        if m.param.model == "qgrsw" and m.param.xperiodic and k in ("pv", "psi"):
+            # x-periodic qgrsw: the reference's WENO loops run over the
+            # flattened array, so stencils of the halo columns 0-2 and
+            # nx+3..nx+5 wrap into the neighbouring row; its raw tendency
+            # there (consumed by the PV before the halo fill) differs from
+            # the local one at the 1e-10 level in the PV of vertex column 3
+            # and entirely in the PV's halo columns. The prognostic fields
+            # stay at the step tolerance; pv (interior columns) and psi are
+            # held to 1e-7.
+            if k == "pv":
+                v, r = v[:, 3:-3], r[:, 3:-3]
+            worst[k] = rel_l2(v, r)
+            assert worst[k] <= 1e-7, (k, worst[k])
+            continue
+        if not np.any(r):
             continue
         if m.param.model in ("euler", "boussinesq") and k == "p":
             # the Neumann pressure is defined up to a constant: compare the
@@ -190,7 +215,8 @@ def compare(m, ref_get, tol, skip=("flx.x", "flx.y")):
             v = np.where(fl, v - v[fl].mean(), 0.0)
             r = np.where(fl, r - r[fl].mean(), 0.0)
         worst[k] = rel_l2(v, r)
-    bad = {k: e for k, e in worst.items() if e > tol}
+    bad = {k: e for k, e in worst.items() if e > tol and not (
+        m.param.model == "qgrsw" and m.param.xperiodic and k in ("pv", "psi"))}
     assert not bad, bad
     return worst
 
@@ -293,6 +319,37 @@ def test_model_flux_methods_vs_oracle(kind, method):
             getattr(s, k)[:] = v
     m.integrator.diag(s)
     for _ in range(3):
+        om.run_steps(1)
+        m.advance(1)
+        assert abs(m.time.dt - om.dt) <= 1e-10 * om.dt
+        compare(m, lambda k: om.s.get(k), STEP_TOL)
+    m.sync()
+
+
+@pytest.mark.parametrize("xper", [False, True])
+def test_qgrsw_projection_and_steps_vs_oracle(xper):
+    """qgrsw at 128x96 with islands: the state-form qg_projection (the
+    reference's initialisation, operators.py:176-183) on the GPU against the
+    oracle's, then whole steps."""
+    from fluids2d_gb300.operators import qg_projection
+    case = wl.rsw_case(n=128, ny=96, seed=9, nislands=3, xperiodic=xper, f0=10.0)
+    z = np.zeros_like(case["fields"]["h"])
+    case["fields"] = {"u.x": z, "u.y": z.copy(), "h": case["fields"]["h"]}
+    om = _oracle_like(case, "qgrsw", cfl=0.5)
+    O.qg_projection(om.mesh, om.s["u.x"], om.s["u.y"], om.s["h"], om.s["pv"],
+                    om.s["psi"])
+    om.diag()
+    m = _model("qgrsw", case["nx"], case["ny"], case["msk"], xperiodic=xper,
+               Lx=case["Lx"], Ly=case["Ly"], f0=case["f0"], g=case["g"], H=case["H"],
+               cfl=0.5, tend=1e300, maxite=10 ** 9)
+    s = m.state
+    s.u.x[:] = case["fields"]["u.x"]
+    s.u.y[:] = case["fields"]["u.y"]
+    s.h[:] = case["fields"]["h"]
+    qg_projection(m.mesh, s.u, s.h, s.pv, s.psi)
+    m.integrator.diag(m.state)
+    compare(m, lambda k: om.s.get(k), STEP_TOL)
+    for _ in range(4):
         om.run_steps(1)
         m.advance(1)
         assert abs(m.time.dt - om.dt) <= 1e-10 * om.dt

@@ -110,7 +110,8 @@ MODEL_FILES = ["model_eulerpsi.npz", "model_eulerpsi_islands.npz",
                "model_euler_lfra_periodic.npz", "model_boussinesq.npz",
                "model_boussinesq_periodic.npz", "model_boussinesq_lfra.npz",
                "model_eulerpsi_tracer.npz", "model_qg_tracer_lfra.npz",
-               "model_rsw_tracer.npz", "model_boussinesq_tracer.npz"]
+               "model_rsw_tracer.npz", "model_boussinesq_tracer.npz",
+               "model_qgrsw.npz", "model_qgrsw_periodic.npz", "model_qgrsw_lfra.npz"]
 
 
 def oracle_from_golden(g, pysq=True):
@@ -118,7 +119,8 @@ def oracle_from_golden(g, pysq=True):
     Lx, Ly, f0, beta, gg, H, cfl = (float(v) for v in g["scalars"])
     model = [k for k in g.files if k.startswith("ic/")]
     names = {k[3:] for k in model}
-    kind = ("eulerpsi" if "omega" in names else
+    kind = (str(g["model"]) if "model" in g.files else
+            "eulerpsi" if "omega" in names else
             "rsw" if "h" in names else "boussinesq" if "b" in names else
             "euler" if "u.x" in names else "qg")
     integ = str(g["integrator"]) if "integrator" in g.files else "rk3"
@@ -140,6 +142,11 @@ def _compare_state(m, g, prefix, tol):
     worst = 0.0
     for k, v in m.s.items():
         ref = g[f"{prefix}/{k}"]
+        # the reference writes nan where qg_projection divides by a zero
+        # count of wet vertices (land cells): same places, finite elsewhere
+        fin = np.isfinite(ref)
+        np.testing.assert_array_equal(np.isfinite(v), fin, err_msg=f"{prefix} {k}")
+        v, ref = v[fin], ref[fin]
         scale = max(np.max(np.abs(ref)), 1e-300)
         err = np.max(np.abs(v - ref)) / scale
         assert err <= tol, (prefix, k, err)
@@ -157,6 +164,9 @@ def test_model_steps_vs_reference(fname):
     m.rhs(m.s, ds)
     for k, v in ds.items():
         ref = g["rhs0/" + k]
+        fin = np.isfinite(ref)
+        np.testing.assert_array_equal(np.isfinite(v), fin, err_msg=k)
+        v, ref = v[fin], ref[fin]
         assert np.max(np.abs(v - ref)) <= 1e-13 * max(np.max(np.abs(ref)),
                                                        1e-300), k
     dts = g["dt"]
