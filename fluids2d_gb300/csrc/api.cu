@@ -534,6 +534,7 @@ static int rec_qgrsw_stage(f2d_model_s* m, int k, int par, cudaStream_t s)
     a.dh = ds("h", kt);
     a.fc = m->fc;
     void* om = fb(m, "omega");
+    a.w = om;
     CKI(make_tmap(m, (void*)a.h));
     CKI(make_tmap(m, om));
     CKI(launch_rsw_stage(m->p.vortexforce, m->prec, tmap(m, (void*)a.h), tmap(m, om), a,

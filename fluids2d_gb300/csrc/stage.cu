@@ -63,6 +63,23 @@ k_rsw_stage(const __grid_constant__ CUtensorMap th,
     const T* __restrict__ Uy = (const T*)a.Uy;
 
     if (!stage_tiles<T>(sh, &th, sw, &tw, i0, j0, &bar, &sc->status)) return;
+    // qgrsw consumes the raw tendency of the x-periodic halo columns (its PV
+    // is formed before the halo fill, operators.py:179-180), where the
+    // reference's stencils over the raveled array run into the neighbouring
+    // row: the edge tiles take those values in place of the out-of-array 0
+    const bool wrap = a.euler == 3 && g.xper;
+    if (wrap && (i0 < OX || i0 - OX + SW > g.NX)) {
+        const T* __restrict__ hg = (const T*)a.h;
+        const T* __restrict__ wg = (const T*)a.w;
+        for (int e = t; e < SH * SW; e += TX * TY) {
+            const int r = e / SW, c = e % SW;
+            const int gj = j0 - OY + r, gi = i0 - OX + c;
+            if (gi >= 0 && gi < g.NX) continue;
+            sh[r][c] = ldw(hg, gj, gi, g);
+            sw[r][c] = ldw(wg, gj, gi, g);
+        }
+        __syncthreads();
+    }
 
     // mass fluxes U*h at the faces (compflux, weno.py:349-363)
     auto xface = [&](int r, int c) {
@@ -120,8 +137,12 @@ k_rsw_stage(const __grid_constant__ CUtensorMap th,
     {
         const int L = lev(cd, SH_OVY);
         if (L) {
-            const T Vm = T(0.25) * (((Uy[o] + ldz(Uy, j + 1, i, g)) + ldz(Uy, j, i - 1, g)) +
-                                    ldz(Uy, j + 1, i - 1, g));
+            const T Vm = wrap ? T(0.25) * (((Uy[o] + ldw(Uy, j + 1, i, g)) +
+                                            ldw(Uy, j, i - 1, g)) +
+                                           ldw(Uy, j + 1, i - 1, g))
+                              : T(0.25) * (((Uy[o] + ldz(Uy, j + 1, i, g)) +
+                                            ldz(Uy, j, i - 1, g)) +
+                                           ldz(Uy, j + 1, i - 1, g));
             const int c = tx + OX, r = ty + OY;
             dux = face_value<M, T>(L, Vm, sw[r - 2][c], sw[r - 1][c], sw[r][c],
                                    sw[r + 1][c], sw[r + 2][c], sw[r + 3][c]) *
@@ -133,8 +154,12 @@ k_rsw_stage(const __grid_constant__ CUtensorMap th,
     {
         const int L = lev(cd, SH_OVX);
         if (L) {
-            const T Vm = T(0.25) * (((Ux[o] + ldz(Ux, j, i + 1, g)) + ldz(Ux, j - 1, i, g)) +
-                                    ldz(Ux, j - 1, i + 1, g));
+            const T Vm = wrap ? T(0.25) * (((Ux[o] + ldw(Ux, j, i + 1, g)) +
+                                            ldw(Ux, j - 1, i, g)) +
+                                           ldw(Ux, j - 1, i + 1, g))
+                              : T(0.25) * (((Ux[o] + ldz(Ux, j, i + 1, g)) +
+                                            ldz(Ux, j - 1, i, g)) +
+                                           ldz(Ux, j - 1, i + 1, g));
             const T* w = &sw[ty + OY][tx + OX - 2];
             duy = -face_value<M, T>(L, Vm, w[0], w[1], w[2], w[3], w[4], w[5]) * Vm;
         }

@@ -6,6 +6,7 @@ namespace f2d {
 
 struct RswIn {
     const void *ux, *uy, *h;        // prognostic, stage input
+    const void* w;                  // omega (qgrsw: the wrap of the edge tiles)
     void *uxo, *uyo, *ho;           // prognostic, stage output
     const void *Ux, *Uy, *ke, *p;   // diagnostics of the stage input
     void *dux, *duy, *dh;           // this stage's tendencies (stored if != 0)

@@ -22,6 +22,22 @@ __device__ __forceinline__ T ldz(const T* __restrict__ a, int j, int i,
                                                       : T(0);
 }
 
+// Load with the reference's flattened-array semantics (its WENO loops index
+// the raveled (NY, NX) array, weno.py:349-411): a column outside [0, NX)
+// continues in the previous / next row; outside the array: 0.
+template <typename T>
+__device__ __forceinline__ T ldw(const T* __restrict__ a, int j, int i, const Geom& g)
+{
+    if (i < 0) {
+        i += g.NX;
+        j -= 1;
+    } else if (i >= g.NX) {
+        i -= g.NX;
+        j += 1;
+    }
+    return (j >= 0 && j < g.NY && i >= 0 && i < g.NX) ? a[(long long)j * g.P + i] : T(0);
+}
+
 // The RK3 increment of stage k (1, 2, 3) in the reference's evaluation order:
 // y += ((0 + c1*ds1) + c2*ds2) + c3*ds3 with (c) = (dt), (-3dt/4, dt/4),
 // (-dt/12, -dt/12, 2dt/3).

@@ -189,20 +189,13 @@ def compare(m, ref_get, tol, skip=("flx.x", "flx.y")):
             fl = (m.mesh.mskv if k in ("pv", "psi") else m.mesh.msk) > 0
             assert not np.any(~fin & fl), k
             v, r = np.where(fin, v, 0.0), np.where(fin, r, 0.0)
-        if m.param.model == "qgrsw" and m.param.xperiodic and k in ("pv", "psi"):
-            # x-periodic qgrsw: the reference's WENO loops run over the
-            # flattened array, so stencils of the halo columns 0-2 and
-            # nx+3..nx+5 wrap into the neighbouring row; its raw tendency
-            # there (consumed by the PV before the halo fill) differs from
-            # the local one at the 1e-10 level in the PV of vertex column 3
-            # and entirely in the PV's halo columns. The prognostic fields
-            # stay at the step tolerance; pv (interior columns) and psi are
-            # held to 1e-7.
-            if k == "pv":
-                v, r = v[:, 3:-3], r[:, 3:-3]
-            worst[k] = rel_l2(v, r)
-            assert worst[k] <= 1e-7, (k, worst[k])
-            continue
+        if m.param.model == "qgrsw" and m.param.xperiodic and k == "pv":
+            # x-periodic qgrsw: the PV of the halo columns is formed from the
+            # raw tendency before its fill, whose last column the reference's
+            # div (operators.py:104-107) leaves at the scratch array's
+            # previous content; the PV of the interior vertices (the solve's
+            # right-hand side) is compared
+            v, r = v[:, 3:-3], r[:, 3:-3]
         if not np.any(r):
             continue
         if m.param.model in ("euler", "boussinesq") and k == "p":
@@ -215,8 +208,7 @@ def compare(m, ref_get, tol, skip=("flx.x", "flx.y")):
             v = np.where(fl, v - v[fl].mean(), 0.0)
             r = np.where(fl, r - r[fl].mean(), 0.0)
         worst[k] = rel_l2(v, r)
-    bad = {k: e for k, e in worst.items() if e > tol and not (
-        m.param.model == "qgrsw" and m.param.xperiodic and k in ("pv", "psi"))}
+    bad = {k: e for k, e in worst.items() if e > tol}
     assert not bad, bad
     return worst
 
