@@ -11,5 +11,7 @@ from .param import Param  # noqa: F401
 from .model import Model  # noqa: F401
 from . import tools  # noqa: F401
 from . import operators  # noqa: F401
+from . import diagnostics  # noqa: F401
+from . import io  # noqa: F401
 from .ensemble import Ensemble  # noqa: F401
 from ._lib import F2DError  # noqa: F401

@@ -77,6 +77,9 @@ _SIGS = {
     "f2d_set_coriolis": ([c_void_p, c_void_p], c_int),
     "f2d_diag": ([c_void_p], c_int),
     "f2d_qg_projection": ([c_void_p], c_int),
+    "f2d_field_get_f32": ([c_void_p, ctypes.c_char_p, c_void_p], c_int),
+    "f2d_bulk_record": ([c_void_p], c_int),
+    "f2d_bulk_read": ([c_void_p, c_void_p, c_int, ctypes.POINTER(c_int)], c_int),
     "f2d_step": ([c_void_p, c_int], c_int),
     "f2d_run": ([c_void_p, c_int], c_int),
     "f2d_set_dt": ([c_void_p], c_int),

@@ -105,6 +105,10 @@ struct f2d_model_s {
     void* d_fv = nullptr;  // mesh.f (qg beta-plane)
     DevScalars* sc = nullptr;
     double* partials = nullptr;
+    // Bulk diagnostics ring (records of 5 doubles) and FP32 snapshot staging
+    double* bulk_ring = nullptr;
+    int* bulk_count = nullptr;
+    float* f32_stage = nullptr;
     std::map<std::string, Field> fields;
     std::vector<void*> allocs;
     double dx, dy, area, rdx2, rdy2, goa, fc, maindiag, cx, cy, dt_const;
@@ -1136,6 +1140,73 @@ int f2d_field_set(f2d_model m, const char* name, const double* host)
 {
     return field_io(m, name, (double*)host, true, false);
 }
+static const int BULK_CAP = 1000;  // Bulk.ndiags (diagnostics.py:21)
+
+int f2d_bulk_record(f2d_model m)
+{
+    if (!m) return fail(1, "null model");
+    if (!fb(m, "ke") || !fb(m, "omega"))
+        return fail(1, "Bulk needs the ke and omega fields (rsw, euler, boussinesq, qgrsw)");
+    if (!m->bulk_ring) {
+        m->bulk_ring = (double*)dalloc(m, sizeof(double) * 5 * BULK_CAP);
+        m->bulk_count = (int*)dalloc(m, sizeof(int));
+        if (!m->bulk_ring || !m->bulk_count) return fail(2, "out of device memory");
+    }
+    // domsum(msk) over the whole array (diagnostics.py:15)
+    double summsk = 0.0;
+    for (int8_t v : m->mesh.msk) summsk += v;
+    if (summsk <= 0) return fail(1, "the mask has no wet cell");
+    BulkArgs a;
+    a.ke = fb(m, "ke");
+    a.omega = fb(m, "omega");
+    a.Ux = fb(m, "U.x");
+    a.Uy = fb(m, "U.y");
+    a.ring = m->bulk_ring;
+    a.count = m->bulk_count;
+    a.cap = BULK_CAP;
+    a.summsk = summsk;
+    a.area = m->area;
+    a.dx = m->dx;
+    a.dy = m->dy;
+    CKI(launch_bulk(m->prec, a, m->g, m->sc, m->partials, m->stream));
+    return 0;
+}
+
+int f2d_bulk_read(f2d_model m, double* host, int capacity, int* nrec)
+{
+    if (!m || !nrec) return fail(1, "null argument");
+    *nrec = 0;
+    if (!m->bulk_ring) return 0;
+    int n = 0;
+    CK(cudaMemcpyAsync(&n, m->bulk_count, sizeof(int), cudaMemcpyDeviceToHost, m->stream));
+    CK(cudaStreamSynchronize(m->stream));
+    if (n > capacity) return fail(1, "host buffer too small for the Bulk records");
+    if (n > 0) {
+        CK(cudaMemcpyAsync(host, m->bulk_ring, sizeof(double) * 5 * n, cudaMemcpyDeviceToHost,
+                           m->stream));
+        CK(cudaMemsetAsync(m->bulk_count, 0, sizeof(int), m->stream));
+        CK(cudaStreamSynchronize(m->stream));
+    }
+    *nrec = n;
+    return 0;
+}
+
+int f2d_field_get_f32(f2d_model m, const char* name, float* host)
+{
+    if (!m || !name || !host) return fail(1, "null argument");
+    void* d = fb(m, name);
+    if (!d) return fail(8, std::string("no field named ") + name);
+    if (!m->f32_stage) {
+        m->f32_stage = (float*)dalloc(m, sizeof(float) * (size_t)m->g.NY * m->g.NX);
+        if (!m->f32_stage) return fail(2, "out of device memory");
+    }
+    CKI(launch_to_f32(field_es(m, name) == 8 ? 0 : 1, d, m->f32_stage, m->g, m->stream));
+    CK(cudaMemcpyAsync(host, m->f32_stage, sizeof(float) * (size_t)m->g.NY * m->g.NX,
+                       cudaMemcpyDeviceToHost, m->stream));
+    CK(cudaStreamSynchronize(m->stream));
+    return 0;
+}
+
 int f2d_field_get(f2d_model m, const char* name, double* host)
 {
     return field_io(m, name, host, false, false);

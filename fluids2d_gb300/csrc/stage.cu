@@ -828,6 +828,79 @@ int launch_qgrsw_update(int prec, const QgProj& a, const double* psi, const uint
     return (int)cudaGetLastError();
 }
 
+// ---------------------------------------------------------------------------
+// Bulk diagnostics (Bulk.__call__, diagnostics.py:39-57): domain sums over
+// the whole array of ke, omega^2, omega, U.y * xv and U.x * yu (xv, yu: the
+// y-face x and x-face y coordinates, meshes.py:57-68), divided by sum(msk);
+// the last block appends {t, ke, ens, vort, angular} to the device ring.
+// The grid strides over rows so that 5 partials per block fit the model's
+// reduction scratch.
+// ---------------------------------------------------------------------------
+template <typename T>
+__global__ void k_bulk(BulkArgs a, Geom g, DevScalars* sc, double* partials)
+{
+    double w[5] = {0.0, 0.0, 0.0, 0.0, 0.0};
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < g.NX) {
+        const T* ke = (const T*)a.ke;
+        const T* om = (const T*)a.omega;
+        const T* ux = (const T*)a.Ux;
+        const T* uy = (const T*)a.Uy;
+        const double xv = (i - 3 + 0.5) * a.dx;
+        for (int j = blockIdx.y * blockDim.y + threadIdx.y; j < g.NY;
+             j += gridDim.y * blockDim.y) {
+            const long long o = (long long)j * g.P + i;
+            const double yu = (j - 3 + 0.5) * a.dy;
+            const double w0 = (double)om[o];
+            w[0] += (double)ke[o];
+            w[1] += w0 * w0;
+            w[2] += w0;
+            w[3] += (double)uy[o] * xv;
+            w[4] += (double)ux[o] * yu;
+        }
+    }
+    if (grid_reduce<5, false>(w, partials, &sc->counter[6])) {
+        const int k = *a.count;
+        if (k < a.cap) {
+            double* r = a.ring + 5 * (size_t)k;
+            const double S = a.summsk;
+            r[0] = sc->t;
+            r[1] = w[0] / S;
+            r[2] = 0.5 * (w[1] / S) / (a.area * a.area);
+            r[3] = (w[2] / S) / a.area;
+            r[4] = (w[3] / S) * a.dx - (w[4] / S) * a.dy;
+            *a.count = k + 1;
+        }
+    }
+}
+
+int launch_bulk(int prec, const BulkArgs& a, const Geom& g, DevScalars* sc, double* partials,
+                cudaStream_t s)
+{
+    const dim3 full = pt_grid(g);
+    const dim3 gr(full.x, max(1u, full.y / 2)), bl(32, 8);
+    if (prec == 0) k_bulk<double><<<gr, bl, 0, s>>>(a, g, sc, partials);
+    else k_bulk<float><<<gr, bl, 0, s>>>(a, g, sc, partials);
+    return (int)cudaGetLastError();
+}
+
+template <typename T>
+__global__ void k_to_f32(const T* __restrict__ in, float* __restrict__ out, Geom g)
+{
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    const int j = blockIdx.y * blockDim.y + threadIdx.y;
+    if (j >= g.NY || i >= g.NX) return;
+    out[(long long)j * g.NX + i] = (float)in[(long long)j * g.P + i];
+}
+
+int launch_to_f32(int prec, const void* in, float* out, const Geom& g, cudaStream_t s)
+{
+    const dim3 gr = pt_grid(g), bl(32, 8);
+    if (prec == 0) k_to_f32<double><<<gr, bl, 0, s>>>((const double*)in, out, g);
+    else k_to_f32<float><<<gr, bl, 0, s>>>((const float*)in, out, g);
+    return (int)cudaGetLastError();
+}
+
 size_t pt_grid_blocks(const Geom& g)
 {
     dim3 d = pt_grid(g);

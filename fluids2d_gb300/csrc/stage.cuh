@@ -79,6 +79,18 @@ int launch_qgrsw_pv(int prec, const void* ux, const void* uy, const void* h, dou
                     cudaStream_t s);
 int launch_qgrsw_update(int prec, const QgProj& a, const double* psi, const uint32_t* code,
                         int stage, const Geom& g, DevScalars* sc, cudaStream_t s);
+// Bulk diagnostics (diagnostics.py:39-57) appended to a device ring
+struct BulkArgs {
+    const void *ke, *omega, *Ux, *Uy;
+    double* ring;      // records of {t, ke, ens, vort, angular}
+    int* count;        // records in the ring
+    int cap;
+    double summsk, area, dx, dy;
+};
+int launch_bulk(int prec, const BulkArgs& a, const Geom& g, DevScalars* sc, double* partials,
+                cudaStream_t s);
+// a field as packed (NY, NX) float32 (the history's dtype "f", io.py:71)
+int launch_to_f32(int prec, const void* in, float* out, const Geom& g, cudaStream_t s);
 int launch_euler_project(int prec, void* ux, void* uy, const double* p, const uint32_t* code,
                          const Geom& g, cudaStream_t s);
 

@@ -19,6 +19,7 @@ from collections import namedtuple
 import numpy as np
 
 from . import _lib
+from . import io as _io
 from ._lib import check, lib, ptr
 from .param import Param
 
@@ -274,6 +275,7 @@ class Model:
         self.callbacks = []
         self.diags = []
         self.stop = False
+        self.io = _io.IO(param, self.mesh, None, self.time)
 
     def __del__(self):
         h = getattr(self, "_h", None)
@@ -360,20 +362,46 @@ class Model:
         tic = _time.time()
         p = self.param
         try:
+            self.save_to_file()
             while not self.time.finished and not self.stop:
                 _, _, ite = self.time._get()
                 left = self.time.ite0 + p.maxite - ite
-                # with an infinite end time, the step count alone decides
+                # with an infinite end time, the step count alone decides;
+                # callbacks, diagnostics and history run at every iteration
+                # they would see in the reference
                 n = left if not math.isfinite(p.tend) or p.tend >= 1e300 else 1
+                if self.callbacks or self.diags:
+                    n = 1
+                if p.nhis > 0:
+                    n = min(n, p.nhis - ite % p.nhis)
                 self.advance(max(1, min(n, left)))
                 self.execute_callbacks()
                 self.compute_diags()
+                self.save_to_file()
             self.sync()
         finally:
             if old is not None:
                 signal.signal(signal.SIGINT, old)
         toc = _time.time()
         self.print_perf(toc - tic)
+        self.finalize()
+
+    def save_to_file(self):
+        """model.py:109-111 with timeline.py:46-51 (every nhis iterations and
+        at the end)."""
+        p = self.param
+        if p.nhis == 0:
+            return
+        _, _, ite = self.time._get()
+        if ite % p.nhis == 0 or self.time.finished:
+            self.io.write(self)
+
+    def finalize(self):
+        """model.py:61-65, and the history file written out."""
+        for d in self.diags:
+            d.finalize()
+        if self.param.nhis > 0:
+            self.io.flush()
 
     def print_perf(self, elapsed):
         nite = self.time.ite - self.time.ite0

@@ -127,6 +127,16 @@ int f2d_field_device(f2d_model m, const char *name, void **ptr,
                      int64_t *pitch, int *elem_size);
 /* Names of the fields of the model, comma-separated. */
 int f2d_field_names(f2d_model m, char *buf, size_t len);
+/* A field as packed (ny+6, nx+6) float32, the history's dtype "f"
+ * (io.py:12-33, 71): converted on the device, then copied to host. */
+int f2d_field_get_f32(f2d_model m, const char *name, float *host);
+
+/* Bulk diagnostics (diagnostics.py:39-57) on the device: f2d_bulk_record
+ * appends {t, ke, ens, vort, angular} of the current state to a device ring
+ * of 1000 records (no host synchronisation; models with ke and omega);
+ * f2d_bulk_read copies the records out (5 doubles each) and empties it. */
+int f2d_bulk_record(f2d_model m);
+int f2d_bulk_read(f2d_model m, double *host, int capacity, int *nrec);
 
 /* mesh.f, the vertex Coriolis term of the beta-plane (qg_inversion,
  * operators.py:186-191); (ny+6, nx+6) float64. */

@@ -716,6 +716,27 @@ class Model:
         return dts
 
 
+def bulk(m):
+    """Bulk.__call__ (diagnostics.py:44-57) on an oracle model: (t, ke, ens,
+    vort, angular) with domavg = sum over the whole array / sum(msk) and the
+    y-face x / x-face y coordinates of meshes.py:57-68."""
+    mesh, s = m.mesh, m.s
+    h = m.p.halowidth
+    S = np.sum(mesh.msk, axis=None)
+
+    def domavg(x):
+        return np.sum(x, axis=None) / S
+
+    ix = np.arange(mesh.nx + 2 * h) - h
+    iy = np.arange(mesh.ny + 2 * h) - h
+    xv, _ = np.meshgrid((ix + 0.5) * mesh.dx, iy * mesh.dy)
+    _, yu = np.meshgrid(ix * mesh.dx, (iy + 0.5) * mesh.dy)
+    area = mesh.area
+    return (m.t, domavg(s["ke"]), 0.5 * domavg(s["omega"] ** 2) / area ** 2,
+            domavg(s["omega"]) / area,
+            domavg(s["U.y"] * xv) * mesh.dx - domavg(s["U.x"] * yu) * mesh.dy)
+
+
 def num_threads():
     return int(lib().oracle_num_threads())
 

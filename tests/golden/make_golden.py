@@ -340,6 +340,53 @@ def qgrsw_cases():
         run_model(c, 4, fname, cfl=0.5, extra=extra, setup=project)
 
 
+def bulk_cases():
+    """Bulk diagnostics (diagnostics.py:39-57) along a trajectory: the
+    reference's Bulk.__call__ after every step (it records every third
+    iteration). The NetCDF file it would create is skipped (netCDF4 is
+    absent): get_number_of_records is made to report an existing file."""
+    from fluids2d import diagnostics as rdiag
+    rdiag.get_number_of_records = lambda ncfile: 1
+    cases = ((wl.rsw_case(n=40, ny=32, seed=3, nislands=2), "bulk_rsw.npz", None),
+             (wl.euler_case(n=40, ny=32, seed=5, nislands=2), "bulk_euler.npz", 0.5))
+    for case, fname, cfl in cases:
+        kw = dict(xperiodic=case.get("xperiodic", False), Lx=case["Lx"],
+                  Ly=case["Ly"], tend=1e9, maxite=10 ** 9)
+        for k in ("f0", "g", "H", "beta"):
+            if k in case:
+                kw[k] = case[k]
+        if cfl is not None:
+            kw["cfl"] = cfl
+        p = make_param(case["model"], case["nx"], case["ny"], **kw)
+        m = fd.Model(p)
+        m.mesh.msk[:] = case["msk"]
+        m.mesh.finalize()
+        for k, v in case["fields"].items():
+            if "." in k:
+                getattr(getattr(m.state, k.split(".")[0]), k.split(".")[1])[:] = v
+            else:
+                getattr(m.state, k)[:] = v
+        m.integrator.diag(m.state)
+        b = rdiag.Bulk(m)
+        b()
+        dts = []
+        for _ in range(7):
+            m.set_dt()
+            dts.append(m.time.dt)
+            m.step(1)
+            b()
+        out = {"msk": case["msk"].copy(), "model": np.array(case["model"]),
+               "params": np.array([case["nx"], case["ny"], int(kw["xperiodic"])]),
+               "scalars": np.array([case["Lx"], case["Ly"], p.f0, p.beta, p.g,
+                                    p.H, p.cfl]),
+               "dt": np.array(dts),
+               "bulk": np.stack([x[:b.kt] for x in b.data], axis=1)}
+        for k, v in case["fields"].items():
+            out["ic/" + k] = v.copy()
+        np.savez_compressed(os.path.join(HERE, fname), **out)
+        print(fname, "records", b.kt)
+
+
 def integrator_cases():
     """The reference's other Runge-Kutta integrators (integrators.py:116-155)."""
     c = wl.eulerpsi_case(n=40, ny=32, seed=2, nislands=2, nvortices=5,
@@ -371,7 +418,7 @@ def lfra_cases():
 
 if __name__ == "__main__":
     which = sys.argv[1:] or ["mesh", "sweeps", "poisson", "models", "integrators",
-                             "euler", "boussinesq", "tracer", "qgrsw"]
+                             "euler", "boussinesq", "tracer", "qgrsw", "bulk"]
     if "lfra" in which:
         lfra_cases()
     if "boussinesq" in which:
@@ -380,6 +427,8 @@ if __name__ == "__main__":
         tracer_cases()
     if "qgrsw" in which:
         qgrsw_cases()
+    if "bulk" in which:
+        bulk_cases()
     if "mesh" in which:
         mesh_cases()
     if "sweeps" in which:

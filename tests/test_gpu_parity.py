@@ -349,6 +349,46 @@ def test_qgrsw_projection_and_steps_vs_oracle(xper):
     m.sync()
 
 
+@pytest.mark.parametrize("fname", ["bulk_rsw.npz", "bulk_euler.npz"])
+def test_bulk_diagnostics_vs_reference(fname, tmp_path):
+    """Bulk (diagnostics.py:39-57) reduced on the GPU into the device ring
+    along the reference's trajectory: records at ite 0, 3, 6."""
+    from fluids2d_gb300.diagnostics import Bulk
+    g = load(fname)
+    m = model_from_golden(g)
+    b = Bulk(m, ncfile=str(tmp_path / "bulk.nc"))
+    m.diags.append(b)
+    b()
+    for _ in range(len(g["dt"])):
+        m.advance(1)
+        m.compute_diags()
+    b.finalize()
+    data = b.read()
+    got = np.stack([getattr(data, n) for n in Bulk.variables], axis=1)
+    ref = g["bulk"]
+    assert got.shape == ref.shape
+    for c in range(5):
+        scale = max(np.abs(ref[:, c]).max(), 1e-300)
+        assert np.abs(got[:, c] - ref[:, c]).max() <= 1e-10 * scale, (c, got[:, c], ref[:, c])
+
+
+def test_history_float32_snapshots(tmp_path):
+    """Model.run with nhis: t, ite, dt and var_to_store as float32 records
+    (io.py:12-21, dtype "f"), every nhis iterations and at the end."""
+    case = wl.rsw_case(n=64, ny=48, seed=2, nislands=2)
+    m = _model("rsw", 64, 48, case["msk"], xperiodic=True, tend=1e300, maxite=7,
+               nhis=3, var_to_store=["h", "u"], outputfile=str(tmp_path / "hist.nc"))
+    m.state.h[:] = case["fields"]["h"]
+    m.integrator.diag(m.state)
+    m.run()
+    f = np.load(tmp_path / "hist.npz")
+    assert list(f["ite"]) == [0, 3, 6, 7]
+    assert f["h"].dtype == np.float32 and f["h"].shape == (4, 54, 70)
+    np.testing.assert_array_equal(f["h"][-1], m.state.h.astype(np.float32))
+    np.testing.assert_array_equal(f["ux"][-1], m.state.u.x.astype(np.float32))
+    assert abs(float(f["t"][-1]) - np.float32(m.time.t)) == 0
+
+
 # --------------------------------------------- size-independent checks ----
 def test_tracer_constant_and_conserved_periodic():
     """x-periodic boussinesq channel at 256^2 with a passive tracer: a tracer

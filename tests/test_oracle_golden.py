@@ -176,3 +176,23 @@ def test_model_steps_vs_reference(fname):
         m.step(1)
         _compare_state(m, g, f"step{k}", 1e-12)
     assert abs(m.t - float(g["t"])) <= 1e-13 * float(g["t"])
+
+
+@pytest.mark.parametrize("fname", ["bulk_rsw.npz", "bulk_euler.npz"])
+def test_bulk_diagnostics_vs_reference(fname):
+    """diagnostics.py:39-57 along 7 steps (records at ite 0, 3, 6)."""
+    g = load(fname)
+    m = oracle_from_golden(g)
+    recs = [O.bulk(m)]
+    for k, dt in enumerate(g["dt"], start=1):
+        m.set_dt()
+        assert abs(m.dt - dt) <= 1e-13 * dt
+        m.step(1)
+        if m.ite % 3 == 0:
+            recs.append(O.bulk(m))
+    ref = g["bulk"]
+    got = np.array(recs)
+    assert got.shape == ref.shape
+    for c in range(5):
+        scale = max(np.abs(ref[:, c]).max(), 1e-300)
+        assert np.abs(got[:, c] - ref[:, c]).max() <= 1e-12 * scale, c
