@@ -1474,6 +1474,42 @@ int f2d_time_stage(f2d_model m, int stage, int reps, int flush_l2, double* avg_m
     return 0;
 }
 
+int f2d_autotune(f2d_model m, int reps, int* th, int* nu, double* tol_in, double* ms)
+{
+    if (!m || reps < 1) return fail(1, "bad autotune arguments");
+    if (m->p.model == F2D_MODEL_RSW || projected(m->p.model))
+        return fail(1, "the autotuner tunes the multigrid of eulerpsi, qg and qgrsw");
+    const int which = m->p.model == F2D_MODEL_EULERPSI ? 0 : 1;
+    // the right-hand side and solution of the current state's diagnostics
+    int e = run_graph(m, 0);
+    if (e) return e;
+    const void* b = fb(m, which == 0 ? "vomega" : "work");
+    if (m->p.model == F2D_MODEL_QGRSW) {
+        // the right-hand side of the first stage's projection
+        int e0 = ensure_mg(m, 1);
+        if (e0) return e0;
+        e0 = launch_qgrsw_tendency(m, 1, m->cur, m->stream);
+        if (e0) return e0;
+        CKI(launch_qgrsw_pv(m->prec, fb(m, "ds3.u.x"), fb(m, "ds3.u.y"), fb(m, "ds3.h"),
+                            (double*)fb(m, "pv"), m->d_code, -m->p.f0 / m->p.H, 0.0, m->g,
+                            m->stream));
+        b = fb(m, "pv");
+    }
+    CK(cudaStreamSynchronize(m->stream));
+    BSTune t;
+    memset(&t, 0, sizeof(t));
+    const int err = bs_autotune(m->bs[which], m->stream, m->s2, fb(m, "psi"), b,
+                                field_bytes(m, 8), reps, &t);
+    drop_graphs(m);
+    if (err) return fail(err, "multigrid autotune failed");
+    m->body_launches = 0;
+    if (th) *th = t.th;
+    if (nu) *nu = t.nu;
+    if (tol_in) *tol_in = t.tol_in;
+    if (ms) *ms = t.ms;
+    return 0;
+}
+
 int f2d_time_solver(f2d_model m, int reps, int flush_l2, double* avg_ms, int64_t* nodes,
                     int* elem_bytes)
 {

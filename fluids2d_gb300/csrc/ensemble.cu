@@ -661,6 +661,33 @@ int f2d_ensemble_diag(f2d_ensemble e)
     return ens_run_graph(e, 0);
 }
 
+int f2d_ensemble_autotune(f2d_ensemble e, int reps, int* th, int* nu, double* tol_in,
+                          double* ms)
+{
+    if (!e || reps < 1) return f2d_internal_fail(1, "bad autotune arguments");
+    // the right-hand side and solution of the current state
+    int r = ens_run_graph(e, 0);
+    if (r) return r;
+    ECK(cudaStreamSynchronize(e->stream));
+    BSTune t;
+    memset(&t, 0, sizeof(t));
+    const int err = bs_autotune(e->bs, e->stream, e->s2, e->ar.psi, e->ar.rhs,
+                                e->total * sizeof(double), reps, &t);
+    // the step and diagnostic graphs captured the previous schedule
+    for (auto& k : e->gx)
+        for (auto& g : k)
+            if (g) {
+                cudaGraphExecDestroy(g);
+                g = nullptr;
+            }
+    if (err) return f2d_internal_fail(err, "multigrid autotune failed");
+    if (th) *th = t.th;
+    if (nu) *nu = t.nu;
+    if (tol_in) *tol_in = t.tol_in;
+    if (ms) *ms = t.ms;
+    return 0;
+}
+
 int f2d_ensemble_run(f2d_ensemble e, int nsteps)
 {
     if (!e) return f2d_internal_fail(1, "null ensemble");

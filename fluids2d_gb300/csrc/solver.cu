@@ -1089,6 +1089,8 @@ int bs_build(BatchSolver& s, const std::vector<BSMemberDesc>& members, const uin
     s.mode = mode;
     s.v = v;
     s.scs = scs;
+    s.descs = members;
+    s.dmask = dmask;
     s.mg.resize(s.n);
     std::vector<MGLevel> levs((size_t)s.n * BS_LMAX);
     std::vector<BSInfo> info(s.n);
@@ -1118,7 +1120,7 @@ int bs_build(BatchSolver& s, const std::vector<BSMemberDesc>& members, const uin
         long long n0 = 0;
         for (int b = 0; b < s.n; ++b)
             n0 += (long long)levs[(size_t)b * BS_LMAX].nyn * levs[(size_t)b * BS_LMAX].nxn;
-        s.th = n0 >= 2ll * 1024 * 1024 ? 64 : 32;
+        s.th = s.th_force ? s.th_force : n0 >= 2ll * 1024 * 1024 ? 64 : 32;
     }
     const int TH = s.th;
     // Tile tables of 32 x TH nodes. Level 0 (all members; the Krylov
@@ -1221,6 +1223,135 @@ int bs_build(BatchSolver& s, const std::vector<BSMemberDesc>& members, const uin
         tail_attr[ti] = s.tail_smem;
     }
     return 0;
+}
+
+// x = f * src over n doubles (the autotuner's warm start)
+__global__ void k_bs_scale(double* __restrict__ x, const double* __restrict__ src, double f,
+                           size_t n)
+{
+    for (size_t k = blockIdx.x * (size_t)blockDim.x + threadIdx.x; k < n;
+         k += (size_t)gridDim.x * blockDim.x)
+        x[k] = f * src[k];
+}
+
+// the same members with tile rows th: level-0 masks from the multigrid
+// hierarchy, the device layout and settings unchanged
+static int bs_rebuild(BatchSolver& s, int th)
+{
+    std::vector<BSMemberDesc> descs = s.descs;
+    std::vector<std::vector<uint8_t>> hm(s.n);
+    for (int b = 0; b < s.n; ++b) {
+        BSMemberDesc& d = descs[b];
+        const std::vector<uint8_t>& m0 = s.mg[b].hmask[0];
+        hm[b].assign((size_t)(d.nyn - 1) * d.pitch + d.nxn, 0);
+        for (int J = 0; J < d.nyn; ++J)
+            for (int I = 0; I < d.nxn; ++I)
+                hm[b][(size_t)J * d.pitch + I] = m0[(size_t)J * d.nxn + I];
+        d.hmask = hm[b].data();
+        d.hoff0 = 0;
+    }
+    const BSVecs v = s.v;
+    DevScalars* scs = s.scs;
+    const uint8_t* dmask = s.dmask;
+    const double tol = s.tol, tol_in = s.tol_in;
+    const int maxit = s.maxit, maxit_in = s.maxit_in, maxouter = s.maxouter, nu = s.nu;
+    s.th_force = th;
+    const int e = bs_build(s, descs, dmask, s.mode, v, scs);
+    s.tol = tol;
+    s.tol_in = tol_in;
+    s.maxit = maxit;
+    s.maxit_in = maxit_in;
+    s.maxouter = maxouter;
+    s.nu = nu;
+    return e;
+}
+
+int bs_autotune(BatchSolver& s, cudaStream_t st, cudaStream_t st2, void* x, const void* b,
+                size_t xbytes, int reps, BSTune* out)
+{
+    if (s.n == 0 || s.mg.empty()) return 9;
+    const size_t n = xbytes / sizeof(double);
+    double* saved = nullptr;
+    if (cudaMalloc(&saved, xbytes) != cudaSuccess) return 2;
+    cudaMemcpyAsync(saved, x, xbytes, cudaMemcpyDeviceToDevice, st);
+    cudaEvent_t ea, eb;
+    cudaEventCreate(&ea);
+    cudaEventCreate(&eb);
+    const double tin[3] = {1e-6, 1e-5, 1e-4};
+    const int ntin = s.mode == 1 ? 3 : 1;
+    BSTune best{0, 0, 0.0, 1e300, 0};
+    int err = 0;
+    for (int th : {32, 64}) {
+        if (th != s.th && (err = bs_rebuild(s, th))) break;
+        for (int nu : {1, 2}) {
+            for (int k = 0; k < ntin && !err; ++k) {
+                s.nu = nu;
+                s.tol_in = s.mode == 1 ? tin[k] : s.tol_in;
+                s.v.x64 = x;
+                s.v.b64 = (void*)b;
+                cudaGraph_t g = nullptr;
+                cudaGraphExec_t gx = nullptr;
+                int fixed = 0;
+                if (cudaStreamBeginCapture(st, cudaStreamCaptureModeRelaxed) != cudaSuccess) {
+                    err = 3;
+                    break;
+                }
+                int e = bs_record(s, st, st2, &fixed);
+                cudaError_t ce = cudaStreamEndCapture(st, &g);
+                if (e || ce != cudaSuccess || cudaGraphInstantiate(&gx, g, 0) != cudaSuccess) {
+                    if (g) cudaGraphDestroy(g);
+                    err = e ? e : 3;
+                    break;
+                }
+                cudaGraphDestroy(g);
+                BSGlobals zero;
+                memset(&zero, 0, sizeof(zero));
+                cudaMemcpyAsync(s.eg, &zero, sizeof(zero), cudaMemcpyHostToDevice, st);
+                double total = 0.0;
+                // one untimed solve, then the timed ones
+                for (int r = -1; r < reps; ++r) {
+                    k_bs_scale<<<1024, 256, 0, st>>>((double*)x, saved, 0.999, n);
+                    cudaEventRecord(ea, st);
+                    cudaGraphLaunch(gx, st);
+                    cudaEventRecord(eb, st);
+                    if (cudaEventSynchronize(eb) != cudaSuccess) {
+                        err = 3;
+                        break;
+                    }
+                    float ms = 0.f;
+                    cudaEventElapsedTime(&ms, ea, eb);
+                    if (r >= 0) total += ms;
+                }
+                cudaGraphExecDestroy(gx);
+                if (err) break;
+                BSGlobals hg;
+                cudaMemcpy(&hg, s.eg, sizeof(hg), cudaMemcpyDeviceToHost);
+                const double ms = total / std::max(1, reps);
+                ++best.ncand;
+                if (hg.status == 0 && ms < best.ms) best = BSTune{th, nu, s.tol_in, ms, best.ncand};
+            }
+            if (err) break;
+        }
+        if (err) break;
+    }
+    const int ncand = best.ncand;
+    if (!err && best.th == 0) err = 10;  // no candidate converged
+    best.ncand = ncand;
+    if (!err) {
+        if (best.th != s.th) err = bs_rebuild(s, best.th);
+        s.nu = best.nu;
+        s.tol_in = best.tol_in;
+    }
+    BSGlobals zero;
+    memset(&zero, 0, sizeof(zero));
+    if (s.eg) cudaMemcpyAsync(s.eg, &zero, sizeof(zero), cudaMemcpyHostToDevice, st);
+    cudaMemcpyAsync(x, saved, xbytes, cudaMemcpyDeviceToDevice, st);
+    cudaStreamSynchronize(st);
+    cudaFree(saved);
+    cudaEventDestroy(ea);
+    cudaEventDestroy(eb);
+    if (out) *out = best;
+    return err;
 }
 
 void bs_free(BatchSolver& s)

@@ -71,6 +71,9 @@ struct BatchSolver {
     int maxit = 200, maxit_in = 30, maxouter = 20;
     int nu = 2;  // red-black sweeps before and after each coarse correction (1 or 2)
     int th = 32;  // tile rows (32 or 64), chosen by bs_build
+    int th_force = 0;  // tile rows set by the autotuner (0: bs_build's rule)
+    std::vector<BSMemberDesc> descs;  // as built (host mask pointers stale)
+    const uint8_t* dmask = nullptr;
     int body_launches = 0;
     cudaStream_t s3 = nullptr;  // capture stream of the inner loop body (own per solver)
     std::vector<void*> owned;
@@ -79,6 +82,22 @@ struct BatchSolver {
 int bs_build(BatchSolver& s, const std::vector<BSMemberDesc>& members,
              const uint8_t* dmask, int mode, const BSVecs& v, DevScalars* scs);
 void bs_free(BatchSolver& s);
+
+// Autotuner of the multigrid schedule: tile rows (32, 64) x sweeps per leg
+// (1, 2) x, in the FP32 refinement form, inner tolerance (1e-6, 1e-5, 1e-4).
+// Each candidate's solve is captured as a graph and timed over `reps` solves
+// of the current right-hand side b from the warm start 0.999 x* (x* = the
+// current solution in x, FP64, xbytes); candidates that stop short of the
+// tolerance are discarded. The fastest is applied (the solver rebuilt for
+// its tile rows) and x is restored. The caller drops graphs that captured
+// the solver before.
+struct BSTune {
+    int th, nu;
+    double tol_in, ms;
+    int ncand;
+};
+int bs_autotune(BatchSolver& s, cudaStream_t st, cudaStream_t st2, void* x, const void* b,
+                size_t xbytes, int reps, BSTune* out);
 // measurement hook: mean ms of the level-0 down kernel over `reps` launches
 int bs_time_down(BatchSolver& s, cudaStream_t st, int reps, int flush_l2, double* avg_ms,
                  long long* nodes, int* es);

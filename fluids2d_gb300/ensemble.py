@@ -78,6 +78,19 @@ class Ensemble:
     def diag(self):
         check(lib().f2d_ensemble_diag(self._h))
 
+    def autotune(self, reps=3):
+        """Pick the multigrid schedule (tile rows, sweeps per leg, inner
+        tolerance) of the batched solver by timing each candidate's solve of
+        the current state on the GPU (f2d_ensemble_autotune); the state is
+        unchanged. Returns the chosen schedule."""
+        th, nu = ctypes.c_int(), ctypes.c_int()
+        tin, ms = ctypes.c_double(), ctypes.c_double()
+        check(lib().f2d_ensemble_autotune(self._h, int(reps), ctypes.byref(th),
+                                          ctypes.byref(nu), ctypes.byref(tin),
+                                          ctypes.byref(ms)))
+        return {"tile_rows": th.value, "sweeps": nu.value, "tol_in": tin.value,
+                "ms_per_solve": ms.value}
+
     def run(self, nsteps):
         check(lib().f2d_ensemble_run(self._h, int(nsteps)))
 

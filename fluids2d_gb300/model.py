@@ -338,6 +338,20 @@ class Model:
         self._push()
         check(lib().f2d_set_dt(self._h))
 
+    def autotune(self, reps=3):
+        """Pick the multigrid schedule (tile rows, sweeps per leg, inner
+        tolerance) of the Poisson/Helmholtz solver by timing each
+        candidate's solve of the current state on the GPU (f2d_autotune);
+        the state is unchanged. Returns the chosen schedule."""
+        self._push()
+        th, nu = ctypes.c_int(), ctypes.c_int()
+        tin, ms = ctypes.c_double(), ctypes.c_double()
+        check(lib().f2d_autotune(self._h, int(reps), ctypes.byref(th), ctypes.byref(nu),
+                                 ctypes.byref(tin), ctypes.byref(ms)))
+        self._device_newer = True
+        return {"tile_rows": th.value, "sweeps": nu.value, "tol_in": tin.value,
+                "ms_per_solve": ms.value}
+
     def advance(self, nsteps):
         """nsteps iterations of the run-loop body: set_dt then step(1)."""
         self._push()

@@ -175,6 +175,15 @@ int f2d_sync(f2d_model m);
  * No reference counterpart: the measurement hook of the benchmark. */
 int f2d_time_stage(f2d_model m, int stage, int reps, int flush_l2,
                    double *avg_ms);
+/* Autotuner of the multigrid schedule (tile rows 32/64, sweeps per leg 1/2,
+ * and in the FP32 form the inner tolerance 1e-6/1e-5/1e-4): each candidate's
+ * solve of the current state's right-hand side is captured as a graph and
+ * timed over `reps` solves from the warm start 0.999 psi; the fastest that
+ * reaches the tolerance is kept (the step graphs are re-captured). The state
+ * is unchanged. Outputs may be NULL. Models with a vertex Poisson/Helmholtz
+ * solve (eulerpsi, qg, qgrsw) and ensembles. */
+int f2d_autotune(f2d_model m, int reps, int *tile_rows, int *sweeps, double *tol_in,
+                 double *ms_per_solve);
 /* Time `reps` launches of the Poisson solver's level-0 down kernel
  * (pre-smoothing + residual + restriction of the V-cycle, the solver's largest
  * share) on the current right-hand side, L2 flushed between launches when
@@ -217,6 +226,9 @@ int f2d_ensemble_field_get_async(f2d_ensemble e, int member, const char *name,
                                  double *host);
 /* integrator.diag of every member (equations.py:80-84, 99-101) */
 int f2d_ensemble_diag(f2d_ensemble e);
+/* The autotuner (see f2d_autotune) on the ensemble's batched solver. */
+int f2d_ensemble_autotune(f2d_ensemble e, int reps, int *tile_rows, int *sweeps,
+                          double *tol_in, double *ms_per_solve);
 /* n iterations of set_dt + step(1) for every member (model.py:45-51) */
 int f2d_ensemble_run(f2d_ensemble e, int nsteps);
 int f2d_ensemble_time_get(f2d_ensemble e, int member, double *t, double *dt,

@@ -670,6 +670,64 @@ def test_ensemble_members_match_single_models(precision, integrator):
         assert ite == 4 and abs(t - m.time.t) <= 1e-12 * t
 
 
+def test_autotune_ensemble_keeps_results():
+    """The autotuner changes the multigrid schedule, not the solution: the
+    tuned FP32 ensemble matches an untuned one to the FP32 tolerance."""
+    members = [wl.eulerpsi_case(n=64, ny=48, seed=31, nislands=2),
+               wl.eulerpsi_case(n=128, ny=96, seed=32, nislands=1)]
+    e1 = _ensemble(members, "fp32")
+    e1.run(3)
+    e1.sync()
+    e2 = _ensemble(members, "fp32")
+    cfg = e2.autotune(reps=1)
+    assert cfg["tile_rows"] in (32, 64) and cfg["sweeps"] in (1, 2)
+    assert cfg["tol_in"] in (1e-6, 1e-5, 1e-4) and cfg["ms_per_solve"] > 0
+    e2.run(3)
+    e2.sync()
+    for b in range(len(members)):
+        for k in ("omega", "psi"):
+            assert rel_l2(e2.get_field(b, k), e1.get_field(b, k)) <= 1e-6, (b, k)
+
+
+@pytest.mark.parametrize("kind", ["qg", "qgrsw"])
+def test_autotune_model_vs_oracle(kind):
+    """A tuned FP64 model still matches the oracle at the step tolerance."""
+    if kind == "qg":
+        case = wl.qg_case(n=96, ny=96, seed=33, nislands=3)
+    else:
+        case = wl.rsw_case(n=96, ny=80, seed=34, nislands=2, xperiodic=False, f0=10.0)
+        z = np.zeros_like(case["fields"]["h"])
+        case["fields"] = {"u.x": z, "u.y": z.copy(), "h": case["fields"]["h"]}
+    om = _oracle_like(case, kind, cfl=0.5)
+    if kind == "qgrsw":
+        O.qg_projection(om.mesh, om.s["u.x"], om.s["u.y"], om.s["h"], om.s["pv"],
+                        om.s["psi"])
+        om.diag()
+    kw = dict(Lx=case["Lx"], Ly=case["Ly"], tend=1e300, maxite=10 ** 9, cfl=0.5)
+    for k in ("f0", "g", "H", "beta"):
+        if k in case:
+            kw[k] = case[k]
+    m = _model(kind, case["nx"], case["ny"], case["msk"], **kw)
+    if "f" in case:
+        m.mesh.f = case["f"]
+    s = m.state
+    for k, v in case["fields"].items():
+        if "." in k:
+            getattr(getattr(s, k.split(".")[0]), k.split(".")[1])[:] = v
+        else:
+            getattr(s, k)[:] = v
+    if kind == "qgrsw":
+        m.qg_projection()
+    m.integrator.diag(m.state)
+    cfg = m.autotune(reps=1)
+    assert cfg["tile_rows"] in (32, 64) and cfg["sweeps"] in (1, 2)
+    for _ in range(3):
+        om.run_steps(1)
+        m.advance(1)
+        compare(m, lambda k: om.s.get(k), STEP_TOL)
+    m.sync()
+
+
 def test_ensemble_vs_oracle():
     members = [wl.eulerpsi_case(n=48, ny=40, seed=21, nislands=2),
                wl.eulerpsi_case(n=72, ny=64, seed=22, nislands=1)]
