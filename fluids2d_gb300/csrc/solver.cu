@@ -62,6 +62,14 @@ __device__ __forceinline__ bool in_level(const MGLevel& L, int J, int& I)
     return I >= 0 && I < L.nxn;
 }
 
+// true when the staged region of halo H around the tile at (J0, I0) lies
+// inside the level (no periodic wrap, no out-of-level node)
+template <int H, int W, int WY>
+__device__ __forceinline__ bool region_inside(const MGLevel& L, int J0, int I0)
+{
+    return J0 - H >= 0 && J0 - H + WY <= L.nyn && I0 - H >= 0 && I0 - H + W <= L.nxn;
+}
+
 // Stage mask and up to two arrays of a level on the region of halo H around
 // the tile at (J0, I0). Values at non-fluid nodes are staged as 0.
 template <int H, int TH, typename S, typename T2>
@@ -210,24 +218,43 @@ k_bs_down(const int4* __restrict__ tiles, const BSInfo* __restrict__ info,
         // stage b and the mask; x = b/diag on red fluid nodes, 0 elsewhere
         constexpr int IT = (N + 255) / 256;
         const S* __restrict__ gb = lb<S>(F);
+        if (region_inside<H, W, WY>(F, J0, I0)) {
+            // the whole region inside the level: offsets from one base
+            const long long base = nidx(F, J0 - H, I0 - H);
+            const int pitch = (int)F.pitch;
 #pragma unroll
-        for (int k2 = 0; k2 < IT; ++k2) {
-            const int e = t + k2 * 256;
-            if (e < N) {
-                const int r = e / W, c = e - r * W;
-                const int J = J0 - H + r;
-                int I = I0 - H + c;
-                uint8_t mv = 0;
-                S bv = S(0);
-                if (in_level(F, J, I)) {
-                    const long long k = nidx(F, J, I);
-                    mv = F.m[k];
-                    bv = gb[k];
+            for (int k2 = 0; k2 < IT; ++k2) {
+                const int e = t + k2 * 256;
+                if (e < N) {
+                    const int r = e / W, c = e - r * W;
+                    const long long k = base + (r * pitch + c);
+                    const uint8_t mv = F.m[k];
+                    const S bv = mv ? gb[k] : S(0);
+                    sm[e] = mv;
+                    sb[e] = bv;
+                    sx[e] = (((r + c) & 1) == 0) ? bv * id : S(0);
                 }
-                bv = mv ? bv : S(0);
-                sm[e] = mv;
-                sb[e] = bv;
-                sx[e] = (((r + c) & 1) == 0) ? bv * id : S(0);
+            }
+        } else {
+#pragma unroll
+            for (int k2 = 0; k2 < IT; ++k2) {
+                const int e = t + k2 * 256;
+                if (e < N) {
+                    const int r = e / W, c = e - r * W;
+                    const int J = J0 - H + r;
+                    int I = I0 - H + c;
+                    uint8_t mv = 0;
+                    S bv = S(0);
+                    if (in_level(F, J, I)) {
+                        const long long k = nidx(F, J, I);
+                        mv = F.m[k];
+                        bv = gb[k];
+                    }
+                    bv = mv ? bv : S(0);
+                    sm[e] = mv;
+                    sb[e] = bv;
+                    sx[e] = (((r + c) & 1) == 0) ? bv * id : S(0);
+                }
             }
         }
     }
@@ -331,45 +358,67 @@ k_bs_up(const int4* __restrict__ tiles, const BSInfo* __restrict__ info,
         }
     }
     const S cx = Coef<S>::cx(F), cy = Coef<S>::cy(F), id = Coef<S>::idiag(F);
+    constexpr int IT = (N + 255) / 256;
     {
-        constexpr int IT = (N + 255) / 256;
         const S* __restrict__ gx = (const S*)F.xa;
         const S* __restrict__ gb = lb<S>(F);
+        if (region_inside<H, W, WY>(F, J0, I0)) {
+            // the whole region inside the level: offsets from one base
+            const long long base = nidx(F, J0 - H, I0 - H);
+            const int pitch = (int)F.pitch;
 #pragma unroll
-        for (int k2 = 0; k2 < IT; ++k2) {
-            const int e = t + k2 * 256;
-            if (e < N) {
-                const int r = e / W, c = e - r * W;
-                const int J = J0 - H + r;
-                int I = I0 - H + c;
-                uint8_t mv = 0;
-                S xv = S(0), bv = S(0);
-                if (in_level(F, J, I)) {
-                    const long long k = nidx(F, J, I);
-                    mv = F.m[k];
-                    xv = gx[k];
-                    bv = gb[k];
+            for (int k2 = 0; k2 < IT; ++k2) {
+                const int e = t + k2 * 256;
+                if (e < N) {
+                    const int r = e / W, c = e - r * W;
+                    const long long k = base + (r * pitch + c);
+                    const uint8_t mv = F.m[k];
+                    sm[e] = mv;
+                    sx[e] = mv ? gx[k] : S(0);
+                    sb[e] = mv ? gb[k] : S(0);
                 }
-                sm[e] = mv;
-                sx[e] = mv ? xv : S(0);
-                sb[e] = mv ? bv : S(0);
+            }
+        } else {
+#pragma unroll
+            for (int k2 = 0; k2 < IT; ++k2) {
+                const int e = t + k2 * 256;
+                if (e < N) {
+                    const int r = e / W, c = e - r * W;
+                    const int J = J0 - H + r;
+                    int I = I0 - H + c;
+                    uint8_t mv = 0;
+                    S xv = S(0), bv = S(0);
+                    if (in_level(F, J, I)) {
+                        const long long k = nidx(F, J, I);
+                        mv = F.m[k];
+                        xv = gx[k];
+                        bv = gb[k];
+                    }
+                    sm[e] = mv;
+                    sx[e] = mv ? xv : S(0);
+                    sb[e] = mv ? bv : S(0);
+                }
             }
         }
     }
     __syncthreads();
-    for (int e = t; e < N; e += 256) {
-        if (!sm[e]) continue;
-        const int r = e / W, c = e - r * W;
-        // coarse indices relative to the staged coarse region
-        const int J = J0 - H + r, I = I0 - H + c;
-        const int q = ((J >> 1) - cj0) * CW + ((I >> 1) - ci0);
-        const int oj = J & 1, oi = I & 1;
-        S v;
-        if (!oj && !oi) v = sc2[q];
-        else if (!oj) v = S(0.5) * (sc2[q] + sc2[q + 1]);
-        else if (!oi) v = S(0.5) * (sc2[q] + sc2[q + CW]);
-        else v = S(0.25) * ((sc2[q] + sc2[q + 1]) + (sc2[q + CW] + sc2[q + CW + 1]));
-        sx[e] += v;
+    // x += P (coarse x) at the fluid nodes: bilinear, written branch-free as
+    // the average of two row averages (an even index repeats its node, so
+    // the weights 1, 1/2, 1/4 come out exactly)
+#pragma unroll
+    for (int k2 = 0; k2 < IT; ++k2) {
+        const int e = t + k2 * 256;
+        if (e < N) {
+            const int r = e / W, c = e - r * W;
+            // coarse indices relative to the staged coarse region
+            const int J = J0 - H + r, I = I0 - H + c;
+            const int q = ((J >> 1) - cj0) * CW + ((I >> 1) - ci0);
+            const int oj = (J & 1) * CW, oi = I & 1;
+            const S a = sc2[q], b = sc2[q + oi];
+            const S h0 = S(0.5) * (a + b);
+            const S h1 = S(0.5) * (sc2[q + oj] + sc2[q + oj + oi]);
+            sx[e] += sm[e] ? S(0.5) * (h0 + h1) : S(0);
+        }
     }
     __syncthreads();
 #pragma unroll
