@@ -229,7 +229,8 @@ k_bs_down(const int4* __restrict__ tiles, const BSInfo* __restrict__ info,
                     const int r = e / W, c = e - r * W;
                     const long long k = base + (r * pitch + c);
                     const uint8_t mv = F.m[k];
-                    const S bv = mv ? gb[k] : S(0);
+                    S bv = gb[k];
+                    bv = mv ? bv : S(0);
                     sm[e] = mv;
                     sb[e] = bv;
                     sx[e] = (((r + c) & 1) == 0) ? bv * id : S(0);
@@ -373,9 +374,10 @@ k_bs_up(const int4* __restrict__ tiles, const BSInfo* __restrict__ info,
                     const int r = e / W, c = e - r * W;
                     const long long k = base + (r * pitch + c);
                     const uint8_t mv = F.m[k];
+                    const S xv = gx[k], bv = gb[k];
                     sm[e] = mv;
-                    sx[e] = mv ? gx[k] : S(0);
-                    sb[e] = mv ? gb[k] : S(0);
+                    sx[e] = mv ? xv : S(0);
+                    sb[e] = mv ? bv : S(0);
                 }
             }
         } else {
