@@ -102,31 +102,77 @@ __device__ __forceinline__ void stage_region(const MGLevel& L, int J0, int I0,
     }
 }
 
+// Red-black split layout of a staged region (W x WY nodes, W even): the
+// nodes of each colour of a row are packed, HW = W/2 per row, so that the
+// lanes of a half sweep touch consecutive words (with the interleaved layout
+// every access of a sweep was a 2-way bank conflict). Colour of region node
+// (r, c): (r + c) & 1 (0 = red); its packed index r*HW + c/2. Each colour
+// array of S takes CS bytes and each mask array CM bytes, both 64 past a
+// multiple of 128, so that a warp storing both colours of consecutive nodes
+// touches each bank once. Layout: x red, x black, b red, b black, mask red,
+// mask black (then the up kernel's coarse region).
+template <typename S, int W, int WY>
+struct RBL {
+    static constexpr int HW = W / 2, NH = WY * HW;
+    static constexpr size_t CS = ((NH * sizeof(S) + 127) / 128) * 128 + 64;
+    static constexpr size_t CM = ((NH + 127) / 128) * 128 + 64;
+    static constexpr size_t BYTES = 4 * CS + 2 * CM;
+    static_assert(W % 2 == 0, "even region width");
+};
+
+template <typename S, int W, int WY>
+struct RBRegion {
+    S* x[2];
+    S* b[2];
+    uint8_t* m[2];
+    __device__ __forceinline__ explicit RBRegion(unsigned char* base)
+    {
+        using L = RBL<S, W, WY>;
+        x[0] = (S*)base;
+        x[1] = (S*)(base + L::CS);
+        b[0] = (S*)(base + 2 * L::CS);
+        b[1] = (S*)(base + 3 * L::CS);
+        m[0] = base + 4 * L::CS;
+        m[1] = base + 4 * L::CS + L::CM;
+    }
+    // packed index and colour of region node (r, c)
+    __device__ __forceinline__ static int idx(int r, int c) { return r * (W / 2) + (c >> 1); }
+    __device__ __forceinline__ static int col(int r, int c) { return (r + c) & 1; }
+};
+
 // Red-black half sweep of colour `color` (0: (J+I) even) on the staged
 // region: every node of that colour in rows 1..WY-2 gets
-// x = (b - offdiag(x)) / diag at fluid nodes (non-fluid nodes keep x = 0). The tile origin is even, so the colour of
-// a region node is the parity of its region coordinates. Nodes within s of
-// the region edge are updated from neighbours that are no longer exact (or,
-// in columns 0 and W-1, from the neighbouring row); by induction the values
-// at distance >= s from the edge are exact after half sweep s, and the kernels
-// only read those afterwards. Updating the whole region keeps the loop free
-// of range tests, with a compile-time trip count.
+// x = (b - offdiag(x)) / diag at fluid nodes (non-fluid nodes keep x = 0).
+// The tile origin is even, so the colour of a region node is the parity of
+// its region coordinates. In row rr the colour's nodes sit at columns
+// 2j + p, p = (color + rr) & 1; the other colour's west/east neighbours are
+// its packed nodes j - 1 + p and j + p of the row, the north/south ones its
+// packed node j of rows rr -+ 1. Nodes within s of the region edge are
+// updated from neighbours that are no longer exact (or, in columns 0 and
+// W-1, from the neighbouring row); by induction the values at distance >= s
+// from the edge are exact after half sweep s, and the kernels only read
+// those afterwards. Updating the whole region keeps the loop free of range
+// tests, with a compile-time trip count.
 template <typename S, int W, int WY>
-__device__ __forceinline__ void half_sweep(S* sx, const S* sb, const uint8_t* sm, int color,
-                                           S cx, S cy, S id)
+__device__ __forceinline__ void half_sweep(const RBRegion<S, W, WY>& R, int color, S cx,
+                                           S cy, S id)
 {
     constexpr int HW = W / 2, n = (WY - 2) * HW, IT = (n + 255) / 256;
     const int t = tid256();
+    S* __restrict__ xo = R.x[color];
+    const S* __restrict__ xn = R.x[color ^ 1];
+    const S* __restrict__ bo = R.b[color];
+    const uint8_t* __restrict__ mo = R.m[color];
 #pragma unroll
     for (int it = 0; it < IT; ++it) {
         const int e = t + 256 * it;
         if (n % 256 != 0 && e >= n) break;
         const int rr = 1 + e / HW;
-        const int cc = 2 * (e % HW) + ((color + rr) & 1);
-        const int q = rr * W + cc;
-        const S off = cx * (sx[q - 1] + sx[q + 1]) + cy * (sx[q - W] + sx[q + W]);
-        const S v = (sb[q] - off) * id;
-        sx[q] = sm[q] ? v : S(0);
+        const int q = HW + e;  // = rr*HW + j
+        const int p = (color + rr) & 1;
+        const S off = cx * (xn[q - 1 + p] + xn[q + p]) + cy * (xn[q - HW] + xn[q + HW]);
+        const S v = (bo[q] - off) * id;
+        xo[q] = mo[q] ? v : S(0);
     }
 }
 
@@ -203,89 +249,82 @@ k_bs_down(const int4* __restrict__ tiles, const BSInfo* __restrict__ info,
           const MGLevel* __restrict__ levs, int l, const DevScalars* __restrict__ scs, int ir)
 {
     constexpr int H = 2 * NU + 1, W = Reg<H, TH>::WX, WY = Reg<H, TH>::WY,
-                  N = Reg<H, TH>::N, TQ = TH / 8;
-    extern __shared__ __align__(16) unsigned char dsm[];
-    S* sx = (S*)dsm;
-    S* sb = sx + N;
-    uint8_t* sm = (uint8_t*)(sb + N);
+                  N = Reg<H, TH>::N, TQ = TH / 8, HW = W / 2;
+    extern __shared__ __align__(128) unsigned char dsm[];
+    const RBRegion<S, W, WY> R(dsm);
     const int4 tl = tiles[blockIdx.x];
     if (info[tl.x].ltail <= l || bs_skip(scs[tl.x], ir)) return;
     const MGLevel F = levs[tl.x * BS_LMAX + l];
     const int I0 = tl.y, J0 = tl.z, t = tid256();
-    const S cx = Coef<S>::cx(F), cy = Coef<S>::cy(F), d = Coef<S>::diag(F),
-            id = Coef<S>::idiag(F);
+    const S cx = Coef<S>::cx(F), cy = Coef<S>::cy(F), id = Coef<S>::idiag(F);
     {
         // stage b and the mask; x = b/diag on red fluid nodes, 0 elsewhere
         constexpr int IT = (N + 255) / 256;
         const S* __restrict__ gb = lb<S>(F);
-        if (region_inside<H, W, WY>(F, J0, I0)) {
-            // the whole region inside the level: offsets from one base
-            const long long base = nidx(F, J0 - H, I0 - H);
-            const int pitch = (int)F.pitch;
+        const bool inner = region_inside<H, W, WY>(F, J0, I0);
+        const long long base = F.off + (long long)(J0 - H) * F.pitch + (I0 - H);
+        const int pitch = (int)F.pitch;
 #pragma unroll
-            for (int k2 = 0; k2 < IT; ++k2) {
-                const int e = t + k2 * 256;
-                if (e < N) {
-                    const int r = e / W, c = e - r * W;
+        for (int k2 = 0; k2 < IT; ++k2) {
+            const int e = t + k2 * 256;
+            if (e < N) {
+                const int r = e / W, c = e - r * W;
+                uint8_t mv = 0;
+                S bv = S(0);
+                if (inner) {
+                    // the whole region inside the level: offsets from one base
                     const long long k = base + (r * pitch + c);
-                    const uint8_t mv = F.m[k];
-                    S bv = gb[k];
-                    bv = mv ? bv : S(0);
-                    sm[e] = mv;
-                    sb[e] = bv;
-                    sx[e] = (((r + c) & 1) == 0) ? bv * id : S(0);
-                }
-            }
-        } else {
-#pragma unroll
-            for (int k2 = 0; k2 < IT; ++k2) {
-                const int e = t + k2 * 256;
-                if (e < N) {
-                    const int r = e / W, c = e - r * W;
-                    const int J = J0 - H + r;
+                    mv = F.m[k];
+                    bv = gb[k];
+                } else {
                     int I = I0 - H + c;
-                    uint8_t mv = 0;
-                    S bv = S(0);
-                    if (in_level(F, J, I)) {
-                        const long long k = nidx(F, J, I);
+                    if (in_level(F, J0 - H + r, I)) {
+                        const long long k = nidx(F, J0 - H + r, I);
                         mv = F.m[k];
                         bv = gb[k];
                     }
-                    bv = mv ? bv : S(0);
-                    sm[e] = mv;
-                    sb[e] = bv;
-                    sx[e] = (((r + c) & 1) == 0) ? bv * id : S(0);
                 }
+                bv = mv ? bv : S(0);
+                const int k = R.col(r, c), q = R.idx(r, c);
+                R.m[k][q] = mv;
+                R.b[k][q] = bv;
+                R.x[k][q] = k == 0 ? bv * id : S(0);
             }
         }
     }
     __syncthreads();
 #pragma unroll
     for (int s = 1; s < 2 * NU; ++s) {
-        half_sweep<S, W, WY>(sx, sb, sm, s & 1, cx, cy, id);
+        half_sweep<S, W, WY>(R, s & 1, cx, cy, id);
         __syncthreads();
     }
     // residual at the red nodes (in place of b; exact at distance >= 2 NU
     // from the region edge, which is all the restriction reads)
     {
-        constexpr int HW = W / 2, n = (WY - 2) * HW, IT = (n + 255) / 256;
+        constexpr int n = (WY - 2) * HW, IT = (n + 255) / 256;
         const S md = Coef<S>::md(F);
+        const S* __restrict__ xr = R.x[0];
+        const S* __restrict__ xb = R.x[1];
+        S* __restrict__ br = R.b[0];
+        const uint8_t* __restrict__ mr = R.m[0];
 #pragma unroll
         for (int it = 0; it < IT; ++it) {
             const int e = t + 256 * it;
             if (n % 256 != 0 && e >= n) break;
             const int rr = 1 + e / HW;
-            const int cc = 2 * (e % HW) + (rr & 1);
-            const int q = rr * W + cc;
-            const S v = sb[q] - apply_diff<S>(cx, cy, md, sx[q], sx[q - 1], sx[q + 1],
-                                              sx[q - W], sx[q + W]);
-            sb[q] = sm[q] ? v : S(0);
+            const int q = HW + e;
+            const int p = rr & 1;
+            const S v = br[q] - apply_diff<S>(cx, cy, md, xr[q], xb[q - 1 + p], xb[q + p],
+                                              xb[q - HW], xb[q + HW]);
+            br[q] = mr[q] ? v : S(0);
         }
     }
     __syncthreads();
     {
-        // coarse nodes with their centre in the tile: (TH/2) x (BS_TW/2)
+        // coarse nodes with their centre in the tile: (TH/2) x (BS_TW/2);
+        // the centre and its four diagonal neighbours are red
         const MGLevel C = levs[tl.x * BS_LMAX + l + 1];
+        const S* __restrict__ br = R.b[0];
         static_assert((TH / 2) * (BS_TW / 2) % 256 == 0, "coarse nodes per thread");
 #pragma unroll
         for (int k2 = 0; k2 < (TH / 2) * (BS_TW / 2) / 256; ++k2) {
@@ -296,10 +335,10 @@ k_bs_down(const int4* __restrict__ tiles, const BSInfo* __restrict__ info,
                 const long long k = nidx(C, cJ, cI);
                 S v = S(0);
                 if (C.m[k]) {
-                    const int q = (H + 2 * a) * W + H + 2 * b;
-                    const S c4 =
-                        (sb[q - W - 1] + sb[q - W + 1]) + (sb[q + W - 1] + sb[q + W + 1]);
-                    v = sb[q] + S(0.25) * c4;
+                    const int r0 = H + 2 * a, c0 = H + 2 * b;
+                    const S c4 = (br[R.idx(r0 - 1, c0 - 1)] + br[R.idx(r0 - 1, c0 + 1)]) +
+                                 (br[R.idx(r0 + 1, c0 - 1)] + br[R.idx(r0 + 1, c0 + 1)]);
+                    v = br[R.idx(r0, c0)] + S(0.25) * c4;
                 }
                 lb<S>(C)[k] = v;
             }
@@ -310,7 +349,8 @@ k_bs_down(const int4* __restrict__ tiles, const BSInfo* __restrict__ info,
     for (int qr = 0; qr < TQ; ++qr) {
         const int r = threadIdx.y + 8 * qr, c = threadIdx.x;
         const int J = J0 + r, I = I0 + c;
-        if (J < F.nyn && I < F.nxn) xa[nidx(F, J, I)] = sx[(r + H) * W + c + H];
+        if (J < F.nyn && I < F.nxn)
+            xa[nidx(F, J, I)] = R.x[R.col(r + H, c + H)][R.idx(r + H, c + H)];
     }
 }
 
@@ -331,11 +371,9 @@ k_bs_up(const int4* __restrict__ tiles, const BSInfo* __restrict__ info,
     constexpr int H = 2 * NU, W = Reg<H, TH>::WX, WY = Reg<H, TH>::WY, N = Reg<H, TH>::N;
     constexpr int CW = BS_TW / 2 + 1 + H, CWY = TH / 2 + 1 + H, CN = CW * CWY, TQ = TH / 8;
     constexpr int CIT = (CN + 255) / 256;
-    extern __shared__ __align__(16) unsigned char dsm[];
-    S* sx = (S*)dsm;
-    S* sb = sx + N;
-    S* sc2 = sb + N;
-    uint8_t* sm = (uint8_t*)(sc2 + CN);
+    extern __shared__ __align__(128) unsigned char dsm[];
+    const RBRegion<S, W, WY> R(dsm);
+    S* sc2 = (S*)(dsm + RBL<S, W, WY>::BYTES);
     const int4 tl = tiles[blockIdx.x];
     DevScalars& sc = scs[tl.x];
     const BSInfo in = info[tl.x];
@@ -363,43 +401,35 @@ k_bs_up(const int4* __restrict__ tiles, const BSInfo* __restrict__ info,
     {
         const S* __restrict__ gx = (const S*)F.xa;
         const S* __restrict__ gb = lb<S>(F);
-        if (region_inside<H, W, WY>(F, J0, I0)) {
-            // the whole region inside the level: offsets from one base
-            const long long base = nidx(F, J0 - H, I0 - H);
-            const int pitch = (int)F.pitch;
+        const bool inner = region_inside<H, W, WY>(F, J0, I0);
+        const long long base = F.off + (long long)(J0 - H) * F.pitch + (I0 - H);
+        const int pitch = (int)F.pitch;
 #pragma unroll
-            for (int k2 = 0; k2 < IT; ++k2) {
-                const int e = t + k2 * 256;
-                if (e < N) {
-                    const int r = e / W, c = e - r * W;
+        for (int k2 = 0; k2 < IT; ++k2) {
+            const int e = t + k2 * 256;
+            if (e < N) {
+                const int r = e / W, c = e - r * W;
+                uint8_t mv = 0;
+                S xv = S(0), bv = S(0);
+                if (inner) {
+                    // the whole region inside the level: offsets from one base
                     const long long k = base + (r * pitch + c);
-                    const uint8_t mv = F.m[k];
-                    const S xv = gx[k], bv = gb[k];
-                    sm[e] = mv;
-                    sx[e] = mv ? xv : S(0);
-                    sb[e] = mv ? bv : S(0);
-                }
-            }
-        } else {
-#pragma unroll
-            for (int k2 = 0; k2 < IT; ++k2) {
-                const int e = t + k2 * 256;
-                if (e < N) {
-                    const int r = e / W, c = e - r * W;
-                    const int J = J0 - H + r;
+                    mv = F.m[k];
+                    xv = gx[k];
+                    bv = gb[k];
+                } else {
                     int I = I0 - H + c;
-                    uint8_t mv = 0;
-                    S xv = S(0), bv = S(0);
-                    if (in_level(F, J, I)) {
-                        const long long k = nidx(F, J, I);
+                    if (in_level(F, J0 - H + r, I)) {
+                        const long long k = nidx(F, J0 - H + r, I);
                         mv = F.m[k];
                         xv = gx[k];
                         bv = gb[k];
                     }
-                    sm[e] = mv;
-                    sx[e] = mv ? xv : S(0);
-                    sb[e] = mv ? bv : S(0);
                 }
+                const int k = R.col(r, c), q = R.idx(r, c);
+                R.m[k][q] = mv;
+                R.x[k][q] = mv ? xv : S(0);
+                R.b[k][q] = mv ? bv : S(0);
             }
         }
     }
@@ -419,13 +449,14 @@ k_bs_up(const int4* __restrict__ tiles, const BSInfo* __restrict__ info,
             const S a = sc2[q], b = sc2[q + oi];
             const S h0 = S(0.5) * (a + b);
             const S h1 = S(0.5) * (sc2[q + oj] + sc2[q + oj + oi]);
-            sx[e] += sm[e] ? S(0.5) * (h0 + h1) : S(0);
+            const int k = R.col(r, c), qq = R.idx(r, c);
+            R.x[k][qq] += R.m[k][qq] ? S(0.5) * (h0 + h1) : S(0);
         }
     }
     __syncthreads();
 #pragma unroll
     for (int s = 1; s <= 2 * NU; ++s) {
-        half_sweep<S, W, WY>(sx, sb, sm, s & 1, cx, cy, id);
+        half_sweep<S, W, WY>(R, s & 1, cx, cy, id);
         __syncthreads();
     }
     S* x = lx<S>(F);
@@ -434,10 +465,10 @@ k_bs_up(const int4* __restrict__ tiles, const BSInfo* __restrict__ info,
     for (int qr = 0; qr < TQ; ++qr) {
         const int r = threadIdx.y + 8 * qr, c = threadIdx.x;
         const int J = J0 + r, I = I0 + c;
-        const int q = (r + H) * W + c + H;
+        const int k = R.col(r + H, c + H), q = R.idx(r + H, c + H);
         if (J < F.nyn && I < F.nxn) {
-            x[nidx(F, J, I)] = sx[q];
-            if (RZ) acc += sb[q] * sx[q];  // 0 at non-fluid nodes
+            x[nidx(F, J, I)] = R.x[k][q];
+            if (RZ) acc += R.b[k][q] * R.x[k][q];  // 0 at non-fluid nodes
         }
     }
     if (RZ) {
@@ -863,15 +894,15 @@ static bool bs_eager()
 template <typename S, int NU, int TH>
 static size_t down_smem()
 {
-    constexpr size_t N = Reg<2 * NU + 1, TH>::N;
-    return 2 * N * sizeof(S) + N;
+    constexpr int H = 2 * NU + 1;
+    return RBL<S, Reg<H, TH>::WX, Reg<H, TH>::WY>::BYTES;
 }
 template <typename S, int NU, int TH>
 static size_t up_smem()
 {
     constexpr int H = 2 * NU;
-    constexpr size_t N = Reg<H, TH>::N, CN = (size_t)(BS_TW / 2 + 1 + H) * (TH / 2 + 1 + H);
-    return (2 * N + CN) * sizeof(S) + N;
+    constexpr size_t CN = (size_t)(BS_TW / 2 + 1 + H) * (TH / 2 + 1 + H);
+    return RBL<S, Reg<H, TH>::WX, Reg<H, TH>::WY>::BYTES + CN * sizeof(S);
 }
 
 template <typename S, int NU, int TH>
