@@ -122,19 +122,14 @@ struct RBL {
 
 template <typename S, int W, int WY>
 struct RBRegion {
-    S* x[2];
-    S* b[2];
-    uint8_t* m[2];
-    __device__ __forceinline__ explicit RBRegion(unsigned char* base)
-    {
-        using L = RBL<S, W, WY>;
-        x[0] = (S*)base;
-        x[1] = (S*)(base + L::CS);
-        b[0] = (S*)(base + 2 * L::CS);
-        b[1] = (S*)(base + 3 * L::CS);
-        m[0] = base + 4 * L::CS;
-        m[1] = base + 4 * L::CS + L::CM;
-    }
+    unsigned char* base;
+    using L = RBL<S, W, WY>;
+    __device__ __forceinline__ explicit RBRegion(unsigned char* p) : base(p) {}
+    // colour arrays by arithmetic on the base (no runtime-indexed pointer
+    // array, which would live in local memory)
+    __device__ __forceinline__ S* x(int k) const { return (S*)(base + k * L::CS); }
+    __device__ __forceinline__ S* b(int k) const { return (S*)(base + (2 + k) * L::CS); }
+    __device__ __forceinline__ uint8_t* m(int k) const { return base + 4 * L::CS + k * L::CM; }
     // packed index and colour of region node (r, c)
     __device__ __forceinline__ static int idx(int r, int c) { return r * (W / 2) + (c >> 1); }
     __device__ __forceinline__ static int col(int r, int c) { return (r + c) & 1; }
@@ -159,10 +154,10 @@ __device__ __forceinline__ void half_sweep(const RBRegion<S, W, WY>& R, int colo
 {
     constexpr int HW = W / 2, n = (WY - 2) * HW, IT = (n + 255) / 256;
     const int t = tid256();
-    S* __restrict__ xo = R.x[color];
-    const S* __restrict__ xn = R.x[color ^ 1];
-    const S* __restrict__ bo = R.b[color];
-    const uint8_t* __restrict__ mo = R.m[color];
+    S* __restrict__ xo = R.x(color);
+    const S* __restrict__ xn = R.x(color ^ 1);
+    const S* __restrict__ bo = R.b(color);
+    const uint8_t* __restrict__ mo = R.m(color);
 #pragma unroll
     for (int it = 0; it < IT; ++it) {
         const int e = t + 256 * it;
@@ -286,9 +281,9 @@ k_bs_down(const int4* __restrict__ tiles, const BSInfo* __restrict__ info,
                 }
                 bv = mv ? bv : S(0);
                 const int k = R.col(r, c), q = R.idx(r, c);
-                R.m[k][q] = mv;
-                R.b[k][q] = bv;
-                R.x[k][q] = k == 0 ? bv * id : S(0);
+                R.m(k)[q] = mv;
+                R.b(k)[q] = bv;
+                R.x(k)[q] = k == 0 ? bv * id : S(0);
             }
         }
     }
@@ -303,10 +298,10 @@ k_bs_down(const int4* __restrict__ tiles, const BSInfo* __restrict__ info,
     {
         constexpr int n = (WY - 2) * HW, IT = (n + 255) / 256;
         const S md = Coef<S>::md(F);
-        const S* __restrict__ xr = R.x[0];
-        const S* __restrict__ xb = R.x[1];
-        S* __restrict__ br = R.b[0];
-        const uint8_t* __restrict__ mr = R.m[0];
+        const S* __restrict__ xr = R.x(0);
+        const S* __restrict__ xb = R.x(1);
+        S* __restrict__ br = R.b(0);
+        const uint8_t* __restrict__ mr = R.m(0);
 #pragma unroll
         for (int it = 0; it < IT; ++it) {
             const int e = t + 256 * it;
@@ -324,7 +319,7 @@ k_bs_down(const int4* __restrict__ tiles, const BSInfo* __restrict__ info,
         // coarse nodes with their centre in the tile: (TH/2) x (BS_TW/2);
         // the centre and its four diagonal neighbours are red
         const MGLevel C = levs[tl.x * BS_LMAX + l + 1];
-        const S* __restrict__ br = R.b[0];
+        const S* __restrict__ br = R.b(0);
         static_assert((TH / 2) * (BS_TW / 2) % 256 == 0, "coarse nodes per thread");
 #pragma unroll
         for (int k2 = 0; k2 < (TH / 2) * (BS_TW / 2) / 256; ++k2) {
@@ -350,7 +345,7 @@ k_bs_down(const int4* __restrict__ tiles, const BSInfo* __restrict__ info,
         const int r = threadIdx.y + 8 * qr, c = threadIdx.x;
         const int J = J0 + r, I = I0 + c;
         if (J < F.nyn && I < F.nxn)
-            xa[nidx(F, J, I)] = R.x[R.col(r + H, c + H)][R.idx(r + H, c + H)];
+            xa[nidx(F, J, I)] = R.x(R.col(r + H, c + H))[R.idx(r + H, c + H)];
     }
 }
 
@@ -427,9 +422,9 @@ k_bs_up(const int4* __restrict__ tiles, const BSInfo* __restrict__ info,
                     }
                 }
                 const int k = R.col(r, c), q = R.idx(r, c);
-                R.m[k][q] = mv;
-                R.x[k][q] = mv ? xv : S(0);
-                R.b[k][q] = mv ? bv : S(0);
+                R.m(k)[q] = mv;
+                R.x(k)[q] = mv ? xv : S(0);
+                R.b(k)[q] = mv ? bv : S(0);
             }
         }
     }
@@ -450,7 +445,7 @@ k_bs_up(const int4* __restrict__ tiles, const BSInfo* __restrict__ info,
             const S h0 = S(0.5) * (a + b);
             const S h1 = S(0.5) * (sc2[q + oj] + sc2[q + oj + oi]);
             const int k = R.col(r, c), qq = R.idx(r, c);
-            R.x[k][qq] += R.m[k][qq] ? S(0.5) * (h0 + h1) : S(0);
+            R.x(k)[qq] += R.m(k)[qq] ? S(0.5) * (h0 + h1) : S(0);
         }
     }
     __syncthreads();
@@ -467,8 +462,8 @@ k_bs_up(const int4* __restrict__ tiles, const BSInfo* __restrict__ info,
         const int J = J0 + r, I = I0 + c;
         const int k = R.col(r + H, c + H), q = R.idx(r + H, c + H);
         if (J < F.nyn && I < F.nxn) {
-            x[nidx(F, J, I)] = R.x[k][q];
-            if (RZ) acc += R.b[k][q] * R.x[k][q];  // 0 at non-fluid nodes
+            x[nidx(F, J, I)] = R.x(k)[q];
+            if (RZ) acc += R.b(k)[q] * R.x(k)[q];  // 0 at non-fluid nodes
         }
     }
     if (RZ) {
