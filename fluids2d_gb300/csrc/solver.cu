@@ -1354,6 +1354,7 @@ int bs_autotune(BatchSolver& s, cudaStream_t st, cudaStream_t st2, void* x, cons
     cudaEvent_t ea, eb;
     cudaEventCreate(&ea);
     cudaEventCreate(&eb);
+    const bool eager = bs_eager();
     const double tin[3] = {1e-6, 1e-5, 1e-4};
     const int ntin = s.mode == 1 ? 3 : 1;
     BSTune best{0, 0, 0.0, 1e300, 0};
@@ -1369,18 +1370,22 @@ int bs_autotune(BatchSolver& s, cudaStream_t st, cudaStream_t st2, void* x, cons
                 cudaGraph_t g = nullptr;
                 cudaGraphExec_t gx = nullptr;
                 int fixed = 0;
-                if (cudaStreamBeginCapture(st, cudaStreamCaptureModeRelaxed) != cudaSuccess) {
-                    err = 3;
-                    break;
+                // the eager profiling mode runs the solve's loops from the
+                // host (no capture); otherwise the solve is one graph
+                if (!eager) {
+                    if (cudaStreamBeginCapture(st, cudaStreamCaptureModeRelaxed) != cudaSuccess) {
+                        err = 3;
+                        break;
+                    }
+                    int e = bs_record(s, st, st2, &fixed);
+                    cudaError_t ce = cudaStreamEndCapture(st, &g);
+                    if (e || ce != cudaSuccess || cudaGraphInstantiate(&gx, g, 0) != cudaSuccess) {
+                        if (g) cudaGraphDestroy(g);
+                        err = e ? e : 3;
+                        break;
+                    }
+                    cudaGraphDestroy(g);
                 }
-                int e = bs_record(s, st, st2, &fixed);
-                cudaError_t ce = cudaStreamEndCapture(st, &g);
-                if (e || ce != cudaSuccess || cudaGraphInstantiate(&gx, g, 0) != cudaSuccess) {
-                    if (g) cudaGraphDestroy(g);
-                    err = e ? e : 3;
-                    break;
-                }
-                cudaGraphDestroy(g);
                 BSGlobals zero;
                 memset(&zero, 0, sizeof(zero));
                 cudaMemcpyAsync(s.eg, &zero, sizeof(zero), cudaMemcpyHostToDevice, st);
@@ -1389,7 +1394,15 @@ int bs_autotune(BatchSolver& s, cudaStream_t st, cudaStream_t st2, void* x, cons
                 for (int r = -1; r < reps; ++r) {
                     k_bs_scale<<<1024, 256, 0, st>>>((double*)x, saved, 0.999, n);
                     cudaEventRecord(ea, st);
-                    cudaGraphLaunch(gx, st);
+                    if (eager) {
+                        const int e = bs_record(s, st, st2, &fixed);
+                        if (e) {
+                            err = e;
+                            break;
+                        }
+                    } else {
+                        cudaGraphLaunch(gx, st);
+                    }
                     cudaEventRecord(eb, st);
                     if (cudaEventSynchronize(eb) != cudaSuccess) {
                         err = 3;
@@ -1399,7 +1412,7 @@ int bs_autotune(BatchSolver& s, cudaStream_t st, cudaStream_t st2, void* x, cons
                     cudaEventElapsedTime(&ms, ea, eb);
                     if (r >= 0) total += ms;
                 }
-                cudaGraphExecDestroy(gx);
+                if (gx) cudaGraphExecDestroy(gx);
                 if (err) break;
                 BSGlobals hg;
                 cudaMemcpy(&hg, s.eg, sizeof(hg), cudaMemcpyDeviceToHost);
