@@ -558,23 +558,17 @@ def run_gpu_ensemble(args, rank, world):
                       "single FP64 model, 2 warm-up + 3 timed steps, summed "
                       "per-step times scaled to all members"}
     # end to end: every member's vorticity from pinned host memory and back
-    host = []
-    for b, c in enumerate(members):
-        t = torch.empty((c["ny"] + 6, c["nx"] + 6), dtype=torch.float64,
-                        pin_memory=True)
-        check(L.f2d_ensemble_field_get(h, b, b"omega", ctypes.c_void_p(t.data_ptr())))
-        host.append(t)
+    # (all members' vorticity in one pinned buffer, one copy each way per step)
+    host = torch.empty(e.packed_size(), dtype=torch.float64, pin_memory=True)
+    hp = ctypes.c_void_p(host.data_ptr())
+    check(L.f2d_ensemble_fields_get(h, b"omega", hp, 0))
     e2e_steps = max(1, min(args.steps, 20))
     torch.cuda.synchronize()
     t0 = time.perf_counter()
     for _ in range(e2e_steps):
-        for b, t in enumerate(host):
-            check(L.f2d_ensemble_field_set_async(h, b, b"omega",
-                                                 ctypes.c_void_p(t.data_ptr())))
+        check(L.f2d_ensemble_fields_set(h, b"omega", hp, 1))
         check(L.f2d_ensemble_run(h, 1))
-        for b, t in enumerate(host):
-            check(L.f2d_ensemble_field_get_async(h, b, b"omega",
-                                                 ctypes.c_void_p(t.data_ptr())))
+        check(L.f2d_ensemble_fields_get(h, b"omega", hp, 1))
     e.sync()
     e2e_s = time.perf_counter() - t0
     io = sum((c["ny"] + 6) * (c["nx"] + 6) * 8 for c in members)

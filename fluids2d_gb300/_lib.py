@@ -79,6 +79,9 @@ _SIGS = {
     "f2d_qg_projection": ([c_void_p], c_int),
     "f2d_field_get_f32": ([c_void_p, ctypes.c_char_p, c_void_p], c_int),
     "f2d_bulk_record": ([c_void_p], c_int),
+    "f2d_ensemble_fields_set": ([c_void_p, ctypes.c_char_p, c_void_p, c_int], c_int),
+    "f2d_ensemble_fields_get": ([c_void_p, ctypes.c_char_p, c_void_p, c_int], c_int),
+    "f2d_ensemble_packed_size": ([c_void_p], ctypes.c_int64),
     "f2d_autotune": ([c_void_p, c_int, ctypes.POINTER(c_int), ctypes.POINTER(c_int),
                       ctypes.POINTER(c_dbl), ctypes.POINTER(c_dbl)], c_int),
     "f2d_ensemble_autotune": ([c_void_p, c_int, ctypes.POINTER(c_int), ctypes.POINTER(c_int),

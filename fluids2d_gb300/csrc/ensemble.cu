@@ -40,6 +40,8 @@ struct Member {
     int n0, nn;         // range in the level-0 node-tile table
     int nl, ltail, ksweeps;
     int pad;
+    long long poff;     // offset of the member's packed (NY, NX) array in the
+                        // all-members host layout of f2d_ensemble_fields_*
 };
 
 struct EnsGlobals {
@@ -237,6 +239,8 @@ struct f2d_ensemble_s {
     int4* cell_tiles = nullptr;
     int ncell = 0;
     size_t total = 0;  // elements per arena
+    size_t packed = 0;  // elements of all members' packed (NY, NX) arrays
+    double* io64 = nullptr;  // device copy of the packed layout (lazy)
     EnsArenas ar;
     BatchSolver bs;
     void* code = nullptr;
@@ -423,7 +427,7 @@ int f2d_ensemble_create(const f2d_params* p, int count, const int* nxs, const in
     // member geometry and arena offsets
     std::vector<MeshHost> meshes(count);
     e->hmem.resize(count);
-    size_t off = 0;
+    size_t off = 0, poff = 0;
     for (int b = 0; b < count; ++b) {
         f2d_params q = *p;
         q.nx = nxs[b];
@@ -441,6 +445,8 @@ int f2d_ensemble_create(const f2d_params* p, int count, const int* nxs, const in
         g.P = (g.NX + 15) / 16 * 16;
         g.xper = q.xperiodic ? 1 : 0;
         mb.off = (long long)off;
+        mb.poff = (long long)poff;
+        poff += (size_t)g.NX * g.NY;
         const double dx = q.Lx / q.nx, dy = q.Ly / q.ny;
         mb.rdx2 = 1 / pow(dx, 2.0);
         mb.rdy2 = 1 / pow(dy, 2.0);
@@ -449,6 +455,7 @@ int f2d_ensemble_create(const f2d_params* p, int count, const int* nxs, const in
         off += ((size_t)g.P * g.NY + 31) / 32 * 32;
     }
     e->total = off;
+    e->packed = poff;
     const size_t es = e->es;
     auto A = [&](size_t bytes_per) { return ens_alloc(e, e->total * bytes_per); };
     e->ar.q[0] = A(es);
@@ -653,6 +660,73 @@ int f2d_ensemble_field_set_async(f2d_ensemble e, int member, const char* name,
 int f2d_ensemble_field_get_async(f2d_ensemble e, int member, const char* name, double* host)
 {
     return ens_io(e, member, name, host, false, true);
+}
+
+// All members' field at once: between the arena (pitched, precision T) and
+// the packed FP64 layout (member b's (NY, NX) array at poff_b), one cell
+// tile (32 columns x FTY rows) per block
+extern "C++" {
+template <typename T, bool SET>
+__global__ void k_ens_pack(const int4* __restrict__ tiles, const Member* __restrict__ mem,
+                           T* arena, double* packed)
+{
+    const int4 tl = tiles[blockIdx.x];
+    const Member& mb = mem[tl.x];
+    const int i = tl.y + threadIdx.x;
+    if (i >= mb.g.NX) return;
+#pragma unroll
+    for (int q = 0; q < FTY / 8; ++q) {
+        const int j = tl.z + threadIdx.y + 8 * q;
+        if (j >= mb.g.NY) break;
+        const long long a = mb.off + (long long)j * mb.g.P + i;
+        const long long k = mb.poff + (long long)j * mb.g.NX + i;
+        if (SET) arena[a] = (T)packed[k];
+        else packed[k] = (double)arena[a];
+    }
+}
+}  // extern "C++"
+
+static int ens_io_all(f2d_ensemble e, const char* name, double* host, bool set, bool async)
+{
+    if (!e || !name || !host) return f2d_internal_fail(1, "null argument");
+    int es = 8;
+    void* base = ens_field(e, name, &es);
+    if (!base) return f2d_internal_fail(8, (std::string("no ensemble field ") + name).c_str());
+    if (!e->io64) {
+        e->io64 = (double*)ens_alloc(e, e->packed * sizeof(double));
+        if (!e->io64) return f2d_internal_fail(2, "out of device memory");
+    }
+    const size_t bytes = e->packed * sizeof(double);
+    const dim3 blk(32, 8);
+#define ENS_PACK(T, SET)                                                                 \
+    k_ens_pack<T, SET><<<e->ncell, blk, 0, e->stream>>>(e->cell_tiles, e->dmem, (T*)base, \
+                                                          e->io64)
+    if (set) {
+        ECK(cudaMemcpyAsync(e->io64, host, bytes, cudaMemcpyHostToDevice, e->stream));
+        if (es == 8) ENS_PACK(double, true);
+        else ENS_PACK(float, true);
+    } else {
+        if (es == 8) ENS_PACK(double, false);
+        else ENS_PACK(float, false);
+        ECK(cudaMemcpyAsync(host, e->io64, bytes, cudaMemcpyDeviceToHost, e->stream));
+    }
+#undef ENS_PACK
+    ECK(cudaGetLastError());
+    if (!async) ECK(cudaStreamSynchronize(e->stream));
+    return 0;
+}
+
+int f2d_ensemble_fields_set(f2d_ensemble e, const char* name, const double* host, int async)
+{
+    return ens_io_all(e, name, (double*)host, true, async != 0);
+}
+int f2d_ensemble_fields_get(f2d_ensemble e, const char* name, double* host, int async)
+{
+    return ens_io_all(e, name, host, false, async != 0);
+}
+int64_t f2d_ensemble_packed_size(f2d_ensemble e)
+{
+    return e ? (int64_t)e->packed : -1;
 }
 
 int f2d_ensemble_diag(f2d_ensemble e)

@@ -72,6 +72,37 @@ class Ensemble:
         check(lib().f2d_ensemble_field_get(self._h, b, name.encode(), ptr(out)))
         return out
 
+    def packed_size(self):
+        """Elements of the packed all-members layout."""
+        return int(lib().f2d_ensemble_packed_size(self._h))
+
+    def set_fields(self, name, arrays):
+        """Field `name` of every member from a list of (ny+6, nx+6) arrays
+        (or one packed float64 array), in one copy and one kernel."""
+        packed = self._pack(arrays)
+        check(lib().f2d_ensemble_fields_set(self._h, name.encode(), ptr(packed), 0))
+
+    def get_fields(self, name):
+        """Field `name` of every member as a list of (ny+6, nx+6) arrays."""
+        packed = np.empty(self.packed_size())
+        check(lib().f2d_ensemble_fields_get(self._h, name.encode(), ptr(packed), 0))
+        out, k = [], 0
+        for b in range(len(self.sizes)):
+            ny, nx = self.shape(b)
+            out.append(packed[k:k + ny * nx].reshape(ny, nx))
+            k += ny * nx
+        return out
+
+    def _pack(self, arrays):
+        if isinstance(arrays, np.ndarray) and arrays.ndim == 1:
+            packed = np.ascontiguousarray(arrays, dtype=np.float64)
+        else:
+            packed = np.concatenate([np.ascontiguousarray(a, dtype=np.float64).ravel()
+                                     for a in arrays])
+        if packed.size != self.packed_size():
+            raise ValueError("packed size does not match the ensemble")
+        return packed
+
     def set_stream(self, stream_ptr):
         check(lib().f2d_ensemble_set_stream(self._h, ctypes.c_void_p(stream_ptr)))
 

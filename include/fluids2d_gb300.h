@@ -213,6 +213,16 @@ int f2d_ensemble_create(const f2d_params *p, int count, const int *nx,
                         f2d_ensemble *out);
 int f2d_ensemble_destroy(f2d_ensemble e);
 int f2d_ensemble_set_stream(f2d_ensemble e, void *stream);
+/* A field of ALL members at once, in the packed host layout: member b's
+ * (ny_b+6, nx_b+6) float64 array at offset f2d_ensemble_packed_size-style
+ * prefix sums (member order), one host<->device copy and one gather/scatter
+ * kernel for the whole ensemble. async != 0: no stream synchronisation (the
+ * host buffer must then be pinned and stay alive until f2d_ensemble_sync). */
+int f2d_ensemble_fields_set(f2d_ensemble e, const char *name, const double *host,
+                            int async);
+int f2d_ensemble_fields_get(f2d_ensemble e, const char *name, double *host, int async);
+/* Elements of the packed layout (sum over members of (ny+6)(nx+6)). */
+int64_t f2d_ensemble_packed_size(f2d_ensemble e);
 /* Fields of member b by the reference's names ("omega" or "pv", "psi",
  * "vomega" or "work", "U.x", "U.y"; "f" sets the qg vertex Coriolis term);
  * (ny[b]+6, nx[b]+6) float64 host arrays. */

@@ -728,6 +728,28 @@ def test_autotune_model_vs_oracle(kind):
     m.sync()
 
 
+def test_ensemble_fields_all_members_roundtrip():
+    """f2d_ensemble_fields_set/get (all members, packed layout) agree with
+    the per-member calls, FP64 and FP32 arenas."""
+    members = [wl.eulerpsi_case(n=40, ny=24, seed=41, nislands=1),
+               wl.eulerpsi_case(n=72, ny=56, seed=42, nislands=2),
+               wl.eulerpsi_case(n=33, ny=47, seed=43, nislands=0)]
+    for prec in ("fp64", "fp32"):
+        e = _ensemble(members, prec)
+        got = e.get_fields("omega")
+        for b, c in enumerate(members):
+            np.testing.assert_array_equal(got[b], e.get_field(b, "omega"))
+        rng = np.random.default_rng(5)
+        new = [rng.standard_normal(e.shape(b)) for b in range(len(members))]
+        e.set_fields("omega", new)
+        for b in range(len(members)):
+            ref = new[b] if prec == "fp64" else new[b].astype(np.float32)
+            np.testing.assert_array_equal(e.get_field(b, "omega"), ref)
+        psi = e.get_fields("psi")
+        for b in range(len(members)):
+            np.testing.assert_array_equal(psi[b], e.get_field(b, "psi"))
+
+
 def test_ensemble_vs_oracle():
     members = [wl.eulerpsi_case(n=48, ny=40, seed=21, nislands=2),
                wl.eulerpsi_case(n=72, ny=64, seed=22, nislands=1)]
