@@ -73,6 +73,15 @@ WORKLOADS = {
                  "SSP-RK3, cfl 0.5, FP64, RSW tendency projected on the QG "
                  "manifold by an MG-PCG Helmholtz solve every stage; initial "
                  "state = qg_projection of a thickness bump"),
+    "euler1024": ("euler", dict(n=1024, seed=0, nislands=3),
+                  "euler 1024x1024 closed basin, 3 islands, FP64 (profiling size: "
+                  "working set above the L2)"),
+    "boussinesq1024": ("boussinesq", dict(n=1024, seed=0, nislands=3),
+                       "boussinesq 1024x1024 closed basin, 3 islands, FP64 (profiling "
+                       "size)"),
+    "qgrsw1024": ("qgrsw", dict(n=1024, seed=0, nislands=3, xperiodic=False, f0=10.0),
+                  "qgrsw 1024x1024 closed basin, 3 islands, f0=10, FP64 (profiling "
+                  "size)"),
     "rsw1024": ("rsw", dict(n=1024, seed=0, nislands=3),
                 "rsw 1024x1024 x-periodic channel, 3 islands, FP64 (profiling "
                 "size: working set above the L2)"),
