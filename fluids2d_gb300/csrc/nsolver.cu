@@ -127,72 +127,22 @@ __global__ void k_ns_zero(const NLevel* __restrict__ levs, int l)
     if (cell(L, J, I)) L.x[cidx(L, J, I)] = 0.0;
 }
 
-// The levels l0..nl-1 of a V-cycle in one block: coarse levels small enough
-// that one SM sweeping them beats a launch per sweep and transfer (the same
-// operations as the grid kernels, phase by phase with block barriers)
-__device__ __forceinline__ void nb_smooth(const NLevel& L, int color)
+// coarsest level: (R,B)^k (B,R)^k from x = 0, one block
+__global__ void __launch_bounds__(1024) k_ns_coarse(const NLevel* __restrict__ levs, int l,
+                                                    int ksweeps)
 {
+    const NLevel L = levs[l];
     const int n = L.nyn * L.nxn;
-    for (int e = threadIdx.x; e < n; e += blockDim.x) {
-        const int J = e / L.nxn, I = e - J * L.nxn;
-        if (((J + I) & 1) == color) n_smooth_cell(L, J, I);
-    }
+    for (int e = threadIdx.x; e < n; e += blockDim.x) L.x[cidx(L, e / L.nxn, e % L.nxn)] = 0.0;
     __syncthreads();
-}
-
-__global__ void __launch_bounds__(1024) k_ns_tail(const NLevel* __restrict__ levs, int l0,
-                                                  int nl, int nu, int ksweeps)
-{
-    if (l0 == 0) {
-        // the cycle starts here: x = 0 before the pre-smoothing
-        const NLevel L = levs[0];
-        const int n = L.nyn * L.nxn;
-        for (int e = threadIdx.x; e < n; e += blockDim.x)
-            L.x[cidx(L, e / L.nxn, e % L.nxn)] = 0.0;
-        __syncthreads();
-    }
-    for (int l = l0; l < nl - 1; ++l) {
-        const NLevel F = levs[l], C = levs[l + 1];
-        for (int k = 0; k < nu; ++k) {
-            nb_smooth(F, 0);
-            nb_smooth(F, 1);
-        }
-        // coarse b = sum of the fluid children's residuals; coarse x = 0
-        const int n = C.nyn * C.nxn;
-        for (int e = threadIdx.x; e < n; e += blockDim.x) {
-            const int J = e / C.nxn, I = e - J * C.nxn;
-            double v = 0.0;
-            for (int a = 0; a < 2; ++a)
-                for (int c = 0; c < 2; ++c) {
-                    const int fj = 2 * J + a, fi = 2 * I + c;
-                    if (fj >= F.nyn || fi >= F.nxn) continue;
-                    const long long k = cidx(F, fj, fi);
-                    if (F.m[k]) v += F.b[k] - n_apply(F, F.x, fj, fi, nullptr);
-                }
-            const long long kc = cidx(C, J, I);
-            C.b[kc] = C.m[kc] ? v : 0.0;
-            C.x[kc] = 0.0;
-        }
-        __syncthreads();
-    }
-    {
-        // coarsest level: (R,B)^k (B,R)^k from x = 0
-        const NLevel L = levs[nl - 1];
-        for (int s = 0; s < 2 * ksweeps; ++s)
-            for (int h = 0; h < 2; ++h) nb_smooth(L, s < ksweeps ? h : 1 - h);
-    }
-    for (int l = nl - 2; l >= l0; --l) {
-        const NLevel F = levs[l], C = levs[l + 1];
-        const int n = F.nyn * F.nxn;
-        for (int e = threadIdx.x; e < n; e += blockDim.x) {
-            const int J = e / F.nxn, I = e - J * F.nxn;
-            const long long k = cidx(F, J, I);
-            if (F.m[k]) F.x[k] += C.x[cidx(C, J >> 1, I >> 1)];
-        }
-        __syncthreads();
-        for (int k = 0; k < nu; ++k) {
-            nb_smooth(F, 1);
-            nb_smooth(F, 0);
+    for (int s = 0; s < 2 * ksweeps; ++s) {
+        for (int h = 0; h < 2; ++h) {
+            const int color = s < ksweeps ? h : 1 - h;
+            for (int e = threadIdx.x; e < n; e += blockDim.x) {
+                const int J = e / L.nxn, I = e % L.nxn;
+                if (((J + I) & 1) == color) n_smooth_cell(L, J, I);
+            }
+            __syncthreads();
         }
     }
 }
@@ -341,20 +291,13 @@ __global__ void k_ns_setup(DevScalars* sc, double tol2, int maxit)
 // ---- host ----------------------------------------------------------------------
 static dim3 ngrid(const NLevel& L) { return dim3((L.nxn + 31) / 32, (L.nyn + 7) / 8); }
 
-// cells of the largest level the one-block tail takes
-static const int NS_TAIL_CELLS = 4096;
-
 static int ns_vcycle(NSolver& s, cudaStream_t st)
 {
     const dim3 blk(32, 8);
     const int nl = (int)s.lev.size();
     int cnt = 0;
-    // the tail: the first level (from the top) of at most NS_TAIL_CELLS
-    // cells and everything below it, in one block
-    int lt = nl - 1;
-    while (lt > 0 && (long long)s.lev[lt - 1].nyn * s.lev[lt - 1].nxn <= NS_TAIL_CELLS) --lt;
     // level 0 of the cycle: x = z (from zero), b = r
-    for (int l = 0; l < lt; ++l) {
+    for (int l = 0; l < nl - 1; ++l) {
         // x = 0 before the pre-smoothing (coarse levels: set by the restriction)
         if (l == 0) k_ns_zero<<<ngrid(s.lev[l]), blk, 0, st>>>(s.dlev, l);
         for (int k = 0; k < s.nu; ++k) {
@@ -364,9 +307,9 @@ static int ns_vcycle(NSolver& s, cudaStream_t st)
         k_ns_restrict<<<ngrid(s.lev[l + 1]), blk, 0, st>>>(s.dlev, l);
         cnt += (l == 0 ? 2 : 1) + 2 * s.nu;
     }
-    k_ns_tail<<<1, 1024, 0, st>>>(s.dlev, lt, nl, s.nu, s.ksweeps);
+    k_ns_coarse<<<1, 1024, 0, st>>>(s.dlev, nl - 1, s.ksweeps);
     cnt += 1;
-    for (int l = lt - 1; l >= 0; --l) {
+    for (int l = nl - 2; l >= 0; --l) {
         k_ns_prolong<<<ngrid(s.lev[l]), blk, 0, st>>>(s.dlev, l);
         for (int k = 0; k < s.nu; ++k) {
             k_ns_smooth<<<ngrid(s.lev[l]), blk, 0, st>>>(s.dlev, l, 1);
