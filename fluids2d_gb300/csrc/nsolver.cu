@@ -84,11 +84,14 @@ __device__ __forceinline__ void n_smooth_cell(const NLevel& L, int J, int I)
     if (cs > 0.0) L.x[k] = ((ax + cs * L.x[k]) - L.b[k]) / cs;
 }
 
+// one thread per cell of the colour: thread column I' of row J takes cell
+// I = 2 I' + ((J + color) & 1)
 __global__ void k_ns_smooth(const NLevel* __restrict__ levs, int l, int color)
 {
     const NLevel L = levs[l];
-    int J, I;
-    if (!cell(L, J, I) || ((J + I) & 1) != color) return;
+    const int J = blockIdx.y * blockDim.y + threadIdx.y;
+    const int I = 2 * (blockIdx.x * blockDim.x + threadIdx.x) + ((J + color) & 1);
+    if (J >= L.nyn || I >= L.nxn) return;
     n_smooth_cell(L, J, I);
 }
 
@@ -290,6 +293,11 @@ __global__ void k_ns_setup(DevScalars* sc, double tol2, int maxit)
 
 // ---- host ----------------------------------------------------------------------
 static dim3 ngrid(const NLevel& L) { return dim3((L.nxn + 31) / 32, (L.nyn + 7) / 8); }
+// the cells of one colour: half the columns
+static dim3 ngrid_half(const NLevel& L)
+{
+    return dim3(((L.nxn + 1) / 2 + 31) / 32, (L.nyn + 7) / 8);
+}
 
 static int ns_vcycle(NSolver& s, cudaStream_t st)
 {
@@ -301,8 +309,8 @@ static int ns_vcycle(NSolver& s, cudaStream_t st)
         // x = 0 before the pre-smoothing (coarse levels: set by the restriction)
         if (l == 0) k_ns_zero<<<ngrid(s.lev[l]), blk, 0, st>>>(s.dlev, l);
         for (int k = 0; k < s.nu; ++k) {
-            k_ns_smooth<<<ngrid(s.lev[l]), blk, 0, st>>>(s.dlev, l, 0);
-            k_ns_smooth<<<ngrid(s.lev[l]), blk, 0, st>>>(s.dlev, l, 1);
+            k_ns_smooth<<<ngrid_half(s.lev[l]), blk, 0, st>>>(s.dlev, l, 0);
+            k_ns_smooth<<<ngrid_half(s.lev[l]), blk, 0, st>>>(s.dlev, l, 1);
         }
         k_ns_restrict<<<ngrid(s.lev[l + 1]), blk, 0, st>>>(s.dlev, l);
         cnt += (l == 0 ? 2 : 1) + 2 * s.nu;
@@ -312,8 +320,8 @@ static int ns_vcycle(NSolver& s, cudaStream_t st)
     for (int l = nl - 2; l >= 0; --l) {
         k_ns_prolong<<<ngrid(s.lev[l]), blk, 0, st>>>(s.dlev, l);
         for (int k = 0; k < s.nu; ++k) {
-            k_ns_smooth<<<ngrid(s.lev[l]), blk, 0, st>>>(s.dlev, l, 1);
-            k_ns_smooth<<<ngrid(s.lev[l]), blk, 0, st>>>(s.dlev, l, 0);
+            k_ns_smooth<<<ngrid_half(s.lev[l]), blk, 0, st>>>(s.dlev, l, 1);
+            k_ns_smooth<<<ngrid_half(s.lev[l]), blk, 0, st>>>(s.dlev, l, 0);
         }
         cnt += 1 + 2 * s.nu;
     }
