@@ -108,6 +108,7 @@ struct f2d_model_s {
     // Bulk diagnostics ring (records of 5 doubles) and FP32 snapshot staging
     double* bulk_ring = nullptr;
     int* bulk_count = nullptr;
+    double bulk_summsk = -1.0;  // domsum(msk), cached per mask
     float* f32_stage = nullptr;
     std::map<std::string, Field> fields;
     std::vector<void*> allocs;
@@ -823,6 +824,7 @@ static int setup_mesh(f2d_model_s* m, const int8_t* msk)
 {
     std::string err;
     if (mesh_build_host(m->p, msk, m->mesh, err)) return fail(7, err);
+    m->bulk_summsk = -1.0;
     const Geom& g = m->g;
     std::vector<uint32_t> code((size_t)g.P * g.NY, 0);
     std::vector<uint8_t> gm((size_t)g.P * g.NY, 0);
@@ -1152,9 +1154,13 @@ int f2d_bulk_record(f2d_model m)
         m->bulk_count = (int*)dalloc(m, sizeof(int));
         if (!m->bulk_ring || !m->bulk_count) return fail(2, "out of device memory");
     }
-    // domsum(msk) over the whole array (diagnostics.py:15)
-    double summsk = 0.0;
-    for (int8_t v : m->mesh.msk) summsk += v;
+    // domsum(msk) over the whole array (diagnostics.py:15), once per mask
+    if (m->bulk_summsk < 0) {
+        double sm = 0.0;
+        for (int8_t v : m->mesh.msk) sm += v;
+        m->bulk_summsk = sm;
+    }
+    const double summsk = m->bulk_summsk;
     if (summsk <= 0) return fail(1, "the mask has no wet cell");
     BulkArgs a;
     a.ke = fb(m, "ke");
