@@ -430,14 +430,17 @@ static int rec_qgrsw_stage(f2d_model_s* m, int k, int par, cudaStream_t s);
 // the fused right-hand-side + RK3-update kernel of stage k, parity par -> 1-par
 static int launch_stage_kernel(f2d_model_s* m, int k, int par, cudaStream_t s)
 {
-    if (m->p.model == F2D_MODEL_QGRSW) return rec_qgrsw_stage(m, k, par, s);
     const Geom& g = m->g;
     const int out = 1 - par;
     const bool lf = m->p.integrator == F2D_INTEG_LFRA;
     auto ds = [&](const char* f, int kk) -> void* {
         return fb(m, (std::string("ds") + std::to_string(kk) + "." + f).c_str());
     };
-    if (m->p.model == F2D_MODEL_RSW || projected(m->p.model)) {
+    if (m->p.model == F2D_MODEL_QGRSW) {
+        // tendency, projection and update (counts its own launches)
+        int e = rec_qgrsw_stage(m, k, par, s);
+        if (e) return e;
+    } else if (m->p.model == F2D_MODEL_RSW || projected(m->p.model)) {
         // rsw; euler = the same momentum kernel without the mass equation,
         // Coriolis and pressure (equations.py:11-15); boussinesq = euler +
         // buoyancy + the flux divergence of b in the place of h (29-35)
@@ -479,6 +482,7 @@ static int launch_stage_kernel(f2d_model_s* m, int k, int par, cudaStream_t s)
         CKI(make_tmap(m, om));
         CKI(launch_rsw_stage(m->p.vortexforce, m->prec, tmap(m, hm), tmap(m, om), a,
                              m->d_code, k | (m->p.integrator << 4), g, m->sc, s));
+        m->rec_launches += 1;
     } else {
         const char* q = m->p.model == F2D_MODEL_EULERPSI ? "omega" : "pv";
         void* qin = fb(m, q, par);
@@ -489,8 +493,8 @@ static int launch_stage_kernel(f2d_model_s* m, int k, int par, cudaStream_t s)
                                   ds(q, lf ? 1 + par : 1), ds(q, 2),
                                   k | (m->p.integrator << 4), g,
                                   m->sc, s));
+        m->rec_launches += 1;
     }
-    m->rec_launches += 1;
     if (m->p.tracer) {
         // the passive tracer equation appended to the model's right-hand side
         // (addtracerequation, equations.py:217-226): divflux of the tracer

@@ -313,6 +313,20 @@ def tracer_cases():
                       name="s", seed=4)
     run_model(c, 4, "model_boussinesq_tracer.npz", cfl=0.5,
               extra={"tracer": "s"})
+    # qgrsw with a tracer: the tracer advected by the projected flow
+    from fluids2d.operators import qg_projection
+
+    def project(m):
+        s = m.state
+        qg_projection(m.mesh, s.u, s.h, s.pv, s.psi)
+    project.fields = ("u.x", "u.y", "h", "pv", "psi", "q")
+    c = wl.rsw_case(n=40, ny=32, seed=11, nislands=2, xperiodic=False, f0=10.0)
+    c["model"] = "qgrsw"
+    c["fields"] = {"u.x": np.zeros_like(c["fields"]["h"]),
+                   "u.y": np.zeros_like(c["fields"]["h"]), "h": c["fields"]["h"]}
+    c = wl.add_tracer(c, seed=5)
+    run_model(c, 4, "model_qgrsw_tracer.npz", cfl=0.5, extra={"tracer": "q"},
+              setup=project)
 
 
 def qgrsw_cases():

@@ -133,7 +133,8 @@ MODEL_FILES = ["model_eulerpsi.npz", "model_eulerpsi_islands.npz",
                "model_boussinesq_periodic.npz", "model_boussinesq_lfra.npz",
                "model_eulerpsi_tracer.npz", "model_qg_tracer_lfra.npz",
                "model_rsw_tracer.npz", "model_boussinesq_tracer.npz",
-               "model_qgrsw.npz", "model_qgrsw_periodic.npz", "model_qgrsw_lfra.npz"]
+               "model_qgrsw.npz", "model_qgrsw_periodic.npz", "model_qgrsw_lfra.npz",
+               "model_qgrsw_tracer.npz"]
 
 
 def model_from_golden(g):
