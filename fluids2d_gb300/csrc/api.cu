@@ -936,8 +936,6 @@ int f2d_model_create(const f2d_params* p, const int8_t* msk, f2d_model* out)
     if (p->precision != F2D_PREC_FP64 && p->precision != F2D_PREC_FP32)
         return fail(1, "unknown precision");
     if (p->model < 0 || p->model > 5) return fail(1, "unknown model");
-    if (projected(p->model) && p->precision != F2D_PREC_FP64)
-        return fail(1, "the euler and boussinesq models run in FP64");
 
     if (p->integrator < F2D_INTEG_RK3 || p->integrator > F2D_INTEG_LFRA)
         return fail(1, "unknown integrator (rk3, ef, enrk3, LFRA)");
@@ -1025,8 +1023,10 @@ int f2d_model_create(const f2d_params* p, const int8_t* msk, f2d_model* out)
     // the Poisson solution and right-hand side are FP64 in both forms; the
     // stencil state has the model's precision
     auto is64 = [&](const char* n) {
+        // the pressure of the Neumann projection is the FP64 solve's unknown
         return !strcmp(n, "psi") || !strcmp(n, "vomega") || !strcmp(n, "work") ||
-               (p->model == F2D_MODEL_QGRSW && !strcmp(n, "pv"));
+               (p->model == F2D_MODEL_QGRSW && !strcmp(n, "pv")) ||
+               (projected(p->model) && !strcmp(n, "p"));
     };
     for (auto& f : fl)
         if ((e = add_field(m, f.first, f.second, is64(f.first) ? 8 : (int)m->es)))

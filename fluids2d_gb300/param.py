@@ -112,9 +112,6 @@ class Param:
             raise NotImplementedError("yperiodic is not supported")
         if self.model in ("rsw", "euler", "boussinesq") and self.innerproduct == "classic":
             raise NotImplementedError("innerproduct='classic' is not implemented")
-        if (self.model in ("euler", "boussinesq")
-                and getattr(self, "precision", "fp64") != "fp64"):
-            raise NotImplementedError(f"the {self.model} model runs in FP64")
         assert self.precision in ("fp64", "fp32")
 
 

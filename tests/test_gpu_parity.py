@@ -534,7 +534,8 @@ def test_poisson_maxit_reports_status():
 # L2 for eulerpsi and qg; 1e-4 for rsw, whose velocity is driven by the
 # gradient of p = g h / area ~ 1 with O(1e-3) anomalies, so FP32 rounding of
 # p (6e-8) is amplified by the cancellation in grad p.
-FP32_STATE_TOL = {"eulerpsi": 2e-5, "qg": 2e-5, "rsw": 1e-4}
+FP32_STATE_TOL = {"eulerpsi": 2e-5, "qg": 2e-5, "rsw": 1e-4, "euler": 1e-4,
+                  "boussinesq": 1e-4}
 
 
 @pytest.mark.parametrize("case", ["islands", "periodic", "helmholtz"])
@@ -552,9 +553,14 @@ def test_fp32_model_poisson_reaches_fp64_accuracy(case):
 
 @pytest.mark.parametrize("kind,integrator",
                          [("eulerpsi", "rk3"), ("rsw", "rk3"), ("qg", "rk3"),
-                          ("eulerpsi", "LFRA"), ("rsw", "LFRA")])
+                          ("eulerpsi", "LFRA"), ("rsw", "LFRA"), ("euler", "rk3"),
+                          ("boussinesq", "rk3")])
 def test_fp32_model_vs_fp64_oracle(kind, integrator):
-    if kind == "eulerpsi":
+    if kind == "euler":
+        case = wl.euler_case(n=128, ny=96, seed=5, nislands=3)
+    elif kind == "boussinesq":
+        case = wl.boussinesq_case(n=128, ny=96, seed=6, nislands=3)
+    elif kind == "eulerpsi":
         case = wl.eulerpsi_case(n=128, ny=96, seed=5, nislands=3)
     elif kind == "rsw":
         case = wl.rsw_case(n=128, ny=96, seed=6, nislands=3)
@@ -571,7 +577,10 @@ def test_fp32_model_vs_fp64_oracle(kind, integrator):
         m.mesh.f = case["f"]
     s = m.state
     for k, v in case["fields"].items():
-        getattr(s, k)[:] = v
+        if "." in k:
+            getattr(getattr(s, k.split(".")[0]), k.split(".")[1])[:] = v
+        else:
+            getattr(s, k)[:] = v
     m.integrator.diag(s)
     for _ in range(5):
         om.run_steps(1)
