@@ -288,7 +288,7 @@ static int ensure_ns(f2d_model_s* m)
         for (int i = 3; i < 3 + g.nx; ++i)
             hm[(size_t)j * g.P + i] = m->mesh.msk[(size_t)j * g.NX + i] ? 1 : 0;
     int e = ns_build(m->ns, g.ny, g.nx, g.P, 3 * (long long)g.P + 3, g.xper, hm.data(),
-                     (double*)fb(m, "p"), m->nrhs, m->cx, m->cy);
+                     (double*)fb(m, "p"), m->nrhs, m->cx, m->cy, m->prec);
     if (e == 6) return fail(4, "the euler model needs at least one fluid cell");
     if (e) return fail(e, "Neumann multigrid setup failed");
     m->ns.tol = m->p.poisson_tol;

@@ -23,7 +23,11 @@
 // smooth errors, and the coarse correction comes out halved - half the sum is
 // the re-discretised coupling where the face is fully open and keeps the
 // partial openings of masked faces.) Coarsest level by (R,B)^k (B,R)^k in one
-// thread block. Single component assumed (a
+// thread block. The FP32 form runs the cycle in FP32 (levels, couplings and
+// smoothing in float; its right-hand side is the FP64 Krylov residual
+// rounded, its result converted back), while the Krylov vectors, the
+// operator products, the dot products and the zero-mean projections stay
+// FP64. Single component assumed (a
 // fluid domain made of several disconnected parts would need a projection
 // per part).
 #include <algorithm>
@@ -39,27 +43,31 @@ __device__ __forceinline__ long long cidx(const NLevel& L, int J, int I)
     return L.off + (long long)J * L.pitch + I;
 }
 
-// A x at fluid cell (J, I); also the sum of its couplings
-__device__ __forceinline__ double n_apply(const NLevel& L, const double* __restrict__ x,
-                                          int J, int I, double* csum)
+// A x at fluid cell (J, I); also the sum of its couplings. S: the value
+// and coupling type of the level (the FP32 cycle's levels are float)
+template <typename S>
+__device__ __forceinline__ S n_apply(const NLevel& L, const S* __restrict__ x, int J, int I,
+                                     S* csum)
 {
+    const S* __restrict__ fx = (const S*)L.fx;
+    const S* __restrict__ fy = (const S*)L.fy;
     const long long k = cidx(L, J, I);
-    const double xc = x[k];
-    const double cw = L.fx[k], cs = L.fy[k];
-    double ce = 0.0, cn = 0.0, xw = 0.0, xe = 0.0, xs = 0.0, xn = 0.0;
+    const S xc = x[k];
+    const S cw = fx[k], cs = fy[k];
+    S ce = S(0), cn = S(0), xw = S(0), xe = S(0), xs = S(0), xn = S(0);
     if (I > 0) xw = x[k - 1];
     else if (L.per) xw = x[cidx(L, J, L.nxn - 1)];
     if (I + 1 < L.nxn) {
-        ce = L.fx[k + 1];
+        ce = fx[k + 1];
         xe = x[k + 1];
     } else if (L.per) {
         const long long k0 = cidx(L, J, 0);
-        ce = L.fx[k0];
+        ce = fx[k0];
         xe = x[k0];
     }
     if (J > 0) xs = x[k - L.pitch];
     if (J + 1 < L.nyn) {
-        cn = L.fy[k + L.pitch];
+        cn = fy[k + L.pitch];
         xn = x[k + L.pitch];
     }
     if (csum) *csum = (cw + ce) + (cs + cn);
@@ -74,80 +82,109 @@ __device__ __forceinline__ bool cell(const NLevel& L, int& J, int& I)
 }
 
 // ---- multigrid -------------------------------------------------------------
+template <typename S>
 __device__ __forceinline__ void n_smooth_cell(const NLevel& L, int J, int I)
 {
+    S* __restrict__ x = (S*)L.x;
+    const S* __restrict__ b = (const S*)L.b;
     const long long k = cidx(L, J, I);
     if (!L.m[k]) return;
-    double cs;
-    const double ax = n_apply(L, L.x, J, I, &cs);
+    S cs;
+    const S ax = n_apply<S>(L, x, J, I, &cs);
     // A x = sum c_n x_n - cs x_c = b  ->  x_c = (sum c_n x_n - b) / cs
-    if (cs > 0.0) L.x[k] = ((ax + cs * L.x[k]) - L.b[k]) / cs;
+    if (cs > S(0)) x[k] = ((ax + cs * x[k]) - b[k]) / cs;
 }
 
 // one thread per cell of the colour: thread column I' of row J takes cell
 // I = 2 I' + ((J + color) & 1)
+template <typename S>
 __global__ void k_ns_smooth(const NLevel* __restrict__ levs, int l, int color)
 {
     const NLevel L = levs[l];
     const int J = blockIdx.y * blockDim.y + threadIdx.y;
     const int I = 2 * (blockIdx.x * blockDim.x + threadIdx.x) + ((J + color) & 1);
     if (J >= L.nyn || I >= L.nxn) return;
-    n_smooth_cell(L, J, I);
+    n_smooth_cell<S>(L, J, I);
 }
 
 // coarse b = sum of the fluid children's residuals; coarse x = 0
+template <typename S>
 __global__ void k_ns_restrict(const NLevel* __restrict__ levs, int l)
 {
     const NLevel F = levs[l], C = levs[l + 1];
     int J, I;
     if (!cell(C, J, I)) return;
-    double v = 0.0;
+    const S* __restrict__ fxv = (const S*)F.x;
+    const S* __restrict__ fb = (const S*)F.b;
+    S v = S(0);
     for (int a = 0; a < 2; ++a)
         for (int c = 0; c < 2; ++c) {
             const int fj = 2 * J + a, fi = 2 * I + c;
             if (fj >= F.nyn || fi >= F.nxn) continue;
             const long long k = cidx(F, fj, fi);
-            if (F.m[k]) v += F.b[k] - n_apply(F, F.x, fj, fi, nullptr);
+            if (F.m[k]) v += fb[k] - n_apply<S>(F, fxv, fj, fi, nullptr);
         }
     const long long kc = cidx(C, J, I);
-    C.b[kc] = C.m[kc] ? v : 0.0;
-    C.x[kc] = 0.0;
+    ((S*)C.b)[kc] = C.m[kc] ? v : S(0);
+    ((S*)C.x)[kc] = S(0);
 }
 
+template <typename S>
 __global__ void k_ns_prolong(const NLevel* __restrict__ levs, int l)
 {
     const NLevel F = levs[l], C = levs[l + 1];
     int J, I;
     if (!cell(F, J, I)) return;
     const long long k = cidx(F, J, I);
-    if (F.m[k]) F.x[k] += C.x[cidx(C, J >> 1, I >> 1)];
+    if (F.m[k]) ((S*)F.x)[k] += ((const S*)C.x)[cidx(C, J >> 1, I >> 1)];
 }
 
+template <typename S>
 __global__ void k_ns_zero(const NLevel* __restrict__ levs, int l)
 {
     const NLevel L = levs[l];
     int J, I;
-    if (cell(L, J, I)) L.x[cidx(L, J, I)] = 0.0;
+    if (cell(L, J, I)) ((S*)L.x)[cidx(L, J, I)] = S(0);
 }
 
 // coarsest level: (R,B)^k (B,R)^k from x = 0, one block
+template <typename S>
 __global__ void __launch_bounds__(1024) k_ns_coarse(const NLevel* __restrict__ levs, int l,
                                                     int ksweeps)
 {
     const NLevel L = levs[l];
     const int n = L.nyn * L.nxn;
-    for (int e = threadIdx.x; e < n; e += blockDim.x) L.x[cidx(L, e / L.nxn, e % L.nxn)] = 0.0;
+    for (int e = threadIdx.x; e < n; e += blockDim.x)
+        ((S*)L.x)[cidx(L, e / L.nxn, e % L.nxn)] = S(0);
     __syncthreads();
     for (int s = 0; s < 2 * ksweeps; ++s) {
         for (int h = 0; h < 2; ++h) {
             const int color = s < ksweeps ? h : 1 - h;
             for (int e = threadIdx.x; e < n; e += blockDim.x) {
                 const int J = e / L.nxn, I = e % L.nxn;
-                if (((J + I) & 1) == color) n_smooth_cell(L, J, I);
+                if (((J + I) & 1) == color) n_smooth_cell<S>(L, J, I);
             }
             __syncthreads();
         }
     }
+}
+
+// FP32 cycle: its level-0 right-hand side from the FP64 Krylov residual, and
+// the preconditioned residual back in FP64
+__global__ void k_ns_to32(NLevel L, const double* __restrict__ r, float* __restrict__ r32)
+{
+    int J, I;
+    if (!cell(L, J, I)) return;
+    const long long k = cidx(L, J, I);
+    r32[k] = (float)r[k];
+}
+
+__global__ void k_ns_to64(NLevel L, const float* __restrict__ z32, double* __restrict__ z)
+{
+    int J, I;
+    if (!cell(L, J, I)) return;
+    const long long k = cidx(L, J, I);
+    z[k] = (double)z32[k];
 }
 
 // ---- Krylov ----------------------------------------------------------------
@@ -174,9 +211,10 @@ __global__ void k_ns_init(NLevel L, double* __restrict__ r, DevScalars* sc, doub
         const long long k = cidx(L, J, I);
         double rv = 0.0;
         if (L.m[k]) {
-            const double bv = L.b[k] - mean;
-            L.b[k] = bv;
-            rv = bv - n_apply(L, L.x, J, I, nullptr);
+            double* b = (double*)L.b;
+            const double bv = b[k] - mean;
+            b[k] = bv;
+            rv = bv - n_apply<double>(L, (const double*)L.x, J, I, nullptr);
             w[0] = bv * bv;
             w[1] = rv * rv;
         }
@@ -229,7 +267,7 @@ __global__ void k_ns_q(NLevel L, const double* __restrict__ p, double* __restric
         const long long k = cidx(L, J, I);
         double qv = 0.0;
         if (L.m[k]) {
-            qv = n_apply(L, p, J, I, nullptr);
+            qv = n_apply<double>(L, p, J, I, nullptr);
             w[0] = p[k] * qv;
         }
         q[k] = qv;
@@ -251,7 +289,7 @@ __global__ void k_ns_xr(NLevel L, const double* __restrict__ p, const double* __
     if (cell(L, J, I)) {
         const long long k = cidx(L, J, I);
         if (L.m[k]) {
-            L.x[k] += a * p[k];
+            ((double*)L.x)[k] += a * p[k];
             const double rv = r[k] - a * q[k];
             r[k] = rv;
             w[0] = rv * rv;
@@ -280,7 +318,7 @@ __global__ void k_ns_center(NLevel L, const DevScalars* sc, long long nfluid)
     int J, I;
     if (!cell(L, J, I)) return;
     const long long k = cidx(L, J, I);
-    if (L.m[k]) L.x[k] -= sc->t / (double)nfluid;
+    if (L.m[k]) ((double*)L.x)[k] -= sc->t / (double)nfluid;
 }
 
 __global__ void k_ns_setup(DevScalars* sc, double tol2, int maxit)
@@ -299,7 +337,8 @@ static dim3 ngrid_half(const NLevel& L)
     return dim3(((L.nxn + 1) / 2 + 31) / 32, (L.nyn + 7) / 8);
 }
 
-static int ns_vcycle(NSolver& s, cudaStream_t st)
+template <typename S>
+static int ns_vcycle_t(NSolver& s, cudaStream_t st)
 {
     const dim3 blk(32, 8);
     const int nl = (int)s.lev.size();
@@ -307,32 +346,44 @@ static int ns_vcycle(NSolver& s, cudaStream_t st)
     // level 0 of the cycle: x = z (from zero), b = r
     for (int l = 0; l < nl - 1; ++l) {
         // x = 0 before the pre-smoothing (coarse levels: set by the restriction)
-        if (l == 0) k_ns_zero<<<ngrid(s.lev[l]), blk, 0, st>>>(s.dlev, l);
+        if (l == 0) k_ns_zero<S><<<ngrid(s.lev[l]), blk, 0, st>>>(s.dlev, l);
         for (int k = 0; k < s.nu; ++k) {
-            k_ns_smooth<<<ngrid_half(s.lev[l]), blk, 0, st>>>(s.dlev, l, 0);
-            k_ns_smooth<<<ngrid_half(s.lev[l]), blk, 0, st>>>(s.dlev, l, 1);
+            k_ns_smooth<S><<<ngrid_half(s.lev[l]), blk, 0, st>>>(s.dlev, l, 0);
+            k_ns_smooth<S><<<ngrid_half(s.lev[l]), blk, 0, st>>>(s.dlev, l, 1);
         }
-        k_ns_restrict<<<ngrid(s.lev[l + 1]), blk, 0, st>>>(s.dlev, l);
+        k_ns_restrict<S><<<ngrid(s.lev[l + 1]), blk, 0, st>>>(s.dlev, l);
         cnt += (l == 0 ? 2 : 1) + 2 * s.nu;
     }
-    k_ns_coarse<<<1, 1024, 0, st>>>(s.dlev, nl - 1, s.ksweeps);
+    k_ns_coarse<S><<<1, 1024, 0, st>>>(s.dlev, nl - 1, s.ksweeps);
     cnt += 1;
     for (int l = nl - 2; l >= 0; --l) {
-        k_ns_prolong<<<ngrid(s.lev[l]), blk, 0, st>>>(s.dlev, l);
+        k_ns_prolong<S><<<ngrid(s.lev[l]), blk, 0, st>>>(s.dlev, l);
         for (int k = 0; k < s.nu; ++k) {
-            k_ns_smooth<<<ngrid_half(s.lev[l]), blk, 0, st>>>(s.dlev, l, 1);
-            k_ns_smooth<<<ngrid_half(s.lev[l]), blk, 0, st>>>(s.dlev, l, 0);
+            k_ns_smooth<S><<<ngrid_half(s.lev[l]), blk, 0, st>>>(s.dlev, l, 1);
+            k_ns_smooth<S><<<ngrid_half(s.lev[l]), blk, 0, st>>>(s.dlev, l, 0);
         }
         cnt += 1 + 2 * s.nu;
     }
     return cnt;
 }
 
+// z = M r: the FP64 cycle works on z and r in place; the FP32 cycle on
+// FP32 copies (r -> r32, cycle, z32 -> z)
+static int ns_vcycle(NSolver& s, cudaStream_t st)
+{
+    if (s.prec == 0) return ns_vcycle_t<double>(s, st);
+    const dim3 blk(32, 8), gr = ngrid(s.prob);
+    k_ns_to32<<<gr, blk, 0, st>>>(s.prob, s.r, s.r32);
+    const int c = ns_vcycle_t<float>(s, st);
+    k_ns_to64<<<gr, blk, 0, st>>>(s.prob, s.z32, s.z);
+    return c + 2;
+}
+
 static int ns_body(NSolver& s, cudaStream_t st, cudaGraphConditionalHandle cond, int* cnt)
 {
     const dim3 blk(32, 8);
-    const NLevel& P = s.lev[0];  // cycle level 0 (x = z, b = r)
-    NLevel prob = P;             // the problem (x = the pressure)
+    const NLevel& P = s.prob;  // the Krylov level: FP64 couplings, level-0 layout
+    NLevel prob = P;           // the problem (x = the pressure)
     prob.x = s.lev_x0;
     const dim3 gr = ngrid(P);
     int c = ns_vcycle(s, st);
@@ -348,13 +399,13 @@ static int ns_body(NSolver& s, cudaStream_t st, cudaGraphConditionalHandle cond,
 int ns_record(NSolver& s, cudaStream_t st, cudaStream_t st2, bool eager, int* launches)
 {
     const dim3 blk(32, 8);
-    NLevel prob = s.lev[0];
+    NLevel prob = s.prob;
     prob.x = s.lev_x0;
     prob.b = s.lev_b0;
     const dim3 gr = ngrid(prob);
     int fixed = 0;
     k_ns_setup<<<1, 1, 0, st>>>(s.sc, s.tol * s.tol, s.maxit);
-    k_ns_sum<<<gr, blk, 0, st>>>(prob, prob.b, s.sc, s.partials);
+    k_ns_sum<<<gr, blk, 0, st>>>(prob, (const double*)prob.b, s.sc, s.partials);
     fixed += 2;
     cudaGraphConditionalHandle cond = 0;
     if (!eager) {
@@ -386,7 +437,7 @@ int ns_record(NSolver& s, cudaStream_t st, cudaStream_t st2, bool eager, int* la
         }
     }
     // zero-mean solution
-    k_ns_sum<<<gr, blk, 0, st>>>(prob, prob.x, s.sc, s.partials);
+    k_ns_sum<<<gr, blk, 0, st>>>(prob, (const double*)prob.x, s.sc, s.partials);
     k_ns_center<<<gr, blk, 0, st>>>(prob, s.sc, s.nfluid);
     fixed += 2;
     if (launches) *launches = fixed;
@@ -394,9 +445,23 @@ int ns_record(NSolver& s, cudaStream_t st, cudaStream_t st2, bool eager, int* la
 }
 
 int ns_build(NSolver& s, int nyn, int nxn, long long pitch, long long off, int per,
-             const uint8_t* hmask, double* x, double* b, double cx, double cy)
+             const uint8_t* hmask, double* x, double* b, double cx, double cy, int prec)
 {
     ns_free(s);
+    s.prec = prec;
+    const size_t es = prec == 0 ? 8 : 4;
+    // host couplings in the cycle's precision
+    auto conv = [&](const std::vector<double>& v) {
+        std::vector<unsigned char> out(v.size() * es);
+        for (size_t k = 0; k < v.size(); ++k) {
+            if (es == 8) memcpy(&out[k * 8], &v[k], 8);
+            else {
+                const float f = (float)v[k];
+                memcpy(&out[k * 4], &f, 4);
+            }
+        }
+        return out;
+    };
     auto dal = [&](size_t bytes) -> void* {
         void* p = nullptr;
         if (cudaMalloc(&p, bytes) != cudaSuccess) return nullptr;
@@ -449,8 +514,6 @@ int ns_build(NSolver& s, int nyn, int nxn, long long pitch, long long off, int p
     }
     NLevel L0;
     memset(&L0, 0, sizeof(L0));
-    L0.x = s.z;  // the cycle's level 0: x = z, b = r
-    L0.b = s.r;
     L0.fx = fx0;
     L0.fy = fy0;
     L0.m = m0;
@@ -459,6 +522,33 @@ int ns_build(NSolver& s, int nyn, int nxn, long long pitch, long long off, int p
     L0.pitch = pitch;
     L0.off = off;
     L0.per = per;
+    s.prob = L0;  // the Krylov level (x, b set per record)
+    if (prec == 0) {
+        L0.x = s.z;  // the cycle's level 0: x = z, b = r
+        L0.b = s.r;
+    } else {
+        // FP32 cycle: its own x, b and couplings in the level-0 layout
+        s.r32 = (float*)dal(n0 * 4);
+        s.z32 = (float*)dal(n0 * 4);
+        void* f32x = dal(n0 * 4);
+        void* f32y = dal(n0 * 4);
+        if (!s.r32 || !s.z32 || !f32x || !f32y) return 2;
+        std::vector<double> hx(n0, 0.0), hy(n0, 0.0);
+        for (int J = 0; J < nyn; ++J)
+            for (int I = 0; I < nxn; ++I) {
+                const size_t k = (size_t)(off + (long long)J * pitch + I);
+                hx[k] = fx[(size_t)J * nxn + I];
+                hy[k] = fy[(size_t)J * nxn + I];
+            }
+        const std::vector<unsigned char> cx4 = conv(hx), cy4 = conv(hy);
+        if (cudaMemcpy(f32x, cx4.data(), n0 * 4, cudaMemcpyHostToDevice) != cudaSuccess ||
+            cudaMemcpy(f32y, cy4.data(), n0 * 4, cudaMemcpyHostToDevice) != cudaSuccess)
+            return 2;
+        L0.x = s.z32;
+        L0.b = s.r32;
+        L0.fx = f32x;
+        L0.fy = f32y;
+    }
     s.lev.push_back(L0);
     s.lev_x0 = x;
     s.lev_b0 = b;
@@ -499,10 +589,10 @@ int ns_build(NSolver& s, int nyn, int nxn, long long pitch, long long off, int p
         C.off = 0;
         C.per = per;
         const size_t n = (size_t)C.pitch * cy_n;
-        double* dx_ = (double*)dal(n * 8);
-        double* db_ = (double*)dal(n * 8);
-        double* dfx = (double*)dal(n * 8);
-        double* dfy = (double*)dal(n * 8);
+        void* dx_ = dal(n * es);
+        void* db_ = dal(n * es);
+        void* dfx = dal(n * es);
+        void* dfy = dal(n * es);
         uint8_t* dm = (uint8_t*)dal(n);
         if (!dx_ || !db_ || !dfx || !dfy || !dm) return 2;
         std::vector<double> hx(n, 0.0), hy(n, 0.0);
@@ -513,8 +603,9 @@ int ns_build(NSolver& s, int nyn, int nxn, long long pitch, long long off, int p
                 hy[(size_t)J * C.pitch + I] = cfy[(size_t)J * cx_n + I];
                 hm[(size_t)J * C.pitch + I] = cm[(size_t)J * cx_n + I];
             }
-        if (cudaMemcpy(dfx, hx.data(), n * 8, cudaMemcpyHostToDevice) != cudaSuccess ||
-            cudaMemcpy(dfy, hy.data(), n * 8, cudaMemcpyHostToDevice) != cudaSuccess ||
+        const std::vector<unsigned char> hxs = conv(hx), hys = conv(hy);
+        if (cudaMemcpy(dfx, hxs.data(), n * es, cudaMemcpyHostToDevice) != cudaSuccess ||
+            cudaMemcpy(dfy, hys.data(), n * es, cudaMemcpyHostToDevice) != cudaSuccess ||
             cudaMemcpy(dm, hm.data(), n, cudaMemcpyHostToDevice) != cudaSuccess)
             return 2;
         C.x = dx_;
@@ -552,6 +643,7 @@ void ns_free(NSolver& s)
     s.sc = nullptr;
     s.partials = nullptr;
     s.r = s.z = s.p = s.q = nullptr;
+    s.r32 = s.z32 = nullptr;
 }
 
 }  // namespace f2d

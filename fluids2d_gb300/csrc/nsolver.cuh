@@ -12,10 +12,10 @@ namespace f2d {
 // fx(J, I) between cells (J, I-1) and (J, I) (column 0: the periodic wrap
 // face, else 0), fy(J, I) between (J-1, I) and (J, I) (row 0: 0).
 struct NLevel {
-    double* x;
-    double* b;
-    const double* fx;
-    const double* fy;
+    void* x;           // the level's precision (FP64; FP32 in the FP32 cycle)
+    void* b;
+    const void* fx;
+    const void* fy;
     const uint8_t* m;
     int nyn, nxn;
     long long pitch, off;
@@ -35,6 +35,9 @@ struct NSolver {
     DevScalars* sc = nullptr;     // iteration state (own)
     double* partials = nullptr;
     double *r = nullptr, *z = nullptr, *p = nullptr, *q = nullptr;  // level-0 layout
+    float *r32 = nullptr, *z32 = nullptr;  // the FP32 cycle's level 0
+    NLevel prob;                  // the Krylov level: FP64 couplings, level-0 layout
+    int prec = 0;                 // 0: FP64 cycle; 1: FP32 cycle
     double* lev_x0 = nullptr;     // the problem: x (the pressure) and b
     double* lev_b0 = nullptr;
     long long nfluid = 0;
@@ -49,7 +52,7 @@ struct NSolver {
 // the cells of the model layout: x = the pressure field, b = the right-hand
 // side (both FP64, level-0 layout). cx = dy/dx (E-W), cy = dx/dy (N-S).
 int ns_build(NSolver& s, int nyn, int nxn, long long pitch, long long off, int per,
-             const uint8_t* hmask, double* x, double* b, double cx, double cy);
+             const uint8_t* hmask, double* x, double* b, double cx, double cy, int prec);
 void ns_free(NSolver& s);
 // Record a solve on `st` (conditional WHILE body on st2 under capture, or
 // host-driven loops otherwise): b is made zero-mean over the fluid cells (the
