@@ -12,11 +12,16 @@ conditions, WENO5, SSP-RK3, per-member CFL, in the FP32 + FP64-refinement
 form; the same run times the plain FP64 form on the same members and reports
 the speed-up and the relative L2 difference of the vorticity between the two
 forms. Other workloads: rsw512 (rotating shallow water channel), eulerpsi256,
-qg1024/qg4096, each also with a _fp32 suffix. Inputs are seeded synthetic
-fields of those configurations' shapes; no dataset is involved.
+eulerpsi512, qg1024/qg4096, euler512, boussinesq512, qgrsw512 (and 1024^2
+profiling sizes), each also with a _fp32 suffix; adjoint512 (the discrete
+adjoint's cost and finite-difference check). Inputs are seeded synthetic
+fields of those configurations' shapes; no dataset is involved. Before the
+warm-up the multigrid autotuner picks the solver's schedule (reported as
+config.schedule; --no-autotune keeps the default).
 
   python bench.py [--gpus N] [--steps K] [--warmup W] [--impl gb300|reference]
-                  [--workload rsw512|eulerpsi256|qg4096|...]
+                  [--workload rsw512|eulerpsi256|qg4096|...] [--no-autotune]
+                  [--no-cpu-baseline] [--no-fp64-form]
 
 --impl gb300 (default): device-timed steps with L2 flushed between steps
 (`value`), end-to-end steps through the C ABI with the prognostic state
