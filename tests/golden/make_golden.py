@@ -202,9 +202,15 @@ def run_model(case, nsteps, fname, cfl=None, extra=None, setup=None):
             getattr(getattr(m.state, k.split(".")[0]), k.split(".")[1])[:] = v
         else:
             getattr(m.state, k)[:] = v
+    pre = {}
     if setup is not None:
         # an initial-state operator of the reference (e.g. qg_projection);
-        # the fixture's initial condition is the state it leaves
+        # the fixture's initial condition is the state it leaves, the state
+        # it was applied to is kept as pre/<field>
+        for name in setup.fields:
+            v = getattr(m.state, name.split(".")[0])
+            v = getattr(v, name.split(".")[1]) if "." in name else v
+            pre[name] = v.copy()
         setup(m)
         case = dict(case)
         case["fields"] = {}
@@ -229,6 +235,8 @@ def run_model(case, nsteps, fname, cfl=None, extra=None, setup=None):
         out["tracer"] = np.array(extra["tracer"])
     for k, v in case["fields"].items():
         out["ic/" + k] = v.copy()
+    for k, v in pre.items():
+        out["pre/" + k] = v
 
     def dump(prefix):
         for name in m.state._fields:

@@ -197,3 +197,23 @@ def test_bulk_diagnostics_vs_reference(fname):
     for c in range(5):
         scale = max(np.abs(ref[:, c]).max(), 1e-300)
         assert np.abs(got[:, c] - ref[:, c]).max() <= 1e-12 * scale, c
+
+
+@pytest.mark.parametrize("fname", ["model_qgrsw.npz", "model_qgrsw_periodic.npz",
+                                   "model_qgrsw_tracer.npz"])
+def test_qg_projection_state_form_vs_reference(fname):
+    """qg_projection (operators.py:176-183, anomaly=False) of the state the
+    reference applied it to (pre/...) against the state it left (ic/...),
+    nan where the reference divides by a zero count of wet vertices."""
+    g = load(fname)
+    m = oracle_from_golden(g)
+    s = m.s
+    for k in ("u.x", "u.y", "h", "pv", "psi"):
+        s[k][:] = g["pre/" + k]
+    O.qg_projection(m.mesh, s["u.x"], s["u.y"], s["h"], s["pv"], s["psi"])
+    for k in ("u.x", "u.y", "h", "pv", "psi"):
+        ref = g["ic/" + k]
+        fin = np.isfinite(ref)
+        np.testing.assert_array_equal(np.isfinite(s[k]), fin, err_msg=k)
+        scale = max(np.abs(ref[fin]).max(), 1e-300)
+        assert np.abs(s[k][fin] - ref[fin]).max() <= 1e-12 * scale, k
