@@ -1,5 +1,9 @@
-// C ABI of the library: models, fields, time stepping captured into CUDA
-// graphs, and the Poisson solve (include/fluids2d_gb300.h).
+// C ABI of the library (include/fluids2d_gb300.h): models (eulerpsi, rsw,
+// qg, euler, boussinesq, qgrsw, with an optional tracer), fields, time
+// stepping recorded once per parity into CUDA graphs (step, run, diagnostics,
+// qg_projection, the adjoint's snapshot and adjoint steps), the Poisson and
+// Neumann solves, the multigrid autotuner, Bulk diagnostics and float32
+// snapshots.
 #include <cudaTypedefs.h>
 
 #include <algorithm>

@@ -1,10 +1,16 @@
-// Fused time-stepping kernels.
+// Fused time-stepping kernels and the element-wise kernels around them.
 //
 // One launch per RK stage computes the right-hand side of the reference's
-// equation set AND applies the SSP-RK3 increment (integrators.py:92-107,
-// addto 154-196) over a tile (32x32 cells for the flux-form models, 32x8
-// for rsw), with the stencil inputs staged in shared
-// memory by TMA (halo of 3 cells) and every face flux evaluated once.
+// equation set AND applies the integrator's update (SSP-RK3, ef, enrk3 or
+// the LFRA step; integrators.py:20-155, addto 154-196) over a tile (32x32
+// cells for the flux-form models and the tracer, 32x8 for the momentum
+// kernel of rsw, euler, boussinesq and qgrsw), with the stencil inputs
+// staged in shared memory by TMA (halo of 3 cells) and every face flux
+// evaluated once. qgrsw's momentum launch writes the raw tendency; its
+// projection around the Helmholtz solve and the update follow in
+// k_qgrsw_pv / k_qgrsw_update. Also here: the diagnostics (vertex average,
+// perpgrad, rsw/euler diagnostics, max|U|), the euler pressure projection
+// around the Neumann solve, the Bulk reduction and the float32 snapshot.
 //
 // Every array point is produced with the numpy-slice semantics of the
 // reference operators, including the halo rows and columns (the reference
