@@ -3,8 +3,11 @@
 CPU restatement of the reference's time-stepping path (pvthinker/Fluids2d):
 mesh masks and stencil orders, the flat-index flux sweeps (through the C
 restatement in ``sweeps.c``), the staggered C-grid operators, the masked
-5-point Poisson/Helmholtz operator solved with SuperLU, SSP-RK3 in increment
-form and the CFL time step. It serves three purposes:
+5-point Poisson/Helmholtz operators (vertex Dirichlet and cell-centred
+Neumann) solved with SuperLU, the eulerpsi, rsw, qg, euler, boussinesq and
+qgrsw equation sets with the passive tracer, the rk3/ef/enrk3/LFRA
+integrators, the CFL time step and the Bulk diagnostics. It serves three
+purposes:
 
 * the checker of the CUDA path in ``tests/`` and in ``__graft_entry__.smoke``;
 * the CPU-baseline leg of ``bench.py`` (numba-equivalent sweeps threaded
