@@ -126,6 +126,7 @@ _SIGS = {
                             c_dbl, c_void_p, c_void_p], c_int),
     "f2d_stats": ([c_void_p, ctypes.POINTER(c_i64), ctypes.POINTER(c_i64),
                    ctypes.POINTER(c_i64)], c_int),
+    "f2d_test_tma_wait": ([c_int, c_dbl], c_int),
 }
 
 

@@ -225,12 +225,6 @@ static const CUtensorMap* tmap(f2d_model_s* m, void* buf) { return &m->tmaps[buf
 // ---------------------------------------------------------------------------
 // Recording of diag / stage / step on a stream (eager or under capture).
 // ---------------------------------------------------------------------------
-static double env_double(const char* name, double dflt)
-{
-    const char* v = getenv(name);
-    return (v && *v) ? atof(v) : dflt;
-}
-
 static int ensure_mg(f2d_model_s* m, int which)
 {
     if (m->bs_ready[which]) return 0;
@@ -272,10 +266,11 @@ static int ensure_mg(f2d_model_s* m, int which)
     if (e) return fail(e, "multigrid setup failed");
     bs.tol = m->p.poisson_tol;
     bs.maxit = m->p.poisson_maxit;
-    bs.tol_in = env_double("F2D_TOL_IN", 1e-6);
-    bs.maxit_in = (int)env_double("F2D_MAXIT_IN", 30);
+    // default schedule (the autotuner may change tol_in and nu)
+    bs.tol_in = 1e-6;
+    bs.maxit_in = 30;
     bs.maxouter = std::max(2, m->p.poisson_maxit / 10);
-    bs.nu = (int)env_double("F2D_NU", 2);
+    bs.nu = 2;
     m->bs_ready[which] = true;
     return 0;
 }
@@ -1426,9 +1421,23 @@ int f2d_sync(f2d_model m)
         std::string msg = "device status:";
         if (st & ST_TMA_TIMEOUT) msg += " TMA tile load timed out;";
         if (st & ST_PCG_MAXIT) msg += " Poisson solve reached max iterations;";
-        if (st & ST_NONFINITE) msg += " non-finite residual;";
+        if (st & ST_NONFINITE) msg += " non-finite value (residual or time step);";
         return fail(100 + st, msg);
     }
+    return 0;
+}
+
+int f2d_test_tma_wait(int enabled, double limit_ms)
+{
+    if (enabled && !(limit_ms > 0 && limit_ms <= 1000))
+        return fail(1, "f2d_test_tma_wait: limit_ms must be in (0, 1000]");
+    const unsigned long long ns =
+        enabled ? (unsigned long long)(limit_ms * 1e6) : 0ull;
+    CK(cudaDeviceSynchronize());
+    int e = tma_wait_test_set_stage(enabled, ns);
+    if (!e) e = tma_wait_test_set_ensemble(enabled, ns);
+    if (e) return fail(e, std::string("f2d_test_tma_wait: ") +
+                              cudaGetErrorString((cudaError_t)e));
     return 0;
 }
 

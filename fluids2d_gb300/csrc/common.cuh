@@ -39,6 +39,13 @@ enum : int {
     ST_NONFINITE = 4,      // a non-finite value reached a reduction
 };
 
+// min(x, cap) with Python's min semantics (the reference's set_dt,
+// model.py:87: min(cfl/maxU, dtmax)): x unless cap < x, so a NaN x stays NaN
+__host__ __device__ __forceinline__ double pymin(double x, double cap)
+{
+    return cap < x ? cap : x;
+}
+
 // Device-resident scalars of one model: the time line (timeline.py:4-35),
 // the CFL reduction and the Poisson-solver state.
 struct DevScalars {
@@ -127,6 +134,17 @@ __device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity,
     }
 }
 
+// Maximum that propagates NaN, as numpy's max does (the reference's set_dt,
+// model.py:83-87, turns a NaN velocity into a NaN time step).
+__host__ __device__ __forceinline__ double nanmax(double a, double b)
+{
+    return (a > b || a != a) ? a : b;
+}
+__host__ __device__ __forceinline__ float nanmaxf(float a, float b)
+{
+    return (a > b || a != a) ? a : b;
+}
+
 // ---------------------------------------------------------------------------
 // Deterministic grid-wide reductions of up to N doubles: every block writes
 // its partial sums, the last block to finish (ticket counter) adds the
@@ -148,7 +166,7 @@ __device__ __forceinline__ void warp_max(double (&v)[N])
     for (int k = 0; k < N; ++k)
 #pragma unroll
         for (int o = 16; o > 0; o >>= 1)
-            v[k] = fmax(v[k], __shfl_xor_sync(0xffffffffu, v[k], o));
+            v[k] = nanmax(v[k], __shfl_xor_sync(0xffffffffu, v[k], o));
 }
 
 // Block-wide reduction; result valid in thread 0. `sh` needs 32*N doubles.
@@ -191,17 +209,17 @@ __device__ __forceinline__ void final_sum(double (&acc)[N], const double* partia
 #pragma unroll
             for (int k = 0; k < N; ++k) {
                 const double p = __ldcg(&partials[(size_t)(t0 + i + u * nth) * N + k]);
-                a[u][k] = MAX ? fmax(a[u][k], p) : a[u][k] + p;
+                a[u][k] = MAX ? nanmax(a[u][k], p) : a[u][k] + p;
             }
     for (int u = 0; i < n; i += nth, ++u)
 #pragma unroll
         for (int k = 0; k < N; ++k) {
             const double p = __ldcg(&partials[(size_t)(t0 + i) * N + k]);
-            a[u & 3][k] = MAX ? fmax(a[u & 3][k], p) : a[u & 3][k] + p;
+            a[u & 3][k] = MAX ? nanmax(a[u & 3][k], p) : a[u & 3][k] + p;
         }
 #pragma unroll
     for (int k = 0; k < N; ++k)
-        acc[k] = MAX ? fmax(fmax(a[0][k], a[1][k]), fmax(a[2][k], a[3][k]))
+        acc[k] = MAX ? nanmax(nanmax(a[0][k], a[1][k]), nanmax(a[2][k], a[3][k]))
                      : (a[0][k] + a[1][k]) + (a[2][k] + a[3][k]);
 }
 
@@ -341,7 +359,7 @@ __device__ __forceinline__ void block_total_f(const float (&a)[N], double (&out)
 #pragma unroll
         for (int o = 16; o > 0; o >>= 1) {
             const float u = __shfl_xor_sync(0xffffffffu, v[k], o);
-            v[k] = MAX ? fmaxf(v[k], u) : v[k] + u;
+            v[k] = MAX ? nanmaxf(v[k], u) : v[k] + u;
         }
     }
     const int tid = threadIdx.y * blockDim.x + threadIdx.x;
@@ -356,7 +374,7 @@ __device__ __forceinline__ void block_total_f(const float (&a)[N], double (&out)
         for (int k = 0; k < N; ++k) {
             double t = MAX ? -INFINITY : 0.0;
             for (int i = 0; i < nw; ++i)
-                t = MAX ? fmax(t, (double)shf[i * N + k]) : t + (double)shf[i * N + k];
+                t = MAX ? nanmax(t, (double)shf[i * N + k]) : t + (double)shf[i * N + k];
             out[k] = t;
         }
 }

@@ -156,8 +156,8 @@ __global__ void k_ens_perpgrad(const int4* __restrict__ tiles, const Member* __r
                 Ux[o] = ux;
                 Uy[o] = uy;
             }
-            m[0] = fmax(m[0], fabs(ux));
-            m[1] = fmax(m[1], fabs(uy));
+            m[0] = nanmax(m[0], fabs(ux));
+            m[1] = nanmax(m[1], fabs(uy));
         }
     }
     DevScalars& sc = scs[tl.x];
@@ -185,12 +185,14 @@ __global__ void k_ens_fill_psi(const Member* __restrict__ mem, EnsArenas a, int 
     }
 }
 
-__global__ void k_ens_set_dt(DevScalars* scs, int n)
+__global__ void k_ens_set_dt(DevScalars* scs, int n, EnsGlobals* eg)
 {
     const int b = blockIdx.x * blockDim.x + threadIdx.x;
     if (b >= n) return;
     DevScalars& s = scs[b];
-    s.dt = fmin(s.cfl / (s.maxUx + s.maxUy + 1e-99), s.dtmax);
+    const double dt = pymin(s.cfl / (s.maxUx + s.maxUy + 1e-99), s.dtmax);
+    s.dt = dt;
+    if (!(dt == dt)) atomicOr(&eg->status, ST_NONFINITE);  // a NaN velocity
 }
 
 __global__ void k_ens_pushforward(DevScalars* scs, int n)
@@ -317,7 +319,7 @@ static int ens_record_diag(f2d_ensemble_s* e, int par, cudaStream_t s)
 static int ens_record_step(f2d_ensemble_s* e, int par, cudaStream_t s)
 {
     const dim3 blk(32, 8);
-    k_ens_set_dt<<<(e->n + 127) / 128, 128, 0, s>>>(e->scs, e->n);
+    k_ens_set_dt<<<(e->n + 127) / 128, 128, 0, s>>>(e->scs, e->n, e->eg);
     e->rec += 1;
     const int nst = e->p.integrator == F2D_INTEG_EF || e->p.integrator == F2D_INTEG_LFRA
                         ? 1 : 3;  // odd: flips the parity
@@ -396,6 +398,17 @@ static void* ens_field(f2d_ensemble_s* e, const char* name, int* es)
     if (!strcmp(name, pv ? "work" : "vomega")) return e->ar.rhs;
     return nullptr;
 }
+
+namespace f2d {
+int tma_wait_test_set_ensemble(int enabled, unsigned long long limit_ns)
+{
+    TmaWaitTest v;
+    v.enabled = enabled ? 1u : 0u;
+    v.pad = 0;
+    v.limit_ns = limit_ns;
+    return (int)cudaMemcpyToSymbol(g_tma_wait_test, &v, sizeof(v));
+}
+}  // namespace f2d
 
 extern "C" {
 
@@ -550,11 +563,10 @@ int f2d_ensemble_create(const f2d_params* p, int count, const int* nxs, const in
         if (r) return bail(f2d_internal_fail(r, "ensemble multigrid set-up failed"));
         e->bs.tol = p->poisson_tol;
         e->bs.maxit = p->poisson_maxit;
-        const char* ti = getenv("F2D_TOL_IN");
-        e->bs.tol_in = (ti && *ti) ? atof(ti) : 1e-6;
+        // default schedule (the autotuner may change tol_in and nu)
+        e->bs.tol_in = 1e-6;
         e->bs.maxouter = std::max(2, p->poisson_maxit / 10);
-        const char* nu = getenv("F2D_NU");
-        e->bs.nu = (nu && *nu) ? atoi(nu) : 2;
+        e->bs.nu = 2;
     }
     e->ncell = (int)cells.size();
     e->cell_tiles = (int4*)ens_alloc(e, cells.size() * sizeof(int4));
@@ -801,7 +813,7 @@ int f2d_ensemble_sync(f2d_ensemble e)
         std::string msg = "ensemble device status:";
         if (h.status & ST_TMA_TIMEOUT) msg += " TMA tile load timed out;";
         if (h.status & ST_PCG_MAXIT) msg += " a Poisson solve reached max iterations;";
-        if (h.status & ST_NONFINITE) msg += " non-finite residual;";
+        if (h.status & ST_NONFINITE) msg += " non-finite value (residual or time step);";
         return f2d_internal_fail(100 + h.status, msg.c_str());
     }
     return 0;

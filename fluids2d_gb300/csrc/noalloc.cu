@@ -1,14 +1,13 @@
 // CFL time step from caller-owned device arrays, without allocating.
 //
-// Some callers cannot call cudaMalloc: code running while a stream is being
-// captured into a CUDA graph (an allocation there is not part of the graph
-// and may synchronise the device), frameworks that own all device memory
+// Some callers cannot call cudaMalloc: frameworks that own all device memory
 // through their own pool allocator and forbid allocations behind their back,
-// and latency-critical loops where cudaMalloc/cudaFree would synchronise the
-// device. For them f2d_cfl_dt_noalloc computes Model.set_dt's CFL step with
-// its reduction scratch (per-block partial maxima and a ticket counter) in a
-// fixed array that is part of the library image, so a call allocates
-// nothing.
+// and latency-critical loops where a cudaMalloc/cudaFree would synchronise
+// the device. For them f2d_cfl_dt_noalloc computes Model.set_dt's CFL step
+// with its reduction scratch (per-block partial maxima and a ticket counter)
+// in a fixed array that is part of the library image, so a call allocates
+// nothing. A NaN in U.x or U.y gives NaN maxima and a NaN time step, as
+// numpy's max and Python's min give in the reference's set_dt.
 //
 // The scratch array holds 8192 blocks' partials (128 KiB + 256 B) and stays
 // resident on every GPU that loads the library until the process exits. It
@@ -18,6 +17,10 @@
 // the GPU (different streams, or other threads) race on it and give wrong
 // results; serialise them on one stream. The ticket counter is cleared at the
 // start of each call; the partials are fully rewritten by every call.
+// The device address of the array is looked up on the first call on each
+// device and kept for the life of the process: a cudaDeviceReset after that
+// first call is not supported (the kept address would belong to the
+// destroyed context).
 #include <mutex>
 #include <string>
 
@@ -62,14 +65,14 @@ k_cfl_dt_noalloc(const double* __restrict__ Ux, const double* __restrict__ Uy,
          k += stride) {
         const long long j = k / pitch;
         if (k - j * pitch < cols) {
-            m[0] = fmax(m[0], fabs(Ux[k]));
-            m[1] = fmax(m[1], fabs(Uy[k]));
+            m[0] = nanmax(m[0], fabs(Ux[k]));
+            m[1] = nanmax(m[1], fabs(Uy[k]));
         }
     }
     if (grid_reduce<2, true>(m, scr->partials, &scr->ticket)) {
         out[0] = m[0];
         out[1] = m[1];
-        out[2] = fmin(cfl / (m[0] + m[1] + 1e-99), dtmax);
+        out[2] = pymin(cfl / (m[0] + m[1] + 1e-99), dtmax);
     }
 }
 

@@ -379,8 +379,8 @@ __global__ void k_perpgrad(const P* __restrict__ psi, T* __restrict__ Ux,
                 Ux[o] = ux;
                 Uy[o] = uy;
             }
-            m[0] = fmax(m[0], fabs(ux));
-            m[1] = fmax(m[1], fabs(uy));
+            m[0] = nanmax(m[0], fabs(ux));
+            m[1] = nanmax(m[1], fabs(uy));
         }
     }
     constexpr bool F = std::is_same<T, float>::value;
@@ -438,7 +438,9 @@ __global__ void k_fill_periodic(T* __restrict__ a, Geom g)
 __global__ void k_set_dt(DevScalars* sc)
 {
     const double maxU = sc->maxUx + sc->maxUy + 1e-99;
-    sc->dt = fmin(sc->cfl / maxU, sc->dtmax);
+    const double dt = pymin(sc->cfl / maxU, sc->dtmax);
+    sc->dt = dt;
+    if (!(dt == dt)) sc->status |= ST_NONFINITE;  // a NaN velocity
 }
 
 // Time.pushforward (timeline.py:20-35): Kahan-summed t, ite += 1
@@ -598,6 +600,16 @@ int launch_fill_periodic(int prec, void* a, const Geom& g, cudaStream_t s)
     if (prec == 0) k_fill_periodic<double><<<grid, block, 0, s>>>((double*)a, g);
     else k_fill_periodic<float><<<grid, block, 0, s>>>((float*)a, g);
     return (int)cudaGetLastError();
+}
+
+// the TMA wait test switch of this translation unit's stage kernels
+int tma_wait_test_set_stage(int enabled, unsigned long long limit_ns)
+{
+    TmaWaitTest v;
+    v.enabled = enabled ? 1u : 0u;
+    v.pad = 0;
+    v.limit_ns = limit_ns;
+    return (int)cudaMemcpyToSymbol(g_tma_wait_test, &v, sizeof(v));
 }
 
 int launch_set_dt(DevScalars* sc, cudaStream_t s)

@@ -52,6 +52,10 @@ int launch_maxabs2(int prec, const void* Ux, const void* Uy, const Geom& g,
                    DevScalars* sc, double* partials, cudaStream_t s);
 int launch_fill_periodic(int prec, void* a, const Geom& g, cudaStream_t s);
 int launch_set_dt(DevScalars* sc, cudaStream_t s);
+// the failure-detection test switch of the stage kernels' TMA waits, one per
+// translation unit (stage.cu, ensemble.cu)
+int tma_wait_test_set_stage(int enabled, unsigned long long limit_ns);
+int tma_wait_test_set_ensemble(int enabled, unsigned long long limit_ns);
 int launch_pushforward(DevScalars* sc, cudaStream_t s);
 size_t pt_grid_blocks(const Geom& g);
 // euler pressure projection around the Neumann solve

@@ -14,6 +14,25 @@ constexpr int OX = 4, OY = 3;            // offset of cell (j0,i0) in the tile
 // 2.19x staged cells per cell.
 constexpr int FRT = 4, FTY = 8 * FRT, FSH = FTY + 6;
 
+// Test hook of the failure detection (f2d_test_tma_wait). When enabled,
+// every stage kernel, once its TMA tile has landed, also waits for the next
+// phase of the tile's barrier, which nothing completes (no thread arrives
+// again), so that wait runs out after limit_ns: the kernel sets
+// ST_TMA_TIMEOUT and returns with no copy in flight. One copy of the switch
+// per translation unit.
+struct TmaWaitTest {
+    unsigned int enabled;
+    unsigned int pad;
+    unsigned long long limit_ns;
+};
+static __device__ TmaWaitTest g_tma_wait_test;
+
+__device__ __forceinline__ bool tma_wait_test(uint64_t* bar)
+{
+    if (!g_tma_wait_test.enabled) return true;
+    return mbar_wait(bar, 1, g_tma_wait_test.limit_ns);
+}
+
 template <typename T>
 __device__ __forceinline__ T ldz(const T* __restrict__ a, int j, int i,
                                  const Geom& g)
@@ -154,7 +173,7 @@ __device__ __forceinline__ bool stage_tiles(T (*s0)[SW], const CUtensorMap* m0,
         tma_load_2d(&s0[0][0], m0, i0 - OX, j0 - OY, bar);
         if (s1) tma_load_2d(&s1[0][0], m1, i0 - OX, j0 - OY, bar);
     }
-    bool ok = mbar_wait(bar, 0);
+    bool ok = mbar_wait(bar, 0) && tma_wait_test(bar);
     int all = __syncthreads_and(ok ? 1 : 0);
     if (!all && t == 0) atomicOr(status, ST_TMA_TIMEOUT);
     return all != 0;
@@ -236,7 +255,7 @@ __device__ __forceinline__ void fluxform_tile(
     }
     // 3. wait for the tile (bounded; uniform time-out exit)
     {
-        const bool ok = mbar_wait(&sm.bar, 0);
+        const bool ok = mbar_wait(&sm.bar, 0) && tma_wait_test(&sm.bar);
         const int all = __syncthreads_and(ok ? 1 : 0);
         if (!all) {
             if (t == 0) atomicOr(status, ST_TMA_TIMEOUT);

@@ -192,6 +192,14 @@ int f2d_autotune(f2d_model m, int reps, int *tile_rows, int *sweeps, double *tol
  * reference counterpart. The model must have solved once. */
 int f2d_time_solver(f2d_model m, int reps, int flush_l2, double *avg_ms,
                     int64_t *nodes, int *elem_bytes);
+/* Failure-detection test switch (no reference counterpart). enabled != 0:
+ * every stage kernel, once its TMA tile has landed, also waits for a barrier
+ * phase that nothing completes, gives up after limit_ms (0 < limit_ms <=
+ * 1000) and records the TMA time-out status, which the next f2d_sync /
+ * f2d_ensemble_sync reports; the stage's output is then not written.
+ * enabled == 0 restores normal operation. Applies to every model and
+ * ensemble of the process; synchronises the device. For tests only. */
+int f2d_test_tma_wait(int enabled, double limit_ms);
 /* Counters: Poisson iterations summed over all solves since creation; the
  * kernels one time step launches outside the Poisson loops; the kernels one
  * Poisson iteration launches. No reference counterpart (instrumentation). */
@@ -283,9 +291,9 @@ int f2d_adjoint_backward(f2d_model m, const double *lamT, double *lam0);
 /* ---- allocation-free entry point ---------------------------------------- */
 
 /* No counterpart in the reference. For callers that must not allocate
- * device memory (code recording a stream into a CUDA graph, frameworks that
- * route all device memory through their own pool, loops where a cudaMalloc
- * would synchronise the device): Model.set_dt's CFL step computed from
+ * device memory (frameworks that route all device memory through their own
+ * pool, loops where a cudaMalloc would synchronise the device):
+ * Model.set_dt's CFL step computed from
  * caller-owned device arrays U.x, U.y of rows x cols points with row pitch
  * `pitch` (elements). Writes out[0] = max|U.x|, out[1] = max|U.y|,
  * out[2] = min(cfl / (out[0] + out[1] + 1e-99), dtmax) to the caller's device
@@ -293,9 +301,11 @@ int f2d_adjoint_backward(f2d_model m, const double *lamT, double *lam0);
  * Its reduction scratch is a fixed 128 KiB array inside the library, kept by
  * every GPU that loads the library until exit, so rows * pitch is limited to
  * 33,554,432 points (larger arrays are refused with an error). The first call
- * on each device looks up that array's device address; make that first call
- * before any stream capture. Calls share the array: calls that overlap on the
- * GPU race and give wrong results, so serialise them on one stream. */
+ * on each device looks up that array's device address (kept until exit, so
+ * cudaDeviceReset after it is not supported); make that first call before
+ * any stream capture. Calls share the array: calls that overlap on the GPU
+ * race and give wrong results, so serialise them on one stream. A NaN in U
+ * gives NaN in out, as numpy's max gives in the reference's set_dt. */
 int f2d_cfl_dt_noalloc(const double *Ux, const double *Uy, int64_t rows,
                        int64_t cols, int64_t pitch, double cfl, double dtmax,
                        double *out, void *stream);

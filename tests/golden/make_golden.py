@@ -2,7 +2,7 @@
 
 Usage (needs the reference source tree, see ``refstubs.py``)::
 
-    python tests/golden/make_golden.py
+    F2D_REFERENCE_SRC=<reference checkout>/src python tests/golden/make_golden.py
 
 Each fixture is a compressed ``.npz`` holding the inputs and the outputs of
 the unmodified reference code (``src/fluids2d``) on small seeded cases:

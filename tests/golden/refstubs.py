@@ -17,7 +17,9 @@ import os
 import sys
 import types
 
-REFERENCE_SRC = os.environ.get("F2D_REFERENCE_SRC", "/root/reference/src")
+# the reference's ``src`` directory (the one holding the ``fluids2d``
+# package); required, no default
+REFERENCE_SRC = os.environ.get("F2D_REFERENCE_SRC", "")
 
 
 def _install_stubs():
@@ -45,8 +47,10 @@ def _install_stubs():
 
 def load_reference():
     """Return the reference ``fluids2d`` package (with stand-in modules)."""
-    if not os.path.isdir(REFERENCE_SRC):
-        raise RuntimeError(f"reference source tree not found: {REFERENCE_SRC}")
+    if not REFERENCE_SRC or not os.path.isdir(REFERENCE_SRC):
+        raise RuntimeError(
+            "set F2D_REFERENCE_SRC to the reference's src directory (the one "
+            f"holding the fluids2d package); got {REFERENCE_SRC!r}")
     _install_stubs()
     if REFERENCE_SRC not in sys.path:
         sys.path.insert(0, REFERENCE_SRC)

@@ -17,12 +17,23 @@ from oracle import oracle as O
 G = np.load(os.path.join(GOLDEN, "mesh.npz"), allow_pickle=False)
 
 
+def _noslip(text):
+    """param.noslip from its fixture text: None, True, False or a list of
+    side names such as "['left', 'top']"."""
+    fixed = {"None": None, "True": True, "False": False}
+    if text in fixed:
+        return fixed[text]
+    if text.startswith("[") and text.endswith("]"):
+        return [w.strip().strip("'\"") for w in text[1:-1].split(",") if w.strip()]
+    raise ValueError(f"unexpected noslip fixture value {text!r}")
+
+
 def _param(case):
     nx, ny, xper, maxo = (int(v) for v in G[case + "/params"])
     p = Param()
     p.model = "rsw"
     p.nx, p.ny, p.xperiodic, p.maxorder = nx, ny, bool(xper), maxo
-    p.noslip = eval(str(G[case + "/noslip"]))
+    p.noslip = _noslip(str(G[case + "/noslip"]))
     return p
 
 

@@ -1,9 +1,9 @@
 """The allocation-free CFL entry point, f2d_cfl_dt_noalloc, against the
 model's own set_dt.
 
-Callers that cannot allocate device memory (graph-recording code, pool-managed
-frameworks, synchronisation-free loops) use f2d_cfl_dt_noalloc with their own
-device arrays; it must give the same max|U| and time step as the existing
+Callers that cannot allocate device memory (frameworks that route all device
+memory through their own pool, loops where a cudaMalloc would synchronise the
+device) use f2d_cfl_dt_noalloc with their own device arrays; it must give the same max|U| and time step as the existing
 path (f2d_field_set -> f2d_set_dt -> f2d_time_get), call after call, although
 its scratch array is shared and reused. Tolerance: 1e-10 relative, as in the
 other GPU parity tests (a maximum is exact, so equality is expected).
@@ -99,3 +99,35 @@ def test_noalloc_cfl_dtmax_and_size_limit():
                                   ctypes.c_void_p(out.data_ptr()), None)
     assert rc != 0
     assert b"too large" in lib().f2d_last_error()
+
+
+def test_noalloc_cfl_propagates_nan_like_set_dt():
+    """A NaN in U gives NaN maxima and a NaN time step, as np.max and min()
+    give in the reference's set_dt (model.py:83-87), and as the model's own
+    set_dt gives; a finite U afterwards gives finite values again."""
+    m = _model(64, 48)
+    rows, cols = m.mesh.shape
+    pux, pitch = _device(m, "U.x")
+    puy, _ = _device(m, "U.y")
+    out = torch.zeros(3, dtype=torch.float64, device="cuda")
+    rng = np.random.default_rng(7)
+    ux = rng.normal(size=m.mesh.shape)
+    uy = rng.normal(size=m.mesh.shape)
+    ux[10, 11] = np.nan
+    dt_ref = _existing_dt(m, ux, uy)
+    assert np.isnan(dt_ref)
+    with pytest.raises(f2d.F2DError, match="non-finite"):
+        m.sync()
+    check(lib().f2d_cfl_dt_noalloc(pux, puy, rows, cols, pitch, 0.8, 9e99,
+                                   ctypes.c_void_p(out.data_ptr()), None))
+    torch.cuda.synchronize()
+    got = out.cpu().numpy()
+    assert np.isnan(got[0]) and not np.isnan(got[1]) and np.isnan(got[2])
+    ux[10, 11] = 0.0
+    dt_ref = _existing_dt(m, ux, uy)
+    check(lib().f2d_cfl_dt_noalloc(pux, puy, rows, cols, pitch, 0.8, 9e99,
+                                   ctypes.c_void_p(out.data_ptr()), None))
+    torch.cuda.synchronize()
+    got = out.cpu().numpy()
+    assert np.isfinite(got).all() and abs(got[2] - dt_ref) <= TOL * dt_ref
+    m.sync()
