@@ -127,6 +127,10 @@ _SIGS = {
     "f2d_stats": ([c_void_p, ctypes.POINTER(c_i64), ctypes.POINTER(c_i64),
                    ctypes.POINTER(c_i64)], c_int),
     "f2d_test_tma_wait": ([c_int, c_dbl], c_int),
+    "f2d_rhs": ([c_void_p], c_int),
+    "f2d_stage": ([c_void_p, c_int], c_int),
+    "f2d_forcing_set": ([c_void_p, ctypes.c_char_p, c_void_p], c_int),
+    "f2d_forcing_clear": ([c_void_p], c_int),
 }
 
 
@@ -179,7 +183,7 @@ def params_struct(p):
     s.compflux = METHODS[p.compflux]
     s.vortexforce = METHODS[p.vortexforce]
     ip = p.innerproduct
-    s.innerproduct = METHODS[ip] if ip in METHODS else -1
+    s.innerproduct = 4 if ip == "classic" else METHODS[ip]
     s.maxorder = int(p.maxorder)
     ns = p.noslip
     if ns is None or ns is False:

@@ -131,9 +131,15 @@ struct f2d_model_s {
     std::map<void*, CUtensorMap> tmaps;
     int cur = 0;
     // graphs: [kind][parity]; kinds: 0 diag, 1 step, 2 run, 3 solve0, 4 solve1,
-    // 5 step with adjoint snapshots, 6 adjoint step
-    cudaGraphExec_t gx[7][2] = {};
-    int launches[7][2] = {};
+    // 5 step with adjoint snapshots, 6 adjoint step, 7 right-hand side alone,
+    // 8-10 integrator stage 1-3 (with its diagnostics; the last stage of a
+    // step also advances the time line)
+    cudaGraphExec_t gx[11][2] = {};
+    int launches[11][2] = {};
+    // prognostic variables (states.py:22-34 order) and whether the forcing
+    // fields "frc.<var>" exist
+    std::vector<std::string> prog;
+    bool has_frc = false;
     AdjState adj;
     // euler: the Neumann cell-centred pressure solve and its right-hand side
     NSolver ns;
@@ -424,20 +430,33 @@ static int rec_diag(f2d_model_s* m, int par, cudaStream_t s)
     return fail(5, "unknown model");
 }
 
-static int rec_qgrsw_stage(f2d_model_s* m, int k, int par, cudaStream_t s);
+static int rec_qgrsw_stage(f2d_model_s* m, int k, int par, cudaStream_t s, bool tend);
 
-// the fused right-hand-side + RK3-update kernel of stage k, parity par -> 1-par
-static int launch_stage_kernel(f2d_model_s* m, int k, int par, cudaStream_t s)
+// the forcing field of prognostic variable f (null without forcing)
+static void* frc(f2d_model_s* m, const char* f)
+{
+    return m->has_frc ? fb(m, (std::string("frc.") + f).c_str()) : nullptr;
+}
+
+// the fused right-hand-side + RK3-update kernel of stage k, parity par -> 1-par;
+// tend: the right-hand side alone (the reference's rhs(s, ds), with any
+// forcing term) into the fields "rhs.<var>", the state untouched
+static int launch_stage_kernel(f2d_model_s* m, int k, int par, cudaStream_t s,
+                               bool tend = false)
 {
     const Geom& g = m->g;
     const int out = 1 - par;
-    const bool lf = m->p.integrator == F2D_INTEG_LFRA;
+    const bool lf = m->p.integrator == F2D_INTEG_LFRA && !tend;
+    const int sk = tend ? (1 | (INTEG_TENDENCY << 4)) : (k | (m->p.integrator << 4));
     auto ds = [&](const char* f, int kk) -> void* {
         return fb(m, (std::string("ds") + std::to_string(kk) + "." + f).c_str());
     };
+    auto rhs = [&](const char* f) -> void* {
+        return fb(m, (std::string("rhs.") + f).c_str());
+    };
     if (m->p.model == F2D_MODEL_QGRSW) {
         // tendency, projection and update (counts its own launches)
-        int e = rec_qgrsw_stage(m, k, par, s);
+        int e = rec_qgrsw_stage(m, k, par, s, tend);
         if (e) return e;
     } else if (m->p.model == F2D_MODEL_RSW || projected(m->p.model)) {
         // rsw; euler = the same momentum kernel without the mass equation,
@@ -463,11 +482,18 @@ static int launch_stage_kernel(f2d_model_s* m, int k, int par, cudaStream_t s)
         // LFRA: the filtered previous state alternates between the two
         // tendency buffers with the parity (in: 1 + par, out: 2 - par)
         const int kin = lf ? 1 + par : 1, kout = lf ? 2 - par : k;
-        if (kout < 3) {
+        if (tend) {
+            a.dux = rhs("u.x");
+            a.duy = rhs("u.y");
+            a.dh = eu ? nullptr : rhs(hn);
+        } else if (kout < 3) {
             a.dux = ds("u.x", kout);
             a.duy = ds("u.y", kout);
             a.dh = eu ? nullptr : ds(hn, kout);
         }
+        a.fx = frc(m, "u.x");
+        a.fy = frc(m, "u.y");
+        a.fh = eu ? nullptr : frc(m, hn);
         a.dux1 = ds("u.x", kin);
         a.duy1 = ds("u.y", kin);
         a.dh1 = eu ? nullptr : ds(hn, kin);
@@ -480,7 +506,7 @@ static int launch_stage_kernel(f2d_model_s* m, int k, int par, cudaStream_t s)
         CKI(make_tmap(m, hm));
         CKI(make_tmap(m, om));
         CKI(launch_rsw_stage(m->p.vortexforce, m->prec, tmap(m, hm), tmap(m, om), a,
-                             m->d_code, k | (m->p.integrator << 4), g, m->sc, s));
+                             m->d_code, sk, g, m->sc, s));
         m->rec_launches += 1;
     } else {
         const char* q = m->p.model == F2D_MODEL_EULERPSI ? "omega" : "pv";
@@ -488,9 +514,8 @@ static int launch_stage_kernel(f2d_model_s* m, int k, int par, cudaStream_t s)
         CKI(make_tmap(m, qin));
         CKI(launch_fluxform_stage(m->p.compflux, m->prec, tmap(m, qin), qin, fb(m, q, out),
                                   fb(m, "U.x"), fb(m, "U.y"), m->d_code,
-                                  lf ? ds(q, 2 - par) : k < 3 ? ds(q, k) : nullptr,
-                                  ds(q, lf ? 1 + par : 1), ds(q, 2),
-                                  k | (m->p.integrator << 4), g,
+                                  tend ? rhs(q) : lf ? ds(q, 2 - par) : k < 3 ? ds(q, k) : nullptr,
+                                  ds(q, lf ? 1 + par : 1), ds(q, 2), frc(m, q), sk, g,
                                   m->sc, s));
         m->rec_launches += 1;
     }
@@ -502,9 +527,11 @@ static int launch_stage_kernel(f2d_model_s* m, int k, int par, cudaStream_t s)
         CKI(make_tmap(m, qin, true));
         CKI(launch_fluxform_stage(m->p.compflux, m->prec, tmap(m, qin), qin,
                                   fb(m, "tracer", out), fb(m, "U.x"), fb(m, "U.y"), m->d_code,
-                                  lf ? ds("tracer", 2 - par) : k < 3 ? ds("tracer", k) : nullptr,
+                                  tend ? rhs("tracer")
+                                       : lf ? ds("tracer", 2 - par)
+                                            : k < 3 ? ds("tracer", k) : nullptr,
                                   ds("tracer", lf ? 1 + par : 1), ds("tracer", 2),
-                                  k | (m->p.integrator << 4), g, m->sc, s));
+                                  frc(m, "tracer"), sk, g, m->sc, s));
         m->rec_launches += 1;
     }
     return 0;
@@ -549,11 +576,11 @@ static int launch_qgrsw_tendency(f2d_model_s* m, int k, int par, cudaStream_t s)
     return 0;
 }
 
-static int rec_qgrsw_stage(f2d_model_s* m, int k, int par, cudaStream_t s)
+static int rec_qgrsw_stage(f2d_model_s* m, int k, int par, cudaStream_t s, bool tend)
 {
     const Geom& g = m->g;
     const int out = 1 - par;
-    const bool lf = m->p.integrator == F2D_INTEG_LFRA;
+    const bool lf = m->p.integrator == F2D_INTEG_LFRA && !tend;
     const int kt = 3;
     const int sk = k | (m->p.integrator << 4);
     auto ds = [&](const char* f, int kk) -> void* {
@@ -590,11 +617,18 @@ static int rec_qgrsw_stage(f2d_model_s* m, int k, int par, cudaStream_t s)
     q.cx = a.dux;
     q.cy = a.duy;
     q.ch = a.dh;
-    if (!lf && k < 3) {
+    if (tend) {
+        q.sx = fb(m, "rhs.u.x");
+        q.sy = fb(m, "rhs.u.y");
+        q.sh = fb(m, "rhs.h");
+    } else if (!lf && k < 3) {
         q.sx = ds("u.x", k);
         q.sy = ds("u.y", k);
         q.sh = ds("h", k);
     }
+    q.fx = frc(m, "u.x");
+    q.fy = frc(m, "u.y");
+    q.fh = frc(m, "h");
     const int k1 = lf ? 1 + par : 1;
     q.d1x = ds("u.x", k1);
     q.d1y = ds("u.y", k1);
@@ -609,8 +643,8 @@ static int rec_qgrsw_stage(f2d_model_s* m, int k, int par, cudaStream_t s)
     }
     // thickness_from_psi's f0 * area / g (operators.py:208)
     q.c2 = m->p.f0 * m->area / m->p.g;
-    q.mode = 0;
-    q.store = !lf && k < 3;
+    q.mode = tend ? 2 : 0;
+    q.store = !lf && k < 3 && !tend;
     CKI(launch_qgrsw_update(m->prec, q, (const double*)fb(m, "psi"), m->d_code, sk, g, m->sc,
                             s));
     m->rec_launches += 1;
@@ -654,6 +688,11 @@ static int rec_stage(f2d_model_s* m, int k, int par, cudaStream_t s)
     return rec_diag(m, 1 - par, s);
 }
 
+static int nstages(const f2d_model_s* m)
+{
+    return m->p.integrator == F2D_INTEG_EF || m->p.integrator == F2D_INTEG_LFRA ? 1 : 3;
+}
+
 static int rec_step(f2d_model_s* m, int par, bool with_dt, cudaStream_t s)
 {
     if (with_dt && m->cfl_dt) {
@@ -662,7 +701,7 @@ static int rec_step(f2d_model_s* m, int par, bool with_dt, cudaStream_t s)
     }
     // SSP-RK3 / enrk3: 3 stages, ef and LFRA: 1 (an odd count: a step flips
     // the parity)
-    const int nst = m->p.integrator == F2D_INTEG_EF || m->p.integrator == F2D_INTEG_LFRA ? 1 : 3;
+    const int nst = nstages(m);
     for (int k = 1; k <= nst; ++k) {
         int e = rec_stage(m, k, par, s);
         if (e) return e;
@@ -743,6 +782,19 @@ static bool eager_mode()
     return v == 1;
 }
 
+// integrator stage k alone (its right-hand side and update, then the
+// diagnostics); the last stage of the step also advances the time line
+static int rec_one_stage(f2d_model_s* m, int k, int par, cudaStream_t s)
+{
+    int e = rec_stage(m, k, par, s);
+    if (e) return e;
+    if (k == nstages(m)) {
+        CKI(launch_pushforward(m->sc, s));
+        m->rec_launches += 1;
+    }
+    return 0;
+}
+
 static int record_kind(f2d_model_s* m, int kind, int par, cudaStream_t s)
 {
     switch (kind) {
@@ -752,11 +804,18 @@ static int record_kind(f2d_model_s* m, int kind, int par, cudaStream_t s)
     case 3: return rec_qg_projection(m, par, s);
     case 5: return rec_step_snap(m, par, s);
     case 6: return rec_adj_step(m, s);
+    case 7: return launch_stage_kernel(m, 1, par, s, true);
+    case 8:
+    case 9:
+    case 10: return rec_one_stage(m, kind - 7, par, s);
     }
     return fail(1, "unknown graph kind");
 }
 
-static bool flips(int kind) { return kind == 1 || kind == 2 || kind == 5; }
+static bool flips(int kind)
+{
+    return kind == 1 || kind == 2 || kind == 5 || (kind >= 8 && kind <= 10);
+}
 
 // capture kind (0 diag, 1 step, 2 run, 3 qg projection of the state,
 // 5 snapshot step, 6 adjoint step) for
@@ -939,6 +998,12 @@ int f2d_model_create(const f2d_params* p, const int8_t* msk, f2d_model* out)
     if (p->integrator < F2D_INTEG_RK3 || p->integrator > F2D_INTEG_LFRA)
         return fail(1, "unknown integrator (rk3, ef, enrk3, LFRA)");
     if (p->xperiodic && p->nx < 6) return fail(1, "x-periodic needs nx >= 6");
+    if (p->compflux < F2D_METHOD_WENO || p->compflux > F2D_METHOD_CWENO ||
+        p->vortexforce < F2D_METHOD_WENO || p->vortexforce > F2D_METHOD_CWENO)
+        return fail(1, "unknown flux method (weno, upwind, centered, cweno)");
+    if (p->innerproduct < F2D_METHOD_WENO || p->innerproduct > F2D_METHOD_CLASSIC)
+        return fail(1, "unknown innerproduct method (weno, upwind, centered, cweno, "
+                       "classic)");
     if ((p->model == F2D_MODEL_RSW || p->model == F2D_MODEL_BOUSSINESQ ||
          p->model == F2D_MODEL_QGRSW) &&
         p->vortexforce != p->compflux)
@@ -1032,6 +1097,7 @@ int f2d_model_create(const f2d_params* p, const int8_t* msk, f2d_model* out)
             return bail(e);
     // qgrsw keeps the third stage's (or LFRA's) tendency too: it is
     // projected between the tendency kernel and the update
+    for (const char* f : prog) m->prog.push_back(f);
     const int nds = p->model == F2D_MODEL_QGRSW ? 3 : 2;
     for (int k = 1; k <= nds; ++k)
         for (const char* f : prog)
@@ -1288,6 +1354,60 @@ int f2d_step(f2d_model m, int n)
     return 0;
 }
 
+int f2d_rhs(f2d_model m)
+{
+    if (!m) return fail(1, "null model");
+    // the tendency fields exist before any capture (allocation)
+    for (const auto& f : m->prog) {
+        const std::string n = "rhs." + f;
+        if (!fb(m, n.c_str())) {
+            int e = add_field(m, n.c_str(), false, (int)m->es);
+            if (e) return e;
+        }
+    }
+    return run_graph(m, 7);
+}
+
+int f2d_stage(f2d_model m, int k)
+{
+    if (!m) return fail(1, "null model");
+    if (k < 1 || k > nstages(m))
+        return fail(1, "stage " + std::to_string(k) + " out of range: the integrator has " +
+                           std::to_string(nstages(m)) + " stage(s)");
+    return run_graph(m, 7 + k);
+}
+
+int f2d_forcing_set(f2d_model m, const char* name, const double* host)
+{
+    if (!m || !name || !host) return fail(1, "null argument");
+    bool known = false;
+    for (const auto& f : m->prog) known = known || f == name;
+    if (!known)
+        return fail(8, std::string("no prognostic variable named ") + name +
+                           " for a forcing term");
+    if (!m->has_frc) {
+        // all forcing fields at once (zero), then every recorded graph is
+        // dropped: the stage kernels are recorded with the forcing pointers
+        for (const auto& f : m->prog) {
+            int e = add_field(m, ("frc." + f).c_str(), false, (int)m->es);
+            if (e) return e;
+        }
+        m->has_frc = true;
+        drop_graphs(m);
+    }
+    return field_io(m, ("frc." + std::string(name)).c_str(), (double*)host, true, false);
+}
+
+int f2d_forcing_clear(f2d_model m)
+{
+    if (!m) return fail(1, "null model");
+    if (!m->has_frc) return 0;
+    for (const auto& f : m->prog)
+        CK(cudaMemsetAsync(fb(m, ("frc." + f).c_str()), 0, field_bytes(m, m->es), m->stream));
+    CK(cudaStreamSynchronize(m->stream));
+    return 0;
+}
+
 int f2d_set_dt(f2d_model m)
 {
     if (!m) return fail(1, "null model");
@@ -1362,7 +1482,13 @@ int f2d_poisson_solve(f2d_model m, int which, const double* b, double* x, int* i
     CK(cudaMemcpy2DAsync(m->sx, g.P * 8, x, g.NX * 8, g.NX * 8, g.NY, cudaMemcpyHostToDevice,
                          m->stream));
     const int kind = 3 + which;
-    if (!m->gx[kind][0]) {
+    if (eager_mode()) {
+        // the profiling mode: the solve's loops driven from the host
+        int e0 = ensure_mg(m, which);
+        if (e0) return e0;
+        int e = rec_solve(m, which, m->sb, m->sx, m->stream);
+        if (e) return e;
+    } else if (!m->gx[kind][0]) {
         int e0 = ensure_mg(m, which);
         if (e0) return e0;
         m->rec_launches = 0;
@@ -1379,7 +1505,7 @@ int f2d_poisson_solve(f2d_model m, int which, const double* b, double* x, int* i
         cudaGraphDestroy(graph);
         if (ce != cudaSuccess) return fail((int)ce, cudaGetErrorString(ce));
     }
-    CK(cudaGraphLaunch(m->gx[kind][0], m->stream));
+    if (!eager_mode()) CK(cudaGraphLaunch(m->gx[kind][0], m->stream));
     CK(cudaMemcpy2DAsync(x, g.NX * 8, m->sx, g.P * 8, g.NX * 8, g.NY, cudaMemcpyDeviceToHost,
                          m->stream));
     DevScalars h;

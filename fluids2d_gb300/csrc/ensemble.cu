@@ -92,7 +92,8 @@ k_ens_fluxform_stage(const int4* __restrict__ tiles, const Member* __restrict__ 
     fluxform_tile<T, M>(sm, &mb.tq[par], at<T>(a.q[par], o), at<T>(a.q[1 - par], o),
                         at<T>(a.Ux, o), at<T>(a.Uy, o), a.code + o,
                         pout ? at<T>(pout, o) : nullptr, at<T>(pin, o), at<T>(a.ds2, o),
-                        stage, mb.g, sc.dt, sc.ragamma, &eg->status, tl.y, tl.z);
+                        (const T*)nullptr, stage, mb.g, sc.dt, sc.ragamma, &eg->status,
+                        tl.y, tl.z);
 }
 
 // centerstovertices (+ beta-plane term) into the FP64 right-hand side

@@ -32,12 +32,14 @@ k_fluxform_stage(const __grid_constant__ CUtensorMap tq, const T* __restrict__ q
                  T* __restrict__ qout, const T* __restrict__ Ux,
                  const T* __restrict__ Uy, const uint32_t* __restrict__ code,
                  T* __restrict__ ds_out, const T* __restrict__ ds1,
-                 const T* __restrict__ ds2, int stage, Geom g, DevScalars* sc)
+                 const T* __restrict__ ds2, const T* __restrict__ frc, int stage, Geom g,
+                 DevScalars* sc)
 {
     __shared__ FluxformSmem<T, M> sm;
     if (((stage >> 4) & 15) == 3 && sc->ite == 0) stage |= 256;  // first LFRA step
-    fluxform_tile<T, M>(sm, &tq, qin, qout, Ux, Uy, code, ds_out, ds1, ds2, stage, g, sc->dt,
-                        sc->ragamma, &sc->status, blockIdx.x * TX, blockIdx.y * FTY);
+    fluxform_tile<T, M, true>(sm, &tq, qin, qout, Ux, Uy, code, ds_out, ds1, ds2, frc, stage,
+                              g, sc->dt, sc->ragamma, &sc->status, blockIdx.x * TX,
+                              blockIdx.y * FTY);
 }
 
 // ---------------------------------------------------------------------------
@@ -204,7 +206,21 @@ k_rsw_stage(const __grid_constant__ CUtensorMap th,
     }
     // mass: dh = -div(flux) * msk
     const T msk = (cd & B_MSK) ? T(1) : T(0);
-    const T dh = (-(sfx[ty][tx + 1] - sfx[ty][tx]) - (sfy[ty + 1][tx] - sfy[ty][tx])) * msk;
+    T dh = (-(sfx[ty][tx + 1] - sfx[ty][tx]) - (sfy[ty + 1][tx] - sfy[ty][tx])) * msk;
+    const bool hm = a.euler != 1;  // mass (rsw) or buoyancy (boussinesq) equation
+    if (a.fx && a.euler != 3) {
+        // the forcing term after the right-hand side (equations.py:229-238)
+        dux += ((const T*)a.fx)[o];
+        duy += ((const T*)a.fy)[o];
+        if (hm) dh += ((const T*)a.fh)[o];
+    }
+    if (((sk >> 4) & 15) == INTEG_TENDENCY && a.euler != 3) {
+        // the tendency alone, with the halo fill of the reference's rhs
+        store_filled((T*)a.dux, g, j, i, dux);
+        store_filled((T*)a.duy, g, j, i, duy);
+        if (hm) store_filled((T*)a.dh, g, j, i, dh);
+        return;
+    }
     if (a.euler == 3) {
         // qgrsw: the raw tendency, projected by the Helmholtz solve before
         // the integrator update
@@ -216,7 +232,6 @@ k_rsw_stage(const __grid_constant__ CUtensorMap th,
 
     const T* dt = srk;
     T ix, iy, ih = T(0);
-    const bool hm = a.euler != 1;  // mass (rsw) or buoyancy (boussinesq) equation
     if (lf) {
         // leap-frog + Robert-Asselin: dux1.. = filtered previous state in,
         // dux.. = out (buffers alternating with the parity)
@@ -297,26 +312,41 @@ k_rsw_diag(const __grid_constant__ CUtensorMap tux,
         store_filled((T*)a.omega, g, j, i, om);
         return;
     }
-    // kinetic energy: innerproduct x then y, times msk*0.5 (operators.py:94-96)
     T ke = T(0);
-    {
-        const int L = lev(cd, SH_OKX);
-        if (L) {
-            const T Um = T(0.5) * (ux * rdx2 + sx[r][c + 1] * rdx2);
-            const T* w = &sx[r][c - 2];
-            ke = face_value<M, T>(L, Um, w[0], w[1], w[2], w[3], w[4], w[5]) * Um;
+    if constexpr (M == METHOD_CLASSIC) {
+        // innerproduct="classic" (operators.py:86-90): u.x U.x at the cell's
+        // two x-faces (ke[:, :-1]), plus u.y U.y at its two y-faces
+        // (ke[:-1, :]), times msk*0.25; U is the sharp of u as stored above
+        if (i <= g.NX - 2) {
+            const T a = sx[r][c + 1];
+            ke = a * (a * rdx2) + ux * (ux * rdx2);
         }
-    }
-    {
-        const int L = lev(cd, SH_OKY);
-        if (L) {
-            const T Um = T(0.5) * (uy * rdy2 + sy[r + 1][c] * rdy2);
-            ke += face_value<M, T>(L, Um, sy[r - 2][c], sy[r - 1][c], sy[r][c],
-                                   sy[r + 1][c], sy[r + 2][c], sy[r + 3][c]) *
-                  Um;
+        if (j <= g.NY - 2) {
+            const T b = sy[r + 1][c];
+            ke += b * (b * rdy2) + uy * (uy * rdy2);
         }
+        ke *= (cd & B_MSK) ? T(0.25) : T(0);
+    } else {
+        // kinetic energy: innerproduct x then y, times msk*0.5 (operators.py:94-96)
+        {
+            const int L = lev(cd, SH_OKX);
+            if (L) {
+                const T Um = T(0.5) * (ux * rdx2 + sx[r][c + 1] * rdx2);
+                const T* w = &sx[r][c - 2];
+                ke = face_value<M, T>(L, Um, w[0], w[1], w[2], w[3], w[4], w[5]) * Um;
+            }
+        }
+        {
+            const int L = lev(cd, SH_OKY);
+            if (L) {
+                const T Um = T(0.5) * (uy * rdy2 + sy[r + 1][c] * rdy2);
+                ke += face_value<M, T>(L, Um, sy[r - 2][c], sy[r - 1][c], sy[r][c],
+                                       sy[r + 1][c], sy[r + 2][c], sy[r + 3][c]) *
+                      Um;
+            }
+        }
+        ke *= (cd & B_MSK) ? T(0.5) : T(0);
     }
-    ke *= (cd & B_MSK) ? T(0.5) : T(0);
     store_filled((T*)a.omega, g, j, i, om);
     store_filled((T*)a.ke, g, j, i, ke);
 }
@@ -469,14 +499,14 @@ static dim3 ftile_grid(const Geom& g)
 int launch_fluxform_stage(int method, int prec, const CUtensorMap* tq,
                           const void* qin, void* qout, const void* Ux,
                           const void* Uy, const uint32_t* code, void* ds_out,
-                          const void* ds1, const void* ds2, int stage,
+                          const void* ds1, const void* ds2, const void* frc, int stage,
                           const Geom& g, DevScalars* sc, cudaStream_t s)
 {
     dim3 grid = ftile_grid(g), block(TX, TY);
 #define F2D_FF(T, M)                                                              \
     k_fluxform_stage<T, M><<<grid, block, 0, s>>>(                                \
         *tq, (const T*)qin, (T*)qout, (const T*)Ux, (const T*)Uy, code, (T*)ds_out, \
-        (const T*)ds1, (const T*)ds2, stage, g, sc)
+        (const T*)ds1, (const T*)ds2, (const T*)frc, stage, g, sc)
 #define F2D_DISPATCH(T)                                                  \
     switch (method) {                                                    \
     case METHOD_WENO: F2D_FF(T, METHOD_WENO); break;                     \
@@ -520,6 +550,7 @@ int launch_rsw_diag(int method, int prec, const CUtensorMap* tux,
     case METHOD_WENO: F2D_RD(T, METHOD_WENO); break;         \
     case METHOD_UPWIND: F2D_RD(T, METHOD_UPWIND); break;     \
     case METHOD_CENTERED: F2D_RD(T, METHOD_CENTERED); break; \
+    case METHOD_CLASSIC: F2D_RD(T, METHOD_CLASSIC); break;   \
     default: F2D_RD(T, METHOD_CWENO); break;                 \
     }
     if (prec == 0) { F2D_DISPATCH(double) } else { F2D_DISPATCH(float) }
@@ -785,6 +816,20 @@ __global__ void k_qgrsw_update(QgProj a, const double* __restrict__ psi,
     // the filled tendency: a periodic halo column takes its interior copy's
     const int io = !g.xper ? i : i < 3 ? i + g.nx : i >= g.nx + 3 ? i - g.nx : i;
     qg_project_point<T>(a, psi, code, g, j, io, dux, duy, dh);
+    if (a.fx) {
+        // the forcing term after the projected right-hand side
+        // (equations.py:229-238), at every point as the reference adds it
+        dux += ((const T*)a.fx)[o];
+        duy += ((const T*)a.fy)[o];
+        dh += ((const T*)a.fh)[o];
+    }
+    if (a.mode == 2) {
+        // the projected tendency alone (the reference's qgrsw rhs)
+        ((T*)a.sx)[o] = dux;
+        ((T*)a.sy)[o] = duy;
+        ((T*)a.sh)[o] = dh;
+        return;
+    }
     const T ux = ((const T*)a.ux)[o], uy = ((const T*)a.uy)[o], h = ((const T*)a.h)[o];
     if (lf) {
         const bool first = sc->ite == 0;

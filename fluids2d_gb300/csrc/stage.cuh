@@ -12,6 +12,7 @@ struct RswIn {
     void *dux, *duy, *dh;           // this stage's tendencies (stored if != 0)
     const void *dux1, *duy1, *dh1;  // earlier tendencies
     const void *dux2, *duy2, *dh2;
+    const void *fx, *fy, *fh;       // forcing terms added to the tendencies (or null)
     double fc;                      // f0 * area * 0.25 (operators.py:33)
     double bdy;                     // 0.5 * dy (addbuoyancy, operators.py:152-153)
     // 0 rsw; 1 euler (vortex force + grad ke only); 2 boussinesq (euler +
@@ -33,7 +34,7 @@ struct RswDiag {
 int launch_fluxform_stage(int method, int prec, const CUtensorMap* tq,
                           const void* qin, void* qout, const void* Ux,
                           const void* Uy, const uint32_t* code, void* ds_out,
-                          const void* ds1, const void* ds2, int stage,
+                          const void* ds1, const void* ds2, const void* frc, int stage,
                           const Geom& g, DevScalars* sc, cudaStream_t s);
 int launch_rsw_stage(int method, int prec, const CUtensorMap* th,
                      const CUtensorMap* tw, const RswIn& a, const uint32_t* code,
@@ -72,10 +73,12 @@ struct QgProj {
     const void *d1x, *d1y, *d1h;    // earlier projected tendencies (RK) or the
     const void *d2x, *d2y, *d2h;    //   filtered previous state (LFRA, d1)
     void *px, *py, *ph;             // LFRA: filtered state out
+    const void *fx, *fy, *fh;       // forcing terms added to the projected tendency
     double c2;                      // f0 * area / g (thickness_from_psi)
     double h0;                      // state mode: H * area - hb, else 0
     int mode;                       // 0: tendency + integrator update;
-                                    // 1: project the state (cx.. in place)
+                                    // 1: project the state (cx.. in place);
+                                    // 2: the projected tendency into sx.. only
     int store;                      // keep the projected tendency in sx..
 };
 int launch_qgrsw_pv(int prec, const void* ux, const void* uy, const void* h, double* pv,

@@ -194,13 +194,22 @@ struct FluxformSmem {
     uint64_t bar;
 };
 
-template <typename T, int M>
+// Integrator code of the tendency-only mode of the stage kernels (the
+// reference's rhs(s, ds) alone, equations.py:73-136): the kernel writes the
+// tendency (with its halo fill and any forcing term) to the tendency output
+// and leaves the state alone.
+constexpr int INTEG_TENDENCY = 15;
+
+// FRC: the kernel takes a forcing field `frc` (may be null at run time),
+// added to the tendency after the right-hand side (addforcingterm,
+// equations.py:229-238).
+template <typename T, int M, bool FRC = false>
 __device__ __forceinline__ void fluxform_tile(
     FluxformSmem<T, M>& sm, const CUtensorMap* tq, const T* __restrict__ qin,
     T* __restrict__ qout, const T* __restrict__ Ux, const T* __restrict__ Uy,
     const uint32_t* __restrict__ code, T* __restrict__ ds_out, const T* __restrict__ ds1,
-    const T* __restrict__ ds2, int stage, const Geom& g, double dt, double gamma,
-    int* status, int i0, int j0)
+    const T* __restrict__ ds2, const T* __restrict__ frc, int stage, const Geom& g,
+    double dt, double gamma, int* status, int i0, int j0)
 {
     auto& sq = sm.sq;
     auto& sfx = sm.sfx;
@@ -208,6 +217,8 @@ __device__ __forceinline__ void fluxform_tile(
     const int tx = threadIdx.x, ty = threadIdx.y, t = ty * TX + tx;
     const int sk = stage;  // stage | integrator << 4 | first LFRA step << 8
     const bool lf = ((sk >> 4) & 15) == 3;
+    const bool tend = ((sk >> 4) & 15) == INTEG_TENDENCY;
+    const bool hasf = FRC && frc != nullptr;
     stage &= 15;
     (void)qin;
     // 1. the TMA load of the staged tile (q with its 3-cell halo) ...
@@ -224,7 +235,7 @@ __device__ __forceinline__ void fluxform_tile(
     // index, then masked), so they are in flight together.
     const int i = i0 + tx;
     uint32_t cd[FRT];
-    T ux[FRT], uy[FRT], d1[FRT], d2[FRT];
+    T ux[FRT], uy[FRT], d1[FRT], d2[FRT], fq[FRT];
 #pragma unroll
     for (int q = 0; q < FRT; ++q) {
         const int j = j0 + ty + 8 * q;
@@ -235,8 +246,9 @@ __device__ __forceinline__ void fluxform_tile(
         cd[q] = in ? c : 0u;
         ux[q] = u;
         uy[q] = v;
-        d1[q] = stage >= 2 || lf ? ds1[o] : T(0);
-        d2[q] = stage == 3 ? ds2[o] : T(0);
+        d1[q] = (stage >= 2 || lf) && !tend ? ds1[o] : T(0);
+        d2[q] = stage == 3 && !tend ? ds2[o] : T(0);
+        fq[q] = hasf ? frc[o] : T(0);
     }
     uint32_t ce = 0u;
     T ue = T(0);
@@ -300,7 +312,12 @@ __device__ __forceinline__ void fluxform_tile(
         const int r = ty + 8 * q, j = j0 + r;
         if (j >= g.NY) break;
         const T msk = (cd[q] & B_MSK) ? T(1) : T(0);
-        const T ds = (-(sfx[r][tx + 1] - sfx[r][tx]) - (sfy[r + 1][tx] - sfy[r][tx])) * msk;
+        T ds = (-(sfx[r][tx + 1] - sfx[r][tx]) - (sfy[r + 1][tx] - sfy[r][tx])) * msk;
+        if (hasf) ds += fq[q];
+        if (tend) {
+            store_filled(ds_out, g, j, i, ds);
+            continue;
+        }
         if (lf) {
             // LFRA: ds1 = the filtered previous state in, ds_out = out
             T qn, pn;

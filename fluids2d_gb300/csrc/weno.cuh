@@ -239,7 +239,8 @@ __device__ __forceinline__ T cweno5z(T qmmm, T qmm, T qm, T qp, T qpp, T qppp)
 }
 
 enum { METHOD_WENO = 0, METHOD_UPWIND = 1, METHOD_CENTERED = 2,
-       METHOD_CWENO = 3 };
+       METHOD_CWENO = 3,
+       METHOD_CLASSIC = 4 /* innerproduct only: the 4-point kinetic energy */ };
 
 // The reference's (f1, f3, f5) triple of each method (weno.py:303-343).
 // Stencil values are q[-3..+2] around the face for the 6-point formula

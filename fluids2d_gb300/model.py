@@ -238,10 +238,15 @@ class Mesh:
 class Integrator:
     """The integrator facade (integrators.py:9-79): RKIntegrator for rk3, ef
     and enrk3, LFRAintegrator for LFRA; the scratch states live on the
-    device."""
+    device. ``rhs`` and ``diag`` are the pair of the reference's
+    get_rhs_and_diag registry (equations.py:190-210) on the GPU."""
 
     def __init__(self, model):
         self._m = model
+
+    @property
+    def nstages(self):
+        return 1 if self._m.param.integrator in ("ef", "LFRA") else 3
 
     def diag(self, state=None):
         m = self._m
@@ -250,6 +255,36 @@ class Integrator:
         m._push()
         check(lib().f2d_diag(m._h))
         m._device_newer = True
+
+    def rhs(self, state, ds):
+        """rhs(s, ds) of equations.py:73-157 (with the tracer equation and
+        the forcing terms): the tendency of the model's state (its
+        diagnostics current, as after diag) computed on the GPU and written
+        into the host arrays of ``ds``, a prognostic namedtuple (or any
+        object with the prognostic variables as attributes, vectors with
+        .x/.y) such as ``model.new_prognostic()`` returns."""
+        m = self._m
+        if state is not m._state:
+            raise ValueError("rhs() acts on the model's own state")
+        if m._forcings:
+            # forcing functions of this state (and time) first
+            f = m._static_term()
+            for fn in m._forcings:
+                fn(m.param, m.mesh, m.state, f)
+            m._upload_forcing(f)
+        m._push()
+        check(lib().f2d_rhs(m._h))
+        _, prog = _specs(m.param)
+        for name in prog:
+            v = getattr(ds, name)
+            if isinstance(v, tuple) and hasattr(v, "x"):
+                targets = ((name + ".x", v.x), (name + ".y", v.y))
+            else:
+                targets = (("tracer" if name == m._tracer else name, v),)
+            for dev, arr in targets:
+                out = np.empty(m.mesh.shape)
+                check(lib().f2d_field_get(m._h, ("rhs." + dev).encode(), ptr(out)))
+                arr[...] = out
 
     def step(self, state=None, time=None):
         self._m.step(1)
@@ -274,6 +309,8 @@ class Model:
         self.time = Time(self)
         self.callbacks = []
         self.diags = []
+        self._forcings = []
+        self._static_forcings = []
         self.stop = False
         self.io = _io.IO(param, self.mesh, None, self.time)
 
@@ -321,6 +358,9 @@ class Model:
     # -- time stepping ---------------------------------------------------
     def step(self, nsteps=1):
         """model.py:67-69 (time.dt is the current device dt)."""
+        if self._forcings:
+            self._stepped_with_forcing(nsteps, with_dt=False)
+            return
         self._push()
         check(lib().f2d_step(self._h, int(nsteps)))
         self._device_newer = True
@@ -354,6 +394,9 @@ class Model:
 
     def advance(self, nsteps):
         """nsteps iterations of the run-loop body: set_dt then step(1)."""
+        if self._forcings:
+            self._stepped_with_forcing(nsteps, with_dt=True)
+            return
         self._push()
         check(lib().f2d_run(self._h, int(nsteps)))
         self._device_newer = True
@@ -431,8 +474,68 @@ class Model:
         for d in self.diags:
             d()
 
-    def add_forcing(self, forcing):
-        raise NotImplementedError("host forcing terms are not part of the GPU path")
+    def new_prognostic(self):
+        """A zero prognostic namedtuple (states.py Prognostic): the shape of
+        the integrator's scratch and of rhs()'s ds argument."""
+        _, prog = _specs(self.param)
+        Prog = namedtuple("prognostic", prog)
+        shape = self.mesh.shape
+        return Prog(**{n: Vector(np.zeros(shape), np.zeros(shape)) if n in VECTORS
+                       else np.zeros(shape) for n in prog})
+
+    def add_forcing(self, forcing, static=False):
+        """Model.add_forcing (model.py:121-123): forcing(param, mesh, s, ds)
+        adds its term to the tendency ds after the right-hand side in every
+        stage (addforcingterm, equations.py:229-238); several forcings apply
+        in the order they were added.
+
+        On the GPU the forcing term is a field per prognostic variable added
+        inside the stage kernels. The function is called with the current
+        state and a zero ``ds`` to form that field, so it must add to ds, as
+        the reference's forcing functions do.
+
+        static=True: the term does not change with time or state; the
+        function is called once here, and steps run at full speed (graphs).
+        static=False (the reference's semantics for any function): the
+        function is called before every stage with the stage's state (and
+        ``mesh.time`` if attached), the field is uploaded and the stage runs
+        alone (f2d_stage), which costs a host round trip per stage."""
+        if static:
+            self._static_forcings.append(forcing)
+            self._upload_forcing(self._static_term())
+        else:
+            self._forcings.append(forcing)
+
+    def _static_term(self):
+        ds = self.new_prognostic()
+        for f in self._static_forcings:
+            f(self.param, self.mesh, self.state, ds)
+        return ds
+
+    def _upload_forcing(self, ds):
+        for name, arr in _flat_fields(ds, self._tracer):
+            a = np.ascontiguousarray(arr, dtype=np.float64)
+            check(lib().f2d_forcing_set(self._h, name.encode(), ptr(a)))
+
+    def _stepped_with_forcing(self, nsteps, with_dt):
+        """Steps with time- or state-dependent forcing functions: each stage
+        alone, its forcing field formed on the host just before it."""
+        base = self._static_term() if self._static_forcings else None
+        for _ in range(int(nsteps)):
+            self._push()
+            if with_dt:
+                check(lib().f2d_set_dt(self._h))
+            for k in range(1, self.integrator.nstages + 1):
+                ds = self.new_prognostic() if base is None else \
+                    type(base)(*[Vector(v.x.copy(), v.y.copy()) if isinstance(v, Vector)
+                                 else v.copy() for v in base])
+                state = self.state
+                for f in self._forcings:
+                    f(self.param, self.mesh, state, ds)
+                self._push()
+                self._upload_forcing(ds)
+                check(lib().f2d_stage(self._h, k))
+                self._device_newer = True
 
     def poisson_iterations(self):
         return self.stats()[0]

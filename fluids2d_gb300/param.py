@@ -110,8 +110,6 @@ class Param:
             raise NotImplementedError("halowidth must be 3")
         if self.yperiodic:
             raise NotImplementedError("yperiodic is not supported")
-        if self.model in ("rsw", "euler", "boussinesq") and self.innerproduct == "classic":
-            raise NotImplementedError("innerproduct='classic' is not implemented")
         assert self.precision in ("fp64", "fp32")
 
 

@@ -25,9 +25,10 @@ extern "C" {
 /* models (param.py:1-2) the GPU path implements */
 enum { F2D_MODEL_EULERPSI = 0, F2D_MODEL_RSW = 1, F2D_MODEL_QG = 2,
        F2D_MODEL_EULER = 3, F2D_MODEL_BOUSSINESQ = 4, F2D_MODEL_QGRSW = 5 };
-/* flux methods (param.py:4, weno.py:338-343) */
+/* flux methods (param.py:4, weno.py:338-343); CLASSIC is accepted for the
+ * innerproduct only (param.py:5, the 4-point product of operators.py:86-90) */
 enum { F2D_METHOD_WENO = 0, F2D_METHOD_UPWIND = 1, F2D_METHOD_CENTERED = 2,
-       F2D_METHOD_CWENO = 3 };
+       F2D_METHOD_CWENO = 3, F2D_METHOD_CLASSIC = 4 };
 /* integrators (integrators.py:9-131): SSP-RK3, Euler forward,
  * energy-conserving RK3, leap-frog with Robert-Asselin filter */
 enum { F2D_INTEG_RK3 = 0, F2D_INTEG_EF = 1, F2D_INTEG_ENRK3 = 2,
@@ -153,6 +154,37 @@ int f2d_step(f2d_model m, int nsteps);
 /* n iterations of the Model.run loop body: set_dt then step(1)
  * (model.py:45-51); the CFL time step is computed on the device. */
 int f2d_run(f2d_model m, int nsteps);
+/* The right-hand side alone, rhs(s, ds) of equations.py:73-157 (the
+ * registry get_rhs_and_diag, equations.py:190-210, with the tracer equation
+ * 217-226 and any forcing term 229-238): the tendency of the current state
+ * (whose diagnostics must be current, as after f2d_diag) into the fields
+ * "rhs.<var>" of every prognostic variable ("rhs.omega", "rhs.u.x",
+ * "rhs.u.y", "rhs.h", "rhs.pv", "rhs.b", "rhs.tracer"), read with
+ * f2d_field_get; the state is not changed (qgrsw: like the reference, the
+ * projection leaves its pv and psi). The plug point that lets the
+ * reference's own integrators (integrators.py:92-155) drive the GPU. */
+int f2d_rhs(f2d_model m);
+/* Stage k (1-based) of the integrator's step (integrators.py:92-155: rk3 and
+ * enrk3 have 3 stages, ef and LFRA 1) with the current time step: the
+ * stage's right-hand side and update, then diag; the last stage also
+ * advances the time line (timeline.py:20-35). f2d_set_dt, then stages
+ * 1..n, is one Model.run iteration; between stages the host may change the
+ * forcing fields (f2d_forcing_set), which is how a forcing function that
+ * depends on time or state runs. */
+int f2d_stage(f2d_model m, int k);
+/* Model.add_forcing (model.py:121-123, addforcingterm equations.py:229-238)
+ * on the device: the forcing term of prognostic variable `name` ("omega",
+ * "u.x", "u.y", "h", "pv", "b", "tracer"; a (ny+6, nx+6) float64 host
+ * array), added to its tendency after the right-hand side in every stage of
+ * step, run, f2d_stage and f2d_rhs until changed or cleared. In an
+ * x-periodic domain the halo columns of the tendency of omega, pv, u, h, b
+ * and the tracer take the forced value of their interior copy (give the
+ * forcing periodic halo columns for the reference's result). The first call
+ * allocates the forcing fields of all variables (zero) and drops the
+ * recorded graphs. */
+int f2d_forcing_set(f2d_model m, const char *name, const double *host);
+/* All forcing terms back to zero (no reference counterpart). */
+int f2d_forcing_clear(f2d_model m);
 /* Model.set_dt (model.py:71-87) */
 int f2d_set_dt(f2d_model m);
 /* Time (timeline.py:4-35) */

@@ -244,6 +244,19 @@ class Mesh:
         self.mskv[1:, 1:] = (msk[:-1, 1:] * msk[:-1, :-1]
                              * msk[1:, 1:] * msk[1:, :-1])
 
+    def x(self, which="c"):
+        """meshes.py:57-62: coordinates of the array columns."""
+        idx = np.arange(self.nx + 2 * self.param.halowidth) - self.param.halowidth
+        return (idx + (0.5 if which in ("c", "y") else 0.0)) * self.dx
+
+    def y(self, which="c"):
+        """meshes.py:63-68: coordinates of the array rows."""
+        idx = np.arange(self.ny + 2 * self.param.halowidth) - self.param.halowidth
+        return (idx + (0.5 if which in ("c", "x") else 0.0)) * self.dy
+
+    def xy(self, which="c"):
+        return np.meshgrid(self.x(which), self.y(which))
+
     def fill(self, a):
         """fill_halo_array, meshes.py:135-143."""
         if self.param.xperiodic:
@@ -384,8 +397,14 @@ def compute_vorticity(mesh, ux, uy, omega):
 
 
 def compute_kinetic_energy(p, mesh, ux, uy, Ux, Uy, ke, pysq):
-    """operators.py:80-96 (the WENO inner-product branch)."""
+    """operators.py:80-96: the 4-point product of innerproduct="classic"
+    (86-90) or the WENO inner product of the other methods (92-96)."""
     ke[:] = 0.
+    if p.innerproduct == "classic":
+        ke[:, :-1] = +ux[:, 1:] * Ux[:, 1:] + ux[:, :-1] * Ux[:, :-1]
+        ke[:-1, :] += uy[1:, :] * Uy[1:, :] + uy[:-1, :] * Uy[:-1, :]
+        ke *= mesh.msk * 0.25
+        return
     innerproduct(ke, Ux, ux, mesh.okx, mesh.xshift, p.innerproduct, pysq)
     innerproduct(ke, Uy, uy, mesh.oky, mesh.yshift, p.innerproduct, pysq)
     ke *= mesh.msk * 0.5
@@ -483,6 +502,28 @@ PROGNOSTIC = {"eulerpsi": ("omega",), "rsw": ("u", "h"), "qg": ("pv",),
 VECTORS = ("u", "U", "flx")
 
 
+class _View:
+    """Attribute access to a state dict the way the reference's namedtuples
+    give it (s.b, ds.u.y, ...), for forcing functions; arrays are the dict's
+    own, so in-place updates reach it."""
+
+    def __init__(self, d):
+        self._d = d
+
+    def __getattr__(self, name):
+        d = self.__dict__["_d"]
+        if name in d:
+            return d[name]
+        if name + ".x" in d:
+            return _Vec(d[name + ".x"], d[name + ".y"])
+        raise AttributeError(name)
+
+
+class _Vec:
+    def __init__(self, x, y):
+        self.x, self.y = x, y
+
+
 def _alloc(names, shape):
     out = {}
     for n in names:
@@ -521,6 +562,17 @@ class Model:
         self.ite = 0
         self._c = 0.0
         self.dt = param.dt if param.dt > 0 else 0.01
+        self.forcings = []
+
+    @property
+    def param(self):
+        return self.p
+
+    def add_forcing(self, forcing):
+        """Model.add_forcing (model.py:121-123): forcing(param, mesh, s, ds)
+        runs after the right-hand side (addforcingterm, equations.py:229-238);
+        several are applied in the order they were added."""
+        self.forcings.append(forcing)
 
     # -- equations ------------------------------------------------------
     def rhs(self, s, ds):
@@ -577,6 +629,8 @@ class Model:
             # addtracerequation (equations.py:217-226): no halo fill
             divflux(p, m, s["flx.x"], s["flx.y"], s[self.tracer], s["U.x"],
                     s["U.y"], ds[self.tracer], sq)
+        for f in self.forcings:
+            f(p, m, _View(s), _View(ds))
 
     def diag(self, s=None):
         s = self.s if s is None else s

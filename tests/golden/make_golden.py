@@ -30,6 +30,7 @@ sys.path.insert(0, HERE)
 sys.path.insert(0, os.path.dirname(os.path.dirname(HERE)))
 
 from refstubs import load_reference  # noqa: E402
+from forcings import BUILDERS as FORCINGS  # noqa: E402
 from fluids2d_gb300 import workloads as wl  # noqa: E402
 
 fd = load_reference()
@@ -181,7 +182,7 @@ def poisson_cases():
 
 
 # -------------------------------------------------------------- models ----
-def run_model(case, nsteps, fname, cfl=None, extra=None, setup=None):
+def run_model(case, nsteps, fname, cfl=None, extra=None, setup=None, forcing=None):
     kw = dict(xperiodic=case.get("xperiodic", False), Lx=case["Lx"],
               Ly=case["Ly"], tend=1e9, maxite=10 ** 9)
     for k in ("f0", "g", "H", "beta"):
@@ -202,6 +203,12 @@ def run_model(case, nsteps, fname, cfl=None, extra=None, setup=None):
             getattr(getattr(m.state, k.split(".")[0]), k.split(".")[1])[:] = v
         else:
             getattr(m.state, k)[:] = v
+    if forcing is not None:
+        # Model.add_forcing (model.py:121-123) with a forcing function of
+        # tests/golden/forcings.py; the time line is attached to the mesh the
+        # way the reference's experiment scripts do it
+        m.mesh.time = m.time
+        m.add_forcing(FORCINGS[forcing](m))
     pre = {}
     if setup is not None:
         # an initial-state operator of the reference (e.g. qg_projection);
@@ -233,6 +240,10 @@ def run_model(case, nsteps, fname, cfl=None, extra=None, setup=None):
         out["RAgamma"] = np.array(float(extra["RAgamma"]))
     if extra and "tracer" in extra:
         out["tracer"] = np.array(extra["tracer"])
+    if extra and "innerproduct" in extra:
+        out["innerproduct"] = np.array(extra["innerproduct"])
+    if forcing is not None:
+        out["forcing"] = np.array(forcing)
     for k, v in case["fields"].items():
         out["ic/" + k] = v.copy()
     for k, v in pre.items():
@@ -438,11 +449,44 @@ def lfra_cases():
               extra={"integrator": "LFRA"})
 
 
+def forcing_cases():
+    """Model.add_forcing (model.py:121-123, equations.py:229-238) with the
+    forcing functions of tests/golden/forcings.py."""
+    c = wl.boussinesq_case(n=40, ny=32, seed=16, nislands=1)
+    run_model(c, 4, "model_boussinesq_forced.npz", cfl=0.5, forcing="buoyancy_rows")
+    c = wl.qg_case(n=40, ny=32, seed=17, nislands=2, kmin=2, kmax=8)
+    run_model(c, 4, "model_qg_forced.npz", forcing="wind_curl")
+    c = wl.euler_case(n=40, ny=32, seed=18, nislands=1)
+    run_model(c, 4, "model_euler_forced_time.npz", cfl=0.5, forcing="wave_maker")
+    c = wl.rsw_case(n=40, ny=32, seed=19, nislands=2)
+    run_model(c, 4, "model_rsw_forced_periodic.npz", forcing="periodic_mass_source")
+    c = wl.euler_case(n=40, ny=32, seed=20, nislands=1)
+    run_model(c, 5, "model_euler_forced_lfra.npz", cfl=0.4, forcing="wave_maker",
+              extra={"integrator": "LFRA"})
+
+
+def classic_cases():
+    """innerproduct="classic" (operators.py:86-98): the 4-point kinetic
+    energy of rsw, euler and boussinesq."""
+    c = wl.rsw_case(n=40, ny=32, seed=13, nislands=2)
+    run_model(c, 4, "model_rsw_classic.npz", extra={"innerproduct": "classic"})
+    c = wl.euler_case(n=40, ny=32, seed=14, nislands=2, xperiodic=True)
+    run_model(c, 4, "model_euler_classic_periodic.npz", cfl=0.5,
+              extra={"innerproduct": "classic"})
+    c = wl.boussinesq_case(n=40, ny=32, seed=15, nislands=1)
+    run_model(c, 4, "model_boussinesq_classic.npz", cfl=0.5,
+              extra={"innerproduct": "classic"})
+
+
 if __name__ == "__main__":
     which = sys.argv[1:] or ["mesh", "sweeps", "poisson", "models", "integrators",
                              "euler", "boussinesq", "tracer", "qgrsw", "bulk"]
     if "lfra" in which:
         lfra_cases()
+    if "classic" in which:
+        classic_cases()
+    if "forcing" in which:
+        forcing_cases()
     if "boussinesq" in which:
         boussinesq_cases()
     if "tracer" in which:

@@ -134,7 +134,8 @@ MODEL_FILES = ["model_eulerpsi.npz", "model_eulerpsi_islands.npz",
                "model_eulerpsi_tracer.npz", "model_qg_tracer_lfra.npz",
                "model_rsw_tracer.npz", "model_boussinesq_tracer.npz",
                "model_qgrsw.npz", "model_qgrsw_periodic.npz", "model_qgrsw_lfra.npz",
-               "model_qgrsw_tracer.npz"]
+               "model_qgrsw_tracer.npz", "model_rsw_classic.npz",
+               "model_euler_classic_periodic.npz", "model_boussinesq_classic.npz"]
 
 
 def model_from_golden(g):
@@ -148,9 +149,10 @@ def model_from_golden(g):
     integ = str(g["integrator"]) if "integrator" in g.files else "rk3"
     gam = float(g["RAgamma"]) if "RAgamma" in g.files else 0.1
     tracer = str(g["tracer"]) if "tracer" in g.files else None
+    ip = str(g["innerproduct"]) if "innerproduct" in g.files else "weno"
     m = _model(kind, nx, ny, g["msk"], xperiodic=bool(xper), Lx=Lx, Ly=Ly, f0=f0,
                beta=beta, g=gg, H=H, cfl=cfl, tend=1e300, maxite=10 ** 9,
-               integrator=integ, RAgamma=gam, tracer=tracer)
+               integrator=integ, RAgamma=gam, tracer=tracer, innerproduct=ip)
     if "f" in g.files:
         m.mesh.f = g["f"]
     s = m.state

@@ -8,6 +8,7 @@ the same library on both sides, the tolerance only covers a different scipy
 build on another machine).
 """
 import os
+import sys
 
 import numpy as np
 import pytest
@@ -15,13 +16,25 @@ import pytest
 from conftest import GOLDEN
 from oracle import oracle as O
 
+if GOLDEN not in sys.path:
+    sys.path.insert(0, GOLDEN)
+from forcings import BUILDERS as FORCINGS  # noqa: E402
+
 
 def load(name):
     return np.load(os.path.join(GOLDEN, name), allow_pickle=False)
 
 
 def _noslip(s):
-    return eval(str(s))  # repr of None / True / list written by the generator
+    """param.noslip from the text the generator wrote: None, True, False or
+    a list of side names such as "['left', 'top']"."""
+    text = str(s)
+    fixed = {"None": None, "True": True, "False": False}
+    if text in fixed:
+        return fixed[text]
+    if text.startswith("[") and text.endswith("]"):
+        return [w.strip().strip("'\"") for w in text[1:-1].split(",") if w.strip()]
+    raise ValueError(f"unexpected noslip fixture value {text!r}")
 
 
 @pytest.mark.parametrize("case", list(load("mesh.npz")["names"]))
@@ -112,7 +125,11 @@ MODEL_FILES = ["model_eulerpsi.npz", "model_eulerpsi_islands.npz",
                "model_eulerpsi_tracer.npz", "model_qg_tracer_lfra.npz",
                "model_rsw_tracer.npz", "model_boussinesq_tracer.npz",
                "model_qgrsw.npz", "model_qgrsw_periodic.npz", "model_qgrsw_lfra.npz",
-               "model_qgrsw_tracer.npz"]
+               "model_qgrsw_tracer.npz", "model_rsw_classic.npz",
+               "model_euler_classic_periodic.npz", "model_boussinesq_classic.npz",
+               "model_boussinesq_forced.npz", "model_qg_forced.npz",
+               "model_euler_forced_time.npz", "model_rsw_forced_periodic.npz",
+               "model_euler_forced_lfra.npz"]
 
 
 def oracle_from_golden(g, pysq=True):
@@ -127,12 +144,17 @@ def oracle_from_golden(g, pysq=True):
     integ = str(g["integrator"]) if "integrator" in g.files else "rk3"
     gam = float(g["RAgamma"]) if "RAgamma" in g.files else 0.1
     tracer = str(g["tracer"]) if "tracer" in g.files else None
+    ip = str(g["innerproduct"]) if "innerproduct" in g.files else "weno"
     p = O.Param(model=kind, nx=nx, ny=ny, xperiodic=bool(xper), Lx=Lx, Ly=Ly,
                 f0=f0, beta=beta, g=gg, H=H, cfl=cfl, tend=1e9,
-                maxite=10 ** 9, integrator=integ, RAgamma=gam, tracer=tracer)
+                maxite=10 ** 9, integrator=integ, RAgamma=gam, tracer=tracer,
+                innerproduct=ip)
     m = O.Model(p, msk=g["msk"], pysq=pysq)
     if "f" in g.files:
         m.mesh.f = g["f"].copy()
+    if "forcing" in g.files:
+        m.mesh.time = m  # forcing functions read mesh.time.t
+        m.add_forcing(FORCINGS[str(g["forcing"])](m))
     for k in names:
         m.s[k][:] = g["ic/" + k]
     m.diag()
