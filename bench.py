@@ -361,63 +361,97 @@ def cpu_oracle_rate(model, case, budget_s, max_steps=None, warmup=1):
 
 
 def ensemble_cpu_rate(budget_s, steps=1, warmup=1):
-    """Oracle port on a sample of the ensemble workload: the members in
-    order, as many as one step of all of them takes budget_s/steps seconds
-    (chosen during the first warm-up step, which also builds the models and
-    factorises their Poisson matrices); then `steps` timed steps, each one
-    model step of every sampled member. Returns (rate, members, seconds,
-    threads, per-step seconds)."""
+    """Oracle port on a stratified sample of the ensemble workload: members
+    taken in turn from each grid size (64 .. 512), in draw order, until one
+    model step of the sample takes budget_s/steps seconds (measured during
+    the first warm-up step, which also builds the models and factorises their
+    Poisson matrices), at least one member of every size. Then `steps` timed
+    steps, each one model step of every sampled member, timed per member. The
+    step time of the whole ensemble is estimated as the sum over sizes of
+    (members of that size) x (mean sampled member step time of that size).
+    Returns (rate over all members' cells, sample description dict, seconds
+    timed, threads, per-step estimated whole-ensemble seconds)."""
     from fluids2d_gb300 import workloads as wl
     from oracle import oracle as O
     members = wl.ensemble_case()
+    sizes = sorted({c["nx"] for c in members})
+    queues = {n: [c for c in members if c["nx"] == n] for n in sizes}
+    count = {n: len(queues[n]) for n in sizes}
     per_step = budget_s / max(1, steps)
-    models, cells, el = [], 0, 0.0
-    for c in members:
-        p = O.Param(model="eulerpsi", nx=c["nx"], ny=c["ny"], cfl=0.8, tend=1e300,
-                    maxite=10 ** 12)
-        om = O.Model(p, msk=c["msk"], pysq=False)
-        om.s["omega"][:] = c["fields"]["omega"]
-        om.diag()
-        t0 = time.perf_counter()
-        om.run_steps(1)
-        el += time.perf_counter() - t0
-        models.append(om)
-        cells += c["nx"] * c["ny"]
+    models, el = [], 0.0
+    taken = {n: 0 for n in sizes}
+    while any(taken[n] < count[n] for n in sizes):
+        for n in sizes:
+            if taken[n] >= count[n]:
+                continue
+            c = queues[n][taken[n]]
+            taken[n] += 1
+            p = O.Param(model="eulerpsi", nx=c["nx"], ny=c["ny"], cfl=0.8, tend=1e300,
+                        maxite=10 ** 12)
+            om = O.Model(p, msk=c["msk"], pysq=False)
+            om.s["omega"][:] = c["fields"]["omega"]
+            om.diag()
+            t0 = time.perf_counter()
+            om.run_steps(1)
+            el += time.perf_counter() - t0
+            models.append((n, om))
         if el >= per_step:
             break
     for _ in range(max(0, warmup - 1)):
-        for om in models:
+        for _, om in models:
             om.run_steps(1)
-    times = []
+    per_member = {n: [] for n in sizes}
+    timed = 0.0
+    est_steps = []
     for _ in range(max(1, steps)):
-        t0 = time.perf_counter()
-        for om in models:
+        step_t = {n: [] for n in sizes}
+        for n, om in models:
+            t0 = time.perf_counter()
             om.run_steps(1)
-        times.append(time.perf_counter() - t0)
-    tot = sum(times)
-    return cells * len(times) / tot, len(models), tot, O.num_threads(), times
+            dt = time.perf_counter() - t0
+            step_t[n].append(dt)
+            timed += dt
+        est_steps.append(sum(count[n] * (sum(step_t[n]) / len(step_t[n])) for n in sizes))
+        for n in sizes:
+            per_member[n].extend(step_t[n])
+    cells_all = sum(c["nx"] * c["ny"] for c in members)
+    est = sum(est_steps) / len(est_steps)
+    sample = {"members_sampled": {str(n): taken[n] for n in sizes},
+              "members_per_size": {str(n): count[n] for n in sizes},
+              "ms_per_member_step": {str(n): 1e3 * sum(per_member[n]) / len(per_member[n])
+                                     for n in sizes}}
+    return cells_all / est, sample, timed, O.num_threads(), est_steps
 
 
 def run_reference(args, rank, world):
     """--impl reference: the CPU implementation of the path on host cores."""
     if is_ensemble(args.workload):
+        from fluids2d_gb300 import workloads as wl
         budget = float(os.environ.get("F2D_REF_BUDGET_S", "60"))
-        rate, n, el, cores, times = ensemble_cpu_rate(budget, args.steps, args.warmup)
+        rate, smp, el, cores, est = ensemble_cpu_rate(budget, args.steps, args.warmup)
+        members = wl.ensemble_case()
+        cells = sum(c["nx"] * c["ny"] for c in members)
+        nsamp = sum(smp["members_sampled"].values())
         line = {
             "metric": "cell-updates/s", "value": rate, "unit": "cell-updates/s",
-            "impl": "reference", "n_gpus": args.gpus, "steps": len(times),
-            "warmup": args.warmup, "ms_per_step": 1e3 * el / len(times),
+            "impl": "reference", "n_gpus": args.gpus, "steps": len(est),
+            "warmup": args.warmup, "ms_per_step": 1e3 * sum(est) / len(est),
             "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f64",
             "data": "synthetic",
-            "config": {"workload": args.workload, "desc": ENSEMBLE_DESC},
+            "config": {"workload": args.workload, "desc": ENSEMBLE_DESC,
+                       "members": len(members), "cells": cells},
             "cpu_baseline": {
                 "value": rate, "unit": "cell-updates/s", "cores": cores,
                 "kind": "port",
-                "sample": f"each step: one model step of each of the first {n} "
-                          f"members (of 256) of {args.workload}; {len(times)} timed "
-                          f"steps, {el:.1f} s on {cores} host threads (set-up and "
-                          f"SuperLU factorisation in the warm-up, untimed)"},
+                "sample": f"stratified: {nsamp} of the {len(members)} members "
+                          f"({smp['members_sampled']} by grid size), one model step of "
+                          f"each per timed step, {len(est)} timed steps, {el:.1f} s on "
+                          f"{cores} host threads (set-up and SuperLU factorisation in "
+                          f"the warm-up, untimed); ms_per_step is the whole-ensemble "
+                          f"step time estimated as the sum over sizes of members x "
+                          f"mean member step time",
+                "per_size": smp},
             "e2e": {"value": rate, "unit": "cell-updates/s",
                     "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
         }
@@ -631,17 +665,27 @@ def run_gpu_ensemble(args, rank, world):
                         + st["launches_per_iter"] * loops,
         "poisson_iters_sum_over_members": pcg_iters,
         "cg_loop_iters": loops,
+        "solver_per_solve": {
+            # 3 solves per member and step (one per RK3 stage diagnostic)
+            "pcg_iters_per_member": pcg_iters / (3 * args.steps * len(members)),
+            "refine_rounds_per_member": (st["refine_rounds"] - st0["refine_rounds"])
+                                        / (3 * args.steps * len(members)),
+            "loop_iters": loops / (3 * args.steps)},
         "clocks": clocks,
     }
     if fp64_form:
         line["fp64_form"] = fp64_form
     if rank == 0 and not args.no_cpu_baseline:
         budget = float(os.environ.get("F2D_CPU_BUDGET_S", "15"))
-        rate, n, el, cores, _ = ensemble_cpu_rate(budget, 1, 1)
+        rate, smp, el, cores, _ = ensemble_cpu_rate(budget, 1, 1)
         line["cpu_baseline"] = {
             "value": rate, "unit": "cell-updates/s", "cores": cores, "kind": "port",
-            "sample": f"one model step of each of the first {n} members (after a "
-                      f"warm-up step), {el:.1f} s on {cores} host threads"}
+            "sample": f"stratified: {sum(smp['members_sampled'].values())} members "
+                      f"({smp['members_sampled']} by grid size), one model step of each "
+                      f"after a warm-up step, {el:.1f} s on {cores} host threads; the "
+                      f"whole-ensemble step time estimated as the sum over sizes of "
+                      f"members x mean member step time",
+            "per_size": smp}
     if rank == 0:
         print(json.dumps(line), flush=True)
 

@@ -128,6 +128,8 @@ _SIGS = {
                    ctypes.POINTER(c_i64)], c_int),
     "f2d_test_tma_wait": ([c_int, c_dbl], c_int),
     "f2d_rhs": ([c_void_p], c_int),
+    "f2d_refine_rounds": ([c_void_p, ctypes.POINTER(c_i64)], c_int),
+    "f2d_ensemble_refine_rounds": ([c_void_p, ctypes.POINTER(c_i64)], c_int),
     "f2d_stage": ([c_void_p, c_int], c_int),
     "f2d_forcing_set": ([c_void_p, ctypes.c_char_p, c_void_p], c_int),
     "f2d_forcing_clear": ([c_void_p], c_int),

@@ -1567,6 +1567,16 @@ int f2d_test_tma_wait(int enabled, double limit_ms)
     return 0;
 }
 
+int f2d_refine_rounds(f2d_model m, int64_t* rounds)
+{
+    if (!m || !rounds) return fail(1, "null argument");
+    DevScalars h;
+    CK(cudaMemcpyAsync(&h, m->sc, sizeof(h), cudaMemcpyDeviceToHost, m->stream));
+    CK(cudaStreamSynchronize(m->stream));
+    *rounds = h.total_outer;
+    return 0;
+}
+
 int f2d_stats(f2d_model m, int64_t* poisson_iters, int64_t* launches_per_step,
               int64_t* launches_per_iter)
 {

@@ -846,6 +846,19 @@ int f2d_ensemble_stats(f2d_ensemble e, int64_t* cells, int64_t* poisson_iters_su
     return 0;
 }
 
+int f2d_ensemble_refine_rounds(f2d_ensemble e, int64_t* rounds)
+{
+    if (!e || !rounds) return f2d_internal_fail(1, "null argument");
+    std::vector<DevScalars> h(e->n);
+    ECK(cudaMemcpyAsync(h.data(), e->scs, sizeof(DevScalars) * e->n, cudaMemcpyDeviceToHost,
+                        e->stream));
+    ECK(cudaStreamSynchronize(e->stream));
+    int64_t r = 0;
+    for (int b = 0; b < e->n; ++b) r += h[b].total_outer;
+    *rounds = r;
+    return 0;
+}
+
 int f2d_ensemble_time_solver(f2d_ensemble e, int reps, int flush_l2, double* avg_ms,
                              int64_t* nodes, int* elem_bytes)
 {

@@ -139,5 +139,8 @@ class Ensemble:
         check(lib().f2d_ensemble_stats(self._h, ctypes.byref(c), ctypes.byref(it),
                                        ctypes.byref(lp), ctypes.byref(ls),
                                        ctypes.byref(li)))
+        r = ctypes.c_int64()
+        check(lib().f2d_ensemble_refine_rounds(self._h, ctypes.byref(r)))
         return dict(cells=c.value, poisson_iters=it.value, loop_iters=lp.value,
-                    launches_per_step=ls.value, launches_per_iter=li.value)
+                    launches_per_step=ls.value, launches_per_iter=li.value,
+                    refine_rounds=r.value)

@@ -232,6 +232,9 @@ int f2d_time_solver(f2d_model m, int reps, int flush_l2, double *avg_ms,
  * enabled == 0 restores normal operation. Applies to every model and
  * ensemble of the process; synchronises the device. For tests only. */
 int f2d_test_tma_wait(int enabled, double limit_ms);
+/* Refinement rounds of the FP32 form's solves summed since creation (see
+ * f2d_ensemble_refine_rounds). Instrumentation. */
+int f2d_refine_rounds(f2d_model m, int64_t *rounds);
 /* Counters: Poisson iterations summed over all solves since creation; the
  * kernels one time step launches outside the Poisson loops; the kernels one
  * Poisson iteration launches. No reference counterpart (instrumentation). */
@@ -291,6 +294,11 @@ int f2d_ensemble_sync(f2d_ensemble e);
 int f2d_ensemble_stats(f2d_ensemble e, int64_t *cells, int64_t *poisson_iters,
                        int64_t *loop_iters, int64_t *launches_per_step,
                        int64_t *launches_per_iter);
+/* Refinement rounds of the FP32 form's Poisson solves (each an inner FP32
+ * CG solve followed by an FP64 residual), summed over all solves and members
+ * since creation; 0 in the FP64 form. Instrumentation, no reference
+ * counterpart. */
+int f2d_ensemble_refine_rounds(f2d_ensemble e, int64_t *rounds);
 /* f2d_time_stage for the batched stage kernel of all members (measurement
  * hook of the benchmark; no reference counterpart). */
 int f2d_ensemble_time_stage(f2d_ensemble e, int stage, int reps, int flush_l2,
