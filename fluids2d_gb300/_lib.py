@@ -128,6 +128,8 @@ _SIGS = {
                    ctypes.POINTER(c_i64)], c_int),
     "f2d_test_tma_wait": ([c_int, c_dbl], c_int),
     "f2d_rhs": ([c_void_p], c_int),
+    "f2d_set_schedule": ([c_void_p, c_int, c_int, c_dbl], c_int),
+    "f2d_ensemble_set_schedule": ([c_void_p, c_int, c_int, c_dbl], c_int),
     "f2d_refine_rounds": ([c_void_p, ctypes.POINTER(c_i64)], c_int),
     "f2d_ensemble_refine_rounds": ([c_void_p, ctypes.POINTER(c_i64)], c_int),
     "f2d_stage": ([c_void_p, c_int], c_int),

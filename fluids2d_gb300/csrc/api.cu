@@ -1482,6 +1482,8 @@ int f2d_poisson_solve(f2d_model m, int which, const double* b, double* x, int* i
     CK(cudaMemcpy2DAsync(m->sx, g.P * 8, x, g.NX * 8, g.NX * 8, g.NY, cudaMemcpyHostToDevice,
                          m->stream));
     const int kind = 3 + which;
+    DevScalars h0;
+    CK(cudaMemcpyAsync(&h0, m->sc, sizeof(h0), cudaMemcpyDeviceToHost, m->stream));
     if (eager_mode()) {
         // the profiling mode: the solve's loops driven from the host
         int e0 = ensure_mg(m, which);
@@ -1511,7 +1513,9 @@ int f2d_poisson_solve(f2d_model m, int which, const double* b, double* x, int* i
     DevScalars h;
     CK(cudaMemcpyAsync(&h, m->sc, sizeof(h), cudaMemcpyDeviceToHost, m->stream));
     CK(cudaStreamSynchronize(m->stream));
-    if (iters) *iters = h.iter;
+    // CG iterations of this solve (the FP32 form: inner iterations summed
+    // over its refinement rounds)
+    if (iters) *iters = (int)(h.total_iters - h0.total_iters);
     if (relres) *relres = h.bb > 0 ? sqrt(h.rr / h.bb) : 0.0;
     return 0;
 }
@@ -1666,6 +1670,23 @@ int f2d_autotune(f2d_model m, int reps, int* th, int* nu, double* tol_in, double
     if (nu) *nu = t.nu;
     if (tol_in) *tol_in = t.tol_in;
     if (ms) *ms = t.ms;
+    return 0;
+}
+
+int f2d_set_schedule(f2d_model m, int tile_rows, int sweeps, double tol_in)
+{
+    if (!m) return fail(1, "null model");
+    if (m->p.model == F2D_MODEL_RSW || projected(m->p.model))
+        return fail(1, "the schedule is that of the multigrid of eulerpsi, qg and qgrsw");
+    const int which = m->p.model == F2D_MODEL_EULERPSI ? 0 : 1;
+    int e = ensure_mg(m, which);
+    if (e) return e;
+    CK(cudaStreamSynchronize(m->stream));
+    e = bs_set_schedule(m->bs[which], tile_rows, sweeps, tol_in);
+    drop_graphs(m);
+    if (e == 1) return fail(1, "schedule: tile_rows 32 or 64, sweeps 1 or 2, 0 < tol_in < 1");
+    if (e) return fail(e, "multigrid rebuild failed");
+    m->body_launches = 0;
     return 0;
 }
 

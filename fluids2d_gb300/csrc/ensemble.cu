@@ -846,6 +846,24 @@ int f2d_ensemble_stats(f2d_ensemble e, int64_t* cells, int64_t* poisson_iters_su
     return 0;
 }
 
+int f2d_ensemble_set_schedule(f2d_ensemble e, int tile_rows, int sweeps, double tol_in)
+{
+    if (!e) return f2d_internal_fail(1, "null ensemble");
+    ECK(cudaStreamSynchronize(e->stream));
+    const int r = bs_set_schedule(e->bs, tile_rows, sweeps, tol_in);
+    // the step and diagnostic graphs captured the previous schedule
+    for (auto& k : e->gx)
+        for (auto& g : k)
+            if (g) {
+                cudaGraphExecDestroy(g);
+                g = nullptr;
+            }
+    if (r == 1)
+        return f2d_internal_fail(1, "schedule: tile_rows 32 or 64, sweeps 1 or 2, 0 < tol_in < 1");
+    if (r) return f2d_internal_fail(r, "ensemble multigrid rebuild failed");
+    return 0;
+}
+
 int f2d_ensemble_refine_rounds(f2d_ensemble e, int64_t* rounds)
 {
     if (!e || !rounds) return f2d_internal_fail(1, "null argument");

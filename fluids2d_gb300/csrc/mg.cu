@@ -98,7 +98,11 @@ int mg_build(MGHost& mg, int nyn0, int nxn0, long long pitch0, long long off0, i
         C.nyn = cyn;
         C.nxn = cxn;
         C.pitch = (cxn + 31) / 32 * 32;
-        C.off = 0;
+        // node (J, I) at element 1 + J*pitch + I: an odd offset, like level
+        // 0's (node (J, I) of the model's array at (3+J)*P + 3+I, P even), so
+        // that node pairs starting on odd columns are 8/16-byte aligned on
+        // every level (the paired loads of the level kernels)
+        C.off = 1;
         C.per = per;
         C.cx = cx;
         C.cy = cy;
@@ -110,7 +114,7 @@ int mg_build(MGHost& mg, int nyn0, int nxn0, long long pitch0, long long off0, i
         C.fidiag = (float)C.idiag;
         C.md = md;
         C.fmd = (float)md;
-        const size_t n = (size_t)C.pitch * cyn;
+        const size_t n = (size_t)C.pitch * cyn + 32;  // + the offset
         void *x, *xa, *b, *m;
         if (cudaMalloc(&x, n * es) != cudaSuccess) return 2;
         mg.owned.push_back(x);
@@ -125,7 +129,7 @@ int mg_build(MGHost& mg, int nyn0, int nxn0, long long pitch0, long long off0, i
         cudaMemset(b, 0, n * es);
         std::vector<uint8_t> hm(n, 0);
         for (int J = 0; J < cyn; ++J)
-            memcpy(&hm[(size_t)J * C.pitch], &cm[(size_t)J * cxn], cxn);
+            memcpy(&hm[C.off + (size_t)J * C.pitch], &cm[(size_t)J * cxn], cxn);
         if (cudaMemcpy(m, hm.data(), n, cudaMemcpyHostToDevice) != cudaSuccess) return 2;
         C.x = x;
         C.xa = xa;

@@ -98,6 +98,10 @@ struct BSTune {
 };
 int bs_autotune(BatchSolver& s, cudaStream_t st, cudaStream_t st2, void* x, const void* b,
                 size_t xbytes, int reps, BSTune* out);
+// Set the schedule directly (tile rows 32/64, sweeps per leg 1/2, inner
+// tolerance of the refinement form in (0, 1)); rebuilds the tile tables when
+// the tile rows change. The caller drops graphs that captured the solver.
+int bs_set_schedule(BatchSolver& s, int th, int nu, double tol_in);
 // measurement hook: mean ms of the level-0 down kernel over `reps` launches
 int bs_time_down(BatchSolver& s, cudaStream_t st, int reps, int flush_l2, double* avg_ms,
                  long long* nodes, int* es);

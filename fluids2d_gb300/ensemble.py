@@ -122,6 +122,12 @@ class Ensemble:
         return {"tile_rows": th.value, "sweeps": nu.value, "tol_in": tin.value,
                 "ms_per_solve": ms.value}
 
+    def set_schedule(self, tile_rows, sweeps, tol_in=1e-6):
+        """Set the batched solver's multigrid schedule directly
+        (f2d_ensemble_set_schedule)."""
+        check(lib().f2d_ensemble_set_schedule(self._h, int(tile_rows), int(sweeps),
+                                              float(tol_in)))
+
     def run(self, nsteps):
         check(lib().f2d_ensemble_run(self._h, int(nsteps)))
 

@@ -392,6 +392,13 @@ class Model:
         return {"tile_rows": th.value, "sweeps": nu.value, "tol_in": tin.value,
                 "ms_per_solve": ms.value}
 
+    def set_schedule(self, tile_rows, sweeps, tol_in=1e-6):
+        """Set the multigrid schedule directly (tile rows 32/64, sweeps per
+        leg 1/2, inner tolerance of the FP32 form), e.g. one an earlier
+        autotune() returned (f2d_set_schedule)."""
+        self._push()
+        check(lib().f2d_set_schedule(self._h, int(tile_rows), int(sweeps), float(tol_in)))
+
     def advance(self, nsteps):
         """nsteps iterations of the run-loop body: set_dt then step(1)."""
         if self._forcings:

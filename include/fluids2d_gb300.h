@@ -193,7 +193,9 @@ int f2d_time_set(f2d_model m, double t, double dt, int64_t ite);
 
 /* Poisson2D.solve(b, x) (elliptic.py:80-87) on the vertex operator
  * (which = 0) or the qg Helmholtz operator (which = 1, meshes.py:42-47):
- * only fluid points of x are written, then the halo fill. Host arrays. */
+ * only fluid points of x are written, then the halo fill. Host arrays.
+ * *iters = CG iterations of the solve (FP32 form: summed over its
+ * refinement rounds), *relres = final relative residual. */
 int f2d_poisson_solve(f2d_model m, int which, const double *b, double *x,
                       int *iters, double *relres);
 
@@ -216,6 +218,11 @@ int f2d_time_stage(f2d_model m, int stage, int reps, int flush_l2,
  * solve (eulerpsi, qg, qgrsw) and ensembles. */
 int f2d_autotune(f2d_model m, int reps, int *tile_rows, int *sweeps, double *tol_in,
                  double *ms_per_solve);
+/* Set the multigrid schedule directly (what f2d_autotune would pick):
+ * tile rows 32 or 64, red-black sweeps per leg 1 or 2, and the inner
+ * tolerance of the FP32 form's refinement rounds (0 < tol_in < 1; unused in
+ * the FP64 form). Recorded graphs are dropped. No reference counterpart. */
+int f2d_set_schedule(f2d_model m, int tile_rows, int sweeps, double tol_in);
 /* Time `reps` launches of the Poisson solver's level-0 down kernel
  * (pre-smoothing + residual + restriction of the V-cycle, the solver's largest
  * share) on the current right-hand side, L2 flushed between launches when
@@ -282,6 +289,8 @@ int f2d_ensemble_diag(f2d_ensemble e);
 /* The autotuner (see f2d_autotune) on the ensemble's batched solver. */
 int f2d_ensemble_autotune(f2d_ensemble e, int reps, int *tile_rows, int *sweeps,
                           double *tol_in, double *ms_per_solve);
+/* f2d_set_schedule for the ensemble's batched solver. */
+int f2d_ensemble_set_schedule(f2d_ensemble e, int tile_rows, int sweeps, double tol_in);
 /* n iterations of set_dt + step(1) for every member (model.py:45-51) */
 int f2d_ensemble_run(f2d_ensemble e, int nsteps);
 int f2d_ensemble_time_get(f2d_ensemble e, int member, double *t, double *dt,

@@ -121,8 +121,8 @@ def test_tma_wait_timeout_reports_then_recovers(kind, tma_wait_switch):
         m = _eulerpsi(case)
     else:
         case = wl.rsw_case(n=64, ny=48, seed=4, nislands=2)
-        m = _model("rsw", 64, 48, case["msk"], xperiodic=True, tend=1e300,
-                   maxite=10 ** 9)
+        m = _model("rsw", 64, 48, case["msk"], xperiodic=True, f0=case["f0"],
+                   g=case["g"], H=case["H"], tend=1e300, maxite=10 ** 9)
         m.state.h[:] = case["fields"]["h"]
     m.integrator.diag(m.state)
     m.sync()
