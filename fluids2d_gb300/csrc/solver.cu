@@ -723,7 +723,12 @@ k_bs_xr(const int4* __restrict__ tiles, const BSInfo* __restrict__ info,
             if (bad) atomicOr(&eg->status, ST_NONFINITE);
             if (ir) {
                 sc.iter_in += 1;
-                const int done = bad || w[0] <= sc.tol_in2 * sc.rr0 || sc.iter_in >= sc.maxit_in;
+                // a round stops at its relative tolerance, or as soon as its
+                // residual is a tenth of what the whole solve must reach
+                // (the last round of a solve needs only the digits missing,
+                // not tol_in more)
+                const double goal = fmax(sc.tol_in2 * sc.rr0, 0.01 * sc.tol2 * sc.bb);
+                const int done = bad || w[0] <= goal || sc.iter_in >= sc.maxit_in;
                 if (done) {
                     sc.conv_in = 1;
                     atomicSub(&eg->active_in, 1);

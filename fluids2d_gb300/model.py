@@ -274,6 +274,11 @@ class Integrator:
             m._upload_forcing(f)
         m._push()
         check(lib().f2d_rhs(m._h))
+        if m.param.model == "qgrsw":
+            # the projection of the tendency leaves its PV and streamfunction
+            # in s.pv and s.psi, as in the reference (equations.py:121)
+            for name in ("pv", "psi"):
+                check(lib().f2d_field_get(m._h, name.encode(), ptr(getattr(m._state, name))))
         _, prog = _specs(m.param)
         for name in prog:
             v = getattr(ds, name)
