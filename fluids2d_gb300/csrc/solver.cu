@@ -102,243 +102,6 @@ __device__ __forceinline__ void stage_region(const MGLevel& L, int J0, int I0,
     }
 }
 
-// Paired red-black layout of a staged region of WY rows x 2*PR columns: each
-// row is cut into PR pairs of adjacent nodes (columns 2j, 2j+1), one of each
-// colour; colour k's node of pair j of row r sits at packed index r*HWP + j
-// of colour k's arrays. HWP = PR rounded up to even, so that packed index
-// pairs (j, j+1), j even, are 8-byte (FP32) / 16-byte (FP64) aligned and a
-// half sweep moves two nodes per shared-memory access. The padding slot of a
-// row (when PR is odd) holds mask 0 and x 0. The x arrays of the two colours
-// are 64 bytes apart modulo 128, so that a warp reading alternate colours of
-// consecutive nodes touches each bank once. Layout: x red, x black, b red,
-// b black, mask red, mask black.
-template <typename S, int PR, int WY>
-struct PRL {
-    static constexpr int HWP = (PR + 1) / 2 * 2;
-    static constexpr int NP = WY * HWP;
-    static constexpr size_t CS = ((NP * sizeof(S) + 127) / 128) * 128 + 64;
-    static constexpr size_t CM = ((NP + 127) / 128) * 128;
-    static constexpr size_t BYTES = 4 * CS + 2 * CM;
-};
-
-template <typename S, int PR, int WY>
-struct PRegion {
-    unsigned char* base;
-    using L = PRL<S, PR, WY>;
-    __device__ __forceinline__ explicit PRegion(unsigned char* p) : base(p) {}
-    __device__ __forceinline__ S* x(int k) const { return (S*)(base + k * L::CS); }
-    __device__ __forceinline__ S* b(int k) const { return (S*)(base + (2 + k) * L::CS); }
-    __device__ __forceinline__ uint8_t* m(int k) const { return base + 4 * L::CS + k * L::CM; }
-};
-
-template <typename S> struct Pair;
-template <> struct Pair<float> { using T = float2; };
-template <> struct Pair<double> { using T = double2; };
-
-template <typename S>
-__device__ __forceinline__ typename Pair<S>::T ld2(const S* p)
-{
-    return *reinterpret_cast<const typename Pair<S>::T*>(p);
-}
-template <typename S>
-__device__ __forceinline__ void st2(S* p, S a, S b)
-{
-    typename Pair<S>::T v;
-    v.x = a;
-    v.y = b;
-    *reinterpret_cast<typename Pair<S>::T*>(p) = v;
-}
-__device__ __forceinline__ unsigned ld_m2(const uint8_t* p)
-{
-    return *reinterpret_cast<const unsigned short*>(p);
-}
-
-// Stage a region whose first column is I0 - HX (HX odd) and first row
-// J0 - HY, colour of region node (r, c) = (r + c + HX + HY) & 1 (the tile
-// origin is even). Down leg (XA = false): b, the mask, and the pre-smoothing
-// start x = b/diag on colour 0, x = 0 on colour 1. Up leg (XA = true, HY
-// even): b, the mask, and x = xa + P (coarse x) from the staged coarse region
-// sc2 (CW = PR + 1 columns from coarse column (I0-HX)>>1, rows from
-// (J0-HY)>>1); bilinear P written as the average of two row averages, an
-// even index repeating its node, so the weights 1, 1/2, 1/4 come out exactly.
-// b and x are 0 at non-fluid nodes. A region inside the level is read in
-// node pairs: node (J, I) of every level sits at an element index of the
-// parity of I + 1 (odd level offsets, even pitches), so a pair that starts
-// at the odd column I0 - HX + 2j starts on an even element (8/16-byte
-// aligned). Regions that cross the level's edge (out-of-level nodes read as
-// non-fluid 0, x-periodic levels wrap) go node by node.
-template <typename S, int HX, int HY, int PR, int WY, bool XA>
-__device__ __forceinline__ void stage_pairs(const PRegion<S, PR, WY>& R, const MGLevel& F,
-                                            int J0, int I0, S id, const S* __restrict__ gxa,
-                                            const S* __restrict__ sc2)
-{
-    static_assert(HX % 2 == 1, "the region starts on an odd column");
-    static_assert(!XA || HY % 2 == 0, "the up leg's region starts on an even row");
-    constexpr int HWP = PRL<S, PR, WY>::HWP, NPAIR = WY * PR, W = 2 * PR;
-    constexpr int CP = (HX + HY) & 1, CW = PR + 1;
-    const int t = tid256();
-    const S* __restrict__ gb = lb<S>(F);
-    if (HWP != PR && t < WY) {
-        // padding slot of row t: mask 0, x 0, b 0
-        const int q = t * HWP + PR;
-        R.m(0)[q] = 0;
-        R.m(1)[q] = 0;
-        R.x(0)[q] = S(0);
-        R.x(1)[q] = S(0);
-        R.b(0)[q] = S(0);
-        R.b(1)[q] = S(0);
-    }
-    const bool inner = J0 - HY >= 0 && J0 - HY + WY <= F.nyn && I0 - HX >= 0 &&
-                       I0 - HX + W <= F.nxn;
-    if (inner) {
-        const long long base = F.off + (long long)(J0 - HY) * F.pitch + (I0 - HX);
-        const int pitch = (int)F.pitch;
-#pragma unroll
-        for (int it = 0; it < (NPAIR + 255) / 256; ++it) {
-            const int e = t + 256 * it;
-            if (NPAIR % 256 != 0 && e >= NPAIR) break;
-            const int r = e / PR, j = e - r * PR;
-            const long long k = base + (r * pitch + 2 * j);
-            const typename Pair<S>::T bv = ld2<S>(gb + k);
-            const unsigned mv = ld_m2(F.m + k);
-            const unsigned m0 = mv & 0xffu, m1 = mv >> 8;
-            const S b0 = m0 ? bv.x : S(0), b1 = m1 ? bv.y : S(0);
-            S x0, x1;
-            if (XA) {
-                // first node: odd column (between coarse columns j, j+1),
-                // second: even column (on coarse column j+1); row r: on
-                // coarse row r/2 (r even) or between r/2 and r/2 + 1
-                const typename Pair<S>::T a = ld2<S>(gxa + k);
-                const int qc = (r >> 1) * CW + j, oj = (r & 1) * CW;
-                const S A = sc2[qc], B = sc2[qc + 1], Cc = sc2[qc + oj], D = sc2[qc + oj + 1];
-                const S h0 = S(0.5) * (A + B), h1 = S(0.5) * (Cc + D);
-                const S g0 = S(0.5) * (B + B), g1 = S(0.5) * (D + D);
-                x0 = m0 ? a.x + S(0.5) * (h0 + h1) : S(0);
-                x1 = m1 ? a.y + S(0.5) * (g0 + g1) : S(0);
-            }
-            const int q = r * HWP + j;
-            // the pair's first node has colour (r + CP) & 1
-            const bool f0 = ((r + CP) & 1) == 0;
-            const S br = f0 ? b0 : b1;
-            R.b(0)[q] = br;
-            R.b(1)[q] = f0 ? b1 : b0;
-            R.m(0)[q] = (uint8_t)(f0 ? m0 : m1);
-            R.m(1)[q] = (uint8_t)(f0 ? m1 : m0);
-            if (XA) {
-                R.x(0)[q] = f0 ? x0 : x1;
-                R.x(1)[q] = f0 ? x1 : x0;
-            } else {
-                R.x(0)[q] = br * id;
-                R.x(1)[q] = S(0);
-            }
-        }
-    } else {
-        constexpr int N = WY * W;
-        const int cj0 = (J0 - HY) >> 1, ci0 = (I0 - HX) >> 1;
-#pragma unroll 4
-        for (int e = t; e < N; e += 256) {
-            const int r = e / W, c = e - r * W;
-            const int J = J0 - HY + r, Iu = I0 - HX + c;
-            int I = Iu;
-            uint8_t mv = 0;
-            S bv = S(0), xv = S(0);
-            if (in_level(F, J, I)) {
-                const long long k = nidx(F, J, I);
-                mv = F.m[k];
-                bv = gb[k];
-                if (XA) xv = gxa[k];
-            }
-            bv = mv ? bv : S(0);
-            const int col = (r + c + CP) & 1, q = r * HWP + (c >> 1);
-            R.m(col)[q] = mv;
-            R.b(col)[q] = bv;
-            if (XA) {
-                // coarse indices relative to the staged coarse region
-                const int qc = ((J >> 1) - cj0) * CW + ((Iu >> 1) - ci0);
-                const int oj = (J & 1) * CW, oi = Iu & 1;
-                const S h0 = S(0.5) * (sc2[qc] + sc2[qc + oi]);
-                const S h1 = S(0.5) * (sc2[qc + oj] + sc2[qc + oj + oi]);
-                R.x(col)[q] = mv ? xv + S(0.5) * (h0 + h1) : S(0);
-            } else {
-                R.x(col)[q] = col == 0 ? bv * id : S(0);
-            }
-        }
-    }
-}
-
-// Red-black half sweep of colour `col` on rows R0..R1 of a paired region
-// (colour of node (r, c) = (r + c + CP) & 1): every node of that colour gets
-// x = (b - offdiag(x)) / diag at fluid nodes, 0 elsewhere. A thread updates
-// the two packed nodes j, j+1 (j even) of a row: in row rr the colour's nodes
-// sit at columns 2j + p, p = (col + rr + CP) & 1, so their west/east
-// neighbours are the other colour's packed nodes j-1+p, j+p, j+1+p (one
-// pair load and one scalar load) and their north/south ones the other
-// colour's packed pairs of rows rr -+ 1. Nodes within s of the region edge
-// are updated from neighbours that are no longer exact; by induction the
-// nodes at distance >= s from the edge are exact after half sweep s, and the
-// callers sweep rows s .. WY-1-s only and read only exact nodes afterwards.
-template <typename S, int PR, int WY, int CP, int R0, int R1>
-__device__ __forceinline__ void sweep_pairs(const PRegion<S, PR, WY>& R, int col, S cx, S cy,
-                                            S id)
-{
-    constexpr int HWP = PRL<S, PR, WY>::HWP, NPR = HWP / 2, n = (R1 - R0 + 1) * NPR;
-    const int t = tid256();
-    S* __restrict__ xo = R.x(col);
-    const S* __restrict__ xn = R.x(col ^ 1);
-    const S* __restrict__ bo = R.b(col);
-    const uint8_t* __restrict__ mo = R.m(col);
-#pragma unroll
-    for (int it = 0; it < (n + 255) / 256; ++it) {
-        const int e = t + 256 * it;
-        if (n % 256 != 0 && e >= n) break;
-        const int rr = R0 + e / NPR;
-        const int q = rr * HWP + 2 * (e - (rr - R0) * NPR);
-        const int p = (col + rr + CP) & 1;
-        const typename Pair<S>::T a = ld2<S>(xn + q);
-        const S sx = xn[p ? q + 2 : q - 1];
-        const typename Pair<S>::T nn = ld2<S>(xn + q - HWP), ss = ld2<S>(xn + q + HWP);
-        const typename Pair<S>::T bb = ld2<S>(bo + q);
-        const unsigned mm = ld_m2(mo + q);
-        const S w0 = p ? a.x : sx, e0 = p ? a.y : a.x;
-        const S w1 = p ? a.y : a.x, e1 = p ? sx : a.y;
-        const S v0 = (bb.x - (cx * (w0 + e0) + cy * (nn.x + ss.x))) * id;
-        const S v1 = (bb.y - (cx * (w1 + e1) + cy * (nn.y + ss.y))) * id;
-        st2<S>(xo + q, (mm & 0xffu) ? v0 : S(0), (mm >> 8) ? v1 : S(0));
-    }
-}
-
-// residual r = b - A x at the colour-0 nodes of rows R0..R1 (in place of b;
-// 0 at non-fluid nodes), two packed nodes per thread as in sweep_pairs
-template <typename S, int PR, int WY, int CP, int R0, int R1>
-__device__ __forceinline__ void residual_pairs(const PRegion<S, PR, WY>& R, S cx, S cy, S md)
-{
-    constexpr int HWP = PRL<S, PR, WY>::HWP, NPR = HWP / 2, n = (R1 - R0 + 1) * NPR;
-    const int t = tid256();
-    const S* __restrict__ xr = R.x(0);
-    const S* __restrict__ xb = R.x(1);
-    S* __restrict__ br = R.b(0);
-    const uint8_t* __restrict__ mr = R.m(0);
-#pragma unroll
-    for (int it = 0; it < (n + 255) / 256; ++it) {
-        const int e = t + 256 * it;
-        if (n % 256 != 0 && e >= n) break;
-        const int rr = R0 + e / NPR;
-        const int q = rr * HWP + 2 * (e - (rr - R0) * NPR);
-        const int p = (rr + CP) & 1;
-        const typename Pair<S>::T c = ld2<S>(xr + q);
-        const typename Pair<S>::T a = ld2<S>(xb + q);
-        const S sx = xb[p ? q + 2 : q - 1];
-        const typename Pair<S>::T ss = ld2<S>(xb + q - HWP), nn = ld2<S>(xb + q + HWP);
-        const typename Pair<S>::T bb = ld2<S>(br + q);
-        const unsigned mm = ld_m2(mr + q);
-        const S w0 = p ? a.x : sx, e0 = p ? a.y : a.x;
-        const S w1 = p ? a.y : a.x, e1 = p ? sx : a.y;
-        const S r0 = bb.x - apply_diff<S>(cx, cy, md, c.x, w0, e0, ss.x, nn.x);
-        const S r1 = bb.y - apply_diff<S>(cx, cy, md, c.y, w1, e1, ss.y, nn.y);
-        st2<S>(br + q, (mm & 0xffu) ? r0 : S(0), (mm >> 8) ? r1 : S(0));
-    }
-}
-
 // per-thread dot-product partial -> what seg_reduce2 expects: FP32 values
 // are summed per warp in FP32 and combined in FP64 (block total in thread 0);
 // FP64 values go to seg_reduce2's own FP64 block reduction.
@@ -398,158 +161,10 @@ __device__ __forceinline__ void set_rz(DevScalars& sc, int ir, double rz)
     sc.rz = rz;
 }
 
-// ---- multigrid --------------------------------------------------------------
-// Down leg of level l (l below the member's tail): pre-smoothing from a zero
-// guess - red x = b/diag, black Gauss-Seidel, then NU-1 more (red, black)
-// sweeps - and restriction of the residual to level l+1 (transpose of the
-// bilinear prolongation). After a black half sweep the black residuals are
-// zero, so only the red fine nodes (centre and corners of a coarse node)
-// contribute. Writes the pre-smoothed x of the tile (to xa) and the coarse
-// right-hand side of the coarse nodes whose centre lies in the tile. The
-// staged region has a halo of 2NU+1 nodes (paired layout, PRL).
-template <typename S, int NU, int TH>
-__global__ void __launch_bounds__(256)
-k_bs_down(const int4* __restrict__ tiles, const BSInfo* __restrict__ info,
-          const MGLevel* __restrict__ levs, int l, const DevScalars* __restrict__ scs, int ir)
-{
-    constexpr int H = 2 * NU + 1, PR = (BS_TW + 2 * H) / 2, WY = TH + 2 * H, TQ = TH / 8;
-    constexpr int HWP = PRL<S, PR, WY>::HWP;
-    extern __shared__ __align__(128) unsigned char dsm[];
-    const PRegion<S, PR, WY> R(dsm);
-    const int4 tl = tiles[blockIdx.x];
-    if (info[tl.x].ltail <= l || bs_skip(scs[tl.x], ir)) return;
-    const MGLevel F = levs[tl.x * BS_LMAX + l];
-    const int I0 = tl.y, J0 = tl.z, t = tid256();
-    const S cx = Coef<S>::cx(F), cy = Coef<S>::cy(F), id = Coef<S>::idiag(F);
-    stage_pairs<S, H, H, PR, WY, false>(R, F, J0, I0, id, nullptr, nullptr);
-    __syncthreads();
-    // black, then (red, black) NU-1 times; rows s .. WY-1-s at half sweep s
-    sweep_pairs<S, PR, WY, 0, 1, WY - 2>(R, 1, cx, cy, id);
-    __syncthreads();
-    if constexpr (NU >= 2) {
-        sweep_pairs<S, PR, WY, 0, 2, WY - 3>(R, 0, cx, cy, id);
-        __syncthreads();
-        sweep_pairs<S, PR, WY, 0, 3, WY - 4>(R, 1, cx, cy, id);
-        __syncthreads();
-    }
-    // residual at the red nodes at distance >= 2 NU from the region edge
-    // (exact there; all the restriction reads)
-    residual_pairs<S, PR, WY, 0, 2 * NU, WY - 1 - 2 * NU>(R, cx, cy, Coef<S>::md(F));
-    __syncthreads();
-    {
-        // coarse nodes with their centre in the tile: (TH/2) x (BS_TW/2);
-        // the centre and its four diagonal neighbours are red
-        const MGLevel C = levs[tl.x * BS_LMAX + l + 1];
-        const S* __restrict__ br = R.b(0);
-        static_assert((TH / 2) * (BS_TW / 2) % 256 == 0, "coarse nodes per thread");
-#pragma unroll
-        for (int k2 = 0; k2 < (TH / 2) * (BS_TW / 2) / 256; ++k2) {
-            const int e = t + 256 * k2;
-            const int a = e / (BS_TW / 2), b = e % (BS_TW / 2);
-            const int cJ = (J0 >> 1) + a, cI = (I0 >> 1) + b;
-            if (cJ < C.nyn && cI < C.nxn) {
-                const long long k = nidx(C, cJ, cI);
-                S v = S(0);
-                if (C.m[k]) {
-                    const int r0 = H + 2 * a, c0 = H + 2 * b;
-                    // c0 odd: the corners (columns c0 -+ 1) are the red
-                    // nodes of packed slots c0>>1 and c0>>1 + 1 of rows r0 -+ 1
-                    const int qc = r0 * HWP + (c0 >> 1);
-                    const int qn = qc - HWP, qs = qc + HWP;
-                    const S c4 = (br[qn] + br[qn + 1]) + (br[qs] + br[qs + 1]);
-                    v = br[qc] + S(0.25) * c4;
-                }
-                lb<S>(C)[k] = v;
-            }
-        }
-    }
-    S* xa = (S*)F.xa;
-#pragma unroll
-    for (int qr = 0; qr < TQ; ++qr) {
-        const int r = threadIdx.y + 8 * qr, c = threadIdx.x;
-        const int J = J0 + r, I = I0 + c;
-        if (J < F.nyn && I < F.nxn)
-            xa[nidx(F, J, I)] = R.x((r + c) & 1)[(r + H) * HWP + ((c + H) >> 1)];
-    }
-}
-
-// Up leg of level l: x = xa + P (coarse x), then NU (black, red)
-// post-smoothing sweeps; writes x of the tile. The staged region has a halo
-// of 2NU rows and 2NU+1 columns (the paired layout starts on the odd column
-// I0-2NU-1); the coarse nodes it interpolates from (columns (I0-2NU-1)/2 ..,
-// rows (J0-2NU)/2 ..) are staged first: 0 outside the coarse level and at
-// non-fluid nodes, wrapped when x-periodic (an even fine period makes the
-// wrapped fine node's coarse neighbours the wrapped coarse ones). On level 0
-// (RZ) the block also forms its part of <r, z> (r = b, z = x) and the
-// member's last block sets rz and beta.
-template <typename S, int NU, bool RZ, int TH>
-__global__ void __launch_bounds__(256)
-k_bs_up(const int4* __restrict__ tiles, const BSInfo* __restrict__ info,
-        const MGLevel* __restrict__ levs, int l, DevScalars* scs, int ir, double* partials,
-        double* gpart, unsigned int* gtick)
-{
-    constexpr int HX = 2 * NU + 1, HY = 2 * NU, PR = (BS_TW + 2 * HX) / 2, WY = TH + 2 * HY;
-    constexpr int CP = (HX + HY) & 1, TQ = TH / 8, HWP = PRL<S, PR, WY>::HWP;
-    constexpr int CW = PR + 1, CWY = WY / 2 + 1, CN = CW * CWY, CIT = (CN + 255) / 256;
-    extern __shared__ __align__(128) unsigned char dsm[];
-    const PRegion<S, PR, WY> R(dsm);
-    S* sc2 = (S*)(dsm + PRL<S, PR, WY>::BYTES);
-    const int4 tl = tiles[blockIdx.x];
-    DevScalars& sc = scs[tl.x];
-    const BSInfo in = info[tl.x];
-    if (in.ltail <= l || bs_skip(sc, ir)) return;
-    const MGLevel F = levs[tl.x * BS_LMAX + l];
-    const MGLevel C = levs[tl.x * BS_LMAX + l + 1];
-    const int I0 = tl.y, J0 = tl.z, t = tid256();
-    const int cj0 = (J0 - HY) >> 1, ci0 = (I0 - HX) >> 1;
-    {
-        const S* __restrict__ cxg = lx<S>(C);
-#pragma unroll
-        for (int k2 = 0; k2 < CIT; ++k2) {
-            const int e = t + k2 * 256;
-            if (e < CN) {
-                const int r = e / CW, c = e - r * CW;
-                int I = ci0 + c;
-                S v = S(0);
-                if (in_level(C, cj0 + r, I)) v = cxg[nidx(C, cj0 + r, I)];
-                sc2[e] = v;
-            }
-        }
-    }
-    __syncthreads();
-    const S cx = Coef<S>::cx(F), cy = Coef<S>::cy(F), id = Coef<S>::idiag(F);
-    stage_pairs<S, HX, HY, PR, WY, true>(R, F, J0, I0, id, (const S*)F.xa, sc2);
-    __syncthreads();
-    // (black, red) NU times; rows s .. WY-1-s at half sweep s
-    sweep_pairs<S, PR, WY, CP, 1, WY - 2>(R, 1, cx, cy, id);
-    __syncthreads();
-    sweep_pairs<S, PR, WY, CP, 2, WY - 3>(R, 0, cx, cy, id);
-    __syncthreads();
-    if constexpr (NU >= 2) {
-        sweep_pairs<S, PR, WY, CP, 3, WY - 4>(R, 1, cx, cy, id);
-        __syncthreads();
-        sweep_pairs<S, PR, WY, CP, 4, WY - 5>(R, 0, cx, cy, id);
-        __syncthreads();
-    }
-    S* x = lx<S>(F);
-    S acc = S(0);
-#pragma unroll
-    for (int qr = 0; qr < TQ; ++qr) {
-        const int r = threadIdx.y + 8 * qr, c = threadIdx.x;
-        const int J = J0 + r, I = I0 + c;
-        const int col = (r + c + HX + HY + CP) & 1;
-        const int q = (r + HY) * HWP + ((c + HX) >> 1);
-        if (J < F.nyn && I < F.nxn) {
-            const S xv = R.x(col)[q];
-            x[nidx(F, J, I)] = xv;
-            if (RZ) acc += R.b(col)[q] * xv;  // 0 at non-fluid nodes
-        }
-    }
-    if (RZ) {
-        double w[1];
-        if (member_dot<S>(acc, w, partials, gpart, gtick, in, &sc.counter[2])) set_rz(sc, ir, w[0]);
-    }
-}
+// ---- multigrid level kernels (register-blocked; mg_reg.cuh) ----------------
+}  // namespace f2d
+#include "mg_reg.cuh"
+namespace f2d {
 
 // Coarse levels of every member in one block each (tail_vcycle). A member
 // whose level 0 is already in the tail also forms <r, z> here.
@@ -968,61 +583,30 @@ static bool bs_eager()
     return v == 1;
 }
 
-// dynamic shared memory of the down and up kernels (staged region, coarse
-// region, mask)
-template <typename S, int NU, int TH>
-static size_t down_smem()
-{
-    constexpr int H = 2 * NU + 1;
-    return PRL<S, (BS_TW + 2 * H) / 2, TH + 2 * H>::BYTES;
-}
-template <typename S, int NU, int TH>
-static size_t up_smem()
-{
-    constexpr int HX = 2 * NU + 1, HY = 2 * NU, PR = (BS_TW + 2 * HX) / 2, WY = TH + 2 * HY;
-    constexpr size_t CN = (size_t)(PR + 1) * (WY / 2 + 1);
-    return PRL<S, PR, WY>::BYTES + CN * sizeof(S);
-}
-
-template <typename S, int NU, int TH>
-static int set_level_attrs()
-{
-    cudaError_t e = cudaFuncSetAttribute(k_bs_down<S, NU, TH>,
-                                         cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                         (int)down_smem<S, NU, TH>());
-    if (e == cudaSuccess)
-        e = cudaFuncSetAttribute(k_bs_up<S, NU, false, TH>,
-                                 cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                 (int)up_smem<S, NU, TH>());
-    if (e == cudaSuccess)
-        e = cudaFuncSetAttribute(k_bs_up<S, NU, true, TH>,
-                                 cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                 (int)up_smem<S, NU, TH>());
-    return (int)e;
-}
-
 // one V-cycle for all members still iterating: a down kernel per grid level,
 // the tail, an up kernel per grid level (the level-0 one also forms <r, z>)
 template <typename S, int NU, int TH>
 static int vcycle_nu(BatchSolver& s, cudaStream_t st, int ir)
 {
-    const dim3 blk(32, 8);
+    const dim3 blk(32, MR_NW);
     int cnt = 0;
     for (int l = 0; l < s.maxl; ++l) {
-        k_bs_down<S, NU, TH><<<s.ntiles[l], blk, down_smem<S, NU, TH>(), st>>>(
-            s.tiles[l], s.dinfo, s.dlevs, l, s.scs, ir);
+        k_mg_down<S, NU><<<s.nmtiles[l], blk, 0, st>>>(s.mtiles[l], s.dinfo, s.dlevs, l,
+                                                       s.scs, ir);
         cnt += 1;
     }
     k_bs_tail<S><<<s.n, 1024, s.tail_smem, st>>>(s.dinfo, s.dlevs, s.scs, ir, NU);
     cnt += 1;
     for (int l = s.maxl - 1; l >= 1; --l) {
-        k_bs_up<S, NU, false, TH><<<s.ntiles[l], blk, up_smem<S, NU, TH>(), st>>>(
-            s.tiles[l], s.dinfo, s.dlevs, l, s.scs, ir, s.partials, s.gpart, s.gtick);
+        k_mg_up<S, NU, false><<<s.nmtiles[l], blk, 0, st>>>(s.mtiles[l], s.dinfo, s.dlevs, l,
+                                                           s.scs, ir, s.partials, s.gpart,
+                                                           s.gtick);
         cnt += 1;
     }
     if (s.maxl > 0) {
-        k_bs_up<S, NU, true, TH><<<s.ntiles[0], blk, up_smem<S, NU, TH>(), st>>>(
-            s.tiles[0], s.dinfo, s.dlevs, 0, s.scs, ir, s.partials, s.gpart, s.gtick);
+        k_mg_up<S, NU, true><<<s.nmtiles[0], blk, 0, st>>>(s.mtiles[0], s.dinfo, s.dlevs, 0,
+                                                          s.scs, ir, s.partials, s.gpart,
+                                                          s.gtick);
         cnt += 1;
     }
     return cnt;
@@ -1185,11 +769,11 @@ __global__ void k_bs_activate(DevScalars* scs, int n)
     }
 }
 
-template <typename S, int NU, int TH>
+template <typename S, int NU>
 static void launch_down0(BatchSolver& s, cudaStream_t st, int ir)
 {
-    k_bs_down<S, NU, TH><<<s.ntiles[0], dim3(32, 8), down_smem<S, NU, TH>(), st>>>(
-        s.tiles[0], s.dinfo, s.dlevs, 0, s.scs, ir);
+    k_mg_down<S, NU><<<s.nmtiles[0], dim3(32, MR_NW), 0, st>>>(s.mtiles[0], s.dinfo, s.dlevs, 0,
+                                                              s.scs, ir);
 }
 
 int bs_time_down(BatchSolver& s, cudaStream_t st, int reps, int flush_l2, double* avg_ms,
@@ -1213,14 +797,9 @@ int bs_time_down(BatchSolver& s, cudaStream_t st, int reps, int flush_l2, double
     for (int r = 0; r < reps && !err; ++r) {
         if (fl) cudaMemsetAsync(fl, r & 0xff, flush_bytes, st);
         cudaEventRecord(a, st);
-        const bool two = s.nu >= 2, big = s.th == 64;
-        if (s.mode == 0) {
-            if (two) big ? launch_down0<double, 2, 64>(s, st, ir) : launch_down0<double, 2, 32>(s, st, ir);
-            else big ? launch_down0<double, 1, 64>(s, st, ir) : launch_down0<double, 1, 32>(s, st, ir);
-        } else {
-            if (two) big ? launch_down0<float, 2, 64>(s, st, ir) : launch_down0<float, 2, 32>(s, st, ir);
-            else big ? launch_down0<float, 1, 64>(s, st, ir) : launch_down0<float, 1, 32>(s, st, ir);
-        }
+        const bool two = s.nu >= 2;
+        if (s.mode == 0) two ? launch_down0<double, 2>(s, st, ir) : launch_down0<double, 1>(s, st, ir);
+        else two ? launch_down0<float, 2>(s, st, ir) : launch_down0<float, 1>(s, st, ir);
         cudaEventRecord(b, st);
         if (cudaEventSynchronize(b) != cudaSuccess) err = 3;
         float ms = 0.f;
@@ -1284,12 +863,10 @@ int bs_build(BatchSolver& s, const std::vector<BSMemberDesc>& members, const uin
         s.th = s.th_force ? s.th_force : n0 >= 2ll * 1024 * 1024 ? 64 : 32;
     }
     const int TH = s.th;
-    // Tile tables of 32 x TH nodes. Level 0 (all members; the Krylov
-    // kernels and the first multigrid level) with the members' reduction
-    // groups of RED_GROUP tiles; level l >= 1 for the members whose grid
-    // levels reach below it. Tiles without a fluid node are left out (their
-    // nodes stay 0 in every vector), but every member keeps at least one
-    // level-0 tile for its reductions.
+    // Tile table of 32 x TH level-0 nodes for the Krylov kernels (all
+    // members) with the members' reduction groups of RED_GROUP tiles. Tiles
+    // without a fluid node are left out (their nodes stay 0 in every
+    // vector), but every member keeps at least one tile for its reductions.
     auto has_fluid = [&](int b, int l, int J0, int I0) {
         const std::vector<uint8_t>& hm = s.mg[b].hmask[l];
         const MGLevel& L = levs[(size_t)b * BS_LMAX + l];
@@ -1298,7 +875,7 @@ int bs_build(BatchSolver& s, const std::vector<BSMemberDesc>& members, const uin
                 if (hm[(size_t)J * L.nxn + I]) return true;
         return false;
     };
-    std::vector<std::vector<int4>> tiles(std::max(1, s.maxl));
+    std::vector<std::vector<int4>> tiles(1);
     std::vector<int4>& rt = tiles[0];
     int ngroups = 0;
     for (int b = 0; b < s.n; ++b) {
@@ -1312,13 +889,25 @@ int bs_build(BatchSolver& s, const std::vector<BSMemberDesc>& members, const uin
         info[b].g0 = ngroups;
         ngroups += (info[b].nn + RED_GROUP - 1) / RED_GROUP;
     }
-    for (int l = 1; l < s.maxl; ++l)
+    // Tile tables of the multigrid level kernels (MR_TW x MR_TH nodes,
+    // register-blocked, mg_reg.cuh) for every grid level below a member's
+    // tail; tiles without a fluid node are left out.
+    auto has_fluid_m = [&](int b, int l, int J0, int I0) {
+        const std::vector<uint8_t>& hm = s.mg[b].hmask[l];
+        const MGLevel& L = levs[(size_t)b * BS_LMAX + l];
+        for (int J = J0; J < std::min(L.nyn, J0 + MR_TH); ++J)
+            for (int I = I0; I < std::min(L.nxn, I0 + MR_TW); ++I)
+                if (hm[(size_t)J * L.nxn + I]) return true;
+        return false;
+    };
+    std::vector<std::vector<int4>> mt(std::max(1, s.maxl));
+    for (int l = 0; l < s.maxl; ++l)
         for (int b = 0; b < s.n; ++b) {
             if (info[b].ltail <= l) continue;
             const MGLevel& L = levs[(size_t)b * BS_LMAX + l];
-            for (int J0 = 0; J0 < L.nyn; J0 += TH)
-                for (int I0 = 0; I0 < L.nxn; I0 += BS_TW)
-                    if (has_fluid(b, l, J0, I0)) tiles[l].push_back(make_int4(b, I0, J0, 0));
+            for (int J0 = 0; J0 < L.nyn; J0 += MR_TH)
+                for (int I0 = 0; I0 < L.nxn; I0 += MR_TW)
+                    if (has_fluid_m(b, l, J0, I0)) mt[l].push_back(make_int4(b, I0, J0, 0));
         }
     auto dal = [&](size_t bytes) -> void* {
         void* p = nullptr;
@@ -1326,6 +915,17 @@ int bs_build(BatchSolver& s, const std::vector<BSMemberDesc>& members, const uin
         s.owned.push_back(p);
         return p;
     };
+    s.mtiles.assign(mt.size(), nullptr);
+    s.nmtiles.assign(mt.size(), 0);
+    for (size_t l = 0; l < mt.size(); ++l) {
+        s.nmtiles[l] = (int)mt[l].size();
+        s.mtiles[l] = (int4*)dal(std::max<size_t>(1, mt[l].size()) * sizeof(int4));
+        if (!s.mtiles[l]) return 2;
+        if (!mt[l].empty() &&
+            cudaMemcpy(s.mtiles[l], mt[l].data(), mt[l].size() * sizeof(int4),
+                       cudaMemcpyHostToDevice) != cudaSuccess)
+            return 2;
+    }
     const int ntab = (int)tiles.size();
     s.tiles.assign(ntab, nullptr);
     s.ntiles.assign(ntab, 0);
@@ -1361,15 +961,6 @@ int bs_build(BatchSolver& s, const std::vector<BSMemberDesc>& members, const uin
     // needs and never lower it, or the launches (and new graph captures) of
     // an existing solver with a larger tail would fail. (One host thread and
     // one device per process, as everywhere in this library.)
-    static bool level_attrs = false;  // constant per kernel instantiation: once
-    if (!level_attrs) {
-        if (set_level_attrs<float, 1, 32>() || set_level_attrs<float, 2, 32>() ||
-            set_level_attrs<double, 1, 32>() || set_level_attrs<double, 2, 32>() ||
-            set_level_attrs<float, 1, 64>() || set_level_attrs<float, 2, 64>() ||
-            set_level_attrs<double, 1, 64>() || set_level_attrs<double, 2, 64>())
-            return 4;
-        level_attrs = true;
-    }
     static size_t tail_attr[2] = {0, 0};
     const int ti = mode == 0 ? 0 : 1;
     if (s.tail_smem > tail_attr[ti]) {

@@ -60,6 +60,8 @@ struct BatchSolver {
     double* partials = nullptr;
     std::vector<int4*> tiles;  // node tiles per level (members reaching it)
     std::vector<int> ntiles;
+    std::vector<int4*> mtiles; // tiles of the multigrid level kernels per level
+    std::vector<int> nmtiles;
     int4* rtiles = nullptr;    // level-0 tiles of the Krylov kernels
     int nrtiles = 0;
     double* gpart = nullptr;   // group sums of the two-level reductions
