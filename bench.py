@@ -423,6 +423,22 @@ def ensemble_cpu_rate(budget_s, steps=1, warmup=1):
     return cells_all / est, sample, timed, O.num_threads(), est_steps
 
 
+def reference_as_shipped():
+    """The unmodified reference's own timing on the ensemble's grid sizes
+    (pure-Python kernels on one core, numba being absent), measured by
+    oracle/time_reference.py where the reference's source is available (it
+    cannot run on the GPU host); None when that measurement is absent."""
+    path = os.path.join(ROOT, "oracle", "reference_timing.json")
+    if not os.path.exists(path):
+        return None
+    with open(path) as f:
+        d = json.load(f)
+    d["note"] = ("measured with oracle/time_reference.py on the host named here, "
+                 "not on this run's host: the reference cannot be installed on the "
+                 "GPU host")
+    return d
+
+
 def run_reference(args, rank, world):
     """--impl reference: the CPU implementation of the path on host cores."""
     if is_ensemble(args.workload):
@@ -455,6 +471,9 @@ def run_reference(args, rank, world):
             "e2e": {"value": rate, "unit": "cell-updates/s",
                     "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
         }
+        ref = reference_as_shipped()
+        if ref:
+            line["cpu_baseline"]["reference_as_shipped"] = ref
         print(json.dumps(line), flush=True)
         return
     model, case, desc = build_case(args.workload)
@@ -686,6 +705,9 @@ def run_gpu_ensemble(args, rank, world):
                       f"whole-ensemble step time estimated as the sum over sizes of "
                       f"members x mean member step time",
             "per_size": smp}
+        ref = reference_as_shipped()
+        if ref:
+            line["cpu_baseline"]["reference_as_shipped"] = ref
     if rank == 0:
         print(json.dumps(line), flush=True)
 

@@ -194,6 +194,19 @@ __global__ void k_adj_snap(const T* __restrict__ w, const T* __restrict__ ux,
 
 __global__ void k_adj_slot(int* slot, int delta) { *slot += delta; }
 
+// The per-stage cache of the forward streamfunctions: store cache[*slot] =
+// psi, or restore psi = cache[*slot] (fields of fsz FP64 elements).
+__global__ void k_adj_psi(double* __restrict__ psi, double* __restrict__ cache, long long fsz,
+                          const int* __restrict__ slot, int store)
+{
+    double* c = cache + (long long)(*slot) * fsz;
+    for (long long k = blockIdx.x * (long long)blockDim.x + threadIdx.x; k < fsz;
+         k += (long long)gridDim.x * blockDim.x) {
+        if (store) c[k] = psi[k];
+        else psi[k] = c[k];
+    }
+}
+
 // RK3 combinations of the adjoint (integrators.py:92-107 reversed):
 // mode 0: d3 = c3 y, d2 = c2 y, d1 = c1 y; mode 1: d1 += c1 y, d2 += c2 y;
 // mode 2: d1 += c1 y
@@ -352,6 +365,14 @@ int launch_adj_snap(int prec, const void* w, const void* ux, const void* uy, voi
     else
         k_adj_snap<float><<<nb, 256, 0, s>>>((const float*)w, (const float*)ux,
                                              (const float*)uy, (float*)arena, fsz, slot);
+    return (int)cudaGetLastError();
+}
+
+int launch_adj_psi(double* psi, double* cache, long long fsz, const int* slot, int store,
+                   cudaStream_t s)
+{
+    const int nb = (int)std::min<long long>((fsz + 255) / 256, 152 * 8);
+    k_adj_psi<<<nb, 256, 0, s>>>(psi, cache, fsz, slot, store);
     return (int)cudaGetLastError();
 }
 

@@ -11,6 +11,10 @@ namespace f2d {
 int launch_adj_snap(int prec, const void* w, const void* ux, const void* uy, void* arena,
                     long long fsz, const int* slot, cudaStream_t s);
 int launch_adj_slot(int* slot, int delta, cudaStream_t s);
+// the per-stage streamfunction cache: store (store != 0) cache[*slot] = psi
+// or restore psi = cache[*slot]
+int launch_adj_psi(double* psi, double* cache, long long fsz, const int* slot, int store,
+                   cudaStream_t s);
 // adjoint RK3 combinations (mode 0: set d3,d2,d1; 1: d1,d2 +=; 2: d1 +=)
 int launch_adj_comb(const Geom& g, const double* yb, double* d1, double* d2, double* d3,
                     int mode, double c1, double c2, double c3, cudaStream_t s);

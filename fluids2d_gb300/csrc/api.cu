@@ -94,6 +94,13 @@ struct AdjState {
     double *yb = nullptr, *d1 = nullptr, *d2 = nullptr, *d3 = nullptr;
     double *gx = nullptr, *gy = nullptr, *ubx = nullptr, *uby = nullptr;
     double *psib = nullptr, *rb = nullptr;
+    // the forward's streamfunction after every stage (slot 3n + k after
+    // stage k of step n, slot 0 after the initial diagnostics), so that the
+    // recompute of a segment needs no Poisson solve; used when it fits
+    double* psic = nullptr;
+    long long psic_slots = 0;
+    int* pslot = nullptr;
+    bool use_psic = false;
 };
 
 struct f2d_model_s {
@@ -133,9 +140,11 @@ struct f2d_model_s {
     // graphs: [kind][parity]; kinds: 0 diag, 1 step, 2 run, 3 solve0, 4 solve1,
     // 5 step with adjoint snapshots, 6 adjoint step, 7 right-hand side alone,
     // 8-10 integrator stage 1-3 (with its diagnostics; the last stage of a
-    // step also advances the time line)
-    cudaGraphExec_t gx[11][2] = {};
-    int launches[11][2] = {};
+    // step also advances the time line), 11 step that caches the
+    // streamfunction of every stage, 12 snapshot step that takes it from the
+    // cache instead of solving
+    cudaGraphExec_t gx[13][2] = {};
+    int launches[13][2] = {};
     // prognostic variables (states.py:22-34 order) and whether the forcing
     // fields "frc.<var>" exist
     std::vector<std::string> prog;
@@ -732,6 +741,65 @@ static int rec_step_snap(f2d_model_s* m, int par, cudaStream_t s)
     return 0;
 }
 
+// the eulerpsi diagnostics of a recomputed stage from the forward's cached
+// streamfunction (slot *pslot, then advanced): perpgrad of it, no solve
+static int rec_diag_cached(f2d_model_s* m, cudaStream_t s)
+{
+    AdjState& a = m->adj;
+    const long long fsz = (long long)m->g.P * m->g.NY;
+    CKI(launch_adj_psi((double*)fb(m, "psi"), a.psic, fsz, a.pslot, 0, s));
+    CKI(launch_adj_slot(a.pslot, 1, s));
+    CKI(launch_perpgrad(0, m->prec, fb(m, "psi"), fb(m, "U.x"), fb(m, "U.y"), m->d_code,
+                        m->rdy2, m->rdx2, 1, m->g, m->sc, m->partials, s));
+    m->rec_launches += 3;
+    return 0;
+}
+
+// the forward's streamfunction into cache slot *pslot, then advanced
+static int rec_psi_store(f2d_model_s* m, cudaStream_t s)
+{
+    AdjState& a = m->adj;
+    const long long fsz = (long long)m->g.P * m->g.NY;
+    CKI(launch_adj_psi((double*)fb(m, "psi"), a.psic, fsz, a.pslot, 1, s));
+    CKI(launch_adj_slot(a.pslot, 1, s));
+    m->rec_launches += 2;
+    return 0;
+}
+
+// one forward step (fixed dt) that caches the streamfunction of every stage
+static int rec_step_store(f2d_model_s* m, int par, cudaStream_t s)
+{
+    for (int k = 1; k <= 3; ++k) {
+        int e = rec_stage(m, k, par, s);
+        if (e) return e;
+        if ((e = rec_psi_store(m, s))) return e;
+        par = 1 - par;
+    }
+    CKI(launch_pushforward(m->sc, s));
+    m->rec_launches += 1;
+    return 0;
+}
+
+// the snapshot step of the recompute with the cached streamfunctions
+static int rec_step_snap_cached(f2d_model_s* m, int par, cudaStream_t s)
+{
+    AdjState& a = m->adj;
+    const long long fsz = (long long)m->g.P * m->g.NY;
+    for (int k = 1; k <= 3; ++k) {
+        CKI(launch_adj_snap(m->prec, fb(m, "omega", par), fb(m, "U.x"), fb(m, "U.y"), a.arena,
+                            fsz, a.slot, s));
+        CKI(launch_adj_slot(a.slot, 1, s));
+        m->rec_launches += 2;
+        int e = launch_stage_kernel(m, k, par, s);
+        if (e) return e;
+        if ((e = rec_diag_cached(m, s))) return e;
+        par = 1 - par;
+    }
+    CKI(launch_pushforward(m->sc, s));
+    m->rec_launches += 1;
+    return 0;
+}
+
 // yb += D'(w)^T db for the stage state of snapshot slot (*slot + soff)
 static int rec_adj_vjp(f2d_model_s* m, int soff, const double* db, cudaStream_t s)
 {
@@ -805,6 +873,8 @@ static int record_kind(f2d_model_s* m, int kind, int par, cudaStream_t s)
     case 5: return rec_step_snap(m, par, s);
     case 6: return rec_adj_step(m, s);
     case 7: return launch_stage_kernel(m, 1, par, s, true);
+    case 11: return rec_step_store(m, par, s);
+    case 12: return rec_step_snap_cached(m, par, s);
     case 8:
     case 9:
     case 10: return rec_one_stage(m, kind - 7, par, s);
@@ -814,7 +884,8 @@ static int record_kind(f2d_model_s* m, int kind, int par, cudaStream_t s)
 
 static bool flips(int kind)
 {
-    return kind == 1 || kind == 2 || kind == 5 || (kind >= 8 && kind <= 10);
+    return kind == 1 || kind == 2 || kind == 5 || (kind >= 8 && kind <= 10) || kind == 11 ||
+           kind == 12;
 }
 
 // capture kind (0 diag, 1 step, 2 run, 3 qg projection of the state,
@@ -1153,6 +1224,7 @@ int f2d_model_destroy(f2d_model m)
     drop_graphs(m);
     for (int w = 0; w < 2; ++w) bs_free(m->bs[w]);
     ns_free(m->ns);
+    if (m->adj.psic) cudaFree(m->adj.psic);
     for (void* p : m->allocs) cudaFree(p);
     if (m->own_stream && m->stream) cudaStreamDestroy(m->stream);
     if (m->s2) cudaStreamDestroy(m->s2);
@@ -1799,13 +1871,44 @@ int f2d_adjoint_forward(f2d_model m, const double* w0, double* wT, int nsteps, d
     m->cfl_dt = false;
     CK(cudaMemcpyAsync(&m->sc->dt, &m->dt_const, 8, cudaMemcpyHostToDevice, m->stream));
     m->dt_applied = true;
+    // the streamfunction cache (3 nsteps + 1 FP64 fields) when it fits in a
+    // third of the free device memory
+    {
+        const long long slots = 3ll * nsteps + 1;
+        size_t free_b = 0, total_b = 0;
+        CK(cudaMemGetInfo(&free_b, &total_b));
+        if (slots > a.psic_slots && (double)slots * fb64 <= free_b / 3.0) {
+            if (a.psic) {
+                cudaFree(a.psic);
+                a.psic = nullptr;
+                a.psic_slots = 0;
+            }
+            void* p = nullptr;
+            if (cudaMalloc(&p, (size_t)slots * fb64) == cudaSuccess) {
+                a.psic = (double*)p;
+                a.psic_slots = slots;
+            }
+            for (int kind : {11, 12})
+                for (auto& k : m->gx[kind])
+                    if (k) {
+                        cudaGraphExecDestroy(k);
+                        k = nullptr;
+                    }
+        }
+        if (!a.pslot && !(a.pslot = (int*)dalloc(m, 256))) return fail(2, "out of device memory");
+        a.use_psic = a.psic && a.psic_slots >= slots;
+    }
     if ((e = adj_put(m, fb(m, "omega", m->cur), w0))) return e;
     if ((e = run_graph(m, 0))) return e;
+    if (a.use_psic) {
+        CK(cudaMemsetAsync(a.pslot, 0, sizeof(int), m->stream));
+        if ((e = rec_psi_store(m, m->stream))) return e;
+    }
     for (int n = 0; n < nsteps; ++n) {
         if (n % every == 0)
             CK(cudaMemcpyAsync(a.ckpt[n / every], fb(m, "omega", m->cur), fbs,
                                cudaMemcpyDeviceToDevice, m->stream));
-        if ((e = run_graph(m, 1))) return e;
+        if ((e = run_graph(m, a.use_psic ? 11 : 1))) return e;
     }
     if ((e = adj_take(m, fb(m, "omega", m->cur), wT))) return e;
     (void)g;
@@ -1834,10 +1937,18 @@ int f2d_adjoint_backward(f2d_model m, const double* lamT, double* lam0)
         if (n <= 0) continue;
         CK(cudaMemcpyAsync(fb(m, "omega", m->cur), a.ckpt[sgm], fbs, cudaMemcpyDeviceToDevice,
                            m->stream));
-        if ((e = run_graph(m, 0))) return e;
+        if (a.use_psic) {
+            // the diagnostics of the checkpoint from the cached streamfunction
+            // (slot 3 n0), then the recomputed stages from slots 3 n0 + 1 ..
+            const int p0 = 3 * n0;
+            CK(cudaMemcpyAsync(a.pslot, &p0, sizeof(int), cudaMemcpyHostToDevice, m->stream));
+            if ((e = rec_diag_cached(m, m->stream))) return e;
+        } else if ((e = run_graph(m, 0))) {
+            return e;
+        }
         CK(cudaMemsetAsync(a.slot, 0, sizeof(int), m->stream));
         for (int k = 0; k < n; ++k)
-            if ((e = run_graph(m, 5))) return e;
+            if ((e = run_graph(m, a.use_psic ? 12 : 5))) return e;
         for (int k = 0; k < n; ++k)
             if ((e = run_graph(m, 6))) return e;
         a.dt_graph = a.dt;
