@@ -1030,8 +1030,8 @@ int bs_autotune(BatchSolver& s, cudaStream_t st, cudaStream_t st2, void* x, cons
     cudaEventCreate(&ea);
     cudaEventCreate(&eb);
     const bool eager = bs_eager();
-    const double tin[3] = {1e-6, 1e-5, 1e-4};
-    const int ntin = s.mode == 1 ? 3 : 1;
+    const double tin[5] = {1e-8, 1e-7, 1e-6, 1e-5, 1e-4};
+    const int ntin = s.mode == 1 ? 5 : 1;
     BSTune best{0, 0, 0.0, 1e300, 0};
     int err = 0;
     for (int th : {32, 64}) {

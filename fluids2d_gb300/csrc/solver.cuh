@@ -86,7 +86,7 @@ int bs_build(BatchSolver& s, const std::vector<BSMemberDesc>& members,
 void bs_free(BatchSolver& s);
 
 // Autotuner of the multigrid schedule: tile rows (32, 64) x sweeps per leg
-// (1, 2) x, in the FP32 refinement form, inner tolerance (1e-6, 1e-5, 1e-4).
+// (1, 2) x, in the FP32 refinement form, inner tolerance (1e-8 .. 1e-4).
 // Each candidate's solve is captured as a graph and timed over `reps` solves
 // of the current right-hand side b from the warm start 0.999 x* (x* = the
 // current solution in x, FP64, xbytes); candidates that stop short of the

@@ -210,7 +210,7 @@ int f2d_sync(f2d_model m);
 int f2d_time_stage(f2d_model m, int stage, int reps, int flush_l2,
                    double *avg_ms);
 /* Autotuner of the multigrid schedule (tile rows 32/64, sweeps per leg 1/2,
- * and in the FP32 form the inner tolerance 1e-6/1e-5/1e-4): each candidate's
+ * and in the FP32 form the inner tolerance 1e-8 .. 1e-4): each candidate's
  * solve of the current state's right-hand side is captured as a graph and
  * timed over `reps` solves from the warm start 0.999 psi; the fastest that
  * reaches the tolerance is kept (the step graphs are re-captured). The state

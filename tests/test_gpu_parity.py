@@ -693,7 +693,7 @@ def test_autotune_ensemble_keeps_results():
     e2 = _ensemble(members, "fp32")
     cfg = e2.autotune(reps=1)
     assert cfg["tile_rows"] in (32, 64) and cfg["sweeps"] in (1, 2)
-    assert cfg["tol_in"] in (1e-6, 1e-5, 1e-4) and cfg["ms_per_solve"] > 0
+    assert cfg["tol_in"] in (1e-8, 1e-7, 1e-6, 1e-5, 1e-4) and cfg["ms_per_solve"] > 0
     e2.run(3)
     e2.sync()
     for b in range(len(members)):
