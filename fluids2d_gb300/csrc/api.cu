@@ -331,7 +331,18 @@ static int rec_solve(f2d_model_s* m, int which, const void* b, void* x, cudaStre
     return 0;
 }
 
-static int rec_diag(f2d_model_s* m, int par, cudaStream_t s)
+// the warm start of the solve of RK3 stage warm+1 (warm < 0: the previous
+// solution as it is)
+static int rec_warm(f2d_model_s* m, int warm, cudaStream_t s)
+{
+    if (warm < 0) return 0;
+    CKI(launch_psi_warm(warm, (double*)fb(m, "psi"), (double*)fb(m, "psi.s0"),
+                        (double*)fb(m, "psi.m1"), (long long)m->g.P * m->g.NY, m->sc, s));
+    m->rec_launches += 1;
+    return 0;
+}
+
+static int rec_diag(f2d_model_s* m, int par, cudaStream_t s, int warm = -1)
 {
     const Geom& g = m->g;
     switch (m->p.model) {
@@ -339,7 +350,9 @@ static int rec_diag(f2d_model_s* m, int par, cudaStream_t s)
         CKI(launch_c2v(m->prec, 0, fb(m, "omega", par), fb(m, "vomega"), m->d_code, nullptr, g,
                        s));
         m->rec_launches += 1;
-        int e = rec_solve(m, 0, fb(m, "vomega"), fb(m, "psi"), s);
+        int e = rec_warm(m, warm, s);
+        if (e) return e;
+        e = rec_solve(m, 0, fb(m, "vomega"), fb(m, "psi"), s);
         if (e) return e;
         CKI(launch_perpgrad(0, m->prec, fb(m, "psi"), fb(m, "U.x"), fb(m, "U.y"), m->d_code,
                             m->rdy2, m->rdx2, 1, g, m->sc, m->partials, s));
@@ -350,7 +363,9 @@ static int rec_diag(f2d_model_s* m, int par, cudaStream_t s)
         const void* fv = m->p.beta != 0 ? m->d_fv : nullptr;
         CKI(launch_c2v(m->prec, 0, fb(m, "pv", par), fb(m, "work"), m->d_code, fv, g, s));
         m->rec_launches += 1;
-        int e = rec_solve(m, 1, fb(m, "work"), fb(m, "psi"), s);
+        int e = rec_warm(m, warm, s);
+        if (e) return e;
+        e = rec_solve(m, 1, fb(m, "work"), fb(m, "psi"), s);
         if (e) return e;
         CKI(launch_perpgrad(0, m->prec, fb(m, "psi"), fb(m, "U.x"), fb(m, "U.y"), m->d_code,
                             m->rdy2, m->rdx2, 0, g, m->sc, m->partials, s));
@@ -689,12 +704,15 @@ static int rec_qg_projection(f2d_model_s* m, int par, cudaStream_t s)
     return 0;
 }
 
-// one RK3 stage from parity `par` to 1-par, then the diagnostics
+// one RK3 stage from parity `par` to 1-par, then the diagnostics (the
+// SSP-RK3 stages of eulerpsi and qg with the extrapolated warm start)
 static int rec_stage(f2d_model_s* m, int k, int par, cudaStream_t s)
 {
     int e = launch_stage_kernel(m, k, par, s);
     if (e) return e;
-    return rec_diag(m, 1 - par, s);
+    const bool warm = m->p.integrator == F2D_INTEG_RK3 &&
+                      (m->p.model == F2D_MODEL_EULERPSI || m->p.model == F2D_MODEL_QG);
+    return rec_diag(m, 1 - par, s, warm ? k - 1 : -1);
 }
 
 static int nstages(const f2d_model_s* m)
@@ -1166,6 +1184,11 @@ int f2d_model_create(const f2d_params* p, const int8_t* msk, f2d_model* out)
     for (auto& f : fl)
         if ((e = add_field(m, f.first, f.second, is64(f.first) ? 8 : (int)m->es)))
             return bail(e);
+    // the streamfunction at the start of this and of the previous step (the
+    // warm start of the stage solves, rec_warm)
+    if (p->model == F2D_MODEL_EULERPSI || p->model == F2D_MODEL_QG)
+        for (const char* f : {"psi.s0", "psi.m1"})
+            if ((e = add_field(m, f, false, 8))) return bail(e);
     // qgrsw keeps the third stage's (or LFRA's) tendency too: it is
     // projected between the tendency kernel and the update
     for (const char* f : prog) m->prog.push_back(f);
@@ -1383,7 +1406,12 @@ int f2d_field_names(f2d_model m, char* buf, size_t len)
     if (!m || !buf || !len) return fail(1, "null argument");
     std::string s;
     for (auto& kv : m->fields) {
-        if (kv.first.rfind("ds", 0) == 0) continue;
+        // the state's fields (not the integrator's scratch, the warm-start
+        // history, the rhs and forcing fields)
+        const std::string& n = kv.first;
+        if (n.rfind("ds", 0) == 0 || n.rfind("psi.", 0) == 0 || n.rfind("rhs.", 0) == 0 ||
+            n.rfind("frc.", 0) == 0)
+            continue;
         if (!s.empty()) s += ",";
         s += kv.first;
     }

@@ -69,6 +69,7 @@ __device__ __forceinline__ T* at(void* base, long long off)
 // ---- stage and diagnostics --------------------------------------------------
 struct EnsArenas {
     void *q[2], *ds1, *ds2, *Ux, *Uy, *rhs, *psi, *fv;
+    double *psi_s0, *psi_m1;  // psi at the start of this / the previous step
     const uint32_t* code;
 };
 
@@ -294,7 +295,10 @@ static int ens_record_solve(f2d_ensemble_s* e, cudaStream_t s)
     return 0;
 }
 
-static int ens_record_diag(f2d_ensemble_s* e, int par, cudaStream_t s)
+// warm: the warm start of the solve of RK3 stage warm+1 (launch_psi_warm,
+// all members at once: they step in lockstep, so member 0's step count is
+// everyone's); warm < 0: the previous solution as it is
+static int ens_record_diag(f2d_ensemble_s* e, int par, cudaStream_t s, int warm = -1)
 {
     const dim3 blk(32, 8);
     const int use_fv = e->p.model == F2D_MODEL_QG && e->p.beta != 0;
@@ -303,6 +307,12 @@ static int ens_record_diag(f2d_ensemble_s* e, int par, cudaStream_t s)
     else
         k_ens_c2v<float><<<e->ncell, blk, 0, s>>>(e->cell_tiles, e->dmem, e->ar, par, use_fv);
     e->rec += 1;
+    if (warm >= 0) {
+        const int rw = launch_psi_warm(warm, (double*)e->ar.psi, e->ar.psi_s0, e->ar.psi_m1,
+                                       (long long)e->total, e->scs, s);
+        if (rw) return f2d_internal_fail(rw, "ensemble warm-start launch failed");
+        e->rec += 1;
+    }
     int r = ens_record_solve(e, s);
     if (r) return r;
     const int fillU = e->p.model == F2D_MODEL_EULERPSI;
@@ -344,7 +354,7 @@ static int ens_record_step(f2d_ensemble_s* e, int par, cudaStream_t s)
 #undef ENS_FF
         e->rec += 1;
         par = 1 - par;
-        int r = ens_record_diag(e, par, s);
+        int r = ens_record_diag(e, par, s, e->p.integrator == F2D_INTEG_RK3 ? k - 1 : -1);
         if (r) return r;
     }
     k_ens_pushforward<<<(e->n + 127) / 128, 128, 0, s>>>(e->scs, e->n);
@@ -480,6 +490,8 @@ int f2d_ensemble_create(const f2d_params* p, int count, const int* nxs, const in
     e->ar.Uy = A(es);
     e->ar.rhs = A(8);
     e->ar.psi = A(8);
+    e->ar.psi_s0 = (double*)A(8);
+    e->ar.psi_m1 = (double*)A(8);
     e->ar.fv = A(8);
     e->code = A(4);
     e->gmask = A(1);
@@ -499,7 +511,8 @@ int f2d_ensemble_create(const f2d_params* p, int count, const int* nxs, const in
     e->scs = (DevScalars*)ens_alloc(e, sizeof(DevScalars) * count);
     e->eg = (EnsGlobals*)ens_alloc(e, sizeof(EnsGlobals));
     for (void* q : {e->ar.q[0], e->ar.q[1], e->ar.ds1, e->ar.ds2, e->ar.Ux, e->ar.Uy,
-                    e->ar.rhs, e->ar.psi, e->ar.fv, e->code, e->gmask, v.r64, v.p, v.p2, v.q, v.z, v.za,
+                    e->ar.rhs, e->ar.psi, (void*)e->ar.psi_s0, (void*)e->ar.psi_m1,
+                    e->ar.fv, e->code, e->gmask, v.r64, v.p, v.p2, v.q, v.z, v.za,
                     v.rin, v.e, e->stage64, (void*)e->scs, (void*)e->eg})
         if (!q) return bail(f2d_internal_fail(2, "out of device memory for the ensemble"));
     e->ar.code = (const uint32_t*)e->code;

@@ -53,6 +53,9 @@ int launch_maxabs2(int prec, const void* Ux, const void* Uy, const Geom& g,
                    DevScalars* sc, double* partials, cudaStream_t s);
 int launch_fill_periodic(int prec, void* a, const Geom& g, cudaStream_t s);
 int launch_set_dt(DevScalars* sc, cudaStream_t s);
+// warm start of the Poisson solve of SSP-RK3 stage mode+1 (stage.cu)
+int launch_psi_warm(int mode, double* psi, double* s0, double* m1, long long n,
+                    const DevScalars* sc, cudaStream_t s);
 // the failure-detection test switch of the stage kernels' TMA waits, one per
 // translation unit (stage.cu, ensemble.cu)
 int tma_wait_test_set_stage(int enabled, unsigned long long limit_ns);
