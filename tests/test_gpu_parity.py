@@ -532,11 +532,13 @@ def test_poisson_maxit_reports_status():
 # Stencils, RK3 state and the multigrid cycle in FP32; the Poisson solution
 # refined to FP64 accuracy by the FP64 CG residual recurrence. The solve
 # itself must match SuperLU to the FP64 tolerance; model states match the
-# FP64 oracle within FP32 rounding accumulated over 5 steps: 2e-5 relative
-# L2 for eulerpsi and qg; 1e-4 for rsw, whose velocity is driven by the
-# gradient of p = g h / area ~ 1 with O(1e-3) anomalies, so FP32 rounding of
-# p (6e-8) is amplified by the cancellation in grad p.
-FP32_STATE_TOL = {"eulerpsi": 2e-5, "qg": 2e-5, "rsw": 1e-4, "euler": 1e-4,
+# FP64 oracle within FP32 rounding accumulated over 5 steps: 1e-6 relative
+# L2 for eulerpsi and qg (the target of the FP32 form); 1e-4 for rsw, euler
+# and boussinesq, whose velocity is driven by the gradient of p = g h / area
+# ~ 1 (rsw) or by a pressure from an FP32 divergence, with O(1e-3) anomalies,
+# so the FP32 rounding of p (6e-8) is amplified ~1e3 by the cancellation in
+# grad p.
+FP32_STATE_TOL = {"eulerpsi": 1e-6, "qg": 1e-6, "rsw": 1e-4, "euler": 1e-4,
                   "boussinesq": 1e-4}
 
 
