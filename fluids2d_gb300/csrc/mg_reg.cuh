@@ -284,7 +284,9 @@ k_mg_down(const int4* __restrict__ tiles, const BSInfo* __restrict__ info,
 // level and at non-fluid nodes, wrapped when x-periodic (an even fine period
 // makes the wrapped fine node's coarse neighbours the wrapped coarse ones).
 // On level 0 (RZ) the block also forms its part of <r, z> (r = b, z = x) and
-// the member's last block sets rz and beta.
+// the member's last block sets rz and beta; partials, gpart and gtick are
+// then the arrays of the segmented reduction over this launch's tile table
+// (the member's segment: mn0, mnn, mg0 of its BSInfo).
 template <typename S, int NU, bool RZ>
 __global__ void __launch_bounds__(256)
 k_mg_up(const int4* __restrict__ tiles, const BSInfo* __restrict__ info,
@@ -351,8 +353,14 @@ k_mg_up(const int4* __restrict__ tiles, const BSInfo* __restrict__ info,
     }
     const S acc = mr_store<S, RZ>(R, F, lx<S>(F), J0, I0);
     if (RZ) {
+        // the member's segment of this launch's tile table (level 0 of the
+        // level kernels, not the Krylov kernels' table)
+        BSInfo mi = in;
+        mi.n0 = in.mn0;
+        mi.nn = in.mnn;
+        mi.g0 = in.mg0;
         double w1[1];
-        if (member_dot<S>(acc, w1, partials, gpart, gtick, in, &sc.counter[2]))
+        if (member_dot<S>(acc, w1, partials, gpart, gtick, mi, &sc.counter[2]))
             set_rz(sc, ir, w1[0]);
     }
 }

@@ -605,8 +605,8 @@ static int vcycle_nu(BatchSolver& s, cudaStream_t st, int ir)
     }
     if (s.maxl > 0) {
         k_mg_up<S, NU, true><<<s.nmtiles[0], blk, 0, st>>>(s.mtiles[0], s.dinfo, s.dlevs, 0,
-                                                          s.scs, ir, s.partials, s.gpart,
-                                                          s.gtick);
+                                                          s.scs, ir, s.mpartials, s.mgpart,
+                                                          s.mgtick);
         cnt += 1;
     }
     return cnt;
@@ -900,14 +900,26 @@ int bs_build(BatchSolver& s, const std::vector<BSMemberDesc>& members, const uin
                 if (hm[(size_t)J * L.nxn + I]) return true;
         return false;
     };
+    // Level 0 also carries the members' segments of the level-0 up leg's
+    // <r, z> reduction (mn0, mnn, mg0): every member that reaches below
+    // level 0 keeps at least one tile there.
     std::vector<std::vector<int4>> mt(std::max(1, s.maxl));
+    int mgroups = 0;
     for (int l = 0; l < s.maxl; ++l)
         for (int b = 0; b < s.n; ++b) {
             if (info[b].ltail <= l) continue;
             const MGLevel& L = levs[(size_t)b * BS_LMAX + l];
+            const int first = (int)mt[l].size();
             for (int J0 = 0; J0 < L.nyn; J0 += MR_TH)
                 for (int I0 = 0; I0 < L.nxn; I0 += MR_TW)
                     if (has_fluid_m(b, l, J0, I0)) mt[l].push_back(make_int4(b, I0, J0, 0));
+            if (l == 0) {
+                if ((int)mt[0].size() == first) mt[0].push_back(make_int4(b, 0, 0, 0));
+                info[b].mn0 = first;
+                info[b].mnn = (int)mt[0].size() - first;
+                info[b].mg0 = mgroups;
+                mgroups += (info[b].mnn + RED_GROUP - 1) / RED_GROUP;
+            }
         }
     auto dal = [&](size_t bytes) -> void* {
         void* p = nullptr;
@@ -944,6 +956,12 @@ int bs_build(BatchSolver& s, const std::vector<BSMemberDesc>& members, const uin
     s.dinfo = (BSInfo*)dal(info.size() * sizeof(BSInfo));
     s.eg = (BSGlobals*)dal(sizeof(BSGlobals));
     s.partials = (double*)dal((rt.size() * 2 + 64) * sizeof(double));
+    s.mpartials = (double*)dal((mt[0].size() * 2 + 64) * sizeof(double));
+    s.mgpart = (double*)dal(((size_t)mgroups * 2 + 64) * sizeof(double));
+    s.mgtick = (unsigned int*)dal(((size_t)mgroups + 64) * sizeof(unsigned int));
+    if (!s.mpartials || !s.mgpart || !s.mgtick ||
+        cudaMemset(s.mgtick, 0, ((size_t)mgroups + 64) * sizeof(unsigned int)) != cudaSuccess)
+        return 2;
     s.gpart = (double*)dal(((size_t)ngroups * 2 + 64) * sizeof(double));
     s.gtick = (unsigned int*)dal(((size_t)ngroups + 64) * sizeof(unsigned int));
     if (!s.gpart || !s.gtick ||

@@ -15,7 +15,10 @@ struct BSInfo {
     int nl, ltail, ksweeps;  // levels, first tail level, coarsest sweeps
     int n0, nn;              // range of the member in the level-0 tile table
     int g0;                  // first reduction group of the member
-    int pad[2];
+    // the same for the level-0 table of the multigrid level kernels (the
+    // <r, z> reduction of the level-0 up leg); mnn = 0 when level 0 is in
+    // the member's tail
+    int mn0, mnn, mg0, pad;
 };
 
 struct BSGlobals {
@@ -62,6 +65,9 @@ struct BatchSolver {
     std::vector<int> ntiles;
     std::vector<int4*> mtiles; // tiles of the multigrid level kernels per level
     std::vector<int> nmtiles;
+    double* mpartials = nullptr;  // the segmented <r, z> reduction over mtiles[0]
+    double* mgpart = nullptr;
+    unsigned int* mgtick = nullptr;
     int4* rtiles = nullptr;    // level-0 tiles of the Krylov kernels
     int nrtiles = 0;
     double* gpart = nullptr;   // group sums of the two-level reductions
