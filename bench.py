@@ -101,10 +101,11 @@ ENSEMBLE_DESC = ("ensemble of 256 eulerpsi closed basins, sizes uniform in "
 
 
 def solver_roofline(timer, handle, workload, peak, peak_src):
-    """Roofline of the solver's dominant kernel (the level-0 down kernel of the
-    V-cycle: b and mask read, the pre-smoothed x written, the restricted
-    right-hand side written at a quarter of the nodes = (2.25 es + 1) bytes
-    per level-0 node), timed alone with CUDA events, L2 flushed."""
+    """Roofline of the solver's largest kernel (k_mg_down on level 0, the
+    V-cycle's down leg: b and mask read, the pre-smoothed x written, the
+    restricted right-hand side written at a quarter of the nodes =
+    (2.25 es + 1) bytes per level-0 node), timed alone with CUDA events, L2
+    flushed."""
     import ctypes
     avg = ctypes.c_double()
     nodes = ctypes.c_int64()
@@ -114,14 +115,13 @@ def solver_roofline(timer, handle, workload, peak, peak_src):
         return None
     alg = nodes.value * (2.25 * es.value + 1)
     achieved = alg / (avg.value * 1e-3) / 1e9
-    kname = "k_bs_down"
+    kname = "k_mg_down"
     return {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
             "frac": achieved / peak,
             "traffic": read_profile_traffic(f"{kname}_{workload}"),
             "kernel": kname + " (level 0)", "kernel_ms": avg.value,
             "alg_bytes_per_launch": alg, "peak_source": peak_src,
-            "binding_roof_ncu": read_profile_value(f"{kname}_{workload}",
-                                                   "binding_roof") and "issue"}
+            "binding_roof_ncu": read_profile_text(f"{kname}_{workload}", "binding")}
 
 
 def max_over_ranks(x, world):
@@ -322,6 +322,17 @@ def read_profile_value(kernel, key):
                 return float(line.split(":", 1)[1].split()[0])
             except ValueError:
                 return None
+    return None
+
+
+def read_profile_text(kernel, key):
+    """The text after `key:` in the committed ncu summary of `kernel`."""
+    path = os.path.join(ROOT, "profiles", f"{kernel}.md")
+    if not os.path.exists(path):
+        return None
+    for line in open(path):
+        if line.startswith(key + ":"):
+            return line.split(":", 1)[1].strip()
     return None
 
 
