@@ -295,43 +295,13 @@ __device__ __forceinline__ void fluxform_tile(
         }
         sfy[r][c] = f;
     };
-    // Tiles whose every face has the full order (level 3; no mask within
-    // three cells) take the 6-point formula without per-face level tests.
-    // Cells outside the array carry code 0 and so keep a tile off this path.
-    bool mine3 = true;
 #pragma unroll
-    for (int q = 0; q < FRT; ++q)
-        mine3 = mine3 && lev(cd[q], SH_OCX) == 3 && lev(cd[q], SH_OCY) == 3;
-    if (ex) mine3 = mine3 && lev(ce, ex == 1 ? SH_OCX : SH_OCY) == 3;
-    if (__syncthreads_and(mine3 ? 1 : 0)) {
-#pragma unroll
-        for (int q = 0; q < FRT; ++q) {
-            const int r = ty + 8 * q;
-            const T* w = &sq[r + OY][tx + OX - 3];
-            sfx[r][tx] = flux6<M, T>(ux[q], w[0], w[1], w[2], w[3], w[4], w[5]) * ux[q];
-            const int cc = tx + OX;
-            sfy[r][tx] = flux6<M, T>(uy[q], sq[r][cc], sq[r + 1][cc], sq[r + 2][cc],
-                                     sq[r + 3][cc], sq[r + 4][cc], sq[r + 5][cc]) *
-                         uy[q];
-        }
-        if (ex == 1) {
-            const T* w = &sq[er + OY][ec + OX - 3];
-            sfx[er][ec] = flux6<M, T>(ue, w[0], w[1], w[2], w[3], w[4], w[5]) * ue;
-        } else if (ex == 2) {
-            const int cc = ec + OX;
-            sfy[er][ec] = flux6<M, T>(ue, sq[er][cc], sq[er + 1][cc], sq[er + 2][cc],
-                                      sq[er + 3][cc], sq[er + 4][cc], sq[er + 5][cc]) *
-                          ue;
-        }
-    } else {
-#pragma unroll
-        for (int q = 0; q < FRT; ++q) {
-            xflux(ty + 8 * q, tx, cd[q], ux[q]);
-            yflux(ty + 8 * q, tx, cd[q], uy[q]);
-        }
-        if (ex == 1) xflux(er, ec, ce, ue);
-        else if (ex == 2) yflux(er, ec, ce, ue);
+    for (int q = 0; q < FRT; ++q) {
+        xflux(ty + 8 * q, tx, cd[q], ux[q]);
+        yflux(ty + 8 * q, tx, cd[q], uy[q]);
     }
+    if (ex == 1) xflux(er, ec, ce, ue);
+    else if (ex == 2) yflux(er, ec, ce, ue);
     if (t == 0) rk3_coefs<T>(sk, dt, sm.rk, gamma);
     __syncthreads();
 
