@@ -100,12 +100,12 @@ ENSEMBLE_DESC = ("ensemble of 256 eulerpsi closed basins, sizes uniform in "
                  "vortices, WENO5, SSP-RK3, per-member CFL 0.8")
 
 
-def solver_roofline(timer, handle, workload, peak, peak_src):
-    """Roofline of the solver's largest kernel (k_mg_down on level 0, the
-    V-cycle's down leg: b and mask read, the pre-smoothed x written, the
-    restricted right-hand side written at a quarter of the nodes =
-    (2.25 es + 1) bytes per level-0 node), timed alone with CUDA events, L2
-    flushed."""
+def solver_roofline(timer, pipelined, handle, workload, peak, peak_src):
+    """Roofline of the solver's largest kernel (the level-0 down leg of the
+    V-cycle, k_mgp_down when the solver runs the pipelined FP32 kernels, else
+    k_mg_down: b and mask read, the pre-smoothed x written, the restricted
+    right-hand side written at a quarter of the nodes = (2.25 es + 1) bytes
+    per level-0 node), timed alone with CUDA events, L2 flushed."""
     import ctypes
     avg = ctypes.c_double()
     nodes = ctypes.c_int64()
@@ -113,9 +113,12 @@ def solver_roofline(timer, handle, workload, peak, peak_src):
     rc = timer(handle, 10, 1, ctypes.byref(avg), ctypes.byref(nodes), ctypes.byref(es))
     if rc != 0:
         return None
+    pipe = ctypes.c_int()
+    if pipelined(handle, ctypes.byref(pipe)) != 0:
+        return None
     alg = nodes.value * (2.25 * es.value + 1)
     achieved = alg / (avg.value * 1e-3) / 1e9
-    kname = "k_mg_down"
+    kname = "k_mgp_down" if pipe.value else "k_mg_down"
     return {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
             "frac": achieved / peak,
             "traffic": read_profile_traffic(f"{kname}_{workload}"),
@@ -684,7 +687,8 @@ def run_gpu_ensemble(args, rank, world):
         "e2e": {"value": e2e, "unit": "cell-updates/s",
                 "h2d_bytes_per_step": io, "d2h_bytes_per_step": io,
                 "steps": e2e_steps},
-        "roofline": solver_roofline(L.f2d_ensemble_time_solver, h, args.workload,
+        "roofline": solver_roofline(L.f2d_ensemble_time_solver,
+                                    L.f2d_ensemble_solver_pipelined, h, args.workload,
                                     peak, peak_src),
         "roofline_stage": {"bound": "hbm", "achieved": achieved, "peak": peak,
                            "unit": "GB/s", "frac": achieved / peak,
@@ -963,7 +967,8 @@ def run_gpu(args, rank, world):
     if model != "rsw":
         # the Poisson solve dominates the step: its largest kernel is the
         # roofline kernel, the fused stage is reported beside it
-        sr = solver_roofline(L.f2d_time_solver, h, args.workload, peak, peak_src)
+        sr = solver_roofline(L.f2d_time_solver, L.f2d_solver_pipelined, h, args.workload,
+                             peak, peak_src)
         if sr is not None:
             line["roofline_stage"] = line["roofline"]
             line["roofline"] = sr

@@ -120,6 +120,8 @@ _SIGS = {
                          ctypes.POINTER(c_i64), ctypes.POINTER(c_int)], c_int),
     "f2d_ensemble_time_solver": ([c_void_p, c_int, c_int, ctypes.POINTER(c_dbl),
                                   ctypes.POINTER(c_i64), ctypes.POINTER(c_int)], c_int),
+    "f2d_solver_pipelined": ([c_void_p, ctypes.POINTER(c_int)], c_int),
+    "f2d_ensemble_solver_pipelined": ([c_void_p, ctypes.POINTER(c_int)], c_int),
     "f2d_adjoint_forward": ([c_void_p, c_void_p, c_void_p, c_int, c_dbl, c_int], c_int),
     "f2d_adjoint_backward": ([c_void_p, c_void_p, c_void_p], c_int),
     "f2d_cfl_dt_noalloc": ([c_void_p, c_void_p, c_i64, c_i64, c_i64, c_dbl,

@@ -1650,6 +1650,7 @@ int f2d_sync(f2d_model m)
         CK(cudaMemcpy(&m->sc->status, &zero, sizeof(int), cudaMemcpyHostToDevice));
         std::string msg = "device status:";
         if (st & ST_TMA_TIMEOUT) msg += " TMA tile load timed out;";
+        if (st & ST_STAGE_ALIGN) msg += " TMA staging buffer misaligned;";
         if (st & ST_PCG_MAXIT) msg += " Poisson solve reached max iterations;";
         if (st & ST_NONFINITE) msg += " non-finite value (residual or time step);";
         return fail(100 + st, msg);
@@ -1807,6 +1808,17 @@ int f2d_time_solver(f2d_model m, int reps, int flush_l2, double* avg_ms, int64_t
     if (e) return fail(e, "solver kernel timing failed (no grid level?)");
     if (nodes) *nodes = n;
     if (elem_bytes) *elem_bytes = es;
+    return 0;
+}
+
+int f2d_solver_pipelined(f2d_model m, int* pipelined)
+{
+    if (!m || !pipelined) return fail(1, "null argument");
+    if (m->p.model == F2D_MODEL_RSW || projected(m->p.model))
+        return fail(1, "the model has no vertex Poisson solve");
+    const int which = m->p.model == F2D_MODEL_EULERPSI ? 0 : 1;
+    if (!m->bs_ready[which]) return fail(9, "the solver has not run yet");
+    *pipelined = m->bs[which].pipe ? 1 : 0;
     return 0;
 }
 

@@ -37,6 +37,7 @@ enum : int {
     ST_TMA_TIMEOUT = 1,    // a TMA tile load did not complete within 1 s
     ST_PCG_MAXIT = 2,      // the Poisson solve stopped at max iterations
     ST_NONFINITE = 4,      // a non-finite value reached a reduction
+    ST_STAGE_ALIGN = 8,    // a TMA staging buffer was not 128-byte aligned (nothing loaded)
 };
 
 // min(x, cap) with Python's min semantics (the reference's set_dt,

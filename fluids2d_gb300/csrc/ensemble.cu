@@ -826,6 +826,7 @@ int f2d_ensemble_sync(f2d_ensemble e)
         ECK(cudaMemcpy(&e->bs.eg->status, &zero, sizeof(int), cudaMemcpyHostToDevice));
         std::string msg = "ensemble device status:";
         if (h.status & ST_TMA_TIMEOUT) msg += " TMA tile load timed out;";
+        if (h.status & ST_STAGE_ALIGN) msg += " TMA staging buffer misaligned;";
         if (h.status & ST_PCG_MAXIT) msg += " a Poisson solve reached max iterations;";
         if (h.status & ST_NONFINITE) msg += " non-finite value (residual or time step);";
         return f2d_internal_fail(100 + h.status, msg.c_str());
@@ -901,6 +902,13 @@ int f2d_ensemble_time_solver(f2d_ensemble e, int reps, int flush_l2, double* avg
     if (r) return f2d_internal_fail(r, "solver kernel timing failed (no grid level?)");
     if (nodes) *nodes = n;
     if (elem_bytes) *elem_bytes = es;
+    return 0;
+}
+
+int f2d_ensemble_solver_pipelined(f2d_ensemble e, int* pipelined)
+{
+    if (!e || !pipelined) return f2d_internal_fail(1, "null argument");
+    *pipelined = e->bs.pipe ? 1 : 0;
     return 0;
 }
 

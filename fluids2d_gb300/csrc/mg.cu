@@ -97,12 +97,15 @@ int mg_build(MGHost& mg, int nyn0, int nxn0, long long pitch0, long long off0, i
         memset(&C, 0, sizeof(C));
         C.nyn = cyn;
         C.nxn = cxn;
-        C.pitch = (cxn + 31) / 32 * 32;
         // node (J, I) at element 1 + J*pitch + I: an odd offset, like level
         // 0's (node (J, I) of the model's array at (3+J)*P + 3+I, P even), so
         // that node pairs starting on odd columns are 8/16-byte aligned on
-        // every level (the paired loads of the level kernels)
+        // every level (the paired loads of the level kernels); the pitch
+        // holds the offset too, so every node row lies inside its own
+        // 32-aligned pitch row (the row the TMA loads of the pipelined level
+        // kernels see)
         C.off = 1;
+        C.pitch = (cxn + C.off + 31) / 32 * 32;
         C.per = per;
         C.cx = cx;
         C.cy = cy;

@@ -283,15 +283,12 @@ k_mg_down(const int4* __restrict__ tiles, const BSInfo* __restrict__ info,
 // interpolates from are staged in shared memory first: 0 outside the coarse
 // level and at non-fluid nodes, wrapped when x-periodic (an even fine period
 // makes the wrapped fine node's coarse neighbours the wrapped coarse ones).
-// On level 0 (RZ) the block also forms its part of <r, z> (r = b, z = x) and
-// the member's last block sets rz and beta; partials, gpart and gtick are
-// then the arrays of the segmented reduction over this launch's tile table
-// (the member's segment: mn0, mnn, mg0 of its BSInfo).
+// On level 0 (RZ) the block also forms its tile's part of <r, z> (r = b,
+// z = x) into tpart[tile] (k_bs_rz sums a member's tiles).
 template <typename S, int NU, bool RZ>
 __global__ void __launch_bounds__(256)
 k_mg_up(const int4* __restrict__ tiles, const BSInfo* __restrict__ info,
-        const MGLevel* __restrict__ levs, int l, DevScalars* scs, int ir, double* partials,
-        double* gpart, unsigned int* gtick)
+        const MGLevel* __restrict__ levs, int l, DevScalars* scs, int ir, double* tpart)
 {
     constexpr int CW = MR_W / 2 + 1, CWY = MR_WY / 2 + 1;
     __shared__ __align__(16) S xch[2][MR_NW][2][MR_W];
@@ -353,15 +350,8 @@ k_mg_up(const int4* __restrict__ tiles, const BSInfo* __restrict__ info,
     }
     const S acc = mr_store<S, RZ>(R, F, lx<S>(F), J0, I0);
     if (RZ) {
-        // the member's segment of this launch's tile table (level 0 of the
-        // level kernels, not the Krylov kernels' table)
-        BSInfo mi = in;
-        mi.n0 = in.mn0;
-        mi.nn = in.mnn;
-        mi.g0 = in.mg0;
-        double w1[1];
-        if (member_dot<S>(acc, w1, partials, gpart, gtick, mi, &sc.counter[2]))
-            set_rz(sc, ir, w1[0]);
+        const double tot = block_sum<S>(acc);
+        if (t == 0) tpart[blockIdx.x] = tot;
     }
 }
 

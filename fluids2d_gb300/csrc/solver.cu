@@ -18,6 +18,7 @@
 //    FP64) to reduce that residual by tol_in, and x += e in FP64. On GB300,
 //    where FP64 arithmetic is scarce, this confines FP64 to one residual per
 //    refinement round while the solution reaches FP64 accuracy.
+#include <cudaTypedefs.h>
 #include <algorithm>
 #include <cstdlib>
 #include <cstring>
@@ -135,6 +136,23 @@ __device__ __forceinline__ bool bs_skip(const DevScalars& sc, int ir)
     return sc.converged || (ir && sc.conv_in);
 }
 
+// Block total of per-thread values in thread 0 (FP32: warp sums in FP32,
+// combined in FP64; FP64: block_reduce), fixed order.
+template <typename V>
+__device__ __forceinline__ double block_sum(V acc)
+{
+    double w[1];
+    if constexpr (std::is_same<V, float>::value) {
+        const float a[1] = {acc};
+        block_total_f<1>(a, w);
+    } else {
+        __shared__ double sh[32];
+        w[0] = acc;
+        block_reduce<1, false>(w, sh);
+    }
+    return w[0];
+}
+
 // Completion of a kernel over all members, counted per member: exactly one
 // block of every member calls this with mine = true (the last block of its
 // segmented reduction, or the first tile of a member whose work is skipped),
@@ -161,9 +179,30 @@ __device__ __forceinline__ void set_rz(DevScalars& sc, int ir, double rz)
     sc.rz = rz;
 }
 
+// <r, z> of every member from the tile totals of the level-0 up leg
+// (tpart[mn0 .. mn0 + mnn), summed in a fixed order), then rz and beta. The
+// up leg writes one total per tile and no more, so its blocks never wait on
+// a fence or a ticket; members whose level 0 is in the tail (mnn = 0) get
+// theirs from k_bs_tail.
+__global__ void __launch_bounds__(256)
+k_bs_rz(const BSInfo* __restrict__ info, DevScalars* scs, const double* __restrict__ tpart,
+        int ir)
+{
+    const int b = blockIdx.x;
+    const BSInfo in = info[b];
+    DevScalars& sc = scs[b];
+    if (in.mnn == 0 || bs_skip(sc, ir)) return;
+    double acc[1] = {0.0};
+    final_sum<1, false>(acc, tpart, in.mn0, in.mnn, threadIdx.x, blockDim.x);
+    __shared__ double sh[32];
+    block_reduce<1, false>(acc, sh);
+    if (threadIdx.x == 0) set_rz(sc, ir, acc[0]);
+}
+
 // ---- multigrid level kernels (register-blocked; mg_reg.cuh) ----------------
 }  // namespace f2d
 #include "mg_reg.cuh"
+#include "mg_pipe.cuh"
 namespace f2d {
 
 // Coarse levels of every member in one block each (tail_vcycle). A member
@@ -585,9 +624,42 @@ static bool bs_eager()
 
 // one V-cycle for all members still iterating: a down kernel per grid level,
 // the tail, an up kernel per grid level (the level-0 one also forms <r, z>)
+// the same with the pipelined FP32 level kernels (persistent blocks)
+template <int NU>
+static int vcycle_pipe(BatchSolver& s, cudaStream_t st, int ir)
+{
+    const dim3 blk(32, MR_NW);
+    const CUtensorMap* maps = (const CUtensorMap*)s.mmaps;
+    int* status = &s.eg->status;
+    int cnt = 0;
+    for (int l = 0; l < s.maxl; ++l) {
+        const int n = s.nmtiles[l];
+        if (n == 0) continue;
+        k_mgp_down<NU><<<std::min(n, s.pipe_gdown), blk, sizeof(MPDown), st>>>(
+            s.mtiles[l], n, s.dlevs, maps, l, s.scs, ir, status);
+        cnt += 1;
+    }
+    k_bs_tail<float><<<s.n, 1024, s.tail_smem, st>>>(s.dinfo, s.dlevs, s.scs, ir, NU);
+    cnt += 1;
+    for (int l = s.maxl - 1; l >= 0; --l) {
+        const int n = s.nmtiles[l];
+        if (n == 0) continue;
+        if (l > 0)
+            k_mgp_up<NU, false><<<std::min(n, s.pipe_gup), blk, sizeof(MPUp), st>>>(
+                s.mtiles[l], n, s.dlevs, maps, l, s.scs, ir, nullptr, status);
+        else
+            k_mgp_up<NU, true><<<std::min(n, s.pipe_gup), blk, sizeof(MPUp), st>>>(
+                s.mtiles[0], n, s.dlevs, maps, 0, s.scs, ir, s.mpartials, status);
+        cnt += 1;
+    }
+    return cnt;
+}
+
 template <typename S, int NU, int TH>
 static int vcycle_nu(BatchSolver& s, cudaStream_t st, int ir)
 {
+    if constexpr (std::is_same<S, float>::value)
+        if (s.pipe) return vcycle_pipe<NU>(s, st, ir);
     const dim3 blk(32, MR_NW);
     int cnt = 0;
     for (int l = 0; l < s.maxl; ++l) {
@@ -599,14 +671,12 @@ static int vcycle_nu(BatchSolver& s, cudaStream_t st, int ir)
     cnt += 1;
     for (int l = s.maxl - 1; l >= 1; --l) {
         k_mg_up<S, NU, false><<<s.nmtiles[l], blk, 0, st>>>(s.mtiles[l], s.dinfo, s.dlevs, l,
-                                                           s.scs, ir, s.partials, s.gpart,
-                                                           s.gtick);
+                                                           s.scs, ir, nullptr);
         cnt += 1;
     }
     if (s.maxl > 0) {
         k_mg_up<S, NU, true><<<s.nmtiles[0], blk, 0, st>>>(s.mtiles[0], s.dinfo, s.dlevs, 0,
-                                                          s.scs, ir, s.mpartials, s.mgpart,
-                                                          s.mgtick);
+                                                          s.scs, ir, s.mpartials);
         cnt += 1;
     }
     return cnt;
@@ -627,6 +697,10 @@ static int cg_body(BatchSolver& s, cudaStream_t st, cudaGraphConditionalHandle c
     V* r = (V*)(ir ? s.v.rin : s.v.r64);
     V* x = (V*)(ir ? s.v.e : s.v.x64);
     int cnt = vcycle<S, TH>(s, st, ir);
+    if (s.maxl > 0) {
+        k_bs_rz<<<s.n, 256, 0, st>>>(s.dinfo, s.scs, s.mpartials, ir);
+        cnt += 1;
+    }
     k_bs_pq<S, V, TH><<<nt, blk, 0, st>>>(s.rtiles, s.dinfo, s.dlevs, (const S*)s.v.z,
                                           (V*)s.v.p, (V*)s.v.p2, (V*)s.v.q, s.scs, s.partials,
                                           s.gpart, s.gtick, ir);
@@ -772,6 +846,14 @@ __global__ void k_bs_activate(DevScalars* scs, int n)
 template <typename S, int NU>
 static void launch_down0(BatchSolver& s, cudaStream_t st, int ir)
 {
+    if constexpr (std::is_same<S, float>::value)
+        if (s.pipe) {
+            k_mgp_down<NU><<<std::min(s.nmtiles[0], s.pipe_gdown), dim3(32, MR_NW),
+                             sizeof(MPDown), st>>>(s.mtiles[0], s.nmtiles[0], s.dlevs,
+                                                   (const CUtensorMap*)s.mmaps, 0, s.scs, ir,
+                                                   &s.eg->status);
+            return;
+        }
     k_mg_down<S, NU><<<s.nmtiles[0], dim3(32, MR_NW), 0, st>>>(s.mtiles[0], s.dinfo, s.dlevs, 0,
                                                               s.scs, ir);
 }
@@ -819,6 +901,143 @@ int bs_record(BatchSolver& s, cudaStream_t st, cudaStream_t st2, int* launches)
 {
     return s.th == 64 ? bs_record_t<64>(s, st, st2, launches)
                       : bs_record_t<32>(s, st, st2, launches);
+}
+
+// ---- pipelined FP32 level kernels (mg_pipe.cuh): layout checks, TMA maps ----
+static PFN_cuTensorMapEncodeTiled_v12000 bs_encode_fn()
+{
+    static PFN_cuTensorMapEncodeTiled_v12000 fn = nullptr;
+    if (!fn) {
+        void* ptr = nullptr;
+        cudaDriverEntryPointQueryResult q;
+        if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &ptr, 12000,
+                                             cudaEnableDefault, &q) == cudaSuccess &&
+            q == cudaDriverEntryPointSuccess)
+            fn = (PFN_cuTensorMapEncodeTiled_v12000)ptr;
+    }
+    return fn;
+}
+
+// What the pipelined kernels assume of the layout: every level's rows start
+// 16 elements aligned (c0 = off mod 16 the column of node 0, node columns
+// inside the pitch, pitch a multiple of 16, coarse levels at off = 1, 16-byte
+// aligned arrays); on a closed level 0 the mask bytes of a node row outside
+// its node columns are 0 (the TMA row spans the whole pitch); the coarse
+// fluid flags are the fine centre nodes' (the restriction takes them from
+// there).
+static bool bs_pipe_layout_ok(BatchSolver& s, const std::vector<MGLevel>& levs,
+                              const std::vector<BSInfo>& info)
+{
+    for (int b = 0; b < s.n; ++b) {
+        const int nl = info[b].nl;
+        for (int l = 0; l < nl; ++l) {
+            const MGLevel& L = levs[(size_t)b * BS_LMAX + l];
+            const long long c0 = L.off & 15;
+            if (L.pitch % 16 || c0 + L.nxn > L.pitch || (l > 0 && L.off != 1)) return false;
+            for (const void* p : {(const void*)L.x, (const void*)L.xa, (const void*)L.b,
+                                  (const void*)L.m})
+                if ((uintptr_t)p % 16) return false;
+        }
+        BSMemberDesc& d = s.descs[b];
+        const MGLevel& L0 = levs[(size_t)b * BS_LMAX];
+        const long long c0 = L0.off & 15;
+        if (d.hwin) {
+            bool ok = d.hoff0 >= c0 && (d.hoff0 & 15) == c0;
+            for (int J = 0; ok && !L0.per && J < L0.nyn; ++J) {
+                const uint8_t* row = d.hmask + (d.hoff0 - c0) + (long long)J * L0.pitch;
+                for (long long c = 0; c < L0.pitch; ++c)
+                    if ((c < c0 || c >= c0 + L0.nxn) && row[c]) {
+                        ok = false;
+                        break;
+                    }
+            }
+            d.win_ok = ok ? 1 : 0;
+        }
+        if (!d.win_ok) return false;
+        for (int l = 0; l < info[b].ltail && l + 1 < nl; ++l) {
+            const MGLevel& F = levs[(size_t)b * BS_LMAX + l];
+            const MGLevel& C = levs[(size_t)b * BS_LMAX + l + 1];
+            const std::vector<uint8_t>& fm = s.mg[b].hmask[l];
+            const std::vector<uint8_t>& cm = s.mg[b].hmask[l + 1];
+            for (int J = 0; J < C.nyn; ++J)
+                for (int I = 0; I < C.nxn; ++I) {
+                    const uint8_t f = 2 * J < F.nyn && 2 * I < F.nxn
+                                          ? fm[(size_t)(2 * J) * F.nxn + 2 * I] : 0;
+                    if ((cm[(size_t)J * C.nxn + I] != 0) != (f != 0)) return false;
+                }
+        }
+    }
+    return true;
+}
+
+template <typename DAL>
+static int bs_pipe_setup(BatchSolver& s, const std::vector<MGLevel>& levs,
+                         const std::vector<BSInfo>& info, DAL& dal)
+{
+    s.pipe = false;
+    s.mmaps = nullptr;
+    if (s.mode != 1 || s.maxl < 1) return 0;
+    auto enc = bs_encode_fn();
+    if (!enc || !bs_pipe_layout_ok(s, levs, info)) return 0;
+    // grid sizes: resident blocks per SM x SMs (persistent blocks)
+    static int gdown = 0, gup = 0;
+    if (!gdown) {
+        int dev = 0, nsm = 0;
+        cudaGetDevice(&dev);
+        cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
+        int lo_d = 1 << 30, lo_u = 1 << 30;
+        auto occ = [&](const void* fn, size_t smem, int& lo) {
+            cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+            int nb = 0;
+            cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, fn, 32 * MR_NW, smem);
+            lo = std::min(lo, nb);
+        };
+        occ((const void*)k_mgp_down<1>, sizeof(MPDown), lo_d);
+        occ((const void*)k_mgp_down<2>, sizeof(MPDown), lo_d);
+        occ((const void*)k_mgp_up<1, false>, sizeof(MPUp), lo_u);
+        occ((const void*)k_mgp_up<1, true>, sizeof(MPUp), lo_u);
+        occ((const void*)k_mgp_up<2, false>, sizeof(MPUp), lo_u);
+        occ((const void*)k_mgp_up<2, true>, sizeof(MPUp), lo_u);
+        if (cudaGetLastError() != cudaSuccess || nsm < 1 || lo_d < 1 || lo_u < 1) return 0;
+        gdown = lo_d * nsm;
+        gup = lo_u * nsm;
+    }
+    const size_t nmap = (size_t)s.n * BS_LMAX * MP_NMAP;
+    std::vector<CUtensorMap> maps(nmap);
+    memset(maps.data(), 0, nmap * sizeof(CUtensorMap));
+    for (int b = 0; b < s.n; ++b)
+        for (int l = 0; l < info[b].nl; ++l) {
+            const MGLevel& L = levs[(size_t)b * BS_LMAX + l];
+            const long long base = L.off - (L.off & 15);
+            CUtensorMap* mp = &maps[((size_t)b * BS_LMAX + l) * MP_NMAP];
+            auto one = [&](CUtensorMap* m, const void* arr, bool u8, int bw, int bh) {
+                const size_t es = u8 ? 1 : 4;
+                cuuint64_t dims[2] = {(cuuint64_t)L.pitch, (cuuint64_t)L.nyn};
+                cuuint64_t strides[1] = {(cuuint64_t)(L.pitch * es)};
+                cuuint32_t box[2] = {(cuuint32_t)bw, (cuuint32_t)bh};
+                cuuint32_t estr[2] = {1, 1};
+                return enc(m, u8 ? CU_TENSOR_MAP_DATA_TYPE_UINT8 : CU_TENSOR_MAP_DATA_TYPE_FLOAT32,
+                           2, (void*)((const char*)arr + base * es), dims, strides, box, estr,
+                           CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE,
+                           CU_TENSOR_MAP_L2_PROMOTION_L2_128B,
+                           CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS;
+            };
+            if (!one(mp + MP_B, L.b, false, MP_BW, MR_WY) ||
+                !one(mp + MP_M, L.m, true, MP_MW, MR_WY) ||
+                !one(mp + MP_XA, L.xa, false, MP_BW, MR_WY) ||
+                !one(mp + MP_X, L.x, false, MP_CW, MP_CH))
+                return 0;  // keep the one-tile-per-block kernels
+        }
+    void* d = dal(nmap * sizeof(CUtensorMap));
+    if (!d) return 2;
+    if (cudaMemcpy(d, maps.data(), nmap * sizeof(CUtensorMap), cudaMemcpyHostToDevice) !=
+        cudaSuccess)
+        return 2;
+    s.mmaps = d;
+    s.pipe_gdown = gdown;
+    s.pipe_gup = gup;
+    s.pipe = true;
+    return 0;
 }
 
 int bs_build(BatchSolver& s, const std::vector<BSMemberDesc>& members, const uint8_t* dmask,
@@ -900,11 +1119,16 @@ int bs_build(BatchSolver& s, const std::vector<BSMemberDesc>& members, const uin
                 if (hm[(size_t)J * L.nxn + I]) return true;
         return false;
     };
-    // Level 0 also carries the members' segments of the level-0 up leg's
-    // <r, z> reduction (mn0, mnn, mg0): every member that reaches below
-    // level 0 keeps at least one tile there.
+    // Level 0 also carries the members' ranges of the level-0 up leg's
+    // <r, z> tile totals (mn0, mnn): every member that reaches below level 0
+    // keeps at least one tile there.
+    // The record's .w serves the pipelined kernels: the column of node 0 in
+    // its row (c0) and MP_SLOW for a region that wraps around the level.
+    auto tile_w = [&](const MGLevel& L, int I0) {
+        const int slow = L.per && (I0 - MR_H < 0 || I0 - MR_H + MR_W > L.nxn) ? MP_SLOW : 0;
+        return (int)(L.off & 15) | slow;
+    };
     std::vector<std::vector<int4>> mt(std::max(1, s.maxl));
-    int mgroups = 0;
     for (int l = 0; l < s.maxl; ++l)
         for (int b = 0; b < s.n; ++b) {
             if (info[b].ltail <= l) continue;
@@ -912,13 +1136,12 @@ int bs_build(BatchSolver& s, const std::vector<BSMemberDesc>& members, const uin
             const int first = (int)mt[l].size();
             for (int J0 = 0; J0 < L.nyn; J0 += MR_TH)
                 for (int I0 = 0; I0 < L.nxn; I0 += MR_TW)
-                    if (has_fluid_m(b, l, J0, I0)) mt[l].push_back(make_int4(b, I0, J0, 0));
+                    if (has_fluid_m(b, l, J0, I0))
+                        mt[l].push_back(make_int4(b, I0, J0, tile_w(L, I0)));
             if (l == 0) {
-                if ((int)mt[0].size() == first) mt[0].push_back(make_int4(b, 0, 0, 0));
+                if ((int)mt[0].size() == first) mt[0].push_back(make_int4(b, 0, 0, tile_w(L, 0)));
                 info[b].mn0 = first;
                 info[b].mnn = (int)mt[0].size() - first;
-                info[b].mg0 = mgroups;
-                mgroups += (info[b].mnn + RED_GROUP - 1) / RED_GROUP;
             }
         }
     auto dal = [&](size_t bytes) -> void* {
@@ -956,18 +1179,18 @@ int bs_build(BatchSolver& s, const std::vector<BSMemberDesc>& members, const uin
     s.dinfo = (BSInfo*)dal(info.size() * sizeof(BSInfo));
     s.eg = (BSGlobals*)dal(sizeof(BSGlobals));
     s.partials = (double*)dal((rt.size() * 2 + 64) * sizeof(double));
-    s.mpartials = (double*)dal((mt[0].size() * 2 + 64) * sizeof(double));
-    s.mgpart = (double*)dal(((size_t)mgroups * 2 + 64) * sizeof(double));
-    s.mgtick = (unsigned int*)dal(((size_t)mgroups + 64) * sizeof(unsigned int));
-    if (!s.mpartials || !s.mgpart || !s.mgtick ||
-        cudaMemset(s.mgtick, 0, ((size_t)mgroups + 64) * sizeof(unsigned int)) != cudaSuccess)
-        return 2;
+    s.mpartials = (double*)dal((mt[0].size() + 64) * sizeof(double));
+    if (!s.mpartials) return 2;
     s.gpart = (double*)dal(((size_t)ngroups * 2 + 64) * sizeof(double));
     s.gtick = (unsigned int*)dal(((size_t)ngroups + 64) * sizeof(unsigned int));
     if (!s.gpart || !s.gtick ||
         cudaMemset(s.gtick, 0, ((size_t)ngroups + 64) * sizeof(unsigned int)) != cudaSuccess)
         return 2;
     if (!s.dlevs || !s.dinfo || !s.eg || !s.partials) return 2;
+    {
+        const int e = bs_pipe_setup(s, levs, info, dal);
+        if (e) return e;
+    }
     if (cudaMemcpy(s.dlevs, levs.data(), levs.size() * sizeof(MGLevel), cudaMemcpyHostToDevice) !=
             cudaSuccess ||
         cudaMemcpy(s.dinfo, info.data(), info.size() * sizeof(BSInfo), cudaMemcpyHostToDevice) !=
@@ -1019,6 +1242,7 @@ static int bs_rebuild(BatchSolver& s, int th)
                 hm[b][(size_t)J * d.pitch + I] = m0[(size_t)J * d.nxn + I];
         d.hmask = hm[b].data();
         d.hoff0 = 0;
+        d.hwin = 0;  // dense node masks: win_ok from the first build stands
     }
     const BSVecs v = s.v;
     DevScalars* scs = s.scs;
@@ -1166,6 +1390,8 @@ void bs_free(BatchSolver& s)
     s.dinfo = nullptr;
     s.eg = nullptr;
     s.partials = nullptr;
+    s.pipe = false;
+    s.mmaps = nullptr;
 }
 
 }  // namespace f2d

@@ -15,10 +15,10 @@ struct BSInfo {
     int nl, ltail, ksweeps;  // levels, first tail level, coarsest sweeps
     int n0, nn;              // range of the member in the level-0 tile table
     int g0;                  // first reduction group of the member
-    // the same for the level-0 table of the multigrid level kernels (the
-    // <r, z> reduction of the level-0 up leg); mnn = 0 when level 0 is in
-    // the member's tail
-    int mn0, mnn, mg0, pad;
+    // the member's range in the level-0 table of the multigrid level kernels
+    // (the tile totals of <r, z> written by the level-0 up leg); mnn = 0 when
+    // level 0 is in the member's tail
+    int mn0, mnn, pad0, pad1;
 };
 
 struct BSGlobals {
@@ -50,6 +50,11 @@ struct BSMemberDesc {
     const uint8_t* hmask;   // host fluid mask, node (J,I) at hoff0 + J*pitch + I
     long long hoff0;
     double cx, cy, maindiag;
+    // hmask holds the whole rows of the level-0 arrays (in-row bytes outside
+    // the node columns included); when not (a rebuild from the dense level
+    // masks), win_ok carries the first build's check of those bytes
+    int hwin = 1;
+    int win_ok = 0;
 };
 
 struct BatchSolver {
@@ -65,9 +70,12 @@ struct BatchSolver {
     std::vector<int> ntiles;
     std::vector<int4*> mtiles; // tiles of the multigrid level kernels per level
     std::vector<int> nmtiles;
-    double* mpartials = nullptr;  // the segmented <r, z> reduction over mtiles[0]
-    double* mgpart = nullptr;
-    unsigned int* mgtick = nullptr;
+    double* mpartials = nullptr;  // <r, z> tile totals of the level-0 up leg (per mtiles[0])
+    // pipelined FP32 level kernels (mg_pipe.cuh): used when the level arrays
+    // pass bs_build's layout checks; TMA maps per member and level, grid sizes
+    bool pipe = false;
+    void* mmaps = nullptr;     // CUtensorMap[n][BS_LMAX][MP_NMAP]
+    int pipe_gdown = 0, pipe_gup = 0;
     int4* rtiles = nullptr;    // level-0 tiles of the Krylov kernels
     int nrtiles = 0;
     double* gpart = nullptr;   // group sums of the two-level reductions

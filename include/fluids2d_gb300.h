@@ -231,6 +231,12 @@ int f2d_set_schedule(f2d_model m, int tile_rows, int sweeps, double tol_in);
  * reference counterpart. The model must have solved once. */
 int f2d_time_solver(f2d_model m, int reps, int flush_l2, double *avg_ms,
                     int64_t *nodes, int *elem_bytes);
+/* Which level kernels the solver timed by f2d_time_solver runs: *pipelined =
+ * 1 for the persistent TMA-staged FP32 kernels (k_mgp_down / k_mgp_up), 0
+ * for the one-tile-per-block kernels (k_mg_down / k_mg_up: the FP64 form,
+ * or level arrays outside the pipelined kernels' layout). Instrumentation,
+ * no reference counterpart. The model must have solved once. */
+int f2d_solver_pipelined(f2d_model m, int *pipelined);
 /* Failure-detection test switch (no reference counterpart). enabled != 0:
  * every stage kernel, once its TMA tile has landed, also waits for a barrier
  * phase that nothing completes, gives up after limit_ms (0 < limit_ms <=
@@ -315,6 +321,8 @@ int f2d_ensemble_time_stage(f2d_ensemble e, int stage, int reps, int flush_l2,
 /* f2d_time_solver for the batched solver of all members. */
 int f2d_ensemble_time_solver(f2d_ensemble e, int reps, int flush_l2, double *avg_ms,
                              int64_t *nodes, int *elem_bytes);
+/* f2d_solver_pipelined for the batched solver of all members. */
+int f2d_ensemble_solver_pipelined(f2d_ensemble e, int *pipelined);
 
 /* ---- discrete adjoint (eulerpsi, closed basin, weno/upwind fluxes) ------ */
 

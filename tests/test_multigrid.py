@@ -6,9 +6,12 @@ of the solution cannot see a broken V-cycle. These tests bound the iteration
 count of solves from a zero initial guess to the 1e-12 relative residual on
 grids with islands, x-periodic channels and the Helmholtz operator, for both
 forms and every multigrid schedule (1 or 2 sweeps per leg, 32- or 64-row
-tiles: the four kernel variants), and check the solution against the plain
-sparse operator.
+tiles), and check the solution against the plain sparse operator; the FP32
+form runs the pipelined level kernels (mg_pipe.cuh), the FP64 form the
+one-tile-per-block ones (mg_reg.cuh).
 """
+import ctypes
+
 import numpy as np
 import pytest
 
@@ -18,6 +21,7 @@ pytestmark = pytest.mark.gpu
 torch = pytest.importorskip("torch")
 
 from fluids2d_gb300 import workloads as wl  # noqa: E402
+from fluids2d_gb300._lib import lib  # noqa: E402
 from test_gpu_parity import _model  # noqa: E402
 
 # a V-cycle with red-black Gauss-Seidel reduces the residual by about 10x per
@@ -53,6 +57,11 @@ def test_poisson_iterations_from_zero(kind, n, precision, schedule):
     print(f"{kind} {n}^2 {precision} {schedule}: {it} iterations, "
           f"relres {solver.last_relres:.1e}")
     assert it <= MAX_ITERS[precision], it
+    # the FP32 form runs the pipelined level kernels on these layouts (the
+    # periodic channel's edge tiles through their element-wise path)
+    pipe = ctypes.c_int(-1)
+    assert lib().f2d_solver_pipelined(m._h, ctypes.byref(pipe)) == 0
+    assert pipe.value == (1 if precision == "fp32" else 0)
     # the true residual with the sparse operator
     om = O.Mesh(O.Param(model=model, nx=n, ny=n, xperiodic=kw.get("xperiodic", False),
                         f0=kw.get("f0", 0.0), g=1.0, H=1.0))
