@@ -25,10 +25,7 @@ namespace f2d {
 static size_t tail_smem(const std::vector<MGLevel>& lev, int l0, size_t es)
 {
     size_t off = 0;
-    for (size_t l = l0; l < lev.size(); ++l) {
-        const size_t n = (size_t)lev[l].nyn * lev[l].nxn;
-        off += 2 * ((n * es + 15) / 16 * 16) + (n + 15) / 16 * 16;
-    }
+    for (size_t l = l0; l < lev.size(); ++l) off += tail_level_bytes(lev[l].nyn, lev[l].nxn, es);
     return off;
 }
 

@@ -27,6 +27,14 @@ struct MGLevel {
     float fmd;
 };
 
+// bytes of one level's arrays (x, b: element size es; mask) in the
+// single-block tail's shared memory, stored with a one-node border
+__host__ __device__ inline size_t tail_level_bytes(int nyn, int nxn, size_t es)
+{
+    const size_t n = (size_t)(nyn + 2) * (nxn + 2);
+    return 2 * ((n * es + 15) / 16 * 16) + (n + 15) / 16 * 16;
+}
+
 struct MGHost {
     std::vector<MGLevel> lev;
     std::vector<void*> owned;  // device allocations of coarse levels

@@ -45,245 +45,231 @@ __device__ __forceinline__ long long nidx(const MGLevel& L, int J, int I)
     return L.off + (long long)J * L.pitch + I;
 }
 
-// value of a neighbour node, 0 outside the level or at non-fluid nodes. The
-// index is clamped into the level and both loads are issued unconditionally
-// (then selected), so the four neighbour loads of a stencil can be in flight
-// together; non-fluid values are never used, whatever they hold.
-template <typename S>
-__device__ __forceinline__ S nbv(const MGLevel& L, const S* __restrict__ x, int J,
-                                 int I)
-{
-    bool ok = (unsigned)J < (unsigned)L.nyn;
-    if (I < 0 || I >= L.nxn) {
-        if (L.per) I = I < 0 ? I + L.nxn : I - L.nxn;
-        else ok = false;
-    }
-    const int Jc = min(max(J, 0), L.nyn - 1), Ic = min(max(I, 0), L.nxn - 1);
-    const long long k = nidx(L, Jc, Ic);
-    const S v = x[k];
-    const uint8_t m = L.m[k];
-    return (ok && m) ? v : S(0);
-}
-
-template <typename S>
-__device__ __forceinline__ S apply_off(const MGLevel& L, const S* __restrict__ x,
-                                       int J, int I)
-{
-    return Coef<S>::cx(L) * (nbv(L, x, J, I - 1) + nbv(L, x, J, I + 1)) +
-           Coef<S>::cy(L) * (nbv(L, x, J - 1, I) + nbv(L, x, J + 1, I));
-}
-
-// ---- node operations (shared by the grid kernels and the tail block) ------
-
-// Gauss-Seidel half sweep of one colour. zero_init (red only): x = b/diag on
-// red nodes and x = 0 elsewhere (the sweep that starts from a zero guess).
-template <typename S>
-__device__ __forceinline__ void op_smooth(const MGLevel& L, int J, int I, int color,
-                                          bool zero_init)
-{
-    const long long k = nidx(L, J, I);
-    S* x = lx<S>(L);
-    const S* b = lb<S>(L);
-    const bool mine = ((J + I) & 1) == color;
-    if (zero_init) {
-        x[k] = (mine && L.m[k]) ? b[k] * Coef<S>::idiag(L) : S(0);
-        return;
-    }
-    if (!mine || !L.m[k]) return;
-    x[k] = (b[k] - apply_off<S>(L, x, J, I)) * Coef<S>::idiag(L);
-}
-
-// residual of the fine level at node (J, I) (0 at non-fluid nodes)
-template <typename S>
-__device__ __forceinline__ S fine_res(const MGLevel& F, int J, int I)
-{
-    if (J < 0 || J >= F.nyn) return S(0);
-    if (I < 0 || I >= F.nxn) {
-        if (!F.per) return S(0);
-        I = I < 0 ? I + F.nxn : I - F.nxn;
-    }
-    const long long k = nidx(F, J, I);
-    if (!F.m[k]) return S(0);
-    const S* x = lx<S>(F);
-    return lb<S>(F)[k] - (apply_off<S>(F, x, J, I) + Coef<S>::diag(F) * x[k]);
-}
-
-// coarse right-hand side = P^T (fine residual). After the pre-smoothing
-// (red from a zero guess, then black) the residual of every black node is
-// zero, and the fine nodes of full weighting that are black are exactly the
-// four edge neighbours of (2J, 2I); only the centre and the four corners
-// (all red) contribute.
-template <typename S>
-__device__ __forceinline__ void op_restrict(const MGLevel& F, const MGLevel& C, int J,
-                                            int I)
-{
-    const long long k = nidx(C, J, I);
-    S v = S(0);
-    if (C.m[k]) {
-        const int fj = 2 * J, fi = 2 * I;
-        const S c = (fine_res<S>(F, fj - 1, fi - 1) + fine_res<S>(F, fj - 1, fi + 1)) +
-                    (fine_res<S>(F, fj + 1, fi - 1) + fine_res<S>(F, fj + 1, fi + 1));
-        v = fine_res<S>(F, fj, fi) + S(0.25) * c;
-    }
-    lb<S>(C)[k] = v;
-}
-
-// coarse node value for prolongation (0 outside / non-fluid: x is 0 there)
-template <typename S>
-__device__ __forceinline__ S cval(const MGLevel& C, int J, int I)
-{
-    if (J < 0 || J >= C.nyn) return S(0);
-    if (I >= C.nxn) {
-        if (!C.per) return S(0);
-        I -= C.nxn;
-    }
-    return lx<S>(C)[nidx(C, J, I)];
-}
-
-// fine x += P (coarse x), bilinear
-template <typename S>
-__device__ __forceinline__ void op_prolong(const MGLevel& C, const MGLevel& F, int J,
-                                           int I)
-{
-    const long long k = nidx(F, J, I);
-    if (!F.m[k]) return;
-    const int cj = J >> 1, ci = I >> 1;
-    const int oj = J & 1, oi = I & 1;
-    S v;
-    if (!oj && !oi) v = cval<S>(C, cj, ci);
-    else if (!oj) v = S(0.5) * (cval<S>(C, cj, ci) + cval<S>(C, cj, ci + 1));
-    else if (!oi) v = S(0.5) * (cval<S>(C, cj, ci) + cval<S>(C, cj + 1, ci));
-    else
-        v = S(0.25) * ((cval<S>(C, cj, ci) + cval<S>(C, cj, ci + 1)) +
-                       (cval<S>(C, cj + 1, ci) + cval<S>(C, cj + 1, ci + 1)));
-    lx<S>(F)[k] += v;
-}
-
-// Pre-smoothing from a zero guess in one pass: red nodes x = b/diag, black
-// nodes one Gauss-Seidel update against those red values, which are
-// recomputed from b instead of read back (same result as two half sweeps).
-template <typename S>
-__device__ __forceinline__ S red_from_zero(const MGLevel& L, int J, int I)
-{
-    if (J < 0 || J >= L.nyn) return S(0);
-    if (I < 0 || I >= L.nxn) {
-        if (!L.per) return S(0);
-        I = I < 0 ? I + L.nxn : I - L.nxn;
-    }
-    const long long k = nidx(L, J, I);
-    return L.m[k] ? lb<S>(L)[k] * Coef<S>::idiag(L) : S(0);
-}
-
 // ---- the single-block tail: levels l0..nl-1 of the V-cycle ---------------
-template <typename S, typename F>
-__device__ __forceinline__ void block_for(const MGLevel& L, F f)
+// One level in shared memory: x, b and the fluid mask of nyn x nxn nodes with
+// a one-node border (row pitch P = nxn + 2, node (J, I) at (J+1) P + I+1).
+// The border of x is 0, or on an x-periodic level the copy of the opposite
+// edge column (written by whichever thread writes that edge node; the two
+// share a colour since a periodic level has an even nxn), so the sweeps read
+// their neighbours without bounds checks.
+template <typename S>
+struct TailLev {
+    S* x;
+    S* b;
+    uint8_t* m;
+    int nyn, nxn, P, per;
+    int hw;           // colour slots per row, (nxn + 1) / 2
+    float rhw, rnx;   // 1/hw and 1/nxn (row of a slot index without a division)
+    S cx, cy, id, dg;
+};
+
+// row of slot k of a row-major table of rows of width w (k < 2^20): the
+// fractional part of (k + 0.5)/w is at least 0.5/w away from an integer,
+// far above the FP32 rounding of the product
+__device__ __forceinline__ int tail_row(int k, float rw)
 {
-    const int n = L.nyn * L.nxn;
-    for (int k = threadIdx.x; k < n; k += blockDim.x) f(k / L.nxn, k % L.nxn);
+    return __float2int_rz((k + 0.5f) * rw);
+}
+
+template <typename S>
+__device__ __forceinline__ void tail_put(const TailLev<S>& L, int e, int I, S v)
+{
+    L.x[e] = v;
+    if (L.per) {
+        if (I == 0) L.x[e + L.nxn] = v;
+        else if (I == L.nxn - 1) L.x[e - L.nxn] = v;
+    }
+}
+
+// Gauss-Seidel half sweep of colour COL ((J + I) & 1 == COL); ZERO: from a
+// zero guess (x = b/diag on the colour; the other colour is 0 already)
+template <typename S, int COL, bool ZERO>
+__device__ __forceinline__ void tail_half(const TailLev<S>& L)
+{
+    const int n = L.nyn * L.hw;
+    for (int k = threadIdx.x; k < n; k += blockDim.x) {
+        const int J = tail_row(k, L.rhw);
+        const int I = 2 * (k - J * L.hw) + ((J + COL) & 1);
+        if (I >= L.nxn) continue;
+        const int e = (J + 1) * L.P + I + 1;
+        S v = S(0);
+        if (L.m[e]) {
+            if (ZERO) v = L.b[e] * L.id;
+            else
+                v = (L.b[e] - (L.cx * (L.x[e - 1] + L.x[e + 1]) +
+                               L.cy * (L.x[e - L.P] + L.x[e + L.P]))) *
+                    L.id;
+        }
+        tail_put(L, e, I, v);
+    }
     __syncthreads();
 }
 
-// Pre-smoothing of one node from a zero guess (red from zero, then one black
-// update against those red values, recomputed from b).
+// residual b - A x at fine node (j, i), 0 outside the level or at non-fluid
+// nodes; i may lie one node outside an x-periodic level (wrapped)
 template <typename S>
-__device__ __forceinline__ void op_presmooth(const MGLevel& L, int J, int I)
+__device__ __forceinline__ S tail_res(const TailLev<S>& F, int j, int i)
 {
-    const long long k = nidx(L, J, I);
-    S v = S(0);
-    if (L.m[k]) {
-        const S* b = lb<S>(L);
-        if (((J + I) & 1) == 0) {
-            v = b[k] * Coef<S>::idiag(L);
-        } else {
-            const S off = Coef<S>::cx(L) * (red_from_zero<S>(L, J, I - 1) + red_from_zero<S>(L, J, I + 1)) +
-                          Coef<S>::cy(L) * (red_from_zero<S>(L, J - 1, I) + red_from_zero<S>(L, J + 1, I));
-            v = (b[k] - off) * Coef<S>::idiag(L);
-        }
+    if (j < 0 || j >= F.nyn) return S(0);
+    if (i < 0 || i >= F.nxn) {
+        if (!F.per) return S(0);
+        i = i < 0 ? i + F.nxn : i - F.nxn;
     }
-    lx<S>(L)[k] = v;
+    const int e = (j + 1) * F.P + i + 1;
+    if (!F.m[e]) return S(0);
+    return F.b[e] - ((F.cx * (F.x[e - 1] + F.x[e + 1]) + F.cy * (F.x[e - F.P] + F.x[e + F.P])) +
+                     F.dg * F.x[e]);
 }
 
-// The V-cycle on levels l0..nl-1 of `lev`, run by one thread block. All
-// these levels live in shared memory (dense nyn x nxn, x, b, mask); only b of
+// coarse b = P^T (fine residual): after the pre-smoothing (ending with a
+// black half sweep) every black residual is zero, and the fine nodes of full
+// weighting that are black are exactly the four edge neighbours of (2J, 2I);
+// only the centre and the four corners (all red) contribute
+template <typename S>
+__device__ __forceinline__ void tail_restrict(const TailLev<S>& F, const TailLev<S>& C)
+{
+    const int n = C.nyn * C.nxn;
+    for (int k = threadIdx.x; k < n; k += blockDim.x) {
+        const int J = tail_row(k, C.rnx), I = k - J * C.nxn;
+        const int e = (J + 1) * C.P + I + 1;
+        S v = S(0);
+        if (C.m[e]) {
+            const int fj = 2 * J, fi = 2 * I;
+            const S c = (tail_res(F, fj - 1, fi - 1) + tail_res(F, fj - 1, fi + 1)) +
+                        (tail_res(F, fj + 1, fi - 1) + tail_res(F, fj + 1, fi + 1));
+            v = tail_res(F, fj, fi) + S(0.25) * c;
+        }
+        C.b[e] = v;
+    }
+    __syncthreads();
+}
+
+// fine x += P (coarse x), bilinear, at the fluid nodes (the coarse border
+// supplies 0 outside the level, or the wrapped column)
+template <typename S>
+__device__ __forceinline__ void tail_prolong(const TailLev<S>& C, const TailLev<S>& F)
+{
+    const int n = F.nyn * F.nxn;
+    for (int k = threadIdx.x; k < n; k += blockDim.x) {
+        const int J = tail_row(k, F.rnx), I = k - J * F.nxn;
+        const int e = (J + 1) * F.P + I + 1;
+        if (!F.m[e]) continue;
+        const int cj = J >> 1, ci = I >> 1, oj = J & 1, oi = I & 1;
+        const int c0 = (cj + 1) * C.P + ci + 1;
+        S v;
+        if (!oj && !oi) v = C.x[c0];
+        else if (!oj) v = S(0.5) * (C.x[c0] + C.x[c0 + 1]);
+        else if (!oi) v = S(0.5) * (C.x[c0] + C.x[c0 + C.P]);
+        else
+            v = S(0.25) * ((C.x[c0] + C.x[c0 + 1]) + (C.x[c0 + C.P] + C.x[c0 + C.P + 1]));
+        tail_put(F, e, I, F.x[e] + v);
+    }
+    __syncthreads();
+}
+
+// The V-cycle on levels l0..nl-1 of `lev` (nt = nl - l0 <= 16), run by one
+// thread block: red-black Gauss-Seidel, nu sweeps per leg, (R,B)^k (B,R)^k
+// on the coarsest level. All these levels live in shared memory; only b of
 // level l0 comes from global memory and only x of level l0 goes back, so each
-// phase costs a barrier, not a global-memory round trip.
+// phase costs a barrier, not a global-memory round trip. On return sl[0]
+// describes level l0 in shared memory.
 template <typename S>
 __device__ __forceinline__ void tail_vcycle(const MGLevel* __restrict__ lev, int l0,
                                             int nl, int ksweeps,
-                                            unsigned char* smem_raw, MGLevel* sl, int nu = 1)
+                                            unsigned char* smem_raw, TailLev<S>* sl, int nu = 1)
 {
+    const int nt = nl - l0;
     if (threadIdx.x == 0) {
         size_t off = 0;
-        for (int l = l0; l < nl; ++l) {
-            MGLevel D = lev[l];
-            const size_t n = (size_t)D.nyn * D.nxn;
-            D.pitch = D.nxn;
-            D.off = 0;
-            D.x = smem_raw + off;
+        for (int q = 0; q < nt; ++q) {
+            const MGLevel& G = lev[l0 + q];
+            TailLev<S>& D = sl[q];
+            D.nyn = G.nyn;
+            D.nxn = G.nxn;
+            D.P = G.nxn + 2;
+            D.per = G.per;
+            D.hw = (G.nxn + 1) / 2;
+            D.rhw = 1.0f / (float)D.hw;
+            D.rnx = 1.0f / (float)G.nxn;
+            D.cx = Coef<S>::cx(G);
+            D.cy = Coef<S>::cy(G);
+            D.id = Coef<S>::idiag(G);
+            D.dg = Coef<S>::diag(G);
+            const size_t n = (size_t)(G.nyn + 2) * D.P;
+            D.x = (S*)(smem_raw + off);
             off += (n * sizeof(S) + 15) / 16 * 16;
-            D.b = smem_raw + off;
+            D.b = (S*)(smem_raw + off);
             off += (n * sizeof(S) + 15) / 16 * 16;
-            D.m = (const uint8_t*)(smem_raw + off);
+            D.m = smem_raw + off;
             off += (n + 15) / 16 * 16;
-            sl[l - l0] = D;
         }
     }
     __syncthreads();
-    for (int l = l0; l < nl; ++l) {
-        const MGLevel& L = lev[l];
-        const MGLevel& D = sl[l - l0];
-        const int n = L.nyn * L.nxn;
-        for (int k = threadIdx.x; k < n; k += blockDim.x) {
-            const long long g = nidx(L, k / L.nxn, k % L.nxn);
-            ((uint8_t*)D.m)[k] = L.m[g];
-            if (l == l0) ((S*)D.b)[k] = ((const S*)L.b)[g];
+    for (int q = 0; q < nt; ++q) {
+        const MGLevel& G = lev[l0 + q];
+        const TailLev<S>& D = sl[q];
+        const int n = (D.nyn + 2) * D.P;
+        for (int e = threadIdx.x; e < n; e += blockDim.x) {
+            const int J = tail_row(e, 1.0f / (float)D.P) - 1, I = e - (J + 1) * D.P - 1;
+            const bool in = J >= 0 && J < D.nyn && I >= 0 && I < D.nxn;
+            uint8_t mv = 0;
+            S bv = S(0);
+            if (in) {
+                const long long g = nidx(G, J, I);
+                mv = G.m[g];
+                if (q == 0) bv = ((const S*)G.b)[g];
+            }
+            D.x[e] = S(0);
+            D.b[e] = bv;
+            D.m[e] = mv;
         }
     }
     __syncthreads();
-    const int nt = nl - l0;
-    // down: pre-smooth (red from zero, black) and restrict
+    // down: pre-smooth (red from zero, black, nu - 1 more (red, black)),
+    // restrict
     for (int q = 0; q < nt - 1; ++q) {
-        const MGLevel L = sl[q], C = sl[q + 1];
-        block_for<S>(L, [&](int J, int I) { op_smooth<S>(L, J, I, 0, true); });
-        block_for<S>(L, [&](int J, int I) { op_smooth<S>(L, J, I, 1, false); });
+        const TailLev<S> L = sl[q];
+        tail_half<S, 0, true>(L);
+        tail_half<S, 1, false>(L);
         for (int k = 1; k < nu; ++k) {
-            block_for<S>(L, [&](int J, int I) { op_smooth<S>(L, J, I, 0, false); });
-            block_for<S>(L, [&](int J, int I) { op_smooth<S>(L, J, I, 1, false); });
+            tail_half<S, 0, false>(L);
+            tail_half<S, 1, false>(L);
         }
-        block_for<S>(C, [&](int J, int I) { op_restrict<S>(L, C, J, I); });
+        tail_restrict<S>(L, sl[q + 1]);
     }
     // coarsest: (R,B)^k (B,R)^k from a zero guess (palindromic = symmetric)
     {
-        const MGLevel L = sl[nt - 1];
-        block_for<S>(L, [&](int J, int I) { op_smooth<S>(L, J, I, 0, true); });
-        block_for<S>(L, [&](int J, int I) { op_smooth<S>(L, J, I, 1, false); });
+        const TailLev<S> L = sl[nt - 1];
+        tail_half<S, 0, true>(L);
+        tail_half<S, 1, false>(L);
         for (int s = 1; s < ksweeps; ++s) {
-            block_for<S>(L, [&](int J, int I) { op_smooth<S>(L, J, I, 0, false); });
-            block_for<S>(L, [&](int J, int I) { op_smooth<S>(L, J, I, 1, false); });
+            tail_half<S, 0, false>(L);
+            tail_half<S, 1, false>(L);
         }
         for (int s = 0; s < ksweeps; ++s) {
-            block_for<S>(L, [&](int J, int I) { op_smooth<S>(L, J, I, 1, false); });
-            block_for<S>(L, [&](int J, int I) { op_smooth<S>(L, J, I, 0, false); });
+            tail_half<S, 1, false>(L);
+            tail_half<S, 0, false>(L);
         }
     }
-    // up: prolongate, post-smooth (black, red)
+    // up: prolongate, post-smooth (black, red) x nu
     for (int q = nt - 2; q >= 0; --q) {
-        const MGLevel L = sl[q], C = sl[q + 1];
-        block_for<S>(L, [&](int J, int I) { op_prolong<S>(C, L, J, I); });
+        const TailLev<S> L = sl[q];
+        tail_prolong<S>(sl[q + 1], L);
         for (int k = 0; k < nu; ++k) {
-            block_for<S>(L, [&](int J, int I) { op_smooth<S>(L, J, I, 1, false); });
-            block_for<S>(L, [&](int J, int I) { op_smooth<S>(L, J, I, 0, false); });
+            tail_half<S, 1, false>(L);
+            tail_half<S, 0, false>(L);
         }
     }
     // level l0's x back to global memory
     {
-        const MGLevel G = lev[l0];
-        const MGLevel L = sl[0];
-        const int n = L.nyn * L.nxn;
-        for (int k = threadIdx.x; k < n; k += blockDim.x)
-            ((S*)G.x)[nidx(G, k / L.nxn, k % L.nxn)] = ((const S*)L.x)[k];
+        const MGLevel& G = lev[l0];
+        const TailLev<S>& D = sl[0];
+        const int n = D.nyn * D.nxn;
+        for (int k = threadIdx.x; k < n; k += blockDim.x) {
+            const int J = tail_row(k, D.rnx), I = k - J * D.nxn;
+            ((S*)G.x)[nidx(G, J, I)] = D.x[(J + 1) * D.P + I + 1];
+        }
     }
 }
-
 
 }  // namespace f2d

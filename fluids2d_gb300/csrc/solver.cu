@@ -103,34 +103,6 @@ __device__ __forceinline__ void stage_region(const MGLevel& L, int J0, int I0,
     }
 }
 
-// per-thread dot-product partial -> what seg_reduce2 expects: FP32 values
-// are summed per warp in FP32 and combined in FP64 (block total in thread 0);
-// FP64 values go to seg_reduce2's own FP64 block reduction.
-template <typename V>
-__device__ __forceinline__ void block_dot(V acc, double (&w)[1]);
-template <>
-__device__ __forceinline__ void block_dot<double>(double acc, double (&w)[1])
-{
-    w[0] = acc;
-}
-template <>
-__device__ __forceinline__ void block_dot<float>(float acc, double (&w)[1])
-{
-    const float a[1] = {acc};
-    w[0] = 0.0;
-    block_total_f<1>(a, w);
-}
-
-template <typename V>
-__device__ __forceinline__ bool member_dot(V acc, double (&w)[1], double* partials,
-                                           double* gpart, unsigned int* gtick,
-                                           const BSInfo& in, unsigned int* ticket)
-{
-    block_dot<V>(acc, w);
-    return seg_reduce2<1, std::is_same<V, float>::value>(w, partials, gpart, gtick, blockIdx.x,
-                                                         in.n0, in.nn, in.g0, ticket);
-}
-
 __device__ __forceinline__ bool bs_skip(const DevScalars& sc, int ir)
 {
     return sc.converged || (ir && sc.conv_in);
@@ -216,15 +188,15 @@ k_bs_tail(const BSInfo* __restrict__ info, const MGLevel* __restrict__ levs, Dev
     DevScalars& sc = scs[b];
     if (bs_skip(sc, ir)) return;
     extern __shared__ __align__(16) unsigned char smem_raw[];
-    __shared__ MGLevel sl[16];
+    __shared__ TailLev<S> sl[16];
     const BSInfo in = info[b];
     tail_vcycle<S>(&levs[b * BS_LMAX], in.ltail, in.nl, in.ksweeps, smem_raw, sl, nu);
     if (in.ltail != 0) return;
-    const MGLevel D = sl[0];
-    const int n = D.nyn * D.nxn;
+    const TailLev<S>& D = sl[0];
+    const int n = (D.nyn + 2) * D.P;
     S acc = S(0);
-    for (int k = threadIdx.x; k < n; k += blockDim.x)
-        if (D.m[k]) acc += ((const S*)D.b)[k] * ((const S*)D.x)[k];
+    for (int e = threadIdx.x; e < n; e += blockDim.x)
+        if (D.m[e]) acc += D.b[e] * D.x[e];  // border: mask 0
     double w[1];
     if constexpr (std::is_same<S, float>::value) {
         const float a[1] = {acc};
@@ -245,19 +217,17 @@ k_bs_tail(const BSInfo* __restrict__ info, const MGLevel* __restrict__ levs, Dev
 // the halo belongs to other blocks and must not be overwritten meanwhile).
 template <typename S, typename V, int TH>
 __global__ void __launch_bounds__(256)
-k_bs_pq(const int4* __restrict__ tiles, const BSInfo* __restrict__ info,
-        const MGLevel* __restrict__ levs, const S* __restrict__ z, V* __restrict__ p0,
-        V* __restrict__ p1, V* __restrict__ q, DevScalars* scs, double* partials, double* gpart,
-        unsigned int* gtick, int ir)
+k_bs_pq(const int4* __restrict__ tiles, const MGLevel* __restrict__ levs,
+        const S* __restrict__ z, V* __restrict__ p0, V* __restrict__ p1, V* __restrict__ q,
+        const DevScalars* __restrict__ scs, double* partials, int ir)
 {
     constexpr int H = 1, W = Reg<H, TH>::WX, N = Reg<H, TH>::N, IT = (N + 255) / 256;
     constexpr int TQ = TH / 8;
     __shared__ V sp[N];
     __shared__ uint8_t sm[N];
     const int4 tl = tiles[blockIdx.x];
-    DevScalars& sc = scs[tl.x];
+    const DevScalars& sc = scs[tl.x];
     if (bs_skip(sc, ir)) return;
-    const BSInfo in = info[tl.x];
     const MGLevel L = levs[tl.x * BS_LMAX];
     const int it = ir ? sc.iter_in : sc.iter;
     const bool first = it == 0;
@@ -302,10 +272,27 @@ k_bs_pq(const int4* __restrict__ tiles, const BSInfo* __restrict__ info,
             acc += pv * qv;
         }
     }
-    double w[1];
-    if (member_dot<V>(acc, w, partials, gpart, gtick, in, &sc.counter[3])) {
-        sc.pq = w[0];
-        sc.alpha = sc.rz / w[0];
+    const double tot = block_sum<V>(acc);
+    if (t == 0) partials[blockIdx.x] = tot;
+}
+
+// <p, q> of every member from k_bs_pq's tile totals (fixed order), alpha =
+// rz / <p, q>. The tile kernels write their totals and no more (no fence or
+// ticket per block); one block per member sums them here.
+__global__ void __launch_bounds__(256)
+k_bs_alpha(const BSInfo* __restrict__ info, DevScalars* scs, const double* __restrict__ tpart,
+           int ir)
+{
+    const BSInfo in = info[blockIdx.x];
+    DevScalars& sc = scs[blockIdx.x];
+    if (bs_skip(sc, ir)) return;
+    double acc[1] = {0.0};
+    final_sum<1, false>(acc, tpart, in.n0, in.nn, threadIdx.x, blockDim.x);
+    __shared__ double sh[32];
+    block_reduce<1, false>(acc, sh);
+    if (threadIdx.x == 0) {
+        sc.pq = acc[0];
+        sc.alpha = sc.rz / acc[0];
     }
 }
 
@@ -315,89 +302,102 @@ k_bs_pq(const int4* __restrict__ tiles, const BSInfo* __restrict__ info,
 // starting residual.
 template <typename V, int TH>
 __global__ void __launch_bounds__(256)
-k_bs_xr(const int4* __restrict__ tiles, const BSInfo* __restrict__ info,
-        const MGLevel* __restrict__ levs, V* __restrict__ x, V* __restrict__ r,
-        const V* __restrict__ p0, const V* __restrict__ p1, const V* __restrict__ q,
-        DevScalars* scs, double* partials, double* gpart, unsigned int* gtick, BSGlobals* eg,
-        cudaGraphConditionalHandle cond, int ir, int nmem)
+k_bs_xr(const int4* __restrict__ tiles, const MGLevel* __restrict__ levs, V* __restrict__ x,
+        V* __restrict__ r, const V* __restrict__ p0, const V* __restrict__ p1,
+        const V* __restrict__ q, const DevScalars* __restrict__ scs, double* partials, int ir)
 {
     const int4 tl = tiles[blockIdx.x];
-    DevScalars& sc = scs[tl.x];
-    const BSInfo in = info[tl.x];
-    bool mine = false;
-    if (bs_skip(sc, ir)) {
-        mine = threadIdx.x == 0 && threadIdx.y == 0 && (int)blockIdx.x == in.n0;
-    } else {
-        const MGLevel L = levs[tl.x * BS_LMAX];
-        const int zero = ir ? 0 : sc.pad1;
-        const int it = ir ? sc.iter_in : sc.iter;
-        const bool first = ir && it == 0;
-        const V* __restrict__ p = (it & 1) ? p0 : p1;  // written by k_bs_pq
-        const V a = V(sc.alpha);
-        V acc = V(0);
-        // rows in batches of 4: the loads of a batch are in flight together,
-        // without the register cost of holding all rows of the tile
-        constexpr int QB = 4;
+    const DevScalars& sc = scs[tl.x];
+    if (bs_skip(sc, ir)) return;
+    const MGLevel L = levs[tl.x * BS_LMAX];
+    const int zero = ir ? 0 : sc.pad1;
+    const int it = ir ? sc.iter_in : sc.iter;
+    const bool first = ir && it == 0;
+    const V* __restrict__ p = (it & 1) ? p0 : p1;  // written by k_bs_pq
+    const V a = V(sc.alpha);
+    V acc = V(0);
+    // rows in batches of 4: the loads of a batch are in flight together,
+    // without the register cost of holding all rows of the tile
+    constexpr int QB = 4;
 #pragma unroll
-        for (int q0 = 0; q0 < TH / 8; q0 += QB) {
-            long long k[QB];
-            bool ok[QB];
-            uint8_t mv[QB];
-            V xv[QB], pv[QB], rv[QB], qv[QB];
+    for (int q0 = 0; q0 < TH / 8; q0 += QB) {
+        long long k[QB];
+        bool ok[QB];
+        uint8_t mv[QB];
+        V xv[QB], pv[QB], rv[QB], qv[QB];
 #pragma unroll
-            for (int qr = 0; qr < QB; ++qr) {
-                const int J = tl.z + threadIdx.y + 8 * (q0 + qr), I = tl.y + threadIdx.x;
-                ok[qr] = J < L.nyn && I < L.nxn;
-                k[qr] = nidx(L, min(J, L.nyn - 1), min(I, L.nxn - 1));
-                mv[qr] = L.m[k[qr]];
-                xv[qr] = first ? V(0) : x[k[qr]];
-                pv[qr] = p[k[qr]];
-                rv[qr] = r[k[qr]];
-                qv[qr] = q[k[qr]];
-            }
-#pragma unroll
-            for (int qr = 0; qr < QB; ++qr) {
-                if (!ok[qr] || !mv[qr]) continue;
-                if (zero) {
-                    x[k[qr]] = V(0);
-                    r[k[qr]] = V(0);
-                    continue;
-                }
-                x[k[qr]] = xv[qr] + a * pv[qr];
-                const V rn = rv[qr] - a * qv[qr];
-                r[k[qr]] = rn;
-                acc += rn * rn;
-            }
+        for (int qr = 0; qr < QB; ++qr) {
+            const int J = tl.z + threadIdx.y + 8 * (q0 + qr), I = tl.y + threadIdx.x;
+            ok[qr] = J < L.nyn && I < L.nxn;
+            k[qr] = nidx(L, min(J, L.nyn - 1), min(I, L.nxn - 1));
+            mv[qr] = L.m[k[qr]];
+            xv[qr] = first ? V(0) : x[k[qr]];
+            pv[qr] = p[k[qr]];
+            rv[qr] = r[k[qr]];
+            qv[qr] = q[k[qr]];
         }
-        double w[1];
-        mine = member_dot<V>(acc, w, partials, gpart, gtick, in, &sc.counter[4]);
-        if (mine) {
-            sc.total_iters += 1;
-            const bool bad = !(w[0] == w[0]);
-            if (bad) atomicOr(&eg->status, ST_NONFINITE);
-            if (ir) {
-                sc.iter_in += 1;
-                // a round stops at its relative tolerance, or as soon as its
-                // residual is a tenth of what the whole solve must reach
-                // (the last round of a solve needs only the digits missing,
-                // not tol_in more)
-                const double goal = fmax(sc.tol_in2 * sc.rr0, 0.01 * sc.tol2 * sc.bb);
-                const int done = bad || w[0] <= goal || sc.iter_in >= sc.maxit_in;
-                if (done) {
-                    sc.conv_in = 1;
-                    atomicSub(&eg->active_in, 1);
-                }
-            } else {
-                sc.rr = w[0];
-                sc.iter += 1;
-                const int conv = bad || zero || (w[0] <= sc.tol2 * sc.bb);
-                sc.pad1 = 0;
-                const int more = !conv && sc.iter < sc.maxit;
-                if (!conv && !more) atomicOr(&eg->status, ST_PCG_MAXIT);
-                if (!more) {
-                    sc.converged = 1;
-                    atomicSub(&eg->active_out, 1);
-                }
+#pragma unroll
+        for (int qr = 0; qr < QB; ++qr) {
+            if (!ok[qr] || !mv[qr]) continue;
+            if (zero) {
+                x[k[qr]] = V(0);
+                r[k[qr]] = V(0);
+                continue;
+            }
+            x[k[qr]] = xv[qr] + a * pv[qr];
+            const V rn = rv[qr] - a * qv[qr];
+            r[k[qr]] = rn;
+            acc += rn * rn;
+        }
+    }
+    const double tot = block_sum<V>(acc);
+    if (threadIdx.x == 0 && threadIdx.y == 0) partials[blockIdx.x] = tot;
+}
+
+// <r, r> of every member from k_bs_xr's tile totals (fixed order), the
+// member's convergence, and the loop condition (the block that completes
+// the count over all members sets it).
+__global__ void __launch_bounds__(256)
+k_bs_conv(const BSInfo* __restrict__ info, DevScalars* scs, const double* __restrict__ tpart,
+          BSGlobals* eg, cudaGraphConditionalHandle cond, int ir, int nmem)
+{
+    const BSInfo in = info[blockIdx.x];
+    DevScalars& sc = scs[blockIdx.x];
+    const bool skip = bs_skip(sc, ir);
+    double w[1] = {0.0};
+    if (!skip) {
+        final_sum<1, false>(w, tpart, in.n0, in.nn, threadIdx.x, blockDim.x);
+        __shared__ double sh[32];
+        block_reduce<1, false>(w, sh);
+    }
+    const bool mine = threadIdx.x == 0;
+    if (mine && !skip) {
+        const int zero = ir ? 0 : sc.pad1;
+        sc.total_iters += 1;
+        const bool bad = !(w[0] == w[0]);
+        if (bad) atomicOr(&eg->status, ST_NONFINITE);
+        if (ir) {
+            sc.iter_in += 1;
+            // a round stops at its relative tolerance, or as soon as its
+            // residual is a tenth of what the whole solve must reach (the
+            // last round of a solve needs only the digits missing, not
+            // tol_in more)
+            const double goal = fmax(sc.tol_in2 * sc.rr0, 0.01 * sc.tol2 * sc.bb);
+            const int done = bad || w[0] <= goal || sc.iter_in >= sc.maxit_in;
+            if (done) {
+                sc.conv_in = 1;
+                atomicSub(&eg->active_in, 1);
+            }
+        } else {
+            sc.rr = w[0];
+            sc.iter += 1;
+            const int conv = bad || zero || (w[0] <= sc.tol2 * sc.bb);
+            sc.pad1 = 0;
+            const int more = !conv && sc.iter < sc.maxit;
+            if (!conv && !more) atomicOr(&eg->status, ST_PCG_MAXIT);
+            if (!more) {
+                sc.converged = 1;
+                atomicSub(&eg->active_out, 1);
             }
         }
     }
@@ -409,16 +409,20 @@ k_bs_xr(const int4* __restrict__ tiles, const BSInfo* __restrict__ info,
 }
 
 // FP64 residual r = b - A x of the tile (x staged with a one-node halo);
-// the per-thread sums of b*b and r*r; optionally the FP32 copy of r.
+// the per-thread sums of b*b (when bb) and r*r; r and its FP32 copy rin
+// where given. GB300's FP64 pipe bounds this kernel, so the Poisson operator
+// (maindiag 0) skips the main-diagonal multiply and later refinement rounds
+// skip <b, b> (both uniform branches).
 template <int TH>
 __device__ __forceinline__ void residual64(const int4& tl, const MGLevel& L,
                                            const double* __restrict__ x,
                                            const double* __restrict__ b, double* __restrict__ r,
-                                           float* __restrict__ rin, double (&w)[2])
+                                           float* __restrict__ rin, double (&w)[2], bool bb)
 {
     constexpr int H = 1, W = Reg<H, TH>::WX, N = Reg<H, TH>::N, TQ = TH / 8;
     __shared__ double sx[N];
     __shared__ uint8_t sm[N];
+    const bool helm = L.md != 0.0;
     stage_region<H, TH, double, double>(L, tl.z, tl.y, x, sx, (const double*)nullptr,
                                         (double*)nullptr, sm);
     double bv[TQ];
@@ -439,13 +443,15 @@ __device__ __forceinline__ void residual64(const int4& tl, const MGLevel& L,
         const int e = (rr + H) * W + c + H;
         double rv = 0.0;
         if (sm[e] && ok[qr]) {
-            rv = bv[qr] - apply_diff<double>(cx, cy, md, sx[e], sx[e - 1], sx[e + 1], sx[e - W],
-                                             sx[e + W]);
-            w[0] += bv[qr] * bv[qr];
+            const double c = sx[e];
+            const double ax = cx * ((sx[e - 1] - c) + (sx[e + 1] - c)) +
+                              cy * ((sx[e - W] - c) + (sx[e + W] - c));
+            rv = bv[qr] - (helm ? ax - md * c : ax);
+            if (bb) w[0] += bv[qr] * bv[qr];
             w[1] += rv * rv;
         }
         if (ok[qr]) {
-            r[k[qr]] = rv;
+            if (r) r[k[qr]] = rv;
             if (rin) rin[k[qr]] = float(rv);
         }
     }
@@ -464,7 +470,7 @@ k_bs_init(const int4* __restrict__ tiles, const BSInfo* __restrict__ info,
     DevScalars& sc = scs[tl.x];
     const MGLevel L = levs[tl.x * BS_LMAX];
     double w[2] = {0.0, 0.0};
-    residual64<TH>(tl, L, x, b, r, nullptr, w);
+    residual64<TH>(tl, L, x, b, r, nullptr, w, true);
     const BSInfo in = info[tl.x];
     const bool mine = seg_reduce2<2>(w, partials, gpart, gtick, blockIdx.x, in.n0, in.nn, in.g0, &sc.counter[1]);
     if (mine) {
@@ -500,12 +506,15 @@ k_bs_refine(const int4* __restrict__ tiles, const BSInfo* __restrict__ info,
     } else {
         const MGLevel L = levs[tl.x * BS_LMAX];
         double w[2] = {0.0, 0.0};
-        residual64<TH>(tl, L, x, b, r, rin, w);
+        // <b, b> once per solve (the first call); the FP64 residual itself is
+        // not stored (the inner solve reads its FP32 copy)
+        residual64<TH>(tl, L, x, b, nullptr, rin, w, first != 0);
         const BSInfo in = info[tl.x];
         mine = seg_reduce2<2>(w, partials, gpart, gtick, blockIdx.x, in.n0, in.nn, in.g0, &sc.counter[1]);
         if (mine) {
             const double rr_prev = sc.rr;
-            sc.bb = w[0];
+            if (first) sc.bb = w[0];
+            else w[0] = sc.bb;
             sc.rr = w[1];
             const int zero = (w[0] == 0.0);
             sc.zero = zero;
@@ -701,13 +710,13 @@ static int cg_body(BatchSolver& s, cudaStream_t st, cudaGraphConditionalHandle c
         k_bs_rz<<<s.n, 256, 0, st>>>(s.dinfo, s.scs, s.mpartials, ir);
         cnt += 1;
     }
-    k_bs_pq<S, V, TH><<<nt, blk, 0, st>>>(s.rtiles, s.dinfo, s.dlevs, (const S*)s.v.z,
-                                          (V*)s.v.p, (V*)s.v.p2, (V*)s.v.q, s.scs, s.partials,
-                                          s.gpart, s.gtick, ir);
-    k_bs_xr<V, TH><<<nt, blk, 0, st>>>(s.rtiles, s.dinfo, s.dlevs, x, r, (const V*)s.v.p,
-                                       (const V*)s.v.p2, (const V*)s.v.q, s.scs, s.partials,
-                                       s.gpart, s.gtick, s.eg, cond, ir, s.n);
-    cnt += 2;
+    k_bs_pq<S, V, TH><<<nt, blk, 0, st>>>(s.rtiles, s.dlevs, (const S*)s.v.z, (V*)s.v.p,
+                                          (V*)s.v.p2, (V*)s.v.q, s.scs, s.partials, ir);
+    k_bs_alpha<<<s.n, 256, 0, st>>>(s.dinfo, s.scs, s.partials, ir);
+    k_bs_xr<V, TH><<<nt, blk, 0, st>>>(s.rtiles, s.dlevs, x, r, (const V*)s.v.p,
+                                       (const V*)s.v.p2, (const V*)s.v.q, s.scs, s.partials, ir);
+    k_bs_conv<<<s.n, 256, 0, st>>>(s.dinfo, s.scs, s.partials, s.eg, cond, ir, s.n);
+    cnt += 4;
     s.body_launches = cnt;
     return (int)cudaGetLastError();
 }
