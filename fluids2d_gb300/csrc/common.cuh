@@ -71,6 +71,9 @@ struct DevScalars {
     // Robert-Asselin filter coefficient of the leap-frog integrator
     // (param.py:50 RAgamma, integrators.py:39-55)
     double ragamma;
+    // time step of the step whose stage increments the warm start keeps
+    // (0: none yet); the next step scales them by dt / dt_warm
+    double dt_warm;
 };
 
 // ---------------------------------------------------------------------------

@@ -69,7 +69,9 @@ __device__ __forceinline__ T* at(void* base, long long off)
 // ---- stage and diagnostics --------------------------------------------------
 struct EnsArenas {
     void *q[2], *ds1, *ds2, *Ux, *Uy, *rhs, *psi, *fv;
-    double *psi_s0, *psi_m1;  // psi at the start of this / the previous step
+    // the warm start of the stage solves (WarmArrays, stage.cuh): psi at the
+    // step start and of stage 1, the previous step's stage increments
+    double *psi_s0, *psi_p1, *psi_d1, *psi_d2;
     const uint32_t* code;
 };
 
@@ -95,6 +97,39 @@ k_ens_fluxform_stage(const int4* __restrict__ tiles, const Member* __restrict__ 
                         pout ? at<T>(pout, o) : nullptr, at<T>(pin, o), at<T>(a.ds2, o),
                         (const T*)nullptr, stage, mb.g, sc.dt, sc.ragamma, &eg->status,
                         tl.y, tl.z);
+}
+
+// Warm start of the solve of RK3 stage mode+1 (psi_warm_point, stage.cuh) on
+// every member's cells, with the member's own step-size ratio; mode 2 also
+// records the member's dt_warm (the block of its first tile).
+__global__ void k_ens_psi_warm(const int4* __restrict__ tiles, const Member* __restrict__ mem,
+                               EnsArenas a, int mode, DevScalars* scs)
+{
+    const int4 tl = tiles[blockIdx.x];
+    const Member& mb = mem[tl.x];
+    const Geom g = mb.g;
+    DevScalars& sc = scs[tl.x];
+    const bool hist = sc.dt_warm > 0.0;
+    const double rho = hist ? sc.dt / sc.dt_warm : 0.0;
+    WarmArrays w;
+    w.psi = at<double>(a.psi, mb.off);
+    w.s0 = a.psi_s0 + mb.off;
+    w.p1 = a.psi_p1 + mb.off;
+    w.d1 = a.psi_d1 + mb.off;
+    w.d2 = a.psi_d2 + mb.off;
+    const int i = tl.y + threadIdx.x;
+    if (i < g.NX) {
+#pragma unroll
+        for (int r = 0; r < FRT; ++r) {
+            const int j = tl.z + threadIdx.y + 8 * r;
+            if (j >= g.NY) break;
+            psi_warm_point(mode, w, (long long)j * g.P + i, hist, rho);
+        }
+    }
+    if (mode == 2 && tl.y == 0 && tl.z == 0) {
+        __syncthreads();  // every thread of the block has read dt_warm
+        if (threadIdx.x == 0 && threadIdx.y == 0) sc.dt_warm = sc.dt;
+    }
 }
 
 // centerstovertices (+ beta-plane term) into the FP64 right-hand side
@@ -308,9 +343,7 @@ static int ens_record_diag(f2d_ensemble_s* e, int par, cudaStream_t s, int warm 
         k_ens_c2v<float><<<e->ncell, blk, 0, s>>>(e->cell_tiles, e->dmem, e->ar, par, use_fv);
     e->rec += 1;
     if (warm >= 0) {
-        const int rw = launch_psi_warm(warm, (double*)e->ar.psi, e->ar.psi_s0, e->ar.psi_m1,
-                                       (long long)e->total, e->scs, s);
-        if (rw) return f2d_internal_fail(rw, "ensemble warm-start launch failed");
+        k_ens_psi_warm<<<e->ncell, blk, 0, s>>>(e->cell_tiles, e->dmem, e->ar, warm, e->scs);
         e->rec += 1;
     }
     int r = ens_record_solve(e, s);
@@ -491,7 +524,9 @@ int f2d_ensemble_create(const f2d_params* p, int count, const int* nxs, const in
     e->ar.rhs = A(8);
     e->ar.psi = A(8);
     e->ar.psi_s0 = (double*)A(8);
-    e->ar.psi_m1 = (double*)A(8);
+    e->ar.psi_p1 = (double*)A(8);
+    e->ar.psi_d1 = (double*)A(8);
+    e->ar.psi_d2 = (double*)A(8);
     e->ar.fv = A(8);
     e->code = A(4);
     e->gmask = A(1);
@@ -511,7 +546,8 @@ int f2d_ensemble_create(const f2d_params* p, int count, const int* nxs, const in
     e->scs = (DevScalars*)ens_alloc(e, sizeof(DevScalars) * count);
     e->eg = (EnsGlobals*)ens_alloc(e, sizeof(EnsGlobals));
     for (void* q : {e->ar.q[0], e->ar.q[1], e->ar.ds1, e->ar.ds2, e->ar.Ux, e->ar.Uy,
-                    e->ar.rhs, e->ar.psi, (void*)e->ar.psi_s0, (void*)e->ar.psi_m1,
+                    e->ar.rhs, e->ar.psi, (void*)e->ar.psi_s0, (void*)e->ar.psi_p1,
+                    (void*)e->ar.psi_d1, (void*)e->ar.psi_d2,
                     e->ar.fv, e->code, e->gmask, v.r64, v.p, v.p2, v.q, v.z, v.za,
                     v.rin, v.e, e->stage64, (void*)e->scs, (void*)e->eg})
         if (!q) return bail(f2d_internal_fail(2, "out of device memory for the ensemble"));

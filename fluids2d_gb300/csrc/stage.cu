@@ -635,42 +635,22 @@ int launch_fill_periodic(int prec, void* a, const Geom& g, cudaStream_t s)
     return (int)cudaGetLastError();
 }
 
-// Warm start of the Poisson solve of SSP-RK3 stage k (mode k-1) from the
-// streamfunctions already known, as a linear extrapolation in time (the
-// stage states approximate t+dt, t+dt/2, t+dt): mode 0, before the solve of
-// stage 1: s0 <- psi (= psi at t), and psi <- 2 psi(t) - psi(t-dt) from the
-// previous step's s0 (kept in m1) once a step has been taken; mode 1, before
-// the solve of stage 2: psi <- (psi(t) + psi(stage 1)) / 2; mode 2, before
-// the solve of stage 3: psi <- 2 psi(stage 2) - psi(t). The guess only moves
-// the solve's starting point (the solve still runs to its tolerance); it
-// cuts the starting residual by two to three orders of magnitude. `ite`
-// points at the time line whose step count tells whether a previous step
-// exists. n: elements of the arrays (every point; non-fluid points stay 0).
-__global__ void k_psi_warm(int mode, double* __restrict__ psi, double* __restrict__ s0,
-                           double* __restrict__ m1, long long n, const DevScalars* sc)
+// Warm start of the Poisson solve of SSP-RK3 stage mode+1 (psi_warm_point,
+// stage.cuh): a grid-stride loop over every element.
+__global__ void k_psi_warm(int mode, WarmArrays w, long long n, DevScalars* sc)
 {
-    const bool hist = sc->ite > 0;
+    const bool hist = sc->dt_warm > 0.0;
+    const double rho = hist ? sc->dt / sc->dt_warm : 0.0;
     for (long long k = blockIdx.x * (long long)blockDim.x + threadIdx.x; k < n;
-         k += (long long)gridDim.x * blockDim.x) {
-        const double a = psi[k];
-        if (mode == 0) {
-            const double old = s0[k];
-            m1[k] = old;
-            s0[k] = a;
-            if (hist) psi[k] = 2.0 * a - old;
-        } else if (mode == 1) {
-            psi[k] = 0.5 * (s0[k] + a);
-        } else {
-            psi[k] = 2.0 * a - s0[k];
-        }
-    }
+         k += (long long)gridDim.x * blockDim.x)
+        psi_warm_point(mode, w, k, hist, rho);
+    if (mode == 2 && blockIdx.x == 0 && threadIdx.x == 0) sc->dt_warm = sc->dt;
 }
 
-int launch_psi_warm(int mode, double* psi, double* s0, double* m1, long long n,
-                    const DevScalars* sc, cudaStream_t s)
+int launch_psi_warm(int mode, const WarmArrays& w, long long n, DevScalars* sc, cudaStream_t s)
 {
     const int nb = (int)std::min<long long>((n + 255) / 256, 152 * 8);
-    k_psi_warm<<<nb, 256, 0, s>>>(mode, psi, s0, m1, n, sc);
+    k_psi_warm<<<nb, 256, 0, s>>>(mode, w, n, sc);
     return (int)cudaGetLastError();
 }
 

@@ -53,9 +53,53 @@ int launch_maxabs2(int prec, const void* Ux, const void* Uy, const Geom& g,
                    DevScalars* sc, double* partials, cudaStream_t s);
 int launch_fill_periodic(int prec, void* a, const Geom& g, cudaStream_t s);
 int launch_set_dt(DevScalars* sc, cudaStream_t s);
-// warm start of the Poisson solve of SSP-RK3 stage mode+1 (stage.cu)
-int launch_psi_warm(int mode, double* psi, double* s0, double* m1, long long n,
-                    const DevScalars* sc, cudaStream_t s);
+// Warm start of the Poisson solve of SSP-RK3 stage mode+1. The stage states
+// are y1 = y0 + dt L1, y2 = y0 + dt/4 (L1 + L2), y3 = y0 + dt/6 (L1 + L2) +
+// 2dt/3 L3 (integrators.py:92-107, L_k the tendency at the stage's input),
+// and psi solves a linear problem in y, so with S_k = dt A^-1 B(L_k):
+// psi1 = psi0 + S1, psi2 = psi0 + (S1 + S2)/4. The guesses extrapolate the
+// S_k, not psi: S1 (the tendency at t) ~ the previous step's S2 (taken at
+// y1 ~ y(t)); S2 (at y1 ~ t+dt) ~ S1 + the previous step's S2 - S1; S3 (at
+// y2 ~ t+dt/2) ~ (S1 + S2)/2. The previous step's increments are kept as
+// d1 = 4 psi2 - 3 psi0 - psi1 = S2 and d2 = 4 psi2 - 2 psi0 - 2 psi1 = S2 - S1,
+// scaled by dt / dt_warm when the step size changed. On eulerpsi 128^2
+// (the oracle's operator) the starting relative residuals of stages 1 and
+// 2 fall from 3.8e-4 and 1.9e-4 (linear extrapolation of psi itself) to
+// 3.2e-5 and 2.0e-5; stage 3's guess, 2 psi2 - psi0, is the same in both
+// (1.3e-5). A guess only moves the solve's starting point.
+struct WarmArrays {
+    double* psi;  // in: the last solution; out: the guess
+    double* s0;   // psi at the step start
+    double* p1;   // psi of stage 1
+    double* d1;   // the previous step's increments (see above)
+    double* d2;
+};
+
+__device__ __forceinline__ void psi_warm_point(int mode, const WarmArrays& w, long long k,
+                                               bool hist, double rho)
+{
+    const double a = w.psi[k];
+    if (mode == 0) {  // a = psi0
+        w.s0[k] = a;
+        if (hist) w.psi[k] = a + rho * w.d1[k];
+    } else if (mode == 1) {  // a = psi1
+        const double s0 = w.s0[k];
+        w.p1[k] = a;
+        double g = s0 + 0.5 * (a - s0);
+        if (hist) g += 0.25 * rho * w.d2[k];
+        w.psi[k] = g;
+    } else {  // a = psi2
+        const double s0 = w.s0[k], p1 = w.p1[k];
+        w.d1[k] = (4.0 * a - 3.0 * s0) - p1;
+        w.d2[k] = (4.0 * a - 2.0 * s0) - 2.0 * p1;
+        w.psi[k] = 2.0 * a - s0;
+    }
+}
+
+// the single-model form over n elements (every point; non-fluid points
+// stay 0); mode 2 records dt_warm
+int launch_psi_warm(int mode, const WarmArrays& w, long long n, DevScalars* sc,
+                    cudaStream_t s);
 // the failure-detection test switch of the stage kernels' TMA waits, one per
 // translation unit (stage.cu, ensemble.cu)
 int tma_wait_test_set_stage(int enabled, unsigned long long limit_ns);
