@@ -93,7 +93,10 @@ struct AdjState {
     int* slot = nullptr;
     double *yb = nullptr, *d1 = nullptr, *d2 = nullptr, *d3 = nullptr;
     double *gx = nullptr, *gy = nullptr, *ubx = nullptr, *uby = nullptr;
-    double *psib = nullptr, *rb = nullptr;
+    // psib: the adjoint Poisson right-hand side; rbs[k]: the adjoint solve's
+    // solution for RK3 stage k+1, kept per stage so that each adjoint solve
+    // starts from the same stage's solution of the step after it
+    double *psib = nullptr, *rbs[3] = {nullptr, nullptr, nullptr};
     // the forward's streamfunction after every stage (slot 3n + k after
     // stage k of step n, slot 0 after the initial diagnostics), so that the
     // recompute of a segment needs no Poisson solve; used when it fits
@@ -336,8 +339,13 @@ static int rec_solve(f2d_model_s* m, int which, const void* b, void* x, cudaStre
 static int rec_warm(f2d_model_s* m, int warm, cudaStream_t s)
 {
     if (warm < 0) return 0;
-    CKI(launch_psi_warm(warm, (double*)fb(m, "psi"), (double*)fb(m, "psi.s0"),
-                        (double*)fb(m, "psi.m1"), (long long)m->g.P * m->g.NY, m->sc, s));
+    WarmArrays w;
+    w.psi = (double*)fb(m, "psi");
+    w.s0 = (double*)fb(m, "psi.s0");
+    w.p1 = (double*)fb(m, "psi.p1");
+    w.d1 = (double*)fb(m, "psi.d1");
+    w.d2 = (double*)fb(m, "psi.d2");
+    CKI(launch_psi_warm(warm, w, (long long)m->g.P * m->g.NY, m->sc, s));
     m->rec_launches += 1;
     return 0;
 }
@@ -827,9 +835,9 @@ static int rec_adj_vjp(f2d_model_s* m, int soff, const double* db, cudaStream_t 
     CKI(launch_adj_vjp_pre(m->p.compflux, m->prec, g, m->d_code, a.arena, fsz, a.slot, soff, db,
                            a.gx, a.gy, a.ubx, a.uby, m->rdx2, m->rdy2, a.psib, s));
     m->rec_launches += 2;
-    int e = rec_solve(m, 0, a.psib, a.rb, s);
+    int e = rec_solve(m, 0, a.psib, a.rbs[soff], s);
     if (e) return e;
-    CKI(launch_adj_vjp_post(g, m->d_code, a.gx, a.gy, fsz, a.rb, a.yb, s));
+    CKI(launch_adj_vjp_post(g, m->d_code, a.gx, a.gy, fsz, a.rbs[soff], a.yb, s));
     m->rec_launches += 1;
     return 0;
 }
@@ -1184,10 +1192,11 @@ int f2d_model_create(const f2d_params* p, const int8_t* msk, f2d_model* out)
     for (auto& f : fl)
         if ((e = add_field(m, f.first, f.second, is64(f.first) ? 8 : (int)m->es)))
             return bail(e);
-    // the streamfunction at the start of this and of the previous step (the
-    // warm start of the stage solves, rec_warm)
+    // the streamfunctions of this step's start and first stage and the
+    // previous step's stage increments (the warm start of the stage solves,
+    // rec_warm)
     if (p->model == F2D_MODEL_EULERPSI || p->model == F2D_MODEL_QG)
-        for (const char* f : {"psi.s0", "psi.m1"})
+        for (const char* f : {"psi.s0", "psi.p1", "psi.d1", "psi.d2"})
             if ((e = add_field(m, f, false, 8))) return bail(e);
     // qgrsw keeps the third stage's (or LFRA's) tendency too: it is
     // projected between the tendency kernel and the update
@@ -1871,7 +1880,8 @@ int f2d_adjoint_forward(f2d_model m, const double* w0, double* wT, int nsteps, d
     const Geom& g = m->g;
     const size_t fb64 = field_bytes(m, 8), fbs = field_bytes(m, m->es);
     if (!a.yb) {
-        double** v[] = {&a.yb, &a.d1, &a.d2, &a.d3, &a.ubx, &a.uby, &a.psib, &a.rb};
+        double** v[] = {&a.yb, &a.d1, &a.d2, &a.d3, &a.ubx, &a.uby, &a.psib,
+                        &a.rbs[0], &a.rbs[1], &a.rbs[2]};
         for (double** p : v)
             if (!(*p = (double*)dalloc(m, fb64))) return fail(2, "out of device memory");
         a.gx = (double*)dalloc(m, 6 * fb64);
@@ -1967,7 +1977,7 @@ int f2d_adjoint_backward(f2d_model m, const double* lamT, double* lam0)
     const size_t fbs = field_bytes(m, m->es);
     CK(cudaMemcpy2DAsync(a.yb, g.P * 8, lamT, g.NX * 8, g.NX * 8, g.NY,
                          cudaMemcpyDeviceToDevice, m->stream));
-    CK(cudaMemsetAsync(a.rb, 0, field_bytes(m, 8), m->stream));
+    for (double* r : a.rbs) CK(cudaMemsetAsync(r, 0, field_bytes(m, 8), m->stream));
     // the time step of the forward run (the model's dt may have changed)
     m->dt_const = a.dt;
     CK(cudaMemcpyAsync(&m->sc->dt, &m->dt_const, 8, cudaMemcpyHostToDevice, m->stream));
