@@ -364,7 +364,7 @@ static int rec_diag(f2d_model_s* m, int par, cudaStream_t s, int warm = -1)
         if (e) return e;
         CKI(launch_perpgrad(0, m->prec, fb(m, "psi"), fb(m, "U.x"), fb(m, "U.y"), m->d_code,
                             m->rdy2, m->rdx2, 1, g, m->sc, m->partials, s));
-        m->rec_launches += 1;
+        m->rec_launches += 2;  // perpgrad + k_umax_finish
         return 0;
     }
     case F2D_MODEL_QG: {
@@ -377,7 +377,7 @@ static int rec_diag(f2d_model_s* m, int par, cudaStream_t s, int warm = -1)
         if (e) return e;
         CKI(launch_perpgrad(0, m->prec, fb(m, "psi"), fb(m, "U.x"), fb(m, "U.y"), m->d_code,
                             m->rdy2, m->rdx2, 0, g, m->sc, m->partials, s));
-        m->rec_launches += 1;
+        m->rec_launches += 2;  // perpgrad + k_umax_finish
         return 0;
     }
     case F2D_MODEL_EULER:
@@ -777,7 +777,7 @@ static int rec_diag_cached(f2d_model_s* m, cudaStream_t s)
     CKI(launch_adj_slot(a.pslot, 1, s));
     CKI(launch_perpgrad(0, m->prec, fb(m, "psi"), fb(m, "U.x"), fb(m, "U.y"), m->d_code,
                         m->rdy2, m->rdx2, 1, m->g, m->sc, m->partials, s));
-    m->rec_launches += 3;
+    m->rec_launches += 4;
     return 0;
 }
 

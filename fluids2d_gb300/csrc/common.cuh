@@ -262,94 +262,6 @@ __device__ __forceinline__ bool grid_reduce(double (&v)[N], double* partials,
     return false;
 }
 
-// Segmented reduction: the blocks t0 .. t0+nt-1 of a launch form one segment
-// (one member of a batch) with its own ticket; true in thread 0 of the last
-// block of the segment, which holds the segment's result in `v`.
-template <int N, bool MAX, bool PRE = false>
-__device__ __forceinline__ bool seg_reduce(double (&v)[N], double* partials, int tile,
-                                           int t0, int nt, unsigned int* ticket)
-{
-    __shared__ double sh[32 * N];
-    __shared__ int s_last;
-    if (!PRE) block_reduce<N, MAX>(v, sh);
-    const int tid = threadIdx.y * blockDim.x + threadIdx.x;
-    if (tid == 0) {
-#pragma unroll
-        for (int k = 0; k < N; ++k) partials[(size_t)tile * N + k] = v[k];
-        __threadfence();
-        const unsigned prev = atomicAdd(ticket, 1u);
-        s_last = (prev == (unsigned)nt - 1);
-    }
-    __syncthreads();
-    if (!s_last) return false;
-    __threadfence();
-    double acc[N];
-    final_sum<N, MAX>(acc, partials, t0, nt, tid, blockDim.x * blockDim.y);
-    block_reduce<N, MAX>(acc, sh);
-    if (tid == 0) {
-#pragma unroll
-        for (int k = 0; k < N; ++k) v[k] = acc[k];
-        *ticket = 0;
-        return true;
-    }
-    return false;
-}
-
-// Two-level segmented reduction: the tiles n0 .. n0+nn-1 of one segment are
-// grouped by 64; the last tile of a group sums the group's partials, the last
-// group of the segment sums the group sums. Same-address atomics stay at <= 64
-// per ticket whatever the segment size; the summation order is fixed.
-constexpr int RED_GROUP = 64;
-
-template <int N, bool PRE = false>
-__device__ __forceinline__ bool seg_reduce2(double (&v)[N], double* tpart, double* gpart,
-                                            unsigned int* gtick, int tile, int n0, int nn,
-                                            int g0, unsigned int* ticket)
-{
-    __shared__ double sh[32 * N];
-    __shared__ int s_last;
-    if (!PRE) block_reduce<N, false>(v, sh);  // PRE: v already the block total in thread 0
-    const int tid = threadIdx.y * blockDim.x + threadIdx.x;
-    const int nth = blockDim.x * blockDim.y;
-    const int lt = tile - n0, g = lt / RED_GROUP;
-    const int gbeg = g * RED_GROUP, gsz = min(RED_GROUP, nn - gbeg);
-    const int ng = (nn + RED_GROUP - 1) / RED_GROUP;
-    if (tid == 0) {
-#pragma unroll
-        for (int k = 0; k < N; ++k) tpart[(size_t)tile * N + k] = v[k];
-        __threadfence();
-        s_last = (atomicAdd(&gtick[g0 + g], 1u) == (unsigned)gsz - 1);
-    }
-    __syncthreads();
-    if (!s_last) return false;
-    __threadfence();
-    double acc[N];
-#pragma unroll
-    for (int k = 0; k < N; ++k)
-        acc[k] = tid < gsz ? __ldcg(&tpart[(size_t)(n0 + gbeg + tid) * N + k]) : 0.0;
-    (void)nth;
-    block_reduce<N, false>(acc, sh);
-    if (tid == 0) {
-#pragma unroll
-        for (int k = 0; k < N; ++k) gpart[(size_t)(g0 + g) * N + k] = acc[k];
-        gtick[g0 + g] = 0;
-        __threadfence();
-        s_last = (atomicAdd(ticket, 1u) == (unsigned)ng - 1);
-    }
-    __syncthreads();
-    if (!s_last) return false;
-    __threadfence();
-    final_sum<N, false>(acc, gpart, g0, ng, tid, nth);
-    block_reduce<N, false>(acc, sh);
-    if (tid == 0) {
-#pragma unroll
-        for (int k = 0; k < N; ++k) v[k] = acc[k];
-        *ticket = 0;
-        return true;
-    }
-    return false;
-}
-
 // Block total of per-thread FP32 values: warp sums in FP32 (shuffles), the
 // warp sums combined in FP64 by thread 0 in a fixed order. Result in thread 0.
 template <int N, bool MAX = false>

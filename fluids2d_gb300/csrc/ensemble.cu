@@ -100,15 +100,17 @@ k_ens_fluxform_stage(const int4* __restrict__ tiles, const Member* __restrict__ 
 }
 
 // Warm start of the solve of RK3 stage mode+1 (psi_warm_point, stage.cuh) on
-// every member's cells, with the member's own step-size ratio; mode 2 also
-// records the member's dt_warm (the block of its first tile).
-__global__ void k_ens_psi_warm(const int4* __restrict__ tiles, const Member* __restrict__ mem,
-                               EnsArenas a, int mode, DevScalars* scs)
+// every member's array (all P x NY elements: the pads are 0 and stay 0),
+// with the member's own step-size ratio: blockIdx.y is the member, the
+// blocks of a member stride over its elements two at a time (the member
+// arrays start 32-element aligned, P is even). Mode 2 also records the
+// member's dt_warm (block 0 of the member; mode 2 reads no dt_warm).
+__global__ void __launch_bounds__(256) k_ens_psi_warm(const Member* __restrict__ mem,
+                                                       EnsArenas a, int mode, DevScalars* scs)
 {
-    const int4 tl = tiles[blockIdx.x];
-    const Member& mb = mem[tl.x];
+    const Member& mb = mem[blockIdx.y];
     const Geom g = mb.g;
-    DevScalars& sc = scs[tl.x];
+    DevScalars& sc = scs[blockIdx.y];
     const bool hist = sc.dt_warm > 0.0;
     const double rho = hist ? sc.dt / sc.dt_warm : 0.0;
     WarmArrays w;
@@ -117,19 +119,13 @@ __global__ void k_ens_psi_warm(const int4* __restrict__ tiles, const Member* __r
     w.p1 = a.psi_p1 + mb.off;
     w.d1 = a.psi_d1 + mb.off;
     w.d2 = a.psi_d2 + mb.off;
-    const int i = tl.y + threadIdx.x;
-    if (i < g.NX) {
-#pragma unroll
-        for (int r = 0; r < FRT; ++r) {
-            const int j = tl.z + threadIdx.y + 8 * r;
-            if (j >= g.NY) break;
-            psi_warm_point(mode, w, (long long)j * g.P + i, hist, rho);
-        }
+    const long long n = g.P * (long long)g.NY;
+    for (long long k = 2 * ((long long)blockIdx.x * blockDim.x + threadIdx.x); k < n;
+         k += 2ll * gridDim.x * blockDim.x) {
+        psi_warm_point(mode, w, k, hist, rho);
+        psi_warm_point(mode, w, k + 1, hist, rho);
     }
-    if (mode == 2 && tl.y == 0 && tl.z == 0) {
-        __syncthreads();  // every thread of the block has read dt_warm
-        if (threadIdx.x == 0 && threadIdx.y == 0) sc.dt_warm = sc.dt;
-    }
+    if (mode == 2 && blockIdx.x == 0 && threadIdx.x == 0) sc.dt_warm = sc.dt;
 }
 
 // centerstovertices (+ beta-plane term) into the FP64 right-hand side
@@ -197,13 +193,38 @@ __global__ void k_ens_perpgrad(const int4* __restrict__ tiles, const Member* __r
             m[1] = nanmax(m[1], fabs(uy));
         }
     }
-    DevScalars& sc = scs[tl.x];
+    // the tile's maxima only (no fence or ticket: k_ens_umax combines a
+    // member's tiles)
+    (void)scs;
     double w[2];
-    block_pre<2, true>(m, w);
-    if (seg_reduce<2, true, std::is_same<T, float>::value>(w, partials, blockIdx.x, mb.t0,
-                                                           mb.nt, &sc.counter[0])) {
-        sc.maxUx = w[0];
-        sc.maxUy = w[1];
+    if constexpr (std::is_same<T, float>::value) {
+        block_total_f<2, true>(m, w);
+    } else {
+        __shared__ double sh[64];
+        w[0] = m[0];
+        w[1] = m[1];
+        block_reduce<2, true>(w, sh);
+    }
+    if (threadIdx.x == 0 && threadIdx.y == 0) {
+        partials[2 * (size_t)blockIdx.x] = w[0];
+        partials[2 * (size_t)blockIdx.x + 1] = w[1];
+    }
+}
+
+// every member's max|U.x|, max|U.y| from k_ens_perpgrad's tile maxima (the
+// member's tiles t0 .. t0+nt), one block per member; NaN propagates
+__global__ void __launch_bounds__(256) k_ens_umax(const Member* __restrict__ mem,
+                                                   DevScalars* scs,
+                                                   const double* __restrict__ partials)
+{
+    const Member& mb = mem[blockIdx.x];
+    double acc[2];
+    final_sum<2, true>(acc, partials, mb.t0, mb.nt, threadIdx.x, blockDim.x);
+    __shared__ double sh[64];
+    block_reduce<2, true>(acc, sh);
+    if (threadIdx.x == 0) {
+        scs[blockIdx.x].maxUx = acc[0];
+        scs[blockIdx.x].maxUy = acc[1];
     }
 }
 
@@ -343,7 +364,7 @@ static int ens_record_diag(f2d_ensemble_s* e, int par, cudaStream_t s, int warm 
         k_ens_c2v<float><<<e->ncell, blk, 0, s>>>(e->cell_tiles, e->dmem, e->ar, par, use_fv);
     e->rec += 1;
     if (warm >= 0) {
-        k_ens_psi_warm<<<e->ncell, blk, 0, s>>>(e->cell_tiles, e->dmem, e->ar, warm, e->scs);
+        k_ens_psi_warm<<<dim3(48, e->n), 256, 0, s>>>(e->dmem, e->ar, warm, e->scs);
         e->rec += 1;
     }
     int r = ens_record_solve(e, s);
@@ -355,7 +376,8 @@ static int ens_record_diag(f2d_ensemble_s* e, int par, cudaStream_t s, int warm 
     else
         k_ens_perpgrad<float><<<e->ncell, blk, 0, s>>>(e->cell_tiles, e->dmem, e->ar, fillU,
                                                        e->scs, e->partials);
-    e->rec += 1;
+    k_ens_umax<<<e->n, 256, 0, s>>>(e->dmem, e->scs, e->partials);
+    e->rec += 2;
     ECK(cudaGetLastError());
     return 0;
 }

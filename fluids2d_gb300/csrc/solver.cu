@@ -409,20 +409,21 @@ k_bs_conv(const BSInfo* __restrict__ info, DevScalars* scs, const double* __rest
 }
 
 // FP64 residual r = b - A x of the tile (x staged with a one-node halo);
-// the per-thread sums of b*b (when bb) and r*r; r and its FP32 copy rin
-// where given. GB300's FP64 pipe bounds this kernel, so the Poisson operator
-// (maindiag 0) skips the main-diagonal multiply and later refinement rounds
-// skip <b, b> (both uniform branches).
-template <int TH>
+// the per-thread sums of b*b (BB) and r*r; r and its FP32 copy rin where
+// given. GB300 runs FP64 at 1/64 of its FP32 rate and this is the FP64
+// kernel of the FP32 form, so the variants are compile-time (a runtime
+// select would issue both sides): HELM, an operator with a main-diagonal
+// term (maindiag != 0; exact for members without one too); UNIT, square
+// cells (cx = cy = 1: the same sums without the multiplies).
+template <int TH, bool HELM, bool UNIT, bool BB>
 __device__ __forceinline__ void residual64(const int4& tl, const MGLevel& L,
                                            const double* __restrict__ x,
                                            const double* __restrict__ b, double* __restrict__ r,
-                                           float* __restrict__ rin, double (&w)[2], bool bb)
+                                           float* __restrict__ rin, double (&w)[2])
 {
     constexpr int H = 1, W = Reg<H, TH>::WX, N = Reg<H, TH>::N, TQ = TH / 8;
     __shared__ double sx[N];
     __shared__ uint8_t sm[N];
-    const bool helm = L.md != 0.0;
     stage_region<H, TH, double, double>(L, tl.z, tl.y, x, sx, (const double*)nullptr,
                                         (double*)nullptr, sm);
     double bv[TQ];
@@ -444,10 +445,14 @@ __device__ __forceinline__ void residual64(const int4& tl, const MGLevel& L,
         double rv = 0.0;
         if (sm[e] && ok[qr]) {
             const double c = sx[e];
-            const double ax = cx * ((sx[e - 1] - c) + (sx[e + 1] - c)) +
-                              cy * ((sx[e - W] - c) + (sx[e + W] - c));
-            rv = bv[qr] - (helm ? ax - md * c : ax);
-            if (bb) w[0] += bv[qr] * bv[qr];
+            const double sxw = (sx[e - 1] - c) + (sx[e + 1] - c);
+            const double syw = (sx[e - W] - c) + (sx[e + W] - c);
+            double ax;
+            if constexpr (UNIT) ax = sxw + syw;
+            else ax = cx * sxw + cy * syw;
+            if constexpr (HELM) ax = ax - md * c;
+            rv = bv[qr] - ax;
+            if constexpr (BB) w[0] += bv[qr] * bv[qr];
             w[1] += rv * rv;
         }
         if (ok[qr]) {
@@ -458,21 +463,38 @@ __device__ __forceinline__ void residual64(const int4& tl, const MGLevel& L,
 }
 
 // FP64 form: r = b - A x, <b,b>, <r,r>, per-member start state
-template <int TH>
+template <int TH, bool HELM, bool UNIT>
 __global__ void __launch_bounds__(256)
-k_bs_init(const int4* __restrict__ tiles, const BSInfo* __restrict__ info,
-          const MGLevel* __restrict__ levs, const double* __restrict__ x,
-          const double* __restrict__ b, double* __restrict__ r, DevScalars* scs,
-          double* partials, double* gpart, unsigned int* gtick, BSGlobals* eg,
-          cudaGraphConditionalHandle cond, int nmem)
+k_bs_init(const int4* __restrict__ tiles, const MGLevel* __restrict__ levs,
+          const double* __restrict__ x, const double* __restrict__ b, double* __restrict__ r,
+          double* partials)
 {
     const int4 tl = tiles[blockIdx.x];
-    DevScalars& sc = scs[tl.x];
     const MGLevel L = levs[tl.x * BS_LMAX];
     double w[2] = {0.0, 0.0};
-    residual64<TH>(tl, L, x, b, r, nullptr, w, true);
-    const BSInfo in = info[tl.x];
-    const bool mine = seg_reduce2<2>(w, partials, gpart, gtick, blockIdx.x, in.n0, in.nn, in.g0, &sc.counter[1]);
+    residual64<TH, HELM, UNIT, true>(tl, L, x, b, r, nullptr, w);
+    __shared__ double sh[64];
+    block_reduce<2, false>(w, sh);
+    if (threadIdx.x == 0 && threadIdx.y == 0) {
+        partials[2 * (size_t)blockIdx.x] = w[0];
+        partials[2 * (size_t)blockIdx.x + 1] = w[1];
+    }
+}
+
+// FP64 form, per member from k_bs_init's tile sums: <b,b>, <r,r>, the start
+// state of the solve; the loop condition (the block completing the count)
+__global__ void __launch_bounds__(256)
+k_bs_init_fin(const BSInfo* __restrict__ info, DevScalars* scs,
+              const double* __restrict__ tpart, BSGlobals* eg,
+              cudaGraphConditionalHandle cond, int nmem)
+{
+    const BSInfo in = info[blockIdx.x];
+    DevScalars& sc = scs[blockIdx.x];
+    double w[2];
+    final_sum<2, false>(w, tpart, in.n0, in.nn, threadIdx.x, blockDim.x);
+    __shared__ double sh[64];
+    block_reduce<2, false>(w, sh);
+    const bool mine = threadIdx.x == 0;
     if (mine) {
         sc.bb = w[0];
         sc.rr = w[1];
@@ -488,61 +510,78 @@ k_bs_init(const int4* __restrict__ tiles, const BSInfo* __restrict__ info,
     }
 }
 
-// Refinement form: r64 = b - A x (FP64), the FP32 copy that drives the next
-// inner solve, <b,b> and <r,r>; per member: converged, or start a new round.
-template <int TH>
+// Refinement form: r = b - A x (FP64) of the tile, its FP32 copy that drives
+// the next inner solve, and the tile's sums of b*b (first call of a solve)
+// and r*r; members already converged are skipped.
+template <int TH, bool HELM, bool UNIT, bool FIRST>
 __global__ void __launch_bounds__(256)
-k_bs_refine(const int4* __restrict__ tiles, const BSInfo* __restrict__ info,
-            const MGLevel* __restrict__ levs, const double* __restrict__ x,
-            const double* __restrict__ b, double* __restrict__ r, float* __restrict__ rin,
-            DevScalars* scs, double* partials, double* gpart, unsigned int* gtick,
-            BSGlobals* eg, int first, cudaGraphConditionalHandle cond, int nmem)
+k_bs_refine(const int4* __restrict__ tiles, const MGLevel* __restrict__ levs,
+            const double* __restrict__ x, const double* __restrict__ b,
+            float* __restrict__ rin, const DevScalars* __restrict__ scs, double* partials)
 {
     const int4 tl = tiles[blockIdx.x];
-    DevScalars& sc = scs[tl.x];
-    bool mine = false;
-    if (sc.converged) {
-        mine = threadIdx.x == 0 && threadIdx.y == 0 && (int)blockIdx.x == info[tl.x].n0;
-    } else {
-        const MGLevel L = levs[tl.x * BS_LMAX];
-        double w[2] = {0.0, 0.0};
-        // <b, b> once per solve (the first call); the FP64 residual itself is
-        // not stored (the inner solve reads its FP32 copy)
-        residual64<TH>(tl, L, x, b, nullptr, rin, w, first != 0);
-        const BSInfo in = info[tl.x];
-        mine = seg_reduce2<2>(w, partials, gpart, gtick, blockIdx.x, in.n0, in.nn, in.g0, &sc.counter[1]);
-        if (mine) {
-            const double rr_prev = sc.rr;
-            if (first) sc.bb = w[0];
-            else w[0] = sc.bb;
-            sc.rr = w[1];
-            const int zero = (w[0] == 0.0);
-            sc.zero = zero;
-            int conv = zero ? (w[1] == 0.0) : (w[1] <= sc.tol2 * w[0]);
-            // the FP64 residual of a round cannot fall below its rounding
-            // floor (about eps * cond(A) relative); a round that no longer
-            // reduces it by 10x has reached that floor
-            if (!first && !conv && w[1] > 0.01 * rr_prev) conv = 1;
-            if (!(w[1] == w[1])) {
-                conv = 1;
-                atomicOr(&eg->status, ST_NONFINITE);
-            }
-            if (!first) {
-                sc.outer += 1;
-                sc.total_outer += 1;
-            }
-            if (!conv && sc.outer >= sc.maxouter) {
-                conv = 1;
-                atomicOr(&eg->status, ST_PCG_MAXIT);
-            }
-            sc.converged = conv;
-            if (!conv) {
-                atomicAdd(&eg->active_out, 1);
-                sc.iter_in = 0;
-                sc.rr0 = w[1];
-                sc.conv_in = zero ? 1 : 0;
-                if (!zero) atomicAdd(&eg->active_in, 1);
-            }
+    if (scs[tl.x].converged) return;
+    const MGLevel L = levs[tl.x * BS_LMAX];
+    double w[2] = {0.0, 0.0};
+    // <b, b> once per solve (the first call); the FP64 residual itself is
+    // not stored (the inner solve reads its FP32 copy)
+    residual64<TH, HELM, UNIT, FIRST>(tl, L, x, b, nullptr, rin, w);
+    __shared__ double sh[64];
+    block_reduce<2, false>(w, sh);
+    if (threadIdx.x == 0 && threadIdx.y == 0) {
+        partials[2 * (size_t)blockIdx.x] = w[0];
+        partials[2 * (size_t)blockIdx.x + 1] = w[1];
+    }
+}
+
+// Refinement form, per member from k_bs_refine's tile sums: converged, or
+// start a new round; the outer loop condition.
+__global__ void __launch_bounds__(256)
+k_bs_refine_fin(const BSInfo* __restrict__ info, DevScalars* scs,
+                const double* __restrict__ tpart, BSGlobals* eg, int first,
+                cudaGraphConditionalHandle cond, int nmem)
+{
+    const BSInfo in = info[blockIdx.x];
+    DevScalars& sc = scs[blockIdx.x];
+    const bool skip = sc.converged != 0;
+    double w[2] = {0.0, 0.0};
+    if (!skip) {
+        final_sum<2, false>(w, tpart, in.n0, in.nn, threadIdx.x, blockDim.x);
+        __shared__ double sh[64];
+        block_reduce<2, false>(w, sh);
+    }
+    const bool mine = threadIdx.x == 0;
+    if (mine && !skip) {
+        const double rr_prev = sc.rr;
+        if (first) sc.bb = w[0];
+        else w[0] = sc.bb;
+        sc.rr = w[1];
+        const int zero = (w[0] == 0.0);
+        sc.zero = zero;
+        int conv = zero ? (w[1] == 0.0) : (w[1] <= sc.tol2 * w[0]);
+        // the FP64 residual of a round cannot fall below its rounding floor
+        // (about eps * cond(A) relative); a round that no longer reduces it
+        // by 10x has reached that floor
+        if (!first && !conv && w[1] > 0.01 * rr_prev) conv = 1;
+        if (!(w[1] == w[1])) {
+            conv = 1;
+            atomicOr(&eg->status, ST_NONFINITE);
+        }
+        if (!first) {
+            sc.outer += 1;
+            sc.total_outer += 1;
+        }
+        if (!conv && sc.outer >= sc.maxouter) {
+            conv = 1;
+            atomicOr(&eg->status, ST_PCG_MAXIT);
+        }
+        sc.converged = conv;
+        if (!conv) {
+            atomicAdd(&eg->active_out, 1);
+            sc.iter_in = 0;
+            sc.rr0 = w[1];
+            sc.conv_in = zero ? 1 : 0;
+            if (!zero) atomicAdd(&eg->active_in, 1);
         }
     }
     if (members_done(mine, &eg->ticket[0], nmem)) {
@@ -648,7 +687,7 @@ static int vcycle_pipe(BatchSolver& s, cudaStream_t st, int ir)
             s.mtiles[l], n, s.dlevs, maps, l, s.scs, ir, status);
         cnt += 1;
     }
-    k_bs_tail<float><<<s.n, 1024, s.tail_smem, st>>>(s.dinfo, s.dlevs, s.scs, ir, NU);
+    k_bs_tail<float><<<s.n, s.tail_threads, s.tail_smem, st>>>(s.dinfo, s.dlevs, s.scs, ir, NU);
     cnt += 1;
     for (int l = s.maxl - 1; l >= 0; --l) {
         const int n = s.nmtiles[l];
@@ -676,7 +715,7 @@ static int vcycle_nu(BatchSolver& s, cudaStream_t st, int ir)
                                                        s.scs, ir);
         cnt += 1;
     }
-    k_bs_tail<S><<<s.n, 1024, s.tail_smem, st>>>(s.dinfo, s.dlevs, s.scs, ir, NU);
+    k_bs_tail<S><<<s.n, s.tail_threads, s.tail_smem, st>>>(s.dinfo, s.dlevs, s.scs, ir, NU);
     cnt += 1;
     for (int l = s.maxl - 1; l >= 1; --l) {
         k_mg_up<S, NU, false><<<s.nmtiles[l], blk, 0, st>>>(s.mtiles[l], s.dinfo, s.dlevs, l,
@@ -729,6 +768,43 @@ static int read_globals(const BatchSolver& s, cudaStream_t st, BSGlobals* h)
     return (int)e;
 }
 
+// the FP64 residual kernels in the solver's operator variant (bs_build:
+// helm = a member has a main-diagonal term, unit = every member has square
+// cells)
+template <int TH, bool FIRST>
+static void launch_refine(const BatchSolver& s, cudaStream_t st)
+{
+    const dim3 blk(32, 8);
+    const int nt = s.nrtiles;
+    const double* x = (const double*)s.v.x64;
+    const double* b = (const double*)s.v.b64;
+    float* rin = (float*)s.v.rin;
+    if (s.helm) {
+        if (s.unit) k_bs_refine<TH, true, true, FIRST><<<nt, blk, 0, st>>>(s.rtiles, s.dlevs, x, b, rin, s.scs, s.partials);
+        else k_bs_refine<TH, true, false, FIRST><<<nt, blk, 0, st>>>(s.rtiles, s.dlevs, x, b, rin, s.scs, s.partials);
+    } else {
+        if (s.unit) k_bs_refine<TH, false, true, FIRST><<<nt, blk, 0, st>>>(s.rtiles, s.dlevs, x, b, rin, s.scs, s.partials);
+        else k_bs_refine<TH, false, false, FIRST><<<nt, blk, 0, st>>>(s.rtiles, s.dlevs, x, b, rin, s.scs, s.partials);
+    }
+}
+
+template <int TH>
+static void launch_init(const BatchSolver& s, cudaStream_t st)
+{
+    const dim3 blk(32, 8);
+    const int nt = s.nrtiles;
+    const double* x = (const double*)s.v.x64;
+    const double* b = (const double*)s.v.b64;
+    double* r = (double*)s.v.r64;
+    if (s.helm) {
+        if (s.unit) k_bs_init<TH, true, true><<<nt, blk, 0, st>>>(s.rtiles, s.dlevs, x, b, r, s.partials);
+        else k_bs_init<TH, true, false><<<nt, blk, 0, st>>>(s.rtiles, s.dlevs, x, b, r, s.partials);
+    } else {
+        if (s.unit) k_bs_init<TH, false, true><<<nt, blk, 0, st>>>(s.rtiles, s.dlevs, x, b, r, s.partials);
+        else k_bs_init<TH, false, false><<<nt, blk, 0, st>>>(s.rtiles, s.dlevs, x, b, r, s.partials);
+    }
+}
+
 template <int TH>
 static int bs_record_t(BatchSolver& s, cudaStream_t st, cudaStream_t st2, int* launches)
 {
@@ -752,10 +828,9 @@ static int bs_record_t(BatchSolver& s, cudaStream_t st, cudaStream_t st2, int* l
             e = cudaGraphConditionalHandleCreate(&cond, graph, 1, cudaGraphCondAssignDefault);
             if (e != cudaSuccess) return (int)e;
         }
-        k_bs_init<TH><<<nt, blk, 0, st>>>(s.rtiles, s.dinfo, s.dlevs, (const double*)s.v.x64,
-                                      (const double*)s.v.b64, (double*)s.v.r64, s.scs,
-                                      s.partials, s.gpart, s.gtick, s.eg, cond, s.n);
-        fixed += 1;
+        launch_init<TH>(s, st);
+        k_bs_init_fin<<<s.n, 256, 0, st>>>(s.dinfo, s.scs, s.partials, s.eg, cond, s.n);
+        fixed += 2;
         if (capturing) {
             int r = add_while(st, st2, &cond, 1, [&](cudaStream_t sb) {
                 return cg_body<double, double, TH>(s, sb, cond, 0);
@@ -784,19 +859,15 @@ static int bs_record_t(BatchSolver& s, cudaStream_t st, cudaStream_t st2, int* l
         if (e != cudaSuccess) return (int)e;
     }
     k_bs_reset<<<1, 1, 0, st>>>(s.eg);
-    k_bs_refine<TH><<<nt, blk, 0, st>>>(s.rtiles, s.dinfo, s.dlevs, (const double*)s.v.x64,
-                                    (const double*)s.v.b64, (double*)s.v.r64, (float*)s.v.rin,
-                                    s.scs, s.partials, s.gpart, s.gtick, s.eg, 1, cond_o,
-                                    s.n);
-    fixed += 2;
+    launch_refine<TH, true>(s, st);
+    k_bs_refine_fin<<<s.n, 256, 0, st>>>(s.dinfo, s.scs, s.partials, s.eg, 1, cond_o, s.n);
+    fixed += 3;
     auto round_tail = [&](cudaStream_t sb) {
         k_bs_correct<TH><<<nt, blk, 0, sb>>>(s.rtiles, s.dlevs, (double*)s.v.x64,
                                          (const float*)s.v.e, s.scs);
         k_bs_reset<<<1, 1, 0, sb>>>(s.eg);
-        k_bs_refine<TH><<<nt, blk, 0, sb>>>(s.rtiles, s.dinfo, s.dlevs, (const double*)s.v.x64,
-                                        (const double*)s.v.b64, (double*)s.v.r64,
-                                        (float*)s.v.rin, s.scs, s.partials, s.gpart, s.gtick,
-                                        s.eg, 0, cond_o, s.n);
+        launch_refine<TH, false>(s, sb);
+        k_bs_refine_fin<<<s.n, 256, 0, sb>>>(s.dinfo, s.scs, s.partials, s.eg, 0, cond_o, s.n);
     };
     if (capturing) {
         int r = add_while(st, st2, &cond_o, 1, [&](cudaStream_t sb) {
@@ -1092,7 +1163,8 @@ int bs_build(BatchSolver& s, const std::vector<BSMemberDesc>& members, const uin
     }
     const int TH = s.th;
     // Tile table of 32 x TH level-0 nodes for the Krylov kernels (all
-    // members) with the members' reduction groups of RED_GROUP tiles. Tiles
+    // members; member b's tiles n0 .. n0+nn, whose per-tile sums the
+    // member's finishing kernels add up). Tiles
     // without a fluid node are left out (their nodes stay 0 in every
     // vector), but every member keeps at least one tile for its reductions.
     auto has_fluid = [&](int b, int l, int J0, int I0) {
@@ -1105,7 +1177,6 @@ int bs_build(BatchSolver& s, const std::vector<BSMemberDesc>& members, const uin
     };
     std::vector<std::vector<int4>> tiles(1);
     std::vector<int4>& rt = tiles[0];
-    int ngroups = 0;
     for (int b = 0; b < s.n; ++b) {
         const MGLevel& L = levs[(size_t)b * BS_LMAX];
         info[b].n0 = (int)rt.size();
@@ -1114,8 +1185,6 @@ int bs_build(BatchSolver& s, const std::vector<BSMemberDesc>& members, const uin
                 if (has_fluid(b, 0, J0, I0)) rt.push_back(make_int4(b, I0, J0, 0));
         if ((int)rt.size() == info[b].n0) rt.push_back(make_int4(b, 0, 0, 0));
         info[b].nn = (int)rt.size() - info[b].n0;
-        info[b].g0 = ngroups;
-        ngroups += (info[b].nn + RED_GROUP - 1) / RED_GROUP;
     }
     // Tile tables of the multigrid level kernels (MR_TW x MR_TH nodes,
     // register-blocked, mg_reg.cuh) for every grid level below a member's
@@ -1190,12 +1259,23 @@ int bs_build(BatchSolver& s, const std::vector<BSMemberDesc>& members, const uin
     s.partials = (double*)dal((rt.size() * 2 + 64) * sizeof(double));
     s.mpartials = (double*)dal((mt[0].size() + 64) * sizeof(double));
     if (!s.mpartials) return 2;
-    s.gpart = (double*)dal(((size_t)ngroups * 2 + 64) * sizeof(double));
-    s.gtick = (unsigned int*)dal(((size_t)ngroups + 64) * sizeof(unsigned int));
-    if (!s.gpart || !s.gtick ||
-        cudaMemset(s.gtick, 0, ((size_t)ngroups + 64) * sizeof(unsigned int)) != cudaSuccess)
-        return 2;
     if (!s.dlevs || !s.dinfo || !s.eg || !s.partials) return 2;
+    // operator variant of the FP64 residual kernels
+    s.helm = false;
+    s.unit = true;
+    for (int b = 0; b < s.n; ++b) {
+        const MGLevel& L = levs[(size_t)b * BS_LMAX];
+        if (L.md != 0.0) s.helm = true;
+        if (!(L.cx == 1.0 && L.cy == 1.0)) s.unit = false;
+    }
+    // the tail's block: 1024 threads while every member has an SM of its own,
+    // else 512 (two blocks per SM: the members' tails run in one wave)
+    {
+        int dev = 0, nsm = 0;
+        cudaGetDevice(&dev);
+        cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
+        s.tail_threads = s.n > nsm ? 512 : 1024;
+    }
     {
         const int e = bs_pipe_setup(s, levs, info, dal);
         if (e) return e;

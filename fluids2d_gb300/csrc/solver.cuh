@@ -14,7 +14,7 @@ constexpr int BS_TW = 32;  // node tile: 32 columns x 32 or 64 rows, 32 x 8 thre
 struct BSInfo {
     int nl, ltail, ksweeps;  // levels, first tail level, coarsest sweeps
     int n0, nn;              // range of the member in the level-0 tile table
-    int g0;                  // first reduction group of the member
+    int pad2;
     // the member's range in the level-0 table of the multigrid level kernels
     // (the tile totals of <r, z> written by the level-0 up leg); mnn = 0 when
     // level 0 is in the member's tail
@@ -78,10 +78,10 @@ struct BatchSolver {
     int pipe_gdown = 0, pipe_gup = 0;
     int4* rtiles = nullptr;    // level-0 tiles of the Krylov kernels
     int nrtiles = 0;
-    double* gpart = nullptr;   // group sums of the two-level reductions
-    unsigned int* gtick = nullptr;
     int maxl = 0;
     size_t tail_smem = 0;
+    int tail_threads = 1024;  // block size of k_bs_tail (bs_build)
+    bool helm = false, unit = false;  // FP64 residual variant (bs_build)
     BSVecs v;
     double tol = 1e-12, tol_in = 1e-6;
     int maxit = 200, maxit_in = 30, maxouter = 20;

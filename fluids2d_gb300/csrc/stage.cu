@@ -415,12 +415,34 @@ __global__ void k_perpgrad(const P* __restrict__ psi, T* __restrict__ Ux,
             m[1] = nanmax(m[1], fabs(uy));
         }
     }
-    constexpr bool F = std::is_same<T, float>::value;
+    // the block's maxima only (no fence or ticket: k_umax_finish combines)
     double w[2];
-    block_pre<2, true>(m, w);
-    if (grid_reduce<2, true, F>(w, partials, &sc->counter[0])) {
-        sc->maxUx = w[0];
-        sc->maxUy = w[1];
+    if constexpr (std::is_same<T, float>::value) {
+        block_total_f<2, true>(m, w);
+    } else {
+        __shared__ double sh[64];
+        w[0] = m[0];
+        w[1] = m[1];
+        block_reduce<2, true>(w, sh);
+    }
+    if (threadIdx.x == 0 && threadIdx.y == 0) {
+        const size_t b = (size_t)blockIdx.y * gridDim.x + blockIdx.x;
+        partials[2 * b] = w[0];
+        partials[2 * b + 1] = w[1];
+    }
+}
+
+// max|U.x|, max|U.y| from k_perpgrad's nb block maxima (NaN propagates)
+__global__ void __launch_bounds__(256) k_umax_finish(const double* __restrict__ partials,
+                                                      int nb, DevScalars* sc)
+{
+    double acc[2];
+    final_sum<2, true>(acc, partials, 0, nb, threadIdx.x, blockDim.x);
+    __shared__ double sh[64];
+    block_reduce<2, true>(acc, sh);
+    if (threadIdx.x == 0) {
+        sc->maxUx = acc[0];
+        sc->maxUy = acc[1];
     }
 }
 
@@ -598,6 +620,7 @@ int launch_perpgrad(int prec_psi, int prec_U, const void* psi, void* Ux, void* U
         k_perpgrad<float, float><<<gr, bl, 0, s>>>((const float*)psi, (float*)Ux,
                                                    (float*)Uy, code, rdy2, rdx2, fillU, g,
                                                    sc, partials);
+    k_umax_finish<<<1, 256, 0, s>>>(partials, (int)(gr.x * gr.y), sc);
     return (int)cudaGetLastError();
 }
 
