@@ -764,6 +764,62 @@ def test_ensemble_fields_all_members_roundtrip():
             np.testing.assert_array_equal(psi[b], e.get_field(b, "psi"))
 
 
+def test_ensemble_fields_pinned():
+    """The packed all-members I/O with pinned host buffers (the bench's
+    end-to-end path) gives the pageable path's result."""
+    import ctypes
+    members = [wl.eulerpsi_case(n=40, ny=24, seed=41, nislands=1),
+               wl.eulerpsi_case(n=72, ny=56, seed=42, nislands=2)]
+    for prec in ("fp64", "fp32"):
+        e = _ensemble(members, prec)
+        n = e.packed_size()
+        pinned = torch.empty(n, dtype=torch.float64, pin_memory=True)
+        pageable = np.zeros(n)
+        L = _lib.lib()
+        assert L.f2d_ensemble_fields_get(e._h, b"omega", ctypes.c_void_p(pinned.data_ptr()),
+                                         0) == 0
+        assert L.f2d_ensemble_fields_get(e._h, b"omega", pageable.ctypes.data, 0) == 0
+        np.testing.assert_array_equal(pinned.numpy(), pageable)
+        rng = np.random.default_rng(9)
+        new = rng.standard_normal(n)
+        pinned.copy_(torch.from_numpy(new))
+        assert L.f2d_ensemble_fields_set(e._h, b"omega", ctypes.c_void_p(pinned.data_ptr()),
+                                         0) == 0
+        back = np.zeros(n)
+        assert L.f2d_ensemble_fields_get(e._h, b"omega", back.ctypes.data, 0) == 0
+        ref = new if prec == "fp64" else new.astype(np.float32).astype(np.float64)
+        # the packed layout covers every member's NY x NX array; compare all
+        np.testing.assert_array_equal(back, ref)
+
+
+def test_field_io_pinned():
+    """f2d_field_set/get with pinned host memory (the bench's end-to-end
+    path) give the pageable path's results, FP64 and FP32 models, an
+    FP64-only field (psi) included."""
+    import ctypes
+    case = wl.eulerpsi_case(n=48, ny=40, seed=3, nislands=1)
+    for prec in ("fp64", "fp32"):
+        m = _model("eulerpsi", 48, 40, case["msk"], precision=prec)
+        m.state.omega[:] = case["fields"]["omega"]
+        m.integrator.diag(m.state)
+        m.sync()
+        L = _lib.lib()
+        shape = m.mesh.shape
+        for name in (b"omega", b"psi"):
+            pinned = torch.empty(shape, dtype=torch.float64, pin_memory=True)
+            pageable = np.zeros(shape)
+            assert L.f2d_field_get(m._h, name, ctypes.c_void_p(pinned.data_ptr())) == 0
+            assert L.f2d_field_get(m._h, name, pageable.ctypes.data) == 0
+            np.testing.assert_array_equal(pinned.numpy(), pageable)
+        new = np.random.default_rng(4).standard_normal(shape)
+        pinned = torch.from_numpy(new.copy()).pin_memory()
+        assert L.f2d_field_set(m._h, b"omega", ctypes.c_void_p(pinned.data_ptr())) == 0
+        back = np.zeros(shape)
+        assert L.f2d_field_get(m._h, b"omega", back.ctypes.data) == 0
+        ref = new if prec == "fp64" else new.astype(np.float32).astype(np.float64)
+        np.testing.assert_array_equal(back, ref)
+
+
 def test_ensemble_vs_oracle():
     members = [wl.eulerpsi_case(n=48, ny=40, seed=21, nislands=2),
                wl.eulerpsi_case(n=72, ny=64, seed=22, nislands=1)]
