@@ -129,6 +129,8 @@ _SIGS = {
     "f2d_stats": ([c_void_p, ctypes.POINTER(c_i64), ctypes.POINTER(c_i64),
                    ctypes.POINTER(c_i64)], c_int),
     "f2d_test_tma_wait": ([c_int, c_dbl], c_int),
+    "f2d_test_conversions": ([c_void_p, c_i64, c_void_p, c_void_p, c_void_p, c_i64,
+                              c_void_p, c_void_p], c_int),
     "f2d_rhs": ([c_void_p], c_int),
     "f2d_set_schedule": ([c_void_p, c_int, c_int, c_dbl], c_int),
     "f2d_ensemble_set_schedule": ([c_void_p, c_int, c_int, c_dbl], c_int),

@@ -1667,6 +1667,61 @@ int f2d_sync(f2d_model m)
     return 0;
 }
 
+// test hook: the integer-pipe conversions against the hardware ones
+__global__ void k_test_conv(const double* __restrict__ x64, long long n64,
+                            float* __restrict__ sw32, float* __restrict__ hw32,
+                            const float* __restrict__ x32, long long n32,
+                            double* __restrict__ sw64, double* __restrict__ hw64)
+{
+    const long long k = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+    if (k < n64) {
+        sw32[k] = f64_to_f32_rn(x64[k]);
+        hw32[k] = __double2float_rn(x64[k]);
+    }
+    if (k < n32) {
+        sw64[k] = f32_to_f64(x32[k]);
+        hw64[k] = (double)x32[k];
+    }
+}
+
+int f2d_test_conversions(const double* x64, int64_t n64, float* sw32, float* hw32,
+                         const float* x32, int64_t n32, double* sw64, double* hw64)
+{
+    if (n64 < 0 || n32 < 0 || (n64 && (!x64 || !sw32 || !hw32)) ||
+        (n32 && (!x32 || !sw64 || !hw64)))
+        return fail(1, "bad arguments");
+    const long long n = std::max<long long>(std::max<long long>(n64, n32), 1);
+    void *d64 = nullptr, *d32 = nullptr, *o32 = nullptr, *o64 = nullptr;
+    const size_t b64 = sizeof(double) * std::max<long long>(n64, 1);
+    const size_t b32 = sizeof(float) * std::max<long long>(n32, 1);
+    int err = 0;
+    if (cudaMalloc(&d64, b64) != cudaSuccess || cudaMalloc(&d32, b32) != cudaSuccess ||
+        cudaMalloc(&o32, 2 * sizeof(float) * std::max<long long>(n64, 1)) != cudaSuccess ||
+        cudaMalloc(&o64, 2 * sizeof(double) * std::max<long long>(n32, 1)) != cudaSuccess)
+        err = fail(2, "out of device memory");
+    if (!err) {
+        if (n64) cudaMemcpy(d64, x64, sizeof(double) * n64, cudaMemcpyHostToDevice);
+        if (n32) cudaMemcpy(d32, x32, sizeof(float) * n32, cudaMemcpyHostToDevice);
+        float* s32 = (float*)o32;
+        double* s64 = (double*)o64;
+        k_test_conv<<<(unsigned)((n + 255) / 256), 256>>>(
+            (const double*)d64, n64, s32, s32 + std::max<long long>(n64, 1), (const float*)d32,
+            n32, s64, s64 + std::max<long long>(n32, 1));
+        if (cudaDeviceSynchronize() != cudaSuccess) err = fail(3, "conversion test kernel failed");
+        if (!err && n64) {
+            cudaMemcpy(sw32, s32, sizeof(float) * n64, cudaMemcpyDeviceToHost);
+            cudaMemcpy(hw32, s32 + n64, sizeof(float) * n64, cudaMemcpyDeviceToHost);
+        }
+        if (!err && n32) {
+            cudaMemcpy(sw64, s64, sizeof(double) * n32, cudaMemcpyDeviceToHost);
+            cudaMemcpy(hw64, s64 + n32, sizeof(double) * n32, cudaMemcpyDeviceToHost);
+        }
+    }
+    for (void* p : {d64, d32, o32, o64})
+        if (p) cudaFree(p);
+    return err;
+}
+
 int f2d_test_tma_wait(int enabled, double limit_ms)
 {
     if (enabled && !(limit_ms > 0 && limit_ms <= 1000))

@@ -111,6 +111,15 @@ __device__ __forceinline__ void tma_load_2d(void* dst, const CUtensorMap* map,
         : "memory");
 }
 
+// Programmatic dependent launch: a kernel launched with programmatic stream
+// serialization may be scheduled while its predecessor drains; it waits here
+// (for the predecessor's completion and memory) before touching anything the
+// predecessor writes. Without such a launch this returns at once.
+__device__ __forceinline__ void pdl_wait()
+{
+    asm volatile("griddepcontrol.wait;" ::: "memory");
+}
+
 __device__ __forceinline__ uint64_t globaltimer_ns()
 {
     uint64_t t;
@@ -136,6 +145,88 @@ __device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity,
         if (spin == 0) t0 = globaltimer_ns();
         else if (globaltimer_ns() - t0 > limit_ns) return false;
     }
+}
+
+// ---------------------------------------------------------------------------
+// binary64 <-> binary32 conversions on the integer pipe. GB300 runs FP64
+// instructions, the hardware conversions between FP64 and FP32 among them, at
+// 1/64 of the FP32 rate, and in the FP32 form's FP64 kernels (refinement
+// residual, perpgrad, correction, centers-to-vertices) the conversions are a
+// large share of that pipe. These follow the IEEE 754 definitions of the two
+// formats (sign, biased exponent, significand; conversion to binary32 rounds
+// to nearest, ties to even, with gradual underflow, overflow to infinity and
+// NaN kept quiet) and give the same bits as the hardware conversions
+// (tests/test_conversions.py checks every class of input on the GPU).
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ float f64_to_f32_rn(double x)
+{
+    const unsigned long long u = (unsigned long long)__double_as_longlong(x);
+    const unsigned hi = (unsigned)(u >> 32), lo = (unsigned)u;
+    const unsigned sign = hi & 0x80000000u;
+    const int e = (int)((hi >> 20) & 0x7ffu);
+    const unsigned m20 = hi & 0xfffffu;  // significand bits 51..32
+    if (e == 0x7ff) {  // infinity, or NaN (quiet, top payload bits kept)
+        const bool nan = (m20 | lo) != 0u;
+        const unsigned pay = (m20 << 3) | (lo >> 29);
+        return __uint_as_float(sign | 0x7f800000u | (nan ? (0x400000u | pay) : 0u));
+    }
+    const int ef = e - 1023 + 127;
+    if (ef >= 255) return __uint_as_float(sign | 0x7f800000u);
+    if (ef >= 1) {
+        // 23 result bits and the 29 bits below them
+        const unsigned mf = (m20 << 3) | (lo >> 29);
+        const unsigned rem = lo & 0x1fffffffu;
+        unsigned bits = sign | ((unsigned)ef << 23) | mf;
+        if (rem > 0x10000000u || (rem == 0x10000000u && (mf & 1u))) bits += 1u;  // may carry to inf
+        return __uint_as_float(bits);
+    }
+    // binary32 subnormal (or zero): the significand with its leading 1,
+    // shifted right by 1 - ef more places, rounded to nearest even
+    if (ef < -24 || e == 0) return __uint_as_float(sign);  // below half the smallest subnormal
+    const unsigned long long sig = (1ull << 52) | ((unsigned long long)m20 << 32) | lo;
+    const int sh = 29 + 1 - ef;  // 30 .. 54
+    const unsigned long long q = sig >> sh;
+    const unsigned long long r = sig & ((1ull << sh) - 1ull), half = 1ull << (sh - 1);
+    unsigned bits = sign | (unsigned)q;
+    if (r > half || (r == half && (q & 1ull))) bits += 1u;  // may round up to the smallest normal
+    return __uint_as_float(bits);
+}
+
+__device__ __forceinline__ double f32_to_f64(float f)
+{
+    const unsigned b = __float_as_uint(f);
+    const unsigned sign = b & 0x80000000u;
+    const unsigned e = (b >> 23) & 0xffu;
+    unsigned m = b & 0x7fffffu;
+    unsigned hi, lo;
+    if (e == 0xffu) {  // infinity or NaN (payload kept, quiet bit set for NaN)
+        hi = sign | 0x7ff00000u | (m ? (0x80000u | (m >> 3)) : 0u);
+        lo = m << 29;
+    } else if (e != 0u) {
+        hi = sign | ((e + 896u) << 20) | (m >> 3);
+        lo = m << 29;
+    } else if (m == 0u) {
+        hi = sign;
+        lo = 0u;
+    } else {  // subnormal m 2^-149: normalise to 1.f 2^(p-149), p its leading bit
+        const int p = 31 - __clz(m);
+        m = (m << (23 - p)) & 0x7fffffu;
+        hi = sign | ((unsigned)(p + 874) << 20) | (m >> 3);
+        lo = m << 29;
+    }
+    return __hiloint2double((int)hi, (int)lo);
+}
+
+// conversions between the working precisions through the functions above
+template <typename To, typename From>
+__device__ __forceinline__ To conv(From x)
+{
+    if constexpr (std::is_same<To, float>::value && std::is_same<From, double>::value)
+        return f64_to_f32_rn(x);
+    else if constexpr (std::is_same<To, double>::value && std::is_same<From, float>::value)
+        return f32_to_f64(x);
+    else
+        return To(x);
 }
 
 // Maximum that propagates NaN, as numpy's max does (the reference's set_dt,

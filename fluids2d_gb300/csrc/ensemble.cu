@@ -150,7 +150,7 @@ __global__ void k_ens_c2v(const int4* __restrict__ tiles, const Member* __restri
         Tin s = Tin(0);  // the average in the precision of the state
         if (j >= 1 && i >= 1 && (code[o] & B_MSKV))
             s = Tin(0.25) * (((q[o - g.P - 1] + q[o - 1]) + q[o - g.P]) + q[o]);
-        double v = s;
+        double v = conv<double>(s);
         if (fv) v -= fv[o];
         rhs[o] = v;
     }
@@ -177,9 +177,9 @@ __global__ void k_ens_perpgrad(const int4* __restrict__ tiles, const Member* __r
             const uint32_t cd = a.code[mb.off + o];
             T ux = T(0), uy = T(0);
             if (j <= g.NY - 2 && (cd & B_MSKX))
-                ux = -T(psi[o + g.P] - psi[o]) * Rd<T>::y(mb);
+                ux = -conv<T>(psi[o + g.P] - psi[o]) * Rd<T>::y(mb);
             if (i <= g.NX - 2 && (cd & B_MSKY))
-                uy = T(psi[o + 1] - psi[o]) * Rd<T>::x(mb);
+                uy = conv<T>(psi[o + 1] - psi[o]) * Rd<T>::x(mb);
             T* Ux = at<T>(a.Ux, mb.off);
             T* Uy = at<T>(a.Uy, mb.off);
             if (fillU) {

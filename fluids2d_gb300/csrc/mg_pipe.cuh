@@ -340,6 +340,7 @@ k_mgp_down(const int4* __restrict__ tiles, int ntiles, const MGLevel* __restrict
            const CUtensorMap* __restrict__ maps, int l, const DevScalars* __restrict__ scs,
            int ir, int* status)
 {
+    pdl_wait();
     extern __shared__ __align__(128) unsigned char mp_dyn[];
     MPDown& st = *reinterpret_cast<MPDown*>(mp_dyn);
     // after a staging failure the rest of the solve is void: skip the work
@@ -444,6 +445,7 @@ k_mgp_up(const int4* __restrict__ tiles, int ntiles, const MGLevel* __restrict__
          const CUtensorMap* __restrict__ maps, int l, const DevScalars* __restrict__ scs,
          int ir, double* tpart, int* status)
 {
+    pdl_wait();
     extern __shared__ __align__(128) unsigned char mp_dyn[];
     MPUp& st = *reinterpret_cast<MPUp*>(mp_dyn);
     // after a staging failure the rest of the solve is void: skip the work

@@ -160,6 +160,7 @@ __global__ void __launch_bounds__(256)
 k_bs_rz(const BSInfo* __restrict__ info, DevScalars* scs, const double* __restrict__ tpart,
         int ir)
 {
+    pdl_wait();
     const int b = blockIdx.x;
     const BSInfo in = info[b];
     DevScalars& sc = scs[b];
@@ -184,6 +185,7 @@ __global__ void __launch_bounds__(1024)
 k_bs_tail(const BSInfo* __restrict__ info, const MGLevel* __restrict__ levs, DevScalars* scs,
           int ir, int nu)
 {
+    pdl_wait();
     const int b = blockIdx.x;
     DevScalars& sc = scs[b];
     if (bs_skip(sc, ir)) return;
@@ -221,6 +223,7 @@ k_bs_pq(const int4* __restrict__ tiles, const MGLevel* __restrict__ levs,
         const S* __restrict__ z, V* __restrict__ p0, V* __restrict__ p1, V* __restrict__ q,
         const DevScalars* __restrict__ scs, double* partials, int ir)
 {
+    pdl_wait();
     constexpr int H = 1, W = Reg<H, TH>::WX, N = Reg<H, TH>::N, IT = (N + 255) / 256;
     constexpr int TQ = TH / 8;
     __shared__ V sp[N];
@@ -283,6 +286,7 @@ __global__ void __launch_bounds__(256)
 k_bs_alpha(const BSInfo* __restrict__ info, DevScalars* scs, const double* __restrict__ tpart,
            int ir)
 {
+    pdl_wait();
     const BSInfo in = info[blockIdx.x];
     DevScalars& sc = scs[blockIdx.x];
     if (bs_skip(sc, ir)) return;
@@ -306,6 +310,7 @@ k_bs_xr(const int4* __restrict__ tiles, const MGLevel* __restrict__ levs, V* __r
         V* __restrict__ r, const V* __restrict__ p0, const V* __restrict__ p1,
         const V* __restrict__ q, const DevScalars* __restrict__ scs, double* partials, int ir)
 {
+    pdl_wait();
     const int4 tl = tiles[blockIdx.x];
     const DevScalars& sc = scs[tl.x];
     if (bs_skip(sc, ir)) return;
@@ -361,6 +366,7 @@ __global__ void __launch_bounds__(256)
 k_bs_conv(const BSInfo* __restrict__ info, DevScalars* scs, const double* __restrict__ tpart,
           BSGlobals* eg, cudaGraphConditionalHandle cond, int ir, int nmem)
 {
+    pdl_wait();
     const BSInfo in = info[blockIdx.x];
     DevScalars& sc = scs[blockIdx.x];
     const bool skip = bs_skip(sc, ir);
@@ -457,7 +463,7 @@ __device__ __forceinline__ void residual64(const int4& tl, const MGLevel& L,
         }
         if (ok[qr]) {
             if (r) r[k[qr]] = rv;
-            if (rin) rin[k[qr]] = float(rv);
+            if (rin) rin[k[qr]] = f64_to_f32_rn(rv);
         }
     }
 }
@@ -619,7 +625,7 @@ k_bs_correct(const int4* __restrict__ tiles, const MGLevel* __restrict__ levs,
     }
 #pragma unroll
     for (int qr = 0; qr < TQ; ++qr)
-        if (ok[qr] && mv[qr]) x[k[qr]] = zero ? 0.0 : xv[qr] + (double)ev[qr];
+        if (ok[qr] && mv[qr]) x[k[qr]] = zero ? 0.0 : xv[qr] + f32_to_f64(ev[qr]);
 }
 
 __global__ void k_bs_setup(DevScalars* scs, int n, double tol2, int maxit, double tol_in2,
@@ -672,6 +678,27 @@ static bool bs_eager()
 
 // one V-cycle for all members still iterating: a down kernel per grid level,
 // the tail, an up kernel per grid level (the level-0 one also forms <r, z>)
+// Launch with programmatic stream serialization (the kernel calls pdl_wait()
+// before touching its predecessor's output): its blocks can be scheduled
+// while the predecessor on the stream drains, which hides part of the launch
+// gap between the many short kernels of the CG loop.
+template <typename... KA, typename... A>
+static void launch_pdl(void (*k)(KA...), dim3 grid, dim3 block, size_t smem, cudaStream_t st,
+                       A... args)
+{
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = grid;
+    cfg.blockDim = block;
+    cfg.dynamicSmemBytes = smem;
+    cfg.stream = st;
+    cudaLaunchAttribute at[1];
+    at[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+    at[0].val.programmaticStreamSerializationAllowed = 1;
+    cfg.attrs = at;
+    cfg.numAttrs = 1;
+    cudaLaunchKernelEx(&cfg, k, args...);
+}
+
 // the same with the pipelined FP32 level kernels (persistent blocks)
 template <int NU>
 static int vcycle_pipe(BatchSolver& s, cudaStream_t st, int ir)
@@ -683,21 +710,25 @@ static int vcycle_pipe(BatchSolver& s, cudaStream_t st, int ir)
     for (int l = 0; l < s.maxl; ++l) {
         const int n = s.nmtiles[l];
         if (n == 0) continue;
-        k_mgp_down<NU><<<std::min(n, s.pipe_gdown), blk, sizeof(MPDown), st>>>(
-            s.mtiles[l], n, s.dlevs, maps, l, s.scs, ir, status);
+        launch_pdl(k_mgp_down<NU>, dim3(std::min(n, s.pipe_gdown)), blk, sizeof(MPDown), st,
+                   (const int4*)s.mtiles[l], n, (const MGLevel*)s.dlevs, maps, l,
+                   (const DevScalars*)s.scs, ir, status);
         cnt += 1;
     }
-    k_bs_tail<float><<<s.n, s.tail_threads, s.tail_smem, st>>>(s.dinfo, s.dlevs, s.scs, ir, NU);
+    launch_pdl(k_bs_tail<float>, dim3(s.n), dim3(s.tail_threads), s.tail_smem, st,
+               (const BSInfo*)s.dinfo, (const MGLevel*)s.dlevs, s.scs, ir, NU);
     cnt += 1;
     for (int l = s.maxl - 1; l >= 0; --l) {
         const int n = s.nmtiles[l];
         if (n == 0) continue;
         if (l > 0)
-            k_mgp_up<NU, false><<<std::min(n, s.pipe_gup), blk, sizeof(MPUp), st>>>(
-                s.mtiles[l], n, s.dlevs, maps, l, s.scs, ir, nullptr, status);
+            launch_pdl(k_mgp_up<NU, false>, dim3(std::min(n, s.pipe_gup)), blk, sizeof(MPUp), st,
+                       (const int4*)s.mtiles[l], n, (const MGLevel*)s.dlevs, maps, l,
+                       (const DevScalars*)s.scs, ir, (double*)nullptr, status);
         else
-            k_mgp_up<NU, true><<<std::min(n, s.pipe_gup), blk, sizeof(MPUp), st>>>(
-                s.mtiles[0], n, s.dlevs, maps, 0, s.scs, ir, s.mpartials, status);
+            launch_pdl(k_mgp_up<NU, true>, dim3(std::min(n, s.pipe_gup)), blk, sizeof(MPUp), st,
+                       (const int4*)s.mtiles[0], n, (const MGLevel*)s.dlevs, maps, 0,
+                       (const DevScalars*)s.scs, ir, s.mpartials, status);
         cnt += 1;
     }
     return cnt;
@@ -746,15 +777,20 @@ static int cg_body(BatchSolver& s, cudaStream_t st, cudaGraphConditionalHandle c
     V* x = (V*)(ir ? s.v.e : s.v.x64);
     int cnt = vcycle<S, TH>(s, st, ir);
     if (s.maxl > 0) {
-        k_bs_rz<<<s.n, 256, 0, st>>>(s.dinfo, s.scs, s.mpartials, ir);
+        launch_pdl(k_bs_rz, dim3(s.n), dim3(256), 0, st, (const BSInfo*)s.dinfo, s.scs,
+                   (const double*)s.mpartials, ir);
         cnt += 1;
     }
-    k_bs_pq<S, V, TH><<<nt, blk, 0, st>>>(s.rtiles, s.dlevs, (const S*)s.v.z, (V*)s.v.p,
-                                          (V*)s.v.p2, (V*)s.v.q, s.scs, s.partials, ir);
-    k_bs_alpha<<<s.n, 256, 0, st>>>(s.dinfo, s.scs, s.partials, ir);
-    k_bs_xr<V, TH><<<nt, blk, 0, st>>>(s.rtiles, s.dlevs, x, r, (const V*)s.v.p,
-                                       (const V*)s.v.p2, (const V*)s.v.q, s.scs, s.partials, ir);
-    k_bs_conv<<<s.n, 256, 0, st>>>(s.dinfo, s.scs, s.partials, s.eg, cond, ir, s.n);
+    launch_pdl(k_bs_pq<S, V, TH>, dim3(nt), blk, 0, st, (const int4*)s.rtiles,
+               (const MGLevel*)s.dlevs, (const S*)s.v.z, (V*)s.v.p, (V*)s.v.p2, (V*)s.v.q,
+               (const DevScalars*)s.scs, s.partials, ir);
+    launch_pdl(k_bs_alpha, dim3(s.n), dim3(256), 0, st, (const BSInfo*)s.dinfo, s.scs,
+               (const double*)s.partials, ir);
+    launch_pdl(k_bs_xr<V, TH>, dim3(nt), blk, 0, st, (const int4*)s.rtiles,
+               (const MGLevel*)s.dlevs, x, r, (const V*)s.v.p, (const V*)s.v.p2,
+               (const V*)s.v.q, (const DevScalars*)s.scs, s.partials, ir);
+    launch_pdl(k_bs_conv, dim3(s.n), dim3(256), 0, st, (const BSInfo*)s.dinfo, s.scs,
+               (const double*)s.partials, s.eg, cond, ir, s.n);
     cnt += 4;
     s.body_launches = cnt;
     return (int)cudaGetLastError();

@@ -376,7 +376,7 @@ __global__ void k_c2v(const Tin* __restrict__ q, T* __restrict__ v,
         Tin a = Tin(0);
         if (j >= 1 && i >= 1 && (code[o] & B_MSKV))
             a = Tin(0.25) * (((q[o - g.P - 1] + q[o - 1]) + q[o - g.P]) + q[o]);
-        T b = T(a);
+        T b = conv<T>(a);
         if (fv) b -= fv[o];
         v[o] = b;
     }
@@ -402,8 +402,8 @@ __global__ void k_perpgrad(const P* __restrict__ psi, T* __restrict__ Ux,
             // the difference in the precision of psi, the scaling in that of U
             const uint32_t cd = code[o];
             T ux = T(0), uy = T(0);
-            if (j <= g.NY - 2 && (cd & B_MSKX)) ux = -T(psi[o + g.P] - psi[o]) * rdy2;
-            if (i <= g.NX - 2 && (cd & B_MSKY)) uy = T(psi[o + 1] - psi[o]) * rdx2;
+            if (j <= g.NY - 2 && (cd & B_MSKX)) ux = -conv<T>(psi[o + g.P] - psi[o]) * rdy2;
+            if (i <= g.NX - 2 && (cd & B_MSKY)) uy = conv<T>(psi[o + 1] - psi[o]) * rdx2;
             if (fillU) {
                 store_filled(Ux, g, j, i, ux);
                 store_filled(Uy, g, j, i, uy);
