@@ -245,6 +245,12 @@ int f2d_solver_pipelined(f2d_model m, int *pipelined);
  * enabled == 0 restores normal operation. Applies to every model and
  * ensemble of the process; synchronises the device. For tests only. */
 int f2d_test_tma_wait(int enabled, double limit_ms);
+/* Test hook (no reference counterpart): the library's integer-pipe
+ * binary64 -> binary32 (round to nearest even) and binary32 -> binary64
+ * conversions next to the hardware conversions, on the device, for host
+ * inputs x64[n64] and x32[n32]; outputs sw32/hw32[n64], sw64/hw64[n32]. */
+int f2d_test_conversions(const double *x64, int64_t n64, float *sw32, float *hw32,
+                         const float *x32, int64_t n32, double *sw64, double *hw64);
 /* Refinement rounds of the FP32 form's solves summed since creation (see
  * f2d_ensemble_refine_rounds). Instrumentation. */
 int f2d_refine_rounds(f2d_model m, int64_t *rounds);
