@@ -279,6 +279,7 @@ static int ensure_mg(f2d_model_s* m, int which)
     v.za = m->pza;
     v.rin = m->prmg;
     v.e = m->pe;
+    v.nelem = (long long)g.P * g.NY;
     BatchSolver& bs = m->bs[which];
     int e = bs_build(bs, {d}, m->d_gmask, m->prec, v, m->sc);
     if (e) return fail(e, "multigrid setup failed");

@@ -74,6 +74,9 @@ struct DevScalars {
     // time step of the step whose stage increments the warm start keeps
     // (0: none yet); the next step scales them by dt / dt_warm
     double dt_warm;
+    // step lengths (FP32) of the inner iterations of the current refinement
+    // round: the round's correction is sum alpha_i p_i (solver.cu)
+    float ahist[32];
 };
 
 // ---------------------------------------------------------------------------

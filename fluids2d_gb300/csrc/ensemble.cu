@@ -142,14 +142,30 @@ __global__ void k_ens_c2v(const int4* __restrict__ tiles, const Member* __restri
     const uint32_t* code = a.code + mb.off;
     const double* fv = use_fv ? at<double>(a.fv, mb.off) : nullptr;
     double* rhs = at<double>(a.rhs, mb.off);
+    // every load of the thread's rows is issued before any is used (clamped
+    // indices, the mask applied after): one memory round trip, not one per
+    // row and condition
+    uint32_t cd[FRT];
+    Tin a0[FRT], a1[FRT], a2[FRT], a3[FRT];
+#pragma unroll
+    for (int r = 0; r < FRT; ++r) {
+        const int j = min(tl.z + threadIdx.y + 8 * r, g.NY - 1);
+        const int jm = max(j - 1, 0), im = max(i - 1, 0);
+        const long long o = (long long)j * g.P + i, om = (long long)jm * g.P;
+        cd[r] = code[o];
+        a0[r] = q[om + im];                  // (j-1, i-1)
+        a1[r] = q[(long long)j * g.P + im];  // (j, i-1)
+        a2[r] = q[om + i];                   // (j-1, i)
+        a3[r] = q[o];                        // (j, i)
+    }
 #pragma unroll
     for (int r = 0; r < FRT; ++r) {
         const int j = tl.z + threadIdx.y + 8 * r;
         if (j >= g.NY) break;
         const long long o = (long long)j * g.P + i;
         Tin s = Tin(0);  // the average in the precision of the state
-        if (j >= 1 && i >= 1 && (code[o] & B_MSKV))
-            s = Tin(0.25) * (((q[o - g.P - 1] + q[o - 1]) + q[o - g.P]) + q[o]);
+        if (j >= 1 && i >= 1 && (cd[r] & B_MSKV))
+            s = Tin(0.25) * (((a0[r] + a1[r]) + a2[r]) + a3[r]);
         double v = conv<double>(s);
         if (fv) v -= fv[o];
         rhs[o] = v;
@@ -165,6 +181,28 @@ __global__ void k_ens_perpgrad(const int4* __restrict__ tiles, const Member* __r
     const Member& mb = mem[tl.x];
     const Geom g = mb.g;
     T m[2] = {T(0), T(0)};
+    // the member's constants and pointers in registers (stores through Ux, Uy
+    // could alias the member table, which would reload them after each)
+    const long long moff = mb.off;
+    const T rx = Rd<T>::x(mb), ry = Rd<T>::y(mb);
+    T* Ux = at<T>(a.Ux, moff);
+    T* Uy = at<T>(a.Uy, moff);
+    const uint32_t* code = a.code + moff;
+    // the loads of all the thread's rows first (clamped indices), then the
+    // masked differences: one memory round trip
+    const double* psi = at<double>(a.psi, moff);
+    const int ic = min(tl.y + threadIdx.x, g.NX - 1);
+    uint32_t cdv[FRT];
+    double p0[FRT], pn[FRT], pe[FRT];
+#pragma unroll
+    for (int r = 0; r < FRT; ++r) {
+        const int jc = min(tl.z + threadIdx.y + 8 * r, g.NY - 1);
+        const long long o = (long long)jc * g.P + ic;
+        cdv[r] = code[o];
+        p0[r] = psi[o];
+        pn[r] = psi[(long long)min(jc + 1, g.NY - 1) * g.P + ic];
+        pe[r] = psi[(long long)jc * g.P + min(ic + 1, g.NX - 1)];
+    }
 #pragma unroll
     for (int r = 0; r < FRT; ++r) {
         const int i = tl.y + threadIdx.x, j = tl.z + threadIdx.y + 8 * r;
@@ -173,15 +211,10 @@ __global__ void k_ens_perpgrad(const int4* __restrict__ tiles, const Member* __r
         const bool own = !fillU || periodic_owner(g, i);
         if (own) {
             // FP64 difference, scaling in the precision of U
-            const double* psi = at<double>(a.psi, mb.off);
-            const uint32_t cd = a.code[mb.off + o];
+            const uint32_t cd = cdv[r];
             T ux = T(0), uy = T(0);
-            if (j <= g.NY - 2 && (cd & B_MSKX))
-                ux = -conv<T>(psi[o + g.P] - psi[o]) * Rd<T>::y(mb);
-            if (i <= g.NX - 2 && (cd & B_MSKY))
-                uy = conv<T>(psi[o + 1] - psi[o]) * Rd<T>::x(mb);
-            T* Ux = at<T>(a.Ux, mb.off);
-            T* Uy = at<T>(a.Uy, mb.off);
+            if (j <= g.NY - 2 && (cd & B_MSKX)) ux = -conv<T>(pn[r] - p0[r]) * ry;
+            if (i <= g.NX - 2 && (cd & B_MSKY)) uy = conv<T>(pe[r] - p0[r]) * rx;
             if (fillU) {
                 store_filled(Ux, g, j, i, ux);
                 store_filled(Uy, g, j, i, uy);
@@ -556,6 +589,7 @@ int f2d_ensemble_create(const f2d_params* p, int count, const int* nxs, const in
     memset(&v, 0, sizeof(v));
     v.x64 = e->ar.psi;
     v.b64 = e->ar.rhs;
+    v.nelem = (long long)e->total;
     v.r64 = A(8);
     v.p = A(8);
     v.p2 = A(8);

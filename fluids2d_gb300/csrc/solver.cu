@@ -221,7 +221,8 @@ template <typename S, typename V, int TH>
 __global__ void __launch_bounds__(256)
 k_bs_pq(const int4* __restrict__ tiles, const MGLevel* __restrict__ levs,
         const S* __restrict__ z, V* __restrict__ p0, V* __restrict__ p1, V* __restrict__ q,
-        const DevScalars* __restrict__ scs, double* partials, int ir)
+        const DevScalars* __restrict__ scs, double* partials, int ir, V* ring,
+        long long rstride)
 {
     pdl_wait();
     constexpr int H = 1, W = Reg<H, TH>::WX, N = Reg<H, TH>::N, IT = (N + 255) / 256;
@@ -234,8 +235,11 @@ k_bs_pq(const int4* __restrict__ tiles, const MGLevel* __restrict__ levs,
     const MGLevel L = levs[tl.x * BS_LMAX];
     const int it = ir ? sc.iter_in : sc.iter;
     const bool first = it == 0;
-    const V* __restrict__ pold = (it & 1) ? p1 : p0;
-    V* __restrict__ pnew = (it & 1) ? p0 : p1;
+    // the direction ring (refinement form: p_it into slot it) or the two
+    // buffers alternating with the iteration's parity (FP64 form)
+    const V* __restrict__ pold =
+        ring ? ring + (long long)max(it - 1, 0) * rstride : ((it & 1) ? p1 : p0);
+    V* __restrict__ pnew = ring ? ring + (long long)it * rstride : ((it & 1) ? p0 : p1);
     const V beta = V(sc.beta);
     const int I0 = tl.y, J0 = tl.z, t = tid256();
 #pragma unroll
@@ -297,13 +301,13 @@ k_bs_alpha(const BSInfo* __restrict__ info, DevScalars* scs, const double* __res
     if (threadIdx.x == 0) {
         sc.pq = acc[0];
         sc.alpha = sc.rz / acc[0];
+        if (ir) sc.ahist[sc.iter_in] = f64_to_f32_rn(sc.alpha);
     }
 }
 
-// x += alpha p, r -= alpha q, rr = <r, r>, per-member convergence, loop
-// condition. FP64 form: x is the solution. Refinement form: x is the inner
-// correction e (started from 0) and convergence is relative to the round's
-// starting residual.
+// x += alpha p (FP64 form, x the solution; x == nullptr in the refinement
+// form, whose correction k_bs_correct forms from the direction ring),
+// r -= alpha q, the tile's part of <r, r> (k_bs_conv decides).
 template <typename V, int TH>
 __global__ void __launch_bounds__(256)
 k_bs_xr(const int4* __restrict__ tiles, const MGLevel* __restrict__ levs, V* __restrict__ x,
@@ -336,8 +340,8 @@ k_bs_xr(const int4* __restrict__ tiles, const MGLevel* __restrict__ levs, V* __r
             ok[qr] = J < L.nyn && I < L.nxn;
             k[qr] = nidx(L, min(J, L.nyn - 1), min(I, L.nxn - 1));
             mv[qr] = L.m[k[qr]];
-            xv[qr] = first ? V(0) : x[k[qr]];
-            pv[qr] = p[k[qr]];
+            xv[qr] = (first || !x) ? V(0) : x[k[qr]];
+            pv[qr] = x ? p[k[qr]] : V(0);
             rv[qr] = r[k[qr]];
             qv[qr] = q[k[qr]];
         }
@@ -345,11 +349,11 @@ k_bs_xr(const int4* __restrict__ tiles, const MGLevel* __restrict__ levs, V* __r
         for (int qr = 0; qr < QB; ++qr) {
             if (!ok[qr] || !mv[qr]) continue;
             if (zero) {
-                x[k[qr]] = V(0);
+                if (x) x[k[qr]] = V(0);
                 r[k[qr]] = V(0);
                 continue;
             }
-            x[k[qr]] = xv[qr] + a * pv[qr];
+            if (x) x[k[qr]] = xv[qr] + a * pv[qr];
             const V rn = rv[qr] - a * qv[qr];
             r[k[qr]] = rn;
             acc += rn * rn;
@@ -600,7 +604,7 @@ k_bs_refine_fin(const BSInfo* __restrict__ info, DevScalars* scs,
 template <int TH>
 __global__ void __launch_bounds__(256)
 k_bs_correct(const int4* __restrict__ tiles, const MGLevel* __restrict__ levs,
-             double* __restrict__ x, const float* __restrict__ e,
+             double* __restrict__ x, const float* __restrict__ ring, long long rstride,
              const DevScalars* __restrict__ scs)
 {
     const int4 tl = tiles[blockIdx.x];
@@ -608,24 +612,49 @@ k_bs_correct(const int4* __restrict__ tiles, const MGLevel* __restrict__ levs,
     if (sc.converged) return;
     const MGLevel L = levs[tl.x * BS_LMAX];
     const int zero = sc.zero;
+    const int kit = sc.iter_in;  // inner iterations of the round
     constexpr int TQ = TH / 8;
     long long k[TQ];
-    bool ok[TQ];
-    uint8_t mv[TQ];
-    double xv[TQ];
     float ev[TQ];
 #pragma unroll
     for (int qr = 0; qr < TQ; ++qr) {
         const int J = tl.z + threadIdx.y + 8 * qr, I = tl.y + threadIdx.x;
-        ok[qr] = J < L.nyn && I < L.nxn;
         k[qr] = nidx(L, min(J, L.nyn - 1), min(I, L.nxn - 1));
+        ev[qr] = 0.f;
+    }
+    // e = sum alpha_i p_i in the order of the iterations, as the iterations
+    // would have accumulated it (e_{i+1} = e_i + alpha_i p_i, FP32); four
+    // directions' loads in flight before their FMAs
+    constexpr int CH = 4;
+    for (int i0 = 0; i0 < kit; i0 += CH) {
+        float pv[CH][TQ];
+#pragma unroll
+        for (int c = 0; c < CH; ++c) {
+            const float* __restrict__ p = ring + (long long)min(i0 + c, kit - 1) * rstride;
+#pragma unroll
+            for (int qr = 0; qr < TQ; ++qr) pv[c][qr] = p[k[qr]];
+        }
+#pragma unroll
+        for (int c = 0; c < CH; ++c) {
+            if (i0 + c >= kit) break;
+            const float a = sc.ahist[i0 + c];
+#pragma unroll
+            for (int qr = 0; qr < TQ; ++qr) ev[qr] = fmaf(a, pv[c][qr], ev[qr]);
+        }
+    }
+    uint8_t mv[TQ];
+    double xv[TQ];
+#pragma unroll
+    for (int qr = 0; qr < TQ; ++qr) {
         mv[qr] = L.m[k[qr]];
         xv[qr] = x[k[qr]];
-        ev[qr] = e[k[qr]];
     }
 #pragma unroll
-    for (int qr = 0; qr < TQ; ++qr)
-        if (ok[qr] && mv[qr]) x[k[qr]] = zero ? 0.0 : xv[qr] + f32_to_f64(ev[qr]);
+    for (int qr = 0; qr < TQ; ++qr) {
+        const int J = tl.z + threadIdx.y + 8 * qr, I = tl.y + threadIdx.x;
+        if (J < L.nyn && I < L.nxn && mv[qr])
+            x[k[qr]] = zero ? 0.0 : xv[qr] + f32_to_f64(ev[qr]);
+    }
 }
 
 __global__ void k_bs_setup(DevScalars* scs, int n, double tol2, int maxit, double tol_in2,
@@ -774,16 +803,17 @@ static int cg_body(BatchSolver& s, cudaStream_t st, cudaGraphConditionalHandle c
     const dim3 blk(32, 8);
     const int nt = s.nrtiles;
     V* r = (V*)(ir ? s.v.rin : s.v.r64);
-    V* x = (V*)(ir ? s.v.e : s.v.x64);
+    V* x = ir ? (V*)nullptr : (V*)s.v.x64;  // the refinement form's x is the ring
     int cnt = vcycle<S, TH>(s, st, ir);
     if (s.maxl > 0) {
         launch_pdl(k_bs_rz, dim3(s.n), dim3(256), 0, st, (const BSInfo*)s.dinfo, s.scs,
                    (const double*)s.mpartials, ir);
         cnt += 1;
     }
+    V* ring = ir ? (V*)s.pring : (V*)nullptr;
     launch_pdl(k_bs_pq<S, V, TH>, dim3(nt), blk, 0, st, (const int4*)s.rtiles,
                (const MGLevel*)s.dlevs, (const S*)s.v.z, (V*)s.v.p, (V*)s.v.p2, (V*)s.v.q,
-               (const DevScalars*)s.scs, s.partials, ir);
+               (const DevScalars*)s.scs, s.partials, ir, ring, (long long)s.v.nelem);
     launch_pdl(k_bs_alpha, dim3(s.n), dim3(256), 0, st, (const BSInfo*)s.dinfo, s.scs,
                (const double*)s.partials, ir);
     launch_pdl(k_bs_xr<V, TH>, dim3(nt), blk, 0, st, (const int4*)s.rtiles,
@@ -848,7 +878,8 @@ static int bs_record_t(BatchSolver& s, cudaStream_t st, cudaStream_t st2, int* l
     const int nt = s.nrtiles;
     int fixed = 0;
     k_bs_setup<<<(s.n + 127) / 128, 128, 0, st>>>(s.scs, s.n, s.tol * s.tol, s.maxit,
-                                                   s.tol_in * s.tol_in, s.maxit_in, s.maxouter,
+                                                   s.tol_in * s.tol_in,
+                                                   std::min(s.maxit_in, BS_RING), s.maxouter,
                                                    s.eg);
     fixed += 1;
     cudaStreamCaptureStatus cs;
@@ -900,7 +931,8 @@ static int bs_record_t(BatchSolver& s, cudaStream_t st, cudaStream_t st2, int* l
     fixed += 3;
     auto round_tail = [&](cudaStream_t sb) {
         k_bs_correct<TH><<<nt, blk, 0, sb>>>(s.rtiles, s.dlevs, (double*)s.v.x64,
-                                         (const float*)s.v.e, s.scs);
+                                             (const float*)s.pring, (long long)s.v.nelem,
+                                             s.scs);
         k_bs_reset<<<1, 1, 0, sb>>>(s.eg);
         launch_refine<TH, false>(s, sb);
         k_bs_refine_fin<<<s.n, 256, 0, sb>>>(s.dinfo, s.scs, s.partials, s.eg, 0, cond_o, s.n);
@@ -1316,6 +1348,11 @@ int bs_build(BatchSolver& s, const std::vector<BSMemberDesc>& members, const uin
         const int e = bs_pipe_setup(s, levs, info, dal);
         if (e) return e;
     }
+    if (mode == 1) {
+        if (v.nelem <= 0) return 1;
+        s.pring = (float*)dal((size_t)BS_RING * v.nelem * sizeof(float));
+        if (!s.pring) return 2;
+    }
     if (cudaMemcpy(s.dlevs, levs.data(), levs.size() * sizeof(MGLevel), cudaMemcpyHostToDevice) !=
             cudaSuccess ||
         cudaMemcpy(s.dinfo, info.data(), info.size() * sizeof(BSInfo), cudaMemcpyHostToDevice) !=
@@ -1517,6 +1554,7 @@ void bs_free(BatchSolver& s)
     s.partials = nullptr;
     s.pipe = false;
     s.mmaps = nullptr;
+    s.pring = nullptr;
 }
 
 }  // namespace f2d

@@ -9,6 +9,7 @@
 namespace f2d {
 
 constexpr int BS_LMAX = 16;           // levels per member
+constexpr int BS_RING = 32;           // inner iterations per refinement round, at most
 constexpr int BS_TW = 32;  // node tile: 32 columns x 32 or 64 rows, 32 x 8 threads
 
 struct BSInfo {
@@ -41,6 +42,7 @@ struct BSVecs {
     void* za;   // level-0 multigrid x after the pre-smoothing (as z)
     void* rin;  // inner residual of the refinement form (float), multigrid rhs
     void* e;    // inner correction of the refinement form (float)
+    long long nelem;  // elements of each arena vector (the direction ring's stride)
 };
 
 struct BSMemberDesc {
@@ -82,6 +84,11 @@ struct BatchSolver {
     size_t tail_smem = 0;
     int tail_threads = 1024;  // block size of k_bs_tail (bs_build)
     bool helm = false, unit = false;  // FP64 residual variant (bs_build)
+    // refinement form: the inner iterations' directions p_0 .. p_{k-1}, one
+    // float arena each (p_i at pring + i * nelem), so the round's correction
+    // sum alpha_i p_i is formed once, by k_bs_correct, instead of an x
+    // update in every iteration; inner iterations are capped at BS_RING
+    float* pring = nullptr;
     BSVecs v;
     double tol = 1e-12, tol_in = 1e-6;
     int maxit = 200, maxit_in = 30, maxouter = 20;

@@ -368,14 +368,29 @@ __global__ void k_c2v(const Tin* __restrict__ q, T* __restrict__ v,
 {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= g.NX) return;
+    // the loads of all the thread's rows first (clamped indices, the mask
+    // applied after): one memory round trip
+    uint32_t cd[FRT];
+    Tin a0[FRT], a1[FRT], a2[FRT], a3[FRT];
+#pragma unroll
+    for (int r = 0; r < FRT; ++r) {
+        const int j = min(blockIdx.y * FTY + threadIdx.y + 8 * r, g.NY - 1);
+        const int jm = max(j - 1, 0), im = max(i - 1, 0);
+        const long long o = (long long)j * g.P + i, om = (long long)jm * g.P;
+        cd[r] = code[o];
+        a0[r] = q[om + im];
+        a1[r] = q[(long long)j * g.P + im];
+        a2[r] = q[om + i];
+        a3[r] = q[o];
+    }
 #pragma unroll
     for (int r = 0; r < FRT; ++r) {
         const int j = blockIdx.y * FTY + threadIdx.y + 8 * r;
         if (j >= g.NY) break;
         const long long o = (long long)j * g.P + i;
         Tin a = Tin(0);
-        if (j >= 1 && i >= 1 && (code[o] & B_MSKV))
-            a = Tin(0.25) * (((q[o - g.P - 1] + q[o - 1]) + q[o - g.P]) + q[o]);
+        if (j >= 1 && i >= 1 && (cd[r] & B_MSKV))
+            a = Tin(0.25) * (((a0[r] + a1[r]) + a2[r]) + a3[r]);
         T b = conv<T>(a);
         if (fv) b -= fv[o];
         v[o] = b;
@@ -392,6 +407,19 @@ __global__ void k_perpgrad(const P* __restrict__ psi, T* __restrict__ Ux,
 {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     T m[2] = {T(0), T(0)};
+    // the loads of all the thread's rows first (clamped indices): one round trip
+    const int ic = min(i, g.NX - 1);
+    uint32_t cdv[FRT];
+    P p0[FRT], pn[FRT], pe[FRT];
+#pragma unroll
+    for (int r = 0; r < FRT; ++r) {
+        const int jc = min(blockIdx.y * FTY + threadIdx.y + 8 * r, g.NY - 1);
+        const long long o = (long long)jc * g.P + ic;
+        cdv[r] = code[o];
+        p0[r] = psi[o];
+        pn[r] = psi[(long long)min(jc + 1, g.NY - 1) * g.P + ic];
+        pe[r] = psi[(long long)jc * g.P + min(ic + 1, g.NX - 1)];
+    }
 #pragma unroll
     for (int r = 0; r < FRT; ++r) {
         const int j = blockIdx.y * FTY + threadIdx.y + 8 * r;
@@ -400,10 +428,10 @@ __global__ void k_perpgrad(const P* __restrict__ psi, T* __restrict__ Ux,
         const bool own = !fillU || periodic_owner(g, i);
         if (own) {
             // the difference in the precision of psi, the scaling in that of U
-            const uint32_t cd = code[o];
+            const uint32_t cd = cdv[r];
             T ux = T(0), uy = T(0);
-            if (j <= g.NY - 2 && (cd & B_MSKX)) ux = -conv<T>(psi[o + g.P] - psi[o]) * rdy2;
-            if (i <= g.NX - 2 && (cd & B_MSKY)) uy = conv<T>(psi[o + 1] - psi[o]) * rdx2;
+            if (j <= g.NY - 2 && (cd & B_MSKX)) ux = -conv<T>(pn[r] - p0[r]) * rdy2;
+            if (i <= g.NX - 2 && (cd & B_MSKY)) uy = conv<T>(pe[r] - p0[r]) * rdx2;
             if (fillU) {
                 store_filled(Ux, g, j, i, ux);
                 store_filled(Uy, g, j, i, uy);
