@@ -132,7 +132,6 @@ struct f2d_model_s {
     // multigrid: [0] vertex Poisson, [1] Helmholtz
     BatchSolver bs[2];  // [0] vertex Poisson, [1] qg Helmholtz
     bool bs_ready[2] = {false, false};
-    void* pe = nullptr;  // inner correction of the refinement form (FP32)
     void *pr = nullptr, *pz = nullptr, *pp = nullptr, *pq = nullptr;
     void *pp2 = nullptr, *pza = nullptr;
     void* prmg = nullptr;  // V-cycle right-hand side (== pr in FP64)
@@ -278,7 +277,6 @@ static int ensure_mg(f2d_model_s* m, int which)
     v.z = m->pz;
     v.za = m->pza;
     v.rin = m->prmg;
-    v.e = m->pe;
     v.nelem = (long long)g.P * g.NY;
     BatchSolver& bs = m->bs[which];
     int e = bs_build(bs, {d}, m->d_gmask, m->prec, v, m->sc);
@@ -1219,9 +1217,8 @@ int f2d_model_create(const f2d_params* p, const int8_t* msk, f2d_model* out)
         m->pp2 = dalloc(m, field_bytes(m, 8));
         m->pza = dalloc(m, field_bytes(m, m->es));
         m->prmg = m->prec == 0 ? m->pr : dalloc(m, field_bytes(m, 4));
-        m->pe = m->prec == 0 ? m->pr : dalloc(m, field_bytes(m, 4));
         m->d_fv = dalloc(m, field_bytes(m, 8));
-        if (!m->pr || !m->pz || !m->pp || !m->pq || !m->d_fv || !m->prmg || !m->pe ||
+        if (!m->pr || !m->pz || !m->pp || !m->pq || !m->d_fv || !m->prmg ||
             !m->pp2 || !m->pza)
             return bail(fail(2, "out of device memory"));
     }

@@ -597,7 +597,6 @@ int f2d_ensemble_create(const f2d_params* p, int count, const int* nxs, const in
     v.z = A(es);
     v.za = A(es);
     v.rin = e->prec == 0 ? v.r64 : A(4);
-    v.e = e->prec == 0 ? v.r64 : A(4);
     e->stage64 = A(8);
     e->scs = (DevScalars*)ens_alloc(e, sizeof(DevScalars) * count);
     e->eg = (EnsGlobals*)ens_alloc(e, sizeof(EnsGlobals));
@@ -605,7 +604,7 @@ int f2d_ensemble_create(const f2d_params* p, int count, const int* nxs, const in
                     e->ar.rhs, e->ar.psi, (void*)e->ar.psi_s0, (void*)e->ar.psi_p1,
                     (void*)e->ar.psi_d1, (void*)e->ar.psi_d2,
                     e->ar.fv, e->code, e->gmask, v.r64, v.p, v.p2, v.q, v.z, v.za,
-                    v.rin, v.e, e->stage64, (void*)e->scs, (void*)e->eg})
+                    v.rin, e->stage64, (void*)e->scs, (void*)e->eg})
         if (!q) return bail(f2d_internal_fail(2, "out of device memory for the ensemble"));
     e->ar.code = (const uint32_t*)e->code;
     // codes, masks, TMA maps, solver descriptors per member

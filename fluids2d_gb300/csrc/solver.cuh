@@ -41,7 +41,6 @@ struct BSVecs {
     void* z;    // preconditioned residual, multigrid precision
     void* za;   // level-0 multigrid x after the pre-smoothing (as z)
     void* rin;  // inner residual of the refinement form (float), multigrid rhs
-    void* e;    // inner correction of the refinement form (float)
     long long nelem;  // elements of each arena vector (the direction ring's stride)
 };
 
