@@ -242,6 +242,13 @@ __host__ __device__ __forceinline__ float nanmaxf(float a, float b)
 {
     return (a > b || a != a) ? a : b;
 }
+// the same for float operands: without it float maxima were promoted to
+// double, two conversions and an FP64 compare per call on GB300's 1/64-rate
+// FP64 pipe
+__host__ __device__ __forceinline__ float nanmax(float a, float b)
+{
+    return nanmaxf(a, b);
+}
 
 // ---------------------------------------------------------------------------
 // Deterministic grid-wide reductions of up to N doubles: every block writes

@@ -218,18 +218,16 @@ k_bs_tail(const BSInfo* __restrict__ info, const MGLevel* __restrict__ levs, Dev
 // buffers chosen by the parity of the member's iteration count (p_old of
 // the halo belongs to other blocks and must not be overwritten meanwhile).
 template <typename S, typename V, int TH>
-__global__ void __launch_bounds__(256)
-k_bs_pq(const int4* __restrict__ tiles, const MGLevel* __restrict__ levs,
-        const S* __restrict__ z, V* __restrict__ p0, V* __restrict__ p1, V* __restrict__ q,
-        const DevScalars* __restrict__ scs, double* partials, int ir, V* ring,
-        long long rstride)
+__device__ __forceinline__ void pq_tile(const int4& tl, int tix, const MGLevel* __restrict__ levs,
+                                        const S* __restrict__ z, V* __restrict__ p0,
+                                        V* __restrict__ p1, V* __restrict__ q,
+                                        const DevScalars* __restrict__ scs, double* partials,
+                                        int ir, V* ring, long long rstride)
 {
-    pdl_wait();
     constexpr int H = 1, W = Reg<H, TH>::WX, N = Reg<H, TH>::N, IT = (N + 255) / 256;
     constexpr int TQ = TH / 8;
     __shared__ V sp[N];
     __shared__ uint8_t sm[N];
-    const int4 tl = tiles[blockIdx.x];
     const DevScalars& sc = scs[tl.x];
     if (bs_skip(sc, ir)) return;
     const MGLevel L = levs[tl.x * BS_LMAX];
@@ -242,23 +240,37 @@ k_bs_pq(const int4* __restrict__ tiles, const MGLevel* __restrict__ levs,
     V* __restrict__ pnew = ring ? ring + (long long)it * rstride : ((it & 1) ? p0 : p1);
     const V beta = V(sc.beta);
     const int I0 = tl.y, J0 = tl.z, t = tid256();
+    // the region in batches of PB elements per thread: the loads of a batch
+    // (index of a node outside the level clamped to node (0, 0), its values
+    // dropped after) are in flight together before any shared-memory write
+    constexpr int PB = 3;
 #pragma unroll
-    for (int k2 = 0; k2 < IT; ++k2) {
-        const int e = t + k2 * 256;
-        if (e < N) {
+    for (int k0 = 0; k0 < IT; k0 += PB) {
+        bool ok[PB];
+        uint8_t mv[PB];
+        S zv[PB];
+        V pv[PB];
+#pragma unroll
+        for (int u = 0; u < PB; ++u) {
+            const int e = t + (k0 + u) * 256;
             const int r = e / W, c = e - r * W;
             const int J = J0 - H + r;
             int I = I0 - H + c;
-            uint8_t mv = 0;
-            V zv = V(0), pv = V(0);
-            if (in_level(L, J, I)) {
-                const long long k = nidx(L, J, I);
-                mv = L.m[k];
-                zv = V(z[k]);
-                if (!first) pv = pold[k];
+            ok[u] = k0 + u < IT && e < N && in_level(L, J, I);
+            const long long k = ok[u] ? nidx(L, J, I) : L.off;
+            mv[u] = L.m[k];
+            zv[u] = z[k];
+            pv[u] = first ? V(0) : pold[k];
+        }
+#pragma unroll
+        for (int u = 0; u < PB; ++u) {
+            const int e = t + (k0 + u) * 256;
+            if (k0 + u < IT && e < N) {
+                const uint8_t m = ok[u] ? mv[u] : 0;
+                const V zz = V(zv[u]);
+                sm[e] = m;
+                sp[e] = m ? (first ? zz : zz + beta * pv[u]) : V(0);
             }
-            sm[e] = mv;
-            sp[e] = mv ? (first ? zv : zv + beta * pv) : V(0);
         }
     }
     __syncthreads();
@@ -280,7 +292,34 @@ k_bs_pq(const int4* __restrict__ tiles, const MGLevel* __restrict__ levs,
         }
     }
     const double tot = block_sum<V>(acc);
-    if (t == 0) partials[blockIdx.x] = tot;
+    if (t == 0) partials[tix] = tot;
+}
+
+// Persistent blocks walk the tile table with the grid's stride; the next
+// tile's record is loaded before the current tile is processed, so a block
+// starts each tile with its record at hand (a block per tile waited on that
+// load, then on the member's scalars, before its first vector load). A
+// converged member's tiles cost one check each. Per-tile totals and their
+// order are those of a block per tile.
+template <typename S, typename V, int TH>
+__global__ void __launch_bounds__(256)
+k_bs_pq(const int4* __restrict__ tiles, int ntiles, const MGLevel* __restrict__ levs,
+        const S* __restrict__ z, V* __restrict__ p0, V* __restrict__ p1, V* __restrict__ q,
+        const DevScalars* __restrict__ scs, double* partials, int ir, V* ring,
+        long long rstride)
+{
+    pdl_wait();
+    int b = blockIdx.x;
+    if (b >= ntiles) return;
+    int4 tl = tiles[b];
+    for (;;) {
+        const int bn = b + gridDim.x;
+        const int4 tn = bn < ntiles ? tiles[bn] : tl;
+        pq_tile<S, V, TH>(tl, b, levs, z, p0, p1, q, scs, partials, ir, ring, rstride);
+        if (bn >= ntiles) break;
+        b = bn;
+        tl = tn;
+    }
 }
 
 // <p, q> of every member from k_bs_pq's tile totals (fixed order), alpha =
@@ -309,13 +348,13 @@ k_bs_alpha(const BSInfo* __restrict__ info, DevScalars* scs, const double* __res
 // form, whose correction k_bs_correct forms from the direction ring),
 // r -= alpha q, the tile's part of <r, r> (k_bs_conv decides).
 template <typename V, int TH>
-__global__ void __launch_bounds__(256)
-k_bs_xr(const int4* __restrict__ tiles, const MGLevel* __restrict__ levs, V* __restrict__ x,
-        V* __restrict__ r, const V* __restrict__ p0, const V* __restrict__ p1,
-        const V* __restrict__ q, const DevScalars* __restrict__ scs, double* partials, int ir)
+__device__ __forceinline__ void xr_tile(const int4& tl, int tix, const MGLevel* __restrict__ levs,
+                                        V* __restrict__ x, V* __restrict__ r,
+                                        const V* __restrict__ p0, const V* __restrict__ p1,
+                                        const V* __restrict__ q,
+                                        const DevScalars* __restrict__ scs, double* partials,
+                                        int ir)
 {
-    pdl_wait();
-    const int4 tl = tiles[blockIdx.x];
     const DevScalars& sc = scs[tl.x];
     if (bs_skip(sc, ir)) return;
     const MGLevel L = levs[tl.x * BS_LMAX];
@@ -360,7 +399,28 @@ k_bs_xr(const int4* __restrict__ tiles, const MGLevel* __restrict__ levs, V* __r
         }
     }
     const double tot = block_sum<V>(acc);
-    if (threadIdx.x == 0 && threadIdx.y == 0) partials[blockIdx.x] = tot;
+    if (threadIdx.x == 0 && threadIdx.y == 0) partials[tix] = tot;
+}
+
+// persistent over the tile table, as k_bs_pq
+template <typename V, int TH>
+__global__ void __launch_bounds__(256)
+k_bs_xr(const int4* __restrict__ tiles, int ntiles, const MGLevel* __restrict__ levs,
+        V* __restrict__ x, V* __restrict__ r, const V* __restrict__ p0, const V* __restrict__ p1,
+        const V* __restrict__ q, const DevScalars* __restrict__ scs, double* partials, int ir)
+{
+    pdl_wait();
+    int b = blockIdx.x;
+    if (b >= ntiles) return;
+    int4 tl = tiles[b];
+    for (;;) {
+        const int bn = b + gridDim.x;
+        const int4 tn = bn < ntiles ? tiles[bn] : tl;
+        xr_tile<V, TH>(tl, b, levs, x, r, p0, p1, q, scs, partials, ir);
+        if (bn >= ntiles) break;
+        b = bn;
+        tl = tn;
+    }
 }
 
 // <r, r> of every member from k_bs_xr's tile totals (fixed order), the
@@ -728,6 +788,23 @@ static void launch_pdl(void (*k)(KA...), dim3 grid, dim3 block, size_t smem, cud
     cudaLaunchKernelEx(&cfg, k, args...);
 }
 
+// Grid of a persistent 256-thread kernel: the blocks that fit on the device
+// at once (occupancy of this kernel, computed on first use), at most one per
+// tile.
+template <auto KERN>
+static int resident_grid(int ntiles)
+{
+    static int resident = 0;
+    if (resident == 0) {
+        int dev = 0, nsm = 0, nb = 0;
+        cudaGetDevice(&dev);
+        cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, KERN, 256, 0);
+        resident = std::max(1, nsm * nb);
+    }
+    return std::max(1, std::min(ntiles, resident));
+}
+
 // the same with the pipelined FP32 level kernels (persistent blocks)
 template <int NU>
 static int vcycle_pipe(BatchSolver& s, cudaStream_t st, int ir)
@@ -811,14 +888,15 @@ static int cg_body(BatchSolver& s, cudaStream_t st, cudaGraphConditionalHandle c
         cnt += 1;
     }
     V* ring = ir ? (V*)s.pring : (V*)nullptr;
-    launch_pdl(k_bs_pq<S, V, TH>, dim3(nt), blk, 0, st, (const int4*)s.rtiles,
-               (const MGLevel*)s.dlevs, (const S*)s.v.z, (V*)s.v.p, (V*)s.v.p2, (V*)s.v.q,
-               (const DevScalars*)s.scs, s.partials, ir, ring, (long long)s.v.nelem);
+    launch_pdl(k_bs_pq<S, V, TH>, dim3(resident_grid<k_bs_pq<S, V, TH>>(nt)), blk, 0, st,
+               (const int4*)s.rtiles, nt, (const MGLevel*)s.dlevs, (const S*)s.v.z, (V*)s.v.p,
+               (V*)s.v.p2, (V*)s.v.q, (const DevScalars*)s.scs, s.partials, ir, ring,
+               (long long)s.v.nelem);
     launch_pdl(k_bs_alpha, dim3(s.n), dim3(256), 0, st, (const BSInfo*)s.dinfo, s.scs,
                (const double*)s.partials, ir);
-    launch_pdl(k_bs_xr<V, TH>, dim3(nt), blk, 0, st, (const int4*)s.rtiles,
-               (const MGLevel*)s.dlevs, x, r, (const V*)s.v.p, (const V*)s.v.p2,
-               (const V*)s.v.q, (const DevScalars*)s.scs, s.partials, ir);
+    launch_pdl(k_bs_xr<V, TH>, dim3(resident_grid<k_bs_xr<V, TH>>(nt)), blk, 0, st,
+               (const int4*)s.rtiles, nt, (const MGLevel*)s.dlevs, x, r, (const V*)s.v.p,
+               (const V*)s.v.p2, (const V*)s.v.q, (const DevScalars*)s.scs, s.partials, ir);
     launch_pdl(k_bs_conv, dim3(s.n), dim3(256), 0, st, (const BSInfo*)s.dinfo, s.scs,
                (const double*)s.partials, s.eg, cond, ir, s.n);
     cnt += 4;
