@@ -102,8 +102,9 @@ k_ens_fluxform_stage(const int4* __restrict__ tiles, const Member* __restrict__ 
 // Warm start of the solve of RK3 stage mode+1 (psi_warm_point, stage.cuh) on
 // every member's array (all P x NY elements: the pads are 0 and stay 0),
 // with the member's own step-size ratio: blockIdx.y is the member, the
-// blocks of a member stride over its elements two at a time (the member
-// arrays start 32-element aligned, P is even). Mode 2 also records the
+// blocks of a member stride over its elements in 16-byte pairs, two pairs
+// per thread and pass (the member arrays start 32-element aligned, P is
+// even). Mode 2 also records the
 // member's dt_warm (block 0 of the member; mode 2 reads no dt_warm).
 __global__ void __launch_bounds__(256) k_ens_psi_warm(const Member* __restrict__ mem,
                                                        EnsArenas a, int mode, DevScalars* scs)
@@ -120,10 +121,19 @@ __global__ void __launch_bounds__(256) k_ens_psi_warm(const Member* __restrict__
     w.d1 = a.psi_d1 + mb.off;
     w.d2 = a.psi_d2 + mb.off;
     const long long n = g.P * (long long)g.NY;
-    for (long long k = 2 * ((long long)blockIdx.x * blockDim.x + threadIdx.x); k < n;
-         k += 2ll * gridDim.x * blockDim.x) {
-        psi_warm_point(mode, w, k, hist, rho);
-        psi_warm_point(mode, w, k + 1, hist, rho);
+    // pairs of elements, two pairs per thread and pass (see psi_warm_pairs)
+    constexpr int U = 2;
+    const long long step = 2ll * gridDim.x * blockDim.x;
+    for (long long k0 = 2 * ((long long)blockIdx.x * blockDim.x + threadIdx.x); k0 < n;
+         k0 += U * step) {
+        long long k[U];
+        bool ok[U];
+#pragma unroll
+        for (int u = 0; u < U; ++u) {
+            k[u] = k0 + u * step;
+            ok[u] = k[u] < n;
+        }
+        psi_warm_pairs<U>(mode, w, k, ok, hist, rho);
     }
     if (mode == 2 && blockIdx.x == 0 && threadIdx.x == 0) sc.dt_warm = sc.dt;
 }

@@ -75,24 +75,72 @@ struct WarmArrays {
     double* d2;
 };
 
+// The arrays do not overlap; every load of a point is issued before its
+// stores (a store ahead of a load through another pointer would hold the
+// load back until the store's address is known not to alias it).
 __device__ __forceinline__ void psi_warm_point(int mode, const WarmArrays& w, long long k,
                                                bool hist, double rho)
 {
     const double a = w.psi[k];
     if (mode == 0) {  // a = psi0
+        const double d1 = hist ? w.d1[k] : 0.0;
         w.s0[k] = a;
-        if (hist) w.psi[k] = a + rho * w.d1[k];
+        if (hist) w.psi[k] = a + rho * d1;
     } else if (mode == 1) {  // a = psi1
         const double s0 = w.s0[k];
+        const double d2 = hist ? w.d2[k] : 0.0;
         w.p1[k] = a;
         double g = s0 + 0.5 * (a - s0);
-        if (hist) g += 0.25 * rho * w.d2[k];
+        if (hist) g += 0.25 * rho * d2;
         w.psi[k] = g;
     } else {  // a = psi2
         const double s0 = w.s0[k], p1 = w.p1[k];
         w.d1[k] = (4.0 * a - 3.0 * s0) - p1;
         w.d2[k] = (4.0 * a - 2.0 * s0) - 2.0 * p1;
         w.psi[k] = 2.0 * a - s0;
+    }
+}
+
+// psi_warm_point on U pairs of elements (k, k+1), k even and every array
+// 16-byte aligned there: 16-byte loads and stores, all the loads of the U
+// pairs before any store. ok[u] false skips pair u.
+template <int U>
+__device__ __forceinline__ void psi_warm_pairs(int mode, const WarmArrays& w,
+                                               const long long (&k)[U], const bool (&ok)[U],
+                                               bool hist, double rho)
+{
+    double2 a[U], s0[U], p1[U], d[U];
+#pragma unroll
+    for (int u = 0; u < U; ++u) {
+        const double2 z = make_double2(0.0, 0.0);
+        a[u] = ok[u] ? *(const double2*)(w.psi + k[u]) : z;
+        s0[u] = ok[u] && mode >= 1 ? *(const double2*)(w.s0 + k[u]) : z;
+        p1[u] = ok[u] && mode == 2 ? *(const double2*)(w.p1 + k[u]) : z;
+        d[u] = ok[u] && mode == 0 && hist ? *(const double2*)(w.d1 + k[u])
+             : (ok[u] && mode == 1 && hist ? *(const double2*)(w.d2 + k[u]) : z);
+    }
+#pragma unroll
+    for (int u = 0; u < U; ++u) {
+        if (!ok[u]) continue;
+        const double2 A = a[u], S = s0[u], P = p1[u], D = d[u];
+        if (mode == 0) {
+            *(double2*)(w.s0 + k[u]) = A;
+            if (hist) *(double2*)(w.psi + k[u]) = make_double2(A.x + rho * D.x, A.y + rho * D.y);
+        } else if (mode == 1) {
+            *(double2*)(w.p1 + k[u]) = A;
+            double gx = S.x + 0.5 * (A.x - S.x), gy = S.y + 0.5 * (A.y - S.y);
+            if (hist) {
+                gx += 0.25 * rho * D.x;
+                gy += 0.25 * rho * D.y;
+            }
+            *(double2*)(w.psi + k[u]) = make_double2(gx, gy);
+        } else {
+            *(double2*)(w.d1 + k[u]) = make_double2((4.0 * A.x - 3.0 * S.x) - P.x,
+                                                    (4.0 * A.y - 3.0 * S.y) - P.y);
+            *(double2*)(w.d2 + k[u]) = make_double2((4.0 * A.x - 2.0 * S.x) - 2.0 * P.x,
+                                                    (4.0 * A.y - 2.0 * S.y) - 2.0 * P.y);
+            *(double2*)(w.psi + k[u]) = make_double2(2.0 * A.x - S.x, 2.0 * A.y - S.y);
+        }
     }
 }
 
