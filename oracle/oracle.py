@@ -9,7 +9,8 @@ qgrsw equation sets with the passive tracer, the rk3/ef/enrk3/LFRA
 integrators, the CFL time step and the Bulk diagnostics. It serves three
 purposes:
 
-* the checker of the CUDA path in ``tests/`` and in ``__graft_entry__.smoke``;
+* the oracle the CUDA path is compared with in ``tests/`` and in
+  ``__graft_entry__.smoke``;
 * the CPU-baseline leg of ``bench.py`` (numba-equivalent sweeps threaded
   with OpenMP, numpy operators, SuperLU solves);
 * a restatement pinned against the reference itself: ``tests/golden/`` holds
