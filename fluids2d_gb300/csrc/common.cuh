@@ -396,37 +396,4 @@ __device__ __forceinline__ void block_total_f(const float (&a)[N], double (&out)
         }
 }
 
-// Block-level value of per-thread partials for the grid/segment reductions
-// below: FP32 partials via block_total_f (result in thread 0), FP64 ones
-// unchanged (the reduction's own FP64 block stage runs).
-template <int N, bool MAX, typename T>
-__device__ __forceinline__ void block_pre(const T (&a)[N], double (&out)[N])
-{
-    if constexpr (std::is_same<T, float>::value) {
-        block_total_f<N, MAX>(a, out);
-    } else {
-#pragma unroll
-        for (int k = 0; k < N; ++k) out[k] = a[k];
-    }
-}
-
-// whole-grid ticket: true in thread 0 of the block that finishes last
-__device__ __forceinline__ bool last_block(unsigned int* ticket)
-{
-    __shared__ int s_last;
-    __syncthreads();
-    if (threadIdx.x == 0 && threadIdx.y == 0) {
-        __threadfence();
-        const unsigned n = gridDim.x * gridDim.y;
-        s_last = (atomicAdd(ticket, 1u) == n - 1);
-    }
-    __syncthreads();
-    if (threadIdx.x == 0 && threadIdx.y == 0 && s_last) {
-        __threadfence();
-        *ticket = 0;
-        return true;
-    }
-    return false;
-}
-
 }  // namespace f2d

@@ -63,14 +63,6 @@ __device__ __forceinline__ bool in_level(const MGLevel& L, int J, int& I)
     return I >= 0 && I < L.nxn;
 }
 
-// true when the staged region of halo H around the tile at (J0, I0) lies
-// inside the level (no periodic wrap, no out-of-level node)
-template <int H, int W, int WY>
-__device__ __forceinline__ bool region_inside(const MGLevel& L, int J0, int I0)
-{
-    return J0 - H >= 0 && J0 - H + WY <= L.nyn && I0 - H >= 0 && I0 - H + W <= L.nxn;
-}
-
 // Stage mask and up to two arrays of a level on the region of halo H around
 // the tile at (J0, I0). Values at non-fluid nodes are staged as 0.
 template <int H, int TH, typename S, typename T2>
