@@ -204,11 +204,12 @@ k_bs_tail(const BSInfo* __restrict__ info, const MGLevel* __restrict__ levs, Dev
 }
 
 // ---- Krylov kernels on level 0 ------------------------------------------------
-// p = z (first iteration) or z + beta p_old, q = A p, <p, q>, alpha = rz/<p,q>.
-// p is formed on the tile and a one-node halo (the halo redundantly, from
-// z and p_old), so A p needs no second pass; p_old and p live in two
-// buffers chosen by the parity of the member's iteration count (p_old of
-// the halo belongs to other blocks and must not be overwritten meanwhile).
+// p = z (first iteration) or z + beta p_old, q = A p, the tile's part of
+// <p, q> (k_bs_alpha forms alpha = rz / <p, q>). p is formed on the tile and
+// a one-node halo (the halo redundantly, from z and p_old), so A p needs no
+// second pass; p_old and p live in two buffers chosen by the parity of the
+// member's iteration count, or in the refinement form's direction ring (p_old
+// of the halo belongs to other blocks and must not be overwritten meanwhile).
 template <typename S, typename V, int TH>
 __device__ __forceinline__ void pq_tile(const int4& tl, int tix, const MGLevel* __restrict__ levs,
                                         const S* __restrict__ z, V* __restrict__ p0,
