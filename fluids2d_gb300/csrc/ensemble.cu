@@ -2,13 +2,15 @@
 // grid sizes and masks advance together, one launch per kernel for all
 // members.
 //
-// * Cells of all members are cut into 32x8 tiles listed in one tile table;
-//   each block of a batched kernel looks up its (member, tile) and runs the
-//   same tile code as the single-model kernels (stage_dev.cuh).
+// * Cells of all members are cut into 32x32 tiles (32 x 8 threads, four rows
+//   each) listed in one tile table; each block of a batched kernel looks up
+//   its (member, tile) and runs the same tile code as the single-model
+//   kernels (stage_dev.cuh).
 // * The Poisson/Helmholtz solves of all members run in one batched solver
 //   (solver.cu): each member has its own multigrid hierarchy and CG state.
-// * max|U| is reduced per member (segmented last-block reductions); each
-//   member has its own CFL time step and Kahan time.
+// * max|U| is reduced per member (per-tile maxima, combined in a fixed order
+//   by one block per member); each member has its own CFL time step and
+//   Kahan time.
 // * Fields of all members live in one arena per field; member b starts at
 //   element offset off_b (a multiple of 32 elements) with its own pitch.
 #include <cudaTypedefs.h>

@@ -4,11 +4,13 @@
 // Operator at a fluid node: A x = cx (xW + xE) + cy (xS + xN) + diag x,
 // non-fluid neighbours Dirichlet 0, diag = -2 (cx + cy) - maindiag. Every
 // member of the batch has its own multigrid hierarchy (mg.cu: mg_build);
-// grid levels are covered by tables of 32x32-node tiles spanning all
-// members, the coarse tail runs one block per member, dot products are
-// reduced per member with deterministic segmented reductions, and the
-// iteration loops are CUDA-graph conditional WHILE nodes that run until every
-// member has converged (converged members' blocks return at once).
+// tile tables spanning all members cover the grid levels (the level kernels:
+// 54x70-node tiles; the Krylov kernels on level 0: 32 columns x 32 or 64
+// rows), the coarse tail runs one block per member, dot products are reduced
+// per member deterministically (per-tile totals summed in a fixed order by
+// one block per member), and the iteration loops are CUDA-graph conditional
+// WHILE nodes that run until every member has converged (converged members'
+// tiles are skipped).
 //
 // Two forms:
 //  * mode 0 (FP64): preconditioned CG in FP64 with an FP64 V-cycle.
@@ -117,11 +119,10 @@ __device__ __forceinline__ double block_sum(V acc)
     return w[0];
 }
 
-// Completion of a kernel over all members, counted per member: exactly one
-// block of every member calls this with mine = true (the last block of its
-// segmented reduction, or the first tile of a member whose work is skipped),
-// so the global ticket sees n increments, not one per block. True in the
-// thread that completes the count.
+// Completion of a kernel over all members, counted per member: the kernels
+// that call it run one block per member, whose thread 0 calls it with
+// mine = true, so the global ticket sees n increments. True in the thread
+// that completes the count.
 __device__ __forceinline__ bool members_done(bool mine, unsigned int* ticket, int n)
 {
     if (!mine) return false;
