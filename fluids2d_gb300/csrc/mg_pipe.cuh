@@ -1,5 +1,5 @@
 // Pipelined FP32 multigrid level kernels: the down and up legs of the
-// V-cycle on the grid levels above a member's tail, in the FP32 refinement
+// V-cycle on the grid levels finer than a member's tail, in the FP32 refinement
 // form (solver.cu launches them when the level arrays pass the layout checks
 // of bs_build; the FP64 form and the other cases keep mg_reg.cuh's kernels).
 //

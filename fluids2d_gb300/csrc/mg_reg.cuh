@@ -1,5 +1,6 @@
 // Register-blocked multigrid level kernels (the V-cycle's down and up legs
-// on every grid level below a member's tail), used by solver.cu.
+// on every grid level finer than a member's tail), used by solver.cu in the
+// FP64 form and where the pipelined FP32 kernels (mg_pipe.cuh) do not apply.
 //
 // A block stages a region of MR_WY x MR_W nodes (a tile of MR_TH x MR_TW
 // nodes and a halo of MR_H nodes) in registers: warp w holds region rows
